@@ -1,0 +1,389 @@
+// binning.cu -- projection, tile counting, instance offsets, key emission and
+// per-tile ranges for sm_103a.
+//
+// Reference path: GSSlam::prepareRasterization (src/GSSlam.cu:408-646) with
+// projectGaussiansWorldToScreen_kernel (src/GSCudaKernels.cu:345-476),
+// countTilesPerGaussian_kernel (549-593), thrust::exclusive_scan
+// (src/GSSlam.cu:556-572), generateTileHashes_kernel (596-667) and
+// computeIndicesRanges_kernel (669-707).
+//
+// Differences in structure (same results):
+//  * projection and counting are one kernel; the tile rectangle is computed
+//    once and kept in a 32-byte binning record;
+//  * the instance total never leaves the device: later kernels read it from
+//    DevStatus, so a tracking iteration needs no host round trip;
+//  * keys are emitted by whole warps over the concatenated tile lists of 32
+//    Gaussians, so writes are contiguous and a large splat does not stall a
+//    thread while its neighbours idle.
+// All key-critical arithmetic uses explicit round-to-nearest intrinsics in the
+// fixed order that the CPU restatement mirrors, so keys are bit-exact.
+#include "fvgs_device.cuh"
+#include "fvgs_launch.h"
+
+namespace fvgs {
+
+__global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const DevPose* P = a.pose;
+    const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
+    float R[3][3];
+    quat_to_R(qc, R);
+    const float4 p = a.pos[i];
+    const float4 s = a.scale[i];
+    const float4 qg4 = a.rot[i];
+    const float4 co = a.col[i];
+    const fvgs_intrinsics K = a.K;
+
+    float u = 0.f, v = 0.f, z = 0.f, cxx = 0.f, cyy = 0.f, cxy = 0.f;
+    float ixx = 0.f, iyy = 0.f, ixy = 0.f, phx = 0.f, phy = 0.f;
+    bool visible = false;
+    {
+        const float d0 = __fsub_rn(p.x, P->t[0]);
+        const float d1 = __fsub_rn(p.y, P->t[1]);
+        const float d2 = __fsub_rn(p.z, P->t[2]);
+        const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[1][0], d1, __fmul_rn(R[0][0], d0)));
+        const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[1][1], d1, __fmul_rn(R[0][1], d0)));
+        const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[1][2], d1, __fmul_rn(R[0][2], d0)));
+        if (pcz > 0.0f) {
+            const float inv_z = __fdiv_rn(1.0f, pcz);
+            const float uu = __fmaf_rn(K.fx, __fmul_rn(pcx, inv_z), K.cx);
+            const float vv = __fmaf_rn(K.fy, __fmul_rn(pcy, inv_z), K.cy);
+            if (!(uu < 0.0f || uu >= (float)a.W || vv < 0.0f || vv >= (float)a.H)) {
+                visible = true;
+                u = uu;
+                v = vv;
+                z = pcz;
+                const float qg[4] = {qg4.x, qg4.y, qg4.z, qg4.w};
+                float Rg[3][3];
+                quat_to_R(qg, Rg);
+                float M[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    M[r][0] = __fmul_rn(Rg[r][0], s.x);
+                    M[r][1] = __fmul_rn(Rg[r][1], s.y);
+                    M[r][2] = __fmul_rn(Rg[r][2], s.z);
+                }
+                float S[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = r; c < 3; ++c) {
+                        S[r][c] = __fmaf_rn(M[r][2], M[c][2], __fmaf_rn(M[r][1], M[c][1], __fmul_rn(M[r][0], M[c][0])));
+                        S[c][r] = S[r][c];
+                    }
+                float A[3][3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        A[k][c] = __fmaf_rn(S[k][2], R[2][c], __fmaf_rn(S[k][1], R[1][c], __fmul_rn(S[k][0], R[0][c])));
+                float C[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = r; c < 3; ++c) {
+                        C[r][c] = __fmaf_rn(R[2][r], A[2][c], __fmaf_rn(R[1][r], A[1][c], __fmul_rn(R[0][r], A[0][c])));
+                        C[c][r] = C[r][c];
+                    }
+                const float j00 = __fmul_rn(K.fx, inv_z);
+                const float j02 = __fmul_rn(__fmul_rn(__fmul_rn(-K.fx, pcx), inv_z), inv_z);
+                const float j11 = __fmul_rn(K.fy, inv_z);
+                const float j12 = __fmul_rn(__fmul_rn(__fmul_rn(-K.fy, pcy), inv_z), inv_z);
+                const float t0 = __fmaf_rn(j02, C[0][2], __fmul_rn(j00, C[0][0]));
+                const float t2 = __fmaf_rn(j02, C[2][2], __fmul_rn(j00, C[0][2]));
+                cxx = __fmaf_rn(j02, t2, __fmul_rn(j00, t0));
+                const float s1 = __fmaf_rn(j12, C[1][2], __fmul_rn(j11, C[1][1]));
+                const float s2 = __fmaf_rn(j12, C[2][2], __fmul_rn(j11, C[1][2]));
+                cyy = __fmaf_rn(j12, s2, __fmul_rn(j11, s1));
+                const float a0 = __fmaf_rn(C[0][2], j12, __fmul_rn(C[0][1], j11));
+                const float a2 = __fmaf_rn(C[2][2], j12, __fmul_rn(C[1][2], j11));
+                cxy = __fmaf_rn(j02, a2, __fmul_rn(j00, a0));
+                const float det = __fmaf_rn(cxx, cyy, -__fmul_rn(cxy, cxy));
+                if (det == 0.0f) {
+                    ixx = 1.0f;
+                    iyy = 1.0f;
+                    ixy = 0.0f;
+                } else {
+                    const float inv_det = __fdiv_rn(1.0f, det);
+                    ixx = __fmul_rn(cyy, inv_det);
+                    iyy = __fmul_rn(cxx, inv_det);
+                    ixy = __fmul_rn(-cxy, inv_det);
+                }
+                phx = __fmul_rn(__fmul_rn(pcx, inv_z), inv_z);
+                phy = __fmul_rn(__fmul_rn(pcy, inv_z), inv_z);
+            }
+        }
+    }
+    // Tile rectangle (countTilesPerGaussian_kernel).  Culled slots see the
+    // zero record and land on tile 0, as the reference's zeroed buffers do.
+    const float rx = __fmul_rn(a.radius_sigma, __fsqrt_rn(cxx));
+    const float ry = __fmul_rn(a.radius_sigma, __fsqrt_rn(cyy));
+    const float bx0 = fmaxf(0.0f, __fsub_rn(u, rx));
+    const float bx1 = fminf((float)(a.W - 1), __fadd_rn(u, rx));
+    const float by0 = fmaxf(0.0f, __fsub_rn(v, ry));
+    const float by1 = fminf((float)(a.H - 1), __fadd_rn(v, ry));
+    int x0 = __float2int_rz(__fdiv_rn(bx0, (float)a.tw));
+    int x1 = __float2int_rz(__fdiv_rn(bx1, (float)a.tw));
+    int y0 = __float2int_rz(__fdiv_rn(by0, (float)a.th));
+    int y1 = __float2int_rz(__fdiv_rn(by1, (float)a.th));
+    x0 = max(0, min(x0, a.ntx - 1));
+    x1 = max(0, min(x1, a.ntx - 1));
+    y0 = max(0, min(y0, a.nty - 1));
+    y1 = max(0, min(y1, a.nty - 1));
+    uint32_t count = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
+    if (!visible && !(a.quirks & FVGS_Q_CULLED_SLOTS)) count = 0;
+
+    const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+    a.rec0[i] = make_float4(u, v, z, co.w);
+    a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);
+    a.rec2[i] = make_float4(phy, co.x, co.y, co.z);
+    a.bin0[i] = make_uint4((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16), count,
+                           __float_as_uint(phy));
+    a.bin1[i] = make_float4(u, v, z, phx);
+    a.counts[i] = count;
+    if (a.dbg_cov) {
+        a.dbg_cov[3 * i] = cxx;
+        a.dbg_cov[3 * i + 1] = cyy;
+        a.dbg_cov[3 * i + 2] = cxy;
+        a.dbg_inv[3 * i] = ixx;
+        a.dbg_inv[3 * i + 1] = iyy;
+        a.dbg_inv[3 * i + 2] = ixy;
+        a.dbg_vis[i] = visible ? 1 : 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of counts: kernel 1 sums 4096-element blocks; kernel 2 lets
+// every block reduce the sums before it (at most a few hundred values) and
+// scan its own block.  Two launches, no inter-block waits, deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_reduce_sum(uint32_t v, uint32_t* smem) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) smem[w] = v;
+    __syncthreads();
+    uint32_t r = 0;
+    if (w == 0) {
+        r = (l < (int)(blockDim.x >> 5)) ? smem[l] : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFullMask, r, o);
+    }
+    __syncthreads();
+    return r;  // valid in warp 0
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_partials_kernel(const uint32_t* counts, int n,
+                                                                     uint32_t* partials) {
+    __shared__ uint32_t sm[32];
+    const int base = blockIdx.x * kScanBlock;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int i = base + k * kScanThreads + threadIdx.x;
+        if (i < n) s += counts[i];
+    }
+    s = block_reduce_sum(s, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_final_kernel(const uint32_t* counts, int n,
+                                                                  const uint32_t* partials, int n_blocks,
+                                                                  uint32_t* offsets, DevStatus* st,
+                                                                  uint32_t capacity) {
+    __shared__ uint32_t sm[32];
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_base;
+    // prefix of all earlier blocks
+    uint32_t pre = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += kScanThreads) pre += partials[b];
+    pre = block_reduce_sum(pre, sm);
+    if (threadIdx.x == 0) s_base = pre;
+    __syncthreads();
+    const uint32_t block_base = s_base;
+    // blocked arrangement: thread t owns items base + t*4 .. +3 (contiguous)
+    const int base = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+    uint32_t c[kScanItems];
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        c[k] = (base + k < n) ? counts[base + k] : 0u;
+        tsum += c[k];
+    }
+    // block exclusive scan of tsum
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    uint32_t incl = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+        if (l >= o) incl += y;
+    }
+    if (l == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = s_warp[l];
+        uint32_t xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, xi, o);
+            if (l >= o) xi += y;
+        }
+        s_warp[l] = xi - x;  // exclusive warp prefix
+    }
+    __syncthreads();
+    uint32_t run = block_base + s_warp[w] + (incl - tsum);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) offsets[base + k] = run;
+        run += c[k];
+    }
+    if (blockIdx.x == n_blocks - 1 && threadIdx.x == kScanThreads - 1) {
+        st->n_instances = run;
+        st->n_instances_clamped = run < capacity ? run : capacity;
+        if (run > capacity) atomicOr(&st->flags, kErrOverflow);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Key emission: a warp takes 32 consecutive Gaussians, whose instances are
+// contiguous in the output, and walks their concatenated tile lists 32 at a
+// time.  Each lane finds its owning Gaussian by a 5-step shuffle search.
+// key = tile << 32 | bits(fmaf(phy, dy, fmaf(phx, dx, z))), dx = tile centre - u.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) emit_keys_kernel(EmitArgs a) {
+    const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+    const int lane = threadIdx.x & 31;
+    if (gbase >= a.n) return;  // whole warp leaves together
+    const int g = gbase + lane;
+    const bool valid = g < a.n;
+    uint4 b0 = make_uint4(0, 0, 0, 0);
+    float4 b1 = make_float4(0, 0, 0, 0);
+    uint32_t off = 0;
+    if (valid) {
+        b0 = a.bin0[g];
+        b1 = a.bin1[g];
+        off = a.offsets[g];
+    }
+    const uint32_t cnt = valid ? b0.z : 0u;
+    // warp-local exclusive prefix of counts
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t excl = incl - cnt;
+    const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+    const uint32_t warp_off = __shfl_sync(kFullMask, off, 0);
+    const uint64_t cap = a.capacity;
+    for (uint32_t m0 = 0; m0 < total; m0 += 32) {
+        const uint32_t m = m0 + lane;
+        // largest l with excl[l] <= m
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t e = __shfl_sync(kFullMask, excl, lo + step);
+            if (e <= m) lo += step;
+        }
+        const uint32_t r0 = __shfl_sync(kFullMask, b0.x, lo);
+        const uint32_t r1 = __shfl_sync(kFullMask, b0.y, lo);
+        const uint32_t phy_bits = __shfl_sync(kFullMask, b0.w, lo);
+        const float u = __shfl_sync(kFullMask, b1.x, lo);
+        const float v = __shfl_sync(kFullMask, b1.y, lo);
+        const float z = __shfl_sync(kFullMask, b1.z, lo);
+        const float phx = __shfl_sync(kFullMask, b1.w, lo);
+        const uint32_t e_lo = __shfl_sync(kFullMask, excl, lo);
+        if (m < total) {
+            const uint32_t local = m - e_lo;
+            const int x0 = (int)(r0 & 0xffffu), y0 = (int)(r0 >> 16);
+            const int x1 = (int)(r1 & 0xffffu);
+            const int w = x1 - x0 + 1;
+            const int tx = x0 + (int)(local % (uint32_t)w);
+            const int ty = y0 + (int)(local / (uint32_t)w);
+            const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)a.tw);
+            const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)a.th);
+            const float dx = __fsub_rn(tcx, u);
+            const float dy = __fsub_rn(tcy, v);
+            const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+            const uint32_t tile = (uint32_t)(ty * a.ntx + tx);
+            const uint64_t dst = (uint64_t)warp_off + m;
+            if (dst < cap) {
+                a.keys[dst] = ((uint64_t)tile << 32) | (uint64_t)__float_as_uint(d);
+                a.vals[dst] = (uint32_t)(gbase + lo);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-tile ranges over the sorted keys (ranges zeroed beforehand).
+// Intended: every boundary.  RANGE_LAUNCH: the reference's literal launch,
+// which only visits the first 256*ceil(T/256) instances and whose first
+// instance never closes its tile.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const DevStatus* st, int num_tiles,
+                                                     uint32_t quirks, uint2* ranges) {
+    const uint32_t n = st->n_instances_clamped;
+    uint32_t limit = n;
+    if (quirks & FVGS_Q_RANGE_LAUNCH) {
+        const uint32_t launched = (uint32_t)((num_tiles + 255) / 256) * 256u;
+        limit = min(limit, launched);
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < limit; i += gridDim.x * blockDim.x) {
+        const uint32_t t = (uint32_t)(keys[i] >> 32);
+        if (quirks & FVGS_Q_RANGE_LAUNCH) {
+            if (i == 0) {
+                ranges[t].x = 0;
+                continue;
+            }
+            const uint32_t pt = (uint32_t)(keys[i - 1] >> 32);
+            if (pt != t) {
+                ranges[pt].y = i;
+                ranges[t].x = i;
+            }
+            if (i == n - 1) ranges[t].y = n;
+        } else {
+            if (i == 0 || (uint32_t)(keys[i - 1] >> 32) != t) ranges[t].x = i;
+            if (i == n - 1 || (uint32_t)(keys[i + 1] >> 32) != t) ranges[t].y = i + 1;
+        }
+    }
+}
+
+// ------------------------------- launchers ---------------------------------
+cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    project_count_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+size_t scan_partials_size(int n) { return (size_t)((n + kScanBlock - 1) / kScanBlock); }
+
+cudaError_t launch_scan(const uint32_t* counts, int n, uint32_t* partials, uint32_t* offsets, DevStatus* st,
+                        uint32_t capacity, cudaStream_t s) {
+    const int nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb == 0) return cudaSuccess;
+    scan_partials_kernel<<<nb, kScanThreads, 0, s>>>(counts, n, partials);
+    scan_final_kernel<<<nb, kScanThreads, 0, s>>>(counts, n, partials, nb, offsets, st, capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_emit_keys(const EmitArgs& a, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    emit_keys_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_tiles, uint32_t quirks,
+                          uint2* ranges, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(ranges, 0, sizeof(uint2) * (size_t)num_tiles, s);
+    if (e != cudaSuccess) return e;
+    ranges_kernel<<<grid, 256, 0, s>>>(keys, st, num_tiles, quirks, ranges);
+    return cudaGetLastError();
+}
+
+}  // namespace fvgs

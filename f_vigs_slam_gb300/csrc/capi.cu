@@ -1,0 +1,757 @@
+// capi.cu -- implementation of the fvgs C-ABI (include/fvgs.h): sessions that
+// own all device state of one SLAM map, and the host-side orchestration of the
+// binning / tracking kernels on the session's stream.
+//
+// The reference keeps this state as GSSlam members resized on every call
+// (src/GSSlam.cu:408-471) and synchronises after every kernel
+// (src/GSSlam.cu:47-66).  Here buffers are sized once per session, the
+// instance count stays on the device, and a call synchronises once, when it
+// has to hand results back to the host.  The instance buffers start at an
+// estimate and grow when the device reports an overflow; the affected call is
+// then re-run, so results never depend on the capacity.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/fvgs.h"
+#include "fvgs_device.cuh"
+#include "fvgs_launch.h"
+
+using namespace fvgs;
+
+namespace {
+
+constexpr int kMaxLevels = 3;
+
+struct FrameLevel {
+    int W = 0, H = 0;
+    size_t cap_px = 0;
+    float* rgb = nullptr;
+    float* depth = nullptr;
+    float* gx = nullptr;
+    float* gy = nullptr;
+};
+
+__global__ void set_pose_kernel(DevPose* dst, fvgs_pose p) {
+    for (int k = 0; k < 3; ++k) {
+        dst->t[k] = p.position[k];
+        dst->td[k] = (double)p.position[k];
+    }
+    for (int k = 0; k < 4; ++k) {
+        dst->q[k] = p.orientation[k];
+        dst->qd[k] = (double)p.orientation[k];
+    }
+}
+
+__global__ void upload_pack_kernel(const float* pos, const float* scl, const float* rot, const float* col,
+                                   const float* opa, uint32_t n, float4* gpos, float4* gscl, float4* grot,
+                                   float4* gcol) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    gpos[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
+    gscl[i] = make_float4(scl[3 * i], scl[3 * i + 1], scl[3 * i + 2], 0.f);
+    grot[i] = make_float4(rot[4 * i], rot[4 * i + 1], rot[4 * i + 2], rot[4 * i + 3]);
+    gcol[i] = make_float4(col[3 * i], col[3 * i + 1], col[3 * i + 2], opa[i]);
+}
+
+__global__ void download_unpack_kernel(const float4* gpos, const float4* gscl, const float4* grot,
+                                       const float4* gcol, uint32_t n, float* pos, float* scl, float* rot,
+                                       float* col, float* opa) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = gpos[i], s = gscl[i], q = grot[i], c = gcol[i];
+    pos[3 * i] = p.x; pos[3 * i + 1] = p.y; pos[3 * i + 2] = p.z;
+    scl[3 * i] = s.x; scl[3 * i + 1] = s.y; scl[3 * i + 2] = s.z;
+    rot[4 * i] = q.x; rot[4 * i + 1] = q.y; rot[4 * i + 2] = q.z; rot[4 * i + 3] = q.w;
+    col[3 * i] = c.x; col[3 * i + 1] = c.y; col[3 * i + 2] = c.z;
+    opa[i] = c.w;
+}
+
+int bits_for(int v) {  // bits needed to represent values 0..v-1
+    int b = 0;
+    while ((1 << b) < v) ++b;
+    return b;
+}
+
+}  // namespace
+
+struct fvgs_session {
+    fvgs_params params{};
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    uint32_t debug = 0;
+    uint32_t cap_g = 0, n_g = 0;
+    int max_w = 0, max_h = 0;
+    uint64_t footprint = 0;
+    std::vector<void*> allocations;
+
+    float4 *pos = nullptr, *scale = nullptr, *rot = nullptr, *col = nullptr;
+    float4 *rec0 = nullptr, *rec1 = nullptr, *rec2 = nullptr;
+    uint4* bin0 = nullptr;
+    float4* bin1 = nullptr;
+    uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
+    float *dbg_cov = nullptr, *dbg_inv = nullptr;
+    uint8_t* dbg_vis = nullptr;
+
+    uint64_t cap_inst = 0;
+    uint64_t* keys = nullptr;
+    uint32_t* vals = nullptr;
+    SortWorkspace sort{};
+
+    int cap_tiles = 0;
+    uint2* ranges = nullptr;
+    float* tile_out = nullptr;
+
+    FrameLevel lv[kMaxLevels];
+
+    DevPose* pose = nullptr;
+    double* jj = nullptr;    // 42 doubles: JtJ[36], Jtr[6]
+    double* step = nullptr;  // 6 doubles
+    DevStatus* st = nullptr;
+    double* h_jj = nullptr;  // pinned mirrors
+    DevStatus* h_st = nullptr;
+    fvgs_pose* h_pose = nullptr;
+    DevPose* h_devpose = nullptr;
+
+    float *img_color = nullptr, *img_depth = nullptr, *img_T = nullptr;
+    uint32_t* img_nc = nullptr;
+    size_t img_cap = 0;
+
+    int last_W = 0, last_H = 0, last_T = 0;
+    bool has_binning = false, has_track = false, dbg_proj_valid = false;
+};
+
+namespace {
+
+thread_local char g_errbuf[256];
+
+int cuda_fail(cudaError_t e, const char* what) {
+    std::snprintf(g_errbuf, sizeof(g_errbuf), "%s: %s", what, cudaGetErrorString(e));
+    return FVGS_E_CUDA;
+}
+
+#define FV_CK(call)                                     \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+template <typename T>
+int dev_alloc(fvgs_session* s, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, sizeof(T) * count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return FVGS_E_NOMEM;
+    }
+    s->allocations.push_back(v);
+    s->footprint += sizeof(T) * count;
+    *p = static_cast<T*>(v);
+    return FVGS_OK;
+}
+
+template <typename T>
+void dev_free(fvgs_session* s, T*& p, size_t count) {
+    if (!p) return;
+    auto it = std::find(s->allocations.begin(), s->allocations.end(), (void*)p);
+    if (it != s->allocations.end()) s->allocations.erase(it);
+    cudaFree(p);
+    s->footprint -= sizeof(T) * (count ? count : 1);
+    p = nullptr;
+}
+
+#define FV_TRY(expr)            \
+    do {                        \
+        int r_ = (expr);        \
+        if (r_ != FVGS_OK) return r_; \
+    } while (0)
+
+int alloc_instances(fvgs_session* s, uint64_t cap) {
+    if (s->keys) {
+        FV_CK(cudaStreamSynchronize(s->stream));
+        dev_free(s, s->keys, s->cap_inst);
+        dev_free(s, s->vals, s->cap_inst);
+        dev_free(s, s->sort.keys_alt, s->cap_inst);
+        dev_free(s, s->sort.vals_alt, s->cap_inst);
+        dev_free(s, s->sort.lookback, sort_lookback_words(s->cap_inst));
+    }
+    s->cap_inst = cap;
+    FV_TRY(dev_alloc(s, &s->keys, cap));
+    FV_TRY(dev_alloc(s, &s->vals, cap));
+    FV_TRY(dev_alloc(s, &s->sort.keys_alt, cap));
+    FV_TRY(dev_alloc(s, &s->sort.vals_alt, cap));
+    FV_TRY(dev_alloc(s, &s->sort.lookback, sort_lookback_words(cap)));
+    FV_CK(cudaMemsetAsync(s->sort.lookback, 0, sizeof(uint64_t) * sort_lookback_words(cap), s->stream));
+    s->sort.max_items = cap;
+    s->sort.epoch = 1;
+    return FVGS_OK;
+}
+
+int ensure_images(fvgs_session* s, size_t px) {
+    if (px <= s->img_cap) return FVGS_OK;
+    dev_free(s, s->img_color, 3 * s->img_cap);
+    dev_free(s, s->img_depth, s->img_cap);
+    dev_free(s, s->img_T, s->img_cap);
+    dev_free(s, s->img_nc, s->img_cap);
+    FV_TRY(dev_alloc(s, &s->img_color, 3 * px));
+    FV_TRY(dev_alloc(s, &s->img_depth, px));
+    FV_TRY(dev_alloc(s, &s->img_T, px));
+    FV_TRY(dev_alloc(s, &s->img_nc, px));
+    s->img_cap = px;
+    return FVGS_OK;
+}
+
+int check_view(fvgs_session* s, int W, int H) {
+    if (W <= 0 || H <= 0 || W > 65535 * s->params.tile_w || H > 65535 * s->params.tile_h) return FVGS_E_INVALID;
+    const int ntx = (W + s->params.tile_w - 1) / s->params.tile_w;
+    const int nty = (H + s->params.tile_h - 1) / s->params.tile_h;
+    if (ntx * nty > s->cap_tiles) return FVGS_E_INVALID;
+    return FVGS_OK;
+}
+
+// Enqueue binning for the pose already in s->pose.
+int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
+    const fvgs_params& P = s->params;
+    const int ntx = (W + P.tile_w - 1) / P.tile_w;
+    const int nty = (H + P.tile_h - 1) / P.tile_h;
+    const int T = ntx * nty;
+    ProjectArgs pa{};
+    pa.pos = s->pos;
+    pa.scale = s->scale;
+    pa.rot = s->rot;
+    pa.col = s->col;
+    pa.n = (int)s->n_g;
+    pa.pose = s->pose;
+    pa.K = *K;
+    pa.W = W;
+    pa.H = H;
+    pa.tw = P.tile_w;
+    pa.th = P.tile_h;
+    pa.ntx = ntx;
+    pa.nty = nty;
+    pa.radius_sigma = P.radius_sigma;
+    pa.quirks = P.quirks;
+    pa.rec0 = s->rec0;
+    pa.rec1 = s->rec1;
+    pa.rec2 = s->rec2;
+    pa.bin0 = s->bin0;
+    pa.bin1 = s->bin1;
+    pa.counts = s->counts;
+    if (s->debug & FVGS_DEBUG_PROJECTION) {
+        pa.dbg_cov = s->dbg_cov;
+        pa.dbg_inv = s->dbg_inv;
+        pa.dbg_vis = s->dbg_vis;
+    }
+    FV_CK(launch_project_count(pa, s->stream));
+    FV_CK(launch_scan(s->counts, (int)s->n_g, s->partials, s->offsets, s->st, (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu), s->stream));
+    EmitArgs ea{};
+    ea.bin0 = s->bin0;
+    ea.bin1 = s->bin1;
+    ea.offsets = s->offsets;
+    ea.n = (int)s->n_g;
+    ea.ntx = ntx;
+    ea.tw = P.tile_w;
+    ea.th = P.tile_h;
+    ea.capacity = s->cap_inst;
+    ea.keys = s->keys;
+    ea.vals = s->vals;
+    FV_CK(launch_emit_keys(ea, s->stream));
+    const int key_bits = 32 + std::max(1, bits_for(T));
+    FV_CK(launch_radix_sort(s->keys, s->vals, s->st, key_bits, &s->sort, &s->st->flags, s->stream));
+    FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+    s->last_W = W;
+    s->last_H = H;
+    s->last_T = T;
+    s->has_binning = true;
+    s->dbg_proj_valid = (s->debug & FVGS_DEBUG_PROJECTION) != 0;
+    return FVGS_OK;
+}
+
+int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
+                  bool images) {
+    const fvgs_params& P = s->params;
+    TrackArgs ta{};
+    ta.rec0 = s->rec0;
+    ta.rec1 = s->rec1;
+    ta.rec2 = s->rec2;
+    ta.ranges = s->ranges;
+    ta.indices = s->vals;
+    ta.obs_rgb = f.rgb;
+    ta.obs_depth = f.depth;
+    ta.gx = f.gx;
+    ta.gy = f.gy;
+    ta.pose = s->pose;
+    ta.K = *K;
+    ta.W = f.W;
+    ta.H = f.H;
+    ta.ntx = (f.W + P.tile_w - 1) / P.tile_w;
+    ta.nty = (f.H + P.tile_h - 1) / P.tile_h;
+    ta.bg[0] = P.bg[0];
+    ta.bg[1] = P.bg[1];
+    ta.bg[2] = P.bg[2];
+    ta.alpha_thresh = P.alpha_thresh;
+    ta.color_thresh = P.color_thresh;
+    ta.depth_thresh = P.depth_thresh;
+    ta.tile_out = s->tile_out;
+    if (images) {
+        ta.img_color = s->img_color;
+        ta.img_depth = s->img_depth;
+        ta.img_T = s->img_T;
+        ta.img_nc = s->img_nc;
+    }
+    ta.render_only = render_only ? 1 : 0;
+    FV_CK(launch_track(ta, s->stream));
+    return FVGS_OK;
+}
+
+int set_pose(fvgs_session* s, const fvgs_pose* p) {
+    set_pose_kernel<<<1, 1, 0, s->stream>>>(s->pose, *p);
+    FV_CK(cudaGetLastError());
+    return FVGS_OK;
+}
+
+int reset_status(fvgs_session* s) {
+    FV_CK(cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream));
+    return FVGS_OK;
+}
+
+// After a synchronised step: grow on overflow (returns 1 = retry).
+int check_status(fvgs_session* s, int* retry) {
+    *retry = 0;
+    const DevStatus st = *s->h_st;
+    if (st.flags & kErrTimeout) return FVGS_E_TIMEOUT;
+    if (st.flags & kErrOverflow) {
+        const uint64_t need = (uint64_t)st.n_instances;
+        uint64_t cap = need + need / 4 + 65536;
+        if (cap > 0xffffffffull) return FVGS_E_CAPACITY;
+        FV_TRY(alloc_instances(s, cap));
+        *retry = 1;
+    }
+    return FVGS_OK;
+}
+
+bool valid_pose(const fvgs_pose* p) { return p != nullptr; }
+
+}  // namespace
+
+extern "C" {
+
+const char* fvgs_status_string(int status) {
+    switch (status) {
+        case FVGS_OK: return "ok";
+        case FVGS_E_INVALID: return "invalid argument";
+        case FVGS_E_NOMEM: return "out of memory";
+        case FVGS_E_CUDA: return g_errbuf[0] ? g_errbuf : "CUDA error";
+        case FVGS_E_CAPACITY: return "capacity exceeded";
+        case FVGS_E_TIMEOUT: return "bounded device wait expired";
+        case FVGS_E_STATE: return "call made in the wrong state";
+        case FVGS_E_ADMISSION: return "not admitted";
+        default: return "unknown status";
+    }
+}
+
+int fvgs_params_default(fvgs_params* p) {
+    if (!p) return FVGS_E_INVALID;
+    std::memset(p, 0, sizeof(*p));
+    p->tile_w = 16;
+    p->tile_h = 16;
+    p->radius_sigma = 3.0f;
+    p->bg[0] = p->bg[1] = p->bg[2] = 0.0f;
+    p->alpha_thresh = 0.2f;
+    p->color_thresh = 0.1f;
+    p->depth_thresh = 0.2f;
+    p->w_depth = 1.0f;
+    p->w_dist = 0.1f;
+    p->lambda_iso = 0.01f;
+    p->adam_beta1 = 0.9f;
+    p->adam_beta2 = 0.999f;
+    p->adam_eps = 1e-8f;
+    p->quirks = FVGS_QUIRKS_DEFAULT;
+    p->eig_eps = 1e-4;
+    return FVGS_OK;
+}
+
+int fvgs_session_destroy(fvgs_session* s) {
+    if (!s) return FVGS_E_INVALID;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->allocations) cudaFree(p);
+    if (s->h_jj) cudaFreeHost(s->h_jj);
+    if (s->h_st) cudaFreeHost(s->h_st);
+    if (s->h_pose) cudaFreeHost(s->h_pose);
+    if (s->h_devpose) cudaFreeHost(s->h_devpose);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+    return FVGS_OK;
+}
+
+int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity_gaussians, int max_width,
+                        int max_height, fvgs_session** out) {
+    if (!out || capacity_gaussians == 0 || max_width <= 0 || max_height <= 0) return FVGS_E_INVALID;
+    *out = nullptr;
+    fvgs_params P;
+    if (params) P = *params;
+    else fvgs_params_default(&P);
+    // The sm_103a tracking kernel is written for 16x16 tiles (one thread per
+    // pixel of a tile); other shapes are rejected rather than mis-rendered.
+    if (P.tile_w != 16 || P.tile_h != 16) return FVGS_E_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return FVGS_E_INVALID;
+    }
+    FV_CK(cudaSetDevice(device));
+    fvgs_session* s = new (std::nothrow) fvgs_session();
+    if (!s) return FVGS_E_NOMEM;
+    s->params = P;
+    s->device = device;
+    s->cap_g = capacity_gaussians;
+    s->max_w = max_width;
+    s->max_h = max_height;
+    int rc = FVGS_OK;
+    auto fail = [&](int r) {
+        fvgs_session_destroy(s);
+        return r;
+    };
+    if (cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return fail(FVGS_E_CUDA);
+    if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FVGS_E_CUDA);
+    s->stream = s->own_stream;
+    const size_t N = capacity_gaussians;
+#define FV_A(ptr, cnt) \
+    if ((rc = dev_alloc(s, &(ptr), (cnt))) != FVGS_OK) return fail(rc)
+    FV_A(s->pos, N);
+    FV_A(s->scale, N);
+    FV_A(s->rot, N);
+    FV_A(s->col, N);
+    FV_A(s->rec0, N);
+    FV_A(s->rec1, N);
+    FV_A(s->rec2, N);
+    FV_A(s->bin0, N);
+    FV_A(s->bin1, N);
+    FV_A(s->counts, N);
+    FV_A(s->offsets, N);
+    FV_A(s->partials, scan_partials_size((int)N) + 1);
+    const int ntx = (max_width + P.tile_w - 1) / P.tile_w, nty = (max_height + P.tile_h - 1) / P.tile_h;
+    s->cap_tiles = ntx * nty;
+    FV_A(s->ranges, (size_t)s->cap_tiles);
+    FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
+    FV_A(s->pose, 1);
+    FV_A(s->jj, 48);
+    FV_A(s->step, 8);
+    FV_A(s->st, 1);
+    FV_A(s->sort.ctrl, sort_ctrl_words());
+#undef FV_A
+    if (cudaMallocHost(&s->h_jj, sizeof(double) * 48) != cudaSuccess ||
+        cudaMallocHost(&s->h_st, sizeof(DevStatus)) != cudaSuccess ||
+        cudaMallocHost(&s->h_pose, sizeof(fvgs_pose)) != cudaSuccess ||
+        cudaMallocHost(&s->h_devpose, sizeof(DevPose)) != cudaSuccess)
+        return fail(FVGS_E_NOMEM);
+    if (sort_init(&s->sort, device) != cudaSuccess) return fail(FVGS_E_CUDA);
+    const uint64_t cap0 = std::max<uint64_t>(1u << 20, 8ull * N);
+    if ((rc = alloc_instances(s, std::min<uint64_t>(cap0, 0xffffffffull))) != FVGS_OK) return fail(rc);
+    if (cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
+    *out = s;
+    return FVGS_OK;
+}
+
+int fvgs_session_set_stream(fvgs_session* s, void* stream) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    s->stream = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+    return FVGS_OK;
+}
+
+int fvgs_session_sync(fvgs_session* s) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_session_set_debug(fvgs_session* s, uint32_t flags) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if ((flags & FVGS_DEBUG_PROJECTION) && !s->dbg_cov) {
+        FV_TRY(dev_alloc(s, &s->dbg_cov, 3 * (size_t)s->cap_g));
+        FV_TRY(dev_alloc(s, &s->dbg_inv, 3 * (size_t)s->cap_g));
+        FV_TRY(dev_alloc(s, &s->dbg_vis, (size_t)s->cap_g));
+    }
+    if (flags & FVGS_DEBUG_IMAGES) FV_TRY(ensure_images(s, (size_t)s->max_w * s->max_h));
+    s->debug = flags;
+    return FVGS_OK;
+}
+
+int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes) {
+    if (!s || !bytes) return FVGS_E_INVALID;
+    *bytes = s->footprint;
+    return FVGS_OK;
+}
+
+int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* scales, const float* orientations,
+                          const float* colors, const float* opacities, uint32_t n) {
+    if (!s || n > s->cap_g || (n && (!positions || !scales || !orientations || !colors || !opacities)))
+        return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    s->n_g = n;
+    s->has_binning = s->has_track = false;
+    if (n == 0) return FVGS_OK;
+    // Stage through rec planes (free until the next binning) so host arrays of
+    // the reference's float3 layout become 16-byte vectors on the device.
+    float* tmp = reinterpret_cast<float*>(s->rec0);  // 4N floats
+    float* tmp2 = reinterpret_cast<float*>(s->rec1);
+    float* tmp3 = reinterpret_cast<float*>(s->rec2);
+    float* tmp4 = reinterpret_cast<float*>(s->bin1);
+    float* tmp5 = reinterpret_cast<float*>(s->bin0);
+    FV_CK(cudaMemcpyAsync(tmp, positions, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(tmp2, scales, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(tmp3, orientations, sizeof(float) * 4 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(tmp4, colors, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(tmp5, opacities, sizeof(float) * n, cudaMemcpyDefault, s->stream));
+    upload_pack_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(tmp, tmp2, tmp3, tmp4, tmp5, n, s->pos, s->scale,
+                                                               s->rot, s->col);
+    FV_CK(cudaGetLastError());
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, float* orientations, float* colors,
+                            float* opacities, uint32_t n) {
+    if (!s || n > s->n_g || (n && (!positions || !scales || !orientations || !colors || !opacities)))
+        return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (n == 0) return FVGS_OK;
+    float* tmp = reinterpret_cast<float*>(s->rec0);
+    float* tmp2 = reinterpret_cast<float*>(s->rec1);
+    float* tmp3 = reinterpret_cast<float*>(s->rec2);
+    float* tmp4 = reinterpret_cast<float*>(s->bin1);
+    float* tmp5 = reinterpret_cast<float*>(s->bin0);
+    download_unpack_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->pos, s->scale, s->rot, s->col, n, tmp, tmp2,
+                                                                   tmp3, tmp4, tmp5);
+    FV_CK(cudaGetLastError());
+    FV_CK(cudaMemcpyAsync(positions, tmp, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(scales, tmp2, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(orientations, tmp3, sizeof(float) * 4 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(colors, tmp4, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(opacities, tmp5, sizeof(float) * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    s->has_binning = s->has_track = false;  // staging overwrote the records
+    return FVGS_OK;
+}
+
+int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* depth, const float* grad_x,
+                   const float* grad_y, int width, int height) {
+    if (!s || level < 0 || level >= kMaxLevels || !rgb || !depth || !grad_x || !grad_y) return FVGS_E_INVALID;
+    if (check_view(s, width, height) != FVGS_OK) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FrameLevel& f = s->lv[level];
+    const size_t px = (size_t)width * height;
+    if (px > f.cap_px) {
+        dev_free(s, f.rgb, 3 * f.cap_px);
+        dev_free(s, f.depth, f.cap_px);
+        dev_free(s, f.gx, 3 * f.cap_px);
+        dev_free(s, f.gy, 3 * f.cap_px);
+        FV_TRY(dev_alloc(s, &f.rgb, 3 * px));
+        FV_TRY(dev_alloc(s, &f.depth, px));
+        FV_TRY(dev_alloc(s, &f.gx, 3 * px));
+        FV_TRY(dev_alloc(s, &f.gy, 3 * px));
+        f.cap_px = px;
+    }
+    f.W = width;
+    f.H = height;
+    FV_CK(cudaMemcpyAsync(f.rgb, rgb, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(f.depth, depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(f.gx, grad_x, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(f.gy, grad_y, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_project_bin(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                     uint32_t* n_instances) {
+    if (!s || !valid_pose(pose) || !K) return FVGS_E_INVALID;
+    FV_TRY(check_view(s, width, height));
+    FV_CK(cudaSetDevice(s->device));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, width, height));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        if (n_instances) *n_instances = s->h_st->n_instances;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_download_projection(fvgs_session* s, float* uv, float* cov2d, float* inv2d, float* depth, float* phat,
+                             uint8_t* visible, uint32_t* tile_counts) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->has_binning) return FVGS_E_STATE;
+    if ((cov2d || inv2d || visible) && !s->dbg_proj_valid) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const size_t n = s->n_g;
+    std::vector<float4> r0(n), r1(n), r2(n);
+    FV_CK(cudaMemcpyAsync(r0.data(), s->rec0, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaMemcpyAsync(r1.data(), s->rec1, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaMemcpyAsync(r2.data(), s->rec2, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    if (cov2d) FV_CK(cudaMemcpyAsync(cov2d, s->dbg_cov, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    if (inv2d) FV_CK(cudaMemcpyAsync(inv2d, s->dbg_inv, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
+    if (visible) FV_CK(cudaMemcpyAsync(visible, s->dbg_vis, n, cudaMemcpyDefault, s->stream));
+    if (tile_counts) FV_CK(cudaMemcpyAsync(tile_counts, s->counts, sizeof(uint32_t) * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    for (size_t i = 0; i < n; ++i) {
+        if (uv) {
+            uv[2 * i] = r0[i].x;
+            uv[2 * i + 1] = r0[i].y;
+        }
+        if (depth) depth[i] = r0[i].z;
+        if (phat) {
+            phat[2 * i] = r1[i].w;
+            phat[2 * i + 1] = r2[i].x;
+        }
+    }
+    return FVGS_OK;
+}
+
+int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uint32_t* ranges,
+                          uint64_t max_instances, uint32_t* n_instances) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->has_binning) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    const uint32_t n = s->h_st->n_instances_clamped;
+    if (n_instances) *n_instances = n;
+    if ((keys || values) && n > max_instances) return FVGS_E_CAPACITY;
+    if (keys && n) FV_CK(cudaMemcpyAsync(keys, s->keys, sizeof(uint64_t) * n, cudaMemcpyDefault, s->stream));
+    if (values && n) FV_CK(cudaMemcpyAsync(values, s->vals, sizeof(uint32_t) * n, cudaMemcpyDefault, s->stream));
+    if (ranges) FV_CK(cudaMemcpyAsync(ranges, s->ranges, sizeof(uint2) * s->last_T, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_track_jacobian(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, double* JtJ,
+                        double* Jtr) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || !JtJ || !Jtr) return FVGS_E_INVALID;
+    const FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const bool images = (s->debug & FVGS_DEBUG_IMAGES) != 0;
+    if (images) FV_TRY(ensure_images(s, (size_t)f.W * f.H));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_track(s, K, f, false, images));
+        FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_jj, s->jj, sizeof(double) * 42, cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        std::memcpy(JtJ, s->h_jj, sizeof(double) * 36);
+        std::memcpy(Jtr, s->h_jj + 36, sizeof(double) * 6);
+        s->has_track = true;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_download_tile_partials(fvgs_session* s, float* tiles, int num_tiles) {
+    if (!s || !tiles) return FVGS_E_INVALID;
+    if (!s->has_track) return FVGS_E_STATE;
+    if (num_tiles < s->last_T) return FVGS_E_CAPACITY;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaMemcpyAsync(tiles, s->tile_out, sizeof(float) * 27 * s->last_T, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_download_track_images(fvgs_session* s, float* color, float* depth, float* final_T, uint32_t* n_contrib) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->has_track || !(s->debug & FVGS_DEBUG_IMAGES)) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px = (size_t)s->last_W * s->last_H;
+    if (color) FV_CK(cudaMemcpyAsync(color, s->img_color, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    if (depth) FV_CK(cudaMemcpyAsync(depth, s->img_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    if (final_T) FV_CK(cudaMemcpyAsync(final_T, s->img_T, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    if (n_contrib) FV_CK(cudaMemcpyAsync(n_contrib, s->img_nc, sizeof(uint32_t) * px, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                     double* last_step) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0) return FVGS_E_INVALID;
+    const FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const fvgs_pose start = *pose;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, &start));
+        for (int it = 0; it < iterations; ++it) {
+            FV_TRY(enqueue_bin(s, K, f.W, f.H));
+            FV_TRY(enqueue_track(s, K, f, false, false));
+            FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+            FV_CK(launch_gn_update(s->jj, s->params.eig_eps, s->pose, s->step, s->stream));
+        }
+        FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        for (int k = 0; k < 3; ++k) pose->position[k] = s->h_devpose->t[k];
+        for (int k = 0; k < 4; ++k) pose->orientation[k] = s->h_devpose->q[k];
+        if (last_step) std::memcpy(last_step, s->h_jj + 42, sizeof(double) * 6);
+        s->has_track = iterations > 0;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height, float* rgb,
+                float* depth, float* final_T, uint32_t* n_contrib) {
+    if (!s || !valid_pose(pose) || !K) return FVGS_E_INVALID;
+    FV_TRY(check_view(s, width, height));
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px = (size_t)width * height;
+    FV_TRY(ensure_images(s, px));
+    FrameLevel view;
+    view.W = width;
+    view.H = height;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, width, height));
+        FV_TRY(enqueue_track(s, K, view, true, true));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        if (rgb) FV_CK(cudaMemcpyAsync(rgb, s->img_color, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+        if (depth) FV_CK(cudaMemcpyAsync(depth, s->img_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+        if (final_T) FV_CK(cudaMemcpyAsync(final_T, s->img_T, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+        if (n_contrib) FV_CK(cudaMemcpyAsync(n_contrib, s->img_nc, sizeof(uint32_t) * px, cudaMemcpyDefault, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+}  // extern "C"

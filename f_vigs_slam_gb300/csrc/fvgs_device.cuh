@@ -1,0 +1,76 @@
+// fvgs_device.cuh -- device-side layouts and helpers shared by the sm_103a
+// kernels of the fvgs library.
+//
+// HBM layout (one session):
+//   Gaussians, SoA of 16-byte vectors (read with 128-bit loads):
+//     g_pos[N]   float4 (x, y, z, 0)
+//     g_scale[N] float4 (sx, sy, sz, 0)
+//     g_rot[N]   float4 (x, y, z, w)      raw quaternion as the reference reads it
+//     g_col[N]   float4 (r, g, b, opacity)
+//   Blending record, 48 B per Gaussian (three float4 planes):
+//     rec0 = (u, v, z, opacity)
+//     rec1 = (c.x, c.y, c.z, phat.x)      c = inverse 2D covariance in the order
+//     rec2 = (phat.y, r, g, b)             the blending kernels consume it
+//   Binning record, 32 B per Gaussian: (rect x0|y0<<16, x1|y1<<16, count, -,
+//     u, v, z, phat.x) and phat.y kept in rec2.x.
+//   Instances: u64 key = tile << 32 | float bits of the tile-centre depth,
+//     u32 value = Gaussian index; two ping-pong buffers for the radix sort.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fvgs_types.h"
+
+namespace fvgs {
+
+constexpr uint32_t kFullMask = 0xffffffffu;
+
+// Device-side status word bits (session->status[0]); host reads after a step.
+constexpr uint32_t kErrOverflow = 1u << 0;  // instance capacity exceeded
+constexpr uint32_t kErrTimeout = 1u << 1;   // bounded wait gave up
+constexpr uint32_t kErrBounds = 1u << 2;    // index check failed (debug builds)
+
+// Status block layout in device memory (u32 words).
+struct DevStatus {
+    uint32_t flags;         // kErr* bits
+    uint32_t n_instances;   // total instances of the last binning (may exceed capacity)
+    uint32_t n_instances_clamped;  // min(total, capacity): the number sorted
+    uint32_t pad;
+};
+
+// Pose state kept on the device so a whole tracking frame runs without the host.
+struct DevPose {
+    float t[3];
+    float q[4];     // (x, y, z, w) as the kernels read it
+    float pad;
+    double td[3];   // master copy of the GN iterate
+    double qd[4];
+};
+
+// quaternionToMatrix (src/GSCudaKernels.cu:319-334) with the fixed FP32
+// operation order shared with the CPU restatement (bit-exact keys).
+__device__ __forceinline__ void quat_to_R(const float q[4], float R[3][3]) {
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    R[0][0] = __fmaf_rn(-2.f, __fmaf_rn(y, y, __fmul_rn(z, z)), 1.f);
+    R[0][1] = __fmul_rn(2.f, __fmaf_rn(x, y, -__fmul_rn(w, z)));
+    R[0][2] = __fmul_rn(2.f, __fmaf_rn(x, z, __fmul_rn(w, y)));
+    R[1][0] = __fmul_rn(2.f, __fmaf_rn(x, y, __fmul_rn(w, z)));
+    R[1][1] = __fmaf_rn(-2.f, __fmaf_rn(x, x, __fmul_rn(z, z)), 1.f);
+    R[1][2] = __fmul_rn(2.f, __fmaf_rn(y, z, -__fmul_rn(w, x)));
+    R[2][0] = __fmul_rn(2.f, __fmaf_rn(x, z, -__fmul_rn(w, y)));
+    R[2][1] = __fmul_rn(2.f, __fmaf_rn(y, z, __fmul_rn(w, x)));
+    R[2][2] = __fmaf_rn(-2.f, __fmaf_rn(x, x, __fmul_rn(y, y)), 1.f);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Bounded spin budget for device-side waits; on expiry a kernel records
+// kErrTimeout and carries on with a safe value instead of hanging.
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+}  // namespace fvgs

@@ -1,0 +1,111 @@
+// fvgs_launch.h -- host-side launchers of the fvgs kernels (internal to the
+// library; the public boundary is include/fvgs.h).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fvgs_types.h"
+
+namespace fvgs {
+
+struct DevStatus;
+struct DevPose;
+
+struct ProjectArgs {
+    const float4* pos;
+    const float4* scale;
+    const float4* rot;
+    const float4* col;
+    int n;
+    const DevPose* pose;
+    fvgs_intrinsics K;
+    int W, H, tw, th, ntx, nty;
+    float radius_sigma;
+    uint32_t quirks;
+    float4* rec0;
+    float4* rec1;
+    float4* rec2;
+    uint4* bin0;
+    float4* bin1;
+    uint32_t* counts;
+    float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
+    float* dbg_inv;    // optional: 3N inverse, stored order (xx, yy, xy)
+    uint8_t* dbg_vis;  // optional: N visibility
+};
+
+struct EmitArgs {
+    const uint4* bin0;
+    const float4* bin1;
+    const uint32_t* offsets;
+    int n;
+    int ntx, tw, th;
+    uint64_t capacity;
+    uint64_t* keys;
+    uint32_t* vals;
+};
+
+cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s);
+size_t scan_partials_size(int n);
+cudaError_t launch_scan(const uint32_t* counts, int n, uint32_t* partials, uint32_t* offsets, DevStatus* st,
+                        uint32_t capacity, cudaStream_t s);
+cudaError_t launch_emit_keys(const EmitArgs& a, cudaStream_t s);
+cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_tiles, uint32_t quirks,
+                          uint2* ranges, int grid, cudaStream_t s);
+
+// ---- radix sort (sort.cu) ----
+struct SortWorkspace {
+    uint64_t* keys_alt;
+    uint32_t* vals_alt;
+    uint64_t* lookback;   // [max_tiles][256] 64-bit status words
+    uint32_t* ctrl;       // [8 passes][256] histograms + [8] tile counters
+    uint64_t max_items;
+    uint32_t epoch;       // advanced per sort call; tags lookback words
+    int persistent_ctas;  // resident CTAs of the onesweep kernel
+};
+size_t sort_lookback_words(uint64_t max_items);
+size_t sort_ctrl_words();
+int sort_num_passes(int key_bits);
+cudaError_t sort_init(SortWorkspace* ws, int device);
+// Stable LSD radix sort of (keys, vals) over key bits [0, key_bits); the item
+// count is read from st->n_instances_clamped.  The result lands back in
+// keys/vals (an even number of passes is always run; passes <= 8 so key_bits
+// <= 64, and key_bits <= 56 whenever the padding pass is needed).
+cudaError_t launch_radix_sort(uint64_t* keys, uint32_t* vals, const DevStatus* st, int key_bits,
+                              SortWorkspace* ws, uint32_t* err_flags, cudaStream_t s);
+
+// ---- tracking (track.cu) ----
+struct TrackArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const float4* rec2;
+    const uint2* ranges;
+    const uint32_t* indices;
+    const float* obs_rgb;    // 3P
+    const float* obs_depth;  // P
+    const float* gx;         // 3P
+    const float* gy;         // 3P
+    const DevPose* pose;
+    fvgs_intrinsics K;
+    int W, H, ntx, nty;
+    float bg[3];
+    float alpha_thresh, color_thresh, depth_thresh;
+    float* tile_out;  // [T][27] camera-frame partials
+    // optional per-pixel outputs of the forward blend
+    float* img_color;    // 3P
+    float* img_depth;    // P
+    float* img_T;        // P
+    uint32_t* img_nc;    // P
+    int render_only;     // 1: forward blend for every in-bounds pixel, no Jacobian
+};
+cudaError_t launch_track(const TrackArgs& a, cudaStream_t s);
+// Sum tile partials in FP64, rotate to the world frame, write out[42] =
+// JtJ[36] (symmetric) then Jtr[6] (negated, as the reference host code does).
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, const DevPose* pose, double* out,
+                                cudaStream_t s);
+// One eigen-regularised Gauss-Newton update of the device pose from out[42].
+cudaError_t launch_gn_update(const double* jtj_jtr, double eig_eps, DevPose* pose, double* step_out,
+                             cudaStream_t s);
+
+}  // namespace fvgs

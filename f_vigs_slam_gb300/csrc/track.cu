@@ -1,0 +1,483 @@
+// track.cu -- fused tracking kernel (forward blend + RGB-D pose Jacobian +
+// per-tile J^T J / J^T r reduction), the frame reduction, and the on-device
+// Gauss-Newton pose update, for sm_103a.
+//
+// Reference: getRgbdPoseJacobians (src/GSCudaKernels.cu:922-1392), the host
+// reduction and sign convention of GSSlam::computeRgbdPoseJacobians
+// (src/GSSlam.cu:2205-2226), the eigen-regularised pseudo factor of
+// RgbdPoseCostFunction::Evaluate (src/RgbdPoseCost.cu:57-106) and the pose
+// update PoseLocalParameterization::Plus (src/PoseLocalParameterization.cpp:22-44).
+//
+// Per-pixel semantics are the reference's (each pixel scans its tile list,
+// thresholds 0.99 / 1/255 / 1e-4 / 0.5 / 1e-3, the pass-1-only v<=0 skip, the
+// second pass over the first n_contrib entries).  The arithmetic is
+// reorganised for the GPU without changing the mathematics:
+//  * every per-Gaussian colour term is rank one (Jt_cam = jt_dl (x) alpha*dC),
+//    so J_pose * JtJ_cam * J_pose^T becomes one 21-FMA update with
+//    u = (jt_dl, d * (ray x jt_dl)) instead of the reference's 3x3 and 6x3
+//    products;
+//  * terms are accumulated in the camera frame (translation rows without R)
+//    and rotated once per frame, in FP64, by diag(R, I);
+//  * the 27 per-thread sums are reduced by a 31-shuffle butterfly
+//    reduce-scatter, then across the 8 warps in a fixed order, and written
+//    once per tile (no atomics: results are run-to-run deterministic).
+#include "fvgs_device.cuh"
+#include "fvgs_launch.h"
+
+namespace fvgs {
+
+constexpr int kTW = 16, kTH = 16, kPix = kTW * kTH;
+constexpr int kBatch = 256;
+constexpr float kInv255 = 1.0f / 255.0f;
+
+__device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
+                                             float r0, float r1, float r2) {
+    // u = (a, d * (r x a))
+    const float u[6] = {a0, a1, a2, d * (r1 * a2 - r2 * a1), d * (r2 * a0 - r0 * a2), d * (r0 * a1 - r1 * a0)};
+    int idx = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const float wu = w * u[i];
+#pragma unroll
+        for (int j = i; j < 6; ++j) A[idx++] += wu * u[j];
+    }
+}
+
+// Butterfly reduce-scatter of 32 values over a warp: lane l ends with the warp
+// sum of value l.
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < o; ++k) {
+            const float send = upper ? v[k] : v[k + o];
+            const float keep = upper ? v[k + o] : v[k];
+            v[k] = keep + __shfl_xor_sync(kFullMask, send, o);
+        }
+    }
+    return v[0];
+}
+
+template <bool RENDER_ONLY>
+__global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
+    __shared__ float4 s0[kBatch];
+    __shared__ float4 s1[kBatch];
+    __shared__ float4 s2[kBatch];
+    __shared__ float s_red[kPix / 32][32];
+    __shared__ uint32_t s_nmax;
+
+    const int tile = blockIdx.x;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int tid = threadIdx.x;
+    const int x = tx * kTW + (tid & (kTW - 1)), y = ty * kTH + tid / kTW;
+    const bool in_bounds = (x < a.W && y < a.H);
+    const size_t p = (size_t)y * a.W + x;
+    const uint2 range = a.ranges[tile];
+    const int n = (int)(range.y - range.x);
+    const float xf = (float)x, yf = (float)y;
+
+    float img_depth = 0.f;
+    if (!RENDER_ONLY && in_bounds) img_depth = a.obs_depth[p];
+    const bool inside = RENDER_ONLY ? in_bounds : (in_bounds && img_depth > 0.1f);
+
+    // ------------------------- pass 1: forward blend -------------------------
+    float T = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, depth = 0.f;
+    uint32_t contributor = 0, last = 0;
+    bool done = !inside;
+    float final_T = 1.f;
+    uint32_t n_contrib = 0;
+    if (n > 0) {
+        for (int base = 0; base < n; base += kBatch) {
+            if (__syncthreads_and(done)) break;
+            const int li = base + tid;
+            if (li < n) {
+                const uint32_t g = a.indices[range.x + li];
+                s0[tid] = a.rec0[g];
+                s1[tid] = a.rec1[g];
+                s2[tid] = a.rec2[g];
+            }
+            __syncthreads();
+            if (!done) {
+                const int cnt = min(kBatch, n - base);
+                for (int j = 0; j < cnt; ++j) {
+                    const float4 r0 = s0[j];
+                    const float4 r1 = s1[j];
+                    ++contributor;
+                    const float dx = r0.x - xf, dy = r0.y - yf;
+                    const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+                    const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
+                    if (alpha < kInv255 || v <= 0.0f) continue;
+                    const float test_T = T * (1.0f - alpha);
+                    if (test_T < 0.0001f) {
+                        done = true;
+                        break;
+                    }
+                    const float4 r2 = s2[j];
+                    cr += r2.y * alpha * T;
+                    cg += r2.z * alpha * T;
+                    cb += r2.w * alpha * T;
+                    const float d = r0.z + dx * r1.w + dy * r2.x;
+                    if (T > 0.5f && test_T < 0.5f) depth = d;
+                    T = test_T;
+                    last = contributor;
+                }
+            }
+        }
+        if (inside) {
+            final_T = T;
+            n_contrib = last;
+            cr += T * a.bg[0];
+            cg += T * a.bg[1];
+            cb += T * a.bg[2];
+        }
+    }
+    if (a.img_color && in_bounds) {
+        a.img_color[3 * p] = cr;
+        a.img_color[3 * p + 1] = cg;
+        a.img_color[3 * p + 2] = cb;
+        a.img_depth[p] = depth;
+        a.img_T[p] = final_T;
+        a.img_nc[p] = n_contrib;
+    }
+    if (RENDER_ONLY) return;
+
+    // ------------------------- per-pixel term -------------------------------
+    const bool do_jac = inside && (final_T < a.alpha_thresh);
+    float A[21];
+    float bv[6];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) A[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) bv[k] = 0.f;
+    const float fx = a.K.fx, fy = a.K.fy, cx = a.K.cx, cy = a.K.cy;
+    float e0 = 0.f, e1 = 0.f, e2 = 0.f, wc = 0.f, derr = 0.f, wd = 0.f;
+    if (do_jac) {
+        e0 = cr - a.obs_rgb[3 * p];
+        e1 = cg - a.obs_rgb[3 * p + 1];
+        e2 = cb - a.obs_rgb[3 * p + 2];
+        derr = (img_depth > 0.1f) ? (depth - img_depth) : 0.0f;
+        const float closs = sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+        wc = (closs < a.color_thresh) ? 1.0f : a.color_thresh / closs;
+        const float rx = (xf - cx) / fx, ry = (yf - cy) / fy;
+        const float inv_id = 1.0f / img_depth;
+        const float j0 = fx * inv_id, j3 = fy * inv_id, j4 = -fx * rx * inv_id, j5 = -fy * ry * inv_id;
+        const float gX[3] = {a.gx[3 * p], a.gx[3 * p + 1], a.gx[3 * p + 2]};
+        const float gY[3] = {a.gy[3 * p], a.gy[3 * p + 1], a.gy[3 * p + 2]};
+        const float ee[3] = {e0, e1, e2};
+        float Jr0 = 0.f, Jr1 = 0.f, Jr2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float c0 = j0 * gX[k], c1 = j3 * gY[k], c2 = j4 * gX[k] + j5 * gY[k];
+            rank1_update(A, wc, c0, c1, c2, img_depth, rx, ry, 1.0f);
+            Jr0 += c0 * ee[k];
+            Jr1 += c1 * ee[k];
+            Jr2 += c2 * ee[k];
+        }
+        Jr0 *= -wc;
+        Jr1 *= -wc;
+        Jr2 *= -wc;
+        const float ld = fabsf(derr);
+        wd = ((ld < a.depth_thresh) ? 1.0f : a.depth_thresh / ld) / img_depth;
+        // wd * ray ray^T: the rotation block gets ray x ray = 0
+        {
+            const float r[3] = {rx, ry, 1.0f};
+            int idx = 0;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                for (int j = i; j < 6; ++j) {
+                    if (j < 3) A[idx] += wd * r[i] * r[j];
+                    ++idx;
+                }
+            }
+        }
+        Jr0 += wd * derr * rx;
+        Jr1 += wd * derr * ry;
+        Jr2 += wd * derr;
+        bv[0] += Jr0;
+        bv[1] += Jr1;
+        bv[2] += Jr2;
+        bv[3] += img_depth * (ry * Jr2 - 1.0f * Jr1);
+        bv[4] += img_depth * (1.0f * Jr0 - rx * Jr2);
+        bv[5] += img_depth * (rx * Jr1 - ry * Jr0);
+    }
+
+    // ------------------- pass 2: per-Gaussian terms --------------------------
+    if (tid == 0) s_nmax = 0;
+    __syncthreads();
+    if (do_jac && n_contrib > 0) atomicMax(&s_nmax, n_contrib);
+    __syncthreads();
+    const int nmax = (int)min((uint32_t)n, s_nmax);
+    float prod_alpha = 1.f, Tm = 1.f, acr = 0.f, acg = 0.f, acb = 0.f;
+    bool done2 = !do_jac;
+    const float inv_fx = 1.0f / fx, inv_fy = 1.0f / fy;
+    for (int base = 0; base < nmax; base += kBatch) {
+        if (__syncthreads_and(done2)) break;
+        const int li = base + tid;
+        if (li < nmax) {
+            const uint32_t g = a.indices[range.x + li];
+            s0[tid] = a.rec0[g];
+            s1[tid] = a.rec1[g];
+            s2[tid] = a.rec2[g];
+        }
+        __syncthreads();
+        if (!done2) {
+            const int cnt = min(kBatch, nmax - base);
+            for (int j = 0; j < cnt; ++j) {
+                if (base + j >= (int)n_contrib) {
+                    done2 = true;
+                    break;
+                }
+                const float4 r0 = s0[j];
+                const float4 r1 = s1[j];
+                const float dx = r0.x - xf, dy = r0.y - yf;
+                const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+                const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
+                if (alpha < kInv255) continue;
+                const float4 r2 = s2[j];
+                const float d = r0.z + dx * r1.w + dy * r2.x;
+                float da0 = r2.y * prod_alpha, da1 = r2.z * prod_alpha, da2 = r2.w * prod_alpha;
+                acr += alpha * da0;
+                acg += alpha * da1;
+                acb += alpha * da2;
+                const float inv1m = 1.0f / (1.0f - alpha);
+                da0 -= (cr - acr) * inv1m;
+                da1 -= (cg - acg) * inv1m;
+                da2 -= (cb - acb) * inv1m;
+                const float dl0 = r1.x * dx + r1.y * dy;
+                const float dl1 = r1.y * dx + r1.z * dy;
+                const float rgx = (r0.x - cx) * inv_fx, rgy = (r0.y - cy) * inv_fy;
+                const float inv_d = 1.0f / d;
+                const float jt0 = fx * inv_d * dl0;
+                const float jt1 = fy * inv_d * dl1;
+                const float jt2 = (-fx * rgx * inv_d) * dl0 + (-fy * rgy * inv_d) * dl1;
+                const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
+                rank1_update(A, w, jt0, jt1, jt2, d, rgx, rgy, 1.0f);
+                const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
+                float Jr0 = coef * jt0, Jr1 = coef * jt1, Jr2 = coef * jt2;
+                prod_alpha *= (1.0f - alpha);
+                if (Tm > 0.5f && prod_alpha <= 0.5f && img_depth > 0.5f) {
+                    Tm = prod_alpha;
+                    const float r[3] = {rgx, rgy, 1.0f};
+                    int idx = 0;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                        for (int jj = i; jj < 6; ++jj) {
+                            if (jj < 3) A[idx] += wd * r[i] * r[jj];
+                            ++idx;
+                        }
+                    }
+                    Jr0 += wd * derr * rgx;
+                    Jr1 += wd * derr * rgy;
+                    Jr2 += wd * derr;
+                }
+                bv[0] += Jr0;
+                bv[1] += Jr1;
+                bv[2] += Jr2;
+                bv[3] += d * (rgy * Jr2 - Jr1);
+                bv[4] += d * (Jr0 - rgx * Jr2);
+                bv[5] += d * (rgx * Jr1 - rgy * Jr0);
+                if (prod_alpha < 0.001f) {
+                    done2 = true;
+                    break;
+                }
+            }
+        }
+    }
+
+    // --------------------------- tile reduction ------------------------------
+    float vals[32];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) vals[k] = bv[k];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) vals[6 + k] = A[k];
+#pragma unroll
+    for (int k = 27; k < 32; ++k) vals[k] = 0.f;
+    const float mine = warp_reduce_scatter32(vals);
+    s_red[tid >> 5][tid & 31] = mine;
+    __syncthreads();
+    if (tid < FVGS_POSEDATA_FLOATS) {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < kPix / 32; ++w) s += s_red[w][tid];
+        a.tile_out[(size_t)tile * FVGS_POSEDATA_FLOATS + tid] = s;
+    }
+}
+
+// FP64 sum over tiles (fixed order), world-frame rotation, symmetric 6x6,
+// Jtr negated.  One CTA of 256 threads.
+__global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles,
+                                                           const DevPose* pose, double* out) {
+    __shared__ double s_part[8][27];
+    __shared__ double s_tot[27];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    // warp w sums tiles w, w+8, ...; lane k < 27 owns value k
+    double acc = 0.0;
+    if (lane < 27)
+        for (int t = w; t < num_tiles; t += 8) acc += (double)tile_out[(size_t)t * 27 + lane];
+    if (lane < 27) s_part[w][lane] = acc;
+    __syncthreads();
+    if (tid < 27) {
+        double s = 0.0;
+        for (int k = 0; k < 8; ++k) s += s_part[k][tid];
+        s_tot[tid] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+        double R[3][3];
+        R[0][0] = 1.0 - 2.0 * (qy * qy + qz * qz);
+        R[0][1] = 2.0 * (qx * qy - qw * qz);
+        R[0][2] = 2.0 * (qx * qz + qw * qy);
+        R[1][0] = 2.0 * (qx * qy + qw * qz);
+        R[1][1] = 1.0 - 2.0 * (qx * qx + qz * qz);
+        R[1][2] = 2.0 * (qy * qz - qw * qx);
+        R[2][0] = 2.0 * (qx * qz - qw * qy);
+        R[2][1] = 2.0 * (qy * qz + qw * qx);
+        R[2][2] = 1.0 - 2.0 * (qx * qx + qy * qy);
+        double Ac[6][6];
+        int idx = 0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) {
+                Ac[i][j] = s_tot[6 + idx];
+                Ac[j][i] = s_tot[6 + idx];
+                ++idx;
+            }
+        double D[6][6];
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) D[i][j] = 0.0;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) D[i][j] = R[i][j];
+        for (int i = 3; i < 6; ++i) D[i][i] = 1.0;
+        double DA[6][6];
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += D[i][k] * Ac[k][j];
+                DA[i][j] = s;
+            }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += DA[i][k] * D[j][k];
+                out[i * 6 + j] = s;
+            }
+        for (int i = 0; i < 6; ++i) {
+            double s = 0.0;
+            for (int k = 0; k < 6; ++k) s += D[i][k] * s_tot[k];
+            out[36 + i] = -s;
+        }
+    }
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 6x6 (FP64), the
+// pseudo-factor step delta = -sum_{lambda_i > eps} (u_i . g / lambda_i) u_i,
+// which is the Gauss-Newton step of the residual/Jacobian pair that
+// RgbdPoseCostFunction::Evaluate hands to Ceres, then Plus on the pose.
+__global__ void gn_update_kernel(const double* __restrict__ jj, double eig_eps, DevPose* pose, double* step_out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double A[6][6], V[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            A[i][j] = jj[i * 6 + j];
+            V[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                tot += A[i][j] * A[i][j];
+                if (i != j) off += A[i][j] * A[i][j];
+            }
+        if (off <= 1e-30 * tot) break;
+        for (int pq = 0; pq < 15; ++pq) {
+            int p = 0, q = 0, c = 0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i + 1; j < 6; ++j) {
+                    if (c == pq) {
+                        p = i;
+                        q = j;
+                    }
+                    ++c;
+                }
+            const double apq = A[p][q];
+            if (apq == 0.0) continue;
+            const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+            for (int k = 0; k < 6; ++k) {
+                const double akp = A[k][p], akq = A[k][q];
+                A[k][p] = cs * akp - sn * akq;
+                A[k][q] = sn * akp + cs * akq;
+            }
+            for (int k = 0; k < 6; ++k) {
+                const double apk = A[p][k], aqk = A[q][k];
+                A[p][k] = cs * apk - sn * aqk;
+                A[q][k] = sn * apk + cs * aqk;
+            }
+            for (int k = 0; k < 6; ++k) {
+                const double vkp = V[k][p], vkq = V[k][q];
+                V[k][p] = cs * vkp - sn * vkq;
+                V[k][q] = sn * vkp + cs * vkq;
+            }
+        }
+    }
+    double delta[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 6; ++i) {
+        const double lam = A[i][i];
+        if (!(lam > eig_eps)) continue;
+        double ug = 0.0;
+        for (int k = 0; k < 6; ++k) ug += V[k][i] * jj[36 + k];
+        for (int k = 0; k < 6; ++k) delta[k] -= (ug / lam) * V[k][i];
+    }
+    for (int k = 0; k < 3; ++k) pose->td[k] += delta[k];
+    const double ax = pose->qd[0], ay = pose->qd[1], az = pose->qd[2], aw = pose->qd[3];
+    const double bx = 0.5 * delta[3], by = 0.5 * delta[4], bz = 0.5 * delta[5];
+    double nx = aw * bx + ax + (ay * bz - az * by);
+    double ny = aw * by + ay + (az * bx - ax * bz);
+    double nz = aw * bz + az + (ax * by - ay * bx);
+    double nw = aw - (ax * bx + ay * by + az * bz);
+    const double nn = sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+    nx /= nn;
+    ny /= nn;
+    nz /= nn;
+    nw /= nn;
+    pose->qd[0] = nx;
+    pose->qd[1] = ny;
+    pose->qd[2] = nz;
+    pose->qd[3] = nw;
+    for (int k = 0; k < 3; ++k) pose->t[k] = (float)pose->td[k];
+    pose->q[0] = (float)nx;
+    pose->q[1] = (float)ny;
+    pose->q[2] = (float)nz;
+    pose->q[3] = (float)nw;
+    if (step_out)
+        for (int k = 0; k < 6; ++k) step_out[k] = delta[k];
+}
+
+cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
+    const int T = a.ntx * a.nty;
+    if (T <= 0) return cudaSuccess;
+    if (a.render_only)
+        track_tile_kernel<true><<<T, kPix, 0, s>>>(a);
+    else
+        track_tile_kernel<false><<<T, kPix, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, const DevPose* pose, double* out,
+                                cudaStream_t s) {
+    track_reduce_kernel<<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gn_update(const double* jtj_jtr, double eig_eps, DevPose* pose, double* step_out,
+                             cudaStream_t s) {
+    gn_update_kernel<<<1, 32, 0, s>>>(jtj_jtr, eig_eps, pose, step_out);
+    return cudaGetLastError();
+}
+
+}  // namespace fvgs

@@ -1,0 +1,284 @@
+"""Python binding of the fvgs C-ABI (include/fvgs.h) via ctypes.
+
+This is the host-side mirror used by tests and the benchmark; the C++
+compatibility layer (GSSlam / RgbdPoseCostFunction shapes) sits on the same
+C-ABI.  There is no CPU fallback: if libfvgs.so is missing or has no GPU to
+run on, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfvgs.so")
+
+FVGS_OK = 0
+STATUS_NAMES = {
+    0: "FVGS_OK", -1: "FVGS_E_INVALID", -2: "FVGS_E_NOMEM", -3: "FVGS_E_CUDA", -4: "FVGS_E_CAPACITY",
+    -5: "FVGS_E_TIMEOUT", -6: "FVGS_E_STATE", -7: "FVGS_E_ADMISSION",
+}
+
+Q_CULLED_SLOTS = 0x1
+Q_RANGE_LAUNCH = 0x2
+Q_INVSIGMA_SWAP = 0x4
+Q_MAP_CAP256 = 0x8
+QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
+
+DEBUG_PROJECTION = 0x1
+DEBUG_IMAGES = 0x2
+
+
+class FvgsError(RuntimeError):
+    def __init__(self, status: int, what: str, msg: str = ""):
+        self.status = status
+        super().__init__("%s failed: %s (%s) %s" % (what, STATUS_NAMES.get(status, status), status, msg))
+
+
+class Pose(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("orientation", C.c_float * 4)]
+
+
+class Intrinsics(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("radius_sigma", C.c_float),
+        ("bg", C.c_float * 3), ("alpha_thresh", C.c_float), ("color_thresh", C.c_float),
+        ("depth_thresh", C.c_float), ("w_depth", C.c_float), ("w_dist", C.c_float),
+        ("lambda_iso", C.c_float), ("adam_beta1", C.c_float), ("adam_beta2", C.c_float),
+        ("adam_eps", C.c_float), ("quirks", C.c_uint32), ("eig_eps", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libfvgs.so (build it with f_vigs_slam_gb300.build first)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(
+                "libfvgs.so not found at %s: build the CUDA library (python -m f_vigs_slam_gb300.build)" % path
+            )
+        lib = C.CDLL(path)
+        lib.fvgs_status_string.restype = C.c_char_p
+        lib.fvgs_status_string.argtypes = [C.c_int]
+        _lib = lib
+    return _lib
+
+
+def _check(status: int, what: str):
+    if status != FVGS_OK:
+        msg = load_library().fvgs_status_string(status).decode()
+        raise FvgsError(status, what, msg)
+
+
+def default_params(quirks: int = QUIRKS_DEFAULT) -> Params:
+    p = Params()
+    _check(load_library().fvgs_params_default(C.byref(p)), "fvgs_params_default")
+    p.quirks = quirks
+    return p
+
+
+def make_pose(pose) -> Pose:
+    t, q = pose
+    p = Pose()
+    p.position[:] = [float(v) for v in np.asarray(t, np.float32)]
+    p.orientation[:] = [float(v) for v in np.asarray(q, np.float32)]
+    return p
+
+
+def make_intr(K) -> Intrinsics:
+    i = Intrinsics()
+    i.fx, i.fy, i.cx, i.cy = [float(np.float32(v)) for v in K]
+    return i
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Session:
+    """One SLAM map resident on one GPU (fvgs_session)."""
+
+    def __init__(self, capacity: int, max_width: int, max_height: int, params: Params | None = None,
+                 device: int = 0):
+        self.lib = load_library()
+        self.params = params if params is not None else default_params()
+        h = C.c_void_p()
+        _check(
+            self.lib.fvgs_session_create(C.byref(self.params), C.c_int(device), C.c_uint32(capacity),
+                                         C.c_int(max_width), C.c_int(max_height), C.byref(h)),
+            "fvgs_session_create",
+        )
+        self.h = h
+        self.n = 0
+        self.tile = (self.params.tile_w, self.params.tile_h)
+
+    def close(self):
+        if self.h:
+            self.lib.fvgs_session_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------------- state
+    def set_debug(self, flags: int):
+        _check(self.lib.fvgs_session_set_debug(self.h, C.c_uint32(flags)), "fvgs_session_set_debug")
+
+    def set_stream(self, stream_handle: int | None):
+        _check(self.lib.fvgs_session_set_stream(self.h, C.c_void_p(stream_handle or 0)), "fvgs_session_set_stream")
+
+    def sync(self):
+        _check(self.lib.fvgs_session_sync(self.h), "fvgs_session_sync")
+
+    def footprint(self) -> int:
+        b = C.c_uint64()
+        _check(self.lib.fvgs_session_footprint(self.h, C.byref(b)), "fvgs_session_footprint")
+        return int(b.value)
+
+    def upload(self, scene):
+        pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
+        col, opa = _f32(scene.colors), _f32(scene.opacities)
+        _check(
+            self.lib.fvgs_upload_gaussians(self.h, _ptr(pos), _ptr(scl), _ptr(rot), _ptr(col), _ptr(opa),
+                                           C.c_uint32(scene.n)),
+            "fvgs_upload_gaussians",
+        )
+        self.n = scene.n
+
+    def download(self):
+        n = self.n
+        pos = np.zeros((n, 3), np.float32)
+        scl = np.zeros((n, 3), np.float32)
+        rot = np.zeros((n, 4), np.float32)
+        col = np.zeros((n, 3), np.float32)
+        opa = np.zeros(n, np.float32)
+        _check(
+            self.lib.fvgs_download_gaussians(self.h, _ptr(pos), _ptr(scl), _ptr(rot), _ptr(col), _ptr(opa),
+                                             C.c_uint32(n)),
+            "fvgs_download_gaussians",
+        )
+        return pos, scl, rot, col, opa
+
+    def set_frame(self, level: int, rgb, depth, gx, gy):
+        rgb, depth, gx, gy = _f32(rgb), _f32(depth), _f32(gx), _f32(gy)
+        H, W = depth.shape
+        _check(
+            self.lib.fvgs_set_frame(self.h, C.c_int(level), _ptr(rgb), _ptr(depth), _ptr(gx), _ptr(gy),
+                                    C.c_int(W), C.c_int(H)),
+            "fvgs_set_frame",
+        )
+
+    # -------------------------------------------------------------- binning
+    def project_bin(self, pose, K, W, H) -> int:
+        n = C.c_uint32()
+        _check(
+            self.lib.fvgs_project_bin(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(W),
+                                      C.c_int(H), C.byref(n)),
+            "fvgs_project_bin",
+        )
+        return int(n.value)
+
+    def download_projection(self, debug: bool = True):
+        n = self.n
+        uv = np.zeros((n, 2), np.float32)
+        dep = np.zeros(n, np.float32)
+        ph = np.zeros((n, 2), np.float32)
+        cnt = np.zeros(n, np.uint32)
+        cov = np.zeros((n, 3), np.float32) if debug else None
+        inv = np.zeros((n, 3), np.float32) if debug else None
+        vis = np.zeros(n, np.uint8) if debug else None
+        _check(
+            self.lib.fvgs_download_projection(self.h, _ptr(uv), _ptr(cov), _ptr(inv), _ptr(dep), _ptr(ph),
+                                              _ptr(vis), _ptr(cnt)),
+            "fvgs_download_projection",
+        )
+        return dict(uv=uv, cov2d=cov, inv2d=inv, depth=dep, phat=ph, visible=vis, counts=cnt)
+
+    def num_tiles(self, W, H):
+        tw, th = self.tile
+        return ((W + tw - 1) // tw) * ((H + th - 1) // th)
+
+    def download_binning(self, W, H, max_instances: int | None = None):
+        n = C.c_uint32()
+        _check(self.lib.fvgs_download_binning(self.h, None, None, None, C.c_uint64(0), C.byref(n)),
+               "fvgs_download_binning")
+        cnt = int(n.value)
+        keys = np.zeros(max(cnt, 1), np.uint64)
+        vals = np.zeros(max(cnt, 1), np.uint32)
+        T = self.num_tiles(W, H)
+        ranges = np.zeros((T, 2), np.uint32)
+        _check(
+            self.lib.fvgs_download_binning(self.h, _ptr(keys), _ptr(vals), _ptr(ranges), C.c_uint64(cnt),
+                                           C.byref(n)),
+            "fvgs_download_binning",
+        )
+        return keys[:cnt], vals[:cnt], ranges
+
+    # ------------------------------------------------------------- tracking
+    def track_jacobian(self, pose, K, level: int = 0):
+        JtJ = np.zeros((6, 6), np.float64)
+        Jtr = np.zeros(6, np.float64)
+        _check(
+            self.lib.fvgs_track_jacobian(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
+                                         _ptr(JtJ), _ptr(Jtr)),
+            "fvgs_track_jacobian",
+        )
+        return JtJ, Jtr
+
+    def download_tile_partials(self, T: int):
+        out = np.zeros((T, 27), np.float32)
+        _check(self.lib.fvgs_download_tile_partials(self.h, _ptr(out), C.c_int(T)), "fvgs_download_tile_partials")
+        return out
+
+    def download_track_images(self, W, H):
+        col = np.zeros((H, W, 3), np.float32)
+        dep = np.zeros((H, W), np.float32)
+        fT = np.zeros((H, W), np.float32)
+        nc = np.zeros((H, W), np.uint32)
+        _check(self.lib.fvgs_download_track_images(self.h, _ptr(col), _ptr(dep), _ptr(fT), _ptr(nc)),
+               "fvgs_download_track_images")
+        return col, dep, fT, nc
+
+    def track_frame(self, pose, K, iterations: int = 20, level: int = 0):
+        p = make_pose(pose)
+        step = np.zeros(6, np.float64)
+        _check(
+            self.lib.fvgs_track_frame(self.h, C.byref(p), C.byref(make_intr(K)), C.c_int(level),
+                                      C.c_int(iterations), _ptr(step)),
+            "fvgs_track_frame",
+        )
+        return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
+
+    def render(self, pose, K, W, H):
+        col = np.zeros((H, W, 3), np.float32)
+        dep = np.zeros((H, W), np.float32)
+        fT = np.zeros((H, W), np.float32)
+        nc = np.zeros((H, W), np.uint32)
+        _check(
+            self.lib.fvgs_render(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(W), C.c_int(H),
+                                 _ptr(col), _ptr(dep), _ptr(fT), _ptr(nc)),
+            "fvgs_render",
+        )
+        return col, dep, fT, nc

@@ -1,0 +1,183 @@
+"""Seeded synthetic scenes and frames for the tracking / mapping workloads.
+
+The reference publishes no dataset; these generators produce inputs with the
+shapes and value distributions of its workloads:
+
+* ``cam_box``  -- N Gaussians with camera-frame means uniform in
+  [-2,2]x[-1.5,1.5]x[1,5] m seen from the identity pose, 640x480,
+  fx=fy=525, cx=319.5, cy=239.5 (the small plain-method workload).
+* ``room``     -- N Gaussians with means uniform in a 10x10x4 m room, a camera
+  trajectory that random-walks 1 cm / 0.5 deg per step, 1280x720
+  (the large plain-method workload).
+
+Distributions for every Gaussian: scales exp(N(-3, 0.5)) per axis,
+orientation normalise(N(0, I4)) stored (x, y, z, w), opacity sigmoid(N(0,1)),
+colour U[0,1].  Poses are returned as ``(t[3], q[4])`` float32 with q in the
+(x, y, z, w) order the kernels read (src/GSCudaKernels.cu:319-334).
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+IDENTITY_Q = np.array([0.0, 0.0, 0.0, 1.0], dtype=np.float32)
+
+
+@dataclasses.dataclass
+class Scene:
+    positions: np.ndarray  # (N,3) float32
+    scales: np.ndarray  # (N,3) float32
+    orientations: np.ndarray  # (N,4) float32, (x,y,z,w)
+    colors: np.ndarray  # (N,3) float32
+    opacities: np.ndarray  # (N,) float32
+
+    @property
+    def n(self) -> int:
+        return int(self.positions.shape[0])
+
+
+@dataclasses.dataclass
+class Camera:
+    width: int
+    height: int
+    fx: float
+    fy: float
+    cx: float
+    cy: float
+
+    @property
+    def intrinsics(self):
+        return (self.fx, self.fy, self.cx, self.cy)
+
+
+CAM_VGA = Camera(640, 480, 525.0, 525.0, 319.5, 239.5)
+CAM_HD = Camera(1280, 720, 1050.0, 1050.0, 639.5, 359.5)
+
+
+def _attributes(rng: np.random.Generator, n: int):
+    scales = np.exp(rng.normal(-3.0, 0.5, size=(n, 3))).astype(np.float32)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    opac = (1.0 / (1.0 + np.exp(-rng.normal(size=n)))).astype(np.float32)
+    col = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    return scales, q.astype(np.float32), col, opac
+
+
+def cam_box(n: int = 50_000, seed: int = 0) -> Scene:
+    """Means uniform in the camera-frame box [-2,2]x[-1.5,1.5]x[1,5] m."""
+    rng = np.random.default_rng(seed)
+    pos = np.stack(
+        [rng.uniform(-2, 2, n), rng.uniform(-1.5, 1.5, n), rng.uniform(1, 5, n)], axis=1
+    ).astype(np.float32)
+    s, q, c, o = _attributes(rng, n)
+    return Scene(pos, s, q, c, o)
+
+
+def room(n: int = 1_000_000, seed: int = 0) -> Scene:
+    """Means uniform in a 10 x 10 x 4 m room centred on the origin (y is the
+    4 m vertical axis, camera convention y down, z forward)."""
+    rng = np.random.default_rng(seed)
+    pos = np.stack(
+        [rng.uniform(-5, 5, n), rng.uniform(-2, 2, n), rng.uniform(-5, 5, n)], axis=1
+    ).astype(np.float32)
+    s, q, c, o = _attributes(rng, n)
+    return Scene(pos, s, q, c, o)
+
+
+# ----------------------------------------------------------------------------
+# quaternion helpers, (x, y, z, w) layout, float64
+# ----------------------------------------------------------------------------
+def qmul(a, b):
+    ax, ay, az, aw = a
+    bx, by, bz, bw = b
+    return np.array(
+        [
+            aw * bx + bw * ax + ay * bz - az * by,
+            aw * by + bw * ay + az * bx - ax * bz,
+            aw * bz + bw * az + ax * by - ay * bx,
+            aw * bw - ax * bx - ay * by - az * bz,
+        ]
+    )
+
+
+def qexp(rotvec):
+    th = float(np.linalg.norm(rotvec))
+    if th < 1e-12:
+        return np.array([0.5 * rotvec[0], 0.5 * rotvec[1], 0.5 * rotvec[2], 1.0])
+    ax = np.asarray(rotvec) / th
+    s = np.sin(0.5 * th)
+    return np.array([ax[0] * s, ax[1] * s, ax[2] * s, np.cos(0.5 * th)])
+
+
+def qrot(q):
+    """Rotation matrix of quaternionToMatrix for q = (x, y, z, w)."""
+    x, y, z, w = q
+    return np.array(
+        [
+            [1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+            [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+            [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)],
+        ]
+    )
+
+
+def pose_error(pa, pb):
+    """(rotation angle rad, translation m) between two poses (t, q)."""
+    ta, qa = pa
+    tb, qb = pb
+    dq = qmul(np.array([-qa[0], -qa[1], -qa[2], qa[3]], dtype=np.float64), np.asarray(qb, np.float64))
+    ang = 2.0 * np.arctan2(np.linalg.norm(dq[:3]), abs(dq[3]))
+    return float(ang), float(np.linalg.norm(np.asarray(ta, np.float64) - np.asarray(tb, np.float64)))
+
+
+def perturb(pose, deg: float, cm: float, rng: np.random.Generator):
+    """Rotate by `deg` degrees about a random axis (right-multiplied, as the
+    pose update PoseLocalParameterization::Plus does) and translate `cm` cm in
+    a random direction."""
+    t, q = pose
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    dq = qexp(ax * np.deg2rad(deg))
+    q2 = qmul(np.asarray(q, np.float64), dq)
+    q2 /= np.linalg.norm(q2)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    t2 = np.asarray(t, np.float64) + d * (cm / 100.0)
+    return t2.astype(np.float32), q2.astype(np.float32)
+
+
+def trajectory(n_poses: int, seed: int = 0, step_cm: float = 1.0, step_deg: float = 0.5):
+    """Random walk from the room centre: each step rotates `step_deg` and
+    translates `step_cm` in random directions."""
+    rng = np.random.default_rng(seed + 7919)
+    pose = (np.zeros(3, np.float32), IDENTITY_Q.copy())
+    out = [pose]
+    for _ in range(n_poses - 1):
+        pose = perturb(pose, step_deg, step_cm, rng)
+        out.append(pose)
+    return out
+
+
+def sobel3(img: np.ndarray):
+    """3x3 Sobel derivatives of an (H, W, C) float image with reflect-101
+    borders, as cv::Sobel(src, dst, CV_32F, 1, 0, 3) / (0, 1, 3) computes them
+    for the reference's gradient pyramid (src/GSSlam.cu:1960-1961)."""
+    p = np.pad(img.astype(np.float32), ((1, 1), (1, 1), (0, 0)), mode="reflect")
+    gx = (
+        (p[:-2, 2:] - p[:-2, :-2])
+        + 2.0 * (p[1:-1, 2:] - p[1:-1, :-2])
+        + (p[2:, 2:] - p[2:, :-2])
+    )
+    gy = (
+        (p[2:, :-2] - p[:-2, :-2])
+        + 2.0 * (p[2:, 1:-1] - p[:-2, 1:-1])
+        + (p[2:, 2:] - p[:-2, 2:])
+    )
+    return gx.astype(np.float32), gy.astype(np.float32)
+
+
+def add_noise(rgb, depth, rng, color_sigma=0.01, depth_sigma=0.005):
+    rgb_n = (rgb + rng.normal(0.0, color_sigma, size=rgb.shape)).astype(np.float32)
+    depth_n = (depth + rng.normal(0.0, depth_sigma, size=depth.shape)).astype(np.float32)
+    return rgb_n, depth_n

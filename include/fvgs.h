@@ -1,0 +1,133 @@
+/*
+ * fvgs.h -- C-ABI of the GB300 (sm_103a) Gaussian-splatting tracking and
+ * mapping library.  Plain pointers and sizes only; every entry point returns
+ * an int status (fvgs_status, 0 = FVGS_OK).
+ *
+ * This boundary replaces the device-side half of the reference's
+ * GSSlam / GSCudaKernels path (jcevasco2003/f_vigs_slam).  Each entry point
+ * names the reference interface it stands in for.  The C++ compatibility
+ * layer (include/f_vigs_slam/*.hpp) keeps the reference's own class
+ * interfaces (GSSlam, RgbdPoseCostFunction) on top of it.
+ *
+ * Memory: the library owns every device buffer of a session; caller arrays
+ * are borrowed for the duration of a call and may be host (pageable or
+ * pinned) or device pointers (CUDA unified addressing decides).
+ * Threading: calls on one session are serialised by the caller; different
+ * sessions are independent and may be driven from different threads.
+ */
+#ifndef FVGS_H
+#define FVGS_H
+
+#include "fvgs_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fvgs_session fvgs_session;
+
+/* Debug outputs (fvgs_session_set_debug). */
+#define FVGS_DEBUG_PROJECTION 0x1u /* keep Sigma2D / inverse / visibility per Gaussian */
+#define FVGS_DEBUG_IMAGES 0x2u     /* tracking kernel writes its forward-blend images */
+
+/* Human-readable name of a status code. */
+const char* fvgs_status_string(int status);
+
+/* Reference defaults of every tunable (see fvgs_params). */
+int fvgs_params_default(fvgs_params* params);
+
+/*
+ * Create a session on CUDA device `device` holding up to `capacity_gaussians`
+ * Gaussians and frames up to max_width x max_height (pyramid level 0).
+ * Stands in for the device state that GSSlam owns
+ * (include/f_vigs_slam/GSSlam.cuh:185-235: gaussians_, positions_2d_, ...,
+ * hashes_, tile_ranges_).
+ */
+int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity_gaussians, int max_width,
+                        int max_height, fvgs_session** out);
+int fvgs_session_destroy(fvgs_session* s);
+/* Run all further work of the session on this cudaStream_t (NULL = the
+ * session's own stream). */
+int fvgs_session_set_stream(fvgs_session* s, void* cuda_stream);
+int fvgs_session_sync(fvgs_session* s);
+int fvgs_session_set_debug(fvgs_session* s, uint32_t flags);
+/* Bytes of device memory the session holds (admission accounting). */
+int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes);
+
+/*
+ * Gaussians in the reference's SoA layout (Gaussians,
+ * include/f_vigs_slam/RepresentationClasses.hpp:53-99): positions[3n],
+ * scales[3n], orientations[4n] as (x,y,z,w), colors[3n], opacities[n].
+ */
+int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* scales,
+                          const float* orientations, const float* colors, const float* opacities, uint32_t n);
+int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, float* orientations,
+                            float* colors, float* opacities, uint32_t n);
+
+/*
+ * Observed frame of pyramid level `level` (0..2): rgb[3P], depth[P],
+ * grad_x[3P], grad_y[3P], dense row-major (the pyr_color_ / pyr_depth_ /
+ * pyr_dx_ / pyr_dy_ images of GSSlam::initAndCopyImgs, src/GSSlam.cu:1913-1969).
+ */
+int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* depth, const float* grad_x,
+                   const float* grad_y, int width, int height);
+
+/*
+ * Projection, tile binning, stable depth-key sort and per-tile ranges for
+ * `pose` (GSSlam::prepareRasterization, src/GSSlam.cu:408-646).  If
+ * n_instances is non-null the call waits for the device and returns the
+ * instance count.
+ */
+int fvgs_project_bin(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                     uint32_t* n_instances);
+/* Results of the last fvgs_project_bin in the reference's buffer layout
+ * (positions_2d_, covariances_2d_, inv_covariances_2d_, depths_, p_hats_,
+ * tile_counts_); cov2d / inv2d / visible need FVGS_DEBUG_PROJECTION.  Any
+ * pointer may be null. */
+int fvgs_download_projection(fvgs_session* s, float* uv, float* cov2d, float* inv2d, float* depth, float* phat,
+                             uint8_t* visible, uint32_t* tile_counts);
+/* Sorted keys (hashes_), values (gaussian_indices_) and ranges[2T]
+ * (tile_ranges_) of the last binning.  Any pointer may be null. */
+int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uint32_t* ranges,
+                          uint64_t max_instances, uint32_t* n_instances);
+
+/*
+ * One RGB-D pose Jacobian evaluation at `pose` against the frame of `level`:
+ * binning + fused tracking kernel + frame reduction.  Outputs the 6x6 JtJ
+ * (row-major, symmetric) and Jtr[6] exactly as GSSlam::computeRgbdPoseJacobians
+ * forms them before its IMU-extrinsic transform (src/GSSlam.cu:2103-2226):
+ * camera frame, Jtr negated.  Replaces that function's device part and the
+ * kernel getRgbdPoseJacobians (src/GSCudaKernels.cu:922-1392).
+ */
+int fvgs_track_jacobian(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level,
+                        double* JtJ, double* Jtr);
+/* Per-tile camera-frame partial sums of the last tracking evaluation:
+ * tiles[27T] = Jtr[6] then JtJ upper triangle [21] (PoseOptimizationRgbdData). */
+int fvgs_download_tile_partials(fvgs_session* s, float* tiles, int num_tiles);
+/* Forward-blend images of the last tracking evaluation (FVGS_DEBUG_IMAGES). */
+int fvgs_download_track_images(fvgs_session* s, float* color, float* depth, float* final_T, uint32_t* n_contrib);
+
+/*
+ * A whole tracking frame on the device: `iterations` Gauss-Newton steps, each
+ * = binning + Jacobian + eigen-regularised pseudo-factor step + pose update
+ * (the Ceres loop of GSSlam::optimizeWithCeres over RgbdPoseCostFunction with
+ * PoseLocalParameterization, src/GSSlam.cu:2246-2297, as plain Gauss-Newton
+ * with identity IMU-camera extrinsics).  pose is read and overwritten.
+ * last_step[6] (nullable) receives the final update.
+ */
+int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                     double* last_step);
+
+/*
+ * Forward blend with the tracking kernel's semantics for every pixel of a
+ * width x height view (observed depth treated as valid everywhere): colour
+ * incl. background, median depth, final transmittance, contributor count.
+ * Outputs may be host or device pointers; any may be null.
+ */
+int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                float* rgb, float* depth, float* final_T, uint32_t* n_contrib);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVGS_H */

@@ -1,0 +1,338 @@
+"""ctypes wrapper of the CPU restatement (oracle/fvgs_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the library.  Builds
+oracle/_build/liboracle.so on first use if it is missing.
+
+Parity unpinned by reference outputs (the reference has no tests or fixtures
+and cannot be built here); pinned by hand-derived known-answer tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "fvgs_oracle.cpp")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with -ffp-contract=off (bit-exact FP32 keys) and OpenMP."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [
+        "g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+        "-fPIC", "-shared", "-o", tmp, SRC,
+    ]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class Pose(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("orientation", C.c_float * 4)]
+
+
+class Intr(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("radius_sigma", C.c_float),
+        ("bg", C.c_float * 3), ("alpha_thresh", C.c_float), ("color_thresh", C.c_float),
+        ("depth_thresh", C.c_float), ("w_depth", C.c_float), ("w_dist", C.c_float),
+        ("lambda_iso", C.c_float), ("adam_beta1", C.c_float), ("adam_beta2", C.c_float),
+        ("adam_eps", C.c_float), ("quirks", C.c_uint32), ("eig_eps", C.c_double),
+    ]
+
+
+Q_CULLED_SLOTS = 0x1
+Q_RANGE_LAUNCH = 0x2
+Q_INVSIGMA_SWAP = 0x4
+Q_MAP_CAP256 = 0x8
+QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
+
+
+def default_params(quirks: int = QUIRKS_DEFAULT, tile=(16, 16)) -> Params:
+    p = Params()
+    p.tile_w, p.tile_h = tile
+    p.radius_sigma = 3.0
+    p.bg[:] = [0.0, 0.0, 0.0]
+    p.alpha_thresh, p.color_thresh, p.depth_thresh = 0.2, 0.1, 0.2
+    p.w_depth, p.w_dist, p.lambda_iso = 1.0, 0.1, 0.01
+    p.adam_beta1, p.adam_beta2, p.adam_eps = 0.9, 0.999, 1e-8
+    p.quirks = quirks
+    p.eig_eps = 1e-4
+    return p
+
+
+def make_pose(pose) -> Pose:
+    t, q = pose
+    p = Pose()
+    p.position[:] = [float(v) for v in np.asarray(t, np.float32)]
+    p.orientation[:] = [float(v) for v in np.asarray(q, np.float32)]
+    return p
+
+
+def make_intr(K) -> Intr:
+    i = Intr()
+    i.fx, i.fy, i.cx, i.cy = [float(np.float32(v)) for v in K]
+    return i
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.oracle_emit_keys.restype = C.c_int64
+        _lib.oracle_buckets.restype = C.c_int64
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Projection:
+    def __init__(self, uv, cov2d, inv2d, depth, phat, visible):
+        self.uv, self.cov2d, self.inv2d = uv, cov2d, inv2d
+        self.depth, self.phat, self.visible = depth, phat, visible
+
+
+def project(scene, pose, K, W, H) -> Projection:
+    n = scene.n
+    uv = np.zeros((n, 2), np.float32)
+    cov = np.zeros((n, 3), np.float32)
+    inv = np.zeros((n, 3), np.float32)
+    dep = np.zeros(n, np.float32)
+    ph = np.zeros((n, 2), np.float32)
+    vis = np.zeros(n, np.uint8)
+    pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
+    lib().oracle_project(
+        _p(pos), _p(scl), _p(rot), C.c_int(n), C.byref(make_pose(pose)), C.byref(make_intr(K)),
+        C.c_int(W), C.c_int(H), _p(uv), _p(cov), _p(inv), _p(dep), _p(ph), _p(vis),
+    )
+    return Projection(uv, cov, inv, dep, ph, vis)
+
+
+def count(proj: Projection, W, H, params: Params):
+    n = proj.uv.shape[0]
+    cnt = np.zeros(n, np.uint32)
+    rect = np.zeros((n, 4), np.int32)
+    lib().oracle_count(
+        _p(proj.uv), _p(proj.cov2d), _p(proj.visible), C.c_int(n), C.c_int(W), C.c_int(H),
+        C.c_int(params.tile_w), C.c_int(params.tile_h), C.c_float(params.radius_sigma),
+        C.c_uint32(params.quirks), _p(cnt), _p(rect),
+    )
+    return cnt, rect
+
+
+def emit_keys(proj: Projection, cnt, rect, W, params: Params):
+    n = proj.uv.shape[0]
+    total = int(cnt.astype(np.int64).sum())
+    keys = np.zeros(max(total, 1), np.uint64)
+    vals = np.zeros(max(total, 1), np.uint32)
+    got = lib().oracle_emit_keys(
+        _p(proj.uv), _p(proj.depth), _p(proj.phat), _p(cnt), _p(rect), C.c_int(n), C.c_int(W),
+        C.c_int(params.tile_w), C.c_int(params.tile_h), C.c_int64(total), _p(keys), _p(vals),
+    )
+    assert got == total
+    return keys[:total].copy(), vals[:total].copy()
+
+
+def num_tiles(W, H, params: Params):
+    return ((W + params.tile_w - 1) // params.tile_w) * ((H + params.tile_h - 1) // params.tile_h)
+
+
+def sort_ranges(keys, vals, W, H, params: Params):
+    keys = keys.copy()
+    vals = vals.copy()
+    T = num_tiles(W, H, params)
+    ranges = np.zeros((T, 2), np.uint32)
+    lib().oracle_sort_ranges(
+        _p(keys), _p(vals), C.c_int64(keys.shape[0]), C.c_int(T), C.c_uint32(params.quirks), _p(ranges)
+    )
+    return keys, vals, ranges
+
+
+def make_records(proj: Projection, scene, params: Params):
+    n = proj.uv.shape[0]
+    rec = np.zeros((n, 12), np.float32)
+    lib().oracle_make_records(
+        _p(proj.uv), _p(proj.inv2d), _p(proj.depth), _p(proj.phat), _p(_f32(scene.colors)),
+        _p(_f32(scene.opacities)), C.c_int(n), C.c_uint32(params.quirks), _p(rec),
+    )
+    return rec
+
+
+class Binning:
+    """Everything prepareRasterization produces (src/GSSlam.cu:408-646)."""
+
+    def __init__(self, proj, cnt, rect, keys_gen, vals_gen, keys, vals, ranges, rec):
+        self.proj, self.cnt, self.rect = proj, cnt, rect
+        self.keys_gen, self.vals_gen = keys_gen, vals_gen
+        self.keys, self.vals, self.ranges, self.rec = keys, vals, ranges, rec
+
+
+def prepare(scene, pose, K, W, H, params: Params) -> Binning:
+    proj = project(scene, pose, K, W, H)
+    cnt, rect = count(proj, W, H, params)
+    kg, vg = emit_keys(proj, cnt, rect, W, params)
+    ks, vs, ranges = sort_ranges(kg, vg, W, H, params)
+    rec = make_records(proj, scene, params)
+    return Binning(proj, cnt, rect, kg, vg, ks, vs, ranges, rec)
+
+
+class TrackResult:
+    def __init__(self, JtJ, Jtr, tiles, color, depth, final_T, n_contrib):
+        self.JtJ, self.Jtr, self.tiles = JtJ, Jtr, tiles
+        self.color, self.depth, self.final_T, self.n_contrib = color, depth, final_T, n_contrib
+
+
+def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True) -> TrackResult:
+    """frame = (rgb (H,W,3), depth (H,W), gx (H,W,3), gy (H,W,3)) float32."""
+    rgb, depth, gx, gy = [_f32(a) for a in frame]
+    T = num_tiles(W, H, params)
+    tiles = np.zeros((T, 27), np.float64)
+    JtJ = np.zeros((6, 6), np.float64)
+    Jtr = np.zeros(6, np.float64)
+    if images:
+        col = np.zeros((H, W, 3), np.float64)
+        dep = np.zeros((H, W), np.float64)
+        fT = np.zeros((H, W), np.float64)
+        nc = np.zeros((H, W), np.uint32)
+        ptrs = (_p(col), _p(dep), _p(fT), _p(nc))
+    else:
+        col = dep = fT = nc = None
+        ptrs = (None, None, None, None)
+    lib().oracle_track(
+        _p(b.rec), _p(b.ranges), _p(b.vals), _p(rgb), _p(depth), _p(gx), _p(gy),
+        C.byref(make_pose(pose)), C.byref(make_intr(K)), C.byref(params), C.c_int(W), C.c_int(H),
+        _p(tiles), _p(JtJ), _p(Jtr), *ptrs,
+    )
+    return TrackResult(JtJ, Jtr, tiles, col, dep, fT, nc)
+
+
+def render(b: Binning, pose, K, W, H, params: Params):
+    """Forward blend of the tracking kernel for every pixel (observed depth
+    treated as valid everywhere): colour (H,W,3), depth, final T, n_contrib."""
+    ones = np.ones((H, W), np.float32)
+    z3 = np.zeros((H, W, 3), np.float32)
+    r = track(b, (z3, ones, z3, z3), pose, K, W, H, params, images=True)
+    return r.color, r.depth, r.final_T, r.n_contrib
+
+
+class MapResult:
+    pass
+
+
+def map_step(scene, b: Binning, frame_rgb, frame_depth, pose, K, W, H, params: Params, eta: float,
+             adam_state=None):
+    """One optimizeGaussiansKeyframe step (src/GSSlam.cu:1083-1320) in FP64.
+    Returns a MapResult with forward images, delta2d (N,13), delta3d (N,14)
+    and the updated parameters / Adam state (float64)."""
+    L = lib()
+    n = scene.n
+    T = num_tiles(W, H, params)
+    BS = params.tile_w * params.tile_h
+    bucket_incl = np.zeros(T, np.uint32)
+    nb = int(L.oracle_buckets(_p(b.ranges), C.c_int(T), _p(bucket_incl)))
+    P = W * H
+    r = MapResult()
+    r.final_T = np.zeros(P, np.float64)
+    r.n_contrib = np.zeros(P, np.uint32)
+    r.max_contrib = np.zeros(T, np.uint32)
+    r.color = np.zeros((P, 3), np.float64)
+    r.depth = np.zeros(P, np.float64)
+    r.color_err = np.zeros((P, 3), np.float64)
+    r.depth_obs = np.zeros(P, np.float64)
+    r.sampled_T = np.zeros(max(nb, 1) * BS, np.float64)
+    r.sampled_ar = np.zeros((max(nb, 1) * BS, 3), np.float64)
+    rgb, dep = _f32(frame_rgb), _f32(frame_depth)
+    L.oracle_map_forward(
+        _p(b.rec), _p(b.ranges), _p(b.vals), _p(bucket_incl), _p(rgb), _p(dep), C.byref(params),
+        C.c_int(W), C.c_int(H), _p(r.final_T), _p(r.n_contrib), _p(r.max_contrib), _p(r.color),
+        _p(r.depth), _p(r.color_err), _p(r.depth_obs), _p(r.sampled_T), _p(r.sampled_ar),
+    )
+    r.delta2d = np.zeros((n, 13), np.float64)
+    L.oracle_map_backward(
+        _p(b.rec), _p(b.ranges), _p(b.vals), _p(bucket_incl), _p(r.sampled_T), _p(r.sampled_ar),
+        _p(r.n_contrib), _p(r.max_contrib), _p(r.color), _p(r.depth), _p(r.color_err),
+        _p(r.depth_obs), C.byref(params), C.c_int(W), C.c_int(H), _p(r.delta2d),
+    )
+    r.delta3d = np.zeros((n, 14), np.float64)
+    pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
+    L.oracle_delta3d(
+        _p(pos), _p(scl), _p(rot), _p(r.delta2d), C.c_int(n), C.byref(make_pose(pose)),
+        C.byref(make_intr(K)), C.c_float(params.lambda_iso), _p(r.delta3d),
+    )
+    r.pos = scene.positions.astype(np.float64).copy()
+    r.scl = scene.scales.astype(np.float64).copy()
+    r.rot = scene.orientations.astype(np.float64).copy()
+    r.col = scene.colors.astype(np.float64).copy()
+    r.opa = scene.opacities.astype(np.float64).copy()
+    r.adam = np.zeros((n, 27), np.float64) if adam_state is None else adam_state.astype(np.float64).copy()
+    L.oracle_adam(
+        _p(r.pos), _p(r.scl), _p(r.rot), _p(r.col), _p(r.opa), _p(r.adam), _p(r.delta3d), C.c_int(n),
+        C.c_float(eta), C.byref(params),
+    )
+    r.bucket_incl = bucket_incl
+    r.num_buckets = nb
+    return r
+
+
+# ----------------------------------------------------------------------------
+# Host FP64 post-processing (src/GSSlam.cu:2233-2243, src/RgbdPoseCost.cu:57-106,
+# src/PoseLocalParameterization.cpp:22-44)
+# ----------------------------------------------------------------------------
+def pseudo_factor(JtJ, Jtr, eps=1e-4):
+    """Eigen-regularised pseudo residual r* = S^-1/2 U^T Jtr and Jacobian
+    J* = S^1/2 U^T (eigenvalues <= eps dropped)."""
+    w, U = np.linalg.eigh(JtJ)
+    keep = w > eps
+    S = np.where(keep, w, 0.0)
+    Sinv = np.where(keep, 1.0 / np.where(keep, w, 1.0), 0.0)
+    Jstar = np.sqrt(S)[:, None] * U.T
+    rstar = np.sqrt(Sinv) * (U.T @ Jtr)
+    return rstar, Jstar
+
+
+def gn_delta(JtJ, Jtr, eps=1e-4):
+    """Gauss-Newton step of the pseudo factor: solve J*^T J* d = -J*^T r*."""
+    rstar, Jstar = pseudo_factor(JtJ, Jtr, eps)
+    return -np.linalg.lstsq(Jstar, rstar, rcond=None)[0]
+
+
+def pose_plus(pose, delta):
+    """PoseLocalParameterization::Plus: p += dp, q = normalise(q (x) [1, dth/2])."""
+    t, q = pose
+    t2 = np.asarray(t, np.float64) + delta[:3]
+    dq = np.array([0.5 * delta[3], 0.5 * delta[4], 0.5 * delta[5], 1.0])
+    x = np.asarray(q, np.float64)
+    ax, ay, az, aw = x
+    bx, by, bz, bw = dq
+    q2 = np.array(
+        [
+            aw * bx + bw * ax + ay * bz - az * by,
+            aw * by + bw * ay + az * bx - ax * bz,
+            aw * bz + bw * az + ax * by - ay * bx,
+            aw * bw - ax * bx - ay * by - az * bz,
+        ]
+    )
+    q2 /= np.linalg.norm(q2)
+    return t2, q2
