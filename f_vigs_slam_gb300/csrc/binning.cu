@@ -335,7 +335,10 @@ __global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const
         limit = min(limit, launched);
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < limit; i += gridDim.x * blockDim.x) {
+        // Tile ids are range-checked: after an instance overflow (the call is
+        // then repeated with larger buffers) unwritten slots hold stale keys.
         const uint32_t t = (uint32_t)(keys[i] >> 32);
+        if (t >= (uint32_t)num_tiles) continue;
         if (quirks & FVGS_Q_RANGE_LAUNCH) {
             if (i == 0) {
                 ranges[t].x = 0;
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const
             }
             const uint32_t pt = (uint32_t)(keys[i - 1] >> 32);
             if (pt != t) {
-                ranges[pt].y = i;
+                if (pt < (uint32_t)num_tiles) ranges[pt].y = i;
                 ranges[t].x = i;
             }
             if (i == n - 1) ranges[t].y = n;

@@ -121,8 +121,36 @@ struct fvgs_session {
     uint32_t* img_nc = nullptr;
     size_t img_cap = 0;
 
+    // mapping state and scratch
+    float4* adam = nullptr;  // 9 planes x cap_g
+    float* delta2d = nullptr;  // [cap_g][16]
+    float* dbg_delta3d = nullptr;
+    size_t map_px = 0;
+    float *m_final_T = nullptr, *m_color = nullptr, *m_depth = nullptr, *m_color_err = nullptr;
+    uint32_t* m_n_contrib = nullptr;
+    uint32_t* m_max_contrib = nullptr;
+    uint32_t* m_bucket_base = nullptr;
+    uint32_t* m_bucket_total = nullptr;
+    float4* m_sampled = nullptr;
+    size_t m_sampled_slots = 0;
+    int m_W = 0, m_H = 0;
+
+    // kernel accounting: launches per class (always), event timing (opt-in)
+    uint32_t timing_mask = 0;
+    uint64_t launches[FVGS_K_COUNT] = {};
+    double kernel_ms[FVGS_K_COUNT] = {};
+    uint64_t timed_launches[FVGS_K_COUNT] = {};
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    struct Pending {
+        int cls;
+        size_t a, b;
+        uint32_t kernels;
+    };
+    std::vector<Pending> pending;
+
     int last_W = 0, last_H = 0, last_T = 0;
-    bool has_binning = false, has_track = false, dbg_proj_valid = false;
+    bool has_binning = false, has_track = false, dbg_proj_valid = false, has_map = false;
 };
 
 namespace {
@@ -215,6 +243,58 @@ int check_view(fvgs_session* s, int W, int H) {
     return FVGS_OK;
 }
 
+cudaEvent_t next_event(fvgs_session* s) {
+    if (s->ev_used == s->ev_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        s->ev_pool.push_back(e);
+    }
+    return s->ev_pool[s->ev_used++];
+}
+
+// Wraps the launches of one kernel class: counts kernels and, when the class
+// is selected for timing, brackets them with CUDA events on the stream.
+struct KScope {
+    fvgs_session* s;
+    int cls;
+    uint32_t kernels;
+    size_t a = (size_t)-1;
+    KScope(fvgs_session* s_, int cls_, uint32_t kernels_) : s(s_), cls(cls_), kernels(kernels_) {
+        s->launches[cls] += kernels;
+        if (s->timing_mask & (1u << cls)) {
+            cudaEvent_t e = next_event(s);
+            if (e) {
+                a = s->ev_used - 1;
+                cudaEventRecord(e, s->stream);
+            }
+        }
+    }
+    ~KScope() {
+        if (a != (size_t)-1) {
+            cudaEvent_t e = next_event(s);
+            if (e) {
+                cudaEventRecord(e, s->stream);
+                s->pending.push_back({cls, a, s->ev_used - 1, kernels});
+            }
+        }
+    }
+};
+
+// Called after the stream has been synchronised.
+void collect_timing(fvgs_session* s) {
+    for (const auto& p : s->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->ev_pool[p.a], s->ev_pool[p.b]) == cudaSuccess) {
+            s->kernel_ms[p.cls] += ms;
+            s->timed_launches[p.cls] += 1;  // one timed call = one event pair
+        } else {
+            cudaGetLastError();
+        }
+    }
+    s->pending.clear();
+    s->ev_used = 0;
+}
+
 // Enqueue binning for the pose already in s->pose.
 int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     const fvgs_params& P = s->params;
@@ -248,8 +328,15 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         pa.dbg_inv = s->dbg_inv;
         pa.dbg_vis = s->dbg_vis;
     }
-    FV_CK(launch_project_count(pa, s->stream));
-    FV_CK(launch_scan(s->counts, (int)s->n_g, s->partials, s->offsets, s->st, (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu), s->stream));
+    {
+        KScope k(s, FVGS_K_PROJECT, 1);
+        FV_CK(launch_project_count(pa, s->stream));
+    }
+    {
+        KScope k(s, FVGS_K_SCAN, 2);
+        FV_CK(launch_scan(s->counts, (int)s->n_g, s->partials, s->offsets, s->st,
+                          (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu), s->stream));
+    }
     EmitArgs ea{};
     ea.bin0 = s->bin0;
     ea.bin1 = s->bin1;
@@ -261,10 +348,19 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     ea.capacity = s->cap_inst;
     ea.keys = s->keys;
     ea.vals = s->vals;
-    FV_CK(launch_emit_keys(ea, s->stream));
+    {
+        KScope k(s, FVGS_K_EMIT, 1);
+        FV_CK(launch_emit_keys(ea, s->stream));
+    }
     const int key_bits = 32 + std::max(1, bits_for(T));
-    FV_CK(launch_radix_sort(s->keys, s->vals, s->st, key_bits, &s->sort, &s->st->flags, s->stream));
-    FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+    {
+        KScope k(s, FVGS_K_SORT, 1 + (uint32_t)sort_num_passes(key_bits));
+        FV_CK(launch_radix_sort(s->keys, s->vals, s->st, key_bits, &s->sort, &s->st->flags, s->stream));
+    }
+    {
+        KScope k(s, FVGS_K_RANGES, 1);
+        FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+    }
     s->last_W = W;
     s->last_H = H;
     s->last_T = T;
@@ -306,6 +402,7 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
         ta.img_nc = s->img_nc;
     }
     ta.render_only = render_only ? 1 : 0;
+    KScope k(s, render_only ? FVGS_K_RENDER : FVGS_K_TRACK, 1);
     FV_CK(launch_track(ta, s->stream));
     return FVGS_OK;
 }
@@ -337,6 +434,101 @@ int check_status(fvgs_session* s, int* retry) {
 }
 
 bool valid_pose(const fvgs_pose* p) { return p != nullptr; }
+
+int ensure_map_buffers(fvgs_session* s, size_t px, bool cap) {
+    if (px > s->map_px) {
+        dev_free(s, s->m_final_T, s->map_px);
+        dev_free(s, s->m_n_contrib, s->map_px);
+        dev_free(s, s->m_color, 3 * s->map_px);
+        dev_free(s, s->m_depth, s->map_px);
+        dev_free(s, s->m_color_err, 3 * s->map_px);
+        FV_TRY(dev_alloc(s, &s->m_final_T, px));
+        FV_TRY(dev_alloc(s, &s->m_n_contrib, px));
+        FV_TRY(dev_alloc(s, &s->m_color, 3 * px));
+        FV_TRY(dev_alloc(s, &s->m_depth, px));
+        FV_TRY(dev_alloc(s, &s->m_color_err, 3 * px));
+        s->map_px = px;
+    }
+    // checkpoint slots: 8 per tile with MAP_CAP256, else one per 32 instances
+    // of every tile (bounded by capacity/32 + tiles)
+    const size_t slots = cap ? (size_t)s->cap_tiles * map_cap_buckets()
+                             : (size_t)(s->cap_inst / 32 + 1) + (size_t)s->cap_tiles;
+    if (slots > s->m_sampled_slots) {
+        dev_free(s, s->m_sampled, s->m_sampled_slots * 256);
+        FV_TRY(dev_alloc(s, &s->m_sampled, slots * 256));
+        s->m_sampled_slots = slots;
+    }
+    return FVGS_OK;
+}
+
+int enqueue_map(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, float eta) {
+    const fvgs_params& P = s->params;
+    const bool cap = (P.quirks & FVGS_Q_MAP_CAP256) != 0;
+    const int ntx = (f.W + P.tile_w - 1) / P.tile_w, nty = (f.H + P.tile_h - 1) / P.tile_h;
+    MapArgs ma{};
+    ma.rec0 = s->rec0;
+    ma.rec1 = s->rec1;
+    ma.rec2 = s->rec2;
+    ma.ranges = s->ranges;
+    ma.indices = s->vals;
+    ma.obs_rgb = f.rgb;
+    ma.obs_depth = f.depth;
+    ma.W = f.W;
+    ma.H = f.H;
+    ma.ntx = ntx;
+    ma.nty = nty;
+    ma.bg[0] = P.bg[0];
+    ma.bg[1] = P.bg[1];
+    ma.bg[2] = P.bg[2];
+    ma.bucket_base = cap ? nullptr : s->m_bucket_base;
+    ma.sampled = s->m_sampled;
+    ma.final_T = s->m_final_T;
+    ma.n_contrib = s->m_n_contrib;
+    ma.color = s->m_color;
+    ma.depth = s->m_depth;
+    ma.color_err = s->m_color_err;
+    ma.max_contrib = s->m_max_contrib;
+    ma.delta2d = s->delta2d;
+    ma.w_depth = P.w_depth;
+    ma.w_dist = P.w_dist;
+    if (!cap) {
+        KScope k(s, FVGS_K_SCAN, 1);
+        FV_CK(launch_bucket_scan(s->ranges, ntx * nty, s->m_bucket_base, s->m_bucket_total, s->stream));
+    }
+    FV_CK(cudaMemsetAsync(s->delta2d, 0, sizeof(float) * 16 * (size_t)s->n_g, s->stream));
+    {
+        KScope k(s, FVGS_K_MAP_FWD, 1);
+        FV_CK(launch_map_forward(ma, cap, s->stream));
+    }
+    {
+        KScope k(s, FVGS_K_MAP_BWD, 1);
+        FV_CK(launch_map_backward(ma, cap, s->stream));
+    }
+    MapUpdateArgs ua{};
+    ua.pos = s->pos;
+    ua.scale = s->scale;
+    ua.rot = s->rot;
+    ua.col = s->col;
+    ua.adam = s->adam;
+    ua.cap = s->cap_g;
+    ua.n = (int)s->n_g;
+    ua.delta2d = s->delta2d;
+    ua.pose = s->pose;
+    ua.K = *K;
+    ua.lambda_iso = P.lambda_iso;
+    ua.eta = eta;
+    ua.beta1 = P.adam_beta1;
+    ua.beta2 = P.adam_beta2;
+    ua.eps = P.adam_eps;
+    ua.dbg_delta3d = (s->debug & FVGS_DEBUG_MAPPING) ? s->dbg_delta3d : nullptr;
+    {
+        KScope k(s, FVGS_K_MAP_UPDATE, 1);
+        FV_CK(launch_map_update(ua, s->st, s->stream));
+    }
+    s->m_W = f.W;
+    s->m_H = f.H;
+    return FVGS_OK;
+}
 
 }  // namespace
 
@@ -382,6 +574,7 @@ int fvgs_session_destroy(fvgs_session* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (void* p : s->allocations) cudaFree(p);
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     if (s->h_jj) cudaFreeHost(s->h_jj);
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_pose) cudaFreeHost(s->h_pose);
@@ -447,6 +640,11 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->step, 8);
     FV_A(s->st, 1);
     FV_A(s->sort.ctrl, sort_ctrl_words());
+    FV_A(s->adam, 9 * N);
+    FV_A(s->delta2d, 16 * N);
+    FV_A(s->m_max_contrib, (size_t)s->cap_tiles);
+    FV_A(s->m_bucket_base, (size_t)s->cap_tiles);
+    FV_A(s->m_bucket_total, 1);
 #undef FV_A
     if (cudaMallocHost(&s->h_jj, sizeof(double) * 48) != cudaSuccess ||
         cudaMallocHost(&s->h_st, sizeof(DevStatus)) != cudaSuccess ||
@@ -486,6 +684,7 @@ int fvgs_session_set_debug(fvgs_session* s, uint32_t flags) {
         FV_TRY(dev_alloc(s, &s->dbg_vis, (size_t)s->cap_g));
     }
     if (flags & FVGS_DEBUG_IMAGES) FV_TRY(ensure_images(s, (size_t)s->max_w * s->max_h));
+    if ((flags & FVGS_DEBUG_MAPPING) && !s->dbg_delta3d) FV_TRY(dev_alloc(s, &s->dbg_delta3d, 16 * (size_t)s->cap_g));
     s->debug = flags;
     return FVGS_OK;
 }
@@ -519,6 +718,8 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     upload_pack_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(tmp, tmp2, tmp3, tmp4, tmp5, n, s->pos, s->scale,
                                                                s->rot, s->col);
     FV_CK(cudaGetLastError());
+    // fresh map: Adam moments and step counters start at zero
+    FV_CK(cudaMemsetAsync(s->adam, 0, sizeof(float4) * 9 * (size_t)s->cap_g, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
     return FVGS_OK;
 }
@@ -585,6 +786,7 @@ int fvgs_project_bin(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsi
         FV_TRY(enqueue_bin(s, K, width, height));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
         int retry = 0;
         FV_TRY(check_status(s, &retry));
         if (retry) continue;
@@ -654,10 +856,14 @@ int fvgs_track_jacobian(fvgs_session* s, const fvgs_pose* pose, const fvgs_intri
         FV_TRY(set_pose(s, pose));
         FV_TRY(enqueue_bin(s, K, f.W, f.H));
         FV_TRY(enqueue_track(s, K, f, false, images));
-        FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+        {
+            KScope k(s, FVGS_K_REDUCE, 1);
+            FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+        }
         FV_CK(cudaMemcpyAsync(s->h_jj, s->jj, sizeof(double) * 42, cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
         int retry = 0;
         FV_TRY(check_status(s, &retry));
         if (retry) continue;
@@ -705,13 +911,20 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
         for (int it = 0; it < iterations; ++it) {
             FV_TRY(enqueue_bin(s, K, f.W, f.H));
             FV_TRY(enqueue_track(s, K, f, false, false));
-            FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
-            FV_CK(launch_gn_update(s->jj, s->params.eig_eps, s->pose, s->step, s->stream));
+            {
+                KScope k(s, FVGS_K_REDUCE, 1);
+                FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+            }
+            {
+                KScope k(s, FVGS_K_GN, 1);
+                FV_CK(launch_gn_update(s->jj, s->params.eig_eps, s->pose, s->step, s->stream));
+            }
         }
         FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
         int retry = 0;
         FV_TRY(check_status(s, &retry));
         if (retry) continue;
@@ -741,6 +954,7 @@ int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K
         FV_TRY(enqueue_track(s, K, view, true, true));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
         int retry = 0;
         FV_TRY(check_status(s, &retry));
         if (retry) continue;
@@ -752,6 +966,78 @@ int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K
         return FVGS_OK;
     }
     return FVGS_E_CAPACITY;
+}
+
+int fvgs_session_set_timing(fvgs_session* s, uint32_t class_mask) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    s->timing_mask = class_mask;
+    return FVGS_OK;
+}
+
+int fvgs_session_get_timing(fvgs_session* s, double* ms, uint64_t* launches, uint64_t* timed_launches, int reset) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    for (int k = 0; k < FVGS_K_COUNT; ++k) {
+        if (ms) ms[k] = s->kernel_ms[k];
+        if (launches) launches[k] = s->launches[k];
+        if (timed_launches) timed_launches[k] = s->timed_launches[k];
+        if (reset) {
+            s->kernel_ms[k] = 0.0;
+            s->launches[k] = 0;
+            s->timed_launches[k] = 0;
+        }
+    }
+    return FVGS_OK;
+}
+
+int fvgs_map_step(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, float eta) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || !(eta >= 0.f)) return FVGS_E_INVALID;
+    const FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const bool cap = (s->params.quirks & FVGS_Q_MAP_CAP256) != 0;
+    FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, cap));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_map(s, K, f, eta));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) {
+            // the instance buffers grew; checkpoint slots follow capacity
+            FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, cap));
+            continue;
+        }
+        s->has_map = true;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_download_map_state(fvgs_session* s, float* final_T, uint32_t* n_contrib, float* color, float* depth,
+                            float* delta2d, float* delta3d) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->has_map) return FVGS_E_STATE;
+    if (delta3d && !(s->debug & FVGS_DEBUG_MAPPING)) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px = (size_t)s->m_W * s->m_H, n = s->n_g;
+    if (final_T) FV_CK(cudaMemcpyAsync(final_T, s->m_final_T, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    if (n_contrib) FV_CK(cudaMemcpyAsync(n_contrib, s->m_n_contrib, sizeof(uint32_t) * px, cudaMemcpyDefault, s->stream));
+    if (color) FV_CK(cudaMemcpyAsync(color, s->m_color, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    if (depth) FV_CK(cudaMemcpyAsync(depth, s->m_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    if (delta2d) FV_CK(cudaMemcpyAsync(delta2d, s->delta2d, sizeof(float) * 16 * n, cudaMemcpyDefault, s->stream));
+    if (delta3d) FV_CK(cudaMemcpyAsync(delta3d, s->dbg_delta3d, sizeof(float) * 16 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
 }
 
 }  // extern "C"

@@ -108,4 +108,46 @@ cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, const DevP
 cudaError_t launch_gn_update(const double* jtj_jtr, double eig_eps, DevPose* pose, double* step_out,
                              cudaStream_t s);
 
+// ---- mapping (map.cu) ----
+struct MapArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const float4* rec2;
+    const uint2* ranges;
+    const uint32_t* indices;
+    const float* obs_rgb;    // 3P
+    const float* obs_depth;  // P
+    int W, H, ntx, nty;
+    float bg[3];
+    const uint32_t* bucket_base;  // [T] exclusive bucket offsets (null with MAP_CAP256)
+    float4* sampled;              // [buckets][256] (T, accumulated colour)
+    float* final_T;               // P
+    uint32_t* n_contrib;          // P
+    float* color;                 // 3P, incl. background
+    float* depth;                 // P
+    float* color_err;             // 3P
+    uint32_t* max_contrib;        // T
+    float* delta2d;               // [N][16]: DeltaGaussian2D fields, n as u32 at 12
+    float w_depth, w_dist;
+};
+struct MapUpdateArgs {
+    float4* pos;
+    float4* scale;
+    float4* rot;
+    float4* col;
+    float4* adam;  // 9 planes of cap float4
+    uint32_t cap;
+    int n;
+    const float* delta2d;
+    const DevPose* pose;
+    fvgs_intrinsics K;
+    float lambda_iso, eta, beta1, beta2, eps;
+    float* dbg_delta3d;  // optional [N][16]
+};
+cudaError_t launch_map_forward(const MapArgs& a, bool cap, cudaStream_t s);
+cudaError_t launch_map_backward(const MapArgs& a, bool cap, cudaStream_t s);
+cudaError_t launch_bucket_scan(const uint2* ranges, int T, uint32_t* bucket_base, uint32_t* total, cudaStream_t s);
+cudaError_t launch_map_update(const MapUpdateArgs& a, const DevStatus* st, cudaStream_t s);
+int map_cap_buckets();
+
 }  // namespace fvgs

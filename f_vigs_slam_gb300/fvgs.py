@@ -29,6 +29,11 @@ QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
 
 DEBUG_PROJECTION = 0x1
 DEBUG_IMAGES = 0x2
+DEBUG_MAPPING = 0x4
+
+KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
+                  "map_update", "render"]
+K = {name: i for i, name in enumerate(KERNEL_CLASSES)}
 
 
 class FvgsError(RuntimeError):
@@ -151,6 +156,22 @@ class Session:
 
     def sync(self):
         _check(self.lib.fvgs_session_sync(self.h), "fvgs_session_sync")
+
+    def set_timing(self, classes=()):
+        mask = 0
+        for c in classes:
+            mask |= 1 << K[c]
+        _check(self.lib.fvgs_session_set_timing(self.h, C.c_uint32(mask)), "fvgs_session_set_timing")
+
+    def get_timing(self, reset: bool = False):
+        n = len(KERNEL_CLASSES)
+        ms = np.zeros(n, np.float64)
+        launches = np.zeros(n, np.uint64)
+        timed = np.zeros(n, np.uint64)
+        _check(self.lib.fvgs_session_get_timing(self.h, _ptr(ms), _ptr(launches), _ptr(timed), C.c_int(int(reset))),
+               "fvgs_session_get_timing")
+        return {c: dict(ms=float(ms[i]), launches=int(launches[i]), timed=int(timed[i]))
+                for i, c in enumerate(KERNEL_CLASSES)}
 
     def footprint(self) -> int:
         b = C.c_uint64()
@@ -282,3 +303,29 @@ class Session:
             "fvgs_render",
         )
         return col, dep, fT, nc
+
+    # -------------------------------------------------------------- mapping
+    def map_step(self, pose, K, eta: float = 0.002, level: int = 0):
+        _check(
+            self.lib.fvgs_map_step(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
+                                   C.c_float(eta)),
+            "fvgs_map_step",
+        )
+
+    def download_map_state(self, W, H, deltas3d: bool = False):
+        n = self.n
+        fT = np.zeros((H, W), np.float32)
+        nc = np.zeros((H, W), np.uint32)
+        col = np.zeros((H, W, 3), np.float32)
+        dep = np.zeros((H, W), np.float32)
+        d2 = np.zeros((n, 16), np.float32)
+        d3 = np.zeros((n, 16), np.float32) if deltas3d else None
+        _check(
+            self.lib.fvgs_download_map_state(self.h, _ptr(fT), _ptr(nc), _ptr(col), _ptr(dep), _ptr(d2), _ptr(d3)),
+            "fvgs_download_map_state",
+        )
+        n2 = d2[:, 12].copy().view(np.uint32).astype(np.float64)
+        d2f = d2[:, :13].astype(np.float64)
+        d2f[:, 12] = n2
+        return dict(final_T=fT, n_contrib=nc, color=col, depth=dep, delta2d=d2f,
+                    delta3d=None if d3 is None else d3[:, :14].astype(np.float64))

@@ -29,6 +29,24 @@ typedef struct fvgs_session fvgs_session;
 /* Debug outputs (fvgs_session_set_debug). */
 #define FVGS_DEBUG_PROJECTION 0x1u /* keep Sigma2D / inverse / visibility per Gaussian */
 #define FVGS_DEBUG_IMAGES 0x2u     /* tracking kernel writes its forward-blend images */
+#define FVGS_DEBUG_MAPPING 0x4u    /* mapping step keeps its 3D deltas */
+
+/* Kernel classes for launch accounting and timing. */
+enum {
+    FVGS_K_PROJECT = 0, /* projection + tile count */
+    FVGS_K_SCAN,        /* instance offsets (and mapping bucket offsets) */
+    FVGS_K_EMIT,        /* tile-key emission */
+    FVGS_K_SORT,        /* radix sort: histogram + digit passes */
+    FVGS_K_RANGES,      /* per-tile ranges */
+    FVGS_K_TRACK,       /* fused tracking blend + Jacobian */
+    FVGS_K_REDUCE,      /* frame reduction of tile partials */
+    FVGS_K_GN,          /* on-device Gauss-Newton pose update */
+    FVGS_K_MAP_FWD,     /* mapping forward with checkpoints */
+    FVGS_K_MAP_BWD,     /* mapping per-Gaussian backward */
+    FVGS_K_MAP_UPDATE,  /* 2D->3D chain rule + Adam */
+    FVGS_K_RENDER,      /* forward-only render */
+    FVGS_K_COUNT
+};
 
 /* Human-readable name of a status code. */
 const char* fvgs_status_string(int status);
@@ -51,6 +69,13 @@ int fvgs_session_destroy(fvgs_session* s);
 int fvgs_session_set_stream(fvgs_session* s, void* cuda_stream);
 int fvgs_session_sync(fvgs_session* s);
 int fvgs_session_set_debug(fvgs_session* s, uint32_t flags);
+/* Time the kernel classes in class_mask (bit k = class k) with CUDA events on
+ * the session's stream; 0 turns timing off.  Launch counts are always kept. */
+int fvgs_session_set_timing(fvgs_session* s, uint32_t class_mask);
+/* Per class: accumulated event time (ms), kernels launched, and timed calls
+ * (one call = the kernels of one class enqueued together, e.g. a whole radix
+ * sort) -- arrays of FVGS_K_COUNT, any may be null; reset != 0 clears them. */
+int fvgs_session_get_timing(fvgs_session* s, double* ms, uint64_t* launches, uint64_t* timed_launches, int reset);
 /* Bytes of device memory the session holds (admission accounting). */
 int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes);
 
@@ -126,6 +151,24 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
  */
 int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
                 float* rgb, float* depth, float* final_T, uint32_t* n_contrib);
+
+/*
+ * One mapping step against the frame of `level` seen from `pose`: binning,
+ * forward blend with checkpoints, per-Gaussian backward to the 2D parameters,
+ * 2D->3D chain rule and an Adam update of every Gaussian parameter
+ * (GSSlam::optimizeGaussiansKeyframe, src/GSSlam.cu:1083-1320, and its
+ * kernels src/GSCudaKernels.cu:2074-2882; eta as eta_gaussian_).  Adam state
+ * lives in the session and starts at zero on upload.
+ */
+int fvgs_map_step(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, float eta);
+/* Results of the last mapping step: forward images (final T, n_contrib,
+ * colour incl. background, median depth) and per-Gaussian deltas with a
+ * 16-float stride -- delta2d = DeltaGaussian2D fields (meanImg.xy,
+ * invSigmaImg.xyz, color.xyz, depth, alpha, pHat.xy, n as uint32), delta3d =
+ * DeltaGaussian3D fields (position, scale, orientation, color, alpha, n as
+ * float; needs FVGS_DEBUG_MAPPING).  Any pointer may be null. */
+int fvgs_download_map_state(fvgs_session* s, float* final_T, uint32_t* n_contrib, float* color, float* depth,
+                            float* delta2d, float* delta3d);
 
 #ifdef __cplusplus
 }
