@@ -912,12 +912,9 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
             FV_TRY(enqueue_bin(s, K, f.W, f.H));
             FV_TRY(enqueue_track(s, K, f, false, false));
             {
-                KScope k(s, FVGS_K_REDUCE, 1);
-                FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
-            }
-            {
                 KScope k(s, FVGS_K_GN, 1);
-                FV_CK(launch_gn_update(s->jj, s->params.eig_eps, s->pose, s->step, s->stream));
+                FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step,
+                                             s->stream));
             }
         }
         FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));

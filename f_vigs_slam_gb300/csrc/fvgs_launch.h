@@ -102,11 +102,12 @@ struct TrackArgs {
 cudaError_t launch_track(const TrackArgs& a, cudaStream_t s);
 // Sum tile partials in FP64, rotate to the world frame, write out[42] =
 // JtJ[36] (symmetric) then Jtr[6] (negated, as the reference host code does).
-cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, const DevPose* pose, double* out,
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                 cudaStream_t s);
-// One eigen-regularised Gauss-Newton update of the device pose from out[42].
-cudaError_t launch_gn_update(const double* jtj_jtr, double eig_eps, DevPose* pose, double* step_out,
-                             cudaStream_t s);
+// The same reduction followed by one eigen-regularised Gauss-Newton update of
+// the device pose (step_out[6] nullable).
+cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
+                                   double eig_eps, double* step_out, cudaStream_t s);
 
 // ---- mapping (map.cu) ----
 struct MapArgs {

@@ -30,6 +30,24 @@ constexpr int kTW = 16, kTH = 16, kPix = kTW * kTH;
 constexpr int kBatch = 256;
 constexpr float kInv255 = 1.0f / 255.0f;
 
+// z + dx*phx + dy*phy with compensated arithmetic (error-free products via
+// FMA, error-free sums via TwoSum): the per-Gaussian depth cancels to values
+// near zero for distant pixels, and its reciprocal enters the Jacobian, so a
+// plain FP32 evaluation would cost several digits there.
+__device__ __forceinline__ float depth_at(float z, float dx, float phx, float dy, float phy) {
+    const float p1 = __fmul_rn(dx, phx);
+    const float e1 = __fmaf_rn(dx, phx, -p1);
+    const float p2 = __fmul_rn(dy, phy);
+    const float e2 = __fmaf_rn(dy, phy, -p2);
+    const float s1 = __fadd_rn(z, p1);
+    const float b1 = __fsub_rn(s1, z);
+    const float r1 = __fadd_rn(__fsub_rn(z, __fsub_rn(s1, b1)), __fsub_rn(p1, b1));
+    const float s2 = __fadd_rn(s1, p2);
+    const float b2 = __fsub_rn(s2, s1);
+    const float r2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(p2, b2));
+    return __fadd_rn(s2, __fadd_rn(__fadd_rn(r1, r2), __fadd_rn(e1, e2)));
+}
+
 __device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
                                              float r0, float r1, float r2) {
     // u = (a, d * (r x a))
@@ -118,8 +136,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
                     cr += r2.y * alpha * T;
                     cg += r2.z * alpha * T;
                     cb += r2.w * alpha * T;
-                    const float d = r0.z + dx * r1.w + dy * r2.x;
-                    if (T > 0.5f && test_T < 0.5f) depth = d;
+                    if (T > 0.5f && test_T < 0.5f) depth = depth_at(r0.z, dx, r1.w, dy, r2.x);
                     T = test_T;
                     last = contributor;
                 }
@@ -237,7 +254,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
                 const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
                 if (alpha < kInv255) continue;
                 const float4 r2 = s2[j];
-                const float d = r0.z + dx * r1.w + dy * r2.x;
+                const float d = depth_at(r0.z, dx, r1.w, dy, r2.x);
                 float da0 = r2.y * prod_alpha, da1 = r2.z * prod_alpha, da2 = r2.w * prod_alpha;
                 acr += alpha * da0;
                 acg += alpha * da1;
@@ -307,132 +324,233 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     }
 }
 
-// FP64 sum over tiles (fixed order), world-frame rotation, symmetric 6x6,
-// Jtr negated.  One CTA of 256 threads.
-__global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles,
-                                                           const DevPose* pose, double* out) {
-    __shared__ double s_part[8][27];
-    __shared__ double s_tot[27];
-    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    // warp w sums tiles w, w+8, ...; lane k < 27 owns value k
-    double acc = 0.0;
-    if (lane < 27)
-        for (int t = w; t < num_tiles; t += 8) acc += (double)tile_out[(size_t)t * 27 + lane];
-    if (lane < 27) s_part[w][lane] = acc;
-    __syncthreads();
-    if (tid < 27) {
-        double s = 0.0;
-        for (int k = 0; k < 8; ++k) s += s_part[k][tid];
-        s_tot[tid] = s;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
-        double R[3][3];
-        R[0][0] = 1.0 - 2.0 * (qy * qy + qz * qz);
-        R[0][1] = 2.0 * (qx * qy - qw * qz);
-        R[0][2] = 2.0 * (qx * qz + qw * qy);
-        R[1][0] = 2.0 * (qx * qy + qw * qz);
-        R[1][1] = 1.0 - 2.0 * (qx * qx + qz * qz);
-        R[1][2] = 2.0 * (qy * qz - qw * qx);
-        R[2][0] = 2.0 * (qx * qz - qw * qy);
-        R[2][1] = 2.0 * (qy * qz + qw * qx);
-        R[2][2] = 1.0 - 2.0 * (qx * qx + qy * qy);
-        double Ac[6][6];
-        int idx = 0;
-        for (int i = 0; i < 6; ++i)
-            for (int j = i; j < 6; ++j) {
-                Ac[i][j] = s_tot[6 + idx];
-                Ac[j][i] = s_tot[6 + idx];
-                ++idx;
-            }
-        double D[6][6];
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) D[i][j] = 0.0;
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) D[i][j] = R[i][j];
-        for (int i = 3; i < 6; ++i) D[i][i] = 1.0;
-        double DA[6][6];
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += D[i][k] * Ac[k][j];
-                DA[i][j] = s;
-            }
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += DA[i][k] * D[j][k];
-                out[i * 6 + j] = s;
-            }
-        for (int i = 0; i < 6; ++i) {
-            double s = 0.0;
-            for (int k = 0; k < 6; ++k) s += D[i][k] * s_tot[k];
-            out[36 + i] = -s;
+// Butterfly reduce-scatter of 32 doubles (lane l ends with value l's sum).
+__device__ __forceinline__ double warp_reduce_scatter32d(double (&v)[32]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < o; ++k) {
+            const double send = upper ? v[k] : v[k + o];
+            const double keep = upper ? v[k + o] : v[k];
+            v[k] = keep + __shfl_xor_sync(kFullMask, send, o);
         }
     }
+    return v[0];
 }
 
-// Cyclic Jacobi eigen-decomposition of a symmetric 6x6 (FP64), the
-// pseudo-factor step delta = -sum_{lambda_i > eps} (u_i . g / lambda_i) u_i,
-// which is the Gauss-Newton step of the residual/Jacobian pair that
-// RgbdPoseCostFunction::Evaluate hands to Ceres, then Plus on the pose.
-__global__ void gn_update_kernel(const double* __restrict__ jj, double eig_eps, DevPose* pose, double* step_out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double A[6][6], V[6][6];
+// Cholesky of a symmetric 6x6 (lower factor in L); false if not positive
+// definite.  Fully unrolled so everything stays in registers.
+__device__ __forceinline__ bool chol6(const double A[6][6], double L[6][6]) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        double s = A[j][j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
+        if (!(s > 0.0)) return false;
+        const double ljj = sqrt(s);
+        L[j][j] = ljj;
+#pragma unroll
+        for (int i = j + 1; i < 6; ++i) {
+            double t = A[i][j];
+#pragma unroll
+            for (int k = 0; k < j; ++k) t -= L[i][k] * L[j][k];
+            L[i][j] = t / ljj;
+        }
+#pragma unroll
+        for (int i = 0; i < j; ++i) L[i][j] = 0.0;
+    }
+    return true;
+}
+
+// delta = -sum_{lambda_i > eps} (u_i . g / lambda_i) u_i for symmetric H:
+// the Gauss-Newton step of the pseudo residual / Jacobian pair that
+// RgbdPoseCostFunction::Evaluate builds from the eigen-decomposition of JtJ
+// (src/RgbdPoseCost.cu:57-78).  When H - eps*I is positive definite every
+// eigenvalue is kept and the step is exactly -H^-1 g (Cholesky); otherwise a
+// cyclic Jacobi eigen-decomposition drops the small eigenvalues.
+__device__ void pseudo_step(const double H[6][6], const double g[6], double eps, double delta[6]) {
+    double L[6][6];
+    double He[6][6];
+#pragma unroll
     for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) He[i][j] = H[i][j] - (i == j ? eps : 0.0);
+    if (chol6(He, L) && chol6(H, L)) {
+        double y[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            double s = g[i];
+#pragma unroll
+            for (int k = 0; k < i; ++k) s -= L[i][k] * y[k];
+            y[i] = s / L[i][i];
+        }
+#pragma unroll
+        for (int i = 5; i >= 0; --i) {
+            double s = y[i];
+#pragma unroll
+            for (int k = i + 1; k < 6; ++k) s -= L[k][i] * delta[k];
+            delta[i] = s / L[i][i];
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) delta[i] = -delta[i];
+        return;
+    }
+    double A[6][6], V[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
         for (int j = 0; j < 6; ++j) {
-            A[i][j] = jj[i * 6 + j];
+            A[i][j] = H[i][j];
             V[i][j] = (i == j) ? 1.0 : 0.0;
         }
     for (int sweep = 0; sweep < 30; ++sweep) {
         double off = 0.0, tot = 0.0;
+#pragma unroll
         for (int i = 0; i < 6; ++i)
+#pragma unroll
             for (int j = 0; j < 6; ++j) {
                 tot += A[i][j] * A[i][j];
                 if (i != j) off += A[i][j] * A[i][j];
             }
         if (off <= 1e-30 * tot) break;
-        for (int pq = 0; pq < 15; ++pq) {
-            int p = 0, q = 0, c = 0;
-            for (int i = 0; i < 6; ++i)
-                for (int j = i + 1; j < 6; ++j) {
-                    if (c == pq) {
-                        p = i;
-                        q = j;
+#pragma unroll
+        for (int p = 0; p < 5; ++p)
+#pragma unroll
+            for (int q = p + 1; q < 6; ++q) {
+                const double apq = A[p][q];
+                if (apq != 0.0) {
+                    const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                    const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                    const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        const double akp = A[k][p], akq = A[k][q];
+                        A[k][p] = cs * akp - sn * akq;
+                        A[k][q] = sn * akp + cs * akq;
                     }
-                    ++c;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        const double apk = A[p][k], aqk = A[q][k];
+                        A[p][k] = cs * apk - sn * aqk;
+                        A[q][k] = sn * apk + cs * aqk;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        const double vkp = V[k][p], vkq = V[k][q];
+                        V[k][p] = cs * vkp - sn * vkq;
+                        V[k][q] = sn * vkp + cs * vkq;
+                    }
                 }
-            const double apq = A[p][q];
-            if (apq == 0.0) continue;
-            const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
-            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-            for (int k = 0; k < 6; ++k) {
-                const double akp = A[k][p], akq = A[k][q];
-                A[k][p] = cs * akp - sn * akq;
-                A[k][q] = sn * akp + cs * akq;
             }
-            for (int k = 0; k < 6; ++k) {
-                const double apk = A[p][k], aqk = A[q][k];
-                A[p][k] = cs * apk - sn * aqk;
-                A[q][k] = sn * apk + cs * aqk;
-            }
-            for (int k = 0; k < 6; ++k) {
-                const double vkp = V[k][p], vkq = V[k][q];
-                V[k][p] = cs * vkp - sn * vkq;
-                V[k][q] = sn * vkp + cs * vkq;
-            }
-        }
     }
-    double delta[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) delta[k] = 0.0;
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
         const double lam = A[i][i];
-        if (!(lam > eig_eps)) continue;
-        double ug = 0.0;
-        for (int k = 0; k < 6; ++k) ug += V[k][i] * jj[36 + k];
-        for (int k = 0; k < 6; ++k) delta[k] -= (ug / lam) * V[k][i];
+        if (lam > eps) {
+            double ug = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ug += V[k][i] * g[k];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) delta[k] -= (ug / lam) * V[k][i];
+        }
     }
+}
+
+// Frame reduction + (optionally) the Gauss-Newton pose update, one CTA:
+// tiles are summed in FP64 in a fixed order (thread t: tiles t, t+256, ...;
+// butterfly across lanes; warps in order), rotated to the world frame by
+// diag(R, I), written as out[42] = JtJ[36] symmetric, Jtr[6] negated
+// (src/GSSlam.cu:2205-2226); then delta = pseudo-factor step and
+// PoseLocalParameterization::Plus on the device pose.
+template <bool DO_GN>
+__global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles,
+                                                           DevPose* pose, double* out, double eig_eps,
+                                                           double* step_out) {
+    __shared__ double s_w[8][32];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    double v[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = 0.0;
+    for (int t = tid; t < num_tiles; t += 256) {
+        const float* row = tile_out + (size_t)t * 27;
+#pragma unroll
+        for (int k = 0; k < 27; ++k) v[k] += (double)row[k];
+    }
+    s_w[w][lane] = warp_reduce_scatter32d(v);
+    __syncthreads();
+    if (tid != 0) return;
+    double tot[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        double s = 0.0;
+#pragma unroll
+        for (int ww = 0; ww < 8; ++ww) s += s_w[ww][k];
+        tot[k] = s;
+    }
+    const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+    double R[3][3];
+    R[0][0] = 1.0 - 2.0 * (qy * qy + qz * qz);
+    R[0][1] = 2.0 * (qx * qy - qw * qz);
+    R[0][2] = 2.0 * (qx * qz + qw * qy);
+    R[1][0] = 2.0 * (qx * qy + qw * qz);
+    R[1][1] = 1.0 - 2.0 * (qx * qx + qz * qz);
+    R[1][2] = 2.0 * (qy * qz - qw * qx);
+    R[2][0] = 2.0 * (qx * qz - qw * qy);
+    R[2][1] = 2.0 * (qy * qz + qw * qx);
+    R[2][2] = 1.0 - 2.0 * (qx * qx + qy * qy);
+    double Ac[6][6];
+    {
+        int idx = 0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = i; j < 6; ++j) {
+                Ac[i][j] = tot[6 + idx];
+                Ac[j][i] = tot[6 + idx];
+                ++idx;
+            }
+    }
+    // H = D Ac D^T, D = diag(R, I); g = -(D b)
+    double H[6][6], g[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            double s = 0.0;
+            if (i < 3 && j < 3) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) s += R[i][a] * Ac[a][b] * R[j][b];
+            } else if (i < 3) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) s += R[i][a] * Ac[a][j];
+            } else if (j < 3) {
+#pragma unroll
+                for (int b = 0; b < 3; ++b) s += Ac[i][b] * R[j][b];
+            } else {
+                s = Ac[i][j];
+            }
+            H[i][j] = s;
+        }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] = -(R[i][0] * tot[0] + R[i][1] * tot[1] + R[i][2] * tot[2]);
+#pragma unroll
+    for (int i = 3; i < 6; ++i) g[i] = -tot[i];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) out[i * 6 + j] = H[i][j];
+        out[36 + i] = g[i];
+    }
+    if (!DO_GN) return;
+    double delta[6];
+    pseudo_step(H, g, eig_eps, delta);
+#pragma unroll
     for (int k = 0; k < 3; ++k) pose->td[k] += delta[k];
     const double ax = pose->qd[0], ay = pose->qd[1], az = pose->qd[2], aw = pose->qd[3];
     const double bx = 0.5 * delta[3], by = 0.5 * delta[4], bz = 0.5 * delta[5];
@@ -449,12 +567,14 @@ __global__ void gn_update_kernel(const double* __restrict__ jj, double eig_eps, 
     pose->qd[1] = ny;
     pose->qd[2] = nz;
     pose->qd[3] = nw;
+#pragma unroll
     for (int k = 0; k < 3; ++k) pose->t[k] = (float)pose->td[k];
     pose->q[0] = (float)nx;
     pose->q[1] = (float)ny;
     pose->q[2] = (float)nz;
     pose->q[3] = (float)nw;
     if (step_out)
+#pragma unroll
         for (int k = 0; k < 6; ++k) step_out[k] = delta[k];
 }
 
@@ -468,15 +588,15 @@ cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, const DevPose* pose, double* out,
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                 cudaStream_t s) {
-    track_reduce_kernel<<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out);
+    track_reduce_kernel<false><<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out, 0.0, nullptr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_gn_update(const double* jtj_jtr, double eig_eps, DevPose* pose, double* step_out,
-                             cudaStream_t s) {
-    gn_update_kernel<<<1, 32, 0, s>>>(jtj_jtr, eig_eps, pose, step_out);
+cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
+                                   double eig_eps, double* step_out, cudaStream_t s) {
+    track_reduce_kernel<true><<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out, eig_eps, step_out);
     return cudaGetLastError();
 }
 
