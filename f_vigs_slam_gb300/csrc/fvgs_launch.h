@@ -98,8 +98,21 @@ struct TrackArgs {
     float* img_T;        // P
     uint32_t* img_nc;    // P
     int render_only;     // 1: forward blend for every in-bounds pixel, no Jacobian
+    // reference buffer layout (launch_track_ref_layout only): float2 uv,
+    // float depth, float3 inverse covariance (stored xx, yy, xy), float2 p_hat,
+    // float3 colour, float opacity per Gaussian
+    const float* ref_uv;
+    const float* ref_depth;
+    const float* ref_inv;
+    const float* ref_phat;
+    const float* ref_col;
+    const float* ref_opa;
+    uint32_t quirks;
 };
 cudaError_t launch_track(const TrackArgs& a, cudaStream_t s);
+// The tracking kernel reading the reference's separate screen-space buffers
+// instead of the packed record planes.
+cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s);
 // Sum tile partials in FP64, rotate to the world frame, write out[42] =
 // JtJ[36] (symmetric) then Jtr[6] (negated, as the reference host code does).
 cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,

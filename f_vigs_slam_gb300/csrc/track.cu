@@ -78,7 +78,27 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
     return v[0];
 }
 
-template <bool RENDER_ONLY>
+// Stage one Gaussian's blending record: from the packed record planes, or
+// (REF_LAYOUT) built from the reference's separate screen-space buffers.
+template <bool REF_LAYOUT>
+__device__ __forceinline__ void load_record(const TrackArgs& a, uint32_t g, float4& r0, float4& r1, float4& r2) {
+    if (!REF_LAYOUT) {
+        r0 = a.rec0[g];
+        r1 = a.rec1[g];
+        r2 = a.rec2[g];
+    } else {
+        const float2 uv = reinterpret_cast<const float2*>(a.ref_uv)[g];
+        const float ixx = a.ref_inv[3 * (size_t)g], iyy = a.ref_inv[3 * (size_t)g + 1],
+                    ixy = a.ref_inv[3 * (size_t)g + 2];
+        const float2 ph = reinterpret_cast<const float2*>(a.ref_phat)[g];
+        const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+        r0 = make_float4(uv.x, uv.y, a.ref_depth[g], a.ref_opa[g]);
+        r1 = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, ph.x);
+        r2 = make_float4(ph.y, a.ref_col[3 * (size_t)g], a.ref_col[3 * (size_t)g + 1], a.ref_col[3 * (size_t)g + 2]);
+    }
+}
+
+template <bool RENDER_ONLY, bool REF_LAYOUT = false>
 __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     __shared__ float4 s0[kBatch];
     __shared__ float4 s1[kBatch];
@@ -110,12 +130,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
         for (int base = 0; base < n; base += kBatch) {
             if (__syncthreads_and(done)) break;
             const int li = base + tid;
-            if (li < n) {
-                const uint32_t g = a.indices[range.x + li];
-                s0[tid] = a.rec0[g];
-                s1[tid] = a.rec1[g];
-                s2[tid] = a.rec2[g];
-            }
+            if (li < n) load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
             __syncthreads();
             if (!done) {
                 const int cnt = min(kBatch, n - base);
@@ -233,12 +248,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
         const int li = base + tid;
-        if (li < nmax) {
-            const uint32_t g = a.indices[range.x + li];
-            s0[tid] = a.rec0[g];
-            s1[tid] = a.rec1[g];
-            s2[tid] = a.rec2[g];
-        }
+        if (li < nmax) load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
         __syncthreads();
         if (!done2) {
             const int cnt = min(kBatch, nmax - base);
@@ -585,6 +595,13 @@ cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
         track_tile_kernel<true><<<T, kPix, 0, s>>>(a);
     else
         track_tile_kernel<false><<<T, kPix, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s) {
+    const int T = a.ntx * a.nty;
+    if (T <= 0) return cudaSuccess;
+    track_tile_kernel<false, true><<<T, kPix, 0, s>>>(a);
     return cudaGetLastError();
 }
 

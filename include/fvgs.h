@@ -170,6 +170,36 @@ int fvgs_map_step(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics*
 int fvgs_download_map_state(fvgs_session* s, float* final_T, uint32_t* n_contrib, float* color, float* depth,
                             float* delta2d, float* delta3d);
 
+/*
+ * Allocation-free pose Jacobian for callers that cannot call cudaMalloc -- a
+ * tracking thread inside a host application whose own allocator owns the GPU
+ * memory budget, or a real-time loop that must not pay cudaMalloc/cudaFree's
+ * implicit synchronisation.  No counterpart in the reference: it is an
+ * additional entry point of this library.
+ *
+ * Same result as fvgs_track_jacobian for an already-binned frame, with every
+ * input a caller-owned device buffer in the reference's layout: ranges[2T]
+ * (tile_ranges_), indices (sorted gaussian_indices_), positions_2d[2N],
+ * depths[N], inv_covariances_2d[3N] stored (xx, yy, xy), p_hats[2N],
+ * colors[3N], opacities[N], and the frame's grad_x / grad_y / observed_rgb
+ * [3P] and observed_depth [P].  params may be null (defaults).  JtJ[36] and
+ * Jtr[6] may be host or device pointers; the call returns after the stream
+ * (a cudaStream_t, NULL = legacy default stream) has finished the work.
+ *
+ * Its scratch is one static device array for at most FVGS_NOALLOC_MAX_TILES
+ * 16x16 tiles (about 1.8 MB, held by every GPU that loads the library until
+ * exit); larger frames return FVGS_E_CAPACITY.  The first call on a device
+ * resolves that array's address (make it before any stream capture).  Calls
+ * share the array: calls that overlap on the GPU race.
+ */
+#define FVGS_NOALLOC_MAX_TILES 16384
+int fvgs_rgbd_pose_jacobians_noalloc(const uint32_t* ranges, const uint32_t* indices, const float* positions_2d,
+                                     const float* depths, const float* inv_covariances_2d, const float* p_hats,
+                                     const float* colors, const float* opacities, const float* grad_x,
+                                     const float* grad_y, const float* observed_rgb, const float* observed_depth,
+                                     const fvgs_pose* pose, const fvgs_intrinsics* K, const fvgs_params* params,
+                                     int width, int height, double* JtJ, double* Jtr, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
