@@ -172,6 +172,23 @@ def load_traffic():
     return {}
 
 
+def max_over_ranks(values, device, world):
+    """Elapsed times are the max over ranks (the slowest replica bounds the job)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def replica_throughput(steps, world, max_ms):
+    """Whole-job frames/s: every rank tracks `steps` frames of its own trajectory."""
+    return steps * world / (max_ms / 1000.0)
+
+
 # ----------------------------------------------------------------------------
 # CPU baseline (the CPU restatement of the reference, FP64, all host threads)
 # ----------------------------------------------------------------------------
@@ -359,13 +376,9 @@ def run_ours(args):
     e2e_ms = e0.elapsed_time(e1)
     e2e_wall = (time.perf_counter() - t0) * 1000.0
 
-    if world > 1:
-        t = torch.tensor([ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
-    frames_total = args.steps * world
-    value = frames_total / (ms / 1000.0)
-    e2e_value = frames_total / (e2e_ms / 1000.0)
+    ms, e2e_ms = max_over_ranks([ms, e2e_ms], dev, world)
+    value = replica_throughput(args.steps, world, ms)
+    e2e_value = replica_throughput(args.steps, world, e2e_ms)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -331,6 +331,16 @@ int oracle_sort_ranges(uint64_t* keys, uint32_t* vals, int64_t n_inst, int num_t
         const int64_t launched = (int64_t)((num_tiles + 255) / 256) * 256;
         limit = std::min(limit, launched);
     }
+    if (!(quirks & FVGS_Q_RANGE_LAUNCH)) {
+        // intended: [first, last + 1) of every tile present
+        for (int64_t idx = 0; idx < n_inst; ++idx) {
+            const uint32_t t = (uint32_t)(keys[idx] >> 32);
+            if (idx == 0 || (uint32_t)(keys[idx - 1] >> 32) != t) ranges[2 * (size_t)t] = (uint32_t)idx;
+            if (idx == n_inst - 1 || (uint32_t)(keys[idx + 1] >> 32) != t)
+                ranges[2 * (size_t)t + 1] = (uint32_t)(idx + 1);
+        }
+        return 0;
+    }
     for (int64_t idx = 0; idx < limit; ++idx) {
         const uint32_t t = (uint32_t)(keys[idx] >> 32);
         if (idx == 0) {
