@@ -63,6 +63,7 @@ struct SortWorkspace {
     uint64_t max_items;
     uint32_t epoch;       // advanced per sort call; tags lookback words
     int persistent_ctas;  // resident CTAs of the onesweep kernel
+    int num_sms;
 };
 size_t sort_lookback_words(uint64_t max_items);
 size_t sort_ctrl_words();

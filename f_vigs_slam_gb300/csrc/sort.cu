@@ -7,10 +7,12 @@
 //
 // Structure: one histogram kernel computes the digit counts of every pass in
 // a single read of the keys; then one "onesweep" kernel per pass ranks a
-// 4096-item tile in shared memory (warp match_any multisplit, stable within
-// the tile), obtains the tile's global digit offsets by decoupled look-back
-// over the preceding tiles, and scatters through shared memory so that runs of
-// equal digits are written contiguously.
+// 4096-item tile (512 threads x 8 items) in shared memory -- a warp finds the
+// lanes sharing its digit with 8 ballots, and only the group's leader bumps
+// the warp's shared counter, so ranks are stable within the tile -- obtains
+// the tile's global digit offsets by decoupled look-back that polls 8
+// predecessor tiles per round trip, and scatters through shared memory so
+// that runs of equal digits are written contiguously.
 //
 // The CTAs are persistent (grid = resident capacity) and take tiles from an
 // atomic counter, so every tile a CTA waits on is owned by a running CTA.
@@ -23,12 +25,13 @@
 
 namespace fvgs {
 
-constexpr int kSortThreads = 256;
+constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096
 constexpr int kRadix = 256;
 constexpr int kMaxPasses = 8;
+constexpr int kLookWindow = 8;
 constexpr size_t kSortSmemBytes = (size_t)kSortTile * (sizeof(uint64_t) + sizeof(uint32_t));
 
 constexpr uint64_t kFlagAgg = 1ull << 32;
@@ -43,7 +46,8 @@ __device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Exclusive scan of one value per thread over a 256-thread block.
+// Exclusive scan of one value per thread over the first 256 threads of the
+// block (all threads must call it).
 __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t x, uint32_t* s_warp) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     uint32_t incl = x;
@@ -52,38 +56,54 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t x, uint32_t* s_w
         const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
         if (l >= o) incl += y;
     }
-    if (l == 31) s_warp[w] = incl;
+    if (l == 31 && w < 8) s_warp[w] = incl;
     __syncthreads();
     if (w == 0) {
-        const uint32_t v = (l < kSortWarps) ? s_warp[l] : 0u;
+        const uint32_t v = (l < 8) ? s_warp[l] : 0u;
         uint32_t vi = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(kFullMask, vi, o);
             if (l >= o) vi += y;
         }
-        if (l < kSortWarps) s_warp[l] = vi - v;
+        if (l < 8) s_warp[l] = vi - v;
     }
     __syncthreads();
-    const uint32_t r = s_warp[w] + incl - x;
+    const uint32_t r = (w < 8) ? s_warp[w] + incl - x : 0u;
     __syncthreads();
     return r;
 }
 
-__global__ void __launch_bounds__(256) radix_hist_kernel(const uint64_t* __restrict__ keys,
-                                                         const DevStatus* st, int n_passes,
-                                                         uint32_t* __restrict__ hist) {
-    __shared__ uint32_t sh[kMaxPasses][kRadix];
-    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&sh[0][0])[i] = 0;
+// Digit histograms of every pass in one read of the keys.  Each warp counts
+// into its own shared histograms, so atomics only conflict among the lanes of
+// one instruction.
+constexpr int kHistThreads = 256;
+__global__ void __launch_bounds__(kHistThreads) radix_hist_kernel(const uint64_t* __restrict__ keys,
+                                                                  const DevStatus* st, int n_passes,
+                                                                  uint32_t* __restrict__ hist) {
+    extern __shared__ uint32_t sh[];  // [warps][n_passes][256]
+    const int nw = kHistThreads / 32, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < nw * n_passes * kRadix; i += kHistThreads) sh[i] = 0;
     __syncthreads();
+    uint32_t* mine = sh + (size_t)w * n_passes * kRadix;
     const uint32_t n = st->n_instances_clamped;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
-        for (int p = 0; p < n_passes; ++p) atomicAdd(&sh[p][(uint32_t)(k >> (8 * p)) & 0xffu], 1u);
+    const uint32_t n2 = n / 2;
+    const ulonglong2* k2 = reinterpret_cast<const ulonglong2*>(keys);
+    for (uint32_t i = blockIdx.x * kHistThreads + threadIdx.x; i < n2; i += gridDim.x * kHistThreads) {
+        const ulonglong2 kk = k2[i];
+        for (int p = 0; p < n_passes; ++p) {
+            atomicAdd(&mine[p * kRadix + ((uint32_t)(kk.x >> (8 * p)) & 0xffu)], 1u);
+            atomicAdd(&mine[p * kRadix + ((uint32_t)(kk.y >> (8 * p)) & 0xffu)], 1u);
+        }
+    }
+    if ((n & 1u) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint64_t k = keys[n - 1];
+        for (int p = 0; p < n_passes; ++p) atomicAdd(&mine[p * kRadix + ((uint32_t)(k >> (8 * p)) & 0xffu)], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n_passes * kRadix; i += blockDim.x) {
-        const uint32_t c = (&sh[0][0])[i];
+    for (int i = threadIdx.x; i < n_passes * kRadix; i += kHistThreads) {
+        uint32_t c = 0;
+        for (int ww = 0; ww < nw; ++ww) c += sh[(size_t)ww * n_passes * kRadix + i];
         if (c) atomicAdd(&hist[i], c);
     }
 }
@@ -100,83 +120,110 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     __shared__ uint32_t s_gbase[kRadix];
     __shared__ uint32_t s_prefix[kRadix];
     __shared__ uint32_t s_lexcl[kRadix];
-    __shared__ uint32_t s_scan[kSortWarps];
+    __shared__ uint32_t s_scan[8];
     __shared__ uint32_t s_tile;
 
     const uint32_t n = st->n_instances_clamped;
     const uint32_t n_tiles = (n + kSortTile - 1) / kSortTile;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const uint64_t ep = (uint64_t)epoch << 34;
+    const bool digit_thread = tid < kRadix;
 
-    s_gbase[tid] = block_excl_scan256(hist[tid], s_scan);
+    {
+        const uint32_t g = block_excl_scan256(digit_thread ? hist[tid] : 0u, s_scan);
+        if (digit_thread) s_gbase[tid] = g;
+    }
 
     for (;;) {
         if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+        for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) (&s_whist[0][0])[i] = 0;
         __syncthreads();
         const uint32_t tile = s_tile;
         if (tile >= n_tiles) break;
-#pragma unroll
-        for (int ww = 0; ww < kSortWarps; ++ww) s_whist[ww][tid] = 0;
-        __syncthreads();
 
+        // ---- rank: warp-striped items, ballot multisplit, leader atomics ----
         const uint32_t base = tile * kSortTile + w * (32 * kSortItems);
         uint64_t k[kSortItems];
         uint32_t v[kSortItems];
         uint32_t rank[kSortItems];
-        const uint32_t lt = lanemask_lt();
 #pragma unroll
         for (int j = 0; j < kSortItems; ++j) {
             const uint32_t idx = base + j * 32 + lane;
             const bool valid = idx < n;
             k[j] = valid ? kin[idx] : 0ull;
             v[j] = valid ? vin[idx] : 0u;
-            const uint32_t dig = (uint32_t)(k[j] >> shift) & 0xffu;
-            const uint32_t peers = __match_any_sync(kFullMask, valid ? dig : 0x100u);
-            const uint32_t cnt = __popc(peers);
-            const uint32_t rin = __popc(peers & lt);
-            const int leader = __ffs(peers) - 1;
-            uint32_t b = 0;
-            if (valid) b = s_whist[w][dig];
-            __syncwarp();
-            if (valid && lane == leader) s_whist[w][dig] = b + cnt;
-            __syncwarp();
-            rank[j] = b + rin;
         }
-        __syncthreads();
-        // thread tid owns digit tid: exclusive offsets across warps, tile count
-        uint32_t run = 0;
+        const uint32_t lt = lanemask_lt();
 #pragma unroll
-        for (int ww = 0; ww < kSortWarps; ++ww) {
-            const uint32_t c = s_whist[ww][tid];
-            s_whist[ww][tid] = run;
-            run += c;
-        }
-        const uint32_t cta_cnt = run;
-        uint64_t* lb = lookback + (size_t)tile * kRadix + tid;
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            st_relaxed(lb, ep | kFlagInc | cta_cnt);
-        } else {
-            st_relaxed(lb, ep | kFlagAgg | cta_cnt);
-            int t = (int)tile - 1;
-            uint32_t spins = 0;
-            while (t >= 0) {
-                const uint64_t wv = ld_relaxed(lookback + (size_t)t * kRadix + tid);
-                if ((wv >> 34) == (uint64_t)epoch && (wv & (3ull << 32))) {
-                    prefix += (uint32_t)wv;
-                    if (wv & kFlagInc) break;
-                    --t;
-                } else if (++spins > kSpinLimit) {
-                    atomicOr(err_flags, kErrTimeout);
-                    break;
-                }
+        for (int j = 0; j < kSortItems; ++j) {
+            const uint32_t idx = base + j * 32 + lane;
+            const bool valid = idx < n;
+            const uint32_t dig = (uint32_t)(k[j] >> shift) & 0xffu;
+            uint32_t peers = __ballot_sync(kFullMask, valid);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const bool bit = (dig >> b) & 1u;
+                const uint32_t vote = __ballot_sync(kFullMask, bit);
+                peers &= bit ? vote : ~vote;
             }
-            st_relaxed(lb, ep | kFlagInc | (prefix + cta_cnt));
+            const int leader = __ffs(peers) - 1;
+            uint32_t b0 = 0;
+            if (valid && lane == leader) b0 = atomicAdd(&s_whist[w][dig], (uint32_t)__popc(peers));
+            b0 = __shfl_sync(kFullMask, b0, valid ? leader : lane);
+            rank[j] = b0 + __popc(peers & lt);
         }
-        s_prefix[tid] = prefix;
-        s_lexcl[tid] = block_excl_scan256(cta_cnt, s_scan);
         __syncthreads();
-        // scatter into shared memory at the tile-local sorted position
+        // ---- per digit: exclusive offsets across warps, tile count ----
+        uint32_t cta_cnt = 0;
+        if (digit_thread) {
+#pragma unroll
+            for (int ww = 0; ww < kSortWarps; ++ww) {
+                const uint32_t c = s_whist[ww][tid];
+                s_whist[ww][tid] = cta_cnt;
+                cta_cnt += c;
+            }
+            // ---- decoupled look-back, kLookWindow predecessors per poll ----
+            uint64_t* lb = lookback + (size_t)tile * kRadix + tid;
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                st_relaxed(lb, ep | kFlagInc | cta_cnt);
+            } else {
+                st_relaxed(lb, ep | kFlagAgg | cta_cnt);
+                int t = (int)tile - 1;
+                uint32_t spins = 0;
+                bool found = false;
+                while (!found && t >= 0) {
+                    uint64_t wv[kLookWindow];
+#pragma unroll
+                    for (int i = 0; i < kLookWindow; ++i)
+                        wv[i] = (t - i >= 0) ? ld_relaxed(lookback + (size_t)(t - i) * kRadix + tid) : 0ull;
+                    int consumed = 0;
+#pragma unroll
+                    for (int i = 0; i < kLookWindow; ++i) {
+                        if (found || consumed != i || t - i < 0) continue;
+                        const uint64_t x = wv[i];
+                        if ((x >> 34) == (uint64_t)epoch && (x & (3ull << 32))) {
+                            prefix += (uint32_t)x;
+                            consumed = i + 1;
+                            if (x & kFlagInc) found = true;
+                        }
+                    }
+                    t -= consumed;
+                    if (consumed == 0 && ++spins > kSpinLimit) {
+                        atomicOr(err_flags, kErrTimeout);
+                        break;
+                    }
+                }
+                st_relaxed(lb, ep | kFlagInc | (prefix + cta_cnt));
+            }
+            s_prefix[tid] = prefix;
+        }
+        {
+            const uint32_t e = block_excl_scan256(cta_cnt, s_scan);
+            if (digit_thread) s_lexcl[tid] = e;
+        }
+        __syncthreads();
+        // ---- scatter into shared memory at the tile-local sorted position ----
 #pragma unroll
         for (int j = 0; j < kSortItems; ++j) {
             const uint32_t idx = base + j * 32 + lane;
@@ -188,6 +235,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
             }
         }
         __syncthreads();
+        // ---- coalesced write-out: runs of equal digits are contiguous ----
         const uint32_t tile_n = min((uint32_t)kSortTile, n - tile * kSortTile);
         for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
             const uint64_t kk = s_keys[i];
@@ -202,8 +250,6 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     }
 }
 
-// Always an even number of passes so the result lands back in the caller's
-// buffers; a padding pass whose digit is zero for every key is a stable copy.
 int sort_num_passes(int key_bits) {
     const int p = (key_bits + 7) / 8;
     return p + (p & 1);
@@ -219,6 +265,9 @@ cudaError_t sort_init(SortWorkspace* ws, int device) {
     cudaError_t e = cudaFuncSetAttribute(radix_onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSortSmemBytes);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(radix_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(uint32_t) * (kHistThreads / 32) * kMaxPasses * kRadix));
+    if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, radix_onesweep_kernel, kSortThreads,
                                                       kSortSmemBytes);
@@ -227,6 +276,7 @@ cudaError_t sort_init(SortWorkspace* ws, int device) {
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return e;
     ws->persistent_ctas = (per_sm > 0 ? per_sm : 1) * sms;
+    ws->num_sms = sms;
     if (ws->epoch == 0) ws->epoch = 1;
     return cudaSuccess;
 }
@@ -243,7 +293,8 @@ cudaError_t launch_radix_sort(uint64_t* keys, uint32_t* vals, const DevStatus* s
     }
     cudaError_t e = cudaMemsetAsync(ws->ctrl, 0, sizeof(uint32_t) * sort_ctrl_words(), s);
     if (e != cudaSuccess) return e;
-    radix_hist_kernel<<<ws->persistent_ctas, 256, 0, s>>>(keys, st, passes, ws->ctrl);
+    radix_hist_kernel<<<ws->num_sms * 2, kHistThreads, sizeof(uint32_t) * (kHistThreads / 32) * passes * kRadix, s>>>(
+        keys, st, passes, ws->ctrl);
     uint64_t* kin = keys;
     uint32_t* vin = vals;
     uint64_t* kout = ws->keys_alt;

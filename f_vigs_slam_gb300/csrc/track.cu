@@ -78,6 +78,16 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
     return v[0];
 }
 
+// A Gaussian of opacity o yields alpha = min(0.99, o exp(-v/2)) < 1/255
+// exactly when v > 2 ln(255 o).  vreject is that bound plus a margin far
+// above the rounding of expf and of the product, so pairs beyond it are
+// rejected without evaluating the exponential, with the same outcome.
+__device__ __forceinline__ float reject_bound(float o) {
+    if (!(o > 0.0f)) return -INFINITY;
+    const float b = 2.0f * logf(255.0f * o);
+    return b + 1e-3f + 1e-4f * fabsf(b);
+}
+
 // Stage one Gaussian's blending record: from the packed record planes, or
 // (REF_LAYOUT) built from the reference's separate screen-space buffers.
 template <bool REF_LAYOUT>
@@ -103,6 +113,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     __shared__ float4 s0[kBatch];
     __shared__ float4 s1[kBatch];
     __shared__ float4 s2[kBatch];
+    __shared__ float s_vrej[kBatch];
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
 
@@ -130,7 +141,10 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
         for (int base = 0; base < n; base += kBatch) {
             if (__syncthreads_and(done)) break;
             const int li = base + tid;
-            if (li < n) load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
+            if (li < n) {
+                load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
+                s_vrej[tid] = reject_bound(s0[tid].w);
+            }
             __syncthreads();
             if (!done) {
                 const int cnt = min(kBatch, n - base);
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
                     ++contributor;
                     const float dx = r0.x - xf, dy = r0.y - yf;
                     const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+                    if (v > s_vrej[j] || v <= 0.0f) continue;
                     const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
                     if (alpha < kInv255 || v <= 0.0f) continue;
                     const float test_T = T * (1.0f - alpha);
@@ -248,7 +263,10 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
         const int li = base + tid;
-        if (li < nmax) load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
+        if (li < nmax) {
+            load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
+            s_vrej[tid] = reject_bound(s0[tid].w);
+        }
         __syncthreads();
         if (!done2) {
             const int cnt = min(kBatch, nmax - base);
@@ -261,6 +279,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
                 const float4 r1 = s1[j];
                 const float dx = r0.x - xf, dy = r0.y - yf;
                 const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+                if (v > s_vrej[j]) continue;
                 const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
                 if (alpha < kInv255) continue;
                 const float4 r2 = s2[j];
@@ -471,8 +490,8 @@ __device__ void pseudo_step(const double H[6][6], const double g[6], double eps,
 }
 
 // Frame reduction + (optionally) the Gauss-Newton pose update, one CTA:
-// tiles are summed in FP64 in a fixed order (thread t: tiles t, t+256, ...;
-// butterfly across lanes; warps in order), rotated to the world frame by
+// tiles are summed in a fixed order (thread t: tiles t, t+256, ... in
+// Kahan-compensated FP32; then FP64 across lanes and warps), rotated to the world frame by
 // diag(R, I), written as out[42] = JtJ[36] symmetric, Jtr[6] negated
 // (src/GSSlam.cu:2205-2226); then delta = pseudo-factor step and
 // PoseLocalParameterization::Plus on the device pose.
@@ -482,14 +501,29 @@ __global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restri
                                                            double* step_out) {
     __shared__ double s_w[8][32];
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    double v[32];
+    // First level in compensated FP32 (Kahan): FP64 adds are scarce on this
+    // part, and one SM would otherwise spend ~50 us on them.
+    float sum[27], comp[27];
 #pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] = 0.0;
+    for (int k = 0; k < 27; ++k) {
+        sum[k] = 0.f;
+        comp[k] = 0.f;
+    }
     for (int t = tid; t < num_tiles; t += 256) {
         const float* row = tile_out + (size_t)t * 27;
 #pragma unroll
-        for (int k = 0; k < 27; ++k) v[k] += (double)row[k];
+        for (int k = 0; k < 27; ++k) {
+            const float y = __fsub_rn(row[k], comp[k]);
+            const float s = __fadd_rn(sum[k], y);
+            comp[k] = __fsub_rn(__fsub_rn(s, sum[k]), y);
+            sum[k] = s;
+        }
     }
+    double v[32];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) v[k] = (double)sum[k] - (double)comp[k];
+#pragma unroll
+    for (int k = 27; k < 32; ++k) v[k] = 0.0;
     s_w[w][lane] = warp_reduce_scatter32d(v);
     __syncthreads();
     if (tid != 0) return;
