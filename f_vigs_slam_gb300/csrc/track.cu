@@ -108,12 +108,90 @@ __device__ __forceinline__ void load_record(const TrackArgs& a, uint32_t g, floa
     }
 }
 
+// A tile-level rejection test, done once per staged Gaussian: if the
+// quadratic form is positive definite and its minimum over the tile's pixel
+// rectangle (a convex function, so the minimum is the origin or lies on one of
+// the four edges at the clamped stationary point) exceeds the rejection bound
+// with a margin covering FP32 rounding at the terms' magnitude, every pixel of
+// the tile would reject this Gaussian.  Such Gaussians are dropped from the
+// staged batch; the ones kept carry their original list index, so contributor
+// counts and all results are unchanged.  Non-finite or indefinite forms are
+// always kept.
+__device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float cb, float cc, float vrej, float x0,
+                                              float y0) {
+    if (vrej == -INFINITY) return true;  // zero opacity: alpha is 0 everywhere
+    if (!(isfinite(u) && isfinite(v) && isfinite(ca) && isfinite(cb) && isfinite(cc) && isfinite(vrej))) return false;
+    if (!(ca > 0.f && cc > 0.f && ca * cc - cb * cb > 0.f)) return false;
+    const float dxlo = u - (x0 + (float)(kTW - 1)), dxhi = u - x0;
+    const float dylo = v - (y0 + (float)(kTH - 1)), dyhi = v - y0;
+    if (dxlo <= 0.f && dxhi >= 0.f && dylo <= 0.f && dyhi >= 0.f) return false;
+    float vmin = INFINITY;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const float X = e ? dxhi : dxlo;
+        const float dy = fminf(fmaxf(-cb * X / cc, dylo), dyhi);
+        vmin = fminf(vmin, ca * X * X + 2.0f * cb * X * dy + cc * dy * dy);
+        const float Y = e ? dyhi : dylo;
+        const float dx = fminf(fmaxf(-cb * Y / ca, dxlo), dxhi);
+        vmin = fminf(vmin, ca * dx * dx + 2.0f * cb * dx * Y + cc * Y * Y);
+    }
+    const float mx = fmaxf(fabsf(dxlo), fabsf(dxhi)), my = fmaxf(fabsf(dylo), fabsf(dyhi));
+    const float mag = ca * mx * mx + 2.0f * fabsf(cb) * mx * my + cc * my * my;
+    return vmin > vrej + 1e-5f * mag + 1e-3f;
+}
+
+// Shared-memory batch of Gaussians, repacked so a rejected pair needs two
+// loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, opacity, z),
+// sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list.
+struct TrackBatch {
+    float4 A[kBatch];
+    float4 B[kBatch];
+    float4 C[kBatch];
+    float D[kBatch];
+    int orig[kBatch];
+    int wcnt[kPix / 32];
+};
+
+// Stage entries [base, min(base+256, limit)) of the tile's list, dropping the
+// ones tile_prunable rejects; returns the number kept.  Ends with a barrier.
+template <bool REF_LAYOUT>
+__device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, uint32_t list0, int base, int limit,
+                                           float x0, float y0) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int li = base + tid;
+    bool keep = false;
+    float4 r0, r1, r2;
+    float vrej = 0.f;
+    if (li < limit) {
+        load_record<REF_LAYOUT>(a, a.indices[list0 + li], r0, r1, r2);
+        vrej = reject_bound(r0.w);
+        keep = !tile_prunable(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+    }
+    const uint32_t bal = __ballot_sync(kFullMask, keep);
+    if (lane == 0) sb.wcnt[w] = __popc(bal);
+    __syncthreads();
+    int wbase = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < kPix / 32; ++k) {
+        const int c = sb.wcnt[k];
+        wbase += (k < w) ? c : 0;
+        total += c;
+    }
+    if (keep) {
+        const int pos = wbase + __popc(bal & lanemask_lt());
+        sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
+        sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
+        sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
+        sb.D[pos] = r2.w;
+        sb.orig[pos] = li;
+    }
+    __syncthreads();
+    return total;
+}
+
 template <bool RENDER_ONLY, bool REF_LAYOUT = false>
 __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
-    __shared__ float4 s0[kBatch];
-    __shared__ float4 s1[kBatch];
-    __shared__ float4 s2[kBatch];
-    __shared__ float s_vrej[kBatch];
+    __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
 
@@ -121,6 +199,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int tid = threadIdx.x;
     const int x = tx * kTW + (tid & (kTW - 1)), y = ty * kTH + tid / kTW;
+    const float x0 = (float)(tx * kTW), y0 = (float)(ty * kTH);
     const bool in_bounds = (x < a.W && y < a.H);
     const size_t p = (size_t)y * a.W + x;
     const uint2 range = a.ranges[tile];
@@ -133,42 +212,35 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
 
     // ------------------------- pass 1: forward blend -------------------------
     float T = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, depth = 0.f;
-    uint32_t contributor = 0, last = 0;
+    uint32_t last = 0;
     bool done = !inside;
     float final_T = 1.f;
     uint32_t n_contrib = 0;
     if (n > 0) {
         for (int base = 0; base < n; base += kBatch) {
             if (__syncthreads_and(done)) break;
-            const int li = base + tid;
-            if (li < n) {
-                load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
-                s_vrej[tid] = reject_bound(s0[tid].w);
-            }
-            __syncthreads();
+            const int cnt = stage_batch<REF_LAYOUT>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
-                const int cnt = min(kBatch, n - base);
                 for (int j = 0; j < cnt; ++j) {
-                    const float4 r0 = s0[j];
-                    const float4 r1 = s1[j];
-                    ++contributor;
-                    const float dx = r0.x - xf, dy = r0.y - yf;
-                    const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
-                    if (v > s_vrej[j] || v <= 0.0f) continue;
-                    const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
-                    if (alpha < kInv255 || v <= 0.0f) continue;
+                    const float4 rA = sb.A[j];
+                    const float4 rB = sb.B[j];
+                    const float dx = rA.x - xf, dy = rA.y - yf;
+                    const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
+                    if (v > rB.y || v <= 0.0f) continue;
+                    const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
+                    if (alpha < kInv255) continue;
                     const float test_T = T * (1.0f - alpha);
                     if (test_T < 0.0001f) {
                         done = true;
                         break;
                     }
-                    const float4 r2 = s2[j];
-                    cr += r2.y * alpha * T;
-                    cg += r2.z * alpha * T;
-                    cb += r2.w * alpha * T;
-                    if (T > 0.5f && test_T < 0.5f) depth = depth_at(r0.z, dx, r1.w, dy, r2.x);
+                    const float4 rC = sb.C[j];
+                    cr += rC.z * alpha * T;
+                    cg += rC.w * alpha * T;
+                    cb += sb.D[j] * alpha * T;
+                    if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, dx, rC.x, dy, rC.y);
                     T = test_T;
-                    last = contributor;
+                    last = (uint32_t)sb.orig[j] + 1u;
                 }
             }
         }
@@ -262,29 +334,23 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     const float inv_fx = 1.0f / fx, inv_fy = 1.0f / fy;
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
-        const int li = base + tid;
-        if (li < nmax) {
-            load_record<REF_LAYOUT>(a, a.indices[range.x + li], s0[tid], s1[tid], s2[tid]);
-            s_vrej[tid] = reject_bound(s0[tid].w);
-        }
-        __syncthreads();
+        const int cnt = stage_batch<REF_LAYOUT>(a, sb, range.x, base, nmax, x0, y0);
         if (!done2) {
-            const int cnt = min(kBatch, nmax - base);
             for (int j = 0; j < cnt; ++j) {
-                if (base + j >= (int)n_contrib) {
+                if (sb.orig[j] >= (int)n_contrib) {
                     done2 = true;
                     break;
                 }
-                const float4 r0 = s0[j];
-                const float4 r1 = s1[j];
-                const float dx = r0.x - xf, dy = r0.y - yf;
-                const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
-                if (v > s_vrej[j]) continue;
-                const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
+                const float4 rA = sb.A[j];
+                const float4 rB = sb.B[j];
+                const float dx = rA.x - xf, dy = rA.y - yf;
+                const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
+                if (v > rB.y) continue;
+                const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
                 if (alpha < kInv255) continue;
-                const float4 r2 = s2[j];
-                const float d = depth_at(r0.z, dx, r1.w, dy, r2.x);
-                float da0 = r2.y * prod_alpha, da1 = r2.z * prod_alpha, da2 = r2.w * prod_alpha;
+                const float4 rC = sb.C[j];
+                const float d = depth_at(rB.w, dx, rC.x, dy, rC.y);
+                float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
                 acr += alpha * da0;
                 acg += alpha * da1;
                 acb += alpha * da2;
@@ -292,9 +358,9 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
                 da0 -= (cr - acr) * inv1m;
                 da1 -= (cg - acg) * inv1m;
                 da2 -= (cb - acb) * inv1m;
-                const float dl0 = r1.x * dx + r1.y * dy;
-                const float dl1 = r1.y * dx + r1.z * dy;
-                const float rgx = (r0.x - cx) * inv_fx, rgy = (r0.y - cy) * inv_fy;
+                const float dl0 = rA.z * dx + rA.w * dy;
+                const float dl1 = rA.w * dx + rB.x * dy;
+                const float rgx = (rA.x - cx) * inv_fx, rgy = (rA.y - cy) * inv_fy;
                 const float inv_d = 1.0f / d;
                 const float jt0 = fx * inv_d * dl0;
                 const float jt1 = fy * inv_d * dl1;
