@@ -108,36 +108,55 @@ __device__ __forceinline__ void load_record(const TrackArgs& a, uint32_t g, floa
     }
 }
 
-// A tile-level rejection test, done once per staged Gaussian: if the
-// quadratic form is positive definite and its minimum over the tile's pixel
-// rectangle (a convex function, so the minimum is the origin or lies on one of
-// the four edges at the clamped stationary point) exceeds the rejection bound
-// with a margin covering FP32 rounding at the terms' magnitude, every pixel of
-// the tile would reject this Gaussian.  Such Gaussians are dropped from the
-// staged batch; the ones kept carry their original list index, so contributor
-// counts and all results are unchanged.  Non-finite or indefinite forms are
-// always kept.
+// Minimum of q(dx, dy) = a dx^2 + 2 b dx dy + c dy^2 over the rectangle
+// [dxlo, dxhi] x [dylo, dyhi].  A positive definite q has its minimum at the
+// origin when the rectangle contains it; otherwise (and for any indefinite or
+// negative q) the minimum lies on the boundary, where each edge is a 1-D
+// quadratic: its endpoints, plus the clamped stationary point when convex.
+__device__ __forceinline__ float quad_min_rect(float a, float b, float c, float dxlo, float dxhi, float dylo,
+                                               float dyhi) {
+    if (a > 0.f && c > 0.f && a * c - b * b > 0.f && dxlo <= 0.f && dxhi >= 0.f && dylo <= 0.f && dyhi >= 0.f)
+        return 0.f;
+    float m = INFINITY;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const float X = e ? dxhi : dxlo;
+        const float Y = e ? dyhi : dylo;
+        // corners (each corner is visited once: (X, dylo), (X, dyhi))
+        m = fminf(m, a * X * X + 2.0f * b * X * dylo + c * dylo * dylo);
+        m = fminf(m, a * X * X + 2.0f * b * X * dyhi + c * dyhi * dyhi);
+        if (c > 0.f) {
+            const float dy = fminf(fmaxf(-b * X / c, dylo), dyhi);
+            m = fminf(m, a * X * X + 2.0f * b * X * dy + c * dy * dy);
+        }
+        if (a > 0.f) {
+            const float dx = fminf(fmaxf(-b * Y / a, dxlo), dxhi);
+            m = fminf(m, a * dx * dx + 2.0f * b * dx * Y + c * Y * Y);
+        }
+    }
+    return m;
+}
+
+// Tile-level rejection, done once per staged Gaussian.  A pixel skips a
+// Gaussian when v > vreject (alpha < 1/255, both passes) or, in the forward
+// pass only, when v <= 0.  If the extremes of v over the tile's pixel
+// rectangle prove one of these for every pixel -- min v > vreject, or (forward
+// pass) max v < 0 -- with a margin covering FP32 rounding at the magnitude of
+// the terms, the Gaussian is dropped from the staged batch.  Kept Gaussians
+// carry their original list index, so contributor counts and all results are
+// unchanged.  Non-finite records are always kept.
+template <bool FORWARD>
 __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float cb, float cc, float vrej, float x0,
                                               float y0) {
     if (vrej == -INFINITY) return true;  // zero opacity: alpha is 0 everywhere
     if (!(isfinite(u) && isfinite(v) && isfinite(ca) && isfinite(cb) && isfinite(cc) && isfinite(vrej))) return false;
-    if (!(ca > 0.f && cc > 0.f && ca * cc - cb * cb > 0.f)) return false;
     const float dxlo = u - (x0 + (float)(kTW - 1)), dxhi = u - x0;
     const float dylo = v - (y0 + (float)(kTH - 1)), dyhi = v - y0;
-    if (dxlo <= 0.f && dxhi >= 0.f && dylo <= 0.f && dyhi >= 0.f) return false;
-    float vmin = INFINITY;
-#pragma unroll
-    for (int e = 0; e < 2; ++e) {
-        const float X = e ? dxhi : dxlo;
-        const float dy = fminf(fmaxf(-cb * X / cc, dylo), dyhi);
-        vmin = fminf(vmin, ca * X * X + 2.0f * cb * X * dy + cc * dy * dy);
-        const float Y = e ? dyhi : dylo;
-        const float dx = fminf(fmaxf(-cb * Y / ca, dxlo), dxhi);
-        vmin = fminf(vmin, ca * dx * dx + 2.0f * cb * dx * Y + cc * Y * Y);
-    }
     const float mx = fmaxf(fabsf(dxlo), fabsf(dxhi)), my = fmaxf(fabsf(dylo), fabsf(dyhi));
-    const float mag = ca * mx * mx + 2.0f * fabsf(cb) * mx * my + cc * my * my;
-    return vmin > vrej + 1e-5f * mag + 1e-3f;
+    const float margin = 1e-5f * (fabsf(ca) * mx * mx + 2.0f * fabsf(cb) * mx * my + fabsf(cc) * my * my) + 1e-3f;
+    if (quad_min_rect(ca, cb, cc, dxlo, dxhi, dylo, dyhi) > vrej + margin) return true;
+    if (FORWARD && -quad_min_rect(-ca, -cb, -cc, dxlo, dxhi, dylo, dyhi) < -margin) return true;
+    return false;
 }
 
 // Shared-memory batch of Gaussians, repacked so a rejected pair needs two
@@ -154,7 +173,7 @@ struct TrackBatch {
 
 // Stage entries [base, min(base+256, limit)) of the tile's list, dropping the
 // ones tile_prunable rejects; returns the number kept.  Ends with a barrier.
-template <bool REF_LAYOUT>
+template <bool REF_LAYOUT, bool FORWARD>
 __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, uint32_t list0, int base, int limit,
                                            float x0, float y0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -165,7 +184,7 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
     if (li < limit) {
         load_record<REF_LAYOUT>(a, a.indices[list0 + li], r0, r1, r2);
         vrej = reject_bound(r0.w);
-        keep = !tile_prunable(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+        keep = !tile_prunable<FORWARD>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
     }
     const uint32_t bal = __ballot_sync(kFullMask, keep);
     if (lane == 0) sb.wcnt[w] = __popc(bal);
@@ -219,7 +238,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     if (n > 0) {
         for (int base = 0; base < n; base += kBatch) {
             if (__syncthreads_and(done)) break;
-            const int cnt = stage_batch<REF_LAYOUT>(a, sb, range.x, base, n, x0, y0);
+            const int cnt = stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
                 for (int j = 0; j < cnt; ++j) {
                     const float4 rA = sb.A[j];
@@ -334,7 +353,7 @@ __global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
     const float inv_fx = 1.0f / fx, inv_fy = 1.0f / fy;
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
-        const int cnt = stage_batch<REF_LAYOUT>(a, sb, range.x, base, nmax, x0, y0);
+        const int cnt = stage_batch<REF_LAYOUT, false>(a, sb, range.x, base, nmax, x0, y0);
         if (!done2) {
             for (int j = 0; j < cnt; ++j) {
                 if (sb.orig[j] >= (int)n_contrib) {
@@ -555,20 +574,55 @@ __device__ void pseudo_step(const double H[6][6], const double g[6], double eps,
     }
 }
 
+__device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(kFullMask, v, src); }
+
+// Lower-triangle lane map: lane l < 21 holds entry (i, j), i >= j,
+// l = i (i + 1) / 2 + j.
+__device__ __forceinline__ int tri_index(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// Warp-parallel Cholesky of a symmetric 6x6 held as one lower-triangle entry
+// per lane (lanes >= 21 idle).  On return lane tri_index(i, j) holds L[i][j];
+// returns false (uniformly) if a pivot is not positive.
+__device__ __forceinline__ bool warp_chol6(double& m, int li, int lj) {
+    const int lane = threadIdx.x & 31;
+    const bool act = lane < 21;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double dkk = shfl_d(m, tri_index(k, k));
+        if (!(dkk > 0.0)) return false;
+        const double s = sqrt(dkk);
+        const double inv = 1.0 / s;
+        if (act && lj == k) m = (li == k) ? s : m * inv;
+        // trailing update m(i, j) -= L(i, k) L(j, k) for j > k
+        const double lik = shfl_d(m, act ? tri_index(li, k) : 0);
+        const double ljk = shfl_d(m, (act && lj > k) ? tri_index(lj, k) : 0);
+        if (act && lj > k) m = fma(-lik, ljk, m);
+    }
+    return true;
+}
+
 // Frame reduction + (optionally) the Gauss-Newton pose update, one CTA:
 // tiles are summed in a fixed order (thread t: tiles t, t+256, ... in
-// Kahan-compensated FP32; then FP64 across lanes and warps), rotated to the world frame by
-// diag(R, I), written as out[42] = JtJ[36] symmetric, Jtr[6] negated
-// (src/GSSlam.cu:2205-2226); then delta = pseudo-factor step and
+// Kahan-compensated FP32; then FP64 across lanes and warps), rotated to the
+// world frame by diag(R, I), written as out[42] = JtJ[36] symmetric, Jtr[6]
+// negated (src/GSSlam.cu:2205-2226); then the pseudo-factor step of
+// RgbdPoseCostFunction (src/RgbdPoseCost.cu:57-78) and
 // PoseLocalParameterization::Plus on the device pose.
+//
+// FP64 is issued slowly on this part, so the 6x6 work is spread over lanes:
+// warp 0 factors H - eps*I (all eigenvalues > eps exactly when it is positive
+// definite, and then the eigen-regularised step equals -H^-1 g), warp 1 factors
+// H and solves; only a failed test falls back to a one-thread Jacobi
+// eigen-decomposition that drops the small eigenvalues.
 template <bool DO_GN>
 __global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles,
                                                            DevPose* pose, double* out, double eig_eps,
                                                            double* step_out) {
     __shared__ double s_w[8][32];
+    __shared__ double s_tot[27];
+    __shared__ double s_R[9];
+    __shared__ int s_pd;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    // First level in compensated FP32 (Kahan): FP64 adds are scarce on this
-    // part, and one SM would otherwise spend ~50 us on them.
     float sum[27], comp[27];
 #pragma unroll
     for (int k = 0; k < 27; ++k) {
@@ -592,74 +646,132 @@ __global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restri
     for (int k = 27; k < 32; ++k) v[k] = 0.0;
     s_w[w][lane] = warp_reduce_scatter32d(v);
     __syncthreads();
-    if (tid != 0) return;
-    double tot[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) {
+    if (w >= 2) return;
+    // ---- warps 0 and 1 only; named barrier 1 over 64 threads ----
+    if (w == 0 && lane < 27) {
         double s = 0.0;
 #pragma unroll
-        for (int ww = 0; ww < 8; ++ww) s += s_w[ww][k];
-        tot[k] = s;
+        for (int ww = 0; ww < 8; ++ww) s += s_w[ww][lane];
+        s_tot[lane] = s;
     }
-    const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
-    double R[3][3];
-    R[0][0] = 1.0 - 2.0 * (qy * qy + qz * qz);
-    R[0][1] = 2.0 * (qx * qy - qw * qz);
-    R[0][2] = 2.0 * (qx * qz + qw * qy);
-    R[1][0] = 2.0 * (qx * qy + qw * qz);
-    R[1][1] = 1.0 - 2.0 * (qx * qx + qz * qz);
-    R[1][2] = 2.0 * (qy * qz - qw * qx);
-    R[2][0] = 2.0 * (qx * qz - qw * qy);
-    R[2][1] = 2.0 * (qy * qz + qw * qx);
-    R[2][2] = 1.0 - 2.0 * (qx * qx + qy * qy);
-    double Ac[6][6];
-    {
-        int idx = 0;
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int j = i; j < 6; ++j) {
-                Ac[i][j] = tot[6 + idx];
-                Ac[j][i] = tot[6 + idx];
-                ++idx;
-            }
-    }
-    // H = D Ac D^T, D = diag(R, I); g = -(D b)
-    double H[6][6], g[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-            double s = 0.0;
-            if (i < 3 && j < 3) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int b = 0; b < 3; ++b) s += R[i][a] * Ac[a][b] * R[j][b];
-            } else if (i < 3) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) s += R[i][a] * Ac[a][j];
-            } else if (j < 3) {
-#pragma unroll
-                for (int b = 0; b < 3; ++b) s += Ac[i][b] * R[j][b];
-            } else {
-                s = Ac[i][j];
-            }
-            H[i][j] = s;
+    if (w == 1 && lane < 9) {
+        const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+        const int i = lane / 3, j = lane % 3;
+        const double q[3] = {qx, qy, qz};
+        double r;
+        if (i == j) {
+            const double a = q[(i + 1) % 3], b = q[(i + 2) % 3];
+            r = 1.0 - 2.0 * (a * a + b * b);
+        } else {
+            // off-diagonal: 2 (q_i q_j -/+ w q_k), sign + when (i, j) is (1,0), (2,1), (0,2)
+            const int k = 3 - i - j;
+            const bool plus = (i == (j + 1) % 3);
+            r = 2.0 * (q[i] * q[j] + (plus ? qw * q[k] : -qw * q[k]));
         }
+        s_R[lane] = r;
+    }
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    // lane l < 21: H entry (li, lj) of H = D A D^T, D = diag(R, I);
+    // lanes 21..26: g = -(D b)
+    int li = 0, lj = 0;
+    if (lane < 21) {
+        while (tri_index(li + 1, 0) <= lane) ++li;
+        lj = lane - tri_index(li, 0);
+    }
+    auto Ac = [&](int a, int b) {
+        const int hi = a > b ? a : b, lo = a > b ? b : a;
+        // upper-triangle row-major index of (lo, hi)
+        return s_tot[6 + lo * 6 - lo * (lo - 1) / 2 + (hi - lo)];
+    };
+    double m = 0.0, gval = 0.0;
+    if (lane < 21) {
+        if (li < 3) {  // then lj < 3
+            double s = 0.0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) g[i] = -(R[i][0] * tot[0] + R[i][1] * tot[1] + R[i][2] * tot[2]);
+            for (int a2 = 0; a2 < 3; ++a2)
 #pragma unroll
-    for (int i = 3; i < 6; ++i) g[i] = -tot[i];
+                for (int b2 = 0; b2 < 3; ++b2) s = fma(s_R[li * 3 + a2] * Ac(a2, b2), s_R[lj * 3 + b2], s);
+            m = s;
+        } else if (lj < 3) {
+            double s = 0.0;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) out[i * 6 + j] = H[i][j];
-        out[36 + i] = g[i];
+            for (int b2 = 0; b2 < 3; ++b2) s = fma(Ac(li, b2), s_R[lj * 3 + b2], s);
+            m = s;
+        } else {
+            m = Ac(li, lj);
+        }
+    } else if (lane < 27) {
+        const int i = lane - 21;
+        if (i < 3)
+            gval = -(s_R[i * 3] * s_tot[0] + s_R[i * 3 + 1] * s_tot[1] + s_R[i * 3 + 2] * s_tot[2]);
+        else
+            gval = -s_tot[i];
+    }
+    if (w == 0) {
+        // full symmetric JtJ and Jtr to the output
+        if (lane < 21) {
+            out[li * 6 + lj] = m;
+            out[lj * 6 + li] = m;
+        } else if (lane < 27) {
+            out[36 + lane - 21] = gval;
+        }
     }
     if (!DO_GN) return;
+    if (w == 0) {
+        double me = m;
+        if (lane < 21 && li == lj) me -= eig_eps;
+        const bool pd = warp_chol6(me, li, lj);
+        if (lane == 0) s_pd = pd ? 1 : 0;
+        asm volatile("bar.sync 1, 64;" ::: "memory");
+        return;
+    }
+    // warp 1
+    double mh = m;
+    const bool pdh = warp_chol6(mh, li, lj);
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    double delta_lane = 0.0;  // lane k < 6 ends with delta[k]
+    if (s_pd && pdh) {
+        // forward substitution L y = g (lane k holds g_k / y_k)
+        double yv = shfl_d(gval, (lane < 6) ? lane + 21 : 21);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double lkk = shfl_d(mh, tri_index(k, k));
+            const double yk = shfl_d(yv, k) / lkk;
+            if (lane == k) yv = yk;
+            const double lik = shfl_d(mh, (lane < 6 && lane > k) ? tri_index(lane, k) : 0);
+            if (lane < 6 && lane > k) yv = fma(-lik, yk, yv);
+        }
+        // back substitution L^T x = y
+#pragma unroll
+        for (int k = 5; k >= 0; --k) {
+            const double lkk = shfl_d(mh, tri_index(k, k));
+            const double xk = shfl_d(yv, k) / lkk;
+            if (lane == k) yv = xk;
+            const double lki = shfl_d(mh, (lane < k) ? tri_index(k, lane) : 0);
+            if (lane < k) yv = fma(-lki, xk, yv);
+        }
+        delta_lane = -yv;
+    } else {
+        // rare: some eigenvalue <= eps -- exact eigen-decomposition on one lane
+        double dl[6] = {0, 0, 0, 0, 0, 0};
+        if (lane == 0) {
+            double H[6][6], g[6];
+            for (int i = 0; i < 6; ++i) {
+                for (int j = 0; j < 6; ++j) H[i][j] = out[i * 6 + j];
+                g[i] = out[36 + i];
+            }
+            pseudo_step(H, g, eig_eps, dl);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double d = shfl_d(dl[k], 0);
+            if (lane == k) delta_lane = d;
+        }
+    }
     double delta[6];
-    pseudo_step(H, g, eig_eps, delta);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) delta[k] = shfl_d(delta_lane, k);
+    if (lane != 0) return;
 #pragma unroll
     for (int k = 0; k < 3; ++k) pose->td[k] += delta[k];
     const double ax = pose->qd[0], ay = pose->qd[1], az = pose->qd[2], aw = pose->qd[3];
@@ -668,11 +780,11 @@ __global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restri
     double ny = aw * by + ay + (az * bx - ax * bz);
     double nz = aw * bz + az + (ax * by - ay * bx);
     double nw = aw - (ax * bx + ay * by + az * bz);
-    const double nn = sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
-    nx /= nn;
-    ny /= nn;
-    nz /= nn;
-    nw /= nn;
+    const double inn = 1.0 / sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+    nx *= inn;
+    ny *= inn;
+    nz *= inn;
+    nw *= inn;
     pose->qd[0] = nx;
     pose->qd[1] = ny;
     pose->qd[2] = nz;
