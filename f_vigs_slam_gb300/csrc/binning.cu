@@ -142,6 +142,14 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
                            __float_as_uint(phy));
     a.bin1[i] = make_float4(u, v, z, phx);
     a.counts[i] = count;
+    if (a.tile_diff && count) {
+        // 2-D difference grid of the tile rectangle: tile counts are its 2-D prefix sums
+        const int gw = a.ntx + 1;
+        atomicAdd(&a.tile_diff[y0 * gw + x0], 1);
+        atomicAdd(&a.tile_diff[y0 * gw + x1 + 1], -1);
+        atomicAdd(&a.tile_diff[(y1 + 1) * gw + x0], -1);
+        atomicAdd(&a.tile_diff[(y1 + 1) * gw + x1 + 1], 1);
+    }
     if (a.dbg_cov) {
         a.dbg_cov[3 * i] = cxx;
         a.dbg_cov[3 * i + 1] = cyy;
@@ -357,6 +365,152 @@ __global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tile offsets from the difference grid (one CTA): 2-D prefix sums give the
+// instance count of every tile; an exclusive scan in row-major tile order gives
+// each tile's [start, end) in the tile-major instance array -- these are the
+// per-tile ranges, and the starts seed the scatter cursors.
+// ---------------------------------------------------------------------------
+constexpr int kOffThreads = 1024;
+constexpr int kOffSmemCells = 48 * 1024;  // 192 KB of grid staged in shared memory
+__global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, int ntx, int nty, uint2* ranges,
+                                                                   uint32_t* fill, DevStatus* st, uint32_t capacity) {
+    extern __shared__ int s_grid[];
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    const int gw = ntx + 1, gh = nty + 1;
+    const bool staged = gw * gh <= kOffSmemCells;
+    int* g = staged ? s_grid : diff;
+    if (staged)
+        for (int i = threadIdx.x; i < gw * gh; i += kOffThreads) s_grid[i] = diff[i];
+    __syncthreads();
+    // row prefix sums (one thread per grid row), then column prefix sums
+    for (int r = threadIdx.x; r < gh; r += kOffThreads) {
+        int acc = 0;
+        for (int c = 0; c < gw; ++c) {
+            acc += g[r * gw + c];
+            g[r * gw + c] = acc;
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < gw; c += kOffThreads) {
+        int acc = 0;
+        for (int r = 0; r < gh; ++r) {
+            acc += g[r * gw + c];
+            g[r * gw + c] = acc;
+        }
+    }
+    __syncthreads();
+    // exclusive scan of tile counts in row-major tile order
+    const int T = ntx * nty;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < T; base += kOffThreads) {
+        const int t = base + threadIdx.x;
+        uint32_t c = 0;
+        if (t < T) c = (uint32_t)g[(t / ntx) * gw + (t % ntx)];
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_w[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            const uint32_t v = s_w[lane];
+            uint32_t vi = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFullMask, vi, o);
+                if (lane >= o) vi += y;
+            }
+            s_w[lane] = vi - v;
+        }
+        __syncthreads();
+        const uint32_t start = s_carry + s_w[w] + incl - c;
+        if (t < T) {
+            ranges[t] = make_uint2(start, start + c);
+            fill[t] = start;
+        }
+        __syncthreads();
+        if (threadIdx.x == kOffThreads - 1) s_carry = start + c;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t total = s_carry;
+        st->n_instances = total;
+        st->n_instances_clamped = total < capacity ? total : capacity;
+        if (total > capacity) atomicOr(&st->flags, kErrOverflow);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scatter emission: the warp-cooperative walk of emit_keys_kernel, but each
+// instance takes the next slot of its tile (atomic cursor) and stores the
+// composite key depth_bits << 32 | Gaussian index.  The order inside a tile is
+// arbitrary here; the per-tile sort on these unique keys restores the
+// reference's (depth, generation order).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st) {
+    if (st->flags & kErrOverflow) return;
+    const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+    const int lane = threadIdx.x & 31;
+    if (gbase >= a.n) return;
+    const int g = gbase + lane;
+    const bool valid = g < a.n;
+    uint4 b0 = make_uint4(0, 0, 0, 0);
+    float4 b1 = make_float4(0, 0, 0, 0);
+    if (valid) {
+        b0 = a.bin0[g];
+        b1 = a.bin1[g];
+    }
+    const uint32_t cnt = valid ? b0.z : 0u;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t excl = incl - cnt;
+    const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+    const uint64_t cap = a.capacity;
+    for (uint32_t m0 = 0; m0 < total; m0 += 32) {
+        const uint32_t m = m0 + lane;
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t e = __shfl_sync(kFullMask, excl, lo + step);
+            if (e <= m) lo += step;
+        }
+        const uint32_t r0 = __shfl_sync(kFullMask, b0.x, lo);
+        const uint32_t r1 = __shfl_sync(kFullMask, b0.y, lo);
+        const uint32_t phy_bits = __shfl_sync(kFullMask, b0.w, lo);
+        const float u = __shfl_sync(kFullMask, b1.x, lo);
+        const float v = __shfl_sync(kFullMask, b1.y, lo);
+        const float z = __shfl_sync(kFullMask, b1.z, lo);
+        const float phx = __shfl_sync(kFullMask, b1.w, lo);
+        const uint32_t e_lo = __shfl_sync(kFullMask, excl, lo);
+        if (m < total) {
+            const uint32_t local = m - e_lo;
+            const int x0 = (int)(r0 & 0xffffu), y0 = (int)(r0 >> 16);
+            const int x1 = (int)(r1 & 0xffffu);
+            const int w = x1 - x0 + 1;
+            const int tx = x0 + (int)(local % (uint32_t)w);
+            const int ty = y0 + (int)(local / (uint32_t)w);
+            const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)a.tw);
+            const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)a.th);
+            const float dx = __fsub_rn(tcx, u);
+            const float dy = __fsub_rn(tcy, v);
+            const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+            const uint32_t tile = (uint32_t)(ty * a.ntx + tx);
+            const uint32_t slot = atomicAdd(&fill[tile], 1u);
+            if (slot < cap) a.keys[slot] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo);
+        }
+    }
+}
+
 // ------------------------------- launchers ---------------------------------
 cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
@@ -386,6 +540,30 @@ cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_til
     cudaError_t e = cudaMemsetAsync(ranges, 0, sizeof(uint2) * (size_t)num_tiles, s);
     if (e != cudaSuccess) return e;
     ranges_kernel<<<grid, 256, 0, s>>>(keys, st, num_tiles, quirks, ranges);
+    return cudaGetLastError();
+}
+
+}  // namespace fvgs
+
+namespace fvgs {
+
+size_t tile_diff_words(int ntx, int nty) { return (size_t)(ntx + 1) * (nty + 1); }
+
+cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
+                                uint32_t capacity, cudaStream_t s) {
+    // set on every launch: cheap, and correct for whichever device is current
+    const cudaError_t e = cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)(sizeof(int) * kOffSmemCells));
+    if (e != cudaSuccess) return e;
+    const size_t cells = tile_diff_words(ntx, nty);
+    const size_t smem = cells <= (size_t)kOffSmemCells ? sizeof(int) * cells : 0;
+    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(diff, ntx, nty, ranges, fill, st, capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, const DevStatus* st, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    emit_scatter_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, fill, st);
     return cudaGetLastError();
 }
 

@@ -105,6 +105,10 @@ struct fvgs_session {
     int cap_tiles = 0;
     uint2* ranges = nullptr;
     float* tile_out = nullptr;
+    int* tile_diff = nullptr;      // (ntx+1) x (nty+1) difference grid of tile counts
+    size_t tile_diff_cells = 0;
+    uint32_t* tile_fill = nullptr;  // scatter cursors
+    SegSortWork seg{};
 
     FrameLevel lv[kMaxLevels];
 
@@ -328,14 +332,15 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         pa.dbg_inv = s->dbg_inv;
         pa.dbg_vis = s->dbg_vis;
     }
+    const bool radix = (s->debug & FVGS_DEBUG_RADIX_SORT) != 0;
+    if (!radix) {
+        if (T > s->cap_tiles || tile_diff_words(ntx, nty) > s->tile_diff_cells) return FVGS_E_INVALID;
+        FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * tile_diff_words(ntx, nty), s->stream));
+        pa.tile_diff = s->tile_diff;
+    }
     {
         KScope k(s, FVGS_K_PROJECT, 1);
         FV_CK(launch_project_count(pa, s->stream));
-    }
-    {
-        KScope k(s, FVGS_K_SCAN, 2);
-        FV_CK(launch_scan(s->counts, (int)s->n_g, s->partials, s->offsets, s->st,
-                          (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu), s->stream));
     }
     EmitArgs ea{};
     ea.bin0 = s->bin0;
@@ -346,20 +351,49 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     ea.tw = P.tile_w;
     ea.th = P.tile_h;
     ea.capacity = s->cap_inst;
-    ea.keys = s->keys;
-    ea.vals = s->vals;
-    {
-        KScope k(s, FVGS_K_EMIT, 1);
-        FV_CK(launch_emit_keys(ea, s->stream));
-    }
-    const int key_bits = 32 + std::max(1, bits_for(T));
-    {
-        KScope k(s, FVGS_K_SORT, 1 + (uint32_t)sort_num_passes(key_bits));
-        FV_CK(launch_radix_sort(s->keys, s->vals, s->st, key_bits, &s->sort, &s->st->flags, s->stream));
-    }
-    {
-        KScope k(s, FVGS_K_RANGES, 1);
-        FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+    const uint32_t cap32 = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+    if (!radix) {
+        // tile-bucket binning: counts -> ranges -> scatter -> per-tile sort
+        {
+            KScope k(s, FVGS_K_SCAN, 1);
+            FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, s->ranges, s->tile_fill, s->st, cap32, s->stream));
+        }
+        ea.keys = s->sort.keys_alt;  // composite keys, tile-major
+        ea.vals = nullptr;
+        {
+            KScope k(s, FVGS_K_EMIT, 1);
+            FV_CK(launch_emit_scatter(ea, s->tile_fill, s->st, s->stream));
+        }
+        {
+            KScope k(s, FVGS_K_SORT, 2);
+            FV_CK(launch_segsort(s->sort.keys_alt, s->keys, s->ranges, T, s->vals, s->keys, s->seg, s->st,
+                                 s->num_sms, s->stream));
+        }
+        if (P.quirks & FVGS_Q_RANGE_LAUNCH) {
+            KScope k(s, FVGS_K_RANGES, 1);
+            FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+        }
+    } else {
+        // global path: offsets scan, generation-order keys, LSD radix sort, ranges
+        {
+            KScope k(s, FVGS_K_SCAN, 2);
+            FV_CK(launch_scan(s->counts, (int)s->n_g, s->partials, s->offsets, s->st, cap32, s->stream));
+        }
+        ea.keys = s->keys;
+        ea.vals = s->vals;
+        {
+            KScope k(s, FVGS_K_EMIT, 1);
+            FV_CK(launch_emit_keys(ea, s->stream));
+        }
+        const int key_bits = 32 + std::max(1, bits_for(T));
+        {
+            KScope k(s, FVGS_K_SORT, 1 + (uint32_t)sort_num_passes(key_bits));
+            FV_CK(launch_radix_sort(s->keys, s->vals, s->st, key_bits, &s->sort, &s->st->flags, s->stream));
+        }
+        {
+            KScope k(s, FVGS_K_RANGES, 1);
+            FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+        }
     }
     s->last_W = W;
     s->last_H = H;
@@ -634,6 +668,11 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     const int ntx = (max_width + P.tile_w - 1) / P.tile_w, nty = (max_height + P.tile_h - 1) / P.tile_h;
     s->cap_tiles = ntx * nty;
     FV_A(s->ranges, (size_t)s->cap_tiles);
+    s->tile_diff_cells = tile_diff_words(ntx, nty);
+    FV_A(s->tile_diff, s->tile_diff_cells);
+    FV_A(s->tile_fill, (size_t)s->cap_tiles);
+    FV_A(s->seg.large_list, (size_t)s->cap_tiles);
+    FV_A(s->seg.large_ctrl, 2);
     FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
     FV_A(s->pose, 1);
     FV_A(s->jj, 48);

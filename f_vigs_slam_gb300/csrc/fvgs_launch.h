@@ -30,6 +30,7 @@ struct ProjectArgs {
     uint4* bin0;
     float4* bin1;
     uint32_t* counts;
+    int* tile_diff;    // optional: (ntx+1) x (nty+1) difference grid of tile counts
     float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
     float* dbg_inv;    // optional: 3N inverse, stored order (xx, yy, xy)
     uint8_t* dbg_vis;  // optional: N visibility
@@ -53,6 +54,22 @@ cudaError_t launch_scan(const uint32_t* counts, int n, uint32_t* partials, uint3
 cudaError_t launch_emit_keys(const EmitArgs& a, cudaStream_t s);
 cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_tiles, uint32_t quirks,
                           uint2* ranges, int grid, cudaStream_t s);
+// Tile-bucket binning: counts from the projection's difference grid, then
+// ranges / cursors, then scatter of composite keys (depth bits << 32 | index).
+size_t tile_diff_words(int ntx, int nty);
+cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
+                                uint32_t capacity, cudaStream_t s);
+cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, const DevStatus* st, cudaStream_t s);
+// Per-tile sort of the composite keys (segsort.cu): writes the sorted Gaussian
+// indices to vals and the reference-format keys (tile << 32 | depth bits) to
+// keys.  Tiles above 4096 instances go through a global merge sort that uses
+// tmp (capacity u64) as scratch.
+struct SegSortWork {
+    uint32_t* large_list;  // [T] tiles too large for one CTA
+    uint32_t* large_ctrl;  // [2]: count, next
+};
+cudaError_t launch_segsort(const uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
+                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid, cudaStream_t s);
 
 // ---- radix sort (sort.cu) ----
 struct SortWorkspace {

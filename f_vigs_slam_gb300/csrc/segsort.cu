@@ -1,0 +1,206 @@
+// segsort.cu -- per-tile sort of tile-bucketed instances for sm_103a.
+//
+// The reference sorts all (tile << 32 | depth bits) keys with a stable 64-bit
+// radix sort (thrust::sort_by_key, src/GSSlam.cu:624-628).  A Gaussian has at
+// most one instance per tile and instances are generated in Gaussian-index
+// order, so inside a tile that stable order is exactly the order of the
+// unique composite key (depth bits << 32 | Gaussian index).  Instances are
+// therefore scattered into per-tile buckets (any order) and each bucket is
+// sorted on its own:
+//  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 16
+//    keys in registers with a bitonic network, then log2(n/16) merge-path
+//    rounds double the sorted runs;
+//  * larger buckets (rare: huge splats, culled slots piled into tile 0) are
+//    listed by the first kernel and sorted by a second one: chunks of 4096 in
+//    shared memory, then merge-path passes through global memory.
+// The outputs are the sorted Gaussian indices and the reference-format keys.
+#include "fvgs_device.cuh"
+#include "fvgs_launch.h"
+
+namespace fvgs {
+
+constexpr int kSegThreads = 256;
+constexpr int kSegItems = 16;
+constexpr int kSegCap = kSegThreads * kSegItems;  // 4096
+constexpr uint64_t kKeyInf = ~0ull;
+
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }  // one pad word per 16 keys
+
+// Sort 16 keys in registers (bitonic network, ascending).
+__device__ __forceinline__ void sort16(uint64_t (&k)[16]) {
+#pragma unroll
+    for (int sz = 2; sz <= 16; sz <<= 1)
+#pragma unroll
+        for (int j = sz >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & sz) == 0;
+                    const uint64_t a = k[i], b = k[l];
+                    if ((a > b) == up) {
+                        k[i] = b;
+                        k[l] = a;
+                    }
+                }
+            }
+}
+
+// Sort s[0..m) (padded layout, m a power of two in [16, 4096]) in shared
+// memory with the CTA.  Threads >= m/16 only take part in the barriers.
+__device__ void block_merge_sort(uint64_t* s, int m) {
+    const int t = threadIdx.x;
+    const int active = m / kSegItems;
+    uint64_t k[16];
+    if (t < active) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) k[j] = s[spad(t * 16 + j)];
+        sort16(k);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s[spad(t * 16 + j)] = k[j];
+    }
+    __syncthreads();
+    for (int L = 16; L < m; L <<= 1) {
+        if (t < active) {
+            const int per_pair = (2 * L) / kSegItems;
+            const int ps = (t / per_pair) * 2 * L;
+            const int d = (t % per_pair) * kSegItems;
+            const uint64_t* A = s;  // run A at [ps, ps+L), run B at [ps+L, ps+2L)
+            int lo = max(0, d - L), hi = min(d, L);
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (A[spad(ps + mid)] <= A[spad(ps + L + d - 1 - mid)])
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            int ai = lo, bj = d - lo;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const uint64_t a = ai < L ? A[spad(ps + ai)] : kKeyInf;
+                const uint64_t b = bj < L ? A[spad(ps + L + bj)] : kKeyInf;
+                const bool ta = a <= b;
+                k[r] = ta ? a : b;
+                ai += ta ? 1 : 0;
+                bj += ta ? 0 : 1;
+            }
+        }
+        __syncthreads();
+        if (t < active) {
+            const int per_pair = (2 * L) / kSegItems;
+            const int ps = (t / per_pair) * 2 * L;
+            const int d = (t % per_pair) * kSegItems;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) s[spad(ps + d + r)] = k[r];
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32_t dst, uint32_t* vals,
+                                             uint64_t* keys) {
+    vals[dst] = (uint32_t)key;
+    keys[dst] = ((uint64_t)tile << 32) | (key >> 32);
+}
+
+__global__ void __launch_bounds__(kSegThreads) segsort_kernel(const uint64_t* __restrict__ comp,
+                                                              const uint2* __restrict__ ranges, uint32_t* vals,
+                                                              uint64_t* keys, SegSortWork w, const DevStatus* st) {
+    __shared__ uint64_t s[kSegCap + kSegCap / 16];
+    if (st->flags & kErrOverflow) return;
+    const uint32_t tile = blockIdx.x;
+    const uint2 r = ranges[tile];
+    const int n = (int)(r.y - r.x);
+    if (n <= 0) return;
+    if (n > kSegCap) {
+        if (threadIdx.x == 0) w.large_list[atomicAdd(&w.large_ctrl[0], 1u)] = tile;
+        return;
+    }
+    int m = kSegItems;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += kSegThreads) s[spad(i)] = i < n ? comp[r.x + i] : kKeyInf;
+    __syncthreads();
+    block_merge_sort(s, m);
+    for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(s[spad(i)], tile, r.x + i, vals, keys);
+}
+
+// Large buckets: persistent CTAs take listed tiles; each sorts 4096-key
+// chunks in shared memory into tmp, then merges runs through global memory
+// (every thread merges 16 outputs after its own merge-path search).
+__global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* comp, uint64_t* tmp,
+                                                                    const uint2* __restrict__ ranges, uint32_t* vals,
+                                                                    uint64_t* keys, SegSortWork w,
+                                                                    const DevStatus* st) {
+    __shared__ uint64_t s[kSegCap + kSegCap / 16];
+    __shared__ uint32_t s_idx;
+    if (st->flags & kErrOverflow) return;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(&w.large_ctrl[1], 1u);
+        __syncthreads();
+        const uint32_t idx = s_idx;
+        __syncthreads();
+        if (idx >= w.large_ctrl[0]) return;
+        const uint32_t tile = w.large_list[idx];
+        const uint2 r = ranges[tile];
+        const int n = (int)(r.y - r.x);
+        uint64_t* src = tmp + r.x;
+        uint64_t* dst = comp + r.x;
+        // sorted chunks of 4096 into src
+        for (int c0 = 0; c0 < n; c0 += kSegCap) {
+            const int cn = min(kSegCap, n - c0);
+            for (int i = threadIdx.x; i < kSegCap; i += kSegThreads) s[spad(i)] = i < cn ? comp[r.x + c0 + i] : kKeyInf;
+            __syncthreads();
+            block_merge_sort(s, kSegCap);
+            for (int i = threadIdx.x; i < cn; i += kSegThreads) src[c0 + i] = s[spad(i)];
+            __syncthreads();
+        }
+        // merge passes src -> dst, runs of L doubling
+        for (int L = kSegCap; L < n; L <<= 1) {
+            for (int o = threadIdx.x * kSegItems; o < n; o += kSegThreads * kSegItems) {
+                const int ps = (o / (2 * L)) * 2 * L;
+                const int d = o - ps;
+                const int la = min(L, n - ps);
+                const int lb = max(0, min(L, n - ps - L));
+                const uint64_t* A = src + ps;
+                const uint64_t* B = src + ps + la;
+                int lo = max(0, d - lb), hi = min(d, la);
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (A[mid] <= B[d - 1 - mid])
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                int ai = lo, bj = d - lo;
+                const int outn = min(kSegItems, la + lb - d);
+                for (int q = 0; q < outn; ++q) {
+                    const uint64_t a = ai < la ? A[ai] : kKeyInf;
+                    const uint64_t b = bj < lb ? B[bj] : kKeyInf;
+                    const bool ta = a <= b;
+                    dst[ps + d + q] = ta ? a : b;
+                    ai += ta ? 1 : 0;
+                    bj += ta ? 0 : 1;
+                }
+            }
+            __syncthreads();
+            uint64_t* tsw = src;
+            src = dst;
+            dst = tsw;
+        }
+        for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(src[i], tile, r.x + i, vals, keys);
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_segsort(const uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
+                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid, cudaStream_t s) {
+    if (num_tiles <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(w.large_ctrl, 0, 2 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, keys, w, st);
+    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(const_cast<uint64_t*>(comp), tmp, ranges, vals, keys, w,
+                                                             st);
+    return cudaGetLastError();
+}
+
+}  // namespace fvgs

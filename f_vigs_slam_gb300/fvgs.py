@@ -30,6 +30,7 @@ QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
 DEBUG_PROJECTION = 0x1
 DEBUG_IMAGES = 0x2
 DEBUG_MAPPING = 0x4
+DEBUG_RADIX_SORT = 0x8
 
 KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
                   "map_update", "render"]

@@ -30,6 +30,8 @@ typedef struct fvgs_session fvgs_session;
 #define FVGS_DEBUG_PROJECTION 0x1u /* keep Sigma2D / inverse / visibility per Gaussian */
 #define FVGS_DEBUG_IMAGES 0x2u     /* tracking kernel writes its forward-blend images */
 #define FVGS_DEBUG_MAPPING 0x4u    /* mapping step keeps its 3D deltas */
+#define FVGS_DEBUG_RADIX_SORT 0x8u /* bin with the global LSD radix sort instead of per-tile sorting
+                                      (an independent implementation of the same order, for checking) */
 
 /* Kernel classes for launch accounting and timing. */
 enum {
