@@ -431,7 +431,8 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
         __syncthreads();
         const uint32_t start = s_carry + s_w[w] + incl - c;
         if (t < T) {
-            ranges[t] = make_uint2(start, start + c);
+            // empty tiles keep the (0, 0) of the reference's zeroed range buffer
+            ranges[t] = c ? make_uint2(start, start + c) : make_uint2(0u, 0u);
             fill[t] = start;
         }
         __syncthreads();
