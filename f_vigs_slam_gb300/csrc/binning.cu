@@ -448,17 +448,16 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
 }
 
 // ---------------------------------------------------------------------------
-// Scatter emission: the warp-cooperative walk of emit_keys_kernel, but each
-// instance takes the next slot of its tile (atomic cursor) and stores the
-// composite key depth_bits << 32 | Gaussian index.  The order inside a tile is
-// arbitrary here; the per-tile sort on these unique keys restores the
-// reference's (depth, generation order).
+// Scatter emission.  A warp takes 32 consecutive Gaussians and walks their
+// concatenated tile lists 32 instances at a time (a 5-step shuffle search
+// finds each lane's Gaussian); every instance yields its tile and the
+// composite key depth_bits << 32 | Gaussian index.  The order inside a tile
+// bucket is arbitrary here; the per-tile sort on these unique keys restores
+// the reference's (depth, generation order).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st) {
-    if (st->flags & kErrOverflow) return;
-    const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+template <typename F>
+__device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&& visit) {
     const int lane = threadIdx.x & 31;
-    if (gbase >= a.n) return;
     const int g = gbase + lane;
     const bool valid = g < a.n;
     uint4 b0 = make_uint4(0, 0, 0, 0);
@@ -476,7 +475,6 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
     }
     const uint32_t excl = incl - cnt;
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-    const uint64_t cap = a.capacity;
     for (uint32_t m0 = 0; m0 < total; m0 += 32) {
         const uint32_t m = m0 + lane;
         int lo = 0;
@@ -506,10 +504,53 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
             const float dy = __fsub_rn(tcy, v);
             const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
             const uint32_t tile = (uint32_t)(ty * a.ntx + tx);
-            const uint32_t slot = atomicAdd(&fill[tile], 1u);
-            if (slot < cap) a.keys[slot] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo);
+            visit(tile, ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo));
         }
     }
+}
+
+// Direct scatter: one global atomic per instance on its tile's cursor.
+__global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st) {
+    if (st->flags & kErrOverflow) return;
+    const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+    if (gbase >= a.n) return;
+    const uint64_t cap = a.capacity;
+    walk_instances(a, gbase, [&](uint32_t tile, uint64_t key) {
+        const uint32_t slot = atomicAdd(&fill[tile], 1u);
+        if (slot < cap) a.keys[slot] = key;
+    });
+}
+
+// Privatised scatter: a CTA walks kEmitPerCta Gaussians twice.  The first walk
+// counts its instances per tile in shared memory; then one global atomic per
+// touched tile reserves a contiguous block of that tile's bucket; the second
+// walk ranks instances locally (shared atomics) into their block.
+constexpr int kEmitPerCta = 2048;
+__global__ void __launch_bounds__(256) emit_scatter_cta_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st,
+                                                               int num_tiles) {
+    extern __shared__ uint32_t s_tiles[];  // [num_tiles] counts, then cursors; [num_tiles] block bases
+    uint32_t* s_cnt = s_tiles;
+    uint32_t* s_base = s_tiles + num_tiles;
+    if (st->flags & kErrOverflow) return;
+    for (int t = threadIdx.x; t < num_tiles; t += blockDim.x) s_cnt[t] = 0;
+    __syncthreads();
+    const int g0 = blockIdx.x * kEmitPerCta;
+    const int w = threadIdx.x >> 5;
+    for (int gb = g0 + w * 32; gb < min(a.n, g0 + kEmitPerCta); gb += 8 * 32)
+        walk_instances(a, gb, [&](uint32_t tile, uint64_t) { atomicAdd(&s_cnt[tile], 1u); });
+    __syncthreads();
+    for (int t = threadIdx.x; t < num_tiles; t += blockDim.x) {
+        const uint32_t c = s_cnt[t];
+        if (c) s_base[t] = atomicAdd(&fill[t], c);
+        s_cnt[t] = 0;
+    }
+    __syncthreads();
+    const uint64_t cap = a.capacity;
+    for (int gb = g0 + w * 32; gb < min(a.n, g0 + kEmitPerCta); gb += 8 * 32)
+        walk_instances(a, gb, [&](uint32_t tile, uint64_t key) {
+            const uint32_t slot = s_base[tile] + atomicAdd(&s_cnt[tile], 1u);
+            if (slot < cap) a.keys[slot] = key;
+        });
 }
 
 // ------------------------------- launchers ---------------------------------
@@ -564,7 +605,16 @@ cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint
 
 cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, const DevStatus* st, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
-    emit_scatter_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, fill, st);
+    const int T = a.ntx * ((a.tiles_y > 0) ? a.tiles_y : 1);
+    const size_t smem = sizeof(uint32_t) * 2 * (size_t)T;
+    if (smem <= 200 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(emit_scatter_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+        emit_scatter_cta_kernel<<<(a.n + kEmitPerCta - 1) / kEmitPerCta, 256, smem, s>>>(a, fill, st, T);
+    } else {
+        emit_scatter_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, fill, st);
+    }
     return cudaGetLastError();
 }
 

@@ -348,6 +348,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     ea.offsets = s->offsets;
     ea.n = (int)s->n_g;
     ea.ntx = ntx;
+    ea.tiles_y = nty;
     ea.tw = P.tile_w;
     ea.th = P.tile_h;
     ea.capacity = s->cap_inst;

@@ -42,6 +42,7 @@ struct EmitArgs {
     const uint32_t* offsets;
     int n;
     int ntx, tw, th;
+    int tiles_y;  // tile rows (scatter emission sizes its per-CTA tile table)
     uint64_t capacity;
     uint64_t* keys;
     uint32_t* vals;

@@ -7,8 +7,8 @@
 // unique composite key (depth bits << 32 | Gaussian index).  Instances are
 // therefore scattered into per-tile buckets (any order) and each bucket is
 // sorted on its own:
-//  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 16
-//    keys in registers with a bitonic network, then log2(n/16) merge-path
+//  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 8
+//    keys in registers with a bitonic network, then log2(n/8) merge-path
 //    rounds double the sorted runs;
 //  * larger buckets (rare: huge splats, culled slots piled into tile 0) are
 //    listed by the first kernel and sorted by a second one: chunks of 4096 in
@@ -19,21 +19,21 @@
 
 namespace fvgs {
 
-constexpr int kSegThreads = 256;
-constexpr int kSegItems = 16;
+constexpr int kSegThreads = 512;
+constexpr int kSegItems = 8;
 constexpr int kSegCap = kSegThreads * kSegItems;  // 4096
 constexpr uint64_t kKeyInf = ~0ull;
 
-__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }  // one pad word per 16 keys
+__device__ __forceinline__ int spad(int i) { return i + (i >> 3); }  // one pad word per 8 keys
 
-// Sort 16 keys in registers (bitonic network, ascending).
-__device__ __forceinline__ void sort16(uint64_t (&k)[16]) {
+// Sort kSegItems keys in registers (bitonic network, ascending).
+__device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
 #pragma unroll
-    for (int sz = 2; sz <= 16; sz <<= 1)
+    for (int sz = 2; sz <= kSegItems; sz <<= 1)
 #pragma unroll
         for (int j = sz >> 1; j > 0; j >>= 1)
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int i = 0; i < kSegItems; ++i) {
                 const int l = i ^ j;
                 if (l > i) {
                     const bool up = (i & sz) == 0;
@@ -46,21 +46,22 @@ __device__ __forceinline__ void sort16(uint64_t (&k)[16]) {
             }
 }
 
-// Sort s[0..m) (padded layout, m a power of two in [16, 4096]) in shared
-// memory with the CTA.  Threads >= m/16 only take part in the barriers.
+// Sort s[0..m) (padded layout, m a power of two in [kSegItems, 4096]) in
+// shared memory with the CTA.  Threads >= m/kSegItems only take part in the
+// barriers.
 __device__ void block_merge_sort(uint64_t* s, int m) {
     const int t = threadIdx.x;
     const int active = m / kSegItems;
-    uint64_t k[16];
+    uint64_t k[kSegItems];
     if (t < active) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) k[j] = s[spad(t * 16 + j)];
-        sort16(k);
+        for (int j = 0; j < kSegItems; ++j) k[j] = s[spad(t * kSegItems + j)];
+        sort_items(k);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s[spad(t * 16 + j)] = k[j];
+        for (int j = 0; j < kSegItems; ++j) s[spad(t * kSegItems + j)] = k[j];
     }
     __syncthreads();
-    for (int L = 16; L < m; L <<= 1) {
+    for (int L = kSegItems; L < m; L <<= 1) {
         if (t < active) {
             const int per_pair = (2 * L) / kSegItems;
             const int ps = (t / per_pair) * 2 * L;
@@ -76,7 +77,7 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
             }
             int ai = lo, bj = d - lo;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) {
+            for (int r = 0; r < kSegItems; ++r) {
                 const uint64_t a = ai < L ? A[spad(ps + ai)] : kKeyInf;
                 const uint64_t b = bj < L ? A[spad(ps + L + bj)] : kKeyInf;
                 const bool ta = a <= b;
@@ -91,7 +92,7 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
             const int ps = (t / per_pair) * 2 * L;
             const int d = (t % per_pair) * kSegItems;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) s[spad(ps + d + r)] = k[r];
+            for (int r = 0; r < kSegItems; ++r) s[spad(ps + d + r)] = k[r];
         }
         __syncthreads();
     }
@@ -106,7 +107,7 @@ __device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32
 __global__ void __launch_bounds__(kSegThreads) segsort_kernel(const uint64_t* __restrict__ comp,
                                                               const uint2* __restrict__ ranges, uint32_t* vals,
                                                               uint64_t* keys, SegSortWork w, const DevStatus* st) {
-    __shared__ uint64_t s[kSegCap + kSegCap / 16];
+    __shared__ uint64_t s[kSegCap + kSegCap / 8];
     if (st->flags & kErrOverflow) return;
     const uint32_t tile = blockIdx.x;
     const uint2 r = ranges[tile];
@@ -126,12 +127,12 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(const uint64_t* __
 
 // Large buckets: persistent CTAs take listed tiles; each sorts 4096-key
 // chunks in shared memory into tmp, then merges runs through global memory
-// (every thread merges 16 outputs after its own merge-path search).
+// (every thread merges kSegItems outputs after its own merge-path search).
 __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* comp, uint64_t* tmp,
                                                                     const uint2* __restrict__ ranges, uint32_t* vals,
                                                                     uint64_t* keys, SegSortWork w,
                                                                     const DevStatus* st) {
-    __shared__ uint64_t s[kSegCap + kSegCap / 16];
+    __shared__ uint64_t s[kSegCap + kSegCap / 8];
     __shared__ uint32_t s_idx;
     if (st->flags & kErrOverflow) return;
     for (;;) {
