@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const
 constexpr int kOffThreads = 1024;
 constexpr int kOffSmemCells = 48 * 1024;  // 192 KB of grid staged in shared memory
 __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, int ntx, int nty, uint2* ranges,
-                                                                   uint32_t* fill, DevStatus* st, uint32_t capacity) {
+                                                                   uint32_t* fill, DevStatus* st, uint32_t capacity,
+                                                                   uint32_t* chunk_counter) {
     extern __shared__ int s_grid[];
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
@@ -441,6 +442,7 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
     }
     if (threadIdx.x == 0) {
         const uint32_t total = s_carry;
+        *chunk_counter = 0;  // the scatter that follows takes Gaussian chunks from it
         st->n_instances = total;
         st->n_instances_clamped = total < capacity ? total : capacity;
         if (total > capacity) atomicOr(&st->flags, kErrOverflow);
@@ -509,48 +511,26 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
     }
 }
 
-// Direct scatter: one global atomic per instance on its tile's cursor.
-__global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st) {
+// Scatter with persistent warps: each warp takes chunks of 32 Gaussians from a
+// global counter, so warps whose chunks hold few instances (culled or small
+// Gaussians) simply take more chunks; every instance takes the next slot of
+// its tile with one global atomic.
+__global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, uint32_t* chunk_counter,
+                                                           const DevStatus* st) {
     if (st->flags & kErrOverflow) return;
-    const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
-    if (gbase >= a.n) return;
     const uint64_t cap = a.capacity;
-    walk_instances(a, gbase, [&](uint32_t tile, uint64_t key) {
-        const uint32_t slot = atomicAdd(&fill[tile], 1u);
-        if (slot < cap) a.keys[slot] = key;
-    });
-}
-
-// Privatised scatter: a CTA walks kEmitPerCta Gaussians twice.  The first walk
-// counts its instances per tile in shared memory; then one global atomic per
-// touched tile reserves a contiguous block of that tile's bucket; the second
-// walk ranks instances locally (shared atomics) into their block.
-constexpr int kEmitPerCta = 2048;
-__global__ void __launch_bounds__(256) emit_scatter_cta_kernel(EmitArgs a, uint32_t* fill, const DevStatus* st,
-                                                               int num_tiles) {
-    extern __shared__ uint32_t s_tiles[];  // [num_tiles] counts, then cursors; [num_tiles] block bases
-    uint32_t* s_cnt = s_tiles;
-    uint32_t* s_base = s_tiles + num_tiles;
-    if (st->flags & kErrOverflow) return;
-    for (int t = threadIdx.x; t < num_tiles; t += blockDim.x) s_cnt[t] = 0;
-    __syncthreads();
-    const int g0 = blockIdx.x * kEmitPerCta;
-    const int w = threadIdx.x >> 5;
-    for (int gb = g0 + w * 32; gb < min(a.n, g0 + kEmitPerCta); gb += 8 * 32)
-        walk_instances(a, gb, [&](uint32_t tile, uint64_t) { atomicAdd(&s_cnt[tile], 1u); });
-    __syncthreads();
-    for (int t = threadIdx.x; t < num_tiles; t += blockDim.x) {
-        const uint32_t c = s_cnt[t];
-        if (c) s_base[t] = atomicAdd(&fill[t], c);
-        s_cnt[t] = 0;
-    }
-    __syncthreads();
-    const uint64_t cap = a.capacity;
-    for (int gb = g0 + w * 32; gb < min(a.n, g0 + kEmitPerCta); gb += 8 * 32)
-        walk_instances(a, gb, [&](uint32_t tile, uint64_t key) {
-            const uint32_t slot = s_base[tile] + atomicAdd(&s_cnt[tile], 1u);
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_chunks = (uint32_t)((a.n + 31) / 32);
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+        chunk = __shfl_sync(kFullMask, chunk, 0);
+        if (chunk >= n_chunks) return;
+        walk_instances(a, (int)chunk * 32, [&](uint32_t tile, uint64_t key) {
+            const uint32_t slot = atomicAdd(&fill[tile], 1u);
             if (slot < cap) a.keys[slot] = key;
         });
+    }
 }
 
 // ------------------------------- launchers ---------------------------------
@@ -592,29 +572,22 @@ namespace fvgs {
 size_t tile_diff_words(int ntx, int nty) { return (size_t)(ntx + 1) * (nty + 1); }
 
 cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
-                                uint32_t capacity, cudaStream_t s) {
+                                uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s) {
     // set on every launch: cheap, and correct for whichever device is current
     const cudaError_t e = cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)(sizeof(int) * kOffSmemCells));
     if (e != cudaSuccess) return e;
     const size_t cells = tile_diff_words(ntx, nty);
     const size_t smem = cells <= (size_t)kOffSmemCells ? sizeof(int) * cells : 0;
-    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(diff, ntx, nty, ranges, fill, st, capacity);
+    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(diff, ntx, nty, ranges, fill, st, capacity, chunk_counter);
     return cudaGetLastError();
 }
 
-cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, const DevStatus* st, cudaStream_t s) {
+cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
+                                const DevStatus* st, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
-    const int T = a.ntx * ((a.tiles_y > 0) ? a.tiles_y : 1);
-    const size_t smem = sizeof(uint32_t) * 2 * (size_t)T;
-    if (smem <= 200 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(emit_scatter_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem);
-        if (e != cudaSuccess) return e;
-        emit_scatter_cta_kernel<<<(a.n + kEmitPerCta - 1) / kEmitPerCta, 256, smem, s>>>(a, fill, st, T);
-    } else {
-        emit_scatter_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, fill, st);
-    }
+    const int needed = (a.n + 255) / 256;
+    emit_scatter_kernel<<<grid < needed ? grid : needed, 256, 0, s>>>(a, fill, chunk_counter, st);
     return cudaGetLastError();
 }
 

@@ -348,7 +348,6 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     ea.offsets = s->offsets;
     ea.n = (int)s->n_g;
     ea.ntx = ntx;
-    ea.tiles_y = nty;
     ea.tw = P.tile_w;
     ea.th = P.tile_h;
     ea.capacity = s->cap_inst;
@@ -357,13 +356,14 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         // tile-bucket binning: counts -> ranges -> scatter -> per-tile sort
         {
             KScope k(s, FVGS_K_SCAN, 1);
-            FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, s->ranges, s->tile_fill, s->st, cap32, s->stream));
+            FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, s->ranges, s->tile_fill, s->st, cap32,
+                                      s->seg.large_ctrl + 2, s->stream));
         }
         ea.keys = s->sort.keys_alt;  // composite keys, tile-major
         ea.vals = nullptr;
         {
             KScope k(s, FVGS_K_EMIT, 1);
-            FV_CK(launch_emit_scatter(ea, s->tile_fill, s->st, s->stream));
+            FV_CK(launch_emit_scatter(ea, s->tile_fill, s->seg.large_ctrl + 2, s->num_sms * 8, s->st, s->stream));
         }
         {
             KScope k(s, FVGS_K_SORT, 2);
@@ -673,7 +673,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->tile_diff, s->tile_diff_cells);
     FV_A(s->tile_fill, (size_t)s->cap_tiles);
     FV_A(s->seg.large_list, (size_t)s->cap_tiles);
-    FV_A(s->seg.large_ctrl, 2);
+    FV_A(s->seg.large_ctrl, 4);  // [0..1] large-bucket list control, [2] scatter chunk counter
     FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
     FV_A(s->pose, 1);
     FV_A(s->jj, 48);

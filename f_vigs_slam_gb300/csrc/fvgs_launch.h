@@ -42,7 +42,6 @@ struct EmitArgs {
     const uint32_t* offsets;
     int n;
     int ntx, tw, th;
-    int tiles_y;  // tile rows (scatter emission sizes its per-CTA tile table)
     uint64_t capacity;
     uint64_t* keys;
     uint32_t* vals;
@@ -59,8 +58,9 @@ cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_til
 // ranges / cursors, then scatter of composite keys (depth bits << 32 | index).
 size_t tile_diff_words(int ntx, int nty);
 cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
-                                uint32_t capacity, cudaStream_t s);
-cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, const DevStatus* st, cudaStream_t s);
+                                uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s);
+cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
+                                const DevStatus* st, cudaStream_t s);
 // Per-tile sort of the composite keys (segsort.cu): writes the sorted Gaussian
 // indices to vals and the reference-format keys (tile << 32 | depth bits) to
 // keys.  Tiles above 4096 instances go through a global merge sort that uses

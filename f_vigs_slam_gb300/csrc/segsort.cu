@@ -7,8 +7,8 @@
 // unique composite key (depth bits << 32 | Gaussian index).  Instances are
 // therefore scattered into per-tile buckets (any order) and each bucket is
 // sorted on its own:
-//  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 8
-//    keys in registers with a bitonic network, then log2(n/8) merge-path
+//  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 16
+//    keys in registers with a bitonic network, then log2(n/16) merge-path
 //    rounds double the sorted runs;
 //  * larger buckets (rare: huge splats, culled slots piled into tile 0) are
 //    listed by the first kernel and sorted by a second one: chunks of 4096 in
@@ -19,12 +19,12 @@
 
 namespace fvgs {
 
-constexpr int kSegThreads = 512;
-constexpr int kSegItems = 8;
+constexpr int kSegThreads = 256;
+constexpr int kSegItems = 16;
 constexpr int kSegCap = kSegThreads * kSegItems;  // 4096
 constexpr uint64_t kKeyInf = ~0ull;
 
-__device__ __forceinline__ int spad(int i) { return i + (i >> 3); }  // one pad word per 8 keys
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }  // one pad word per 16 keys
 
 // Sort kSegItems keys in registers (bitonic network, ascending).
 __device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
@@ -107,7 +107,7 @@ __device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32
 __global__ void __launch_bounds__(kSegThreads) segsort_kernel(const uint64_t* __restrict__ comp,
                                                               const uint2* __restrict__ ranges, uint32_t* vals,
                                                               uint64_t* keys, SegSortWork w, const DevStatus* st) {
-    __shared__ uint64_t s[kSegCap + kSegCap / 8];
+    __shared__ uint64_t s[kSegCap + kSegCap / 16];
     if (st->flags & kErrOverflow) return;
     const uint32_t tile = blockIdx.x;
     const uint2 r = ranges[tile];
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* co
                                                                     const uint2* __restrict__ ranges, uint32_t* vals,
                                                                     uint64_t* keys, SegSortWork w,
                                                                     const DevStatus* st) {
-    __shared__ uint64_t s[kSegCap + kSegCap / 8];
+    __shared__ uint64_t s[kSegCap + kSegCap / 16];
     __shared__ uint32_t s_idx;
     if (st->flags & kErrOverflow) return;
     for (;;) {

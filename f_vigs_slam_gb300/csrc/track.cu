@@ -209,7 +209,7 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
 }
 
 template <bool RENDER_ONLY, bool REF_LAYOUT = false>
-__global__ void __launch_bounds__(kPix, 2) track_tile_kernel(TrackArgs a) {
+__global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
     __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
