@@ -143,12 +143,14 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     a.bin1[i] = make_float4(u, v, z, phx);
     a.counts[i] = count;
     if (a.tile_diff && count) {
-        // 2-D difference grid of the tile rectangle: tile counts are its 2-D prefix sums
+        // 2-D difference grid of the tile rectangle (one layer per sub-bucket
+        // i % kSubBuckets): tile counts are its 2-D prefix sums
         const int gw = a.ntx + 1;
-        atomicAdd(&a.tile_diff[y0 * gw + x0], 1);
-        atomicAdd(&a.tile_diff[y0 * gw + x1 + 1], -1);
-        atomicAdd(&a.tile_diff[(y1 + 1) * gw + x0], -1);
-        atomicAdd(&a.tile_diff[(y1 + 1) * gw + x1 + 1], 1);
+        int* d = a.tile_diff + (size_t)(i & (kSubBuckets - 1)) * gw * (a.nty + 1);
+        atomicAdd(&d[y0 * gw + x0], 1);
+        atomicAdd(&d[y0 * gw + x1 + 1], -1);
+        atomicAdd(&d[(y1 + 1) * gw + x0], -1);
+        atomicAdd(&d[(y1 + 1) * gw + x1 + 1], 1);
     }
     if (a.dbg_cov) {
         a.dbg_cov[3 * i] = cxx;
@@ -379,38 +381,42 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
     extern __shared__ int s_grid[];
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
-    const int gw = ntx + 1, gh = nty + 1;
-    const bool staged = gw * gh <= kOffSmemCells;
+    const int gw = ntx + 1, gh = nty + 1, cells = gw * gh;
+    const bool staged = kSubBuckets * cells <= kOffSmemCells;
     int* g = staged ? s_grid : diff;
     if (staged)
-        for (int i = threadIdx.x; i < gw * gh; i += kOffThreads) s_grid[i] = diff[i];
+        for (int i = threadIdx.x; i < kSubBuckets * cells; i += kOffThreads) s_grid[i] = diff[i];
     __syncthreads();
-    // row prefix sums (one thread per grid row), then column prefix sums
-    for (int r = threadIdx.x; r < gh; r += kOffThreads) {
+    // row prefix sums (one thread per layer row), then column prefix sums
+    for (int r = threadIdx.x; r < kSubBuckets * gh; r += kOffThreads) {
+        int* row = g + (size_t)(r / gh) * cells + (r % gh) * gw;
         int acc = 0;
         for (int c = 0; c < gw; ++c) {
-            acc += g[r * gw + c];
-            g[r * gw + c] = acc;
+            acc += row[c];
+            row[c] = acc;
         }
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < gw; c += kOffThreads) {
+    for (int c = threadIdx.x; c < kSubBuckets * gw; c += kOffThreads) {
+        int* col = g + (size_t)(c / gw) * cells + (c % gw);
         int acc = 0;
         for (int r = 0; r < gh; ++r) {
-            acc += g[r * gw + c];
-            g[r * gw + c] = acc;
+            acc += col[r * gw];
+            col[r * gw] = acc;
         }
     }
     __syncthreads();
-    // exclusive scan of tile counts in row-major tile order
-    const int T = ntx * nty;
+    // exclusive scan over (tile, sub-bucket) in tile-major order: entry
+    // e = t * kSubBuckets + j; a tile's sub-buckets are adjacent lanes
+    const int E = ntx * nty * kSubBuckets;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
-    for (int base = 0; base < T; base += kOffThreads) {
-        const int t = base + threadIdx.x;
+    for (int base = 0; base < E; base += kOffThreads) {
+        const int e = base + threadIdx.x;
+        const int t = e / kSubBuckets, j = e % kSubBuckets;
         uint32_t c = 0;
-        if (t < T) c = (uint32_t)g[(t / ntx) * gw + (t % ntx)];
+        if (e < E) c = (uint32_t)g[(size_t)j * cells + (t / ntx) * gw + (t % ntx)];
         uint32_t incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -431,10 +437,14 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
         }
         __syncthreads();
         const uint32_t start = s_carry + s_w[w] + incl - c;
-        if (t < T) {
+        // tile total over its kSubBuckets adjacent lanes
+        uint32_t ct = c;
+#pragma unroll
+        for (int o = 1; o < kSubBuckets; o <<= 1) ct += __shfl_xor_sync(kFullMask, ct, o);
+        if (e < E) {
+            fill[e] = start;
             // empty tiles keep the (0, 0) of the reference's zeroed range buffer
-            ranges[t] = c ? make_uint2(start, start + c) : make_uint2(0u, 0u);
-            fill[t] = start;
+            if (j == 0) ranges[t] = ct ? make_uint2(start, start + ct) : make_uint2(0u, 0u);
         }
         __syncthreads();
         if (threadIdx.x == kOffThreads - 1) s_carry = start + c;
@@ -527,7 +537,9 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
         chunk = __shfl_sync(kFullMask, chunk, 0);
         if (chunk >= n_chunks) return;
         walk_instances(a, (int)chunk * 32, [&](uint32_t tile, uint64_t key) {
-            const uint32_t slot = atomicAdd(&fill[tile], 1u);
+            // sub-bucket by Gaussian index: spreads the cursor atomics of one
+            // tile over kSubBuckets addresses
+            const uint32_t slot = atomicAdd(&fill[tile * kSubBuckets + ((uint32_t)key & (kSubBuckets - 1))], 1u);
             if (slot < cap) a.keys[slot] = key;
         });
     }
@@ -569,7 +581,7 @@ cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_til
 
 namespace fvgs {
 
-size_t tile_diff_words(int ntx, int nty) { return (size_t)(ntx + 1) * (nty + 1); }
+size_t tile_diff_words(int ntx, int nty) { return (size_t)kSubBuckets * (ntx + 1) * (nty + 1); }
 
 cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
                                 uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s) {

@@ -671,7 +671,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->ranges, (size_t)s->cap_tiles);
     s->tile_diff_cells = tile_diff_words(ntx, nty);
     FV_A(s->tile_diff, s->tile_diff_cells);
-    FV_A(s->tile_fill, (size_t)s->cap_tiles);
+    FV_A(s->tile_fill, (size_t)s->cap_tiles * kSubBuckets);
     FV_A(s->seg.large_list, (size_t)s->cap_tiles);
     FV_A(s->seg.large_ctrl, 4);  // [0..1] large-bucket list control, [2] scatter chunk counter
     FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);

@@ -69,6 +69,10 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Tile buckets are split into this many sub-buckets (by Gaussian index), each
+// with its own scatter cursor, to spread same-address atomics.
+constexpr int kSubBuckets = 8;
+
 // Bounded spin budget for device-side waits; on expiry a kernel records
 // kErrTimeout and carries on with a safe value instead of hanging.
 constexpr uint32_t kSpinLimit = 1u << 24;

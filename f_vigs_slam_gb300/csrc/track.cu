@@ -240,19 +240,13 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
             if (__syncthreads_and(done)) break;
             const int cnt = stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
-                for (int j = 0; j < cnt; ++j) {
-                    const float4 rA = sb.A[j];
+                // one staged Gaussian: returns false when the pixel terminates
+                auto blend = [&](int j, float dx, float dy, float v) -> bool {
                     const float4 rB = sb.B[j];
-                    const float dx = rA.x - xf, dy = rA.y - yf;
-                    const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
-                    if (v > rB.y || v <= 0.0f) continue;
                     const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
-                    if (alpha < kInv255) continue;
+                    if (alpha < kInv255) return true;
                     const float test_T = T * (1.0f - alpha);
-                    if (test_T < 0.0001f) {
-                        done = true;
-                        break;
-                    }
+                    if (test_T < 0.0001f) return false;
                     const float4 rC = sb.C[j];
                     cr += rC.z * alpha * T;
                     cg += rC.w * alpha * T;
@@ -260,6 +254,36 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
                     if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, dx, rC.x, dy, rC.y);
                     T = test_T;
                     last = (uint32_t)sb.orig[j] + 1u;
+                    return true;
+                };
+                int j = 0;
+                // two Gaussians per iteration: both quadratic forms are evaluated
+                // before the (mostly rejecting) branches, in list order
+                for (; j + 1 < cnt; j += 2) {
+                    const float4 rA0 = sb.A[j], rA1 = sb.A[j + 1];
+                    const float2 rB0 = *reinterpret_cast<const float2*>(&sb.B[j]);
+                    const float2 rB1 = *reinterpret_cast<const float2*>(&sb.B[j + 1]);
+                    const float dx0 = rA0.x - xf, dy0 = rA0.y - yf;
+                    const float dx1 = rA1.x - xf, dy1 = rA1.y - yf;
+                    const float v0 = rA0.z * dx0 * dx0 + 2.0f * rA0.w * dx0 * dy0 + rB0.x * dy0 * dy0;
+                    const float v1 = rA1.z * dx1 * dx1 + 2.0f * rA1.w * dx1 * dy1 + rB1.x * dy1 * dy1;
+                    const bool k0 = !(v0 > rB0.y || v0 <= 0.0f);
+                    const bool k1 = !(v1 > rB1.y || v1 <= 0.0f);
+                    if (k0 && !blend(j, dx0, dy0, v0)) {
+                        done = true;
+                        break;
+                    }
+                    if (k1 && !blend(j + 1, dx1, dy1, v1)) {
+                        done = true;
+                        break;
+                    }
+                }
+                if (!done && j < cnt) {
+                    const float4 rA = sb.A[j];
+                    const float2 rB = *reinterpret_cast<const float2*>(&sb.B[j]);
+                    const float dx = rA.x - xf, dy = rA.y - yf;
+                    const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
+                    if (!(v > rB.y || v <= 0.0f) && !blend(j, dx, dy, v)) done = true;
                 }
             }
         }
