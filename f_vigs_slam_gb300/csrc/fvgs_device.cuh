@@ -69,9 +69,11 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-// Tile buckets are split into this many sub-buckets (by Gaussian index), each
-// with its own scatter cursor, to spread same-address atomics.
-constexpr int kSubBuckets = 8;
+// Tile buckets can be split into sub-buckets (by Gaussian index), each with
+// its own scatter cursor, to spread same-address atomics.  Measured on GB300
+// the cursor atomics are not contention-bound and 8 sub-buckets made binning
+// slower, so the split is off (1).
+constexpr int kSubBuckets = 1;
 
 // Bounded spin budget for device-side waits; on expiry a kernel records
 // kErrTimeout and carries on with a safe value instead of hanging.
