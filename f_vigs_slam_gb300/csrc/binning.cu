@@ -487,27 +487,35 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
     }
     const uint32_t excl = incl - cnt;
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-    for (uint32_t m0 = 0; m0 < total; m0 += 32) {
-        const uint32_t m = m0 + lane;
-        int lo = 0;
+    // kWalkBatch instances per lane per round, handed to visit together so
+    // their memory operations can all be in flight at once
+    constexpr int kWalkBatch = 4;
+    for (uint32_t m0 = 0; m0 < total; m0 += 32 * kWalkBatch) {
+        uint32_t tiles[kWalkBatch];
+        uint64_t keys[kWalkBatch];
+        bool ok[kWalkBatch];
 #pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const uint32_t e = __shfl_sync(kFullMask, excl, lo + step);
-            if (e <= m) lo += step;
-        }
-        const uint32_t r0 = __shfl_sync(kFullMask, b0.x, lo);
-        const uint32_t r1 = __shfl_sync(kFullMask, b0.y, lo);
-        const uint32_t phy_bits = __shfl_sync(kFullMask, b0.w, lo);
-        const float u = __shfl_sync(kFullMask, b1.x, lo);
-        const float v = __shfl_sync(kFullMask, b1.y, lo);
-        const float z = __shfl_sync(kFullMask, b1.z, lo);
-        const float phx = __shfl_sync(kFullMask, b1.w, lo);
-        const uint32_t e_lo = __shfl_sync(kFullMask, excl, lo);
-        if (m < total) {
+        for (int q = 0; q < kWalkBatch; ++q) {
+            const uint32_t m = m0 + 32 * q + lane;
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const uint32_t e = __shfl_sync(kFullMask, excl, lo + step);
+                if (e <= m) lo += step;
+            }
+            const uint32_t r0 = __shfl_sync(kFullMask, b0.x, lo);
+            const uint32_t r1 = __shfl_sync(kFullMask, b0.y, lo);
+            const uint32_t phy_bits = __shfl_sync(kFullMask, b0.w, lo);
+            const float u = __shfl_sync(kFullMask, b1.x, lo);
+            const float v = __shfl_sync(kFullMask, b1.y, lo);
+            const float z = __shfl_sync(kFullMask, b1.z, lo);
+            const float phx = __shfl_sync(kFullMask, b1.w, lo);
+            const uint32_t e_lo = __shfl_sync(kFullMask, excl, lo);
+            ok[q] = m < total;
             const uint32_t local = m - e_lo;
             const int x0 = (int)(r0 & 0xffffu), y0 = (int)(r0 >> 16);
             const int x1 = (int)(r1 & 0xffffu);
-            const int w = x1 - x0 + 1;
+            const int w = max(1, x1 - x0 + 1);
             const int tx = x0 + (int)(local % (uint32_t)w);
             const int ty = y0 + (int)(local / (uint32_t)w);
             const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)a.tw);
@@ -515,9 +523,10 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
             const float dx = __fsub_rn(tcx, u);
             const float dy = __fsub_rn(tcy, v);
             const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
-            const uint32_t tile = (uint32_t)(ty * a.ntx + tx);
-            visit(tile, ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo));
+            tiles[q] = (uint32_t)(ty * a.ntx + tx);
+            keys[q] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo);
         }
+        visit(tiles, keys, ok);
     }
 }
 
@@ -536,11 +545,14 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
         if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
         chunk = __shfl_sync(kFullMask, chunk, 0);
         if (chunk >= n_chunks) return;
-        walk_instances(a, (int)chunk * 32, [&](uint32_t tile, uint64_t key) {
-            // sub-bucket by Gaussian index: spreads the cursor atomics of one
-            // tile over kSubBuckets addresses
-            const uint32_t slot = atomicAdd(&fill[tile * kSubBuckets + ((uint32_t)key & (kSubBuckets - 1))], 1u);
-            if (slot < cap) a.keys[slot] = key;
+        walk_instances(a, (int)chunk * 32, [&](const uint32_t* tiles, const uint64_t* keys, const bool* ok) {
+            uint32_t slot[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (ok[q]) slot[q] = atomicAdd(&fill[tiles[q] * kSubBuckets + ((uint32_t)keys[q] & (kSubBuckets - 1))], 1u);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (ok[q] && slot[q] < cap) a.keys[slot[q]] = keys[q];
         });
     }
 }

@@ -46,9 +46,38 @@ __device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
             }
 }
 
+// One merge-path round: thread t produces outputs [16t, 16t+16) of the merged
+// pair of sorted runs of length L that contains them.  Both run heads are
+// re-read from shared memory each step (keeping them in registers and loading
+// one key per step measured slower: more registers, fewer resident CTAs).
+__device__ __forceinline__ void merge_round(const uint64_t* s, int t, int L, uint64_t (&k)[kSegItems]) {
+    const int per_pair = (2 * L) / kSegItems;
+    const int ps = (t / per_pair) * 2 * L;
+    const int d = (t % per_pair) * kSegItems;
+    int lo = max(0, d - L), hi = min(d, L);
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s[spad(ps + mid)] <= s[spad(ps + L + d - 1 - mid)])
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    int ai = lo, bj = d - lo;
+#pragma unroll
+    for (int r = 0; r < kSegItems; ++r) {
+        const uint64_t a = ai < L ? s[spad(ps + ai)] : kKeyInf;
+        const uint64_t b = bj < L ? s[spad(ps + L + bj)] : kKeyInf;
+        const bool ta = a <= b;
+        k[r] = ta ? a : b;
+        ai += ta ? 1 : 0;
+        bj += ta ? 0 : 1;
+    }
+}
+
 // Sort s[0..m) (padded layout, m a power of two in [kSegItems, 4096]) in
 // shared memory with the CTA.  Threads >= m/kSegItems only take part in the
-// barriers.
+// barriers.  While a merged pair spans at most one warp's 512 keys the round
+// touches only that warp's slice, so it synchronises the warp, not the CTA.
 __device__ void block_merge_sort(uint64_t* s, int m) {
     const int t = threadIdx.x;
     const int active = m / kSegItems;
@@ -60,42 +89,25 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
 #pragma unroll
         for (int j = 0; j < kSegItems; ++j) s[spad(t * kSegItems + j)] = k[j];
     }
-    __syncthreads();
+    __syncwarp();
+    constexpr int kWarpSpan = 32 * kSegItems;
     for (int L = kSegItems; L < m; L <<= 1) {
+        const bool warp_local = 2 * L <= kWarpSpan;
+        if (t < active) merge_round(s, t, L, k);
+        if (warp_local)
+            __syncwarp();
+        else
+            __syncthreads();
         if (t < active) {
-            const int per_pair = (2 * L) / kSegItems;
-            const int ps = (t / per_pair) * 2 * L;
-            const int d = (t % per_pair) * kSegItems;
-            const uint64_t* A = s;  // run A at [ps, ps+L), run B at [ps+L, ps+2L)
-            int lo = max(0, d - L), hi = min(d, L);
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (A[spad(ps + mid)] <= A[spad(ps + L + d - 1 - mid)])
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            int ai = lo, bj = d - lo;
 #pragma unroll
-            for (int r = 0; r < kSegItems; ++r) {
-                const uint64_t a = ai < L ? A[spad(ps + ai)] : kKeyInf;
-                const uint64_t b = bj < L ? A[spad(ps + L + bj)] : kKeyInf;
-                const bool ta = a <= b;
-                k[r] = ta ? a : b;
-                ai += ta ? 1 : 0;
-                bj += ta ? 0 : 1;
-            }
+            for (int r = 0; r < kSegItems; ++r) s[spad(t * kSegItems + r)] = k[r];
         }
-        __syncthreads();
-        if (t < active) {
-            const int per_pair = (2 * L) / kSegItems;
-            const int ps = (t / per_pair) * 2 * L;
-            const int d = (t % per_pair) * kSegItems;
-#pragma unroll
-            for (int r = 0; r < kSegItems; ++r) s[spad(ps + d + r)] = k[r];
-        }
-        __syncthreads();
+        if (4 * L <= kWarpSpan)
+            __syncwarp();
+        else
+            __syncthreads();
     }
+    __syncthreads();
 }
 
 __device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32_t dst, uint32_t* vals,
