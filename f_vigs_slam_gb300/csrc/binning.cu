@@ -22,6 +22,15 @@
 
 namespace fvgs {
 
+// Add the inclusive tile rectangle [x0..x1] x [y0..y1] to a 2-D difference
+// grid of row pitch gw = ntx + 1; tile counts are the grid's 2-D prefix sums.
+__device__ __forceinline__ void add_rect(int* d, int gw, int x0, int y0, int x1, int y1) {
+    atomicAdd(&d[y0 * gw + x0], 1);
+    atomicAdd(&d[y0 * gw + x1 + 1], -1);
+    atomicAdd(&d[(y1 + 1) * gw + x0], -1);
+    atomicAdd(&d[(y1 + 1) * gw + x1 + 1], 1);
+}
+
 __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -142,15 +151,50 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
                            __float_as_uint(phy));
     a.bin1[i] = make_float4(u, v, z, phx);
     a.counts[i] = count;
-    if (a.tile_diff && count) {
-        // 2-D difference grid of the tile rectangle (one layer per sub-bucket
-        // i % kSubBuckets): tile counts are its 2-D prefix sums
+    if (a.tile_diff) {
         const int gw = a.ntx + 1;
-        int* d = a.tile_diff + (size_t)(i & (kSubBuckets - 1)) * gw * (a.nty + 1);
-        atomicAdd(&d[y0 * gw + x0], 1);
-        atomicAdd(&d[y0 * gw + x1 + 1], -1);
-        atomicAdd(&d[(y1 + 1) * gw + x0], -1);
-        atomicAdd(&d[(y1 + 1) * gw + x1 + 1], 1);
+        const size_t cells = (size_t)gw * (a.nty + 1);
+        if (count) add_rect(a.tile_diff, gw, x0, y0, x1, y1);
+        if (a.bin0_prev) {
+            // instances entering a tile: the new rectangle minus the previous
+            // one (at most four rectangles around their intersection)
+            uint32_t n_enter = 0;
+            if (count) {
+                int* e = a.tile_diff + cells;
+                const uint4 pb = a.bin0_prev[i];
+                const int px0 = (int)(pb.x & 0xffffu), py0 = (int)(pb.x >> 16);
+                const int px1 = (int)(pb.y & 0xffffu), py1 = (int)(pb.y >> 16);
+                const int ix0 = max(x0, px0), ix1 = min(x1, px1), iy0 = max(y0, py0), iy1 = min(y1, py1);
+                if (pb.z == 0u || ix0 > ix1 || iy0 > iy1) {
+                    add_rect(e, gw, x0, y0, x1, y1);
+                    n_enter = count;
+                } else {
+                    if (iy0 > y0) add_rect(e, gw, x0, y0, x1, iy0 - 1);
+                    if (iy1 < y1) add_rect(e, gw, x0, iy1 + 1, x1, y1);
+                    if (ix0 > x0) add_rect(e, gw, x0, iy0, ix0 - 1, iy1);
+                    if (ix1 < x1) add_rect(e, gw, ix1 + 1, iy0, x1, iy1);
+                    n_enter = count - (uint32_t)((ix1 - ix0 + 1) * (iy1 - iy0 + 1));
+                }
+            }
+            // warp-aggregated: entering total and the list of changed Gaussians
+            uint32_t* ctr = reinterpret_cast<uint32_t*>(a.tile_diff + 2 * cells);
+            const unsigned act = __activemask();
+            const unsigned want = __ballot_sync(act, n_enter != 0u);
+            if (want) {
+                const int leader = __ffs(want) - 1;
+                const uint32_t sum = __reduce_add_sync(act, n_enter);
+                uint32_t base = 0;
+                if ((int)(threadIdx.x & 31) == leader) {
+                    atomicAdd(&ctr[0], sum);
+                    base = atomicAdd(&ctr[1], (uint32_t)__popc(want));
+                }
+                base = __shfl_sync(act, base, leader);
+                if (n_enter) {
+                    const uint32_t idx = base + (uint32_t)__popc(want & lanemask_lt());
+                    if (idx < a.changed_cap) a.changed[idx] = (uint32_t)i;
+                }
+            }
+        }
     }
     if (a.dbg_cov) {
         a.dbg_cov[3 * i] = cxx;
@@ -368,27 +412,42 @@ __global__ void __launch_bounds__(256) ranges_kernel(const uint64_t* keys, const
 }
 
 // ---------------------------------------------------------------------------
-// Tile offsets from the difference grid (one CTA): 2-D prefix sums give the
+// Tile offsets from the difference grids (one CTA): 2-D prefix sums give the
 // instance count of every tile; an exclusive scan in row-major tile order gives
 // each tile's [start, end) in the tile-major instance array -- these are the
-// per-tile ranges, and the starts seed the scatter cursors.
+// per-tile ranges, and the starts seed the scatter cursors.  With a valid
+// previous binning the entering grid is scanned the same way (into a compact
+// array of entering instances) and the binning mode is chosen.
 // ---------------------------------------------------------------------------
 constexpr int kOffThreads = 1024;
 constexpr int kOffSmemCells = 48 * 1024;  // 192 KB of grid staged in shared memory
-__global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, int ntx, int nty, uint2* ranges,
-                                                                   uint32_t* fill, DevStatus* st, uint32_t capacity,
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFullMask, v, o);
+        if (lane >= o) v += y;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* scratch, int ntx, int nty, int hist,
+                                                                   uint32_t enter_cap, uint2* ranges, uint32_t* fill,
+                                                                   uint2* enter_ranges, uint32_t* enter_fill,
+                                                                   DevStatus* st, uint32_t capacity,
                                                                    uint32_t* chunk_counter) {
     extern __shared__ int s_grid[];
-    __shared__ uint32_t s_w[32];
-    __shared__ uint32_t s_carry;
+    __shared__ uint32_t s_w[2][32];
+    __shared__ uint32_t s_carry[2];
     const int gw = ntx + 1, gh = nty + 1, cells = gw * gh;
-    const bool staged = kSubBuckets * cells <= kOffSmemCells;
-    int* g = staged ? s_grid : diff;
+    const int ng = hist ? 2 : 1;
+    const bool staged = ng * cells <= kOffSmemCells;
+    int* g = staged ? s_grid : scratch;
     if (staged)
-        for (int i = threadIdx.x; i < kSubBuckets * cells; i += kOffThreads) s_grid[i] = diff[i];
+        for (int i = threadIdx.x; i < ng * cells; i += kOffThreads) s_grid[i] = scratch[i];
     __syncthreads();
-    // row prefix sums (one thread per layer row), then column prefix sums
-    for (int r = threadIdx.x; r < kSubBuckets * gh; r += kOffThreads) {
+    // row prefix sums (one thread per grid row), then column prefix sums
+    for (int r = threadIdx.x; r < ng * gh; r += kOffThreads) {
         int* row = g + (size_t)(r / gh) * cells + (r % gh) * gw;
         int acc = 0;
         for (int c = 0; c < gw; ++c) {
@@ -397,7 +456,7 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
         }
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < kSubBuckets * gw; c += kOffThreads) {
+    for (int c = threadIdx.x; c < ng * gw; c += kOffThreads) {
         int* col = g + (size_t)(c / gw) * cells + (c % gw);
         int acc = 0;
         for (int r = 0; r < gh; ++r) {
@@ -406,77 +465,92 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* diff, in
         }
     }
     __syncthreads();
-    // exclusive scan over (tile, sub-bucket) in tile-major order: entry
-    // e = t * kSubBuckets + j; a tile's sub-buckets are adjacent lanes
-    const int E = ntx * nty * kSubBuckets;
+    // exclusive scans of both grids over tiles in row-major order
+    const int T = ntx * nty;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_carry = 0;
+    if (threadIdx.x < 2) s_carry[threadIdx.x] = 0;
     __syncthreads();
-    for (int base = 0; base < E; base += kOffThreads) {
-        const int e = base + threadIdx.x;
-        const int t = e / kSubBuckets, j = e % kSubBuckets;
-        uint32_t c = 0;
-        if (e < E) c = (uint32_t)g[(size_t)j * cells + (t / ntx) * gw + (t % ntx)];
-        uint32_t incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) s_w[w] = incl;
-        __syncthreads();
-        if (w == 0) {
-            const uint32_t v = s_w[lane];
-            uint32_t vi = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(kFullMask, vi, o);
-                if (lane >= o) vi += y;
-            }
-            s_w[lane] = vi - v;
+    for (int base = 0; base < T; base += kOffThreads) {
+        const int t = base + threadIdx.x;
+        const int cell = (t / ntx) * gw + (t % ntx);
+        const uint32_t c0 = t < T ? (uint32_t)g[cell] : 0u;
+        const uint32_t c1 = (hist && t < T) ? (uint32_t)g[cells + cell] : 0u;
+        const uint32_t i0 = warp_incl_scan(c0, lane);
+        const uint32_t i1 = warp_incl_scan(c1, lane);
+        if (lane == 31) {
+            s_w[0][w] = i0;
+            s_w[1][w] = i1;
         }
         __syncthreads();
-        const uint32_t start = s_carry + s_w[w] + incl - c;
-        // tile total over its kSubBuckets adjacent lanes
-        uint32_t ct = c;
-#pragma unroll
-        for (int o = 1; o < kSubBuckets; o <<= 1) ct += __shfl_xor_sync(kFullMask, ct, o);
-        if (e < E) {
-            fill[e] = start;
+        if (w < 2) {
+            const uint32_t v = s_w[w][lane];
+            s_w[w][lane] = warp_incl_scan(v, lane) - v;
+        }
+        __syncthreads();
+        const uint32_t start0 = s_carry[0] + s_w[0][w] + i0 - c0;
+        const uint32_t start1 = s_carry[1] + s_w[1][w] + i1 - c1;
+        if (t < T) {
+            fill[t] = start0;
             // empty tiles keep the (0, 0) of the reference's zeroed range buffer
-            if (j == 0) ranges[t] = ct ? make_uint2(start, start + ct) : make_uint2(0u, 0u);
+            ranges[t] = c0 ? make_uint2(start0, start0 + c0) : make_uint2(0u, 0u);
+            if (hist) {
+                enter_fill[t] = start1;
+                enter_ranges[t] = make_uint2(start1, start1 + c1);
+            }
         }
         __syncthreads();
-        if (threadIdx.x == kOffThreads - 1) s_carry = start + c;
+        if (threadIdx.x == kOffThreads - 1) {
+            s_carry[0] = start0 + c0;
+            s_carry[1] = start1 + c1;
+        }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        const uint32_t total = s_carry;
+        const uint32_t total = s_carry[0];
         *chunk_counter = 0;  // the scatter that follows takes Gaussian chunks from it
         st->n_instances = total;
         st->n_instances_clamped = total < capacity ? total : capacity;
         if (total > capacity) atomicOr(&st->flags, kErrOverflow);
+        const uint32_t* ctr = reinterpret_cast<const uint32_t*>(scratch + 2 * (size_t)cells);
+        const uint32_t n_enter = hist ? ctr[0] : total;
+        const uint32_t n_changed = hist ? ctr[1] : 0u;
+        const bool incr = hist && n_enter == s_carry[1] && n_enter <= enter_cap && n_changed <= enter_cap;
+        st->mode = incr ? kBinIncremental : kBinFull;
+        st->n_enter = n_enter;
+        st->n_changed = n_changed;
     }
 }
 
 // ---------------------------------------------------------------------------
-// Scatter emission.  A warp takes 32 consecutive Gaussians and walks their
-// concatenated tile lists 32 instances at a time (a 5-step shuffle search
-// finds each lane's Gaussian); every instance yields its tile and the
-// composite key depth_bits << 32 | Gaussian index.  The order inside a tile
-// bucket is arbitrary here; the per-tile sort on these unique keys restores
-// the reference's (depth, generation order).
+// Scatter emission.  A warp takes 32 Gaussians and walks their concatenated
+// tile lists 32 instances per lane-round (a 5-step shuffle search finds each
+// lane's Gaussian); every instance yields its tile and the composite key
+// depth_bits << 32 | Gaussian index.  The order inside a tile bucket is
+// arbitrary here; the per-tile sort on these unique keys restores the
+// reference's (depth, generation order).
+// Full mode walks Gaussians chunk * 32 + lane and emits every instance.
+// Incremental mode walks the listed (changed) Gaussians and emits only the
+// tiles outside their previous rectangle.
 // ---------------------------------------------------------------------------
-template <typename F>
-__device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&& visit) {
+constexpr int kWalkBatch = 4;  // instances per lane per round, memory ops in flight together
+
+template <bool INCR, typename F>
+__device__ __forceinline__ void walk_instances(const EmitArgs& a, uint32_t first, uint32_t n_items, F&& visit) {
     const int lane = threadIdx.x & 31;
-    const int g = gbase + lane;
-    const bool valid = g < a.n;
+    const uint32_t item = first + (uint32_t)lane;
+    const bool valid = item < n_items;
+    uint32_t g = 0;
     uint4 b0 = make_uint4(0, 0, 0, 0);
     float4 b1 = make_float4(0, 0, 0, 0);
+    uint2 prev = make_uint2(1u, 0u);  // previous rectangle (incremental), empty by default
     if (valid) {
+        g = INCR ? a.changed[item] : item;
         b0 = a.bin0[g];
         b1 = a.bin1[g];
+        if (INCR) {
+            const uint4 p = a.bin0_prev[g];
+            if (p.z) prev = make_uint2(p.x, p.y);
+        }
     }
     const uint32_t cnt = valid ? b0.z : 0u;
     uint32_t incl = cnt;
@@ -487,9 +561,6 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
     }
     const uint32_t excl = incl - cnt;
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-    // kWalkBatch instances per lane per round, handed to visit together so
-    // their memory operations can all be in flight at once
-    constexpr int kWalkBatch = 4;
     for (uint32_t m0 = 0; m0 < total; m0 += 32 * kWalkBatch) {
         uint32_t tiles[kWalkBatch];
         uint64_t keys[kWalkBatch];
@@ -511,22 +582,49 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
             const float z = __shfl_sync(kFullMask, b1.z, lo);
             const float phx = __shfl_sync(kFullMask, b1.w, lo);
             const uint32_t e_lo = __shfl_sync(kFullMask, excl, lo);
-            ok[q] = m < total;
+            const uint32_t g_lo = __shfl_sync(kFullMask, g, lo);
             const uint32_t local = m - e_lo;
             const int x0 = (int)(r0 & 0xffffu), y0 = (int)(r0 >> 16);
             const int x1 = (int)(r1 & 0xffffu);
             const int w = max(1, x1 - x0 + 1);
             const int tx = x0 + (int)(local % (uint32_t)w);
             const int ty = y0 + (int)(local / (uint32_t)w);
-            const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)a.tw);
-            const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)a.th);
-            const float dx = __fsub_rn(tcx, u);
-            const float dy = __fsub_rn(tcy, v);
-            const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+            bool emit = m < total;
+            if (INCR) {
+                const uint32_t p0 = __shfl_sync(kFullMask, prev.x, lo);
+                const uint32_t p1 = __shfl_sync(kFullMask, prev.y, lo);
+                const bool inside_prev = tx >= (int)(p0 & 0xffffu) && tx <= (int)(p1 & 0xffffu) &&
+                                         ty >= (int)(p0 >> 16) && ty <= (int)(p1 >> 16);
+                emit = emit && !inside_prev;
+            }
+            ok[q] = emit;
+            const float d = tile_depth(tx, ty, a.tw, a.th, u, v, z, phx, phy_bits);
             tiles[q] = (uint32_t)(ty * a.ntx + tx);
-            keys[q] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)(uint32_t)(gbase + lo);
+            keys[q] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)g_lo;
         }
         visit(tiles, keys, ok);
+    }
+}
+
+template <bool INCR>
+__device__ __forceinline__ void scatter_chunks(const EmitArgs& a, uint32_t* fill, uint64_t* out, uint64_t cap,
+                                               uint32_t n_items, uint32_t* chunk_counter) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_chunks = (n_items + 31) / 32;
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+        chunk = __shfl_sync(kFullMask, chunk, 0);
+        if (chunk >= n_chunks) return;
+        walk_instances<INCR>(a, chunk * 32, n_items, [&](const uint32_t* tiles, const uint64_t* keys, const bool* ok) {
+            uint32_t slot[kWalkBatch];
+#pragma unroll
+            for (int q = 0; q < kWalkBatch; ++q)
+                if (ok[q]) slot[q] = atomicAdd(&fill[tiles[q]], 1u);
+#pragma unroll
+            for (int q = 0; q < kWalkBatch; ++q)
+                if (ok[q] && slot[q] < cap) out[slot[q]] = keys[q];
+        });
     }
 }
 
@@ -537,24 +635,10 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, int gbase, F&&
 __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, uint32_t* chunk_counter,
                                                            const DevStatus* st) {
     if (st->flags & kErrOverflow) return;
-    const uint64_t cap = a.capacity;
-    const int lane = threadIdx.x & 31;
-    const uint32_t n_chunks = (uint32_t)((a.n + 31) / 32);
-    for (;;) {
-        uint32_t chunk = 0;
-        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
-        chunk = __shfl_sync(kFullMask, chunk, 0);
-        if (chunk >= n_chunks) return;
-        walk_instances(a, (int)chunk * 32, [&](const uint32_t* tiles, const uint64_t* keys, const bool* ok) {
-            uint32_t slot[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (ok[q]) slot[q] = atomicAdd(&fill[tiles[q] * kSubBuckets + ((uint32_t)keys[q] & (kSubBuckets - 1))], 1u);
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (ok[q] && slot[q] < cap) a.keys[slot[q]] = keys[q];
-        });
-    }
+    if (st->mode == kBinIncremental)
+        scatter_chunks<true>(a, a.enter_fill, a.enter_keys, a.enter_cap, a.counters[1], chunk_counter);
+    else
+        scatter_chunks<false>(a, fill, a.keys, a.capacity, (uint32_t)a.n, chunk_counter);
 }
 
 // ------------------------------- launchers ---------------------------------
@@ -593,17 +677,20 @@ cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_til
 
 namespace fvgs {
 
-size_t tile_diff_words(int ntx, int nty) { return (size_t)kSubBuckets * (ntx + 1) * (nty + 1); }
+size_t diff_grid_cells(int ntx, int nty) { return (size_t)(ntx + 1) * (nty + 1); }
+size_t tile_diff_words(int ntx, int nty) { return 2 * diff_grid_cells(ntx, nty) + kCounterWords; }
 
-cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
+cudaError_t launch_tile_offsets(int* scratch, int ntx, int nty, bool hist, uint32_t enter_cap, uint2* ranges,
+                                uint32_t* fill, uint2* enter_ranges, uint32_t* enter_fill, DevStatus* st,
                                 uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s) {
     // set on every launch: cheap, and correct for whichever device is current
     const cudaError_t e = cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)(sizeof(int) * kOffSmemCells));
     if (e != cudaSuccess) return e;
-    const size_t cells = tile_diff_words(ntx, nty);
+    const size_t cells = (hist ? 2 : 1) * diff_grid_cells(ntx, nty);
     const size_t smem = cells <= (size_t)kOffSmemCells ? sizeof(int) * cells : 0;
-    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(diff, ntx, nty, ranges, fill, st, capacity, chunk_counter);
+    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(scratch, ntx, nty, hist ? 1 : 0, enter_cap, ranges, fill,
+                                                     enter_ranges, enter_fill, st, capacity, chunk_counter);
     return cudaGetLastError();
 }
 

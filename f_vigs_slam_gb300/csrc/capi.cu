@@ -92,6 +92,7 @@ struct fvgs_session {
     float4 *pos = nullptr, *scale = nullptr, *rot = nullptr, *col = nullptr;
     float4 *rec0 = nullptr, *rec1 = nullptr, *rec2 = nullptr;
     uint4* bin0 = nullptr;
+    uint4* bin0_prev = nullptr;  // the previous binning's records (swapped with bin0 per binning)
     float4* bin1 = nullptr;
     uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
     float *dbg_cov = nullptr, *dbg_inv = nullptr;
@@ -104,11 +105,20 @@ struct fvgs_session {
 
     int cap_tiles = 0;
     uint2* ranges = nullptr;
+    uint2* ranges_prev = nullptr;  // swapped with ranges per binning (vals with sort.vals_alt)
     float* tile_out = nullptr;
     int* tile_diff = nullptr;      // (ntx+1) x (nty+1) difference grid of tile counts
     size_t tile_diff_cells = 0;
     uint32_t* tile_fill = nullptr;  // scatter cursors
     SegSortWork seg{};
+    // incremental binning: entering instances per tile and the Gaussians with some
+    uint2* enter_ranges = nullptr;
+    uint32_t* enter_fill = nullptr;
+    uint64_t* enter_keys = nullptr;
+    uint32_t* changed = nullptr;
+    uint32_t enter_cap = 0;
+    bool hist_ok = false;  // the last binning left valid (bin0, ranges, vals) for the next one
+    int hist_ntx = 0, hist_nty = 0;
 
     FrameLevel lv[kMaxLevels];
 
@@ -205,6 +215,7 @@ void dev_free(fvgs_session* s, T*& p, size_t count) {
     } while (0)
 
 int alloc_instances(fvgs_session* s, uint64_t cap) {
+    s->hist_ok = false;
     if (s->keys) {
         FV_CK(cudaStreamSynchronize(s->stream));
         dev_free(s, s->keys, s->cap_inst);
@@ -305,6 +316,18 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     const int ntx = (W + P.tile_w - 1) / P.tile_w;
     const int nty = (H + P.tile_h - 1) / P.tile_h;
     const int T = ntx * nty;
+    const bool radix = (s->debug & FVGS_DEBUG_RADIX_SORT) != 0;
+    // Incremental binning needs the previous binning of the same Gaussians on
+    // the same tile grid, with true per-tile ranges (not the reference's
+    // culled-slot or range-launch behaviours).
+    const bool literal = (s->params.quirks & (FVGS_Q_CULLED_SLOTS | FVGS_Q_RANGE_LAUNCH)) != 0;
+    const bool hist = !radix && !literal && s->hist_ok && s->hist_ntx == ntx && s->hist_nty == nty;
+    s->hist_ok = false;  // until this binning is fully enqueued
+    if (!radix) {
+        std::swap(s->bin0, s->bin0_prev);
+        std::swap(s->ranges, s->ranges_prev);
+        std::swap(s->vals, s->sort.vals_alt);
+    }
     ProjectArgs pa{};
     pa.pos = s->pos;
     pa.scale = s->scale;
@@ -332,11 +355,15 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         pa.dbg_inv = s->dbg_inv;
         pa.dbg_vis = s->dbg_vis;
     }
-    const bool radix = (s->debug & FVGS_DEBUG_RADIX_SORT) != 0;
     if (!radix) {
         if (T > s->cap_tiles || tile_diff_words(ntx, nty) > s->tile_diff_cells) return FVGS_E_INVALID;
         FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * tile_diff_words(ntx, nty), s->stream));
         pa.tile_diff = s->tile_diff;
+        if (hist) {
+            pa.bin0_prev = s->bin0_prev;
+            pa.changed = s->changed;
+            pa.changed_cap = s->enter_cap;
+        }
     }
     {
         KScope k(s, FVGS_K_PROJECT, 1);
@@ -356,19 +383,38 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         // tile-bucket binning: counts -> ranges -> scatter -> per-tile sort
         {
             KScope k(s, FVGS_K_SCAN, 1);
-            FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, s->ranges, s->tile_fill, s->st, cap32,
-                                      s->seg.large_ctrl + 2, s->stream));
+            FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, hist, s->enter_cap, s->ranges, s->tile_fill,
+                                      s->enter_ranges, s->enter_fill, s->st, cap32, s->seg.large_ctrl + 2,
+                                      s->stream));
         }
         ea.keys = s->sort.keys_alt;  // composite keys, tile-major
         ea.vals = nullptr;
+        ea.bin0_prev = s->bin0_prev;
+        ea.changed = s->changed;
+        ea.counters = reinterpret_cast<const uint32_t*>(s->tile_diff + 2 * diff_grid_cells(ntx, nty));
+        ea.enter_keys = s->enter_keys;
+        ea.enter_fill = s->enter_fill;
+        ea.enter_cap = s->enter_cap;
         {
             KScope k(s, FVGS_K_EMIT, 1);
             FV_CK(launch_emit_scatter(ea, s->tile_fill, s->seg.large_ctrl + 2, s->num_sms * 8, s->st, s->stream));
         }
+        SegSortIncr inc{};
+        inc.ranges_prev = s->ranges_prev;
+        inc.vals_prev = s->sort.vals_alt;
+        inc.enter_ranges = s->enter_ranges;
+        inc.enter_keys = s->enter_keys;
+        inc.bin0 = s->bin0;
+        inc.bin1 = s->bin1;
+        inc.ntx = ntx;
+        inc.tw = P.tile_w;
+        inc.th = P.tile_h;
+        inc.n_gauss = s->n_g;
+        inc.capacity = s->cap_inst;
         {
             KScope k(s, FVGS_K_SORT, 2);
             FV_CK(launch_segsort(s->sort.keys_alt, s->keys, s->ranges, T, s->vals, s->keys, s->seg, s->st,
-                                 s->num_sms, s->stream));
+                                 s->num_sms, inc, s->stream));
         }
         if (P.quirks & FVGS_Q_RANGE_LAUNCH) {
             KScope k(s, FVGS_K_RANGES, 1);
@@ -399,6 +445,9 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     s->last_W = W;
     s->last_H = H;
     s->last_T = T;
+    s->hist_ok = !radix && !literal;
+    s->hist_ntx = ntx;
+    s->hist_nty = nty;
     s->has_binning = true;
     s->dbg_proj_valid = (s->debug & FVGS_DEBUG_PROJECTION) != 0;
     return FVGS_OK;
@@ -458,6 +507,13 @@ int check_status(fvgs_session* s, int* retry) {
     *retry = 0;
     const DevStatus st = *s->h_st;
     if (st.flags & kErrTimeout) return FVGS_E_TIMEOUT;
+    if (st.flags & kErrBounds) {
+        // an incremental binning did not find the instance count of a tile:
+        // drop the history and repeat the call with full binnings
+        s->hist_ok = false;
+        *retry = 1;
+        return FVGS_OK;
+    }
     if (st.flags & kErrOverflow) {
         const uint64_t need = (uint64_t)st.n_instances;
         uint64_t cap = need + need / 4 + 65536;
@@ -662,6 +718,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->rec1, N);
     FV_A(s->rec2, N);
     FV_A(s->bin0, N);
+    FV_A(s->bin0_prev, N);
     FV_A(s->bin1, N);
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
@@ -669,9 +726,15 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     const int ntx = (max_width + P.tile_w - 1) / P.tile_w, nty = (max_height + P.tile_h - 1) / P.tile_h;
     s->cap_tiles = ntx * nty;
     FV_A(s->ranges, (size_t)s->cap_tiles);
+    FV_A(s->ranges_prev, (size_t)s->cap_tiles);
     s->tile_diff_cells = tile_diff_words(ntx, nty);
     FV_A(s->tile_diff, s->tile_diff_cells);
-    FV_A(s->tile_fill, (size_t)s->cap_tiles * kSubBuckets);
+    FV_A(s->tile_fill, (size_t)s->cap_tiles);
+    FV_A(s->enter_ranges, (size_t)s->cap_tiles);
+    FV_A(s->enter_fill, (size_t)s->cap_tiles);
+    s->enter_cap = std::max<uint32_t>(1u << 16, capacity_gaussians);
+    FV_A(s->enter_keys, (size_t)s->enter_cap);
+    FV_A(s->changed, (size_t)s->enter_cap);
     FV_A(s->seg.large_list, (size_t)s->cap_tiles);
     FV_A(s->seg.large_ctrl, 4);  // [0..1] large-bucket list control, [2] scatter chunk counter
     FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
@@ -729,6 +792,17 @@ int fvgs_session_set_debug(fvgs_session* s, uint32_t flags) {
     return FVGS_OK;
 }
 
+int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
+                              uint32_t* n_changed) {
+    if (!s) return FVGS_E_INVALID;
+    const DevStatus& st = *s->h_st;
+    if (n_instances) *n_instances = st.n_instances;
+    if (incremental) *incremental = st.mode == kBinIncremental ? 1 : 0;
+    if (n_entering) *n_entering = st.n_enter;
+    if (n_changed) *n_changed = st.n_changed;
+    return FVGS_OK;
+}
+
 int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes) {
     if (!s || !bytes) return FVGS_E_INVALID;
     *bytes = s->footprint;
@@ -742,6 +816,7 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     FV_CK(cudaSetDevice(s->device));
     s->n_g = n;
     s->has_binning = s->has_track = false;
+    s->hist_ok = false;
     if (n == 0) return FVGS_OK;
     // Stage through rec planes (free until the next binning) so host arrays of
     // the reference's float3 layout become 16-byte vectors on the device.
@@ -785,6 +860,7 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
     FV_CK(cudaMemcpyAsync(opacities, tmp5, sizeof(float) * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
     s->has_binning = s->has_track = false;  // staging overwrote the records
+    s->hist_ok = false;
     return FVGS_OK;
 }
 

@@ -36,8 +36,21 @@ struct DevStatus {
     uint32_t flags;         // kErr* bits
     uint32_t n_instances;   // total instances of the last binning (may exceed capacity)
     uint32_t n_instances_clamped;  // min(total, capacity): the number sorted
-    uint32_t pad;
+    uint32_t mode;          // last binning: kBinFull or kBinIncremental
+    uint32_t n_enter;       // last binning: instances new to their tile since the binning before
+    uint32_t n_changed;     // last binning: Gaussians with such instances
+    uint32_t pad[2];
 };
+
+// Binning modes.  Full: every instance is scattered into its tile bucket and
+// each bucket is sorted.  Incremental (a previous binning of the same Gaussians
+// on the same tile grid exists): each tile keeps the members of its previous
+// sorted list that are still inside their Gaussian's new tile rectangle, in
+// their previous order, and appends only the instances that entered it; the
+// adaptive per-tile sort then has little left to do.  Both give identical
+// results.
+constexpr uint32_t kBinFull = 0;
+constexpr uint32_t kBinIncremental = 1;
 
 // Pose state kept on the device so a whole tracking frame runs without the host.
 struct DevPose {
@@ -69,11 +82,24 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-// Tile buckets can be split into sub-buckets (by Gaussian index), each with
-// its own scatter cursor, to spread same-address atomics.  Measured on GB300
-// the cursor atomics are not contention-bound and 8 sub-buckets made binning
-// slower, so the split is off (1).
-constexpr int kSubBuckets = 1;
+// Tile-rectangle record of the binning (bin0): x0 | y0 << 16, x1 | y1 << 16
+// (inclusive), instance count (0: no instances), phat.y bits.
+__device__ __forceinline__ bool rect_contains(uint4 b0, int tx, int ty) {
+    return b0.z != 0u && tx >= (int)(b0.x & 0xffffu) && tx <= (int)(b0.y & 0xffffu) && ty >= (int)(b0.x >> 16) &&
+           ty <= (int)(b0.y >> 16);
+}
+
+// Depth of a Gaussian at the centre of tile (tx, ty) -- the sort key of the
+// reference's generateTileHashes_kernel (src/GSCudaKernels.cu:596-667):
+// fmaf(phy, dy, fmaf(phx, dx, z)), d = tile centre - projected mean.
+__device__ __forceinline__ float tile_depth(int tx, int ty, int tw, int th, float u, float v, float z, float phx,
+                                            uint32_t phy_bits) {
+    const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)tw);
+    const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)th);
+    const float dx = __fsub_rn(tcx, u);
+    const float dy = __fsub_rn(tcy, v);
+    return __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+}
 
 // Bounded spin budget for device-side waits; on expiry a kernel records
 // kErrTimeout and carries on with a safe value instead of hanging.

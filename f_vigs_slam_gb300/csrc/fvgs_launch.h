@@ -30,7 +30,13 @@ struct ProjectArgs {
     uint4* bin0;
     float4* bin1;
     uint32_t* counts;
-    int* tile_diff;    // optional: (ntx+1) x (nty+1) difference grid of tile counts
+    int* tile_diff;    // optional: binning scratch (tile_diff_words): count grid, entering grid, counters
+    // incremental binning (optional): the previous binning's rectangles; the
+    // instances new to a tile go to the entering grid, the Gaussians that have
+    // some to changed[] (at most changed_cap listed)
+    const uint4* bin0_prev;
+    uint32_t* changed;
+    uint32_t changed_cap;
     float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
     float* dbg_inv;    // optional: 3N inverse, stored order (xx, yy, xy)
     uint8_t* dbg_vis;  // optional: N visibility
@@ -45,6 +51,14 @@ struct EmitArgs {
     uint64_t capacity;
     uint64_t* keys;
     uint32_t* vals;
+    // incremental mode (tile-bucket path): entering instances of the listed
+    // Gaussians go to enter_keys at the enter_fill cursors
+    const uint4* bin0_prev;
+    const uint32_t* changed;
+    const uint32_t* counters;  // [0] entering instances, [1] listed Gaussians
+    uint64_t* enter_keys;
+    uint32_t* enter_fill;
+    uint32_t enter_cap;
 };
 
 cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s);
@@ -56,8 +70,16 @@ cudaError_t launch_ranges(const uint64_t* keys, const DevStatus* st, int num_til
                           uint2* ranges, int grid, cudaStream_t s);
 // Tile-bucket binning: counts from the projection's difference grid, then
 // ranges / cursors, then scatter of composite keys (depth bits << 32 | index).
+// The binning scratch holds two (ntx+1) x (nty+1) difference grids (all
+// instances, entering instances) and 8 counter words; one memset clears it.
+size_t diff_grid_cells(int ntx, int nty);
 size_t tile_diff_words(int ntx, int nty);
-cudaError_t launch_tile_offsets(int* diff, int ntx, int nty, uint2* ranges, uint32_t* fill, DevStatus* st,
+constexpr int kCounterWords = 8;  // [0] entering instances, [1] listed Gaussians
+// hist: a previous binning on the same tile grid is valid; the kernel then
+// also scans the entering grid and picks incremental mode when the entering
+// instances fit enter_cap (DevStatus::mode).
+cudaError_t launch_tile_offsets(int* scratch, int ntx, int nty, bool hist, uint32_t enter_cap, uint2* ranges,
+                                uint32_t* fill, uint2* enter_ranges, uint32_t* enter_fill, DevStatus* st,
                                 uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s);
 cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
                                 const DevStatus* st, cudaStream_t s);
@@ -69,8 +91,22 @@ struct SegSortWork {
     uint32_t* large_list;  // [T] tiles too large for one CTA
     uint32_t* large_ctrl;  // [2]: count, next
 };
-cudaError_t launch_segsort(const uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
-                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid, cudaStream_t s);
+// Incremental mode inputs: the previous binning's ranges and sorted indices,
+// the entering instances per tile, and the current binning records.
+struct SegSortIncr {
+    const uint2* ranges_prev;
+    const uint32_t* vals_prev;
+    const uint2* enter_ranges;
+    const uint64_t* enter_keys;
+    const uint4* bin0;
+    const float4* bin1;
+    int ntx, tw, th;
+    uint32_t n_gauss;    // indices at or above are rejected
+    uint64_t capacity;   // instance buffer size: previous ranges are clamped to it
+};
+cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
+                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid,
+                           const SegSortIncr& inc, cudaStream_t s);
 
 // ---- radix sort (sort.cu) ----
 struct SortWorkspace {

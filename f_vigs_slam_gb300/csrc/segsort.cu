@@ -5,12 +5,16 @@
 // most one instance per tile and instances are generated in Gaussian-index
 // order, so inside a tile that stable order is exactly the order of the
 // unique composite key (depth bits << 32 | Gaussian index).  Instances are
-// therefore scattered into per-tile buckets (any order) and each bucket is
-// sorted on its own:
+// therefore collected per tile and each tile is sorted on its own:
+//  * full mode: the tile bucket was filled by the scatter (any order);
+//  * incremental mode: the tile's previous sorted list, minus the members
+//    that left the tile, with keys recomputed for the new pose, followed by
+//    the entering instances -- nearly sorted;
 //  * up to 4096 instances: one CTA, in shared memory -- every thread sorts 16
-//    keys in registers with a bitonic network, then log2(n/16) merge-path
-//    rounds double the sorted runs;
-//  * larger buckets (rare: huge splats, culled slots piled into tile 0) are
+//    keys in registers with a bitonic network, then merge-path rounds double
+//    the sorted runs.  Runs already in order (the common case for nearly
+//    sorted input) are recognised by one comparison and left alone;
+//  * larger tiles (rare: huge splats, culled slots piled into tile 0) are
 //    listed by the first kernel and sorted by a second one: chunks of 4096 in
 //    shared memory, then merge-path passes through global memory.
 // The outputs are the sorted Gaussian indices and the reference-format keys.
@@ -46,18 +50,22 @@ __device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
             }
 }
 
-// One merge-path round: thread t produces outputs [16t, 16t+16) of the merged
-// pair of sorted runs of length L that contains them.  Both run heads are
-// re-read from shared memory each step (keeping them in registers and loading
-// one key per step measured slower: more registers, fewer resident CTAs).
-__device__ __forceinline__ void merge_round(const uint64_t* s, int t, int L, uint64_t (&k)[kSegItems]) {
+// One merge-path round over runs of length L of s[0..m) (m a multiple of 16):
+// thread t produces outputs [16t, 16t+16) of the pair of runs containing them.
+// Returns false when the pair is already in order (nothing to write).  Both
+// run heads are re-read from shared memory each step (register-held heads
+// measured slower: more registers, fewer resident CTAs).
+__device__ __forceinline__ bool merge_round(const uint64_t* s, int t, int m, int L, uint64_t (&k)[kSegItems]) {
     const int per_pair = (2 * L) / kSegItems;
     const int ps = (t / per_pair) * 2 * L;
     const int d = (t % per_pair) * kSegItems;
-    int lo = max(0, d - L), hi = min(d, L);
+    const int la = min(L, m - ps);
+    const int lb = min(L, max(0, m - ps - L));
+    if (lb == 0 || s[spad(ps + la - 1)] <= s[spad(ps + la)]) return false;
+    int lo = max(0, d - lb), hi = min(d, la);
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (s[spad(ps + mid)] <= s[spad(ps + L + d - 1 - mid)])
+        if (s[spad(ps + mid)] <= s[spad(ps + la + d - 1 - mid)])
             lo = mid + 1;
         else
             hi = mid;
@@ -65,17 +73,18 @@ __device__ __forceinline__ void merge_round(const uint64_t* s, int t, int L, uin
     int ai = lo, bj = d - lo;
 #pragma unroll
     for (int r = 0; r < kSegItems; ++r) {
-        const uint64_t a = ai < L ? s[spad(ps + ai)] : kKeyInf;
-        const uint64_t b = bj < L ? s[spad(ps + L + bj)] : kKeyInf;
+        const uint64_t a = ai < la ? s[spad(ps + ai)] : kKeyInf;
+        const uint64_t b = bj < lb ? s[spad(ps + la + bj)] : kKeyInf;
         const bool ta = a <= b;
         k[r] = ta ? a : b;
         ai += ta ? 1 : 0;
         bj += ta ? 0 : 1;
     }
+    return true;
 }
 
-// Sort s[0..m) (padded layout, m a power of two in [kSegItems, 4096]) in
-// shared memory with the CTA.  Threads >= m/kSegItems only take part in the
+// Sort s[0..m) (padded layout, m a multiple of kSegItems, <= 4096) in shared
+// memory with the CTA.  Threads >= m/kSegItems only take part in the
 // barriers.  While a merged pair spans at most one warp's 512 keys the round
 // touches only that warp's slice, so it synchronises the warp, not the CTA.
 __device__ void block_merge_sort(uint64_t* s, int m) {
@@ -85,20 +94,28 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
     if (t < active) {
 #pragma unroll
         for (int j = 0; j < kSegItems; ++j) k[j] = s[spad(t * kSegItems + j)];
-        sort_items(k);
+        bool sorted = true;
 #pragma unroll
-        for (int j = 0; j < kSegItems; ++j) s[spad(t * kSegItems + j)] = k[j];
+        for (int j = 0; j + 1 < kSegItems; ++j) sorted = sorted && k[j] <= k[j + 1];
+        if (!sorted) {
+            sort_items(k);
+#pragma unroll
+            for (int j = 0; j < kSegItems; ++j) s[spad(t * kSegItems + j)] = k[j];
+        }
     }
-    __syncwarp();
+    __syncthreads();
+    const bool desc = t + 1 < active && s[spad(t * kSegItems + kSegItems - 1)] > s[spad((t + 1) * kSegItems)];
+    if (!__syncthreads_or(desc)) return;  // every run boundary already in order
     constexpr int kWarpSpan = 32 * kSegItems;
     for (int L = kSegItems; L < m; L <<= 1) {
         const bool warp_local = 2 * L <= kWarpSpan;
-        if (t < active) merge_round(s, t, L, k);
+        bool wrote = false;
+        if (t < active) wrote = merge_round(s, t, m, L, k);
         if (warp_local)
             __syncwarp();
         else
             __syncthreads();
-        if (t < active) {
+        if (wrote) {
 #pragma unroll
             for (int r = 0; r < kSegItems; ++r) s[spad(t * kSegItems + r)] = k[r];
         }
@@ -116,22 +133,107 @@ __device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32
     keys[dst] = ((uint64_t)tile << 32) | (key >> 32);
 }
 
-__global__ void __launch_bounds__(kSegThreads) segsort_kernel(const uint64_t* __restrict__ comp,
-                                                              const uint2* __restrict__ ranges, uint32_t* vals,
-                                                              uint64_t* keys, SegSortWork w, const DevStatus* st) {
+// Incremental mode: collect tile `tile`'s instances into dst (shared memory in
+// the padded layout, or global memory) -- first the members of the previous
+// sorted list whose Gaussian's new rectangle still holds the tile, in their
+// previous order, with the key for the new projection; then the entering
+// instances.  Returns the number collected (the tile's count when consistent);
+// writes stop at n_cap.
+constexpr int kGatherItems = 4;
+template <bool SMEM>
+__device__ int gather_tile(uint64_t* dst, uint32_t tile, int n_cap, const SegSortIncr& inc, uint32_t* s_wsum) {
+    const int tx = (int)(tile % (uint32_t)inc.ntx), ty = (int)(tile / (uint32_t)inc.ntx);
+    uint2 ro = inc.ranges_prev[tile];
+    ro.y = (uint32_t)min((uint64_t)ro.y, inc.capacity);
+    const int n_old = ro.y > ro.x ? (int)(ro.y - ro.x) : 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int kept = 0;
+    for (int c0 = 0; c0 < n_old; c0 += kSegThreads * kGatherItems) {
+        const int i0 = c0 + threadIdx.x * kGatherItems;  // blocked: keeps the previous order
+        uint32_t gid[kGatherItems];
+        uint64_t key[kGatherItems];
+        bool keep[kGatherItems];
+#pragma unroll
+        for (int j = 0; j < kGatherItems; ++j) gid[j] = i0 + j < n_old ? inc.vals_prev[ro.x + i0 + j] : 0xffffffffu;
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kGatherItems; ++j) {
+            keep[j] = false;
+            key[j] = 0;
+            if (gid[j] < inc.n_gauss) {
+                const uint4 b0 = inc.bin0[gid[j]];
+                if (rect_contains(b0, tx, ty)) {
+                    const float4 b1 = inc.bin1[gid[j]];
+                    const float d = tile_depth(tx, ty, inc.tw, inc.th, b1.x, b1.y, b1.z, b1.w, b0.w);
+                    key[j] = ((uint64_t)__float_as_uint(d) << 32) | gid[j];
+                    keep[j] = true;
+                    ++cnt;
+                }
+            }
+        }
+        // CTA exclusive scan of the per-thread counts
+        uint32_t incl = (uint32_t)cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_wsum[w] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int q = 0; q < kSegThreads / 32; ++q) {
+            const uint32_t v = s_wsum[q];
+            before += q < w ? v : 0u;
+            total += v;
+        }
+        int pos = kept + (int)(before + incl) - cnt;
+#pragma unroll
+        for (int j = 0; j < kGatherItems; ++j) {
+            if (keep[j]) {
+                if (pos < n_cap) dst[SMEM ? spad(pos) : pos] = key[j];
+                ++pos;
+            }
+        }
+        kept += (int)total;
+        __syncthreads();
+    }
+    const uint2 re = inc.enter_ranges[tile];
+    const int ne = (int)(re.y - re.x);
+    for (int i = threadIdx.x; i < ne; i += kSegThreads) {
+        const int pos = kept + i;
+        if (pos < n_cap) dst[SMEM ? spad(pos) : pos] = inc.enter_keys[re.x + i];
+    }
+    return kept + ne;
+}
+
+__global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, const uint2* __restrict__ ranges,
+                                                              uint32_t* vals, uint64_t* keys, SegSortWork w,
+                                                              DevStatus* st, SegSortIncr inc) {
     __shared__ uint64_t s[kSegCap + kSegCap / 16];
+    __shared__ uint32_t s_wsum[kSegThreads / 32];
     if (st->flags & kErrOverflow) return;
+    const bool incr = st->mode == kBinIncremental;
     const uint32_t tile = blockIdx.x;
     const uint2 r = ranges[tile];
     const int n = (int)(r.y - r.x);
     if (n <= 0) return;
     if (n > kSegCap) {
+        if (incr) {
+            const int got = gather_tile<false>(comp + r.x, tile, n, inc, s_wsum);
+            if (got != n && threadIdx.x == 0) atomicOr(&st->flags, kErrBounds);
+        }
         if (threadIdx.x == 0) w.large_list[atomicAdd(&w.large_ctrl[0], 1u)] = tile;
         return;
     }
-    int m = kSegItems;
-    while (m < n) m <<= 1;
-    for (int i = threadIdx.x; i < m; i += kSegThreads) s[spad(i)] = i < n ? comp[r.x + i] : kKeyInf;
+    const int m = (n + kSegItems - 1) / kSegItems * kSegItems;
+    if (incr) {
+        const int got = gather_tile<true>(s, tile, n, inc, s_wsum);
+        if (got != n && threadIdx.x == 0) atomicOr(&st->flags, kErrBounds);
+        if (threadIdx.x < m - n) s[spad(n + threadIdx.x)] = kKeyInf;
+    } else {
+        for (int i = threadIdx.x; i < m; i += kSegThreads) s[spad(i)] = i < n ? comp[r.x + i] : kKeyInf;
+    }
     __syncthreads();
     block_merge_sort(s, m);
     for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(s[spad(i)], tile, r.x + i, vals, keys);
@@ -205,14 +307,14 @@ __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* co
     }
 }
 
-cudaError_t launch_segsort(const uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
-                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid, cudaStream_t s) {
+cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
+                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid,
+                           const SegSortIncr& inc, cudaStream_t s) {
     if (num_tiles <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(w.large_ctrl, 0, 2 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, keys, w, st);
-    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(const_cast<uint64_t*>(comp), tmp, ranges, vals, keys, w,
-                                                             st);
+    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, keys, w, const_cast<DevStatus*>(st), inc);
+    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(comp, tmp, ranges, vals, keys, w, st);
     return cudaGetLastError();
 }
 

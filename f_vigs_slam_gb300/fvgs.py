@@ -179,6 +179,14 @@ class Session:
         _check(self.lib.fvgs_session_footprint(self.h, C.byref(b)), "fvgs_session_footprint")
         return int(b.value)
 
+    def binning_info(self) -> dict:
+        """How the last binning read back by the host was formed (see fvgs_session_binning_info)."""
+        n, inc, ne, nc = C.c_uint32(), C.c_int(), C.c_uint32(), C.c_uint32()
+        _check(self.lib.fvgs_session_binning_info(self.h, C.byref(n), C.byref(inc), C.byref(ne), C.byref(nc)),
+               "fvgs_session_binning_info")
+        return dict(n_instances=int(n.value), incremental=bool(inc.value), n_entering=int(ne.value),
+                    n_changed=int(nc.value))
+
     def upload(self, scene):
         pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
         col, opa = _f32(scene.colors), _f32(scene.opacities)
