@@ -143,25 +143,31 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     uint32_t count = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
     if (!visible && !(a.quirks & FVGS_Q_CULLED_SLOTS)) count = 0;
 
-    const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
-    a.rec0[i] = make_float4(u, v, z, co.w);
-    a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);
-    a.rec2[i] = make_float4(phy, co.x, co.y, co.z);
-    a.bin0[i] = make_uint4((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16), count,
-                           __float_as_uint(phy));
-    a.bin1[i] = make_float4(u, v, z, phx);
+    // Records of Gaussians without instances are never read by the blending
+    // kernels; they are written only where the culled-slot behaviour makes
+    // culled Gaussians blend (with the zero record), and the host reports
+    // zeros for them.
+    if (count && (visible || (a.quirks & FVGS_Q_CULLED_SLOTS))) {
+        const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+        a.rec0[i] = make_float4(u, v, z, co.w);
+        a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);
+        a.rec2[i] = make_float4(phy, co.x, co.y, co.z);
+        a.bins[i].p = make_float4(u, v, z, phx);
+    }
+    a.bins[i].r = make_uint4((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16), count,
+                             __float_as_uint(phy));
     a.counts[i] = count;
     if (a.tile_diff) {
         const int gw = a.ntx + 1;
         const size_t cells = (size_t)gw * (a.nty + 1);
         if (count) add_rect(a.tile_diff, gw, x0, y0, x1, y1);
-        if (a.bin0_prev) {
+        if (a.bins_prev) {
             // instances entering a tile: the new rectangle minus the previous
             // one (at most four rectangles around their intersection)
             uint32_t n_enter = 0;
             if (count) {
                 int* e = a.tile_diff + cells;
-                const uint4 pb = a.bin0_prev[i];
+                const uint4 pb = a.bins_prev[i].r;
                 const int px0 = (int)(pb.x & 0xffffu), py0 = (int)(pb.x >> 16);
                 const int px1 = (int)(pb.y & 0xffffu), py1 = (int)(pb.y >> 16);
                 const int ix0 = max(x0, px0), ix1 = min(x1, px1), iy0 = max(y0, py0), iy1 = min(y1, py1);
@@ -319,9 +325,9 @@ __global__ void __launch_bounds__(256) emit_keys_kernel(EmitArgs a) {
     float4 b1 = make_float4(0, 0, 0, 0);
     uint32_t off = 0;
     if (valid) {
-        b0 = a.bin0[g];
-        b1 = a.bin1[g];
+        b0 = a.bins[g].r;
         off = a.offsets[g];
+        if (b0.z) b1 = a.bins[g].p;
     }
     const uint32_t cnt = valid ? b0.z : 0u;
     // warp-local exclusive prefix of counts
@@ -545,10 +551,10 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, uint32_t first
     uint2 prev = make_uint2(1u, 0u);  // previous rectangle (incremental), empty by default
     if (valid) {
         g = INCR ? a.changed[item] : item;
-        b0 = a.bin0[g];
-        b1 = a.bin1[g];
+        b0 = a.bins[g].r;
+        if (b0.z) b1 = a.bins[g].p;
         if (INCR) {
-            const uint4 p = a.bin0_prev[g];
+            const uint4 p = a.bins_prev[g].r;
             if (p.z) prev = make_uint2(p.x, p.y);
         }
     }

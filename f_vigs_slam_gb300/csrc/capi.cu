@@ -91,9 +91,8 @@ struct fvgs_session {
 
     float4 *pos = nullptr, *scale = nullptr, *rot = nullptr, *col = nullptr;
     float4 *rec0 = nullptr, *rec1 = nullptr, *rec2 = nullptr;
-    uint4* bin0 = nullptr;
-    uint4* bin0_prev = nullptr;  // the previous binning's records (swapped with bin0 per binning)
-    float4* bin1 = nullptr;
+    BinRec* bins = nullptr;
+    BinRec* bins_prev = nullptr;  // the previous binning's records (swapped with bins per binning)
     uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
     float *dbg_cov = nullptr, *dbg_inv = nullptr;
     uint8_t* dbg_vis = nullptr;
@@ -117,7 +116,8 @@ struct fvgs_session {
     uint64_t* enter_keys = nullptr;
     uint32_t* changed = nullptr;
     uint32_t enter_cap = 0;
-    bool hist_ok = false;  // the last binning left valid (bin0, ranges, vals) for the next one
+    bool hist_ok = false;  // the last binning left valid (bins, ranges, vals) for the next one
+    bool keys_valid = false;  // keys[] holds the last binning's reference-format keys
     int hist_ntx = 0, hist_nty = 0;
 
     FrameLevel lv[kMaxLevels];
@@ -324,7 +324,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     const bool hist = !radix && !literal && s->hist_ok && s->hist_ntx == ntx && s->hist_nty == nty;
     s->hist_ok = false;  // until this binning is fully enqueued
     if (!radix) {
-        std::swap(s->bin0, s->bin0_prev);
+        std::swap(s->bins, s->bins_prev);
         std::swap(s->ranges, s->ranges_prev);
         std::swap(s->vals, s->sort.vals_alt);
     }
@@ -347,8 +347,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     pa.rec0 = s->rec0;
     pa.rec1 = s->rec1;
     pa.rec2 = s->rec2;
-    pa.bin0 = s->bin0;
-    pa.bin1 = s->bin1;
+    pa.bins = s->bins;
     pa.counts = s->counts;
     if (s->debug & FVGS_DEBUG_PROJECTION) {
         pa.dbg_cov = s->dbg_cov;
@@ -360,7 +359,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * tile_diff_words(ntx, nty), s->stream));
         pa.tile_diff = s->tile_diff;
         if (hist) {
-            pa.bin0_prev = s->bin0_prev;
+            pa.bins_prev = s->bins_prev;
             pa.changed = s->changed;
             pa.changed_cap = s->enter_cap;
         }
@@ -370,8 +369,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         FV_CK(launch_project_count(pa, s->stream));
     }
     EmitArgs ea{};
-    ea.bin0 = s->bin0;
-    ea.bin1 = s->bin1;
+    ea.bins = s->bins;
     ea.offsets = s->offsets;
     ea.n = (int)s->n_g;
     ea.ntx = ntx;
@@ -389,7 +387,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         }
         ea.keys = s->sort.keys_alt;  // composite keys, tile-major
         ea.vals = nullptr;
-        ea.bin0_prev = s->bin0_prev;
+        ea.bins_prev = s->bins_prev;
         ea.changed = s->changed;
         ea.counters = reinterpret_cast<const uint32_t*>(s->tile_diff + 2 * diff_grid_cells(ntx, nty));
         ea.enter_keys = s->enter_keys;
@@ -404,8 +402,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         inc.vals_prev = s->sort.vals_alt;
         inc.enter_ranges = s->enter_ranges;
         inc.enter_keys = s->enter_keys;
-        inc.bin0 = s->bin0;
-        inc.bin1 = s->bin1;
+        inc.bins = s->bins;
         inc.ntx = ntx;
         inc.tw = P.tile_w;
         inc.th = P.tile_h;
@@ -413,12 +410,17 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         inc.capacity = s->cap_inst;
         {
             KScope k(s, FVGS_K_SORT, 2);
-            FV_CK(launch_segsort(s->sort.keys_alt, s->keys, s->ranges, T, s->vals, s->keys, s->seg, s->st,
-                                 s->num_sms, inc, s->stream));
+            FV_CK(launch_segsort(s->sort.keys_alt, s->keys, s->ranges, T, s->vals, s->seg, s->st, s->num_sms, inc,
+                                 s->stream));
         }
+        s->keys_valid = false;
         if (P.quirks & FVGS_Q_RANGE_LAUNCH) {
-            KScope k(s, FVGS_K_RANGES, 1);
+            // the literal range pass reads the reference-format keys
+            KScope k(s, FVGS_K_RANGES, 2);
+            FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, T, ntx, P.tile_w, P.tile_h, s->st, s->keys,
+                                   s->stream));
             FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
+            s->keys_valid = true;
         }
     } else {
         // global path: offsets scan, generation-order keys, LSD radix sort, ranges
@@ -441,6 +443,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
             KScope k(s, FVGS_K_RANGES, 1);
             FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
         }
+        s->keys_valid = true;
     }
     s->last_W = W;
     s->last_H = H;
@@ -717,9 +720,8 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->rec0, N);
     FV_A(s->rec1, N);
     FV_A(s->rec2, N);
-    FV_A(s->bin0, N);
-    FV_A(s->bin0_prev, N);
-    FV_A(s->bin1, N);
+    FV_A(s->bins, N);
+    FV_A(s->bins_prev, N);
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
     FV_A(s->partials, scan_partials_size((int)N) + 1);
@@ -823,8 +825,8 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     float* tmp = reinterpret_cast<float*>(s->rec0);  // 4N floats
     float* tmp2 = reinterpret_cast<float*>(s->rec1);
     float* tmp3 = reinterpret_cast<float*>(s->rec2);
-    float* tmp4 = reinterpret_cast<float*>(s->bin1);
-    float* tmp5 = reinterpret_cast<float*>(s->bin0);
+    float* tmp4 = reinterpret_cast<float*>(s->bins);       // 8N floats
+    float* tmp5 = reinterpret_cast<float*>(s->bins_prev);
     FV_CK(cudaMemcpyAsync(tmp, positions, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(tmp2, scales, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(tmp3, orientations, sizeof(float) * 4 * n, cudaMemcpyDefault, s->stream));
@@ -848,8 +850,8 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
     float* tmp = reinterpret_cast<float*>(s->rec0);
     float* tmp2 = reinterpret_cast<float*>(s->rec1);
     float* tmp3 = reinterpret_cast<float*>(s->rec2);
-    float* tmp4 = reinterpret_cast<float*>(s->bin1);
-    float* tmp5 = reinterpret_cast<float*>(s->bin0);
+    float* tmp4 = reinterpret_cast<float*>(s->bins);       // 8N floats
+    float* tmp5 = reinterpret_cast<float*>(s->bins_prev);
     download_unpack_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->pos, s->scale, s->rot, s->col, n, tmp, tmp2,
                                                                    tmp3, tmp4, tmp5);
     FV_CK(cudaGetLastError());
@@ -926,9 +928,14 @@ int fvgs_download_projection(fvgs_session* s, float* uv, float* cov2d, float* in
     if (cov2d) FV_CK(cudaMemcpyAsync(cov2d, s->dbg_cov, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     if (inv2d) FV_CK(cudaMemcpyAsync(inv2d, s->dbg_inv, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     if (visible) FV_CK(cudaMemcpyAsync(visible, s->dbg_vis, n, cudaMemcpyDefault, s->stream));
-    if (tile_counts) FV_CK(cudaMemcpyAsync(tile_counts, s->counts, sizeof(uint32_t) * n, cudaMemcpyDefault, s->stream));
+    std::vector<uint32_t> cnt(n);
+    FV_CK(cudaMemcpyAsync(cnt.data(), s->counts, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
+    if (tile_counts) std::memcpy(tile_counts, cnt.data(), sizeof(uint32_t) * n);
     for (size_t i = 0; i < n; ++i) {
+        // Gaussians without instances keep no record on the device; the
+        // reference's buffers hold zeros for them
+        if (cnt[i] == 0) r0[i] = r1[i] = r2[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (uv) {
             uv[2 * i] = r0[i].x;
             uv[2 * i + 1] = r0[i].y;
@@ -952,6 +959,12 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
     const uint32_t n = s->h_st->n_instances_clamped;
     if (n_instances) *n_instances = n;
     if ((keys || values) && n > max_instances) return FVGS_E_CAPACITY;
+    if (keys && n && !s->keys_valid) {
+        const int ntx = (s->last_W + s->params.tile_w - 1) / s->params.tile_w;
+        FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->last_T, ntx, s->params.tile_w, s->params.tile_h, s->st,
+                               s->keys, s->stream));
+        s->keys_valid = true;
+    }
     if (keys && n) FV_CK(cudaMemcpyAsync(keys, s->keys, sizeof(uint64_t) * n, cudaMemcpyDefault, s->stream));
     if (values && n) FV_CK(cudaMemcpyAsync(values, s->vals, sizeof(uint32_t) * n, cudaMemcpyDefault, s->stream));
     if (ranges) FV_CK(cudaMemcpyAsync(ranges, s->ranges, sizeof(uint2) * s->last_T, cudaMemcpyDefault, s->stream));

@@ -13,6 +13,14 @@ namespace fvgs {
 struct DevStatus;
 struct DevPose;
 
+// Binning record of one Gaussian, 32 bytes so that one gather touches one
+// sector: r = (x0 | y0 << 16, x1 | y1 << 16 (inclusive tile rectangle),
+// instance count (0: none), phat.y bits), p = (u, v, z, phat.x).
+struct __align__(32) BinRec {
+    uint4 r;
+    float4 p;
+};
+
 struct ProjectArgs {
     const float4* pos;
     const float4* scale;
@@ -27,14 +35,13 @@ struct ProjectArgs {
     float4* rec0;
     float4* rec1;
     float4* rec2;
-    uint4* bin0;
-    float4* bin1;
+    BinRec* bins;
     uint32_t* counts;
     int* tile_diff;    // optional: binning scratch (tile_diff_words): count grid, entering grid, counters
     // incremental binning (optional): the previous binning's rectangles; the
     // instances new to a tile go to the entering grid, the Gaussians that have
     // some to changed[] (at most changed_cap listed)
-    const uint4* bin0_prev;
+    const BinRec* bins_prev;
     uint32_t* changed;
     uint32_t changed_cap;
     float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
@@ -43,8 +50,7 @@ struct ProjectArgs {
 };
 
 struct EmitArgs {
-    const uint4* bin0;
-    const float4* bin1;
+    const BinRec* bins;
     const uint32_t* offsets;
     int n;
     int ntx, tw, th;
@@ -53,7 +59,7 @@ struct EmitArgs {
     uint32_t* vals;
     // incremental mode (tile-bucket path): entering instances of the listed
     // Gaussians go to enter_keys at the enter_fill cursors
-    const uint4* bin0_prev;
+    const BinRec* bins_prev;
     const uint32_t* changed;
     const uint32_t* counters;  // [0] entering instances, [1] listed Gaussians
     uint64_t* enter_keys;
@@ -84,9 +90,8 @@ cudaError_t launch_tile_offsets(int* scratch, int ntx, int nty, bool hist, uint3
 cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
                                 const DevStatus* st, cudaStream_t s);
 // Per-tile sort of the composite keys (segsort.cu): writes the sorted Gaussian
-// indices to vals and the reference-format keys (tile << 32 | depth bits) to
-// keys.  Tiles above 4096 instances go through a global merge sort that uses
-// tmp (capacity u64) as scratch.
+// indices to vals.  Tiles above 4096 instances go through a global merge sort
+// that uses tmp (capacity u64) as scratch.
 struct SegSortWork {
     uint32_t* large_list;  // [T] tiles too large for one CTA
     uint32_t* large_ctrl;  // [2]: count, next
@@ -98,15 +103,19 @@ struct SegSortIncr {
     const uint32_t* vals_prev;
     const uint2* enter_ranges;
     const uint64_t* enter_keys;
-    const uint4* bin0;
-    const float4* bin1;
+    const BinRec* bins;
     int ntx, tw, th;
     uint32_t n_gauss;    // indices at or above are rejected
     uint64_t capacity;   // instance buffer size: previous ranges are clamped to it
 };
 cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
-                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid,
-                           const SegSortIncr& inc, cudaStream_t s);
+                           SegSortWork w, const DevStatus* st, int large_grid, const SegSortIncr& inc,
+                           cudaStream_t s);
+// Reference-format keys (tile << 32 | depth bits) of a tile-bucket binning,
+// rebuilt from its ranges, sorted indices and binning records with the
+// emission's arithmetic (the tracking path itself never reads them).
+cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, int num_tiles, int ntx,
+                             int tw, int th, const DevStatus* st, uint64_t* keys, cudaStream_t s);
 
 // ---- radix sort (sort.cu) ----
 struct SortWorkspace {

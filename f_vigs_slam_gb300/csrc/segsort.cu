@@ -17,7 +17,9 @@
 //  * larger tiles (rare: huge splats, culled slots piled into tile 0) are
 //    listed by the first kernel and sorted by a second one: chunks of 4096 in
 //    shared memory, then merge-path passes through global memory.
-// The outputs are the sorted Gaussian indices and the reference-format keys.
+// The output is the sorted Gaussian indices; the reference-format keys are
+// rebuilt on request (make_keys_kernel) since the blending kernels only read
+// ranges and indices.
 #include "fvgs_device.cuh"
 #include "fvgs_launch.h"
 
@@ -127,10 +129,8 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
     __syncthreads();
 }
 
-__device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32_t dst, uint32_t* vals,
-                                             uint64_t* keys) {
+__device__ __forceinline__ void write_sorted(uint64_t key, uint32_t dst, uint32_t* vals) {
     vals[dst] = (uint32_t)key;
-    keys[dst] = ((uint64_t)tile << 32) | (key >> 32);
 }
 
 // Incremental mode: collect tile `tile`'s instances into dst (shared memory in
@@ -141,7 +141,8 @@ __device__ __forceinline__ void write_sorted(uint64_t key, uint32_t tile, uint32
 // writes stop at n_cap.
 constexpr int kGatherItems = 4;
 template <bool SMEM>
-__device__ int gather_tile(uint64_t* dst, uint32_t tile, int n_cap, const SegSortIncr& inc, uint32_t* s_wsum) {
+__device__ int gather_tile(uint64_t* dst, uint32_t tile, int n_cap, const SegSortIncr& inc, uint32_t* s_wsum,
+                           int* n_kept) {
     const int tx = (int)(tile % (uint32_t)inc.ntx), ty = (int)(tile / (uint32_t)inc.ntx);
     uint2 ro = inc.ranges_prev[tile];
     ro.y = (uint32_t)min((uint64_t)ro.y, inc.capacity);
@@ -155,21 +156,25 @@ __device__ int gather_tile(uint64_t* dst, uint32_t tile, int n_cap, const SegSor
         bool keep[kGatherItems];
 #pragma unroll
         for (int j = 0; j < kGatherItems; ++j) gid[j] = i0 + j < n_old ? inc.vals_prev[ro.x + i0 + j] : 0xffffffffu;
+        uint4 b0[kGatherItems];
+        float4 b1[kGatherItems];
+#pragma unroll
+        for (int j = 0; j < kGatherItems; ++j) {
+            // both halves of the 32-byte record at once: one dependent step
+            b0[j] = make_uint4(0, 0, 0, 0);
+            b1[j] = make_float4(0, 0, 0, 0);
+            if (gid[j] < inc.n_gauss) {
+                b0[j] = inc.bins[gid[j]].r;
+                b1[j] = inc.bins[gid[j]].p;
+            }
+        }
         int cnt = 0;
 #pragma unroll
         for (int j = 0; j < kGatherItems; ++j) {
-            keep[j] = false;
-            key[j] = 0;
-            if (gid[j] < inc.n_gauss) {
-                const uint4 b0 = inc.bin0[gid[j]];
-                if (rect_contains(b0, tx, ty)) {
-                    const float4 b1 = inc.bin1[gid[j]];
-                    const float d = tile_depth(tx, ty, inc.tw, inc.th, b1.x, b1.y, b1.z, b1.w, b0.w);
-                    key[j] = ((uint64_t)__float_as_uint(d) << 32) | gid[j];
-                    keep[j] = true;
-                    ++cnt;
-                }
-            }
+            keep[j] = gid[j] < inc.n_gauss && rect_contains(b0[j], tx, ty);
+            const float d = tile_depth(tx, ty, inc.tw, inc.th, b1[j].x, b1[j].y, b1[j].z, b1[j].w, b0[j].w);
+            key[j] = ((uint64_t)__float_as_uint(d) << 32) | gid[j];
+            cnt += keep[j] ? 1 : 0;
         }
         // CTA exclusive scan of the per-thread counts
         uint32_t incl = (uint32_t)cnt;
@@ -204,14 +209,55 @@ __device__ int gather_tile(uint64_t* dst, uint32_t tile, int n_cap, const SegSor
         const int pos = kept + i;
         if (pos < n_cap) dst[SMEM ? spad(pos) : pos] = inc.enter_keys[re.x + i];
     }
+    *n_kept = kept;
     return kept + ne;
 }
 
+// Nearly sorted survivors: bounded odd-even transposition passes over
+// s[0..ns).  Returns true (uniformly) once a pass of each parity found nothing
+// to swap, false when the pass budget ran out first.
+constexpr int kFixMaxPasses = 24;
+constexpr int kFixMaxDescents = 64;
+constexpr int kMaxEntering = 32;
+__device__ bool odd_even_fix(uint64_t* s, int ns) {
+    int quiet = 0;
+    for (int pass = 0; pass < kFixMaxPasses; ++pass) {
+        bool swapped = false;
+        for (int i = 2 * (int)threadIdx.x + (pass & 1); i + 1 < ns; i += 2 * kSegThreads) {
+            const uint64_t a = s[spad(i)], b = s[spad(i + 1)];
+            if (a > b) {
+                s[spad(i)] = b;
+                s[spad(i + 1)] = a;
+                swapped = true;
+            }
+        }
+        if (__syncthreads_or(swapped))
+            quiet = 0;
+        else if (++quiet == 2)
+            return true;
+    }
+    return false;
+}
+
+// Number of keys of the sorted s[base..base+len) below key (keys are unique).
+__device__ __forceinline__ int rank_in(const uint64_t* s, int base, int len, uint64_t key) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s[spad(base + mid)] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, const uint2* __restrict__ ranges,
-                                                              uint32_t* vals, uint64_t* keys, SegSortWork w,
-                                                              DevStatus* st, SegSortIncr inc) {
+                                                              uint32_t* vals, SegSortWork w, DevStatus* st,
+                                                              SegSortIncr inc) {
     __shared__ uint64_t s[kSegCap + kSegCap / 16];
     __shared__ uint32_t s_wsum[kSegThreads / 32];
+    __shared__ int s_desc;
     if (st->flags & kErrOverflow) return;
     const bool incr = st->mode == kBinIncremental;
     const uint32_t tile = blockIdx.x;
@@ -220,7 +266,8 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, co
     if (n <= 0) return;
     if (n > kSegCap) {
         if (incr) {
-            const int got = gather_tile<false>(comp + r.x, tile, n, inc, s_wsum);
+            int kept;
+            const int got = gather_tile<false>(comp + r.x, tile, n, inc, s_wsum, &kept);
             if (got != n && threadIdx.x == 0) atomicOr(&st->flags, kErrBounds);
         }
         if (threadIdx.x == 0) w.large_list[atomicAdd(&w.large_ctrl[0], 1u)] = tile;
@@ -228,15 +275,49 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, co
     }
     const int m = (n + kSegItems - 1) / kSegItems * kSegItems;
     if (incr) {
-        const int got = gather_tile<true>(s, tile, n, inc, s_wsum);
+        int kept;
+        const int got = gather_tile<true>(s, tile, n, inc, s_wsum, &kept);
         if (got != n && threadIdx.x == 0) atomicOr(&st->flags, kErrBounds);
+        const int ns = min(kept, n), ne = n - ns;
+        if (threadIdx.x == 0) s_desc = 0;
+        __syncthreads();
+        int desc = 0;
+        for (int i = threadIdx.x; i + 1 < ns; i += kSegThreads) desc += s[spad(i)] > s[spad(i + 1)] ? 1 : 0;
+        if (desc) atomicAdd(&s_desc, desc);
+        __syncthreads();
+        const int n_desc = s_desc;
+        bool fixed = ne <= kMaxEntering && n_desc <= kFixMaxDescents;
+        if (fixed && n_desc > 0) fixed = odd_even_fix(s, ns);
+        if (fixed) {
+            // survivors sorted: rank the few entering keys among themselves,
+            // then every key goes straight to its merged position
+            if (ne > 1 && threadIdx.x < 32) {
+                const int j = threadIdx.x;
+                const uint64_t key = j < ne ? s[spad(ns + j)] : kKeyInf;
+                int rank = 0;
+                for (int q = 0; q < ne; ++q) rank += s[spad(ns + q)] < key ? 1 : 0;
+                __syncwarp();
+                if (j < ne) s[spad(ns + rank)] = key;
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < ns; i += kSegThreads) {
+                const uint64_t key = s[spad(i)];
+                const int before = ne ? rank_in(s, ns, ne, key) : 0;
+                write_sorted(key, r.x + i + before, vals);
+            }
+            for (int j = threadIdx.x; j < ne; j += kSegThreads) {
+                const uint64_t key = s[spad(ns + j)];
+                write_sorted(key, r.x + j + rank_in(s, 0, ns, key), vals);
+            }
+            return;
+        }
         if (threadIdx.x < m - n) s[spad(n + threadIdx.x)] = kKeyInf;
     } else {
         for (int i = threadIdx.x; i < m; i += kSegThreads) s[spad(i)] = i < n ? comp[r.x + i] : kKeyInf;
     }
     __syncthreads();
     block_merge_sort(s, m);
-    for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(s[spad(i)], tile, r.x + i, vals, keys);
+    for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(s[spad(i)], r.x + i, vals);
 }
 
 // Large buckets: persistent CTAs take listed tiles; each sorts 4096-key
@@ -244,8 +325,7 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, co
 // (every thread merges kSegItems outputs after its own merge-path search).
 __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* comp, uint64_t* tmp,
                                                                     const uint2* __restrict__ ranges, uint32_t* vals,
-                                                                    uint64_t* keys, SegSortWork w,
-                                                                    const DevStatus* st) {
+                                                                    SegSortWork w, const DevStatus* st) {
     __shared__ uint64_t s[kSegCap + kSegCap / 16];
     __shared__ uint32_t s_idx;
     if (st->flags & kErrOverflow) return;
@@ -302,19 +382,43 @@ __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* co
             src = dst;
             dst = tsw;
         }
-        for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(src[i], tile, r.x + i, vals, keys);
+        for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(src[i], r.x + i, vals);
         __syncthreads();
     }
 }
 
 cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, int num_tiles, uint32_t* vals,
-                           uint64_t* keys, SegSortWork w, const DevStatus* st, int large_grid,
-                           const SegSortIncr& inc, cudaStream_t s) {
+                           SegSortWork w, const DevStatus* st, int large_grid, const SegSortIncr& inc,
+                           cudaStream_t s) {
     if (num_tiles <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(w.large_ctrl, 0, 2 * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, keys, w, const_cast<DevStatus*>(st), inc);
-    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(comp, tmp, ranges, vals, keys, w, st);
+    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, w, const_cast<DevStatus*>(st), inc);
+    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(comp, tmp, ranges, vals, w, st);
+    return cudaGetLastError();
+}
+
+// One CTA per tile: key = tile << 32 | bits of the tile-centre depth of the
+// Gaussian at each sorted position.
+__global__ void __launch_bounds__(256) make_keys_kernel(const BinRec* __restrict__ bins,
+                                                        const uint2* __restrict__ ranges,
+                                                        const uint32_t* __restrict__ vals, int ntx, int tw, int th,
+                                                        const DevStatus* st, uint64_t* keys) {
+    if (st->flags & kErrOverflow) return;
+    const uint32_t tile = blockIdx.x;
+    const uint2 r = ranges[tile];
+    const int tx = (int)(tile % (uint32_t)ntx), ty = (int)(tile / (uint32_t)ntx);
+    for (uint32_t i = r.x + threadIdx.x; i < r.y; i += blockDim.x) {
+        const BinRec b = bins[vals[i]];
+        const float d = tile_depth(tx, ty, tw, th, b.p.x, b.p.y, b.p.z, b.p.w, b.r.w);
+        keys[i] = ((uint64_t)tile << 32) | __float_as_uint(d);
+    }
+}
+
+cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, int num_tiles, int ntx,
+                             int tw, int th, const DevStatus* st, uint64_t* keys, cudaStream_t s) {
+    if (num_tiles <= 0) return cudaSuccess;
+    make_keys_kernel<<<num_tiles, 256, 0, s>>>(bins, ranges, vals, ntx, tw, th, st, keys);
     return cudaGetLastError();
 }
 
