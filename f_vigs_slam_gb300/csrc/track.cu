@@ -21,8 +21,12 @@
 //  * the 27 per-thread sums are reduced by a 31-shuffle butterfly
 //    reduce-scatter, then across the 8 warps in a fixed order, and written
 //    once per tile (no atomics: results are run-to-run deterministic).
+#include <cooperative_groups.h>
+
 #include "fvgs_device.cuh"
 #include "fvgs_launch.h"
+
+namespace cg = cooperative_groups;
 
 namespace fvgs {
 
@@ -209,7 +213,7 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
 }
 
 template <bool RENDER_ONLY, bool REF_LAYOUT = false>
-__global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
+__global__ void __launch_bounds__(kPix, 4) track_tile_kernel(TrackArgs a) {
     __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
@@ -217,7 +221,9 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int tid = threadIdx.x;
-    const int x = tx * kTW + (tid & (kTW - 1)), y = ty * kTH + tid / kTW;
+    // each warp covers an 8 x 4 pixel block (compact footprint: less divergence)
+    const int wq = tid >> 5, lq = tid & 31;
+    const int x = tx * kTW + (wq & 1) * 8 + (lq & 7), y = ty * kTH + (wq >> 1) * 4 + (lq >> 3);
     const float x0 = (float)(tx * kTW), y0 = (float)(ty * kTH);
     const bool in_bounds = (x < a.W && y < a.H);
     const size_t p = (size_t)y * a.W + x;
@@ -240,6 +246,7 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
             if (__syncthreads_and(done)) break;
             const int cnt = stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
+                int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
                 auto blend = [&](int j, float dx, float dy, float v) -> bool {
                     const float4 rB = sb.B[j];
@@ -253,7 +260,7 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
                     cb += sb.D[j] * alpha * T;
                     if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, dx, rC.x, dy, rC.y);
                     T = test_T;
-                    last = (uint32_t)sb.orig[j] + 1u;
+                    last_j = j;
                     return true;
                 };
                 int j = 0;
@@ -285,6 +292,7 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
                     const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
                     if (!(v > rB.y || v <= 0.0f) && !blend(j, dx, dy, v)) done = true;
                 }
+                if (last_j >= 0) last = (uint32_t)sb.orig[last_j] + 1u;
             }
         }
         if (inside) {
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
         const float closs = sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
         wc = (closs < a.color_thresh) ? 1.0f : a.color_thresh / closs;
         const float rx = (xf - cx) / fx, ry = (yf - cy) / fy;
-        const float inv_id = 1.0f / img_depth;
+        const float inv_id = __frcp_rn(img_depth);
         const float j0 = fx * inv_id, j3 = fy * inv_id, j4 = -fx * rx * inv_id, j5 = -fy * ry * inv_id;
         const float gX[3] = {a.gx[3 * p], a.gx[3 * p + 1], a.gx[3 * p + 2]};
         const float gY[3] = {a.gy[3 * p], a.gy[3 * p + 1], a.gy[3 * p + 2]};
@@ -374,7 +382,7 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
     const int nmax = (int)min((uint32_t)n, s_nmax);
     float prod_alpha = 1.f, Tm = 1.f, acr = 0.f, acg = 0.f, acb = 0.f;
     bool done2 = !do_jac;
-    const float inv_fx = 1.0f / fx, inv_fy = 1.0f / fy;
+    const float inv_fx = __frcp_rn(fx), inv_fy = __frcp_rn(fy);
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
         const int cnt = stage_batch<REF_LAYOUT, false>(a, sb, range.x, base, nmax, x0, y0);
@@ -397,14 +405,14 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
                 acr += alpha * da0;
                 acg += alpha * da1;
                 acb += alpha * da2;
-                const float inv1m = 1.0f / (1.0f - alpha);
+                const float inv1m = __frcp_rn(1.0f - alpha);  // == 1.0f / x, correctly rounded
                 da0 -= (cr - acr) * inv1m;
                 da1 -= (cg - acg) * inv1m;
                 da2 -= (cb - acb) * inv1m;
                 const float dl0 = rA.z * dx + rA.w * dy;
                 const float dl1 = rA.w * dx + rB.x * dy;
                 const float rgx = (rA.x - cx) * inv_fx, rgy = (rA.y - cy) * inv_fy;
-                const float inv_d = 1.0f / d;
+                const float inv_d = __frcp_rn(d);
                 const float jt0 = fx * inv_d * dl0;
                 const float jt1 = fy * inv_d * dl1;
                 const float jt2 = (-fx * rgx * inv_d) * dl0 + (-fy * rgy * inv_d) * dl1;
@@ -460,22 +468,6 @@ __global__ void __launch_bounds__(kPix, 3) track_tile_kernel(TrackArgs a) {
         for (int w = 0; w < kPix / 32; ++w) s += s_red[w][tid];
         a.tile_out[(size_t)tile * FVGS_POSEDATA_FLOATS + tid] = s;
     }
-}
-
-// Butterfly reduce-scatter of 32 doubles (lane l ends with value l's sum).
-__device__ __forceinline__ double warp_reduce_scatter32d(double (&v)[32]) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        const bool upper = (lane & o) != 0;
-#pragma unroll
-        for (int k = 0; k < o; ++k) {
-            const double send = upper ? v[k] : v[k + o];
-            const double keep = upper ? v[k + o] : v[k];
-            v[k] = keep + __shfl_xor_sync(kFullMask, send, o);
-        }
-    }
-    return v[0];
 }
 
 // Cholesky of a symmetric 6x6 (lower factor in L); false if not positive
@@ -604,33 +596,36 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 // l = i (i + 1) / 2 + j.
 __device__ __forceinline__ int tri_index(int i, int j) { return i * (i + 1) / 2 + j; }
 
-// Warp-parallel Cholesky of a symmetric 6x6 held as one lower-triangle entry
-// per lane (lanes >= 21 idle).  On return lane tri_index(i, j) holds L[i][j];
-// returns false (uniformly) if a pivot is not positive.
-__device__ __forceinline__ bool warp_chol6(double& m, int li, int lj) {
+// Warp-parallel LDL^T factorisation of a symmetric 6x6 held as one
+// lower-triangle entry per lane (lanes >= 21 idle), without square roots: on
+// return lane tri_index(i, j) holds L[i][j] (i > j, unit diagonal implied) or
+// D[i] (i == j).  Returns false (uniformly) when a pivot is not positive, i.e.
+// the matrix is not positive definite.
+__device__ __forceinline__ bool warp_ldl6(double& m, int li, int lj) {
     const int lane = threadIdx.x & 31;
     const bool act = lane < 21;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        const double dkk = shfl_d(m, tri_index(k, k));
-        if (!(dkk > 0.0)) return false;
-        const double s = sqrt(dkk);
-        const double inv = 1.0 / s;
-        if (act && lj == k) m = (li == k) ? s : m * inv;
-        // trailing update m(i, j) -= L(i, k) L(j, k) for j > k
-        const double lik = shfl_d(m, act ? tri_index(li, k) : 0);
+        const double dk = shfl_d(m, tri_index(k, k));
+        if (!(dk > 0.0)) return false;
+        const double inv = __drcp_rn(dk);
+        // entries still holding L(i, k) D(k) for i > k
+        const double lik = shfl_d(m, (act && li > k) ? tri_index(li, k) : 0);
         const double ljk = shfl_d(m, (act && lj > k) ? tri_index(lj, k) : 0);
-        if (act && lj > k) m = fma(-lik, ljk, m);
+        if (act && lj > k) m = fma(-lik * inv, ljk, m);
+        if (act && lj == k && li > k) m *= inv;
     }
     return true;
 }
 
-// Frame reduction + (optionally) the Gauss-Newton pose update, one CTA:
-// tiles are summed in a fixed order (thread t: tiles t, t+256, ... in
-// Kahan-compensated FP32; then FP64 across lanes and warps), rotated to the
-// world frame by diag(R, I), written as out[42] = JtJ[36] symmetric, Jtr[6]
-// negated (src/GSSlam.cu:2205-2226); then the pseudo-factor step of
-// RgbdPoseCostFunction (src/RgbdPoseCost.cu:57-78) and
+// Frame reduction + (optionally) the Gauss-Newton pose update, one cluster of
+// kRedCtas CTAs: warp k of the cluster sums tiles k, k + 8 kRedCtas, ... with
+// lane l < 27 holding column l (Kahan-compensated FP32, fixed order), the
+// CTA combines its warps in FP64, and CTA 0 gathers the CTAs' sums over
+// distributed shared memory in rank order (deterministic).  The total is
+// rotated to the world frame by diag(R, I) and written as out[42] = JtJ[36]
+// symmetric, Jtr[6] negated (src/GSSlam.cu:2205-2226); then the pseudo-factor
+// step of RgbdPoseCostFunction (src/RgbdPoseCost.cu:57-78) and
 // PoseLocalParameterization::Plus on the device pose.
 //
 // FP64 is issued slowly on this part, so the 6x6 work is spread over lanes:
@@ -638,65 +633,62 @@ __device__ __forceinline__ bool warp_chol6(double& m, int li, int lj) {
 // definite, and then the eigen-regularised step equals -H^-1 g), warp 1 factors
 // H and solves; only a failed test falls back to a one-thread Jacobi
 // eigen-decomposition that drops the small eigenvalues.
+constexpr int kRedCtas = 8;
+constexpr int kRedUnroll = 8;
 template <bool DO_GN>
-__global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles,
-                                                           DevPose* pose, double* out, double eig_eps,
-                                                           double* step_out) {
+__global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
+    track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles, DevPose* pose, double* out,
+                        double eig_eps, double* step_out) {
     __shared__ double s_w[8][32];
+    __shared__ double s_part[32];
     __shared__ double s_tot[27];
     __shared__ double s_R[9];
     __shared__ int s_pd;
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    float sum[27], comp[27];
+    const int col = lane < FVGS_POSEDATA_FLOATS ? lane : 0;
+    const int stride = kRedCtas * 8;
+    float sum = 0.f, comp = 0.f;
+    int t = (int)rank * 8 + w;
+    for (; t + (kRedUnroll - 1) * stride < num_tiles; t += kRedUnroll * stride) {
+        float x[kRedUnroll];
 #pragma unroll
-    for (int k = 0; k < 27; ++k) {
-        sum[k] = 0.f;
-        comp[k] = 0.f;
-    }
-    for (int t = tid; t < num_tiles; t += 256) {
-        const float* row = tile_out + (size_t)t * 27;
+        for (int u = 0; u < kRedUnroll; ++u) x[u] = tile_out[(size_t)(t + u * stride) * FVGS_POSEDATA_FLOATS + col];
 #pragma unroll
-        for (int k = 0; k < 27; ++k) {
-            const float y = __fsub_rn(row[k], comp[k]);
-            const float s = __fadd_rn(sum[k], y);
-            comp[k] = __fsub_rn(__fsub_rn(s, sum[k]), y);
-            sum[k] = s;
+        for (int u = 0; u < kRedUnroll; ++u) {
+            const float y = __fsub_rn(x[u], comp);
+            const float s = __fadd_rn(sum, y);
+            comp = __fsub_rn(__fsub_rn(s, sum), y);
+            sum = s;
         }
     }
-    double v[32];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) v[k] = (double)sum[k] - (double)comp[k];
-#pragma unroll
-    for (int k = 27; k < 32; ++k) v[k] = 0.0;
-    s_w[w][lane] = warp_reduce_scatter32d(v);
+    for (; t < num_tiles; t += stride) {
+        const float y = __fsub_rn(tile_out[(size_t)t * FVGS_POSEDATA_FLOATS + col], comp);
+        const float s = __fadd_rn(sum, y);
+        comp = __fsub_rn(__fsub_rn(s, sum), y);
+        sum = s;
+    }
+    s_w[w][lane] = lane < FVGS_POSEDATA_FLOATS ? (double)sum - (double)comp : 0.0;
     __syncthreads();
-    if (w >= 2) return;
-    // ---- warps 0 and 1 only; named barrier 1 over 64 threads ----
-    if (w == 0 && lane < 27) {
-        double s = 0.0;
+    if (w == 0) {
+        double c = 0.0;
 #pragma unroll
-        for (int ww = 0; ww < 8; ++ww) s += s_w[ww][lane];
-        s_tot[lane] = s;
+        for (int ww = 0; ww < 8; ++ww) c += s_w[ww][lane];
+        s_part[lane] = c;
     }
-    if (w == 1 && lane < 9) {
-        const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
-        const int i = lane / 3, j = lane % 3;
-        const double q[3] = {qx, qy, qz};
-        double r;
-        if (i == j) {
-            const double a = q[(i + 1) % 3], b = q[(i + 2) % 3];
-            r = 1.0 - 2.0 * (a * a + b * b);
-        } else {
-            // off-diagonal: 2 (q_i q_j -/+ w q_k), sign + when (i, j) is (1,0), (2,1), (0,2)
-            const int k = 3 - i - j;
-            const bool plus = (i == (j + 1) % 3);
-            r = 2.0 * (q[i] * q[j] + (plus ? qw * q[k] : -qw * q[k]));
-        }
-        s_R[lane] = r;
+    cluster.sync();  // every CTA's column sums are visible cluster-wide
+    if (rank == 0 && w == 0 && lane < FVGS_POSEDATA_FLOATS) {
+        double c = 0.0;
+#pragma unroll
+        for (int r = 0; r < kRedCtas; ++r) c += cluster.map_shared_rank(s_part, r)[lane];
+        s_tot[lane] = c;
     }
-    asm volatile("bar.sync 1, 64;" ::: "memory");
-    // lane l < 21: H entry (li, lj) of H = D A D^T, D = diag(R, I);
-    // lanes 21..26: g = -(D b)
+    cluster.sync();  // CTA 0 has read the remote sums; the others may leave
+    if (rank != 0) return;
+    if (w >= 2) return;
+    // ---- CTA 0, warps 0 and 1 only; named barrier 1 over 64 threads ----
+    // lane l < 21 holds lower-triangle entry (li, lj) of a symmetric 6x6
     int li = 0, lj = 0;
     if (lane < 21) {
         while (tri_index(li + 1, 0) <= lane) ++li;
@@ -704,98 +696,120 @@ __global__ void __launch_bounds__(256) track_reduce_kernel(const float* __restri
     }
     auto Ac = [&](int a, int b) {
         const int hi = a > b ? a : b, lo = a > b ? b : a;
-        // upper-triangle row-major index of (lo, hi)
+        // upper-triangle row-major index of (lo, hi) among the 21 JtJ sums
         return s_tot[6 + lo * 6 - lo * (lo - 1) / 2 + (hi - lo)];
     };
-    double m = 0.0, gval = 0.0;
-    if (lane < 21) {
-        if (li < 3) {  // then lj < 3
-            double s = 0.0;
-#pragma unroll
-            for (int a2 = 0; a2 < 3; ++a2)
-#pragma unroll
-                for (int b2 = 0; b2 < 3; ++b2) s = fma(s_R[li * 3 + a2] * Ac(a2, b2), s_R[lj * 3 + b2], s);
-            m = s;
-        } else if (lj < 3) {
-            double s = 0.0;
-#pragma unroll
-            for (int b2 = 0; b2 < 3; ++b2) s = fma(Ac(li, b2), s_R[lj * 3 + b2], s);
-            m = s;
-        } else {
-            m = Ac(li, lj);
+    if (!DO_GN) {
+        // world-frame JtJ = D A D^T and Jtr = -(D b), D = diag(R, I)
+        if (w == 1 && lane < 9) {
+            const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+            const int i = lane / 3, j = lane % 3;
+            const double q[3] = {qx, qy, qz};
+            double r;
+            if (i == j) {
+                const double a = q[(i + 1) % 3], b2 = q[(i + 2) % 3];
+                r = 1.0 - 2.0 * (a * a + b2 * b2);
+            } else {
+                // off-diagonal: 2 (q_i q_j -/+ w q_k), sign + when (i, j) is (1,0), (2,1), (0,2)
+                const int k = 3 - i - j;
+                const bool plus = (i == (j + 1) % 3);
+                r = 2.0 * (q[i] * q[j] + (plus ? qw * q[k] : -qw * q[k]));
+            }
+            s_R[lane] = r;
         }
-    } else if (lane < 27) {
-        const int i = lane - 21;
-        if (i < 3)
-            gval = -(s_R[i * 3] * s_tot[0] + s_R[i * 3 + 1] * s_tot[1] + s_R[i * 3 + 2] * s_tot[2]);
-        else
-            gval = -s_tot[i];
-    }
-    if (w == 0) {
-        // full symmetric JtJ and Jtr to the output
+        asm volatile("bar.sync 1, 64;" ::: "memory");
+        if (w != 0) return;
         if (lane < 21) {
+            double m;
+            if (li < 3) {  // then lj < 3
+                double s = 0.0;
+#pragma unroll
+                for (int a2 = 0; a2 < 3; ++a2)
+#pragma unroll
+                    for (int b2 = 0; b2 < 3; ++b2) s = fma(s_R[li * 3 + a2] * Ac(a2, b2), s_R[lj * 3 + b2], s);
+                m = s;
+            } else if (lj < 3) {
+                double s = 0.0;
+#pragma unroll
+                for (int b2 = 0; b2 < 3; ++b2) s = fma(Ac(li, b2), s_R[lj * 3 + b2], s);
+                m = s;
+            } else {
+                m = Ac(li, lj);
+            }
             out[li * 6 + lj] = m;
             out[lj * 6 + li] = m;
         } else if (lane < 27) {
-            out[36 + lane - 21] = gval;
+            const int i = lane - 21;
+            out[36 + i] = i < 3 ? -(s_R[i * 3] * s_tot[0] + s_R[i * 3 + 1] * s_tot[1] + s_R[i * 3 + 2] * s_tot[2])
+                                : -s_tot[i];
         }
+        return;
     }
-    if (!DO_GN) return;
+    // Gauss-Newton step.  With H = D A D^T and g = -(D b) the step
+    // -H^-1 g equals D x for A x = b, and H, A share their eigenvalues, so the
+    // camera-frame system is factored and only the step is rotated.
+    double m = lane < 21 ? Ac(li, lj) : 0.0;
     if (w == 0) {
-        double me = m;
-        if (lane < 21 && li == lj) me -= eig_eps;
-        const bool pd = warp_chol6(me, li, lj);
+        if (lane < 21 && li == lj) m -= eig_eps;
+        const bool pd = warp_ldl6(m, li, lj);
         if (lane == 0) s_pd = pd ? 1 : 0;
         asm volatile("bar.sync 1, 64;" ::: "memory");
         return;
     }
     // warp 1
-    double mh = m;
-    const bool pdh = warp_chol6(mh, li, lj);
+    const bool pdh = warp_ldl6(m, li, lj);
     asm volatile("bar.sync 1, 64;" ::: "memory");
-    double delta_lane = 0.0;  // lane k < 6 ends with delta[k]
+    double xv = lane < 6 ? s_tot[lane] : 0.0;  // lane k < 6 ends with x[k]
     if (s_pd && pdh) {
-        // forward substitution L y = g (lane k holds g_k / y_k)
-        double yv = shfl_d(gval, (lane < 6) ? lane + 21 : 21);
+        // L y = b (unit lower)
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            const double lkk = shfl_d(mh, tri_index(k, k));
-            const double yk = shfl_d(yv, k) / lkk;
-            if (lane == k) yv = yk;
-            const double lik = shfl_d(mh, (lane < 6 && lane > k) ? tri_index(lane, k) : 0);
-            if (lane < 6 && lane > k) yv = fma(-lik, yk, yv);
+            const double yk = shfl_d(xv, k);
+            const double lik = shfl_d(m, (lane < 6 && lane > k) ? tri_index(lane, k) : 0);
+            if (lane < 6 && lane > k) xv = fma(-lik, yk, xv);
         }
-        // back substitution L^T x = y
+        // D z = y
+        const double dl = shfl_d(m, lane < 6 ? tri_index(lane, lane) : 0);
+        if (lane < 6) xv = xv / dl;
+        // L^T x = z (unit upper)
 #pragma unroll
         for (int k = 5; k >= 0; --k) {
-            const double lkk = shfl_d(mh, tri_index(k, k));
-            const double xk = shfl_d(yv, k) / lkk;
-            if (lane == k) yv = xk;
-            const double lki = shfl_d(mh, (lane < k) ? tri_index(k, lane) : 0);
-            if (lane < k) yv = fma(-lki, xk, yv);
+            const double xk = shfl_d(xv, k);
+            const double lki = shfl_d(m, (lane < k) ? tri_index(k, lane) : 0);
+            if (lane < k) xv = fma(-lki, xk, xv);
         }
-        delta_lane = -yv;
     } else {
         // rare: some eigenvalue <= eps -- exact eigen-decomposition on one lane
         double dl[6] = {0, 0, 0, 0, 0, 0};
         if (lane == 0) {
-            double H[6][6], g[6];
+            double A[6][6], g[6];
             for (int i = 0; i < 6; ++i) {
-                for (int j = 0; j < 6; ++j) H[i][j] = out[i * 6 + j];
-                g[i] = out[36 + i];
+                for (int j = 0; j < 6; ++j) A[i][j] = Ac(i, j);
+                g[i] = -s_tot[i];
             }
-            pseudo_step(H, g, eig_eps, dl);
+            pseudo_step(A, g, eig_eps, dl);
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const double d = shfl_d(dl[k], 0);
-            if (lane == k) delta_lane = d;
+            if (lane == k) xv = d;
         }
     }
+    double x[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) x[k] = shfl_d(xv, k);
+    if (lane != 0) return;
+    // delta = (R x_t, x_r), R of the pose the Jacobians were taken at
+    const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+    const double R[3][3] = {
+        {1.0 - 2.0 * (qy * qy + qz * qz), 2.0 * (qx * qy - qw * qz), 2.0 * (qx * qz + qw * qy)},
+        {2.0 * (qx * qy + qw * qz), 1.0 - 2.0 * (qx * qx + qz * qz), 2.0 * (qy * qz - qw * qx)},
+        {2.0 * (qx * qz - qw * qy), 2.0 * (qy * qz + qw * qx), 1.0 - 2.0 * (qx * qx + qy * qy)}};
     double delta[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) delta[k] = shfl_d(delta_lane, k);
-    if (lane != 0) return;
+    for (int i = 0; i < 3; ++i) delta[i] = R[i][0] * x[0] + R[i][1] * x[1] + R[i][2] * x[2];
+#pragma unroll
+    for (int i = 3; i < 6; ++i) delta[i] = x[i];
 #pragma unroll
     for (int k = 0; k < 3; ++k) pose->td[k] += delta[k];
     const double ax = pose->qd[0], ay = pose->qd[1], az = pose->qd[2], aw = pose->qd[3];
@@ -843,13 +857,13 @@ cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s) {
 
 cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                 cudaStream_t s) {
-    track_reduce_kernel<false><<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out, 0.0, nullptr);
+    track_reduce_kernel<false><<<kRedCtas, 256, 0, s>>>(tile_out, num_tiles, pose, out, 0.0, nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                    double eig_eps, double* step_out, cudaStream_t s) {
-    track_reduce_kernel<true><<<1, 256, 0, s>>>(tile_out, num_tiles, pose, out, eig_eps, step_out);
+    track_reduce_kernel<true><<<kRedCtas, 256, 0, s>>>(tile_out, num_tiles, pose, out, eig_eps, step_out);
     return cudaGetLastError();
 }
 
