@@ -38,10 +38,10 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
     float R[3][3];
     quat_to_R(qc, R);
+    // Only the position is needed to decide visibility; scale, rotation and
+    // colour are loaded for the Gaussians that need them (most of a large
+    // map is outside any one view).
     const float4 p = a.pos[i];
-    const float4 s = a.scale[i];
-    const float4 qg4 = a.rot[i];
-    const float4 co = a.col[i];
     const fvgs_intrinsics K = a.K;
 
     float u = 0.f, v = 0.f, z = 0.f, cxx = 0.f, cyy = 0.f, cxy = 0.f;
@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
                 u = uu;
                 v = vv;
                 z = pcz;
+                const float4 s = a.scale[i];
+                const float4 qg4 = a.rot[i];
                 const float qg[4] = {qg4.x, qg4.y, qg4.z, qg4.w};
                 float Rg[3][3];
                 quat_to_R(qg, Rg);
@@ -148,6 +150,7 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     // culled Gaussians blend (with the zero record), and the host reports
     // zeros for them.
     if (count && (visible || (a.quirks & FVGS_Q_CULLED_SLOTS))) {
+        const float4 co = a.col[i];
         const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
         a.rec0[i] = make_float4(u, v, z, co.w);
         a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);
@@ -617,10 +620,19 @@ __device__ __forceinline__ void scatter_chunks(const EmitArgs& a, uint32_t* fill
                                                uint32_t n_items, uint32_t* chunk_counter) {
     const int lane = threadIdx.x & 31;
     const uint32_t n_chunks = (n_items + 31) / 32;
+    // Incremental mode has a few chunks: static assignment, so the idle warps
+    // leave without touching the shared counter.
+    const uint32_t warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t next = warp_id;
     for (;;) {
-        uint32_t chunk = 0;
-        if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
-        chunk = __shfl_sync(kFullMask, chunk, 0);
+        uint32_t chunk = next;
+        if (INCR) {
+            next += n_warps;
+        } else {
+            if (lane == 0) chunk = atomicAdd(chunk_counter, 1u);
+            chunk = __shfl_sync(kFullMask, chunk, 0);
+        }
         if (chunk >= n_chunks) return;
         walk_instances<INCR>(a, chunk * 32, n_items, [&](const uint32_t* tiles, const uint64_t* keys, const bool* ok) {
             uint32_t slot[kWalkBatch];

@@ -417,7 +417,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         if (P.quirks & FVGS_Q_RANGE_LAUNCH) {
             // the literal range pass reads the reference-format keys
             KScope k(s, FVGS_K_RANGES, 2);
-            FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, T, ntx, P.tile_w, P.tile_h, s->st, s->keys,
+            FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, T, ntx, P.tile_w, P.tile_h, s->st, s->keys,
                                    s->stream));
             FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
             s->keys_valid = true;
@@ -465,6 +465,8 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
     ta.rec2 = s->rec2;
     ta.ranges = s->ranges;
     ta.indices = s->vals;
+    ta.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+    ta.n_gauss = s->n_g;
     ta.obs_rgb = f.rgb;
     ta.obs_depth = f.depth;
     ta.gx = f.gx;
@@ -565,6 +567,8 @@ int enqueue_map(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, 
     ma.rec2 = s->rec2;
     ma.ranges = s->ranges;
     ma.indices = s->vals;
+    ma.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+    ma.n_gauss = s->n_g;
     ma.obs_rgb = f.rgb;
     ma.obs_depth = f.depth;
     ma.W = f.W;
@@ -961,8 +965,8 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
     if ((keys || values) && n > max_instances) return FVGS_E_CAPACITY;
     if (keys && n && !s->keys_valid) {
         const int ntx = (s->last_W + s->params.tile_w - 1) / s->params.tile_w;
-        FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->last_T, ntx, s->params.tile_w, s->params.tile_h, s->st,
-                               s->keys, s->stream));
+        FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, s->last_T, ntx, s->params.tile_w,
+                               s->params.tile_h, s->st, s->keys, s->stream));
         s->keys_valid = true;
     }
     if (keys && n) FV_CK(cudaMemcpyAsync(keys, s->keys, sizeof(uint64_t) * n, cudaMemcpyDefault, s->stream));

@@ -114,8 +114,9 @@ cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, i
 // Reference-format keys (tile << 32 | depth bits) of a tile-bucket binning,
 // rebuilt from its ranges, sorted indices and binning records with the
 // emission's arithmetic (the tracking path itself never reads them).
-cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, int num_tiles, int ntx,
-                             int tw, int th, const DevStatus* st, uint64_t* keys, cudaStream_t s);
+cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, uint32_t n_gauss,
+                             int num_tiles, int ntx, int tw, int th, const DevStatus* st, uint64_t* keys,
+                             cudaStream_t s);
 
 // ---- radix sort (sort.cu) ----
 struct SortWorkspace {
@@ -146,6 +147,10 @@ struct TrackArgs {
     const float4* rec2;
     const uint2* ranges;
     const uint32_t* indices;
+    // list entries at or beyond n_list and indices at or above n_gauss are
+    // skipped (defensive: the binning never produces them)
+    uint32_t n_list;
+    uint32_t n_gauss;
     const float* obs_rgb;    // 3P
     const float* obs_depth;  // P
     const float* gx;         // 3P
@@ -193,6 +198,8 @@ struct MapArgs {
     const float4* rec2;
     const uint2* ranges;
     const uint32_t* indices;
+    uint32_t n_list;   // as TrackArgs
+    uint32_t n_gauss;
     const float* obs_rgb;    // 3P
     const float* obs_depth;  // P
     int W, H, ntx, nty;

@@ -38,8 +38,9 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
     const int tid = threadIdx.x;
     const int x = tx * 16 + (tid & 15), y = ty * 16 + (tid >> 4);
     const bool inside = (x < a.W && y < a.H);
-    const uint2 range = a.ranges[tile];
-    const int n = (int)(range.y - range.x);
+    uint2 range = a.ranges[tile];
+    range.y = min(range.y, a.n_list);
+    const int n = range.y > range.x ? (int)(range.y - range.x) : 0;
     const uint32_t base_slot = CAP ? (uint32_t)tile * kCapBuckets : a.bucket_base[tile];
     const float xf = (float)x, yf = (float)y;
     if (tid == 0) s_max = 0;
@@ -51,9 +52,10 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
         const int li = base + tid;
         if (li < n) {
             const uint32_t g = a.indices[range.x + li];
-            s0[tid] = a.rec0[g];
-            s1[tid] = a.rec1[g];
-            s2[tid] = a.rec2[g];
+            const bool ok = g < a.n_gauss;  // zero opacity otherwise: never blends
+            s0[tid] = ok ? a.rec0[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s1[tid] = ok ? a.rec1[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s2[tid] = ok ? a.rec2[g] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         __syncthreads();
         if (!done) {
@@ -113,8 +115,9 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint2 range = a.ranges[tile];
-    const uint32_t n = range.y - range.x;
+    uint2 range = a.ranges[tile];
+    range.y = min(range.y, a.n_list);
+    const uint32_t n = range.y > range.x ? range.y - range.x : 0u;
     const uint32_t maxc = a.max_contrib[tile];
     uint32_t nb = (n + 31) / 32;
     if (CAP) nb = min(nb, (uint32_t)kCapBuckets);
@@ -137,11 +140,14 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
     for (uint32_t b = warp; b < nb; b += kMPix / 32) {
         if (b * 32 >= maxc) break;
         const uint32_t j = b * 32 + lane;
-        const bool valid_splat = j < n && (!CAP || j < 32u * kCapBuckets);
+        bool valid_splat = j < n && (!CAP || j < 32u * kCapBuckets);
         float4 r0 = make_float4(0, 0, 0, 0), r1 = r0, r2 = r0;
         uint32_t gid = 0;
         if (valid_splat) {
             gid = a.indices[range.x + j];
+            valid_splat = gid < a.n_gauss;
+        }
+        if (valid_splat) {
             r0 = a.rec0[gid];
             r1 = a.rec1[gid];
             r2 = a.rec2[gid];

@@ -110,6 +110,8 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     std::memset(&ta, 0, sizeof(ta));
     ta.ranges = reinterpret_cast<const uint2*>(ranges);
     ta.indices = indices;
+    ta.n_list = 0xffffffffu;   // the caller's buffers: sizes are not passed (as in the reference)
+    ta.n_gauss = 0xffffffffu;
     ta.obs_rgb = observed_rgb;
     ta.obs_depth = observed_depth;
     ta.gx = grad_x;

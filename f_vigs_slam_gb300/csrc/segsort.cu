@@ -402,23 +402,26 @@ cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, i
 // Gaussian at each sorted position.
 __global__ void __launch_bounds__(256) make_keys_kernel(const BinRec* __restrict__ bins,
                                                         const uint2* __restrict__ ranges,
-                                                        const uint32_t* __restrict__ vals, int ntx, int tw, int th,
-                                                        const DevStatus* st, uint64_t* keys) {
+                                                        const uint32_t* __restrict__ vals, uint32_t n_gauss, int ntx,
+                                                        int tw, int th, const DevStatus* st, uint64_t* keys) {
     if (st->flags & kErrOverflow) return;
     const uint32_t tile = blockIdx.x;
     const uint2 r = ranges[tile];
     const int tx = (int)(tile % (uint32_t)ntx), ty = (int)(tile / (uint32_t)ntx);
     for (uint32_t i = r.x + threadIdx.x; i < r.y; i += blockDim.x) {
-        const BinRec b = bins[vals[i]];
+        const uint32_t g = vals[i];
+        if (g >= n_gauss) continue;
+        const BinRec b = bins[g];
         const float d = tile_depth(tx, ty, tw, th, b.p.x, b.p.y, b.p.z, b.p.w, b.r.w);
         keys[i] = ((uint64_t)tile << 32) | __float_as_uint(d);
     }
 }
 
-cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, int num_tiles, int ntx,
-                             int tw, int th, const DevStatus* st, uint64_t* keys, cudaStream_t s) {
+cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint32_t* vals, uint32_t n_gauss,
+                             int num_tiles, int ntx, int tw, int th, const DevStatus* st, uint64_t* keys,
+                             cudaStream_t s) {
     if (num_tiles <= 0) return cudaSuccess;
-    make_keys_kernel<<<num_tiles, 256, 0, s>>>(bins, ranges, vals, ntx, tw, th, st, keys);
+    make_keys_kernel<<<num_tiles, 256, 0, s>>>(bins, ranges, vals, n_gauss, ntx, tw, th, st, keys);
     return cudaGetLastError();
 }
 

@@ -186,9 +186,12 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
     float4 r0, r1, r2;
     float vrej = 0.f;
     if (li < limit) {
-        load_record<REF_LAYOUT>(a, a.indices[list0 + li], r0, r1, r2);
-        vrej = reject_bound(r0.w);
-        keep = !tile_prunable<FORWARD>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+        const uint32_t g = a.indices[list0 + li];
+        if (g < a.n_gauss) {
+            load_record<REF_LAYOUT>(a, g, r0, r1, r2);
+            vrej = reject_bound(r0.w);
+            keep = !tile_prunable<FORWARD>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+        }
     }
     const uint32_t bal = __ballot_sync(kFullMask, keep);
     if (lane == 0) sb.wcnt[w] = __popc(bal);
@@ -227,8 +230,9 @@ __global__ void __launch_bounds__(kPix, 4) track_tile_kernel(TrackArgs a) {
     const float x0 = (float)(tx * kTW), y0 = (float)(ty * kTH);
     const bool in_bounds = (x < a.W && y < a.H);
     const size_t p = (size_t)y * a.W + x;
-    const uint2 range = a.ranges[tile];
-    const int n = (int)(range.y - range.x);
+    uint2 range = a.ranges[tile];
+    range.y = min(range.y, a.n_list);
+    const int n = range.y > range.x ? (int)(range.y - range.x) : 0;
     const float xf = (float)x, yf = (float)y;
 
     float img_depth = 0.f;
