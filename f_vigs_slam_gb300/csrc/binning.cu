@@ -145,6 +145,14 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
     uint32_t count = (uint32_t)((x1 - x0 + 1) * (y1 - y0 + 1));
     if (!visible && !(a.quirks & FVGS_Q_CULLED_SLOTS)) count = 0;
 
+    // The previous binning's rectangle (incremental mode: bins and counts
+    // still hold it; read before anything of Gaussian i is overwritten).
+    uint32_t old_count = 0;
+    uint4 old_r = make_uint4(0, 0, 0, 0);
+    if (a.hist) {
+        old_count = a.counts[i];
+        if (old_count) old_r = a.bins[i].r;
+    }
     // Records of Gaussians without instances are never read by the blending
     // kernels; they are written only where the culled-slot behaviour makes
     // culled Gaussians blend (with the zero record), and the host reports
@@ -157,32 +165,32 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
         a.rec2[i] = make_float4(phy, co.x, co.y, co.z);
         a.bins[i].p = make_float4(u, v, z, phx);
     }
-    a.bins[i].r = make_uint4((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16), count,
-                             __float_as_uint(phy));
-    a.counts[i] = count;
+    // bins[i].r.z == counts[i] after every binning; a Gaussian without
+    // instances before and now needs no write (most of a large map).
+    if (!a.hist || count || old_count) {
+        a.bins[i].r = make_uint4((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16), count,
+                                 __float_as_uint(phy));
+        a.counts[i] = count;
+    }
     if (a.tile_diff) {
         const int gw = a.ntx + 1;
         const size_t cells = (size_t)gw * (a.nty + 1);
         if (count) add_rect(a.tile_diff, gw, x0, y0, x1, y1);
-        if (a.bins_prev) {
-            // instances entering a tile: the new rectangle minus the previous
-            // one (at most four rectangles around their intersection)
+        if (a.hist) {
+            // instances entering a tile: the new rectangle minus the previous one
             uint32_t n_enter = 0;
             if (count) {
+                const EnterSplit es = enter_split(x0, y0, x1, y1, old_count != 0, (int)(old_r.x & 0xffffu),
+                                                  (int)(old_r.x >> 16), (int)(old_r.y & 0xffffu), (int)(old_r.y >> 16));
+                n_enter = entering_count(es);
                 int* e = a.tile_diff + cells;
-                const uint4 pb = a.bins_prev[i].r;
-                const int px0 = (int)(pb.x & 0xffffu), py0 = (int)(pb.x >> 16);
-                const int px1 = (int)(pb.y & 0xffffu), py1 = (int)(pb.y >> 16);
-                const int ix0 = max(x0, px0), ix1 = min(x1, px1), iy0 = max(y0, py0), iy1 = min(y1, py1);
-                if (pb.z == 0u || ix0 > ix1 || iy0 > iy1) {
+                if (es.whole) {
                     add_rect(e, gw, x0, y0, x1, y1);
-                    n_enter = count;
                 } else {
-                    if (iy0 > y0) add_rect(e, gw, x0, y0, x1, iy0 - 1);
-                    if (iy1 < y1) add_rect(e, gw, x0, iy1 + 1, x1, y1);
-                    if (ix0 > x0) add_rect(e, gw, x0, iy0, ix0 - 1, iy1);
-                    if (ix1 < x1) add_rect(e, gw, ix1 + 1, iy0, x1, iy1);
-                    n_enter = count - (uint32_t)((ix1 - ix0 + 1) * (iy1 - iy0 + 1));
+                    if (es.iy0 > y0) add_rect(e, gw, x0, y0, x1, es.iy0 - 1);
+                    if (es.iy1 < y1) add_rect(e, gw, x0, es.iy1 + 1, x1, y1);
+                    if (es.ix0 > x0) add_rect(e, gw, x0, es.iy0, es.ix0 - 1, es.iy1);
+                    if (es.ix1 < x1) add_rect(e, gw, es.ix1 + 1, es.iy0, x1, es.iy1);
                 }
             }
             // warp-aggregated: entering total and the list of changed Gaussians
@@ -200,7 +208,7 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
                 base = __shfl_sync(act, base, leader);
                 if (n_enter) {
                     const uint32_t idx = base + (uint32_t)__popc(want & lanemask_lt());
-                    if (idx < a.changed_cap) a.changed[idx] = (uint32_t)i;
+                    if (idx < a.changed_cap) a.changed[idx] = make_uint4((uint32_t)i, old_r.x, old_r.y, old_count);
                 }
             }
         }
@@ -551,17 +559,27 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, uint32_t first
     uint32_t g = 0;
     uint4 b0 = make_uint4(0, 0, 0, 0);
     float4 b1 = make_float4(0, 0, 0, 0);
-    uint2 prev = make_uint2(1u, 0u);  // previous rectangle (incremental), empty by default
+    uint4 prev = make_uint4(0, 0, 0, 0);  // incremental: (index, previous rectangle, previous count)
+    uint32_t cnt = 0;
     if (valid) {
-        g = INCR ? a.changed[item] : item;
+        if (INCR) {
+            prev = a.changed[item];
+            g = prev.x;
+        } else {
+            g = item;
+        }
         b0 = a.bins[g].r;
         if (b0.z) b1 = a.bins[g].p;
         if (INCR) {
-            const uint4 p = a.bins_prev[g].r;
-            if (p.z) prev = make_uint2(p.x, p.y);
+            cnt = b0.z ? entering_count(enter_split((int)(b0.x & 0xffffu), (int)(b0.x >> 16), (int)(b0.y & 0xffffu),
+                                                    (int)(b0.y >> 16), prev.w != 0u, (int)(prev.y & 0xffffu),
+                                                    (int)(prev.y >> 16), (int)(prev.z & 0xffffu),
+                                                    (int)(prev.z >> 16)))
+                       : 0u;
+        } else {
+            cnt = b0.z;
         }
     }
-    const uint32_t cnt = valid ? b0.z : 0u;
     uint32_t incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -594,19 +612,21 @@ __device__ __forceinline__ void walk_instances(const EmitArgs& a, uint32_t first
             const uint32_t g_lo = __shfl_sync(kFullMask, g, lo);
             const uint32_t local = m - e_lo;
             const int x0 = (int)(r0 & 0xffffu), y0 = (int)(r0 >> 16);
-            const int x1 = (int)(r1 & 0xffffu);
-            const int w = max(1, x1 - x0 + 1);
-            const int tx = x0 + (int)(local % (uint32_t)w);
-            const int ty = y0 + (int)(local / (uint32_t)w);
-            bool emit = m < total;
+            const int x1 = (int)(r1 & 0xffffu), y1 = (int)(r1 >> 16);
+            int tx, ty;
             if (INCR) {
-                const uint32_t p0 = __shfl_sync(kFullMask, prev.x, lo);
-                const uint32_t p1 = __shfl_sync(kFullMask, prev.y, lo);
-                const bool inside_prev = tx >= (int)(p0 & 0xffffu) && tx <= (int)(p1 & 0xffffu) &&
-                                         ty >= (int)(p0 >> 16) && ty <= (int)(p1 >> 16);
-                emit = emit && !inside_prev;
+                const uint32_t p0 = __shfl_sync(kFullMask, prev.y, lo);
+                const uint32_t p1 = __shfl_sync(kFullMask, prev.z, lo);
+                const uint32_t pc = __shfl_sync(kFullMask, prev.w, lo);
+                entering_tile(enter_split(x0, y0, x1, y1, pc != 0u, (int)(p0 & 0xffffu), (int)(p0 >> 16),
+                                          (int)(p1 & 0xffffu), (int)(p1 >> 16)),
+                              local, tx, ty);
+            } else {
+                const int w = max(1, x1 - x0 + 1);
+                tx = x0 + (int)(local % (uint32_t)w);
+                ty = y0 + (int)(local / (uint32_t)w);
             }
-            ok[q] = emit;
+            ok[q] = m < total;
             const float d = tile_depth(tx, ty, a.tw, a.th, u, v, z, phx, phy_bits);
             tiles[q] = (uint32_t)(ty * a.ntx + tx);
             keys[q] = ((uint64_t)__float_as_uint(d) << 32) | (uint64_t)g_lo;

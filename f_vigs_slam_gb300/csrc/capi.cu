@@ -91,8 +91,7 @@ struct fvgs_session {
 
     float4 *pos = nullptr, *scale = nullptr, *rot = nullptr, *col = nullptr;
     float4 *rec0 = nullptr, *rec1 = nullptr, *rec2 = nullptr;
-    BinRec* bins = nullptr;
-    BinRec* bins_prev = nullptr;  // the previous binning's records (swapped with bins per binning)
+    BinRec* bins = nullptr;  // binning records; bins[i].r.z == counts[i] after every binning
     uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
     float *dbg_cov = nullptr, *dbg_inv = nullptr;
     uint8_t* dbg_vis = nullptr;
@@ -114,9 +113,9 @@ struct fvgs_session {
     uint2* enter_ranges = nullptr;
     uint32_t* enter_fill = nullptr;
     uint64_t* enter_keys = nullptr;
-    uint32_t* changed = nullptr;
+    uint4* changed = nullptr;  // (index, previous rectangle, previous count) per changed Gaussian
     uint32_t enter_cap = 0;
-    bool hist_ok = false;  // the last binning left valid (bins, ranges, vals) for the next one
+    bool hist_ok = false;  // the last binning left valid (bins, counts, ranges, vals) for the next one
     bool keys_valid = false;  // keys[] holds the last binning's reference-format keys
     int hist_ntx = 0, hist_nty = 0;
 
@@ -324,7 +323,6 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     const bool hist = !radix && !literal && s->hist_ok && s->hist_ntx == ntx && s->hist_nty == nty;
     s->hist_ok = false;  // until this binning is fully enqueued
     if (!radix) {
-        std::swap(s->bins, s->bins_prev);
         std::swap(s->ranges, s->ranges_prev);
         std::swap(s->vals, s->sort.vals_alt);
     }
@@ -359,7 +357,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * tile_diff_words(ntx, nty), s->stream));
         pa.tile_diff = s->tile_diff;
         if (hist) {
-            pa.bins_prev = s->bins_prev;
+            pa.hist = 1;
             pa.changed = s->changed;
             pa.changed_cap = s->enter_cap;
         }
@@ -387,7 +385,6 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         }
         ea.keys = s->sort.keys_alt;  // composite keys, tile-major
         ea.vals = nullptr;
-        ea.bins_prev = s->bins_prev;
         ea.changed = s->changed;
         ea.counters = reinterpret_cast<const uint32_t*>(s->tile_diff + 2 * diff_grid_cells(ntx, nty));
         ea.enter_keys = s->enter_keys;
@@ -725,7 +722,6 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->rec1, N);
     FV_A(s->rec2, N);
     FV_A(s->bins, N);
-    FV_A(s->bins_prev, N);
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
     FV_A(s->partials, scan_partials_size((int)N) + 1);
@@ -830,7 +826,7 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     float* tmp2 = reinterpret_cast<float*>(s->rec1);
     float* tmp3 = reinterpret_cast<float*>(s->rec2);
     float* tmp4 = reinterpret_cast<float*>(s->bins);       // 8N floats
-    float* tmp5 = reinterpret_cast<float*>(s->bins_prev);
+    float* tmp5 = reinterpret_cast<float*>(s->offsets);
     FV_CK(cudaMemcpyAsync(tmp, positions, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(tmp2, scales, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(tmp3, orientations, sizeof(float) * 4 * n, cudaMemcpyDefault, s->stream));
@@ -855,7 +851,7 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
     float* tmp2 = reinterpret_cast<float*>(s->rec1);
     float* tmp3 = reinterpret_cast<float*>(s->rec2);
     float* tmp4 = reinterpret_cast<float*>(s->bins);       // 8N floats
-    float* tmp5 = reinterpret_cast<float*>(s->bins_prev);
+    float* tmp5 = reinterpret_cast<float*>(s->offsets);
     download_unpack_kernel<<<(n + 255) / 256, 256, 0, s->stream>>>(s->pos, s->scale, s->rot, s->col, n, tmp, tmp2,
                                                                    tmp3, tmp4, tmp5);
     FV_CK(cudaGetLastError());

@@ -89,6 +89,67 @@ __device__ __forceinline__ bool rect_contains(uint4 b0, int tx, int ty) {
            ty <= (int)(b0.y >> 16);
 }
 
+// Tiles of rectangle R1 = [x0..x1] x [y0..y1] outside R0 (has_prev: R0 =
+// [px0..px1] x [py0..py1]), as at most four rectangles around their
+// intersection I in a fixed order: rows above I, rows below I (full width),
+// columns left of I, columns right of I (rows of I).  entering_count gives
+// their number, entering_tile the local-th of them.
+struct EnterSplit {
+    int x0, y0, x1, y1;      // R1
+    int ix0, iy0, ix1, iy1;  // I (when overlapping)
+    bool whole;              // no overlap: every tile of R1 enters
+};
+__device__ __forceinline__ EnterSplit enter_split(int x0, int y0, int x1, int y1, bool has_prev, int px0, int py0,
+                                                  int px1, int py1) {
+    EnterSplit e;
+    e.x0 = x0;
+    e.y0 = y0;
+    e.x1 = x1;
+    e.y1 = y1;
+    e.ix0 = max(x0, px0);
+    e.ix1 = min(x1, px1);
+    e.iy0 = max(y0, py0);
+    e.iy1 = min(y1, py1);
+    e.whole = !has_prev || e.ix0 > e.ix1 || e.iy0 > e.iy1;
+    return e;
+}
+__device__ __forceinline__ uint32_t entering_count(const EnterSplit& e) {
+    const uint32_t all = (uint32_t)((e.x1 - e.x0 + 1) * (e.y1 - e.y0 + 1));
+    return e.whole ? all : all - (uint32_t)((e.ix1 - e.ix0 + 1) * (e.iy1 - e.iy0 + 1));
+}
+__device__ __forceinline__ void entering_tile(const EnterSplit& e, uint32_t local, int& tx, int& ty) {
+    const int w = e.x1 - e.x0 + 1;
+    if (e.whole) {
+        tx = e.x0 + (int)(local % (uint32_t)w);
+        ty = e.y0 + (int)(local / (uint32_t)w);
+        return;
+    }
+    const uint32_t top = (uint32_t)((e.iy0 - e.y0) * w);
+    if (local < top) {
+        tx = e.x0 + (int)(local % (uint32_t)w);
+        ty = e.y0 + (int)(local / (uint32_t)w);
+        return;
+    }
+    local -= top;
+    const uint32_t bottom = (uint32_t)((e.y1 - e.iy1) * w);
+    if (local < bottom) {
+        tx = e.x0 + (int)(local % (uint32_t)w);
+        ty = e.iy1 + 1 + (int)(local / (uint32_t)w);
+        return;
+    }
+    local -= bottom;
+    const int wl = e.ix0 - e.x0, h = e.iy1 - e.iy0 + 1;
+    if (local < (uint32_t)(wl * h)) {
+        tx = e.x0 + (int)(local % (uint32_t)wl);
+        ty = e.iy0 + (int)(local / (uint32_t)wl);
+        return;
+    }
+    local -= (uint32_t)(wl * h);
+    const int wr = e.x1 - e.ix1;
+    tx = e.ix1 + 1 + (int)(local % (uint32_t)wr);
+    ty = e.iy0 + (int)(local / (uint32_t)wr);
+}
+
 // Depth of a Gaussian at the centre of tile (tx, ty) -- the sort key of the
 // reference's generateTileHashes_kernel (src/GSCudaKernels.cu:596-667):
 // fmaf(phy, dy, fmaf(phx, dx, z)), d = tile centre - projected mean.

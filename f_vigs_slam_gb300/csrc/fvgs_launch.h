@@ -38,11 +38,12 @@ struct ProjectArgs {
     BinRec* bins;
     uint32_t* counts;
     int* tile_diff;    // optional: binning scratch (tile_diff_words): count grid, entering grid, counters
-    // incremental binning (optional): the previous binning's rectangles; the
-    // instances new to a tile go to the entering grid, the Gaussians that have
-    // some to changed[] (at most changed_cap listed)
-    const BinRec* bins_prev;
-    uint32_t* changed;
+    // incremental binning (hist != 0): bins and counts still hold the previous
+    // binning; the instances new to a tile go to the entering grid and the
+    // Gaussians that have some to changed[] as (index, previous rectangle r.x,
+    // r.y, previous count), at most changed_cap listed
+    int hist;
+    uint4* changed;
     uint32_t changed_cap;
     float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
     float* dbg_inv;    // optional: 3N inverse, stored order (xx, yy, xy)
@@ -59,8 +60,7 @@ struct EmitArgs {
     uint32_t* vals;
     // incremental mode (tile-bucket path): entering instances of the listed
     // Gaussians go to enter_keys at the enter_fill cursors
-    const BinRec* bins_prev;
-    const uint32_t* changed;
+    const uint4* changed;
     const uint32_t* counters;  // [0] entering instances, [1] listed Gaussians
     uint64_t* enter_keys;
     uint32_t* enter_fill;
