@@ -5,9 +5,9 @@
  *
  * This boundary replaces the device-side half of the reference's
  * GSSlam / GSCudaKernels path (jcevasco2003/f_vigs_slam).  Each entry point
- * names the reference interface it stands in for.  The C++ compatibility
- * layer (include/f_vigs_slam/*.hpp) keeps the reference's own class
- * interfaces (GSSlam, RgbdPoseCostFunction) on top of it.
+ * names the reference interface it stands in for.  The reference's own
+ * classes (GSSlam, RgbdPoseCostFunction) keep their interfaces: the bodies of
+ * their member functions call these entry points.
  *
  * Memory: the library owns every device buffer of a session; caller arrays
  * are borrowed for the duration of a call and may be host (pageable or
