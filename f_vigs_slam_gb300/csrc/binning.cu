@@ -31,26 +31,19 @@ __device__ __forceinline__ void add_rect(int* d, int gw, int x0, int y0, int x1,
     atomicAdd(&d[(y1 + 1) * gw + x1 + 1], 1);
 }
 
-__global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const DevPose* P = a.pose;
-    const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
-    float R[3][3];
-    quat_to_R(qc, R);
-    // Only the position is needed to decide visibility; scale, rotation and
-    // colour are loaded for the Gaussians that need them (most of a large
-    // map is outside any one view).
-    const float4 p = a.pos[i];
+// One Gaussian: p is its position, prev_count its instance count in the
+// previous binning (incremental mode), R and tw the camera pose.
+__device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 p, uint32_t prev_count,
+                                            const float (&R)[3][3], const float (&tw)[3]) {
     const fvgs_intrinsics K = a.K;
 
     float u = 0.f, v = 0.f, z = 0.f, cxx = 0.f, cyy = 0.f, cxy = 0.f;
     float ixx = 0.f, iyy = 0.f, ixy = 0.f, phx = 0.f, phy = 0.f;
     bool visible = false;
     {
-        const float d0 = __fsub_rn(p.x, P->t[0]);
-        const float d1 = __fsub_rn(p.y, P->t[1]);
-        const float d2 = __fsub_rn(p.z, P->t[2]);
+        const float d0 = __fsub_rn(p.x, tw[0]);
+        const float d1 = __fsub_rn(p.y, tw[1]);
+        const float d2 = __fsub_rn(p.z, tw[2]);
         const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[1][0], d1, __fmul_rn(R[0][0], d0)));
         const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[1][1], d1, __fmul_rn(R[0][1], d0)));
         const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[1][2], d1, __fmul_rn(R[0][2], d0)));
@@ -147,12 +140,9 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
 
     // The previous binning's rectangle (incremental mode: bins and counts
     // still hold it; read before anything of Gaussian i is overwritten).
-    uint32_t old_count = 0;
+    const uint32_t old_count = a.hist ? prev_count : 0u;
     uint4 old_r = make_uint4(0, 0, 0, 0);
-    if (a.hist) {
-        old_count = a.counts[i];
-        if (old_count) old_r = a.bins[i].r;
-    }
+    if (old_count) old_r = a.bins[i].r;
     // Records of Gaussians without instances are never read by the blending
     // kernels; they are written only where the culled-slot behaviour makes
     // culled Gaussians blend (with the zero record), and the host reports
@@ -221,6 +211,35 @@ __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
         a.dbg_inv[3 * i + 1] = iyy;
         a.dbg_inv[3 * i + 2] = ixy;
         a.dbg_vis[i] = visible ? 1 : 0;
+    }
+}
+
+// Grid-stride over the Gaussians with the next position and previous count
+// loaded one step ahead: only the position decides visibility, so the
+// dependent-load chain of one thread is short and overlapped.
+__global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
+    const DevPose* P = a.pose;
+    const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
+    float R[3][3];
+    quat_to_R(qc, R);
+    const float tw[3] = {P->t[0], P->t[1], P->t[2]};
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t c_next = 0;
+    if (i < a.n) {
+        p_next = a.pos[i];
+        if (a.hist) c_next = a.counts[i];
+    }
+    for (; i < a.n; i += stride) {
+        const float4 p = p_next;
+        const uint32_t c = c_next;
+        const int j = i + stride;
+        if (j < a.n) {
+            p_next = a.pos[j];
+            if (a.hist) c_next = a.counts[j];
+        }
+        project_one(a, i, p, c, R, tw);
     }
 }
 
@@ -680,9 +699,10 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
 }
 
 // ------------------------------- launchers ---------------------------------
-cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s) {
+cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
-    project_count_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    const int need = (a.n + 255) / 256;
+    project_count_kernel<<<max_ctas > 0 && max_ctas < need ? max_ctas : need, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -364,7 +364,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     }
     {
         KScope k(s, FVGS_K_PROJECT, 1);
-        FV_CK(launch_project_count(pa, s->stream));
+        FV_CK(launch_project_count(pa, s->num_sms * 4, s->stream));
     }
     EmitArgs ea{};
     ea.bins = s->bins;

@@ -67,7 +67,8 @@ struct EmitArgs {
     uint32_t enter_cap;
 };
 
-cudaError_t launch_project_count(const ProjectArgs& a, cudaStream_t s);
+// max_ctas caps the grid (the kernel strides over the Gaussians); <= 0: one thread per Gaussian.
+cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s);
 size_t scan_partials_size(int n);
 cudaError_t launch_scan(const uint32_t* counts, int n, uint32_t* partials, uint32_t* offsets, DevStatus* st,
                         uint32_t capacity, cudaStream_t s);
