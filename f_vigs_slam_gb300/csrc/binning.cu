@@ -218,6 +218,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
 // loaded one step ahead: only the position decides visibility, so the
 // dependent-load chain of one thread is short and overlapped.
 __global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
+    pdl_begin();
     const DevPose* P = a.pose;
     const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
     float R[3][3];
@@ -471,17 +472,29 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* scratch,
                                                                    uint32_t enter_cap, uint2* ranges, uint32_t* fill,
                                                                    uint2* enter_ranges, uint32_t* enter_fill,
                                                                    DevStatus* st, uint32_t capacity,
-                                                                   uint32_t* chunk_counter) {
+                                                                   uint32_t* seg_ctrl) {
+    pdl_begin();
     extern __shared__ int s_grid[];
     __shared__ uint32_t s_w[2][32];
     __shared__ uint32_t s_carry[2];
+    __shared__ uint32_t s_ctr[2];
     const int gw = ntx + 1, gh = nty + 1, cells = gw * gh;
     const int ng = hist ? 2 : 1;
     const bool staged = ng * cells <= kOffSmemCells;
     int* g = staged ? s_grid : scratch;
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(scratch + 2 * (size_t)cells);
+    if (threadIdx.x == 0) {
+        s_ctr[0] = ctr[0];
+        s_ctr[1] = ctr[1];
+    }
     if (staged)
         for (int i = threadIdx.x; i < ng * cells; i += kOffThreads) s_grid[i] = scratch[i];
     __syncthreads();
+    // the scratch is left zeroed for the next binning (staged: right away)
+    if (staged) {
+        for (int i = threadIdx.x; i < ng * cells; i += kOffThreads) scratch[i] = 0;
+        if (threadIdx.x < kCounterWords) ctr[threadIdx.x] = 0u;
+    }
     // row prefix sums (one thread per grid row), then column prefix sums
     for (int r = threadIdx.x; r < ng * gh; r += kOffThreads) {
         int* row = g + (size_t)(r / gh) * cells + (r % gh) * gw;
@@ -541,15 +554,22 @@ __global__ void __launch_bounds__(kOffThreads) tile_offsets_kernel(int* scratch,
         }
         __syncthreads();
     }
+    if (!staged) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < ng * cells; i += kOffThreads) scratch[i] = 0;
+        if (threadIdx.x < kCounterWords) ctr[threadIdx.x] = 0u;
+    }
     if (threadIdx.x == 0) {
         const uint32_t total = s_carry[0];
-        *chunk_counter = 0;  // the scatter that follows takes Gaussian chunks from it
+        // list counters of the per-tile sort and the scatter's chunk counter
+        seg_ctrl[0] = 0u;
+        seg_ctrl[1] = 0u;
+        seg_ctrl[2] = 0u;
         st->n_instances = total;
         st->n_instances_clamped = total < capacity ? total : capacity;
         if (total > capacity) atomicOr(&st->flags, kErrOverflow);
-        const uint32_t* ctr = reinterpret_cast<const uint32_t*>(scratch + 2 * (size_t)cells);
-        const uint32_t n_enter = hist ? ctr[0] : total;
-        const uint32_t n_changed = hist ? ctr[1] : 0u;
+        const uint32_t n_enter = hist ? s_ctr[0] : total;
+        const uint32_t n_changed = hist ? s_ctr[1] : 0u;
         const bool incr = hist && n_enter == s_carry[1] && n_enter <= enter_cap && n_changed <= enter_cap;
         st->mode = incr ? kBinIncremental : kBinFull;
         st->n_enter = n_enter;
@@ -691,9 +711,10 @@ __device__ __forceinline__ void scatter_chunks(const EmitArgs& a, uint32_t* fill
 // its tile with one global atomic.
 __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t* fill, uint32_t* chunk_counter,
                                                            const DevStatus* st) {
+    pdl_begin();
     if (st->flags & kErrOverflow) return;
     if (st->mode == kBinIncremental)
-        scatter_chunks<true>(a, a.enter_fill, a.enter_keys, a.enter_cap, a.counters[1], chunk_counter);
+        scatter_chunks<true>(a, a.enter_fill, a.enter_keys, a.enter_cap, st->n_changed, chunk_counter);
     else
         scatter_chunks<false>(a, fill, a.keys, a.capacity, (uint32_t)a.n, chunk_counter);
 }
@@ -702,8 +723,8 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
 cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
     const int need = (a.n + 255) / 256;
-    project_count_kernel<<<max_ctas > 0 && max_ctas < need ? max_ctas : need, 256, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_chained(project_count_kernel, dim3(max_ctas > 0 && max_ctas < need ? max_ctas : need), dim3(256), 0,
+                          s, a);
 }
 
 size_t scan_partials_size(int n) { return (size_t)((n + kScanBlock - 1) / kScanBlock); }
@@ -740,24 +761,23 @@ size_t tile_diff_words(int ntx, int nty) { return 2 * diff_grid_cells(ntx, nty) 
 
 cudaError_t launch_tile_offsets(int* scratch, int ntx, int nty, bool hist, uint32_t enter_cap, uint2* ranges,
                                 uint32_t* fill, uint2* enter_ranges, uint32_t* enter_fill, DevStatus* st,
-                                uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s) {
+                                uint32_t capacity, uint32_t* seg_ctrl, cudaStream_t s) {
     // set on every launch: cheap, and correct for whichever device is current
     const cudaError_t e = cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)(sizeof(int) * kOffSmemCells));
     if (e != cudaSuccess) return e;
     const size_t cells = (hist ? 2 : 1) * diff_grid_cells(ntx, nty);
     const size_t smem = cells <= (size_t)kOffSmemCells ? sizeof(int) * cells : 0;
-    tile_offsets_kernel<<<1, kOffThreads, smem, s>>>(scratch, ntx, nty, hist ? 1 : 0, enter_cap, ranges, fill,
-                                                     enter_ranges, enter_fill, st, capacity, chunk_counter);
-    return cudaGetLastError();
+    return launch_chained(tile_offsets_kernel, dim3(1), dim3(kOffThreads), smem, s, scratch, ntx, nty, hist ? 1 : 0,
+                          enter_cap, ranges, fill, enter_ranges, enter_fill, st, capacity, seg_ctrl);
 }
 
 cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
                                 const DevStatus* st, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
     const int needed = (a.n + 255) / 256;
-    emit_scatter_kernel<<<grid < needed ? grid : needed, 256, 0, s>>>(a, fill, chunk_counter, st);
-    return cudaGetLastError();
+    return launch_chained(emit_scatter_kernel, dim3(grid < needed ? grid : needed), dim3(256), 0, s, a, fill,
+                          chunk_counter, st);
 }
 
 }  // namespace fvgs

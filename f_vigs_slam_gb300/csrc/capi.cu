@@ -35,6 +35,7 @@ struct FrameLevel {
 };
 
 __global__ void set_pose_kernel(DevPose* dst, fvgs_pose p) {
+    pdl_begin();
     for (int k = 0; k < 3; ++k) {
         dst->t[k] = p.position[k];
         dst->td[k] = (double)p.position[k];
@@ -105,8 +106,9 @@ struct fvgs_session {
     uint2* ranges = nullptr;
     uint2* ranges_prev = nullptr;  // swapped with ranges per binning (vals with sort.vals_alt)
     float* tile_out = nullptr;
-    int* tile_diff = nullptr;      // (ntx+1) x (nty+1) difference grid of tile counts
+    int* tile_diff = nullptr;      // binning scratch: difference grids of tile counts + counters
     size_t tile_diff_cells = 0;
+    bool diff_clean = false;       // the scratch is all zero (the tile-offsets kernel leaves it so)
     uint32_t* tile_fill = nullptr;  // scatter cursors
     SegSortWork seg{};
     // incremental binning: entering instances per tile and the Gaussians with some
@@ -354,7 +356,8 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     }
     if (!radix) {
         if (T > s->cap_tiles || tile_diff_words(ntx, nty) > s->tile_diff_cells) return FVGS_E_INVALID;
-        FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * tile_diff_words(ntx, nty), s->stream));
+        if (!s->diff_clean) FV_CK(cudaMemsetAsync(s->tile_diff, 0, sizeof(int) * s->tile_diff_cells, s->stream));
+        s->diff_clean = false;  // until the tile-offsets kernel of this binning is enqueued
         pa.tile_diff = s->tile_diff;
         if (hist) {
             pa.hist = 1;
@@ -380,13 +383,12 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         {
             KScope k(s, FVGS_K_SCAN, 1);
             FV_CK(launch_tile_offsets(s->tile_diff, ntx, nty, hist, s->enter_cap, s->ranges, s->tile_fill,
-                                      s->enter_ranges, s->enter_fill, s->st, cap32, s->seg.large_ctrl + 2,
-                                      s->stream));
+                                      s->enter_ranges, s->enter_fill, s->st, cap32, s->seg.large_ctrl, s->stream));
+            s->diff_clean = true;
         }
         ea.keys = s->sort.keys_alt;  // composite keys, tile-major
         ea.vals = nullptr;
         ea.changed = s->changed;
-        ea.counters = reinterpret_cast<const uint32_t*>(s->tile_diff + 2 * diff_grid_cells(ntx, nty));
         ea.enter_keys = s->enter_keys;
         ea.enter_fill = s->enter_fill;
         ea.enter_cap = s->enter_cap;
@@ -494,8 +496,7 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
 }
 
 int set_pose(fvgs_session* s, const fvgs_pose* p) {
-    set_pose_kernel<<<1, 1, 0, s->stream>>>(s->pose, *p);
-    FV_CK(cudaGetLastError());
+    FV_CK(launch_chained(set_pose_kernel, dim3(1), dim3(1), 0, s->stream, s->pose, *p));
     return FVGS_OK;
 }
 

@@ -162,6 +162,16 @@ __device__ __forceinline__ float tile_depth(int tx, int ty, int tw, int th, floa
     return __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
 }
 
+// Programmatic dependent launch.  Kernels of the binning / tracking / mapping
+// chains are launched with programmatic stream serialisation: each lets the
+// next kernel be scheduled once all of its own CTAs have started, and waits
+// (in hardware, until its predecessor grid has completed and its memory is
+// visible) before touching any data.  Outside such a launch both are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Bounded spin budget for device-side waits; on expiry a kernel records
 // kErrTimeout and carries on with a safe value instead of hanging.
 constexpr uint32_t kSpinLimit = 1u << 24;

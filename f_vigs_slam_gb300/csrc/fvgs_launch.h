@@ -13,6 +13,26 @@ namespace fvgs {
 struct DevStatus;
 struct DevPose;
 
+#ifdef __CUDACC__
+// Launch with programmatic stream serialisation (see pdl_begin): the kernel
+// may be scheduled while its predecessor in the stream drains.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                           Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#endif
+
 // Binning record of one Gaussian, 32 bytes so that one gather touches one
 // sector: r = (x0 | y0 << 16, x1 | y1 << 16 (inclusive tile rectangle),
 // instance count (0: none), phat.y bits), p = (u, v, z, phat.x).
@@ -60,8 +80,7 @@ struct EmitArgs {
     uint32_t* vals;
     // incremental mode (tile-bucket path): entering instances of the listed
     // Gaussians go to enter_keys at the enter_fill cursors
-    const uint4* changed;
-    const uint32_t* counters;  // [0] entering instances, [1] listed Gaussians
+    const uint4* changed;  // DevStatus::n_changed entries
     uint64_t* enter_keys;
     uint32_t* enter_fill;
     uint32_t enter_cap;
@@ -85,9 +104,11 @@ constexpr int kCounterWords = 8;  // [0] entering instances, [1] listed Gaussian
 // hist: a previous binning on the same tile grid is valid; the kernel then
 // also scans the entering grid and picks incremental mode when the entering
 // instances fit enter_cap (DevStatus::mode).
+// It also leaves the binning scratch zeroed for the next binning, and zeroes
+// the scatter chunk counter and the sort's list counters (seg_ctrl[0..2]).
 cudaError_t launch_tile_offsets(int* scratch, int ntx, int nty, bool hist, uint32_t enter_cap, uint2* ranges,
                                 uint32_t* fill, uint2* enter_ranges, uint32_t* enter_fill, DevStatus* st,
-                                uint32_t capacity, uint32_t* chunk_counter, cudaStream_t s);
+                                uint32_t capacity, uint32_t* seg_ctrl, cudaStream_t s);
 cudaError_t launch_emit_scatter(const EmitArgs& a, uint32_t* fill, uint32_t* chunk_counter, int grid,
                                 const DevStatus* st, cudaStream_t s);
 // Per-tile sort of the composite keys (segsort.cu): writes the sorted Gaussian

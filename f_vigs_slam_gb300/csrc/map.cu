@@ -29,6 +29,7 @@ constexpr float kMInv255 = 1.0f / 255.0f;
 
 template <bool CAP>
 __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
+    pdl_begin();
     __shared__ float4 s0[kMBatch];
     __shared__ float4 s1[kMBatch];
     __shared__ float4 s2[kMBatch];
@@ -109,6 +110,7 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
 
 template <bool CAP>
 __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
+    pdl_begin();
     __shared__ float4 s_pc[kMPix];  // final colour (incl. background), median depth
     __shared__ float4 s_pe[kMPix];  // colour error, observed depth
     __shared__ uint32_t s_nc[kMPix];
@@ -276,6 +278,7 @@ __device__ __forceinline__ float adam_step(float& m, float& v, float g, float et
 }
 
 __global__ void __launch_bounds__(256) map_update_kernel(MapUpdateArgs a, const DevStatus* st) {
+    pdl_begin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     // An instance overflow leaves the binning incomplete; the host re-runs the
@@ -561,6 +564,7 @@ __global__ void __launch_bounds__(256) map_update_kernel(MapUpdateArgs a, const 
 // Exclusive scan of per-tile bucket counts ceil(n_t/32) (one CTA).
 __global__ void __launch_bounds__(1024) bucket_scan_kernel(const uint2* ranges, int T, uint32_t* bucket_base,
                                                            uint32_t* total) {
+    pdl_begin();
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
     if (threadIdx.x == 0) s_carry = 0;
@@ -600,31 +604,23 @@ __global__ void __launch_bounds__(1024) bucket_scan_kernel(const uint2* ranges, 
 
 cudaError_t launch_map_forward(const MapArgs& a, bool cap, cudaStream_t s) {
     const int T = a.ntx * a.nty;
-    if (cap)
-        map_forward_kernel<true><<<T, kMPix, 0, s>>>(a);
-    else
-        map_forward_kernel<false><<<T, kMPix, 0, s>>>(a);
-    return cudaGetLastError();
+    if (cap) return launch_chained(map_forward_kernel<true>, dim3(T), dim3(kMPix), 0, s, a);
+    return launch_chained(map_forward_kernel<false>, dim3(T), dim3(kMPix), 0, s, a);
 }
 
 cudaError_t launch_map_backward(const MapArgs& a, bool cap, cudaStream_t s) {
     const int T = a.ntx * a.nty;
-    if (cap)
-        map_backward_kernel<true><<<T, kMPix, 0, s>>>(a);
-    else
-        map_backward_kernel<false><<<T, kMPix, 0, s>>>(a);
-    return cudaGetLastError();
+    if (cap) return launch_chained(map_backward_kernel<true>, dim3(T), dim3(kMPix), 0, s, a);
+    return launch_chained(map_backward_kernel<false>, dim3(T), dim3(kMPix), 0, s, a);
 }
 
 cudaError_t launch_bucket_scan(const uint2* ranges, int T, uint32_t* bucket_base, uint32_t* total, cudaStream_t s) {
-    bucket_scan_kernel<<<1, 1024, 0, s>>>(ranges, T, bucket_base, total);
-    return cudaGetLastError();
+    return launch_chained(bucket_scan_kernel, dim3(1), dim3(1024), 0, s, ranges, T, bucket_base, total);
 }
 
 cudaError_t launch_map_update(const MapUpdateArgs& a, const DevStatus* st, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
-    map_update_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, st);
-    return cudaGetLastError();
+    return launch_chained(map_update_kernel, dim3((a.n + 255) / 256), dim3(256), 0, s, a, st);
 }
 
 int map_cap_buckets() { return kCapBuckets; }

@@ -70,6 +70,7 @@ int scratch_for_current_device(unsigned char** out) {
 }
 
 __global__ void noalloc_set_pose_kernel(DevPose* dst, fvgs_pose p) {
+    fvgs::pdl_begin();
     for (int k = 0; k < 3; ++k) {
         dst->t[k] = p.position[k];
         dst->td[k] = (double)p.position[k];

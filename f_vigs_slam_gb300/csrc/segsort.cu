@@ -255,6 +255,7 @@ __device__ __forceinline__ int rank_in(const uint64_t* s, int base, int len, uin
 __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, const uint2* __restrict__ ranges,
                                                               uint32_t* vals, SegSortWork w, DevStatus* st,
                                                               SegSortIncr inc) {
+    pdl_begin();
     __shared__ uint64_t s[kSegCap + kSegCap / 16];
     __shared__ uint32_t s_wsum[kSegThreads / 32];
     __shared__ int s_desc;
@@ -326,6 +327,7 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, co
 __global__ void __launch_bounds__(kSegThreads) segsort_large_kernel(uint64_t* comp, uint64_t* tmp,
                                                                     const uint2* __restrict__ ranges, uint32_t* vals,
                                                                     SegSortWork w, const DevStatus* st) {
+    pdl_begin();
     __shared__ uint64_t s[kSegCap + kSegCap / 16];
     __shared__ uint32_t s_idx;
     if (st->flags & kErrOverflow) return;
@@ -391,11 +393,12 @@ cudaError_t launch_segsort(uint64_t* comp, uint64_t* tmp, const uint2* ranges, i
                            SegSortWork w, const DevStatus* st, int large_grid, const SegSortIncr& inc,
                            cudaStream_t s) {
     if (num_tiles <= 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(w.large_ctrl, 0, 2 * sizeof(uint32_t), s);
+    // the list counters were zeroed by the tile-offsets kernel of this binning
+    cudaError_t e = launch_chained(segsort_kernel, dim3(num_tiles), dim3(kSegThreads), 0, s, comp, ranges, vals, w,
+                                   const_cast<DevStatus*>(st), inc);
     if (e != cudaSuccess) return e;
-    segsort_kernel<<<num_tiles, kSegThreads, 0, s>>>(comp, ranges, vals, w, const_cast<DevStatus*>(st), inc);
-    segsort_large_kernel<<<large_grid, kSegThreads, 0, s>>>(comp, tmp, ranges, vals, w, st);
-    return cudaGetLastError();
+    return launch_chained(segsort_large_kernel, dim3(large_grid), dim3(kSegThreads), 0, s, comp, tmp, ranges, vals, w,
+                          st);
 }
 
 // One CTA per tile: key = tile << 32 | bits of the tile-centre depth of the
@@ -404,6 +407,7 @@ __global__ void __launch_bounds__(256) make_keys_kernel(const BinRec* __restrict
                                                         const uint2* __restrict__ ranges,
                                                         const uint32_t* __restrict__ vals, uint32_t n_gauss, int ntx,
                                                         int tw, int th, const DevStatus* st, uint64_t* keys) {
+    pdl_begin();
     if (st->flags & kErrOverflow) return;
     const uint32_t tile = blockIdx.x;
     const uint2 r = ranges[tile];
@@ -421,8 +425,8 @@ cudaError_t launch_make_keys(const BinRec* bins, const uint2* ranges, const uint
                              int num_tiles, int ntx, int tw, int th, const DevStatus* st, uint64_t* keys,
                              cudaStream_t s) {
     if (num_tiles <= 0) return cudaSuccess;
-    make_keys_kernel<<<num_tiles, 256, 0, s>>>(bins, ranges, vals, n_gauss, ntx, tw, th, st, keys);
-    return cudaGetLastError();
+    return launch_chained(make_keys_kernel, dim3(num_tiles), dim3(256), 0, s, bins, ranges, vals, n_gauss, ntx, tw,
+                          th, st, keys);
 }
 
 }  // namespace fvgs

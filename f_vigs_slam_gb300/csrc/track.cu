@@ -217,6 +217,7 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
 
 template <bool RENDER_ONLY, bool REF_LAYOUT = false>
 __global__ void __launch_bounds__(kPix, 4) track_tile_kernel(TrackArgs a) {
+    pdl_begin();
     __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
@@ -643,6 +644,7 @@ template <bool DO_GN>
 __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles, DevPose* pose, double* out,
                         double eig_eps, double* step_out) {
+    pdl_begin();
     __shared__ double s_w[8][32];
     __shared__ double s_part[32];
     __shared__ double s_tot[27];
@@ -845,30 +847,26 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
 cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
     const int T = a.ntx * a.nty;
     if (T <= 0) return cudaSuccess;
-    if (a.render_only)
-        track_tile_kernel<true><<<T, kPix, 0, s>>>(a);
-    else
-        track_tile_kernel<false><<<T, kPix, 0, s>>>(a);
-    return cudaGetLastError();
+    if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a);
+    return launch_chained(track_tile_kernel<false>, dim3(T), dim3(kPix), 0, s, a);
 }
 
 cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s) {
     const int T = a.ntx * a.nty;
     if (T <= 0) return cudaSuccess;
-    track_tile_kernel<false, true><<<T, kPix, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_chained(track_tile_kernel<false, true>, dim3(T), dim3(kPix), 0, s, a);
 }
 
 cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                 cudaStream_t s) {
-    track_reduce_kernel<false><<<kRedCtas, 256, 0, s>>>(tile_out, num_tiles, pose, out, 0.0, nullptr);
-    return cudaGetLastError();
+    return launch_chained(track_reduce_kernel<false>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles, pose, out,
+                          0.0, static_cast<double*>(nullptr));
 }
 
 cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                    double eig_eps, double* step_out, cudaStream_t s) {
-    track_reduce_kernel<true><<<kRedCtas, 256, 0, s>>>(tile_out, num_tiles, pose, out, eig_eps, step_out);
-    return cudaGetLastError();
+    return launch_chained(track_reduce_kernel<true>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles, pose, out,
+                          eig_eps, step_out);
 }
 
 }  // namespace fvgs
