@@ -46,6 +46,20 @@ __global__ void set_pose_kernel(DevPose* dst, fvgs_pose p) {
     }
 }
 
+// The same from a pose in device memory (filled by a host-to-device copy that
+// a captured frame graph replays with the current request's pose).
+__global__ void set_pose_dev_kernel(DevPose* dst, const fvgs_pose* src) {
+    pdl_begin();
+    for (int k = 0; k < 3; ++k) {
+        dst->t[k] = src->position[k];
+        dst->td[k] = (double)src->position[k];
+    }
+    for (int k = 0; k < 4; ++k) {
+        dst->q[k] = src->orientation[k];
+        dst->qd[k] = (double)src->orientation[k];
+    }
+}
+
 __global__ void upload_pack_kernel(const float* pos, const float* scl, const float* rot, const float* col,
                                    const float* opa, uint32_t n, float4* gpos, float4* gscl, float4* grot,
                                    float4* gcol) {
@@ -166,6 +180,35 @@ struct fvgs_session {
 
     int last_W = 0, last_H = 0, last_T = 0;
     bool has_binning = false, has_track = false, dbg_proj_valid = false, has_map = false;
+
+    // Asynchronous frames (fvgs_frame_submit / fvgs_frame_wait).  A frame
+    // whose binning history is valid is captured once as a CUDA graph and
+    // replayed; the request's pose reaches it through d_pose_in.  gen changes
+    // with every device allocation (a graph holds buffer addresses).
+    struct FrameGraph {
+        bool valid = false;
+        int level = 0, iterations = 0, W = 0, H = 0;
+        fvgs_intrinsics K{};
+        float eta = -1.f;
+        uint64_t gen = 0;
+        uint32_t *vals_in = nullptr, *vals_out = nullptr, *vals_alt_out = nullptr;
+        uint2 *ranges_in = nullptr, *ranges_out = nullptr, *ranges_prev_out = nullptr;
+        uint64_t launches[FVGS_K_COUNT] = {};
+        cudaGraphExec_t exec = nullptr;
+    };
+    FrameGraph graphs[2];
+    int graph_next = 0;
+    uint64_t gen = 1;
+    fvgs_pose* d_pose_in = nullptr;
+    cudaEvent_t frame_done = nullptr;
+    bool frame_pending = false;
+    struct FrameRequest {
+        fvgs_pose pose{};
+        fvgs_intrinsics K{};
+        int level = 0, iterations = 0;
+        float eta = -1.f;
+    } req;
+    uint64_t frames_graphed = 0, frames_eager = 0;
 };
 
 namespace {
@@ -195,6 +238,7 @@ int dev_alloc(fvgs_session* s, T** p, size_t count) {
     }
     s->allocations.push_back(v);
     s->footprint += sizeof(T) * count;
+    ++s->gen;
     *p = static_cast<T*>(v);
     return FVGS_OK;
 }
@@ -206,6 +250,7 @@ void dev_free(fvgs_session* s, T*& p, size_t count) {
     if (it != s->allocations.end()) s->allocations.erase(it);
     cudaFree(p);
     s->footprint -= sizeof(T) * (count ? count : 1);
+    ++s->gen;
     p = nullptr;
 }
 
@@ -675,6 +720,9 @@ int fvgs_session_destroy(fvgs_session* s) {
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_pose) cudaFreeHost(s->h_pose);
     if (s->h_devpose) cudaFreeHost(s->h_devpose);
+    for (auto& g : s->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (s->frame_done) cudaEventDestroy(s->frame_done);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return FVGS_OK;
@@ -742,6 +790,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->seg.large_ctrl, 4);  // [0..1] large-bucket list control, [2] scatter chunk counter
     FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
     FV_A(s->pose, 1);
+    FV_A(s->d_pose_in, 1);
     FV_A(s->jj, 48);
     FV_A(s->step, 8);
     FV_A(s->st, 1);
@@ -757,6 +806,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
         cudaMallocHost(&s->h_pose, sizeof(fvgs_pose)) != cudaSuccess ||
         cudaMallocHost(&s->h_devpose, sizeof(DevPose)) != cudaSuccess)
         return fail(FVGS_E_NOMEM);
+    if (cudaEventCreateWithFlags(&s->frame_done, cudaEventDisableTiming) != cudaSuccess) return fail(FVGS_E_CUDA);
     if (sort_init(&s->sort, device) != cudaSuccess) return fail(FVGS_E_CUDA);
     const uint64_t cap0 = std::max<uint64_t>(1u << 20, 8ull * N);
     if ((rc = alloc_instances(s, std::min<uint64_t>(cap0, 0xffffffffull))) != FVGS_OK) return fail(rc);
@@ -783,6 +833,7 @@ int fvgs_session_sync(fvgs_session* s) {
 
 int fvgs_session_set_debug(fvgs_session* s, uint32_t flags) {
     if (!s) return FVGS_E_INVALID;
+    ++s->gen;  // captured frames follow the debug outputs of their capture
     FV_CK(cudaSetDevice(s->device));
     if ((flags & FVGS_DEBUG_PROJECTION) && !s->dbg_cov) {
         FV_TRY(dev_alloc(s, &s->dbg_cov, 3 * (size_t)s->cap_g));
@@ -1064,6 +1115,240 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
     return FVGS_E_CAPACITY;
 }
 
+namespace {
+
+// One frame on the session's stream: the request's pose (already in the
+// pinned staging s->h_pose) to the device, `iterations` Gauss-Newton steps,
+// optionally a mapping step at the tracked pose, then the result pose, last
+// step and status back to pinned host memory.
+int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
+    const FrameLevel& f = s->lv[r.level];
+    FV_TRY(reset_status(s));
+    FV_CK(cudaMemcpyAsync(s->d_pose_in, s->h_pose, sizeof(fvgs_pose), cudaMemcpyHostToDevice, s->stream));
+    FV_CK(launch_chained(set_pose_dev_kernel, dim3(1), dim3(1), 0, s->stream, s->pose,
+                         static_cast<const fvgs_pose*>(s->d_pose_in)));
+    for (int it = 0; it < r.iterations; ++it) {
+        FV_TRY(enqueue_bin(s, &r.K, f.W, f.H));
+        FV_TRY(enqueue_track(s, &r.K, f, false, false));
+        KScope k(s, FVGS_K_GN, 1);
+        FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step, s->stream));
+    }
+    if (r.eta >= 0.f) {
+        FV_TRY(enqueue_bin(s, &r.K, f.W, f.H));
+        FV_TRY(enqueue_map(s, &r.K, f, r.eta));
+    }
+    FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+    return FVGS_OK;
+}
+
+bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
+                       const fvgs_session::FrameRequest& r) {
+    const FrameLevel& f = s->lv[r.level];
+    return g.valid && g.gen == s->gen && g.level == r.level && g.iterations == r.iterations && g.W == f.W &&
+           g.H == f.H && g.eta == r.eta && g.K.fx == r.K.fx && g.K.fy == r.K.fy && g.K.cx == r.K.cx &&
+           g.K.cy == r.K.cy && g.vals_in == s->vals && g.ranges_in == s->ranges;
+}
+
+// Whether a frame may run from a captured graph: the binning history must be
+// valid (every binning of the frame is then incremental and needs no
+// host-side memset), and no per-call host work may be involved.
+bool frame_graphable(const fvgs_session* s, const fvgs_session::FrameRequest& r) {
+    const FrameLevel& f = s->lv[r.level];
+    const int ntx = (f.W + s->params.tile_w - 1) / s->params.tile_w;
+    const int nty = (f.H + s->params.tile_h - 1) / s->params.tile_h;
+    const bool literal = (s->params.quirks & (FVGS_Q_CULLED_SLOTS | FVGS_Q_RANGE_LAUNCH)) != 0;
+    return s->hist_ok && s->diff_clean && s->hist_ntx == ntx && s->hist_nty == nty && s->timing_mask == 0 &&
+           !(s->debug & FVGS_DEBUG_RADIX_SORT) && !literal;
+}
+
+int launch_frame(fvgs_session* s) {
+    const fvgs_session::FrameRequest& r = s->req;
+    *s->h_pose = r.pose;
+    if (!frame_graphable(s, r)) {
+        ++s->frames_eager;
+        return enqueue_frame(s, r);
+    }
+    for (auto& g : s->graphs) {
+        if (!frame_key_matches(g, s, r)) continue;
+        FV_CK(cudaGraphLaunch(g.exec, s->stream));
+        s->vals = g.vals_out;
+        s->sort.vals_alt = g.vals_alt_out;
+        s->ranges = g.ranges_out;
+        s->ranges_prev = g.ranges_prev_out;
+        for (int c = 0; c < FVGS_K_COUNT; ++c) s->launches[c] += g.launches[c];
+        s->has_binning = true;
+        ++s->frames_graphed;
+        return FVGS_OK;
+    }
+    // capture this frame shape (two slots: a frame with an odd number of
+    // binnings leaves the ping-pong buffers swapped, so consecutive frames
+    // alternate between two graphs)
+    fvgs_session::FrameGraph& g = s->graphs[s->graph_next];
+    s->graph_next ^= 1;
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    g.valid = false;
+    // host-side binning state before the capture: a capture enqueues nothing,
+    // so if it fails the frame runs eagerly from exactly this state
+    uint64_t before[FVGS_K_COUNT];
+    std::memcpy(before, s->launches, sizeof(before));
+    uint32_t* const vals0 = s->vals;
+    uint32_t* const vals_alt0 = s->sort.vals_alt;
+    uint2* const ranges0 = s->ranges;
+    uint2* const ranges_prev0 = s->ranges_prev;
+    const bool hist0 = s->hist_ok, clean0 = s->diff_clean, keys0 = s->keys_valid, binned0 = s->has_binning;
+    const int ntx0 = s->hist_ntx, nty0 = s->hist_nty, lw0 = s->last_W, lh0 = s->last_H, lt0 = s->last_T;
+    g.vals_in = s->vals;
+    g.ranges_in = s->ranges;
+    cudaGraph_t graph = nullptr;
+    int rc = FVGS_OK;
+    cudaError_t ec = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (ec == cudaSuccess) {
+        rc = enqueue_frame(s, r);
+        ec = cudaStreamEndCapture(s->stream, &graph);
+    }
+    if (rc == FVGS_OK && ec == cudaSuccess && graph) ec = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != FVGS_OK || ec != cudaSuccess || !g.exec) {
+        cudaGetLastError();
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        std::memcpy(s->launches, before, sizeof(before));
+        s->vals = vals0;
+        s->sort.vals_alt = vals_alt0;
+        s->ranges = ranges0;
+        s->ranges_prev = ranges_prev0;
+        s->hist_ok = hist0;
+        s->diff_clean = clean0;
+        s->keys_valid = keys0;
+        s->has_binning = binned0;
+        s->hist_ntx = ntx0;
+        s->hist_nty = nty0;
+        s->last_W = lw0;
+        s->last_H = lh0;
+        s->last_T = lt0;
+        ++s->frames_eager;
+        return enqueue_frame(s, r);
+    }
+    const FrameLevel& f = s->lv[r.level];
+    g.level = r.level;
+    g.iterations = r.iterations;
+    g.W = f.W;
+    g.H = f.H;
+    g.K = r.K;
+    g.eta = r.eta;
+    g.gen = s->gen;
+    g.vals_out = s->vals;
+    g.vals_alt_out = s->sort.vals_alt;
+    g.ranges_out = s->ranges;
+    g.ranges_prev_out = s->ranges_prev;
+    for (int c = 0; c < FVGS_K_COUNT; ++c) g.launches[c] = s->launches[c] - before[c];
+    g.valid = true;
+    FV_CK(cudaGraphLaunch(g.exec, s->stream));
+    ++s->frames_graphed;
+    return FVGS_OK;
+}
+
+}  // namespace
+
+int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                      float map_eta) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0 || !(map_eta == map_eta))
+        return FVGS_E_INVALID;
+    if (s->frame_pending) return FVGS_E_STATE;
+    const FrameLevel& f = s->lv[level];
+    if (!f.rgb || s->n_g == 0) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    if (map_eta >= 0.f) FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
+    s->req.pose = *pose;
+    s->req.K = *K;
+    s->req.level = level;
+    s->req.iterations = iterations;
+    s->req.eta = map_eta >= 0.f ? map_eta : -1.f;
+    FV_TRY(launch_frame(s));
+    FV_CK(cudaEventRecord(s->frame_done, s->stream));
+    s->frame_pending = true;
+    return FVGS_OK;
+}
+
+int fvgs_frame_poll(fvgs_session* s, int* done) {
+    if (!s || !done) return FVGS_E_INVALID;
+    if (!s->frame_pending) return FVGS_E_STATE;
+    const cudaError_t e = cudaEventQuery(s->frame_done);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return FVGS_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventQuery");
+    *done = 1;
+    return FVGS_OK;
+}
+
+int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->frame_pending) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    s->frame_pending = false;
+    FV_CK(cudaEventSynchronize(s->frame_done));
+    collect_timing(s);
+    int retry = 0;
+    FV_TRY(check_status(s, &retry));
+    // An instance overflow (the buffers have grown) or an inconsistent
+    // incremental binning: run the frame again, eagerly, from the same pose.
+    for (int attempt = 0; retry && attempt < 4; ++attempt) {
+        const FrameLevel& f = s->lv[s->req.level];
+        if (s->req.eta >= 0.f)
+            FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
+        *s->h_pose = s->req.pose;
+        ++s->frames_eager;
+        FV_TRY(enqueue_frame(s, s->req));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        FV_TRY(check_status(s, &retry));
+    }
+    if (retry) return FVGS_E_CAPACITY;
+    if (pose) {
+        for (int k = 0; k < 3; ++k) pose->position[k] = s->h_devpose->t[k];
+        for (int k = 0; k < 4; ++k) pose->orientation[k] = s->h_devpose->q[k];
+    }
+    if (last_step) std::memcpy(last_step, s->h_jj + 42, sizeof(double) * 6);
+    s->has_track = s->req.iterations > 0;
+    if (s->req.eta >= 0.f) s->has_map = true;
+    return FVGS_OK;
+}
+
+int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K, const int* levels,
+                    int iterations, const float* map_etas, int n) {
+    if (!sessions || !poses || !K || n < 0) return FVGS_E_INVALID;
+    int first_error = FVGS_OK;
+    int submitted = 0;
+    for (; submitted < n; ++submitted) {
+        const int rc = fvgs_frame_submit(sessions[submitted], &poses[submitted], &K[submitted],
+                                         levels ? levels[submitted] : 0, iterations,
+                                         map_etas ? map_etas[submitted] : -1.f);
+        if (rc != FVGS_OK) {
+            first_error = rc;
+            break;
+        }
+    }
+    for (int i = 0; i < submitted; ++i) {
+        const int rc = fvgs_frame_wait(sessions[i], &poses[i], nullptr);
+        if (rc != FVGS_OK && first_error == FVGS_OK) first_error = rc;
+    }
+    return first_error;
+}
+
+int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager) {
+    if (!s) return FVGS_E_INVALID;
+    if (graphed) *graphed = s->frames_graphed;
+    if (eager) *eager = s->frames_eager;
+    return FVGS_OK;
+}
+
 int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height, float* rgb,
                 float* depth, float* final_T, uint32_t* n_contrib) {
     if (!s || !valid_pose(pose) || !K) return FVGS_E_INVALID;
@@ -1101,6 +1386,7 @@ int fvgs_session_set_timing(fvgs_session* s, uint32_t class_mask) {
     FV_CK(cudaStreamSynchronize(s->stream));
     collect_timing(s);
     s->timing_mask = class_mask;
+    ++s->gen;
     return FVGS_OK;
 }
 

@@ -338,3 +338,114 @@ class Session:
         d2f[:, 12] = n2
         return dict(final_T=fT, n_contrib=nc, color=col, depth=dep, delta2d=d2f,
                     delta3d=None if d3 is None else d3[:, :14].astype(np.float64))
+
+    # ---- asynchronous frames (CUDA-graph replay once the binning history is valid)
+    def frame_submit(self, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None):
+        _check(self.lib.fvgs_frame_submit(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
+                                          C.c_int(iterations), C.c_float(-1.0 if map_eta is None else map_eta)),
+               "fvgs_frame_submit")
+
+    def frame_poll(self) -> bool:
+        d = C.c_int()
+        _check(self.lib.fvgs_frame_poll(self.h, C.byref(d)), "fvgs_frame_poll")
+        return bool(d.value)
+
+    def frame_wait(self):
+        p = Pose()
+        step = np.zeros(6, np.float64)
+        _check(self.lib.fvgs_frame_wait(self.h, C.byref(p), _ptr(step)), "fvgs_frame_wait")
+        return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
+
+    def frame_stats(self) -> dict:
+        g, e = C.c_uint64(), C.c_uint64()
+        _check(self.lib.fvgs_session_frame_stats(self.h, C.byref(g), C.byref(e)), "fvgs_session_frame_stats")
+        return dict(graphed=int(g.value), eager=int(e.value))
+
+
+def frames_run(sessions, poses, Ks, iterations: int = 20, levels=None, map_etas=None):
+    """One frame on each session, overlapped on the device (fvgs_frames_run)."""
+    lib = load_library()
+    n = len(sessions)
+    hs = (C.c_void_p * n)(*[s.h for s in sessions])
+    ps = (Pose * n)(*[make_pose(p) for p in poses])
+    ks = (Intrinsics * n)(*[make_intr(k) for k in Ks])
+    lv = None if levels is None else (C.c_int * n)(*levels)
+    et = None if map_etas is None else (C.c_float * n)(*[(-1.0 if e is None else e) for e in map_etas])
+    _check(lib.fvgs_frames_run(hs, ps, ks, lv, C.c_int(iterations), et, C.c_int(n)), "fvgs_frames_run")
+    return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
+
+
+# ---- serving (include/fvgs_server.h) ----
+class ServerRequest(C.Structure):
+    _fields_ = [("pose", Pose), ("K", Intrinsics), ("level", C.c_int), ("iterations", C.c_int),
+                ("map_eta", C.c_float), ("tag", C.c_uint64), ("t_arrival", C.c_double)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("slot", C.c_int), ("status", C.c_int), ("pose", Pose),
+                ("last_step", C.c_double * 6), ("t_arrival", C.c_double), ("t_launch", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class Server:
+    """Continuous-batching server over many sessions (fvgs_server_*)."""
+
+    def __init__(self, memory_budget_bytes: int, max_inflight: int = 16):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        _check(self.lib.fvgs_server_create(C.c_uint64(memory_budget_bytes), C.c_int(max_inflight),
+                                           C.byref(self.h)), "fvgs_server_create")
+
+    def close(self):
+        if self.h:
+            _check(self.lib.fvgs_server_destroy(self.h), "fvgs_server_destroy")
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def admit(self, session) -> int:
+        slot = C.c_int()
+        _check(self.lib.fvgs_server_admit(self.h, session.h, C.byref(slot)), "fvgs_server_admit")
+        return int(slot.value)
+
+    def release(self, slot: int):
+        _check(self.lib.fvgs_server_release(self.h, C.c_int(slot)), "fvgs_server_release")
+
+    @staticmethod
+    def now() -> float:
+        t = C.c_double()
+        _check(load_library().fvgs_server_now(C.byref(t)), "fvgs_server_now")
+        return float(t.value)
+
+    def submit(self, slot: int, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None,
+               tag: int = 0, t_arrival: float = 0.0):
+        r = ServerRequest()
+        r.pose = make_pose(pose)
+        r.K = make_intr(K)
+        r.level, r.iterations = level, iterations
+        r.map_eta = -1.0 if map_eta is None else map_eta
+        r.tag, r.t_arrival = tag, t_arrival
+        _check(self.lib.fvgs_server_submit(self.h, C.c_int(slot), C.byref(r)), "fvgs_server_submit")
+
+    def results(self, wait_for: int = 0, max_results: int = 4096):
+        buf = (ServerResult * max_results)()
+        n = C.c_int()
+        _check(self.lib.fvgs_server_results(self.h, buf, C.c_int(max_results), C.c_int(wait_for), C.byref(n)),
+               "fvgs_server_results")
+        out = []
+        for r in buf[:n.value]:
+            out.append(dict(tag=int(r.tag), slot=int(r.slot), status=int(r.status),
+                            pose=(np.array(r.pose.position[:], np.float32), np.array(r.pose.orientation[:], np.float32)),
+                            t_arrival=r.t_arrival, t_launch=r.t_launch, t_done=r.t_done))
+        return out
+
+    def stats(self) -> dict:
+        ab, inf, la, co = C.c_uint64(), C.c_int(), C.c_uint64(), C.c_uint64()
+        _check(self.lib.fvgs_server_stats(self.h, C.byref(ab), C.byref(inf), C.byref(la), C.byref(co)),
+               "fvgs_server_stats")
+        return dict(admitted_bytes=int(ab.value), inflight=int(inf.value), launched=int(la.value),
+                    completed=int(co.value))

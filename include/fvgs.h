@@ -154,6 +154,32 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
                      double* last_step);
 
 /*
+ * Asynchronous frames, for serving and batching many sessions at once.
+ * fvgs_frame_submit enqueues one frame on the session's stream and returns:
+ * `iterations` Gauss-Newton steps from `pose` (as fvgs_track_frame), then,
+ * when map_eta >= 0, one mapping step at the tracked pose (as fvgs_map_step).
+ * Once the session's binning history is valid, a frame of a given shape
+ * (level, iterations, intrinsics, mapping) is captured as a CUDA graph on
+ * first use and replayed afterwards.  fvgs_frame_poll reports completion
+ * without blocking; fvgs_frame_wait completes the frame (repeating it
+ * eagerly if the instance buffers had to grow) and returns the pose and last
+ * step (both nullable).  One frame per session may be in flight.  The
+ * reference has no counterpart: it tracks one frame at a time on one map.
+ */
+int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                      float map_eta);
+int fvgs_frame_poll(fvgs_session* s, int* done);
+int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step);
+/* Batched frames: submit one frame on each of n sessions (each on its own
+ * stream, so their kernels overlap on the device), then wait for all;
+ * poses[i] is read and overwritten, levels and map_etas nullable (level 0,
+ * no mapping).  Returns the first error. */
+int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K, const int* levels,
+                    int iterations, const float* map_etas, int n);
+/* Frames of the session that ran from a captured graph / eagerly. */
+int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager);
+
+/*
  * Forward blend with the tracking kernel's semantics for every pixel of a
  * width x height view (observed depth treated as valid everywhere): colour
  * incl. background, median depth, final transmittance, contributor count.

@@ -1,0 +1,176 @@
+"""Asynchronous, batched and served frames.
+
+A frame submitted asynchronously (and, once the binning history is valid,
+replayed from a captured CUDA graph) must give exactly the result of the
+synchronous per-frame path; frames of several sessions run together
+(fvgs_frames_run, or the continuous-batching server) must give exactly the
+results each session gives alone.  Every session's kernels touch only its own
+buffers, in the same order, so tracking results agree bit for bit.  The
+mapping backward pass sums per-Gaussian gradients with float atomics, whose
+rounding depends on the order the tiles finish in (run to run, alone or not),
+so after mapping steps the following poses are compared within 1e-5 and
+the parameters within 1e-3 relative: Adam divides by the root of the second
+moment, so an update whose gradient is near zero turns last-bit gradient
+differences into larger relative parameter differences, and they compound
+over steps (two identical runs of one session differ the same way).
+"""
+import numpy as np
+import pytest
+
+from conftest import make_frame, scaled_camera
+from f_vigs_slam_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+ITERS = 6
+MAP_RTOL = 1e-3
+POSE_ATOL = 1e-5
+
+
+def _scene_frame(oracle, seed, n, scale):
+    W, H, K = scaled_camera(scale)
+    scene = S.cam_box(n, seed=seed)
+    P = oracle.default_params()
+    rng = np.random.default_rng(seed + 100)
+    true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
+    rgb, d, gx, gy = make_frame(oracle, scene, true_pose, K, W, H, P)
+    starts = [S.perturb(true_pose, 0.5, 1.0, rng) for _ in range(4)]
+    return dict(W=W, H=H, K=K, scene=scene, frame=(rgb, d, gx, gy), starts=starts)
+
+
+def _session(fv, case):
+    s = fv.Session(case["scene"].n, case["W"], case["H"])
+    s.upload(case["scene"])
+    s.set_frame(0, *case["frame"])
+    return s
+
+
+def _same(a, b):
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def _close(a, b):
+    np.testing.assert_allclose(a[0], b[0], rtol=0, atol=POSE_ATOL)
+    np.testing.assert_allclose(a[1], b[1], rtol=0, atol=POSE_ATOL)
+
+
+def test_async_frames_equal_sync_frames(oracle, fvgs_lib):
+    """submit/wait (eager first, then graph replays) equals track_frame bit
+    for bit; with a mapping step in the frame it equals track_frame +
+    map_step within the mapping tolerance."""
+    fv = fvgs_lib
+    case = _scene_frame(oracle, 1, 20_000, 0.5)
+    eta = 0.002
+    with _session(fv, case) as a, _session(fv, case) as b:
+        for start in case["starts"]:
+            pa, _ = a.track_frame(start, case["K"], iterations=ITERS)
+            b.frame_submit(start, case["K"], iterations=ITERS)
+            pb, _ = b.frame_wait()
+            _same(pa, pb)
+        st = b.frame_stats()
+        assert st["graphed"] >= 2, st  # later frames replayed the captured graph
+        for start in case["starts"]:
+            pa, _ = a.track_frame(start, case["K"], iterations=ITERS)
+            a.map_step(pa, case["K"], eta)
+            b.frame_submit(start, case["K"], iterations=ITERS, map_eta=eta)
+            pb, _ = b.frame_wait()
+            _close(pa, pb)
+        assert b.frame_stats()["graphed"] >= st["graphed"] + 2
+        ga, gb = a.download(), b.download()
+        for x, y in zip(ga, gb):
+            np.testing.assert_allclose(x, y, rtol=MAP_RTOL, atol=1e-5)
+
+
+def test_batched_frames_equal_alone(oracle, fvgs_lib):
+    """fvgs_frames_run over sessions of different sizes equals each alone."""
+    fv = fvgs_lib
+    cases = [_scene_frame(oracle, 2, 20_000, 0.5), _scene_frame(oracle, 3, 5_000, 0.25),
+             _scene_frame(oracle, 4, 40_000, 0.5)]
+    alone = []
+    for c in cases:
+        with _session(fv, c) as s:
+            seq = []
+            for start in c["starts"][:3]:
+                s.frame_submit(start, c["K"], iterations=ITERS)
+                seq.append(s.frame_wait()[0])
+            alone.append(seq)
+    sessions = [_session(fv, c) for c in cases]
+    try:
+        for k in range(3):
+            got = fv.frames_run(sessions, [c["starts"][k] for c in cases], [c["K"] for c in cases],
+                                iterations=ITERS)
+            for i in range(len(cases)):
+                _same(got[i], alone[i][k])
+    finally:
+        for s in sessions:
+            s.close()
+
+
+def test_server_same_alone_and_in_mix(oracle, fvgs_lib):
+    """Requests of three sessions submitted at once to the server (running
+    concurrently on the device) return the poses each session gives alone:
+    bit for bit for tracking requests, within the mapping tolerance after a
+    request that carried a mapping step."""
+    fv = fvgs_lib
+    cases = [_scene_frame(oracle, 5, 20_000, 0.5), _scene_frame(oracle, 6, 10_000, 0.25),
+             _scene_frame(oracle, 7, 30_000, 0.5)]
+    mapped = 2  # request k == 2 carries a mapping step
+    alone = []
+    for c in cases:
+        with _session(fv, c) as s:
+            seq = []
+            for k, start in enumerate(c["starts"]):
+                s.frame_submit(start, c["K"], iterations=ITERS, map_eta=0.002 if k == mapped else None)
+                seq.append(s.frame_wait()[0])
+            alone.append(seq)
+    sessions = [_session(fv, c) for c in cases]
+    try:
+        with fv.Server(memory_budget_bytes=1 << 40, max_inflight=8) as sv:
+            slots = [sv.admit(s) for s in sessions]
+            for k in range(4):
+                for i, c in enumerate(cases):
+                    sv.submit(slots[i], c["starts"][k], c["K"], iterations=ITERS,
+                              map_eta=0.002 if k == mapped else None, tag=100 * i + k)
+            res = []
+            while len(res) < 12:
+                res += sv.results(wait_for=12 - len(res))
+            assert all(r["status"] == 0 for r in res)
+            for r in res:
+                i, k = divmod(r["tag"], 100)
+                if k <= mapped:
+                    _same(r["pose"], alone[i][k])
+                else:
+                    _close(r["pose"], alone[i][k])
+                assert r["t_arrival"] <= r["t_launch"] <= r["t_done"]
+            # a session's requests complete in order
+            for i in range(3):
+                order = [r["tag"] % 100 for r in res if r["tag"] // 100 == i]
+                assert order == sorted(order)
+            assert sv.stats()["completed"] == 12
+    finally:
+        for s in sessions:
+            s.close()
+
+
+def test_server_admission_by_footprint(fvgs_lib):
+    """A session is admitted only while the admitted footprints fit the budget."""
+    fv = fvgs_lib
+    W, H, K = scaled_camera(0.25)
+    a = fv.Session(5000, W, H)
+    b = fv.Session(5000, W, H)
+    try:
+        fa, fb = a.footprint(), b.footprint()
+        with fv.Server(memory_budget_bytes=fa + fb // 2, max_inflight=2) as sv:
+            sa = sv.admit(a)
+            with pytest.raises(fv.FvgsError) as e:
+                sv.admit(b)
+            assert e.value.status == -7  # FVGS_E_ADMISSION
+            assert sv.stats()["admitted_bytes"] == fa
+            sv.release(sa)
+            sb = sv.admit(b)
+            assert sv.stats()["admitted_bytes"] == fb
+            sv.release(sb)
+    finally:
+        a.close()
+        b.close()
