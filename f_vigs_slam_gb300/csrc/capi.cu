@@ -194,10 +194,13 @@ struct fvgs_session {
         uint32_t *vals_in = nullptr, *vals_out = nullptr, *vals_alt_out = nullptr;
         uint2 *ranges_in = nullptr, *ranges_out = nullptr, *ranges_prev_out = nullptr;
         uint64_t launches[FVGS_K_COUNT] = {};
+        uint64_t last_use = 0;
         cudaGraphExec_t exec = nullptr;
     };
-    FrameGraph graphs[2];
-    int graph_next = 0;
+    // frame shapes x ping-pong parities in use (a frame with an odd number of
+    // binnings swaps the parity for the next one)
+    FrameGraph graphs[4];
+    uint64_t graph_clock = 0;
     uint64_t gen = 1;
     fvgs_pose* d_pose_in = nullptr;
     cudaEvent_t frame_done = nullptr;
@@ -1173,6 +1176,7 @@ int launch_frame(fvgs_session* s) {
     for (auto& g : s->graphs) {
         if (!frame_key_matches(g, s, r)) continue;
         FV_CK(cudaGraphLaunch(g.exec, s->stream));
+        g.last_use = ++s->graph_clock;
         s->vals = g.vals_out;
         s->sort.vals_alt = g.vals_alt_out;
         s->ranges = g.ranges_out;
@@ -1182,11 +1186,16 @@ int launch_frame(fvgs_session* s) {
         ++s->frames_graphed;
         return FVGS_OK;
     }
-    // capture this frame shape (two slots: a frame with an odd number of
-    // binnings leaves the ping-pong buffers swapped, so consecutive frames
-    // alternate between two graphs)
-    fvgs_session::FrameGraph& g = s->graphs[s->graph_next];
-    s->graph_next ^= 1;
+    // capture this frame shape into a free or the least recently used slot
+    int victim = 0;
+    for (int i = 0; i < 4; ++i) {
+        if (!s->graphs[i].valid || s->graphs[i].gen != s->gen) {
+            victim = i;
+            break;
+        }
+        if (s->graphs[i].last_use < s->graphs[victim].last_use) victim = i;
+    }
+    fvgs_session::FrameGraph& g = s->graphs[victim];
     if (g.exec) {
         cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
@@ -1248,6 +1257,7 @@ int launch_frame(fvgs_session* s) {
     g.ranges_prev_out = s->ranges_prev;
     for (int c = 0; c < FVGS_K_COUNT; ++c) g.launches[c] = s->launches[c] - before[c];
     g.valid = true;
+    g.last_use = ++s->graph_clock;
     FV_CK(cudaGraphLaunch(g.exec, s->stream));
     ++s->frames_graphed;
     return FVGS_OK;

@@ -78,7 +78,12 @@ struct fvgs_server {
                     sl.running = sl.queue.front();
                     sl.queue.pop_front();
                     const fvgs_server_request& r = sl.running;
-                    const int rc = fvgs_frame_submit(sl.session, &r.pose, &r.K, r.level, r.iterations, r.map_eta);
+                    int rc = FVGS_OK;
+                    if (r.rgb)
+                        rc = fvgs_set_frame(sl.session, r.level, r.rgb, r.depth, r.grad_x, r.grad_y, r.width,
+                                            r.height);
+                    if (rc == FVGS_OK)
+                        rc = fvgs_frame_submit(sl.session, &r.pose, &r.K, r.level, r.iterations, r.map_eta);
                     sl.t_launch = now_s();
                     if (rc != FVGS_OK) {
                         fvgs_server_result res{};

@@ -378,7 +378,9 @@ def frames_run(sessions, poses, Ks, iterations: int = 20, levels=None, map_etas=
 # ---- serving (include/fvgs_server.h) ----
 class ServerRequest(C.Structure):
     _fields_ = [("pose", Pose), ("K", Intrinsics), ("level", C.c_int), ("iterations", C.c_int),
-                ("map_eta", C.c_float), ("tag", C.c_uint64), ("t_arrival", C.c_double)]
+                ("map_eta", C.c_float), ("tag", C.c_uint64), ("t_arrival", C.c_double),
+                ("rgb", C.c_void_p), ("depth", C.c_void_p), ("grad_x", C.c_void_p), ("grad_y", C.c_void_p),
+                ("width", C.c_int), ("height", C.c_int)]
 
 
 class ServerResult(C.Structure):
@@ -422,13 +424,17 @@ class Server:
         return float(t.value)
 
     def submit(self, slot: int, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None,
-               tag: int = 0, t_arrival: float = 0.0):
+               tag: int = 0, t_arrival: float = 0.0, frame=None):
+        """frame: optional (rgb_ptr, depth_ptr, gx_ptr, gy_ptr, W, H) of memory that stays valid (pinned
+        host or device) until the result is back."""
         r = ServerRequest()
         r.pose = make_pose(pose)
         r.K = make_intr(K)
         r.level, r.iterations = level, iterations
         r.map_eta = -1.0 if map_eta is None else map_eta
         r.tag, r.t_arrival = tag, t_arrival
+        if frame is not None:
+            r.rgb, r.depth, r.grad_x, r.grad_y, r.width, r.height = frame
         _check(self.lib.fvgs_server_submit(self.h, C.c_int(slot), C.byref(r)), "fvgs_server_submit")
 
     def results(self, wait_for: int = 0, max_results: int = 4096):

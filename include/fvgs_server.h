@@ -29,6 +29,16 @@ typedef struct fvgs_server_request {
     float map_eta;         /* >= 0: a mapping step with this learning rate follows */
     uint64_t tag;          /* caller's request id, returned with the result */
     double t_arrival;      /* arrival time (fvgs_server_now clock); <= 0: time of submission */
+    /* Optional new observed frame for `level` (as fvgs_set_frame; host
+     * memory should be pinned so the copies overlap): copied to the device on
+     * the session's stream right before the frame.  rgb == NULL: keep the
+     * session's current frame.  The buffers must stay valid until the result
+     * is returned. */
+    const float* rgb;
+    const float* depth;
+    const float* grad_x;
+    const float* grad_y;
+    int width, height;
 } fvgs_server_request;
 
 typedef struct fvgs_server_result {
