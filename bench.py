@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GAUSS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sessions", type=int, default=32)
+    ap.add_argument("--plain-only", action="store_true",
+                    help="only the large plain workload (for profiling runs; not the benchmark line)")
     return ap.parse_args()
 
 
@@ -532,7 +534,7 @@ def run_serving(args, fvgs, S, torch, dev):
         r = 0
         while True:
             t += rng.exponential(1.0 / hz)
-            if t > SERVE_SECONDS:
+            if t > SERVE_SECONDS and r > 0:  # at least one request per session
                 break
             f = w["frames"][r % len(w["frames"])]
             preqs.append((i, r, f, ETA if r % MAP_EVERY == MAP_EVERY - 1 else None))
@@ -606,6 +608,10 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
 
     large = run_large(args, fvgs, S, torch, dev, stream, rank, world)
+    if args.plain_only:
+        if rank == 0:
+            print(json.dumps({"metric": "large plain workload only (profiling run)", "large_plain": large}), flush=True)
+        return 0
     srv = run_serving(args, fvgs, S, torch, dev)
     srv_fps, plain_fps, e2e_fps = max_over_ranks_rate([srv["served_frames_per_s"], srv["plain_frames_per_s"],
                                                        srv["e2e_frames_per_s"]], dev, world)

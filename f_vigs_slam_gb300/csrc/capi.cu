@@ -136,6 +136,11 @@ struct fvgs_session {
     int hist_ntx = 0, hist_nty = 0;
 
     FrameLevel lv[kMaxLevels];
+    // frame preprocessing: 8-bit colour pyramid and the raw depth of a frame
+    uint8_t* pre_u8[kMaxLevels] = {};
+    size_t pre_u8_px[kMaxLevels] = {};
+    uint8_t* pre_raw = nullptr;  // camera depth as given (float or uint16)
+    size_t pre_raw_bytes = 0;
 
     DevPose* pose = nullptr;
     double* jj = nullptr;    // 42 doubles: JtJ[36], Jtr[6]
@@ -921,11 +926,9 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
     return FVGS_OK;
 }
 
-int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* depth, const float* grad_x,
-                   const float* grad_y, int width, int height) {
-    if (!s || level < 0 || level >= kMaxLevels || !rgb || !depth || !grad_x || !grad_y) return FVGS_E_INVALID;
-    if (check_view(s, width, height) != FVGS_OK) return FVGS_E_INVALID;
-    FV_CK(cudaSetDevice(s->device));
+namespace {
+
+int ensure_level(fvgs_session* s, int level, int width, int height) {
     FrameLevel& f = s->lv[level];
     const size_t px = (size_t)width * height;
     if (px > f.cap_px) {
@@ -941,6 +944,77 @@ int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* de
     }
     f.W = width;
     f.H = height;
+    return FVGS_OK;
+}
+
+}  // namespace
+
+int fvgs_preprocess_frame(fvgs_session* s, const uint8_t* color, const void* depth, int depth_u16_mm, int width,
+                          int height, int levels, int double_scale) {
+    if (!s || !color || !depth || levels < 1 || levels > kMaxLevels) return FVGS_E_INVALID;
+    if (check_view(s, width, height) != FVGS_OK) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px0 = (size_t)width * height;
+    const size_t raw_bytes = px0 * (depth_u16_mm ? sizeof(uint16_t) : sizeof(float));
+    if (raw_bytes > s->pre_raw_bytes) {
+        dev_free(s, s->pre_raw, s->pre_raw_bytes);
+        FV_TRY(dev_alloc(s, &s->pre_raw, raw_bytes));
+        s->pre_raw_bytes = raw_bytes;
+    }
+    int W = width, H = height;
+    for (int l = 0; l < levels; ++l) {
+        if (l > 0) {
+            W = (W + 1) / 2;
+            H = (H + 1) / 2;
+        }
+        const size_t px = (size_t)W * H;
+        if (px > s->pre_u8_px[l]) {
+            dev_free(s, s->pre_u8[l], 3 * s->pre_u8_px[l]);
+            FV_TRY(dev_alloc(s, &s->pre_u8[l], 3 * px));
+            s->pre_u8_px[l] = px;
+        }
+        FV_TRY(ensure_level(s, l, W, H));
+    }
+    FV_CK(cudaMemcpyAsync(s->pre_u8[0], color, 3 * px0, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaMemcpyAsync(s->pre_raw, depth, raw_bytes, cudaMemcpyDefault, s->stream));
+    FV_CK(launch_depth_in(s->pre_raw, depth_u16_mm, px0, s->lv[0].depth, s->stream));
+    for (int l = 0; l < levels; ++l) {
+        FrameLevel& f = s->lv[l];
+        if (l > 0) {
+            const FrameLevel& g = s->lv[l - 1];
+            FV_CK(launch_pyrdown_u8(s->pre_u8[l - 1], g.W, g.H, 3, s->pre_u8[l], s->stream));
+            FV_CK(launch_pyrdown_f32(g.depth, g.W, g.H, f.depth, s->stream));
+        }
+        FV_CK(launch_color_sobel(s->pre_u8[l], f.W, f.H, double_scale, f.rgb, f.gx, f.gy, s->stream));
+    }
+    return FVGS_OK;
+}
+
+int fvgs_download_frame(fvgs_session* s, int level, float* rgb, float* depth, float* grad_x, float* grad_y,
+                        int* width, int* height) {
+    if (!s || level < 0 || level >= kMaxLevels) return FVGS_E_INVALID;
+    const FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px = (size_t)f.W * f.H;
+    if (width) *width = f.W;
+    if (height) *height = f.H;
+    if (rgb) FV_CK(cudaMemcpyAsync(rgb, f.rgb, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    if (depth) FV_CK(cudaMemcpyAsync(depth, f.depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+    if (grad_x) FV_CK(cudaMemcpyAsync(grad_x, f.gx, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    if (grad_y) FV_CK(cudaMemcpyAsync(grad_y, f.gy, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* depth, const float* grad_x,
+                   const float* grad_y, int width, int height) {
+    if (!s || level < 0 || level >= kMaxLevels || !rgb || !depth || !grad_x || !grad_y) return FVGS_E_INVALID;
+    if (check_view(s, width, height) != FVGS_OK) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FrameLevel& f = s->lv[level];
+    const size_t px = (size_t)width * height;
+    FV_TRY(ensure_level(s, level, width, height));
     FV_CK(cudaMemcpyAsync(f.rgb, rgb, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.depth, depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.gx, grad_x, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
@@ -1384,6 +1458,54 @@ int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K
         if (depth) FV_CK(cudaMemcpyAsync(depth, s->img_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
         if (final_T) FV_CK(cudaMemcpyAsync(final_T, s->img_T, sizeof(float) * px, cudaMemcpyDefault, s->stream));
         if (n_contrib) FV_CK(cudaMemcpyAsync(n_contrib, s->img_nc, sizeof(uint32_t) * px, cudaMemcpyDefault, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_render_view(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                     float* rgb, float* depth, uint8_t* rgb8) {
+    if (!s || !valid_pose(pose) || !K) return FVGS_E_INVALID;
+    FV_TRY(check_view(s, width, height));
+    FV_CK(cudaSetDevice(s->device));
+    const size_t px = (size_t)width * height;
+    FV_TRY(ensure_images(s, px));
+    // the 8-bit copy lives in the contributor-count image (4 bytes per pixel)
+    uint8_t* rgb8_dev = rgb8 ? reinterpret_cast<uint8_t*>(s->img_nc) : nullptr;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, width, height));
+        RenderArgs ra{};
+        ra.rec0 = s->rec0;
+        ra.rec1 = s->rec1;
+        ra.rec2 = s->rec2;
+        ra.ranges = s->ranges;
+        ra.indices = s->vals;
+        ra.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+        ra.n_gauss = s->n_g;
+        ra.W = width;
+        ra.H = height;
+        ra.ntx = (width + s->params.tile_w - 1) / s->params.tile_w;
+        ra.nty = (height + s->params.tile_h - 1) / s->params.tile_h;
+        ra.quirks = s->params.quirks;
+        ra.out_rgb = s->img_color;
+        ra.out_depth = s->img_depth;
+        ra.out_rgb8 = rgb8_dev;
+        {
+            KScope k(s, FVGS_K_RENDER, 1);
+            FV_CK(launch_render_view(ra, s->stream));
+        }
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        if (rgb) FV_CK(cudaMemcpyAsync(rgb, s->img_color, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+        if (depth) FV_CK(cudaMemcpyAsync(depth, s->img_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+        if (rgb8) FV_CK(cudaMemcpyAsync(rgb8, rgb8_dev, 3 * px, cudaMemcpyDefault, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
         return FVGS_OK;
     }

@@ -213,6 +213,29 @@ cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* p
 cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                    double eig_eps, double* step_out, cudaStream_t s);
 
+// ---- render form (render.cu) ----
+struct RenderArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const float4* rec2;
+    const uint2* ranges;
+    const uint32_t* indices;
+    uint32_t n_list, n_gauss;  // as TrackArgs
+    int W, H, ntx, nty;
+    uint32_t quirks;
+    float* out_rgb;      // 3P
+    float* out_depth;    // P
+    uint8_t* out_rgb8;   // optional 3P
+};
+cudaError_t launch_render_view(const RenderArgs& a, cudaStream_t s);
+
+// ---- frame preprocessing (preprocess.cu) ----
+cudaError_t launch_pyrdown_u8(const uint8_t* src, int W, int H, int c, uint8_t* dst, cudaStream_t s);
+cudaError_t launch_pyrdown_f32(const float* src, int W, int H, float* dst, cudaStream_t s);
+cudaError_t launch_depth_in(const void* src, int u16_mm, size_t n, float* dst, cudaStream_t s);
+cudaError_t launch_color_sobel(const uint8_t* img, int W, int H, int double_scale, float* rgb, float* gx, float* gy,
+                               cudaStream_t s);
+
 // ---- mapping (map.cu) ----
 struct MapArgs {
     const float4* rec0;

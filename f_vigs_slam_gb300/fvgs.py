@@ -301,6 +301,40 @@ class Session:
         )
         return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
 
+    def render_view(self, pose, K, W, H, rgb8: bool = False):
+        """Render-form image (fvgs_render_view): float rgb (H,W,3), depth (H,W), optional 8-bit rgb."""
+        col = np.zeros((H, W, 3), np.float32)
+        dep = np.zeros((H, W), np.float32)
+        c8 = np.zeros((H, W, 3), np.uint8) if rgb8 else None
+        _check(self.lib.fvgs_render_view(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(W),
+                                         C.c_int(H), _ptr(col), _ptr(dep), _ptr(c8)), "fvgs_render_view")
+        return (col, dep, c8) if rgb8 else (col, dep)
+
+    def preprocess_frame(self, color_u8, depth, levels: int = 3, double_scale: bool = False):
+        """Camera frame -> pyramid levels on the device (fvgs_preprocess_frame); depth float32 metres or
+        uint16 millimetres."""
+        col = np.ascontiguousarray(color_u8, np.uint8)
+        H, W = col.shape[:2]
+        if depth.dtype == np.uint16:
+            dep, mm = np.ascontiguousarray(depth), 1
+        else:
+            dep, mm = np.ascontiguousarray(depth, np.float32), 0
+        _check(self.lib.fvgs_preprocess_frame(self.h, _ptr(col), _ptr(dep), C.c_int(mm), C.c_int(W), C.c_int(H),
+                                              C.c_int(levels), C.c_int(int(double_scale))), "fvgs_preprocess_frame")
+
+    def download_frame(self, level: int = 0):
+        w, h = C.c_int(), C.c_int()
+        _check(self.lib.fvgs_download_frame(self.h, C.c_int(level), None, None, None, None, C.byref(w), C.byref(h)),
+               "fvgs_download_frame")
+        W, H = w.value, h.value
+        rgb = np.zeros((H, W, 3), np.float32)
+        dep = np.zeros((H, W), np.float32)
+        gx = np.zeros((H, W, 3), np.float32)
+        gy = np.zeros((H, W, 3), np.float32)
+        _check(self.lib.fvgs_download_frame(self.h, C.c_int(level), _ptr(rgb), _ptr(dep), _ptr(gx), _ptr(gy),
+                                            None, None), "fvgs_download_frame")
+        return rgb, dep, gx, gy
+
     def render(self, pose, K, W, H):
         col = np.zeros((H, W, 3), np.float32)
         dep = np.zeros((H, W), np.float32)

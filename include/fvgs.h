@@ -180,6 +180,39 @@ int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_
 int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager);
 
 /*
+ * The viewer's image: binning + the render-form forward pass
+ * (GSSlam::rasterize / renderView, src/GSSlam.cu:648-799, kernel
+ * forwardPassTileKernel, src/GSCudaKernels.cu:710-859), with its own
+ * semantics: Sigma2D inverted in its true layout, every Gaussian of a tile
+ * list blended without the tracking kernels' 0.99 / 1/255 thresholds, stop at
+ * accumulated alpha >= 0.99, median depth at the 0.5 crossing (1e10 where
+ * none), no background.  rgb[3P] float (the reference writes it into an 8-bit
+ * image, overrunning it), depth[P]; rgb8[3P] (nullable) = round(255 c)
+ * saturated.  Outputs may be host or device pointers; any may be null.
+ */
+int fvgs_render_view(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                     float* rgb, float* depth, uint8_t* rgb8);
+
+/*
+ * Frame preprocessing on the device (GSSlam::initAndCopyImgs,
+ * src/GSSlam.cu:1913-1969, done on the host in the reference): from one camera
+ * frame -- colour 8-bit, 3 channels, dense (channel order kept as given);
+ * depth float metres, or uint16 millimetres when depth_u16_mm -- build pyramid
+ * levels 0..levels-1 by pyrDown (5-tap binomial, reflect-101 borders; 8-bit
+ * colour in integers, depth in float) and set each level's observed colour
+ * (c / 255, and / 255 once more when double_scale, as computeRgbdPoseJacobians
+ * scales it again, src/GSSlam.cu:2158), depth and 3x3 Sobel gradients of the
+ * c / 255 colour, as fvgs_set_frame would.  Inputs may be host or device
+ * pointers.
+ */
+int fvgs_preprocess_frame(fvgs_session* s, const uint8_t* color, const void* depth, int depth_u16_mm, int width,
+                          int height, int levels, int double_scale);
+/* A level's current frame (rgb[3P], depth[P], grad_x[3P], grad_y[3P], any
+ * nullable) and its size. */
+int fvgs_download_frame(fvgs_session* s, int level, float* rgb, float* depth, float* grad_x, float* grad_y,
+                        int* width, int* height);
+
+/*
  * Forward blend with the tracking kernel's semantics for every pixel of a
  * width x height view (observed depth treated as valid everywhere): colour
  * incl. background, median depth, final transmittance, contributor count.

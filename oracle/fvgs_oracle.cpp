@@ -1093,4 +1093,103 @@ int oracle_adam(double* pos, double* scl, double* rot, double* col, double* opa,
     return 0;
 }
 
+/*
+ * Render-form forward pass forwardPassTileKernel (src/GSCudaKernels.cu:710-859)
+ * in FP64, one pixel at a time over its tile's whole sorted list: the inverse
+ * of Sigma2D in its true (xx, xy, yy) layout (the kernel inverts Sigma2D
+ * itself, 817, with invert2x2, 1411-1437 -- the FP32 values the projection
+ * stores, inv2d (xx, yy, xy)), w = opacity * exp(-0.5 (ixx dx^2 + iyy dy^2 +
+ * 2 ixy dx dy)) with d = pixel - mean, colour += (1 - A) w c, A += (1 - A) w,
+ * no alpha clamp or 1/255 threshold, stop once A >= 0.99, median depth
+ * z + phat . d at the first 0.5 crossing of 1 - A (1e10 if none), no
+ * background.  color[3P], depth[P].
+ */
+int oracle_render_view(const float* uv, const float* inv2d, const float* depth, const float* phat,
+                       const float* colors, const float* opac, const uint32_t* ranges, const uint32_t* indices,
+                       int W, int H, int tw, int th, double* color, double* out_depth) {
+    const int ntx = (W + tw - 1) / tw;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int p = 0; p < W * H; ++p) {
+        const int x = p % W, y = p / W;
+        const int tile = (y / th) * ntx + (x / tw);
+        const uint32_t r0 = ranges[2 * (size_t)tile], r1 = ranges[2 * (size_t)tile + 1];
+        double c[3] = {0.0, 0.0, 0.0};
+        double A = 0.0, d = 1e10;
+        bool has_depth = false;
+        for (uint32_t k = r0; k < r1; ++k) {
+            const uint32_t g = indices[k];
+            const double dx = (double)x - uv[2 * (size_t)g], dy = (double)y - uv[2 * (size_t)g + 1];
+            const double ixx = inv2d[3 * (size_t)g], iyy = inv2d[3 * (size_t)g + 1], ixy = inv2d[3 * (size_t)g + 2];
+            const double w = (double)opac[g] * std::exp(-0.5 * (ixx * dx * dx + iyy * dy * dy + 2.0 * ixy * dx * dy));
+            const double Tb = 1.0 - A;
+            for (int ch = 0; ch < 3; ++ch) c[ch] += Tb * w * colors[3 * (size_t)g + ch];
+            A += Tb * w;
+            const double Ta = 1.0 - A;
+            if (!has_depth && Tb > 0.5 && Ta <= 0.5) {
+                d = (double)depth[g] + (double)phat[2 * (size_t)g] * dx + (double)phat[2 * (size_t)g + 1] * dy;
+                has_depth = true;
+            }
+            if (A >= 0.99) break;
+        }
+        for (int ch = 0; ch < 3; ++ch) color[3 * (size_t)p + ch] = c[ch];
+        out_depth[p] = d;
+    }
+    return 0;
+}
+
+/*
+ * Frame preprocessing of GSSlam::initAndCopyImgs (src/GSSlam.cu:1913-1969):
+ * one cv::pyrDown step (5-tap binomial [1 4 6 4 1]/16 in each direction,
+ * reflect-101 borders, output ((W+1)/2, (H+1)/2)).  8-bit images: integer
+ * sums, (sum + 128) >> 8; float images: the same weights in float, rows first
+ * then columns, times 1/256.  c channels, dense row-major.
+ */
+static inline int reflect101(int i, int n) {
+    if (n == 1) return 0;
+    while (i < 0 || i >= n) i = (i < 0) ? -i : 2 * n - 2 - i;
+    return i;
+}
+
+int oracle_pyrdown_u8(const uint8_t* src, int W, int H, int c, uint8_t* dst) {
+    const int W2 = (W + 1) / 2, H2 = (H + 1) / 2;
+    const int wts[5] = {1, 4, 6, 4, 1};
+    std::vector<int> row((size_t)H * W2 * c);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W2; ++x)
+            for (int ch = 0; ch < c; ++ch) {
+                int s = 0;
+                for (int k = -2; k <= 2; ++k) s += wts[k + 2] * src[((size_t)y * W + reflect101(2 * x + k, W)) * c + ch];
+                row[((size_t)y * W2 + x) * c + ch] = s;
+            }
+    for (int y = 0; y < H2; ++y)
+        for (int x = 0; x < W2; ++x)
+            for (int ch = 0; ch < c; ++ch) {
+                int s = 0;
+                for (int k = -2; k <= 2; ++k) s += wts[k + 2] * row[((size_t)reflect101(2 * y + k, H) * W2 + x) * c + ch];
+                dst[((size_t)y * W2 + x) * c + ch] = (uint8_t)((s + 128) >> 8);
+            }
+    return 0;
+}
+
+int oracle_pyrdown_f32(const float* src, int W, int H, int c, float* dst) {
+    const int W2 = (W + 1) / 2, H2 = (H + 1) / 2;
+    const float wts[5] = {1.f, 4.f, 6.f, 4.f, 1.f};
+    std::vector<float> row((size_t)H * W2 * c);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W2; ++x)
+            for (int ch = 0; ch < c; ++ch) {
+                float s = 0.f;
+                for (int k = -2; k <= 2; ++k) s += wts[k + 2] * src[((size_t)y * W + reflect101(2 * x + k, W)) * c + ch];
+                row[((size_t)y * W2 + x) * c + ch] = s;
+            }
+    for (int y = 0; y < H2; ++y)
+        for (int x = 0; x < W2; ++x)
+            for (int ch = 0; ch < c; ++ch) {
+                float s = 0.f;
+                for (int k = -2; k <= 2; ++k) s += wts[k + 2] * row[((size_t)reflect101(2 * y + k, H) * W2 + x) * c + ch];
+                dst[((size_t)y * W2 + x) * c + ch] = s * (1.0f / 256.0f);
+            }
+    return 0;
+}
+
 }  // extern "C"

@@ -237,6 +237,59 @@ def render(b: Binning, pose, K, W, H, params: Params):
     return r.color, r.depth, r.final_T, r.n_contrib
 
 
+def render_view(scene, b: Binning, W, H, params: Params):
+    """Render-form forward pass (forwardPassTileKernel, src/GSCudaKernels.cu:710-859)
+    in FP64: colour (H,W,3) without background, median depth (H,W), 1e10 where
+    the accumulated alpha never crosses 0.5."""
+    col = np.zeros((H, W, 3), np.float64)
+    dep = np.zeros((H, W), np.float64)
+    p = b.proj
+    lib().oracle_render_view(
+        _p(_f32(p.uv)), _p(_f32(p.inv2d)), _p(_f32(p.depth)), _p(_f32(p.phat)), _p(_f32(scene.colors)),
+        _p(_f32(scene.opacities)), _p(b.ranges), _p(b.vals), C.c_int(W), C.c_int(H), C.c_int(params.tile_w),
+        C.c_int(params.tile_h), _p(col), _p(dep))
+    return col, dep
+
+
+def pyrdown(img):
+    """One cv::pyrDown step (5-tap binomial, reflect-101 borders) of an (H, W)
+    or (H, W, C) uint8 or float32 image (src/GSSlam.cu:1942-1944)."""
+    a = np.ascontiguousarray(img)
+    H, W = a.shape[:2]
+    c = 1 if a.ndim == 2 else a.shape[2]
+    shape = ((H + 1) // 2, (W + 1) // 2) + (() if a.ndim == 2 else (c,))
+    if a.dtype == np.uint8:
+        out = np.zeros(shape, np.uint8)
+        lib().oracle_pyrdown_u8(_p(a), C.c_int(W), C.c_int(H), C.c_int(c), _p(out))
+    else:
+        a = a.astype(np.float32)
+        out = np.zeros(shape, np.float32)
+        lib().oracle_pyrdown_f32(_p(a), C.c_int(W), C.c_int(H), C.c_int(c), _p(out))
+    return out
+
+
+def preprocess(color_u8, depth, levels=3, depth_mm=False, double_scale=False):
+    """GSSlam::initAndCopyImgs (src/GSSlam.cu:1913-1969) for one frame: per
+    pyramid level the colour as float [0,1] (x 1/255 once more with
+    double_scale, the scaling computeRgbdPoseJacobians adds, 2158), the depth
+    in metres (uint16 millimetres x 0.001), and the 3x3 Sobel gradients of the
+    float colour.  Returns a list of (rgb, depth, gx, gy)."""
+    from f_vigs_slam_gb300 import synthetic as S
+
+    col = np.ascontiguousarray(color_u8, np.uint8)
+    dep = (depth.astype(np.float32) * np.float32(0.001)) if depth_mm else np.ascontiguousarray(depth, np.float32)
+    out = []
+    for lv in range(levels):
+        if lv > 0:
+            col = pyrdown(col)
+            dep = pyrdown(dep)
+        f = col.astype(np.float32) * np.float32(1.0 / 255.0)
+        gx, gy = S.sobel3(f)
+        rgb = f * np.float32(1.0 / 255.0) if double_scale else f
+        out.append((rgb, dep.copy(), gx, gy))
+    return out
+
+
 class MapResult:
     pass
 

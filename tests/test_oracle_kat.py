@@ -229,3 +229,47 @@ def test_adam_first_step(oracle):
     g = d3[0, 0:3]
     np.testing.assert_allclose(pos[0], 0.002 * g / np.sqrt(g * g + np.float64(np.float32(1e-8))), rtol=1e-6)
     assert np.all(pos[1] == 0) and adam[1, 26] == 0 and adam[0, 26] == 1
+
+
+def test_kat_pyrdown_impulse(oracle):
+    """cv::pyrDown of a 5x5 impulse at (2, 2): weights [1 4 6 4 1]/16 per
+    axis with reflect-101 borders give the centre 6/16 and each border
+    output 1/16 + 1/16 (the impulse is reached from both sides), so the 3x3
+    result is 255 * (2, 6, 2)^T (2, 6, 2) / 256, rounded: (4, 12, 4),
+    (12, 36, 12), (4, 12, 4)."""
+    import numpy as np
+
+    img = np.zeros((5, 5), np.uint8)
+    img[2, 2] = 255
+    out = oracle.pyrdown(img)
+    np.testing.assert_array_equal(out, np.array([[4, 12, 4], [12, 36, 12], [4, 12, 4]], np.uint8))
+    outf = oracle.pyrdown(img.astype(np.float32))
+    np.testing.assert_allclose(outf, np.outer([2, 6, 2], [2, 6, 2]) * 255.0 / 256.0, rtol=1e-6)
+
+
+def test_kat_render_view_single_gaussian(oracle):
+    """forwardPassTileKernel with one Gaussian of opacity 0.5 centred on pixel
+    (3, 2), inverse covariance diag(1, 1), colour (1, 0, 0), depth 2, zero
+    phat: that pixel gets colour 0.5 and, as 1 - A falls from 1 to 0.5
+    (crossing 0.5), depth 2; its neighbour (4, 2) gets 0.5 exp(-1/2) and no
+    crossing (depth 1e10)."""
+    import ctypes as C
+
+    import numpy as np
+
+    W, H = 8, 4
+    uv = np.array([[3.0, 2.0]], np.float32)
+    inv2d = np.array([[1.0, 1.0, 0.0]], np.float32)  # (xx, yy, xy)
+    depth = np.array([2.0], np.float32)
+    phat = np.zeros((1, 2), np.float32)
+    col = np.array([[1.0, 0.0, 0.0]], np.float32)
+    opa = np.array([0.5], np.float32)
+    ranges = np.array([0, 1], np.uint32)  # one 16x16 tile
+    vals = np.array([0], np.uint32)
+    out_c = np.zeros((H, W, 3), np.float64)
+    out_d = np.zeros((H, W), np.float64)
+    p = lambda a: C.c_void_p(a.ctypes.data)
+    oracle.lib().oracle_render_view(p(uv), p(inv2d), p(depth), p(phat), p(col), p(opa), p(ranges), p(vals),
+                                    C.c_int(W), C.c_int(H), C.c_int(16), C.c_int(16), p(out_c), p(out_d))
+    assert abs(out_c[2, 3, 0] - 0.5) < 1e-15 and out_d[2, 3] == 2.0
+    assert abs(out_c[2, 4, 0] - 0.5 * np.exp(-0.5)) < 1e-15 and out_d[2, 4] == 1e10
