@@ -432,9 +432,12 @@ def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session, s
             rgb, d = S.add_noise(col, dep, rng)
             gx, gy = S.sobel3(rgb)
             f = {"rgb": rgb, "depth": d, "gx": gx, "gy": gy}
+            raw_color = np.clip(np.rint(np.clip(rgb, 0.0, 1.0) * 255.0), 0, 255).astype(np.uint8)
             frames.append({"pose": traj[k + 1], "prev": traj[k],
                            "dev": {k2: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k2, v in f.items()},
-                           "host": {k2: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k2, v in f.items()}})
+                           "host": {k2: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k2, v in f.items()},
+                           "raw": {"color": torch.from_numpy(raw_color).pin_memory(),
+                                   "depth": torch.from_numpy(np.ascontiguousarray(d)).pin_memory()}})
         out.append({"sess": sess, "W": W, "H": H, "K": K, "n": int(ns[i]), "frames": frames})
     torch.cuda.synchronize()
     return out
@@ -492,8 +495,12 @@ def run_serving(args, fvgs, S, torch, dev):
             if arrivals is None:
                 for j, (i, r, f, eta) in enumerate(reqs_):
                     w = ws[i]
-                    sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
-                              frame=frame_ptrs(fvgs, f[frames_key], w["W"], w["H"]))
+                    if frames_key == "raw":
+                        sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
+                                  raw=(f["raw"]["color"].data_ptr(), f["raw"]["depth"].data_ptr(), w["W"], w["H"]))
+                    else:
+                        sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
+                                  frame=frame_ptrs(fvgs, f[frames_key], w["W"], w["H"]))
             else:
                 order = sorted(range(len(reqs_)), key=lambda j: arrivals[j])
                 for j in order:
@@ -524,6 +531,7 @@ def run_serving(args, fvgs, S, torch, dev):
     sat = served("dev", reqs)
     clk = clocks.stop()
     e2e = served("host", reqs)
+    e2e_raw = served("raw", reqs)
     # latency under Poisson arrivals: 30 Hz per session, or 70% of the measured
     # capacity if the GPU cannot sustain that rate
     hz = min(SERVE_HZ, 0.7 * sat["frames_per_s"] / len(ws))
@@ -549,6 +557,8 @@ def run_serving(args, fvgs, S, torch, dev):
         "served_frames_per_s": sat["frames_per_s"], "served_span_s": sat["span_s"],
         "plain_frames_per_s": len(reqs) / plain_s, "plain_span_s": plain_s,
         "e2e_frames_per_s": e2e["frames_per_s"],
+        "e2e_raw_frames_per_s": e2e_raw["frames_per_s"],
+        "h2d_raw_bytes_per_round": int(sum(7 * w["W"] * w["H"] for w in ws)),
         "h2d_bytes_per_round": int(sum(frame_bytes)), "d2h_bytes_per_round": 160 * len(ws),
         "launches": sat["launches"], "clocks": clk,
         "poisson": {"hz_per_session": hz, "spec_hz_per_session": SERVE_HZ, "seconds": SERVE_SECONDS,
@@ -644,7 +654,12 @@ def run_ours(args):
                           "identical; tests/test_serving_gpu.py), so pose error is equal by construction",
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": srv["h2d_bytes_per_round"],
                     "d2h_bytes_per_step": srv["d2h_bytes_per_round"],
-                    "path": "server requests carrying pinned host frames (fvgs_server_submit), copies inside"},
+                    "path": "server requests carrying pinned host frames (fvgs_server_submit), copies inside",
+                    "raw_camera_frames": {"value": srv["e2e_raw_frames_per_s"], "unit": "frames/s",
+                                          "h2d_bytes_per_step": srv["h2d_raw_bytes_per_round"],
+                                          "path": "requests carrying 8-bit colour + float depth camera frames, "
+                                                  "pyramid level, colour scaling and Sobel gradients built on the "
+                                                  "device (fvgs_preprocess_frame)"}},
             "gpu_launches": srv["launches"],
             "graphed_frames": srv["graphed_frames"],
             "roofline": large["roofline"],

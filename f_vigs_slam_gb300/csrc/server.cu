@@ -82,6 +82,9 @@ struct fvgs_server {
                     if (r.rgb)
                         rc = fvgs_set_frame(sl.session, r.level, r.rgb, r.depth, r.grad_x, r.grad_y, r.width,
                                             r.height);
+                    else if (r.raw_color)
+                        rc = fvgs_preprocess_frame(sl.session, r.raw_color, r.raw_depth, r.raw_depth_u16_mm, r.width,
+                                                   r.height, r.raw_levels > 0 ? r.raw_levels : 1, r.raw_double_scale);
                     if (rc == FVGS_OK)
                         rc = fvgs_frame_submit(sl.session, &r.pose, &r.K, r.level, r.iterations, r.map_eta);
                     sl.t_launch = now_s();

@@ -414,7 +414,8 @@ class ServerRequest(C.Structure):
     _fields_ = [("pose", Pose), ("K", Intrinsics), ("level", C.c_int), ("iterations", C.c_int),
                 ("map_eta", C.c_float), ("tag", C.c_uint64), ("t_arrival", C.c_double),
                 ("rgb", C.c_void_p), ("depth", C.c_void_p), ("grad_x", C.c_void_p), ("grad_y", C.c_void_p),
-                ("width", C.c_int), ("height", C.c_int)]
+                ("width", C.c_int), ("height", C.c_int), ("raw_color", C.c_void_p), ("raw_depth", C.c_void_p),
+                ("raw_depth_u16_mm", C.c_int), ("raw_levels", C.c_int), ("raw_double_scale", C.c_int)]
 
 
 class ServerResult(C.Structure):
@@ -458,9 +459,10 @@ class Server:
         return float(t.value)
 
     def submit(self, slot: int, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None,
-               tag: int = 0, t_arrival: float = 0.0, frame=None):
+               tag: int = 0, t_arrival: float = 0.0, frame=None, raw=None):
         """frame: optional (rgb_ptr, depth_ptr, gx_ptr, gy_ptr, W, H) of memory that stays valid (pinned
-        host or device) until the result is back."""
+        host or device) until the result is back; raw: optional (color_u8_ptr, depth_ptr, W, H[, depth_u16])
+        camera frame, preprocessed on the device (level 0)."""
         r = ServerRequest()
         r.pose = make_pose(pose)
         r.K = make_intr(K)
@@ -469,6 +471,10 @@ class Server:
         r.tag, r.t_arrival = tag, t_arrival
         if frame is not None:
             r.rgb, r.depth, r.grad_x, r.grad_y, r.width, r.height = frame
+        if raw is not None:
+            r.raw_color, r.raw_depth, r.width, r.height = raw[:4]
+            r.raw_depth_u16_mm = int(raw[4]) if len(raw) > 4 else 0
+            r.raw_levels = 1
         _check(self.lib.fvgs_server_submit(self.h, C.c_int(slot), C.byref(r)), "fvgs_server_submit")
 
     def results(self, wait_for: int = 0, max_results: int = 4096):

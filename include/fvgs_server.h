@@ -39,6 +39,15 @@ typedef struct fvgs_server_request {
     const float* grad_x;
     const float* grad_y;
     int width, height;
+    /* Optional raw camera frame instead (as fvgs_preprocess_frame: 8-bit
+     * colour, float metres or uint16 millimetre depth): the pyramid levels
+     * 0..raw_levels-1 are built on the device right before the frame.  Used
+     * when raw_color != NULL and rgb == NULL. */
+    const uint8_t* raw_color;
+    const void* raw_depth;
+    int raw_depth_u16_mm;
+    int raw_levels;
+    int raw_double_scale;
 } fvgs_server_request;
 
 typedef struct fvgs_server_result {

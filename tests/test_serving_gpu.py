@@ -174,3 +174,30 @@ def test_server_admission_by_footprint(fvgs_lib):
     finally:
         a.close()
         b.close()
+
+
+def test_server_raw_camera_frames(oracle, fvgs_lib):
+    """A request carrying a raw camera frame (8-bit colour, uint16 mm depth)
+    is preprocessed on the device and tracked; the pose equals that of the
+    same session preprocessing the frame itself and tracking alone."""
+    fv = fvgs_lib
+    case = _scene_frame(oracle, 8, 20_000, 0.5)
+    rgb, d, _, _ = case["frame"]
+    color = np.clip(np.rint(np.clip(rgb, 0, 1) * 255), 0, 255).astype(np.uint8)
+    depth_mm = np.clip(np.rint(d * 1000.0), 0, 65535).astype(np.uint16)
+    W, H, K = case["W"], case["H"], case["K"]
+    with _session(fv, case) as s:
+        s.preprocess_frame(color, depth_mm, levels=1)
+        s.frame_submit(case["starts"][0], K, iterations=ITERS)
+        alone = s.frame_wait()[0]
+    torch = pytest.importorskip("torch")
+    c_pin = torch.from_numpy(color).pin_memory()
+    d_pin = torch.from_numpy(depth_mm).pin_memory()
+    with _session(fv, case) as s, fv.Server(memory_budget_bytes=1 << 40, max_inflight=2) as sv:
+        slot = sv.admit(s)
+        sv.submit(slot, case["starts"][0], K, iterations=ITERS, tag=1,
+                  raw=(c_pin.data_ptr(), d_pin.data_ptr(), W, H, True))
+        res = sv.results(wait_for=1)
+        sv.release(slot)
+    assert len(res) == 1 and res[0]["status"] == 0
+    _same(res[0]["pose"], alone)
