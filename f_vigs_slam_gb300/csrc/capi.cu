@@ -169,6 +169,20 @@ struct fvgs_session {
     size_t m_sampled_slots = 0;
     int m_W = 0, m_H = 0;
 
+    // map maintenance: second set of Gaussian planes (compaction target,
+    // swapped in afterwards), its optimiser-state twin (allocated when the
+    // moments move with their Gaussians), marks, scores and visibility masks
+    float4 *pos_alt = nullptr, *scale_alt = nullptr, *rot_alt = nullptr, *col_alt = nullptr;
+    float4* adam_alt = nullptr;
+    uint8_t* mk_states = nullptr;
+    uint8_t *vis_a = nullptr, *vis_b = nullptr;
+    float *mk_total_alpha = nullptr, *mk_outlier_prob = nullptr;
+    uint32_t *mk_block_keep = nullptr, *mk_block_base = nullptr;
+    uint32_t* mk_ctr = nullptr;    // [0] survivors, [1] removed, [2] intersection, [3] union
+    uint32_t* h_mk_ctr = nullptr;  // pinned mirror
+    uint32_t mk_n = 0;             // Gaussians covered by the last marking
+    bool mk_scores = false;        // the last marking was an outlier pass (scores valid)
+
     // kernel accounting: launches per class (always), event timing (opt-in)
     uint32_t timing_mask = 0;
     uint64_t launches[FVGS_K_COUNT] = {};
@@ -728,6 +742,7 @@ int fvgs_session_destroy(fvgs_session* s) {
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_pose) cudaFreeHost(s->h_pose);
     if (s->h_devpose) cudaFreeHost(s->h_devpose);
+    if (s->h_mk_ctr) cudaFreeHost(s->h_mk_ctr);
     for (auto& g : s->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (s->frame_done) cudaEventDestroy(s->frame_done);
@@ -808,11 +823,24 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->m_max_contrib, (size_t)s->cap_tiles);
     FV_A(s->m_bucket_base, (size_t)s->cap_tiles);
     FV_A(s->m_bucket_total, 1);
+    FV_A(s->pos_alt, N);
+    FV_A(s->scale_alt, N);
+    FV_A(s->rot_alt, N);
+    FV_A(s->col_alt, N);
+    FV_A(s->mk_states, N);
+    FV_A(s->vis_a, N);
+    FV_A(s->vis_b, N);
+    FV_A(s->mk_total_alpha, N);
+    FV_A(s->mk_outlier_prob, N);
+    FV_A(s->mk_block_keep, N / kCompactBlock + 1);
+    FV_A(s->mk_block_base, N / kCompactBlock + 1);
+    FV_A(s->mk_ctr, 4);
 #undef FV_A
     if (cudaMallocHost(&s->h_jj, sizeof(double) * 48) != cudaSuccess ||
         cudaMallocHost(&s->h_st, sizeof(DevStatus)) != cudaSuccess ||
         cudaMallocHost(&s->h_pose, sizeof(fvgs_pose)) != cudaSuccess ||
-        cudaMallocHost(&s->h_devpose, sizeof(DevPose)) != cudaSuccess)
+        cudaMallocHost(&s->h_devpose, sizeof(DevPose)) != cudaSuccess ||
+        cudaMallocHost(&s->h_mk_ctr, sizeof(uint32_t) * 4) != cudaSuccess)
         return fail(FVGS_E_NOMEM);
     if (cudaEventCreateWithFlags(&s->frame_done, cudaEventDisableTiming) != cudaSuccess) return fail(FVGS_E_CUDA);
     if (sort_init(&s->sort, device) != cudaSuccess) return fail(FVGS_E_CUDA);
@@ -1581,6 +1609,264 @@ int fvgs_download_map_state(fvgs_session* s, float* final_T, uint32_t* n_contrib
     if (depth) FV_CK(cudaMemcpyAsync(depth, s->m_depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
     if (delta2d) FV_CK(cudaMemcpyAsync(delta2d, s->delta2d, sizeof(float) * 16 * n, cudaMemcpyDefault, s->stream));
     if (delta3d) FV_CK(cudaMemcpyAsync(delta3d, s->dbg_delta3d, sizeof(float) * 16 * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Map maintenance (GSSlam::removeOutliers, prune, computeCovisibilityRatio,
+// src/GSSlam.cu:1467-1904).
+namespace {
+
+// Bin one view and flag the Gaussians that some pixel of it sees.  vis must be
+// cleared first; returns the view's instance count in *n_inst.
+int visibility_pass(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int W, int H, uint8_t* vis,
+                    uint32_t* n_inst) {
+    FV_TRY(check_view(s, W, H));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, W, H));
+        FV_CK(cudaMemsetAsync(vis, 0, s->n_g, s->stream));
+        VisArgs va{};
+        va.rec0 = s->rec0;
+        va.rec1 = s->rec1;
+        va.ranges = s->ranges;
+        va.indices = s->vals;
+        va.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+        va.n_gauss = s->n_g;
+        va.W = W;
+        va.H = H;
+        va.ntx = (W + s->params.tile_w - 1) / s->params.tile_w;
+        va.nty = (H + s->params.tile_h - 1) / s->params.tile_h;
+        va.cap = (s->params.quirks & FVGS_Q_VIS_CAP256) ? 256 : 0;
+        va.vis = vis;
+        {
+            KScope k(s, FVGS_K_MAINT, 1);
+            FV_CK(launch_visibility(va, s->stream));
+        }
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        *n_inst = s->h_st->n_instances;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+// Enqueue marking (prune criteria or outlier scores), the survivor scan and,
+// when remove is set, the scatter into the second set of planes.
+int enqueue_mark_compact(fvgs_session* s, MarkMode mode, const MarkArgs& proto, bool remove) {
+    const uint32_t n = s->n_g;
+    MarkArgs ma = proto;
+    ma.n = n;
+    ma.states = s->mk_states;
+    ma.block_keep = s->mk_block_keep;
+    KScope k(s, FVGS_K_MAINT, remove ? 3 : 2);
+    FV_CK(launch_mark(mode, ma, s->stream));
+    FV_CK(launch_compact_scan(s->mk_block_keep, n, s->mk_block_base, s->mk_ctr, s->stream));
+    if (remove) {
+        const bool move_adam = !(s->params.quirks & FVGS_Q_ADAM_STAY);
+        if (move_adam && !s->adam_alt) FV_TRY(dev_alloc(s, &s->adam_alt, 9 * (size_t)s->cap_g));
+        CompactArgs ca{};
+        ca.n = n;
+        ca.states = s->mk_states;
+        ca.block_base = s->mk_block_base;
+        ca.counters = s->mk_ctr;
+        ca.pos = s->pos;
+        ca.scale = s->scale;
+        ca.rot = s->rot;
+        ca.col = s->col;
+        ca.pos_out = s->pos_alt;
+        ca.scale_out = s->scale_alt;
+        ca.rot_out = s->rot_alt;
+        ca.col_out = s->col_alt;
+        ca.adam = move_adam ? s->adam : nullptr;
+        ca.adam_out = move_adam ? s->adam_alt : nullptr;
+        ca.cap = s->cap_g;
+        FV_CK(launch_compact_scatter(ca, s->stream));
+    }
+    FV_CK(cudaMemcpyAsync(s->h_mk_ctr, s->mk_ctr, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, s->stream));
+    s->mk_n = n;
+    return FVGS_OK;
+}
+
+// After the stream is synchronised: adopt the compacted planes.
+void finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
+    const uint32_t removed = s->h_mk_ctr[1];
+    if (n_marked) *n_marked = removed;
+    if (!remove || removed == 0) return;
+    std::swap(s->pos, s->pos_alt);
+    std::swap(s->scale, s->scale_alt);
+    std::swap(s->rot, s->rot_alt);
+    std::swap(s->col, s->col_alt);
+    if (!(s->params.quirks & FVGS_Q_ADAM_STAY)) std::swap(s->adam, s->adam_alt);
+    s->n_g = s->h_mk_ctr[0];
+    // every per-Gaussian index of the last binning is stale now
+    s->has_binning = s->has_track = s->has_map = false;
+    s->hist_ok = false;
+    s->keys_valid = false;
+    s->dbg_proj_valid = false;
+    ++s->gen;  // captured frame graphs hold the old plane addresses
+}
+
+}  // namespace
+
+int fvgs_visibility(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                    uint8_t* visibility, uint32_t* n_visible) {
+    if (!s || !valid_pose(pose) || !K) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (s->n_g == 0) {
+        if (n_visible) *n_visible = 0;
+        return FVGS_OK;
+    }
+    uint32_t n_inst = 0;
+    FV_TRY(visibility_pass(s, pose, K, width, height, s->vis_a, &n_inst));
+    FV_CK(cudaMemsetAsync(s->mk_ctr + 2, 0, sizeof(uint32_t) * 2, s->stream));
+    {
+        KScope k(s, FVGS_K_MAINT, 1);
+        FV_CK(launch_covis_count(s->vis_a, s->vis_a, s->n_g, s->mk_ctr + 2, s->stream));
+    }
+    FV_CK(cudaMemcpyAsync(s->h_mk_ctr + 2, s->mk_ctr + 2, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, s->stream));
+    if (visibility) FV_CK(cudaMemcpyAsync(visibility, s->vis_a, s->n_g, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    if (n_visible) *n_visible = s->h_mk_ctr[3];
+    return FVGS_OK;
+}
+
+int fvgs_covisibility(fvgs_session* s, const fvgs_pose* pose_a, const fvgs_intrinsics* K_a, int width_a,
+                      int height_a, const fvgs_pose* pose_b, const fvgs_intrinsics* K_b, int width_b, int height_b,
+                      uint32_t* n_inter, uint32_t* n_union, float* ratio) {
+    if (!s || !valid_pose(pose_a) || !K_a || !valid_pose(pose_b) || !K_b) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (n_inter) *n_inter = 0;
+    if (n_union) *n_union = 0;
+    if (s->n_g == 0) {  // the reference returns 1 for an empty map
+        if (ratio) *ratio = 1.0f;
+        return FVGS_OK;
+    }
+    if (ratio) *ratio = 0.0f;
+    uint32_t n_inst = 0;
+    FV_TRY(visibility_pass(s, pose_a, K_a, width_a, height_a, s->vis_a, &n_inst));
+    if (n_inst == 0) return FVGS_OK;  // no instances in a view: ratio 0, as the reference
+    FV_TRY(visibility_pass(s, pose_b, K_b, width_b, height_b, s->vis_b, &n_inst));
+    if (n_inst == 0) return FVGS_OK;
+    FV_CK(cudaMemsetAsync(s->mk_ctr + 2, 0, sizeof(uint32_t) * 2, s->stream));
+    {
+        KScope k(s, FVGS_K_MAINT, 1);
+        FV_CK(launch_covis_count(s->vis_a, s->vis_b, s->n_g, s->mk_ctr + 2, s->stream));
+    }
+    FV_CK(cudaMemcpyAsync(s->h_mk_ctr + 2, s->mk_ctr + 2, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    const uint32_t inter = s->h_mk_ctr[2], uni = s->h_mk_ctr[3];
+    if (n_inter) *n_inter = inter;
+    if (n_union) *n_union = uni;
+    if (ratio) *ratio = uni == 0 ? 0.0f : (float)inter / (float)uni;
+    return FVGS_OK;
+}
+
+int fvgs_remove_outliers(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level,
+                         float threshold, int remove, uint32_t* n_marked) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels) return FVGS_E_INVALID;
+    const FrameLevel& f = s->lv[level];
+    if (!f.depth || f.W <= 0 || f.H <= 0) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    if (n_marked) *n_marked = 0;
+    s->mk_n = 0;
+    if (s->n_g == 0) return FVGS_OK;
+    FV_TRY(check_view(s, f.W, f.H));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_CK(cudaMemsetAsync(s->mk_total_alpha, 0, sizeof(float) * s->n_g, s->stream));
+        FV_CK(cudaMemsetAsync(s->mk_outlier_prob, 0, sizeof(float) * s->n_g, s->stream));
+        OutlierArgs oa{};
+        oa.rec0 = s->rec0;
+        oa.rec1 = s->rec1;
+        oa.rec2 = s->rec2;
+        oa.ranges = s->ranges;
+        oa.indices = s->vals;
+        oa.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+        oa.n_gauss = s->n_g;
+        oa.obs_depth = f.depth;
+        oa.W = f.W;
+        oa.H = f.H;
+        oa.ntx = (f.W + s->params.tile_w - 1) / s->params.tile_w;
+        oa.nty = (f.H + s->params.tile_h - 1) / s->params.tile_h;
+        oa.total_alpha = s->mk_total_alpha;
+        oa.outlier_prob = s->mk_outlier_prob;
+        {
+            KScope k(s, FVGS_K_MAINT, 1);
+            FV_CK(launch_outliers(oa, s->stream));
+        }
+        MarkArgs ma{};
+        ma.total_alpha = s->mk_total_alpha;
+        ma.outlier_prob = s->mk_outlier_prob;
+        ma.threshold = threshold;
+        FV_TRY(enqueue_mark_compact(s, kMarkOutliers, ma, remove != 0));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;  // the planes were only read: repeat from the start
+        s->mk_scores = true;
+        finish_compact(s, remove != 0, n_marked);
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int fvgs_prune(fvgs_session* s, float alpha_threshold, float scale_ratio_threshold, float min_scale, int remove,
+               uint32_t* n_marked) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (n_marked) *n_marked = 0;
+    s->mk_n = 0;
+    if (s->n_g == 0) return FVGS_OK;
+    MarkArgs ma{};
+    ma.scale = s->scale;
+    ma.col = s->col;
+    ma.alpha_thr = alpha_threshold;
+    ma.ratio_thr = scale_ratio_threshold;
+    ma.min_scale = min_scale;
+    FV_TRY(enqueue_mark_compact(s, kMarkPrune, ma, remove != 0));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    s->mk_scores = false;
+    finish_compact(s, remove != 0, n_marked);
+    return FVGS_OK;
+}
+
+int fvgs_download_marks(fvgs_session* s, uint8_t* states, float* total_alpha, float* outlier_prob, uint32_t n) {
+    if (!s || n > s->mk_n) return FVGS_E_INVALID;
+    if ((total_alpha || outlier_prob) && !s->mk_scores) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    if (n == 0) return FVGS_OK;
+    if (states) FV_CK(cudaMemcpyAsync(states, s->mk_states, n, cudaMemcpyDefault, s->stream));
+    if (total_alpha)
+        FV_CK(cudaMemcpyAsync(total_alpha, s->mk_total_alpha, sizeof(float) * n, cudaMemcpyDefault, s->stream));
+    if (outlier_prob)
+        FV_CK(cudaMemcpyAsync(outlier_prob, s->mk_outlier_prob, sizeof(float) * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_download_adam_state(fvgs_session* s, float* state, uint32_t n) {
+    if (!s || n > s->n_g || (n && !state)) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (n == 0) return FVGS_OK;
+    // nine planes of n float4, plane p at state + 4 n p
+    for (int p = 0; p < 9; ++p)
+        FV_CK(cudaMemcpyAsync(state + (size_t)4 * n * p, s->adam + (size_t)p * s->cap_g, sizeof(float4) * n,
+                              cudaMemcpyDefault, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
     return FVGS_OK;
 }

@@ -280,4 +280,59 @@ cudaError_t launch_bucket_scan(const uint2* ranges, int T, uint32_t* bucket_base
 cudaError_t launch_map_update(const MapUpdateArgs& a, const DevStatus* st, cudaStream_t s);
 int map_cap_buckets();
 
+// ---- map maintenance (maintenance.cu) ----
+struct VisArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const uint2* ranges;
+    const uint32_t* indices;
+    uint32_t n_list, n_gauss;  // as TrackArgs
+    int W, H, ntx, nty;
+    int cap;       // Gaussians considered per tile (0: all)
+    uint8_t* vis;  // [n_gauss], set to 1 where visible (cleared by the caller)
+};
+struct OutlierArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const float4* rec2;
+    const uint2* ranges;
+    const uint32_t* indices;
+    uint32_t n_list, n_gauss;
+    const float* obs_depth;  // P
+    int W, H, ntx, nty;
+    float* total_alpha;   // [n_gauss], zeroed by the caller
+    float* outlier_prob;  // [n_gauss], zeroed by the caller
+};
+enum MarkMode { kMarkPrune = 0, kMarkOutliers = 1 };
+struct MarkArgs {
+    uint32_t n;
+    const float4* scale;  // prune: scales and (col.w) opacities
+    const float4* col;
+    float alpha_thr, ratio_thr, min_scale;
+    const float* total_alpha;  // outliers: accumulators and threshold
+    const float* outlier_prob;
+    float threshold;
+    uint8_t* states;      // [n]: 0 keep, 0xff remove
+    uint32_t* block_keep;  // [ceil(n / kCompactBlock)]
+};
+constexpr int kCompactBlock = 256;
+struct CompactArgs {
+    uint32_t n;
+    const uint8_t* states;
+    const uint32_t* block_base;  // exclusive survivors before each block
+    const uint32_t* counters;    // [0] survivors, [1] removed
+    const float4 *pos, *scale, *rot, *col;
+    float4 *pos_out, *scale_out, *rot_out, *col_out;
+    const float4* adam;  // 9 planes of cap (null: the optimiser state stays in place)
+    float4* adam_out;
+    uint32_t cap;
+};
+cudaError_t launch_visibility(const VisArgs& a, cudaStream_t s);
+cudaError_t launch_outliers(const OutlierArgs& a, cudaStream_t s);
+cudaError_t launch_mark(MarkMode mode, const MarkArgs& a, cudaStream_t s);
+cudaError_t launch_compact_scan(const uint32_t* block_keep, uint32_t n, uint32_t* block_base, uint32_t* counters,
+                                cudaStream_t s);
+cudaError_t launch_compact_scatter(const CompactArgs& a, cudaStream_t s);
+cudaError_t launch_covis_count(const uint8_t* va, const uint8_t* vb, uint32_t n, uint32_t* counters, cudaStream_t s);
+
 }  // namespace fvgs

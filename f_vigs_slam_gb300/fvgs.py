@@ -1,9 +1,8 @@
 """Python binding of the fvgs C-ABI (include/fvgs.h) via ctypes.
 
-This is the host-side mirror used by tests and the benchmark; the C++
-compatibility layer (GSSlam / RgbdPoseCostFunction shapes) sits on the same
-C-ABI.  There is no CPU fallback: if libfvgs.so is missing or has no GPU to
-run on, calls raise.
+This is the host-side mirror of the reference's GSSlam device calls used by
+tests and the benchmark.  There is no CPU fallback: if libfvgs.so is missing
+or has no GPU to run on, calls raise.
 """
 from __future__ import annotations
 
@@ -25,7 +24,9 @@ Q_CULLED_SLOTS = 0x1
 Q_RANGE_LAUNCH = 0x2
 Q_INVSIGMA_SWAP = 0x4
 Q_MAP_CAP256 = 0x8
-QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
+Q_VIS_CAP256 = 0x10
+Q_ADAM_STAY = 0x20
+QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY
 
 DEBUG_PROJECTION = 0x1
 DEBUG_IMAGES = 0x2
@@ -33,7 +34,7 @@ DEBUG_MAPPING = 0x4
 DEBUG_RADIX_SORT = 0x8
 
 KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
-                  "map_update", "render"]
+                  "map_update", "render", "maint"]
 K = {name: i for i, name in enumerate(KERNEL_CLASSES)}
 
 
@@ -372,6 +373,60 @@ class Session:
         d2f[:, 12] = n2
         return dict(final_T=fT, n_contrib=nc, color=col, depth=dep, delta2d=d2f,
                     delta3d=None if d3 is None else d3[:, :14].astype(np.float64))
+
+    def download_adam_state(self):
+        """Optimiser state (fvgs_download_adam_state): (9, n, 4) float32 planes."""
+        n = self.n
+        st = np.zeros((9, n, 4), np.float32)
+        _check(self.lib.fvgs_download_adam_state(self.h, _ptr(st), C.c_uint32(n)), "fvgs_download_adam_state")
+        return st
+
+    # ---- map maintenance
+    def remove_outliers(self, pose, K, level: int = 0, threshold: float = 0.6, remove: bool = True) -> int:
+        """GSSlam::removeOutliers (fvgs_remove_outliers): number of Gaussians marked (removed when remove)."""
+        m = C.c_uint32()
+        _check(self.lib.fvgs_remove_outliers(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
+                                             C.c_float(threshold), C.c_int(int(remove)), C.byref(m)),
+               "fvgs_remove_outliers")
+        if remove:
+            self.n -= int(m.value)
+        return int(m.value)
+
+    def prune(self, alpha_threshold: float = 0.05, scale_ratio_threshold: float = 0.05, min_scale: float = 0.005,
+              remove: bool = True) -> int:
+        """GSSlam::prune (fvgs_prune): number of Gaussians marked (removed when remove)."""
+        m = C.c_uint32()
+        _check(self.lib.fvgs_prune(self.h, C.c_float(alpha_threshold), C.c_float(scale_ratio_threshold),
+                                   C.c_float(min_scale), C.c_int(int(remove)), C.byref(m)), "fvgs_prune")
+        if remove:
+            self.n -= int(m.value)
+        return int(m.value)
+
+    def download_marks(self, n: int, scores: bool = False):
+        """States of the last marking (and outlier scores): states or (states, total_alpha, outlier_prob)."""
+        st = np.zeros(n, np.uint8)
+        ta = np.zeros(n, np.float32) if scores else None
+        op = np.zeros(n, np.float32) if scores else None
+        _check(self.lib.fvgs_download_marks(self.h, _ptr(st), _ptr(ta), _ptr(op), C.c_uint32(n)),
+               "fvgs_download_marks")
+        return (st, ta, op) if scores else st
+
+    def visibility(self, pose, K, W, H):
+        """computeGaussiansVisibility_kernel (fvgs_visibility): (uint8 mask per Gaussian, count)."""
+        vis = np.zeros(self.n, np.uint8)
+        c = C.c_uint32()
+        _check(self.lib.fvgs_visibility(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(W),
+                                        C.c_int(H), _ptr(vis), C.byref(c)), "fvgs_visibility")
+        return vis, int(c.value)
+
+    def covisibility(self, pose_a, K_a, W_a, H_a, pose_b, K_b, W_b, H_b):
+        """GSSlam::computeCovisibilityRatio (fvgs_covisibility): (inter, union, ratio)."""
+        i, u, r = C.c_uint32(), C.c_uint32(), C.c_float()
+        _check(self.lib.fvgs_covisibility(self.h, C.byref(make_pose(pose_a)), C.byref(make_intr(K_a)), C.c_int(W_a),
+                                          C.c_int(H_a), C.byref(make_pose(pose_b)), C.byref(make_intr(K_b)),
+                                          C.c_int(W_b), C.c_int(H_b), C.byref(i), C.byref(u), C.byref(r)),
+               "fvgs_covisibility")
+        return int(i.value), int(u.value), float(r.value)
 
     # ---- asynchronous frames (CUDA-graph replay once the binning history is valid)
     def frame_submit(self, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None):

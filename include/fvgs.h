@@ -47,6 +47,7 @@ enum {
     FVGS_K_MAP_BWD,     /* mapping per-Gaussian backward */
     FVGS_K_MAP_UPDATE,  /* 2D->3D chain rule + Adam */
     FVGS_K_RENDER,      /* forward-only render */
+    FVGS_K_MAINT,       /* map maintenance: visibility, outlier scores, marking, compaction */
     FVGS_K_COUNT
 };
 
@@ -238,6 +239,63 @@ int fvgs_map_step(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics*
  * float; needs FVGS_DEBUG_MAPPING).  Any pointer may be null. */
 int fvgs_download_map_state(fvgs_session* s, float* final_T, uint32_t* n_contrib, float* color, float* depth,
                             float* delta2d, float* delta3d);
+/* Optimiser state of the first n Gaussians: nine planes of n float4 (plane p
+ * at state + 4 n p): m and v of position, scale, orientation, colour, then
+ * (m_alpha, v_alpha, step count, unused). */
+int fvgs_download_adam_state(fvgs_session* s, float* state, uint32_t n);
+
+/*
+ * Map maintenance.  Removal keeps the survivors in their order at the front
+ * and shrinks the session's Gaussian count, as the reference's
+ * thrust::sort_by_key on the 0 / 0xff states followed by
+ * n_Gaussians -= nb_removed (src/GSSlam.cu:1536-1569, 1668-1701); with
+ * FVGS_Q_ADAM_STAY the optimiser state stays at its index.  Removing
+ * Gaussians renumbers them, so the next binning is a full one.
+ *
+ * fvgs_remove_outliers: GSSlam::removeOutliers (src/GSSlam.cu:1581-1711) --
+ * bin the view of `level` at `pose`, accumulate per Gaussian the alpha of
+ * every (pixel, Gaussian) pair of its tiles with alpha >= 1/255 and rendered
+ * depth > 0 (total_alpha) and the part of it where the observed depth is
+ * > 0.1 and the rendered depth < 0.8 x observed (outlier_prob), and mark the
+ * Gaussians with total_alpha > 1 and outlier_prob / total_alpha > threshold
+ * (0.6 in the reference); computeOutliers_kernel / removeOutliers_kernel,
+ * src/GSCudaKernels.cu:1620-1739.  remove = 0 only marks (fvgs_download_marks
+ * reads the states and scores); *n_marked = number marked (= removed).
+ */
+int fvgs_remove_outliers(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level,
+                         float threshold, int remove, uint32_t* n_marked);
+/*
+ * GSSlam::prune (src/GSSlam.cu:1467-1579), pruneGaussians_kernel
+ * (src/GSCudaKernels.cu:1566-1618): mark Gaussians with opacity <
+ * alpha_threshold, or whose middle scale / largest scale < scale_ratio_threshold
+ * or largest scale < min_scale (0.05, 0.05, 0.005 in the reference).
+ */
+int fvgs_prune(fvgs_session* s, float alpha_threshold, float scale_ratio_threshold, float min_scale, int remove,
+               uint32_t* n_marked);
+/* States (0 keep, 0xff remove) of the last marking, and the outlier scores of
+ * the last fvgs_remove_outliers, for its first n Gaussians (numbered as
+ * before any removal).  Any pointer may be null. */
+int fvgs_download_marks(fvgs_session* s, uint8_t* states, float* total_alpha, float* outlier_prob, uint32_t n);
+/*
+ * computeGaussiansVisibility_kernel (src/GSCudaKernels.cu:1455-1537) on the
+ * view (pose, K, width x height): visibility[i] = 1 where some pixel blends
+ * Gaussian i with alpha = min(0.99, opacity exp(-q/2)) >= 1/255 before its
+ * transmittance falls below 0.5 (the first 256 Gaussians of each tile with
+ * FVGS_Q_VIS_CAP256).  visibility (n bytes, host or device) may be null;
+ * *n_visible = number of visible Gaussians.
+ */
+int fvgs_visibility(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int width, int height,
+                    uint8_t* visibility, uint32_t* n_visible);
+/*
+ * GSSlam::computeCovisibilityRatio (src/GSSlam.cu:1713-1904): visibility of
+ * view a (the keyframe) and view b (the current frame), then
+ * ratio = |a and b| / |a or b| (computeGaussiansCovisibility_kernel,
+ * src/GSCudaKernels.cu:1539-1560); 1 for an empty map, 0 when a view has no
+ * instances or the union is empty.
+ */
+int fvgs_covisibility(fvgs_session* s, const fvgs_pose* pose_a, const fvgs_intrinsics* K_a, int width_a,
+                      int height_a, const fvgs_pose* pose_b, const fvgs_intrinsics* K_b, int width_b, int height_b,
+                      uint32_t* n_inter, uint32_t* n_union, float* ratio);
 
 /*
  * Allocation-free pose Jacobian for callers that cannot call cudaMalloc -- a

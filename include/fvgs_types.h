@@ -57,14 +57,24 @@ typedef enum fvgs_status {
  *                Clear: the true quadratic form.
  *  MAP_CAP256    optimizeGaussiansPerGaussianPass only gives gradients to the
  *                first 256 Gaussians of each tile (src/GSCudaKernels.cu:2329).
+ *  VIS_CAP256    computeGaussiansVisibility_kernel only considers the first
+ *                256 Gaussians of each tile (src/GSCudaKernels.cu:1476).
+ *  ADAM_STAY     removeOutliers / prune reorder the five parameter arrays but
+ *                not adam_states_ (src/GSSlam.cu:1536-1548,1668-1680), so a
+ *                surviving Gaussian that moves down inherits the optimiser
+ *                moments of the one that held its new index.  Clear: the
+ *                moments move with their Gaussian.
  */
 #define FVGS_Q_CULLED_SLOTS  0x1u
 #define FVGS_Q_RANGE_LAUNCH  0x2u
 #define FVGS_Q_INVSIGMA_SWAP 0x4u
 #define FVGS_Q_MAP_CAP256    0x8u
-/* Default: the reference's arithmetic (swap, cap) with the two launch/slot
- * defects that make its outputs degenerate (NaN tile 0, empty ranges) off. */
-#define FVGS_QUIRKS_DEFAULT  (FVGS_Q_INVSIGMA_SWAP | FVGS_Q_MAP_CAP256)
+#define FVGS_Q_VIS_CAP256    0x10u
+#define FVGS_Q_ADAM_STAY     0x20u
+/* Default: the reference's arithmetic (swap, caps, optimiser state left in
+ * place) with the two launch/slot defects that make its outputs degenerate
+ * (NaN tile 0, empty ranges) off. */
+#define FVGS_QUIRKS_DEFAULT  (FVGS_Q_INVSIGMA_SWAP | FVGS_Q_MAP_CAP256 | FVGS_Q_VIS_CAP256 | FVGS_Q_ADAM_STAY)
 
 typedef struct fvgs_pose {
     float position[3];     /* camera centre in world frame */

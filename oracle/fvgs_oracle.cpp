@@ -1192,4 +1192,127 @@ int oracle_pyrdown_f32(const float* src, int W, int H, int c, float* dst) {
     return 0;
 }
 
+
+/*
+ * Map maintenance (src/GSCudaKernels.cu:1455-1739, drivers src/GSSlam.cu:
+ * 1467-1904).  rec[12N] are the blending records of oracle_make_records
+ * (u, v, z, opacity, c.x, c.y, c.z, phat.x, phat.y, r, g, b), c the inverse
+ * 2D covariance in the order the reference's kernels consume the stored
+ * inverse.
+ *
+ * computeGaussiansVisibility_kernel (1455-1537): every pixel inside the image
+ * walks the first min(n, cap) Gaussians of its tile list (cap <= 0: all), in
+ * order: d = mean - pixel, q = c.x dx^2 + 2 c.y dx dy + c.z dy^2,
+ * alpha = min(0.99, opacity exp(-q/2)); alpha < 1/255 skips the Gaussian;
+ * otherwise the Gaussian is visible and T *= 1 - alpha; the pixel stops once
+ * T < 0.5.  FP64.  vis[i] is set to 1 for visible Gaussians (not cleared).
+ */
+int oracle_visibility(const float* rec, const uint32_t* ranges, const uint32_t* indices, int n_gauss, int W, int H,
+                      int tw, int th, int cap, uint8_t* vis) {
+    const int ntx = (W + tw - 1) / tw;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const int tile = (y / th) * ntx + (x / tw);
+            const uint32_t r0 = ranges[2 * (size_t)tile], r1 = ranges[2 * (size_t)tile + 1];
+            uint32_t n = r1 > r0 ? r1 - r0 : 0;
+            if (cap > 0 && n > (uint32_t)cap) n = (uint32_t)cap;
+            double T = 1.0;
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t g = indices[r0 + k];
+                if ((int)g >= n_gauss) continue;
+                const float* r = rec + 12 * (size_t)g;
+                const double dx = (double)r[0] - x, dy = (double)r[1] - y;
+                const double q = r[4] * dx * dx + 2.0 * r[5] * dx * dy + r[6] * dy * dy;
+                const double alpha = std::min(0.99, (double)r[3] * std::exp(-0.5 * q));
+                if (alpha < 1.0 / 255.0) continue;
+                vis[g] = 1;
+                T *= 1.0 - alpha;
+                if (T < 0.5) break;
+            }
+        }
+    return 0;
+}
+
+/*
+ * computeOutliers_kernel (1620-1715): for every pixel inside the image and
+ * every Gaussian of its tile list: d = pixel - mean, rendered depth
+ * z + phat . d, q = c.x dx^2 + c.z dy^2 + 2 c.y dx dy (evalGaussian2D,
+ * 1401-1409, called with the stored inverse's x, z, y components),
+ * alpha = opacity exp(-q/2); alpha < 1/255 or rendered depth <= 0 skips;
+ * total_alpha += alpha, and outlier_prob += alpha where the observed depth is
+ * > 0.1 and the rendered depth < 0.8 x observed.  No alpha clamp and no
+ * early stop.  FP64 arithmetic, with each alpha rounded to FP32 (the
+ * reference's float: with the stored-layout inverse the quadratic form can be
+ * indefinite, and exp(-q/2) then overflows to inf as in FP32); FP64 sums,
+ * accumulated into the outputs (not cleared).
+ */
+int oracle_outlier_scores(const float* rec, const uint32_t* ranges, const uint32_t* indices, int n_gauss,
+                          const float* obs_depth, int W, int H, int tw, int th, double* total_alpha,
+                          double* outlier_prob) {
+    const int ntx = (W + tw - 1) / tw;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const int tile = (y / th) * ntx + (x / tw);
+            const uint32_t r0 = ranges[2 * (size_t)tile], r1 = ranges[2 * (size_t)tile + 1];
+            const double d_obs = obs_depth[(size_t)y * W + x];
+            for (uint32_t k = r0; k < r1; ++k) {
+                const uint32_t g = indices[k];
+                if ((int)g >= n_gauss) continue;
+                const float* r = rec + 12 * (size_t)g;
+                const double dx = x - (double)r[0], dy = y - (double)r[1];
+                const double dr = (double)r[2] + (double)r[7] * dx + (double)r[8] * dy;
+                const double q = r[4] * dx * dx + r[6] * dy * dy + 2.0 * r[5] * dx * dy;
+                const double alpha = (double)(float)((double)r[3] * std::exp(-0.5 * q));
+                if (alpha < 1.0 / 255.0 || dr <= 0.0) continue;
+                total_alpha[g] += alpha;
+                if (d_obs > 0.1 && dr < 0.8 * d_obs) outlier_prob[g] += alpha;
+            }
+        }
+    return 0;
+}
+
+/*
+ * removeOutliers_kernel (1717-1739) on the FP32 accumulators of the reference
+ * (the sums rounded to float): state 0xff where total_alpha > 1 and
+ * outlier_prob / total_alpha > threshold in FP32 (an infinite total gives a
+ * share of 0 or NaN: kept), else 0.  Returns the number marked.
+ */
+int oracle_outlier_states(const double* total_alpha, const double* outlier_prob, int n, float threshold,
+                          uint8_t* states) {
+    int marked = 0;
+    for (int i = 0; i < n; ++i) {
+        const float ta = (float)total_alpha[i], op = (float)outlier_prob[i];
+        const bool rm = ta > 1.0f && op / ta > threshold;
+        states[i] = rm ? 0xff : 0;
+        marked += rm;
+    }
+    return marked;
+}
+
+/*
+ * pruneGaussians_kernel (1566-1618), in FP32 as the reference: state 0xff
+ * where opacity < alpha_threshold, else where (s_x + s_y + s_z - s_max -
+ * s_min) / s_max < scale_ratio_threshold or s_max < min_scale.  Returns the
+ * number marked.
+ */
+int oracle_prune_states(const float* scales, const float* opac, int n, float alpha_threshold,
+                        float scale_ratio_threshold, float min_scale, uint8_t* states) {
+    int marked = 0;
+    for (int i = 0; i < n; ++i) {
+        bool rm;
+        if (opac[i] < alpha_threshold) {
+            rm = true;
+        } else {
+            const float sx = scales[3 * (size_t)i], sy = scales[3 * (size_t)i + 1], sz = scales[3 * (size_t)i + 2];
+            const float smax = std::fmax(sx, std::fmax(sy, sz));
+            const float smin = std::fmin(sx, std::fmin(sy, sz));
+            const float smed = sx + sy + sz - smax - smin;
+            rm = smed / smax < scale_ratio_threshold || smax < min_scale;
+        }
+        states[i] = rm ? 0xff : 0;
+        marked += rm;
+    }
+    return marked;
+}
+
 }  // extern "C"

@@ -58,7 +58,9 @@ Q_CULLED_SLOTS = 0x1
 Q_RANGE_LAUNCH = 0x2
 Q_INVSIGMA_SWAP = 0x4
 Q_MAP_CAP256 = 0x8
-QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256
+Q_VIS_CAP256 = 0x10
+Q_ADAM_STAY = 0x20
+QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY
 
 
 def default_params(quirks: int = QUIRKS_DEFAULT, tile=(16, 16)) -> Params:
@@ -389,3 +391,62 @@ def pose_plus(pose, delta):
     )
     q2 /= np.linalg.norm(q2)
     return t2, q2
+
+
+# ----------------------------------------------------------------------------
+# map maintenance (src/GSCudaKernels.cu:1455-1739, src/GSSlam.cu:1467-1904)
+# ----------------------------------------------------------------------------
+def visibility(b: Binning, W, H, params: Params, cap: int | None = None):
+    """computeGaussiansVisibility_kernel over the binned view: uint8 mask per
+    Gaussian (1 = some pixel blends it before its T falls below 0.5).  cap
+    defaults to 256 with Q_VIS_CAP256 set in params.quirks, else all."""
+    n = b.rec.shape[0]
+    if cap is None:
+        cap = 256 if (params.quirks & Q_VIS_CAP256) else 0
+    vis = np.zeros(max(n, 1), np.uint8)
+    lib().oracle_visibility(_p(b.rec), _p(b.ranges), _p(b.vals), C.c_int(n), C.c_int(W), C.c_int(H),
+                            C.c_int(params.tile_w), C.c_int(params.tile_h), C.c_int(cap), _p(vis))
+    return vis[:n]
+
+
+def outlier_scores(b: Binning, obs_depth, W, H, params: Params):
+    """computeOutliers_kernel sums in FP64: (total_alpha, outlier_prob) per Gaussian."""
+    n = b.rec.shape[0]
+    ta = np.zeros(max(n, 1), np.float64)
+    op = np.zeros(max(n, 1), np.float64)
+    lib().oracle_outlier_scores(_p(b.rec), _p(b.ranges), _p(b.vals), C.c_int(n), _p(_f32(obs_depth)), C.c_int(W),
+                                C.c_int(H), C.c_int(params.tile_w), C.c_int(params.tile_h), _p(ta), _p(op))
+    return ta[:n], op[:n]
+
+
+def outlier_states(total_alpha, outlier_prob, threshold: float = 0.6):
+    """removeOutliers_kernel: 0xff where total_alpha > 1 and the outlier share > threshold."""
+    ta = np.ascontiguousarray(total_alpha, np.float64)
+    op = np.ascontiguousarray(outlier_prob, np.float64)
+    st = np.zeros(max(ta.shape[0], 1), np.uint8)
+    lib().oracle_outlier_states(_p(ta), _p(op), C.c_int(ta.shape[0]), C.c_float(threshold), _p(st))
+    return st[:ta.shape[0]]
+
+
+def prune_states(scene, alpha_threshold=0.05, scale_ratio_threshold=0.05, min_scale=0.005):
+    """pruneGaussians_kernel in FP32: 0xff for Gaussians to prune."""
+    sc, op = _f32(scene.scales), _f32(scene.opacities)
+    st = np.zeros(max(scene.n, 1), np.uint8)
+    lib().oracle_prune_states(_p(sc), _p(op), C.c_int(scene.n), C.c_float(alpha_threshold),
+                              C.c_float(scale_ratio_threshold), C.c_float(min_scale), _p(st))
+    return st[:scene.n]
+
+
+def compact_order(states):
+    """Order of thrust::sort_by_key on the 0 / 0xff states (radix sort of
+    unsigned char keys, stable): survivors in order, then the removed ones."""
+    return np.argsort(np.asarray(states, np.uint8), kind="stable")
+
+
+def covisibility(vis_a, vis_b):
+    """computeGaussiansCovisibility_kernel + the driver's ratio: (inter, union,
+    inter / union as float32, 0 for an empty union)."""
+    a = np.asarray(vis_a) != 0
+    b = np.asarray(vis_b) != 0
+    inter, uni = int(np.sum(a & b)), int(np.sum(a | b))
+    return inter, uni, (np.float32(inter) / np.float32(uni)) if uni else np.float32(0.0)

@@ -273,3 +273,86 @@ def test_kat_render_view_single_gaussian(oracle):
                                     C.c_int(W), C.c_int(H), C.c_int(16), C.c_int(16), p(out_c), p(out_d))
     assert abs(out_c[2, 3, 0] - 0.5) < 1e-15 and out_d[2, 3] == 2.0
     assert abs(out_c[2, 4, 0] - 0.5 * np.exp(-0.5)) < 1e-15 and out_d[2, 4] == 1e10
+
+
+class _Bin:
+    """A hand-made binned view: records rec[12N], one tile list."""
+
+    def __init__(self, rec, order):
+        self.rec = np.ascontiguousarray(rec, np.float32)
+        self.vals = np.asarray(order, np.uint32)
+        self.ranges = np.array([[0, len(order)]], np.uint32)
+
+
+def _rec(u, v, z, opa, c=(1.0, 0.0, 1.0), phat=(0.0, 0.0)):
+    return [u, v, z, opa, c[0], c[1], c[2], phat[0], phat[1], 0.5, 0.5, 0.5]
+
+
+def test_kat_visibility(oracle):
+    """computeGaussiansVisibility_kernel (src/GSCudaKernels.cu:1455-1537), one
+    tile of 8x4 pixels: g0 (opacity 0.6 on pixel (1,1)) is seen and stops that
+    pixel (T = 0.4 < 0.5); g1 (0.9, same place, behind g0) is seen from pixel
+    (2,1), where g0 leaves T = 1 - 0.6 e^-1/2; g2 is far outside the image;
+    g3 (opacity 0.003) never reaches alpha 1/255.  With a cap of one Gaussian
+    per tile only g0 is considered."""
+    b = _Bin([_rec(1, 1, 1, 0.6), _rec(1, 1, 2, 0.9), _rec(100, 100, 1, 0.9), _rec(5, 2, 1, 0.003)],
+             [0, 1, 2, 3])
+    P = oracle.default_params()
+    np.testing.assert_array_equal(oracle.visibility(b, 8, 4, P, cap=0), [1, 1, 0, 0])
+    np.testing.assert_array_equal(oracle.visibility(b, 8, 4, P, cap=1), [1, 0, 0, 0])
+    # seen only through pixel (1,1): g1 first in the list hides g0 there, but
+    # g0 still reaches alpha >= 1/255 on other pixels
+    np.testing.assert_array_equal(oracle.visibility(_Bin(b.rec, [1, 0]), 8, 4, P, cap=0), [1, 1, 0, 0])
+
+
+def test_kat_outlier_scores_and_states(oracle):
+    """computeOutliers_kernel / removeOutliers_kernel (src/GSCudaKernels.cu:
+    1620-1739): one Gaussian of opacity 0.5 at pixel (3,2), unit inverse
+    covariance, depth 2, zero phat, over an 8x4 image whose observed depth is
+    3 for x < 4 (rendered 2 < 0.8 * 3: outlier evidence) and 2 elsewhere;
+    a second Gaussian at depth -1 never counts (rendered depth <= 0)."""
+    W, H = 8, 4
+    b = _Bin([_rec(3, 2, 2, 0.5), _rec(3, 2, -1, 0.5)], [0, 1])
+    obs = np.full((H, W), 2.0, np.float32)
+    obs[:, :4] = 3.0
+    ta, op = oracle.outlier_scores(b, obs, W, H, oracle.default_params())
+    want_t = want_o = 0.0
+    for y in range(H):
+        for x in range(W):
+            a = float(np.float32(0.5 * np.exp(-0.5 * ((x - 3) ** 2 + (y - 2) ** 2))))
+            if a < 1 / 255:
+                continue
+            want_t += a
+            want_o += a if x < 4 else 0.0
+    assert ta[0] == want_t and op[0] == want_o and ta[1] == 0.0 and op[1] == 0.0
+    share = want_o / want_t
+    assert want_t > 1.0 and 0.65 < share < 0.75
+    np.testing.assert_array_equal(oracle.outlier_states(ta, op, 0.6), [0xff, 0])
+    np.testing.assert_array_equal(oracle.outlier_states(ta, op, 0.75), [0, 0])
+    # FP32 edges: a share of exactly 0.6f is not above 0.6f; an infinite
+    # total gives a share of 0 (or NaN): kept; a total of at most 1: kept
+    ta2 = np.array([0.5, 2.0, 2.0, 2.0, np.inf, np.inf])
+    op2 = np.array([0.5, 1.3, 1.1, 1.2, 1.0, np.inf])
+    np.testing.assert_array_equal(oracle.outlier_states(ta2, op2, 0.6), [0, 0xff, 0, 0, 0, 0])
+
+
+def test_kat_prune_states(oracle):
+    """pruneGaussians_kernel (src/GSCudaKernels.cu:1566-1618) with the
+    reference's thresholds 0.05 / 0.05 / 0.005."""
+    scales = np.array([[0.1, 0.1, 0.1], [0.1, 0.1, 0.1], [0.1, 0.1, 0.1], [0.1, 0.004, 0.1],
+                       [0.1, 0.004, 0.0001], [0.004, 0.004, 0.004], [0.0049, 0.0049, 0.006]], np.float32)
+    opac = np.array([0.5, 0.04, 0.05, 0.5, 0.5, 0.5, 0.5], np.float32)
+    sc = S.Scene(np.zeros((7, 3), np.float32), scales, np.tile(S.IDENTITY_Q, (7, 1)),
+                 np.zeros((7, 3), np.float32), opac)
+    #        keep, transparent, at threshold, flat but wide, needle, tiny, max >= 0.005
+    want = [0, 0xff, 0, 0, 0xff, 0xff, 0]
+    np.testing.assert_array_equal(oracle.prune_states(sc), want)
+
+
+def test_kat_compaction_order_and_covisibility(oracle):
+    """thrust::sort_by_key on 0 / 0xff states (src/GSSlam.cu:1536-1548) keeps
+    the survivors in order, then the removed ones; computeCovisibilityRatio
+    (src/GSSlam.cu:1713-1904) divides |a and b| by |a or b|."""
+    np.testing.assert_array_equal(oracle.compact_order([0, 0xff, 0, 0xff, 0]), [0, 2, 4, 1, 3])
+    assert oracle.covisibility([1, 1, 0, 1, 0], [0, 1, 1, 1, 0]) == (2, 4, np.float32(0.5))
+    assert oracle.covisibility([0, 0], [0, 0]) == (0, 0, np.float32(0.0))
