@@ -377,6 +377,9 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     e2e_ms = e0.elapsed_time(e1)
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], dev, world)
 
+    maint = measure_maintenance(fvgs, sess, frames, K, W, H, reps=max(3, args.steps),
+                                with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+
     dominant = max((c for c in timing if timing[c]["timed"]), key=lambda c: timing[c]["ms"])
     peak, peak_kind = load_peaks()
     per_launch_ms = timing[dominant]["ms"] / max(1, timing[dominant]["timed"])
@@ -398,7 +401,74 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": load_traffic().get(dominant), "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": algo, "ms_per_launch": per_launch_ms},
+        "maintenance": maint,
     }
+
+
+def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
+    """Map maintenance on the large workload's map (GSSlam::removeOutliers,
+    computeCovisibilityRatio, prune): per-call wall time of the synchronous
+    C-ABI calls (median of `reps`, marking only, so the map stays the same),
+    the maintenance kernels' CUDA-event time, then one removal of each kind
+    (which compacts the map).  The outlier pass scores every (pixel,
+    Gaussian) pair of the view's tile lists: `pairs` per call."""
+    pose, kf_pose = frames[-1]["pose"], frames[0]["pose"]
+    out = {}
+
+    def timed(fn):
+        fn()  # warm (binning history, buffers)
+        sess.set_timing(["maint"])
+        sess.get_timing(reset=True)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            r = fn()
+            ts.append(time.perf_counter() - t0)
+        t = sess.get_timing(reset=True)["maint"]
+        sess.set_timing(())
+        return r, 1000.0 * float(np.median(ts)), t["ms"] / max(1, t["timed"]), t["launches"] // max(1, reps)
+
+    marked, ms, kms, kl = timed(lambda: sess.remove_outliers(pose, K, level=0, remove=False))
+    n_inst = int(sess.binning_info()["n_instances"])
+    out["remove_outliers"] = {"call_ms": ms, "maint_kernels_ms": kms, "launches": kl, "marked": marked,
+                              "pairs": n_inst * 256,
+                              "pairs_per_s": n_inst * 256 / (kms / 1000.0) if kms > 0 else None}
+    cov, ms, kms, kl = timed(lambda: sess.covisibility(kf_pose, K, W, H, pose, K, W, H))
+    out["covisibility"] = {"call_ms": ms, "maint_kernels_ms": kms, "launches": kl, "ratio": cov[2]}
+    marked, ms, kms, kl = timed(lambda: sess.prune(remove=False))
+    out["prune_mark"] = {"call_ms": ms, "maint_kernels_ms": kms, "marked": marked}
+    n0 = sess.n
+    t0 = time.perf_counter()
+    removed = sess.remove_outliers(pose, K, level=0)
+    out["remove_outliers_compact"] = {"call_ms": 1000.0 * (time.perf_counter() - t0), "removed": removed,
+                                      "gaussians_before": n0}
+    t0 = time.perf_counter()
+    removed = sess.prune()
+    out["prune_compact"] = {"call_ms": 1000.0 * (time.perf_counter() - t0), "removed": removed}
+    if with_cpu:
+        out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["depth"])
+    return out
+
+
+def cpu_outlier_sample(sess, pose, K, W, H, depth, band_rows=64):
+    """The oracle's outlier scores (computeOutliers_kernel restated, one
+    thread) on a band of rows through the image centre, scaled to the frame."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from f_vigs_slam_gb300 import synthetic as S
+
+    O.build()
+    pos, scl, rot, col, opa = sess.download()
+    scene = S.Scene(pos, scl, rot, col, opa)
+    P = O.default_params()
+    y0 = ((H - band_rows) // 2 // 16) * 16
+    K_band = (K[0], K[1], K[2], K[3] - y0)
+    b = O.prepare(scene, pose, K_band, W, band_rows, P)
+    t0 = time.perf_counter()
+    O.outlier_scores(b, np.ascontiguousarray(depth[y0:y0 + band_rows]), W, band_rows, P)
+    t = time.perf_counter() - t0
+    return {"outlier_scores_ms_per_frame": 1000.0 * t * H / band_rows, "cores": 1, "kind": "port",
+            "sample": "%d rows of %d, %.2f s, scaled by rows" % (band_rows, H, t)}
 
 
 def set_frame_tensors(fvgs, sess, level, fr, W, H):
@@ -663,7 +733,8 @@ def run_ours(args):
             "gpu_launches": srv["launches"],
             "graphed_frames": srv["graphed_frames"],
             "roofline": large["roofline"],
-            "large_plain": {k: v for k, v in large.items() if k != "roofline"},
+            "large_plain": {k: v for k, v in large.items() if k not in ("roofline", "maintenance")},
+            "maintenance": large["maintenance"],
             "clocks": srv["clocks"],
             "cpu_baseline": cpu,
         }

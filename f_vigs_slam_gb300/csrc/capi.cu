@@ -141,6 +141,8 @@ struct fvgs_session {
     size_t pre_u8_px[kMaxLevels] = {};
     uint8_t* pre_raw = nullptr;  // camera depth as given (float or uint16)
     size_t pre_raw_bytes = 0;
+    int pre_w = 0, pre_h = 0;
+    bool pre_valid = false;  // pre_u8[0] and lv[0].depth hold the same camera frame
 
     DevPose* pose = nullptr;
     double* jj = nullptr;    // 42 doubles: JtJ[36], Jtr[6]
@@ -182,6 +184,8 @@ struct fvgs_session {
     uint32_t* h_mk_ctr = nullptr;  // pinned mirror
     uint32_t mk_n = 0;             // Gaussians covered by the last marking
     bool mk_scores = false;        // the last marking was an outlier pass (scores valid)
+    uint32_t *sd_block_keep = nullptr, *sd_block_base = nullptr;  // seeding: per block of sample cells
+    size_t sd_blocks = 0;
 
     // kernel accounting: launches per class (always), event timing (opt-in)
     uint32_t timing_mask = 0;
@@ -207,6 +211,7 @@ struct fvgs_session {
     struct FrameGraph {
         bool valid = false;
         int level = 0, iterations = 0, W = 0, H = 0;
+        uint32_t n_g = 0;  // launch shapes and kernel arguments depend on the Gaussian count
         fvgs_intrinsics K{};
         float eta = -1.f;
         uint64_t gen = 0;
@@ -835,6 +840,9 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->mk_block_keep, N / kCompactBlock + 1);
     FV_A(s->mk_block_base, N / kCompactBlock + 1);
     FV_A(s->mk_ctr, 4);
+    s->sd_blocks = (size_t)max_width * max_height / kCompactBlock + 2;  // one sample cell per pixel at most
+    FV_A(s->sd_block_keep, s->sd_blocks);
+    FV_A(s->sd_block_base, s->sd_blocks);
 #undef FV_A
     if (cudaMallocHost(&s->h_jj, sizeof(double) * 48) != cudaSuccess ||
         cudaMallocHost(&s->h_st, sizeof(DevStatus)) != cudaSuccess ||
@@ -1003,6 +1011,9 @@ int fvgs_preprocess_frame(fvgs_session* s, const uint8_t* color, const void* dep
         }
         FV_TRY(ensure_level(s, l, W, H));
     }
+    s->pre_valid = true;
+    s->pre_w = width;
+    s->pre_h = height;
     FV_CK(cudaMemcpyAsync(s->pre_u8[0], color, 3 * px0, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(s->pre_raw, depth, raw_bytes, cudaMemcpyDefault, s->stream));
     FV_CK(launch_depth_in(s->pre_raw, depth_u16_mm, px0, s->lv[0].depth, s->stream));
@@ -1043,6 +1054,7 @@ int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* de
     FrameLevel& f = s->lv[level];
     const size_t px = (size_t)width * height;
     FV_TRY(ensure_level(s, level, width, height));
+    if (level == 0) s->pre_valid = false;  // level 0 no longer holds the preprocessed camera frame
     FV_CK(cudaMemcpyAsync(f.rgb, rgb, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.depth, depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.gx, grad_x, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
@@ -1253,7 +1265,7 @@ bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
     const FrameLevel& f = s->lv[r.level];
     return g.valid && g.gen == s->gen && g.level == r.level && g.iterations == r.iterations && g.W == f.W &&
            g.H == f.H && g.eta == r.eta && g.K.fx == r.K.fx && g.K.fy == r.K.fy && g.K.cx == r.K.cx &&
-           g.K.cy == r.K.cy && g.vals_in == s->vals && g.ranges_in == s->ranges;
+           g.K.cy == r.K.cy && g.n_g == s->n_g && g.vals_in == s->vals && g.ranges_in == s->ranges;
 }
 
 // Whether a frame may run from a captured graph: the binning history must be
@@ -1315,6 +1327,7 @@ int launch_frame(fvgs_session* s) {
     const int ntx0 = s->hist_ntx, nty0 = s->hist_nty, lw0 = s->last_W, lh0 = s->last_H, lt0 = s->last_T;
     g.vals_in = s->vals;
     g.ranges_in = s->ranges;
+    g.n_g = s->n_g;
     cudaGraph_t graph = nullptr;
     int rc = FVGS_OK;
     cudaError_t ec = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
@@ -1869,6 +1882,129 @@ int fvgs_download_adam_state(fvgs_session* s, float* state, uint32_t n) {
                               cudaMemcpyDefault, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
     return FVGS_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Seeding from the camera frame (GSSlam::initializeGaussiansFromRgbd,
+// src/GSSlam.cu:271-407; GSSlam::densify, src/GSSlam.cu:1351-1465).
+namespace {
+
+SeedArgs seed_args(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int sample) {
+    SeedArgs a{};
+    a.bgr = s->pre_u8[0];
+    a.depth = s->lv[0].depth;
+    a.W = s->pre_w;
+    a.H = s->pre_h;
+    a.sample = sample;
+    a.ncx = (a.W + sample - 1) / sample;
+    a.ncy = (a.H + sample - 1) / sample;
+    a.K = *K;
+    a.pose_q = make_float4(pose->orientation[0], pose->orientation[1], pose->orientation[2], pose->orientation[3]);
+    a.pose_t = make_float3(pose->position[0], pose->position[1], pose->position[2]);
+    a.cap = s->cap_g;
+    a.block_keep = s->sd_block_keep;
+    a.block_base = s->sd_block_base;
+    a.pos = s->pos;
+    a.scale = s->scale;
+    a.rot = s->rot;
+    a.col = s->col;
+    return a;
+}
+
+int enqueue_seed(fvgs_session* s, SeedMode mode, const SeedArgs& a) {
+    const uint32_t cells = (uint32_t)a.ncx * (uint32_t)a.ncy;
+    if ((cells + kCompactBlock - 1) / kCompactBlock > s->sd_blocks) return FVGS_E_INVALID;
+    KScope k(s, FVGS_K_MAINT, 3);
+    FV_CK(launch_seed_count(mode, a, s->stream));
+    FV_CK(launch_compact_scan(s->sd_block_keep, cells, s->sd_block_base, s->mk_ctr, s->stream));
+    FV_CK(launch_seed_emit(mode, a, s->stream));
+    FV_CK(cudaMemcpyAsync(s->h_mk_ctr, s->mk_ctr, sizeof(uint32_t) * 2, cudaMemcpyDeviceToHost, s->stream));
+    return FVGS_OK;
+}
+
+void map_grew(fvgs_session* s, uint32_t n) {
+    s->n_g = n;
+    s->has_binning = s->has_track = s->has_map = false;
+    s->hist_ok = false;  // the new Gaussians have no previous binning
+    s->keys_valid = false;
+    s->dbg_proj_valid = false;
+    ++s->gen;
+}
+
+}  // namespace
+
+int fvgs_init_gaussians(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int sample_px,
+                        float init_scale, float init_opacity, uint32_t* n_gaussians) {
+    if (!s || !valid_pose(pose) || !K || sample_px < 1) return FVGS_E_INVALID;
+    if (!s->pre_valid) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    SeedArgs a = seed_args(s, pose, K, sample_px);
+    a.init_scale = init_scale;
+    a.init_opacity = init_opacity;
+    a.n0 = 0;
+    // a new map: optimiser state starts at zero, as the reference's empty adam_states_
+    FV_CK(cudaMemsetAsync(s->adam, 0, sizeof(float4) * 9 * (size_t)s->cap_g, s->stream));
+    FV_TRY(enqueue_seed(s, kSeedInit, a));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    collect_timing(s);
+    map_grew(s, std::min<uint32_t>(s->h_mk_ctr[0], s->cap_g));
+    if (n_gaussians) *n_gaussians = s->n_g;
+    return FVGS_OK;
+}
+
+int fvgs_densify(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int sample_px, float* mask,
+                 uint32_t* n_added) {
+    if (!s || !valid_pose(pose) || !K || sample_px < 1) return FVGS_E_INVALID;
+    if (!s->pre_valid) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    if (n_added) *n_added = 0;
+    if (s->n_g == 0) return FVGS_OK;  // as the reference: nothing to densify against
+    const int W = s->pre_w, H = s->pre_h;
+    FV_TRY(check_view(s, W, H));
+    const size_t px = (size_t)W * H;
+    FV_TRY(ensure_images(s, px));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, W, H));
+        DensityArgs da{};
+        da.rec0 = s->rec0;
+        da.rec1 = s->rec1;
+        da.rec2 = s->rec2;
+        da.ranges = s->ranges;
+        da.indices = s->vals;
+        da.n_list = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
+        da.n_gauss = s->n_g;
+        da.obs_depth = s->lv[0].depth;
+        da.W = W;
+        da.H = H;
+        da.ntx = (W + s->params.tile_w - 1) / s->params.tile_w;
+        da.nty = (H + s->params.tile_h - 1) / s->params.tile_h;
+        da.mask = s->img_T;  // the density mask lives in the final-transmittance image
+        {
+            KScope k(s, FVGS_K_MAINT, 1);
+            FV_CK(launch_density_mask(da, s->stream));
+        }
+        SeedArgs a = seed_args(s, pose, K, sample_px);
+        a.mask = s->img_T;
+        a.n0 = s->n_g;
+        a.adam = (s->params.quirks & FVGS_Q_ADAM_STAY) ? nullptr : s->adam;
+        FV_TRY(enqueue_seed(s, kSeedDensify, a));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        if (mask) FV_CK(cudaMemcpyAsync(mask, s->img_T, sizeof(float) * px, cudaMemcpyDefault, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;  // seeds past the map were written but not adopted
+        const uint64_t total = (uint64_t)s->n_g + s->h_mk_ctr[0];
+        const uint32_t n_new = (uint32_t)std::min<uint64_t>(total, s->cap_g);
+        if (n_added) *n_added = n_new - s->n_g;
+        if (n_new != s->n_g) map_grew(s, n_new);
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
 }
 
 }  // extern "C"

@@ -172,6 +172,17 @@ __device__ __forceinline__ void pdl_begin() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// A Gaussian of opacity o yields alpha = min(0.99, o exp(-v/2)) < 1/255
+// (with or without the clamp) exactly when v > 2 ln(255 o).  The bound
+// returned is that value plus a margin far above the rounding of expf and of
+// the product, so pairs beyond it are rejected without evaluating the
+// exponential, with the same outcome.
+__device__ __forceinline__ float reject_bound(float o) {
+    if (!(o > 0.0f)) return -INFINITY;
+    const float b = 2.0f * logf(255.0f * o);
+    return b + 1e-3f + 1e-4f * fabsf(b);
+}
+
 // Bounded spin budget for device-side waits; on expiry a kernel records
 // kErrTimeout and carries on with a safe value instead of hanging.
 constexpr uint32_t kSpinLimit = 1u << 24;

@@ -335,4 +335,38 @@ cudaError_t launch_compact_scan(const uint32_t* block_keep, uint32_t n, uint32_t
 cudaError_t launch_compact_scatter(const CompactArgs& a, cudaStream_t s);
 cudaError_t launch_covis_count(const uint8_t* va, const uint8_t* vb, uint32_t n, uint32_t* counters, cudaStream_t s);
 
+// ---- seeding from an RGB-D frame (seed.cu) ----
+enum SeedMode { kSeedInit = 0, kSeedDensify = 1 };
+struct SeedArgs {
+    const uint8_t* bgr;   // W x H x 3 bytes, (b, g, r)
+    const float* depth;   // W x H, metres
+    const float* mask;    // densify: W x H density mask
+    int W, H;
+    int sample;           // sample cell edge in pixels
+    int ncx, ncy;         // sample cells
+    fvgs_intrinsics K;
+    float4 pose_q;        // raw, read as (w, x, y, z)
+    float3 pose_t;
+    float init_scale, init_opacity;
+    uint32_t n0, cap;     // first slot written; slots >= cap are dropped
+    uint32_t* block_keep;        // count: seeds per block of cells
+    const uint32_t* block_base;  // emit: seeds before each block
+    float4 *pos, *scale, *rot, *col;
+    float4* adam;  // emit: zero the optimiser state of each seed (null: leave it)
+};
+struct DensityArgs {
+    const float4* rec0;
+    const float4* rec1;
+    const float4* rec2;
+    const uint2* ranges;
+    const uint32_t* indices;
+    uint32_t n_list, n_gauss;
+    const float* obs_depth;  // P
+    int W, H, ntx, nty;
+    float* mask;  // P
+};
+cudaError_t launch_seed_count(SeedMode mode, const SeedArgs& a, cudaStream_t s);
+cudaError_t launch_seed_emit(SeedMode mode, const SeedArgs& a, cudaStream_t s);
+cudaError_t launch_density_mask(const DensityArgs& a, cudaStream_t s);
+
 }  // namespace fvgs

@@ -22,10 +22,10 @@
 //    a Gaussian's flag is written once per tile, from a shared hit mask,
 //    instead of once per pixel;
 //  * outlier scores: the reference adds every (pixel, Gaussian) contribution
-//    with two global atomics.  Here four lanes take one Gaussian of the tile
-//    list and four rows of pixels each, the quad sums its partials in a fixed
-//    order and one lane adds the tile's total with one atomic per
-//    accumulator: the same sums, one global update per (tile, Gaussian);
+//    with two global atomics.  Here a thread takes one Gaussian of the tile
+//    list, sums its contributions over the tile's pixels in a fixed order and
+//    adds the tile's totals with one atomic per accumulator: the same sums,
+//    one global update per (tile, Gaussian);
 //  * compaction: mark (state + survivors per block) -> one-CTA scan of the
 //    block counts -> scatter into the session's second set of planes, after
 //    which the host swaps the plane pointers.  The source planes are never
@@ -93,7 +93,6 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * 16, y0 = ty * 16;
-    const int w = min(16, a.W - x0);
     const int tid = threadIdx.x;
     {
         const int x = x0 + (tid & 15), y = y0 + (tid >> 4);
@@ -102,43 +101,35 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
     uint2 range = a.ranges[tile];
     range.y = min(range.y, a.n_list);
     const int n = range.y > range.x ? (int)(range.y - range.x) : 0;
+    const int w = min(16, a.W - x0), h = min(16, a.H - y0);
     __syncthreads();
-    const int quad = tid & 3;
-    // rows quad*4 .. quad*4+3 of the tile, clipped to the image
-    const int r_begin = quad * 4, r_end = min(quad * 4 + 4, a.H - y0);
-    const int items = n * 4;
-    const int rounds = (items + kMPix - 1) / kMPix;  // uniform: every quad stays whole for the shuffles
-    for (int it = 0; it < rounds; ++it) {
-        const int item = it * kMPix + tid;
-        const int li = item >> 2;
+    // One thread per Gaussian of the tile list, over all pixels of the tile
+    // in row-major order (every lane of a warp reads the same pixel's depth:
+    // a shared-memory broadcast); its sums go out with one atomic each.
+    for (int li = tid; li < n; li += kMPix) {
+        const uint32_t g = a.indices[range.x + li];
+        if (g >= a.n_gauss) continue;
+        const float4 r0 = a.rec0[g], r1 = a.rec1[g];
+        const float phy = a.rec2[g].x;
         float ta = 0.f, to = 0.f;
-        uint32_t g = 0xffffffffu;
-        if (li < n) g = a.indices[range.x + li];
-        if (g < a.n_gauss) {
-            const float4 r0 = a.rec0[g], r1 = a.rec1[g];
-            const float phy = a.rec2[g].x;
-            for (int yy = r_begin; yy < r_end; ++yy) {
-                const float dy = (float)(y0 + yy) - r0.y;
-                for (int xx = 0; xx < w; ++xx) {
-                    const float dx = (float)(x0 + xx) - r0.x;
-                    const float dr = r0.z + r1.w * dx + phy * dy;
-                    const float q = r1.x * dx * dx + r1.z * dy * dy + 2.0f * r1.y * dx * dy;
-                    const float alpha = r0.w * expf(-0.5f * q);
-                    if (alpha < 1.0f / 255.0f || dr <= 0.0f) continue;
-                    ta += alpha;
-                    const float d_obs = sD[yy * 16 + xx];
-                    if (d_obs > 0.1f && dr < 0.8f * d_obs) to += alpha;
-                }
+        for (int yy = 0; yy < h; ++yy) {
+            const float dy = (float)(y0 + yy) - r0.y;
+            const float q_row = r1.z * dy * dy, b_row = 2.0f * r1.y * dy;
+            const float dr_row = r0.z + phy * dy;
+#pragma unroll 4
+            for (int xx = 0; xx < w; ++xx) {
+                const float dx = (float)(x0 + xx) - r0.x;
+                const float q = (r1.x * dx + b_row) * dx + q_row;
+                const float alpha = r0.w * expf(-0.5f * q);
+                const float dr = dr_row + r1.w * dx;
+                if (alpha < 1.0f / 255.0f || dr <= 0.0f) continue;
+                ta += alpha;
+                const float d_obs = sD[yy * 16 + xx];
+                if (d_obs > 0.1f && dr < 0.8f * d_obs) to += alpha;
             }
         }
-        ta += __shfl_xor_sync(0xffffffffu, ta, 1);
-        to += __shfl_xor_sync(0xffffffffu, to, 1);
-        ta += __shfl_xor_sync(0xffffffffu, ta, 2);
-        to += __shfl_xor_sync(0xffffffffu, to, 2);
-        if (quad == 0 && g < a.n_gauss) {
-            if (ta != 0.f) atomicAdd(a.total_alpha + g, ta);
-            if (to != 0.f) atomicAdd(a.outlier_prob + g, to);
-        }
+        if (ta != 0.f) atomicAdd(a.total_alpha + g, ta);
+        if (to != 0.f) atomicAdd(a.outlier_prob + g, to);
     }
 }
 

@@ -82,16 +82,6 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
     return v[0];
 }
 
-// A Gaussian of opacity o yields alpha = min(0.99, o exp(-v/2)) < 1/255
-// exactly when v > 2 ln(255 o).  vreject is that bound plus a margin far
-// above the rounding of expf and of the product, so pairs beyond it are
-// rejected without evaluating the exponential, with the same outcome.
-__device__ __forceinline__ float reject_bound(float o) {
-    if (!(o > 0.0f)) return -INFINITY;
-    const float b = 2.0f * logf(255.0f * o);
-    return b + 1e-3f + 1e-4f * fabsf(b);
-}
-
 // Stage one Gaussian's blending record: from the packed record planes, or
 // (REF_LAYOUT) built from the reference's separate screen-space buffers.
 template <bool REF_LAYOUT>

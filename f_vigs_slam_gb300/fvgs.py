@@ -428,6 +428,26 @@ class Session:
                "fvgs_covisibility")
         return int(i.value), int(u.value), float(r.value)
 
+    def init_gaussians(self, pose, K, sample_px: int = 10, init_scale: float = 2.0, init_opacity: float = 0.8) -> int:
+        """GSSlam::initializeGaussiansFromRgbd (fvgs_init_gaussians) from the last preprocessed camera frame:
+        the new Gaussian count."""
+        n = C.c_uint32()
+        _check(self.lib.fvgs_init_gaussians(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)),
+                                            C.c_int(sample_px), C.c_float(init_scale), C.c_float(init_opacity),
+                                            C.byref(n)), "fvgs_init_gaussians")
+        self.n = int(n.value)
+        return self.n
+
+    def densify(self, pose, K, sample_px: int = 10, W: int | None = None, H: int | None = None):
+        """GSSlam::densify (fvgs_densify) against the last preprocessed camera frame: Gaussians added, and the
+        density mask (H, W) when W and H are given."""
+        m = np.zeros((H, W), np.float32) if W is not None else None
+        a = C.c_uint32()
+        _check(self.lib.fvgs_densify(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(sample_px),
+                                     _ptr(m), C.byref(a)), "fvgs_densify")
+        self.n += int(a.value)
+        return (int(a.value), m) if m is not None else int(a.value)
+
     # ---- asynchronous frames (CUDA-graph replay once the binning history is valid)
     def frame_submit(self, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None):
         _check(self.lib.fvgs_frame_submit(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),

@@ -298,6 +298,42 @@ int fvgs_covisibility(fvgs_session* s, const fvgs_pose* pose_a, const fvgs_intri
                       uint32_t* n_inter, uint32_t* n_union, float* ratio);
 
 /*
+ * Seeding from the camera frame last given to fvgs_preprocess_frame (its
+ * 8-bit colour, 3 bytes per pixel in the reference's (b, g, r) order, and its
+ * depth in metres; FVGS_E_STATE if fvgs_set_frame has replaced level 0 since).
+ * The pose's orientation is read as (w, x, y, z) and the seeds' orientations
+ * are written in that order, as the reference's seeding kernels do (the
+ * projection reads the same float4 as (x, y, z, w)).  The reference reserves
+ * seed slots with an atomic counter, in no defined order; here seeds are
+ * numbered in row-major order of their sample cell, and seeds beyond the
+ * session's capacity are dropped.
+ *
+ * fvgs_init_gaussians: GSSlam::initializeGaussiansFromRgbd
+ * (src/GSSlam.cu:271-407), computeNormalsFromDepth_kernel +
+ * initGaussiansFromRgbd_kernel (src/GSCudaKernels.cu:87-315).  Replaces the
+ * map: one Gaussian per sample pixel (every sample_px-th pixel in x and y)
+ * with depth > 0 -- back-projected position, scale init_scale, orientation
+ * turning +z onto the depth-map normal, colour / 255, opacity init_opacity
+ * (reference defaults 10, 2.0, 0.8) -- and zeroes the optimiser state.
+ *
+ * fvgs_densify: GSSlam::densify (src/GSSlam.cu:1351-1465),
+ * computeDensityMask_kernel + densifyGaussians_kernel
+ * (src/GSCudaKernels.cu:1741-2066).  Bins the frame's view at `pose`, builds
+ * the density mask (transmittance where the map leaves more than half the
+ * light, 1 where the map's median depth lies more than 20% behind the
+ * observed depth), and appends one Gaussian per sample cell of which at
+ * least half the pixels are marked (sample_px = 1: per marked pixel).
+ * mask (W x H floats, host or device) may be null; *n_added = Gaussians
+ * appended.  With FVGS_Q_ADAM_STAY the new Gaussians keep the optimiser state
+ * found at their slots (the reference's adam_states_ is never shrunk);
+ * otherwise it is zeroed.
+ */
+int fvgs_init_gaussians(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int sample_px,
+                        float init_scale, float init_opacity, uint32_t* n_gaussians);
+int fvgs_densify(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int sample_px, float* mask,
+                 uint32_t* n_added);
+
+/*
  * Allocation-free pose Jacobian for callers that cannot call cudaMalloc -- a
  * tracking thread inside a host application whose own allocator owns the GPU
  * memory budget, or a real-time loop that must not pay cudaMalloc/cudaFree's

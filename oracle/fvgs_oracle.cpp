@@ -1315,4 +1315,246 @@ int oracle_prune_states(const float* scales, const float* opac, int n, float alp
     return marked;
 }
 
+
+/*
+ * Seeding Gaussians from an RGB-D frame: GSSlam::initializeGaussiansFromRgbd
+ * (src/GSSlam.cu:271-407) with computeNormalsFromDepth_kernel and
+ * initGaussiansFromRgbd_kernel (src/GSCudaKernels.cu:87-315), and
+ * GSSlam::densify (src/GSSlam.cu:1351-1465) with computeDensityMask_kernel and
+ * densifyGaussians_kernel (src/GSCudaKernels.cu:1741-2066).
+ *
+ * FP32 in the reference's operation order (-ffp-contract=off): every product,
+ * sum, quotient and square root rounded once, as the CUDA kernels do with
+ * explicit intrinsics, so the seeds are bit-identical.  The quaternion helpers
+ * of src/GSCudaKernels.cu:20-84 read and write float4 as (w, x, y, z): the
+ * camera orientation is taken raw in that order and the seeds' orientations
+ * are written in it.  The colour image is 8-bit, 3 bytes per pixel in the
+ * reference's (b, g, r) order.  The reference hands out seed slots with an
+ * atomic counter (unspecified order); here seeds are written in row-major
+ * order of their sample cell, the first ones up to the capacity.
+ */
+struct V3 {
+    float x, y, z;
+};
+static V3 v3_cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+static float v3_norm(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+// rotateByQuaternion: q = (w, x, y, z) raw, t = 2 (qv x v), v + w t + qv x t
+static V3 quat_rotate(const float* q, V3 v) {
+    const V3 qv = {q[1], q[2], q[3]};
+    const V3 c = v3_cross(qv, v);
+    const V3 t = {2.0f * c.x, 2.0f * c.y, 2.0f * c.z};
+    const V3 c2 = v3_cross(qv, t);
+    return {v.x + q[0] * t.x + c2.x, v.y + q[0] * t.y + c2.y, v.z + q[0] * t.z + c2.z};
+}
+static void quat_mul(const float* a, const float* b, float* out) {
+    const float aw = a[0], ax = a[1], ay = a[2], az = a[3];
+    const float bw = b[0], bx = b[1], by = b[2], bz = b[3];
+    out[0] = aw * bw - ax * bx - ay * by - az * bz;
+    out[1] = aw * bx + ax * bw + ay * bz - az * by;
+    out[2] = aw * by - ax * bz + ay * bw + az * bx;
+    out[3] = aw * bz + ax * by - ay * bx + az * bw;
+}
+static V3 v3_normalize8(V3 v) {
+    const float n = v3_norm(v);
+    if (n > 1e-8f) {
+        const float inv = 1.0f / n;
+        return {v.x * inv, v.y * inv, v.z * inv};
+    }
+    return {0.0f, 0.0f, 0.0f};
+}
+static void quat_from_two(V3 from, V3 to, float* q) {
+    const V3 u = v3_normalize8(from), v = v3_normalize8(to);
+    const float dot = u.x * v.x + u.y * v.y + u.z * v.z;
+    if (dot < -0.999999f) {
+        const V3 axis = (std::fabs(u.x) < 0.1f) ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
+        const V3 o = v3_normalize8(v3_cross(u, axis));
+        q[0] = 0.0f, q[1] = o.x, q[2] = o.y, q[3] = o.z;
+        return;
+    }
+    const V3 c = v3_cross(u, v);
+    float r[4] = {1.0f + dot, c.x, c.y, c.z};
+    const float n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+    if (n > 1e-8f) {
+        const float inv = 1.0f / n;
+        for (int k = 0; k < 4; ++k) r[k] *= inv;
+    } else {
+        r[0] = 1.0f, r[1] = r[2] = r[3] = 0.0f;
+    }
+    for (int k = 0; k < 4; ++k) q[k] = r[k];
+}
+// computeNormalsFromDepth_kernel for pixel (u, v)
+static V3 depth_normal(const float* depth, int W, int H, int u, int v) {
+    V3 n = {0.0f, 0.0f, 1.0f};
+    if (u > 0 && u < W - 1 && v > 0 && v < H - 1) {
+        const float zc = depth[(size_t)v * W + u], zl = depth[(size_t)v * W + u - 1], zr = depth[(size_t)v * W + u + 1];
+        const float zu = depth[(size_t)(v - 1) * W + u], zd = depth[(size_t)(v + 1) * W + u];
+        if (zc > 0.01f && zl > 0.01f && zr > 0.01f && zu > 0.01f && zd > 0.01f) {
+            const float dzx = (zr - zl) / 2.0f, dzy = (zd - zu) / 2.0f;
+            n = v3_cross(V3{1.0f, 0.0f, dzx}, V3{0.0f, 1.0f, dzy});
+            const float nn = v3_norm(n);
+            if (nn > 1e-6f) n = {n.x / nn, n.y / nn, n.z / nn};
+            if (n.z < 0.0f) n = {-n.x, -n.y, -n.z};
+        }
+    }
+    return n;
+}
+
+/*
+ * mode 0 (init): one seed per sample pixel (sx * sample, sy * sample) with
+ * depth z > 0 (finite): position t + R (((u - cx) z / fx, (v - cy) z / fy, z)),
+ * scale init_scale, orientation turning +z onto the normal (camera normal
+ * from the depth map, rotated to the world), colour (r, g, b) / 255, opacity
+ * init_opacity.
+ * mode 1 (densify): with sample > 1, one seed per sample cell holding at
+ * least sample^2 / 2 pixels with mask > 0 and depth > 0 (mean pixel, depth
+ * and colour; scale (s, s, 0.1 s), s = z sample / f; orientation the camera
+ * orientation; opacity 1); with sample = 1, one seed per such pixel (s with a
+ * factor 0.8).  mask: W x H floats.
+ * Writes at most max_out seeds; returns how many were written.
+ */
+int oracle_seed(int mode, const uint8_t* bgr, const float* depth, const float* mask, int W, int H, int sample,
+                const fvgs_intrinsics* K, const float* pose_t, const float* pose_q, float init_scale,
+                float init_opacity, int max_out, float* pos, float* scl, float* rot, float* col, float* opa) {
+    const int sw = (W + sample - 1) / sample, sh = (H + sample - 1) / sample;
+    const float fx = K->fx, fy = K->fy, cx = K->cx, cy = K->cy;
+    int count = 0;
+    auto emit = [&](V3 pw, V3 sc, const float* q, V3 c, float o) {
+        if (count >= max_out) return;
+        const size_t i = (size_t)count++;
+        pos[3 * i] = pw.x, pos[3 * i + 1] = pw.y, pos[3 * i + 2] = pw.z;
+        scl[3 * i] = sc.x, scl[3 * i + 1] = sc.y, scl[3 * i + 2] = sc.z;
+        for (int k = 0; k < 4; ++k) rot[4 * i + k] = q[k];
+        col[3 * i] = c.x, col[3 * i + 1] = c.y, col[3 * i + 2] = c.z;
+        opa[i] = o;
+    };
+    auto to_world = [&](V3 pc) {
+        const V3 r = quat_rotate(pose_q, pc);
+        return V3{pose_t[0] + r.x, pose_t[1] + r.y, pose_t[2] + r.z};
+    };
+    auto rgb_at = [&](int u, int v) {
+        const uint8_t* p = bgr + ((size_t)v * W + u) * 3;
+        return V3{(float)p[2] / 255.0f, (float)p[1] / 255.0f, (float)p[0] / 255.0f};
+    };
+    const V3 zaxis = {0.0f, 0.0f, 1.0f};
+    if (mode == 0) {
+        for (int sy = 0; sy < sh; ++sy)
+            for (int sx = 0; sx < sw; ++sx) {
+                const int u = sx * sample, v = sy * sample;
+                const float z = depth[(size_t)v * W + u];
+                if (!(z > 0.0f) || std::isinf(z) || std::isnan(z)) continue;
+                V3 n = depth_normal(depth, W, H, u, v);
+                const float nl = v3_norm(n);
+                if (nl < 1e-6f) n = zaxis;
+                else n = {n.x / nl, n.y / nl, n.z / nl};
+                const V3 pc = {((float)u - cx) * z / fx, ((float)v - cy) * z / fy, z};
+                V3 nw = quat_rotate(pose_q, n);
+                const float nwl = v3_norm(nw);
+                if (nwl > 1e-6f) nw = {nw.x / nwl, nw.y / nwl, nw.z / nwl};
+                const V3 axis0 = v3_cross(zaxis, nw);
+                const float al = v3_norm(axis0);
+                const float ac = zaxis.x * nw.x + zaxis.y * nw.y + zaxis.z * nw.z;
+                float q[4];
+                if (al < 1e-6f) {
+                    if (ac > 0.0f) q[0] = 1.0f, q[1] = 0.0f, q[2] = 0.0f, q[3] = 0.0f;
+                    else q[0] = 0.0f, q[1] = 1.0f, q[2] = 0.0f, q[3] = 0.0f;
+                } else {
+                    const V3 ax = {axis0.x / al, axis0.y / al, axis0.z / al};
+                    const float hs = std::sqrt(std::fmax(0.0f, (1.0f - ac) / 2.0f));
+                    const float hc = std::sqrt(std::fmax(0.0f, (1.0f + ac) / 2.0f));
+                    q[0] = hc, q[1] = hs * ax.x, q[2] = hs * ax.y, q[3] = hs * ax.z;
+                }
+                emit(to_world(pc), V3{init_scale, init_scale, init_scale}, q, rgb_at(u, v), init_opacity);
+            }
+        return count;
+    }
+    float q_cam[4];
+    quat_from_two(zaxis, zaxis, q_cam);  // normal (0, 0, 1): the reference passes no normal map
+    float q[4];
+    quat_mul(pose_q, q_cam, q);
+    if (sample > 1) {
+        for (int sy = 0; sy < sh; ++sy)
+            for (int sx = 0; sx < sw; ++sx) {
+                const int u0 = sx * sample, v0 = sy * sample;
+                V3 ip = {0.0f, 0.0f, 0.0f}, ca = {0.0f, 0.0f, 0.0f};
+                int n = 0;
+                for (int u = u0; u < u0 + sample && u < W; ++u)
+                    for (int v = v0; v < v0 + sample && v < H; ++v) {
+                        if (!(mask[(size_t)v * W + u] > 0.0f)) continue;
+                        const float d = depth[(size_t)v * W + u];
+                        if (!(d > 0.0f)) continue;
+                        const V3 c = rgb_at(u, v);
+                        ip = {ip.x + (float)u, ip.y + (float)v, ip.z + d};
+                        ca = {ca.x + c.x, ca.y + c.y, ca.z + c.z};
+                        ++n;
+                    }
+                if ((uint32_t)n < (((uint32_t)sample * (uint32_t)sample) >> 1)) continue;
+                const float inv_n = 1.0f / (float)n;
+                ip = {ip.x * inv_n, ip.y * inv_n, ip.z * inv_n};
+                ca = {ca.x * inv_n, ca.y * inv_n, ca.z * inv_n};
+                const V3 pc = {ip.z * (ip.x - cx) / fx, ip.z * (ip.y - cy) / fy, ip.z};
+                const float sx_ = ip.z * (float)sample / fx, sy_ = ip.z * (float)sample / fy;
+                const float s2 = 0.5f * (sx_ + sy_);
+                emit(to_world(pc), V3{s2, s2, 0.1f * s2}, q, ca, 1.0f);
+            }
+        return count;
+    }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            if (!(mask[(size_t)y * W + x] > 0.0f)) continue;
+            const float d = depth[(size_t)y * W + x];
+            if (!(d > 0.0f)) continue;
+            const V3 pc = {d * ((float)x - cx) / fx, d * ((float)y - cy) / fy, d};
+            const float sx_ = 0.8f * d * (float)sample / fx, sy_ = 0.8f * d * (float)sample / fy;
+            const float s2 = 0.5f * (sx_ + sy_);
+            emit(to_world(pc), V3{s2, s2, 0.1f * s2}, q, rgb_at(x, y), 1.0f);
+        }
+    return count;
+}
+
+/*
+ * computeDensityMask_kernel (src/GSCudaKernels.cu:1741-1857) over a binned
+ * view, FP64: every pixel with observed depth >= 0.5 walks its tile list
+ * (d = mean - pixel, q = c.x dx^2 + 2 c.y dx dy + c.z dy^2, alpha =
+ * min(0.99, opacity exp(-q/2)), alpha < 1/255 skipped, P *= 1 - alpha, the
+ * depth z + phat . d where P first falls below 0.5, stop once P < 1e-4).
+ * mask = P where depth > 0.5 and P > 0.5; 1 where depth > 0.5, P <= 0.5 and
+ * the rendered depth exceeds the observed one by more than 0.2 x observed;
+ * else 0.
+ */
+int oracle_density_mask(const float* rec, const uint32_t* ranges, const uint32_t* indices, int n_gauss,
+                        const float* obs_depth, int W, int H, int tw, int th, double* mask) {
+    const int ntx = (W + tw - 1) / tw;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const int tile = (y / th) * ntx + (x / tw);
+            const uint32_t r0 = ranges[2 * (size_t)tile], r1 = ranges[2 * (size_t)tile + 1];
+            const double d_obs = obs_depth[(size_t)y * W + x];
+            double P = 1.0, T = 1.0, dr = 0.0;
+            if (!(d_obs < 0.5)) {
+                for (uint32_t k = r0; k < r1; ++k) {
+                    const uint32_t g = indices[k];
+                    if ((int)g >= n_gauss) continue;
+                    const float* r = rec + 12 * (size_t)g;
+                    const double dx = (double)r[0] - x, dy = (double)r[1] - y;
+                    const double q = r[4] * dx * dx + 2.0 * r[5] * dx * dy + r[6] * dy * dy;
+                    const double alpha = std::min(0.99, (double)r[3] * std::exp(-0.5 * q));
+                    if (alpha < 1.0 / 255.0) continue;
+                    P *= 1.0 - alpha;
+                    if (T > 0.5 && P < 0.5) {
+                        T = P;
+                        dr = (double)r[2] + (double)r[7] * dx + (double)r[8] * dy;
+                    }
+                    if (P < 0.0001) break;
+                }
+            }
+            double val = 0.0;
+            if (d_obs > 0.5) {
+                if (P > 0.5) val = P;
+                else if (d_obs < dr && dr - d_obs > 0.2 * d_obs) val = 1.0;
+            }
+            mask[(size_t)y * W + x] = val;
+        }
+    return 0;
+}
+
 }  // extern "C"

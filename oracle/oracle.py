@@ -450,3 +450,36 @@ def covisibility(vis_a, vis_b):
     b = np.asarray(vis_b) != 0
     inter, uni = int(np.sum(a & b)), int(np.sum(a | b))
     return inter, uni, (np.float32(inter) / np.float32(uni)) if uni else np.float32(0.0)
+
+
+def seed(mode: str, bgr, depth, K, pose_t, pose_q_raw, sample: int, init_scale=2.0, init_opacity=0.8, mask=None,
+         max_out: int | None = None):
+    """initGaussiansFromRgbd_kernel (mode 'init') or densifyGaussians_kernel
+    (mode 'densify', with a W x H float mask) in FP32, seeds in row-major order
+    of their sample cell: (positions, scales, orientations raw (w,x,y,z),
+    colors, opacities)."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    H, W = bgr.shape[:2]
+    dep = _f32(depth)
+    msk = _f32(mask) if mask is not None else np.zeros((H, W), np.float32)
+    cap = W * H if max_out is None else max_out
+    pos = np.zeros((max(cap, 1), 3), np.float32)
+    scl = np.zeros((max(cap, 1), 3), np.float32)
+    rot = np.zeros((max(cap, 1), 4), np.float32)
+    col = np.zeros((max(cap, 1), 3), np.float32)
+    opa = np.zeros(max(cap, 1), np.float32)
+    t = _f32(pose_t)
+    q = _f32(pose_q_raw)
+    n = lib().oracle_seed(C.c_int(0 if mode == "init" else 1), _p(bgr), _p(dep), _p(msk), C.c_int(W), C.c_int(H),
+                          C.c_int(sample), C.byref(make_intr(K)), _p(t), _p(q), C.c_float(init_scale),
+                          C.c_float(init_opacity), C.c_int(cap), _p(pos), _p(scl), _p(rot), _p(col), _p(opa))
+    return pos[:n], scl[:n], rot[:n], col[:n], opa[:n]
+
+
+def density_mask(b: Binning, obs_depth, W, H, params: Params):
+    """computeDensityMask_kernel in FP64: (H, W) mask."""
+    n = b.rec.shape[0]
+    m = np.zeros((H, W), np.float64)
+    lib().oracle_density_mask(_p(b.rec), _p(b.ranges), _p(b.vals), C.c_int(n), _p(_f32(obs_depth)), C.c_int(W),
+                              C.c_int(H), C.c_int(params.tile_w), C.c_int(params.tile_h), _p(m))
+    return m

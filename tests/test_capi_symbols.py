@@ -22,7 +22,7 @@ def test_header_declares_entry_points():
     names = declared_symbols()
     for must in ("fvgs_session_create", "fvgs_project_bin", "fvgs_track_jacobian", "fvgs_track_frame",
                  "fvgs_map_step", "fvgs_render", "fvgs_rgbd_pose_jacobians_noalloc", "fvgs_remove_outliers",
-                 "fvgs_prune", "fvgs_covisibility", "fvgs_visibility"):
+                 "fvgs_prune", "fvgs_covisibility", "fvgs_visibility", "fvgs_init_gaussians", "fvgs_densify"):
         assert must in names
 
 
