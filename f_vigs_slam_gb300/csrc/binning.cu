@@ -56,8 +56,13 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
                 u = uu;
                 v = vv;
                 z = pcz;
-                const float4 s = a.scale[i];
-                const float4 qg4 = a.rot[i];
+                float4 s, qg4;
+                if (a.attr_sr) {
+                    unpack_sr(a.attr_sr[i], s, qg4);
+                } else {
+                    s = a.scale[i];
+                    qg4 = a.rot[i];
+                }
                 const float qg[4] = {qg4.x, qg4.y, qg4.z, qg4.w};
                 float Rg[3][3];
                 quat_to_R(qg, Rg);
@@ -148,7 +153,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
     // culled Gaussians blend (with the zero record), and the host reports
     // zeros for them.
     if (count && (visible || (a.quirks & FVGS_Q_CULLED_SLOTS))) {
-        const float4 co = a.col[i];
+        const float4 co = a.attr_c ? unpack_c(a.attr_c[i]) : a.col[i];
         const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
         a.rec0[i] = make_float4(u, v, z, co.w);
         a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);

@@ -187,6 +187,13 @@ struct fvgs_session {
     uint32_t *sd_block_keep = nullptr, *sd_block_base = nullptr;  // seeding: per block of sample cells
     size_t sd_blocks = 0;
 
+    // precision form: reduced-precision copies of scale/rotation and
+    // colour/opacity that the projection reads; the float4 planes stay the
+    // master copy (mapping updates both)
+    int precision = FVGS_PRECISION_FP32;
+    uint4* attr_sr = nullptr;
+    uint2* attr_c = nullptr;
+
     // kernel accounting: launches per class (always), event timing (opt-in)
     uint32_t timing_mask = 0;
     uint64_t launches[FVGS_K_COUNT] = {};
@@ -286,6 +293,14 @@ void dev_free(fvgs_session* s, T*& p, size_t count) {
         int r_ = (expr);        \
         if (r_ != FVGS_OK) return r_; \
     } while (0)
+
+// Bring the reduced-precision planes up to date with the master planes after
+// a host-side map change (upload, removal, seeding).
+int refresh_reduced(fvgs_session* s) {
+    if (s->precision != FVGS_PRECISION_REDUCED || s->n_g == 0) return FVGS_OK;
+    FV_CK(launch_pack_reduced(s->scale, s->rot, s->col, s->n_g, s->attr_sr, s->attr_c, s->stream));
+    return FVGS_OK;
+}
 
 int alloc_instances(fvgs_session* s, uint64_t cap) {
     s->hist_ok = false;
@@ -405,6 +420,10 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     pa.scale = s->scale;
     pa.rot = s->rot;
     pa.col = s->col;
+    if (s->precision == FVGS_PRECISION_REDUCED) {
+        pa.attr_sr = s->attr_sr;
+        pa.attr_c = s->attr_c;
+    }
     pa.n = (int)s->n_g;
     pa.pose = s->pose;
     pa.K = *K;
@@ -689,6 +708,10 @@ int enqueue_map(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, 
     ua.beta2 = P.adam_beta2;
     ua.eps = P.adam_eps;
     ua.dbg_delta3d = (s->debug & FVGS_DEBUG_MAPPING) ? s->dbg_delta3d : nullptr;
+    if (s->precision == FVGS_PRECISION_REDUCED) {
+        ua.attr_sr = s->attr_sr;
+        ua.attr_c = s->attr_c;
+    }
     {
         KScope k(s, FVGS_K_MAP_UPDATE, 1);
         FV_CK(launch_map_update(ua, s->st, s->stream));
@@ -890,6 +913,21 @@ int fvgs_session_set_debug(fvgs_session* s, uint32_t flags) {
     return FVGS_OK;
 }
 
+int fvgs_session_set_precision(fvgs_session* s, int precision) {
+    if (!s || (precision != FVGS_PRECISION_FP32 && precision != FVGS_PRECISION_REDUCED)) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    if (precision == s->precision) return FVGS_OK;
+    if (precision == FVGS_PRECISION_REDUCED && !s->attr_sr) {
+        FV_TRY(dev_alloc(s, &s->attr_sr, s->cap_g));
+        FV_TRY(dev_alloc(s, &s->attr_c, s->cap_g));
+    }
+    s->precision = precision;
+    ++s->gen;  // captured frame graphs read the other planes
+    FV_TRY(refresh_reduced(s));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    return FVGS_OK;
+}
+
 int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
                               uint32_t* n_changed) {
     if (!s) return FVGS_E_INVALID;
@@ -933,6 +971,7 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     FV_CK(cudaGetLastError());
     // fresh map: Adam moments and step counters start at zero
     FV_CK(cudaMemsetAsync(s->adam, 0, sizeof(float4) * 9 * (size_t)s->cap_g, s->stream));
+    FV_TRY(refresh_reduced(s));
     FV_CK(cudaStreamSynchronize(s->stream));
     return FVGS_OK;
 }
@@ -1709,10 +1748,10 @@ int enqueue_mark_compact(fvgs_session* s, MarkMode mode, const MarkArgs& proto, 
 }
 
 // After the stream is synchronised: adopt the compacted planes.
-void finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
+int finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
     const uint32_t removed = s->h_mk_ctr[1];
     if (n_marked) *n_marked = removed;
-    if (!remove || removed == 0) return;
+    if (!remove || removed == 0) return FVGS_OK;
     std::swap(s->pos, s->pos_alt);
     std::swap(s->scale, s->scale_alt);
     std::swap(s->rot, s->rot_alt);
@@ -1725,6 +1764,7 @@ void finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
     s->keys_valid = false;
     s->dbg_proj_valid = false;
     ++s->gen;  // captured frame graphs hold the old plane addresses
+    return refresh_reduced(s);
 }
 
 }  // namespace
@@ -1831,8 +1871,7 @@ int fvgs_remove_outliers(fvgs_session* s, const fvgs_pose* pose, const fvgs_intr
         FV_TRY(check_status(s, &retry));
         if (retry) continue;  // the planes were only read: repeat from the start
         s->mk_scores = true;
-        finish_compact(s, remove != 0, n_marked);
-        return FVGS_OK;
+        return finish_compact(s, remove != 0, n_marked);
     }
     return FVGS_E_CAPACITY;
 }
@@ -1854,8 +1893,7 @@ int fvgs_prune(fvgs_session* s, float alpha_threshold, float scale_ratio_thresho
     FV_CK(cudaStreamSynchronize(s->stream));
     collect_timing(s);
     s->mk_scores = false;
-    finish_compact(s, remove != 0, n_marked);
-    return FVGS_OK;
+    return finish_compact(s, remove != 0, n_marked);
 }
 
 int fvgs_download_marks(fvgs_session* s, uint8_t* states, float* total_alpha, float* outlier_prob, uint32_t n) {
@@ -1923,13 +1961,14 @@ int enqueue_seed(fvgs_session* s, SeedMode mode, const SeedArgs& a) {
     return FVGS_OK;
 }
 
-void map_grew(fvgs_session* s, uint32_t n) {
+int map_grew(fvgs_session* s, uint32_t n) {
     s->n_g = n;
     s->has_binning = s->has_track = s->has_map = false;
     s->hist_ok = false;  // the new Gaussians have no previous binning
     s->keys_valid = false;
     s->dbg_proj_valid = false;
     ++s->gen;
+    return refresh_reduced(s);
 }
 
 }  // namespace
@@ -1948,7 +1987,7 @@ int fvgs_init_gaussians(fvgs_session* s, const fvgs_pose* pose, const fvgs_intri
     FV_TRY(enqueue_seed(s, kSeedInit, a));
     FV_CK(cudaStreamSynchronize(s->stream));
     collect_timing(s);
-    map_grew(s, std::min<uint32_t>(s->h_mk_ctr[0], s->cap_g));
+    FV_TRY(map_grew(s, std::min<uint32_t>(s->h_mk_ctr[0], s->cap_g)));
     if (n_gaussians) *n_gaussians = s->n_g;
     return FVGS_OK;
 }
@@ -2001,7 +2040,7 @@ int fvgs_densify(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* 
         const uint64_t total = (uint64_t)s->n_g + s->h_mk_ctr[0];
         const uint32_t n_new = (uint32_t)std::min<uint64_t>(total, s->cap_g);
         if (n_added) *n_added = n_new - s->n_g;
-        if (n_new != s->n_g) map_grew(s, n_new);
+        if (n_new != s->n_g) FV_TRY(map_grew(s, n_new));
         return FVGS_OK;
     }
     return FVGS_E_CAPACITY;

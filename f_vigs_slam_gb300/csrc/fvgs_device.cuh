@@ -11,13 +11,19 @@
 //     rec0 = (u, v, z, opacity)
 //     rec1 = (c.x, c.y, c.z, phat.x)      c = inverse 2D covariance in the order
 //     rec2 = (phat.y, r, g, b)             the blending kernels consume it
-//   Binning record, 32 B per Gaussian: (rect x0|y0<<16, x1|y1<<16, count, -,
-//     u, v, z, phat.x) and phat.y kept in rec2.x.
+//   Reduced-precision attributes (precision form; the float4 planes stay the
+//   master copy that mapping updates):
+//     g_sr[N]    uint4 scale bf16 x3, rotation bf16 x4 (raw order), 2 B spare
+//     g_c[N]     uint2 colour and opacity fp16 x4
+//   Binning record, 32 B per Gaussian: (rect x0|y0<<16, x1|y1<<16, count,
+//     phat.y bits, u, v, z, phat.x).
 //   Instances: u64 key = tile << 32 | float bits of the tile-centre depth,
 //     u32 value = Gaussian index; two ping-pong buffers for the radix sort.
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/fvgs_types.h"
@@ -181,6 +187,26 @@ __device__ __forceinline__ float reject_bound(float o) {
     if (!(o > 0.0f)) return -INFINITY;
     const float b = 2.0f * logf(255.0f * o);
     return b + 1e-3f + 1e-4f * fabsf(b);
+}
+
+// Reduced-precision attribute words (round to nearest even).
+__device__ __forceinline__ uint32_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_val(uint32_t b) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)b)); }
+__device__ __forceinline__ uint32_t f16_bits(float x) { return __half_as_ushort(__float2half_rn(x)); }
+__device__ __forceinline__ float f16_val(uint32_t b) { return __half2float(__ushort_as_half((unsigned short)b)); }
+__device__ __forceinline__ uint4 pack_sr(float4 s, float4 q) {
+    return make_uint4(bf16_bits(s.x) | (bf16_bits(s.y) << 16), bf16_bits(s.z) | (bf16_bits(q.x) << 16),
+                      bf16_bits(q.y) | (bf16_bits(q.z) << 16), bf16_bits(q.w));
+}
+__device__ __forceinline__ uint2 pack_c(float4 c) {
+    return make_uint2(f16_bits(c.x) | (f16_bits(c.y) << 16), f16_bits(c.z) | (f16_bits(c.w) << 16));
+}
+__device__ __forceinline__ void unpack_sr(uint4 w, float4& s, float4& q) {
+    s = make_float4(bf16_val(w.x & 0xffffu), bf16_val(w.x >> 16), bf16_val(w.y & 0xffffu), 0.f);
+    q = make_float4(bf16_val(w.y >> 16), bf16_val(w.z & 0xffffu), bf16_val(w.z >> 16), bf16_val(w.w & 0xffffu));
+}
+__device__ __forceinline__ float4 unpack_c(uint2 w) {
+    return make_float4(f16_val(w.x & 0xffffu), f16_val(w.x >> 16), f16_val(w.y & 0xffffu), f16_val(w.y >> 16));
 }
 
 // Bounded spin budget for device-side waits; on expiry a kernel records

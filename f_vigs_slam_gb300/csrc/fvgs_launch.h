@@ -46,6 +46,10 @@ struct ProjectArgs {
     const float4* scale;
     const float4* rot;
     const float4* col;
+    // precision form: scale/rotation and colour/opacity from the reduced
+    // planes instead of scale, rot, col (null: the FP32 planes)
+    const uint4* attr_sr;
+    const uint2* attr_c;
     int n;
     const DevPose* pose;
     fvgs_intrinsics K;
@@ -273,12 +277,17 @@ struct MapUpdateArgs {
     fvgs_intrinsics K;
     float lambda_iso, eta, beta1, beta2, eps;
     float* dbg_delta3d;  // optional [N][16]
+    uint4* attr_sr;      // optional: refresh the reduced-precision planes of updated Gaussians
+    uint2* attr_c;
 };
 cudaError_t launch_map_forward(const MapArgs& a, bool cap, cudaStream_t s);
 cudaError_t launch_map_backward(const MapArgs& a, bool cap, cudaStream_t s);
 cudaError_t launch_bucket_scan(const uint2* ranges, int T, uint32_t* bucket_base, uint32_t* total, cudaStream_t s);
 cudaError_t launch_map_update(const MapUpdateArgs& a, const DevStatus* st, cudaStream_t s);
 int map_cap_buckets();
+// Reduced-precision planes from the FP32 master planes (precision form).
+cudaError_t launch_pack_reduced(const float4* scale, const float4* rot, const float4* col, uint32_t n, uint4* sr,
+                                uint2* c, cudaStream_t s);
 
 // ---- map maintenance (maintenance.cu) ----
 struct VisArgs {

@@ -550,6 +550,10 @@ __global__ void __launch_bounds__(256) map_update_kernel(MapUpdateArgs a, const 
     a.scale[i] = ns;
     a.rot[i] = nr;
     a.col[i] = cw;
+    if (a.attr_sr) {
+        a.attr_sr[i] = pack_sr(ns, nr);
+        a.attr_c[i] = pack_c(cw);
+    }
     S[0 * NN + i] = mp;
     S[1 * NN + i] = vp;
     S[2 * NN + i] = ms;
@@ -624,5 +628,21 @@ cudaError_t launch_map_update(const MapUpdateArgs& a, const DevStatus* st, cudaS
 }
 
 int map_cap_buckets() { return kCapBuckets; }
+
+__global__ void pack_reduced_kernel(const float4* __restrict__ scale, const float4* __restrict__ rot,
+                                    const float4* __restrict__ col, uint32_t n, uint4* __restrict__ sr,
+                                    uint2* __restrict__ c) {
+    pdl_begin();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sr[i] = pack_sr(scale[i], rot[i]);
+    c[i] = pack_c(col[i]);
+}
+
+cudaError_t launch_pack_reduced(const float4* scale, const float4* rot, const float4* col, uint32_t n, uint4* sr,
+                                uint2* c, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    return launch_chained(pack_reduced_kernel, dim3((n + 255) / 256), dim3(256), 0, s, scale, rot, col, n, sr, c);
+}
 
 }  // namespace fvgs

@@ -28,6 +28,9 @@ Q_VIS_CAP256 = 0x10
 Q_ADAM_STAY = 0x20
 QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY
 
+PRECISION_FP32 = 0
+PRECISION_REDUCED = 1
+
 DEBUG_PROJECTION = 0x1
 DEBUG_IMAGES = 0x2
 DEBUG_MAPPING = 0x4
@@ -174,6 +177,10 @@ class Session:
                "fvgs_session_get_timing")
         return {c: dict(ms=float(ms[i]), launches=int(launches[i]), timed=int(timed[i]))
                 for i, c in enumerate(KERNEL_CLASSES)}
+
+    def set_precision(self, precision: int):
+        """Precision form (fvgs_session_set_precision): PRECISION_FP32 or PRECISION_REDUCED."""
+        _check(self.lib.fvgs_session_set_precision(self.h, C.c_int(precision)), "fvgs_session_set_precision")
 
     def footprint(self) -> int:
         b = C.c_uint64()

@@ -181,3 +181,27 @@ def add_noise(rgb, depth, rng, color_sigma=0.01, depth_sigma=0.005):
     rgb_n = (rgb + rng.normal(0.0, color_sigma, size=rgb.shape)).astype(np.float32)
     depth_n = (depth + rng.normal(0.0, depth_sigma, size=depth.shape)).astype(np.float32)
     return rgb_n, depth_n
+
+
+def round_bf16(a):
+    """FP32 -> BF16 -> FP32, round to nearest even (the rounding of
+    __float2bfloat16_rn): keep the top 16 bits after adding 0x7fff plus the
+    lowest kept bit; NaN stays NaN."""
+    x = np.ascontiguousarray(a, np.float32)
+    b = x.view(np.uint32).astype(np.uint64)
+    r = (((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16).astype(np.uint32)
+    out = r.view(np.float32).copy()
+    out[np.isnan(x)] = np.nan
+    return out
+
+
+def round_f16(a):
+    """FP32 -> FP16 -> FP32, round to nearest even."""
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
+
+
+def reduced(scene: Scene) -> Scene:
+    """The attributes the precision form stores: means FP32, scales and
+    rotations BF16, colours and opacities FP16."""
+    return Scene(np.asarray(scene.positions, np.float32).copy(), round_bf16(scene.scales),
+                 round_bf16(scene.orientations), round_f16(scene.colors), round_f16(scene.opacities))

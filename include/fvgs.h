@@ -83,6 +83,21 @@ int fvgs_session_get_timing(fvgs_session* s, double* ms, uint64_t* launches, uin
 int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes);
 
 /*
+ * Precision form.  FVGS_PRECISION_REDUCED stores the attributes the binning
+ * reads in reduced precision -- scale and rotation in BF16, colour and
+ * opacity in FP16, round to nearest even; means stay FP32 -- so a Gaussian
+ * in view costs the projection 40 instead of 64 bytes.  Blending and the
+ * Hessian accumulation stay FP32 (compensated), the 6x6 solve FP64.  The FP32
+ * planes remain the master copy: mapping's Adam update works on them and
+ * refreshes the reduced copy of every Gaussian it changes; uploads, removals
+ * and seeding refresh it too.  Results are those of the FP32 path on the
+ * rounded attributes.  No reference counterpart (the reference stores FP32).
+ */
+#define FVGS_PRECISION_FP32 0
+#define FVGS_PRECISION_REDUCED 1
+int fvgs_session_set_precision(fvgs_session* s, int precision);
+
+/*
  * Gaussians in the reference's SoA layout (Gaussians,
  * include/f_vigs_slam/RepresentationClasses.hpp:53-99): positions[3n],
  * scales[3n], orientations[4n] as (x,y,z,w), colors[3n], opacities[n].
