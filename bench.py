@@ -55,6 +55,7 @@ SERVE_SECONDS = 2.0      # Poisson arrival window of the latency run
 SERVE_FRAMES = 2         # distinct frames per session
 SERVE_BUDGET = 150 * 10**9
 MAP_EVERY = 10
+PREC_N = 2_000_000       # precision-form workload: N = 2 M room, 1280x720
 
 
 def parse():
@@ -68,6 +69,7 @@ def parse():
     ap.add_argument("--sessions", type=int, default=32)
     ap.add_argument("--plain-only", action="store_true",
                     help="only the large plain workload (for profiling runs; not the benchmark line)")
+    ap.add_argument("--prec-n", type=int, default=PREC_N, help="Gaussians of the precision-form workload")
     return ap.parse_args()
 
 
@@ -471,6 +473,51 @@ def cpu_outlier_sample(sess, pose, K, W, H, depth, band_rows=64):
             "sample": "%d rows of %d, %.2f s, scaled by rows" % (band_rows, H, t)}
 
 
+def run_precision(args, fvgs, S, torch, dev, stream, world):
+    """The precision form on an N = 2 M room at 1280x720: the same tracking
+    frames (20 GN iterations, map fixed) with FP32 attributes and with BF16
+    scale/rotation + FP16 colour/opacity; frames/s of both, the pose
+    difference between them and each one's error to the true pose."""
+    n = args.prec_n
+    scene = S.room(n, seed=3)
+    sess = fvgs.Session(n, 1280, 720, device=dev.index or 0)
+    sess.set_stream(stream.cuda_stream)
+    sess.upload(scene)
+    W, H, K, frames = make_workload(sess, args.warmup + args.steps, seed=29)
+    dframes = [{k: torch.from_numpy(np.ascontiguousarray(f[k])).to(dev) for k in ("rgb", "depth", "gx", "gy")}
+               for f in frames]
+    torch.cuda.synchronize()
+    out, poses = {}, {}
+    for name, prec in (("fp32", fvgs.PRECISION_FP32), ("reduced", fvgs.PRECISION_REDUCED)):
+        sess.set_precision(prec)
+
+        def step(k):
+            set_frame_tensors(fvgs, sess, 0, dframes[k], W, H)
+            return sess.track_frame(frames[k]["prev"], K, iterations=ITERS)[0]
+
+        for k in range(args.warmup):
+            step(k)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        got = [step(args.warmup + i) for i in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max_over_ranks([e0.elapsed_time(e1)], dev, world)[0]
+        poses[name] = got
+        errs = [S.pose_error(p, frames[args.warmup + i]["pose"]) for i, p in enumerate(got)]
+        out[name] = {"frames_per_s": replica_throughput(args.steps, world, ms), "ms_per_frame": ms / args.steps,
+                     "pose_error_median": {"rad": float(np.median([e[0] for e in errs])),
+                                           "m": float(np.median([e[1] for e in errs]))},
+                     "footprint_gb": sess.footprint() / 1e9}
+    d = [S.pose_error(a, b) for a, b in zip(poses["reduced"], poses["fp32"])]
+    sess.close()
+    out["workload"] = "room N=%d, 1280x720, 20 GN iterations per frame, map fixed" % n
+    out["pose_difference_max"] = {"rad": float(max(e[0] for e in d)), "m": float(max(e[1] for e in d))}
+    out["speedup_reduced_over_fp32"] = out["reduced"]["frames_per_s"] / out["fp32"]["frames_per_s"]
+    return out
+
+
 def set_frame_tensors(fvgs, sess, level, fr, W, H):
     st = sess.lib.fvgs_set_frame(sess.h, level, *(fvgs.C.c_void_p(fr[k].data_ptr()) for k in ("rgb", "depth", "gx", "gy")),
                                  W, H)
@@ -692,6 +739,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": "large plain workload only (profiling run)", "large_plain": large}), flush=True)
         return 0
+    prec = run_precision(args, fvgs, S, torch, dev, stream, world)
     srv = run_serving(args, fvgs, S, torch, dev)
     srv_fps, plain_fps, e2e_fps = max_over_ranks_rate([srv["served_frames_per_s"], srv["plain_frames_per_s"],
                                                        srv["e2e_frames_per_s"]], dev, world)
@@ -735,6 +783,7 @@ def run_ours(args):
             "roofline": large["roofline"],
             "large_plain": {k: v for k, v in large.items() if k not in ("roofline", "maintenance")},
             "maintenance": large["maintenance"],
+            "precision": prec,
             "clocks": srv["clocks"],
             "cpu_baseline": cpu,
         }
