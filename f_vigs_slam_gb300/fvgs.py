@@ -577,3 +577,119 @@ class Server:
                "fvgs_server_stats")
         return dict(admitted_bytes=int(ab.value), inflight=int(inf.value), launched=int(la.value),
                     completed=int(co.value))
+
+
+# ----------------------------------------------------------------------------
+# host FP64 estimator glue (include/fvgs_estimator.h)
+# ----------------------------------------------------------------------------
+def _d(a, n=None):
+    a = np.ascontiguousarray(a, np.float64)
+    if n is not None and a.size != n:
+        raise ValueError("expected %d values, got %d" % (n, a.size))
+    return a
+
+
+def jacobian_cam_to_imu(JtJ, Jtr, q_imu_cam, t_imu_cam, q_imu):
+    """fvgs_jacobian_cam_to_imu: the IMU-frame 6x6 system (quaternions x, y, z, w)."""
+    H = np.zeros((6, 6))
+    g = np.zeros(6)
+    _check(load_library().fvgs_jacobian_cam_to_imu(_ptr(_d(JtJ, 36)), _ptr(_d(Jtr, 6)), _ptr(_d(q_imu_cam, 4)),
+                                                   _ptr(_d(t_imu_cam, 3)), _ptr(_d(q_imu, 4)), _ptr(H), _ptr(g)),
+           "fvgs_jacobian_cam_to_imu")
+    return H, g
+
+
+def pseudo_factor(JtJ, Jtr, eps=1e-4):
+    """fvgs_pseudo_factor: (r* [6], J* [6x6])."""
+    r = np.zeros(6)
+    J = np.zeros((6, 6))
+    _check(load_library().fvgs_pseudo_factor(_ptr(_d(JtJ, 36)), _ptr(_d(Jtr, 6)), C.c_double(eps), _ptr(r), _ptr(J)),
+           "fvgs_pseudo_factor")
+    return r, J
+
+
+class Preintegration:
+    """fvgs_preint_*: IMU preintegration between two keyframes."""
+
+    def __init__(self, acc0, gyr0, ba, bg, acc_n, gyr_n, acc_w, gyr_w):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.fvgs_preint_create(_ptr(_d(acc0, 3)), _ptr(_d(gyr0, 3)), _ptr(_d(ba, 3)), _ptr(_d(bg, 3)),
+                                           C.c_double(acc_n), C.c_double(gyr_n), C.c_double(acc_w),
+                                           C.c_double(gyr_w), C.byref(h)), "fvgs_preint_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.fvgs_preint_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, dt, acc, gyr):
+        _check(self.lib.fvgs_preint_add(self.h, C.c_double(dt), _ptr(_d(acc, 3)), _ptr(_d(gyr, 3))), "fvgs_preint_add")
+
+    def repropagate(self, ba, bg):
+        _check(self.lib.fvgs_preint_repropagate(self.h, _ptr(_d(ba, 3)), _ptr(_d(bg, 3))), "fvgs_preint_repropagate")
+
+    def state(self):
+        dp, dq, dv = np.zeros(3), np.zeros(4), np.zeros(3)
+        T = C.c_double()
+        jac, cov = np.zeros((15, 15)), np.zeros((15, 15))
+        _check(self.lib.fvgs_preint_state(self.h, _ptr(dp), _ptr(dq), _ptr(dv), C.byref(T), _ptr(jac), _ptr(cov)),
+               "fvgs_preint_state")
+        return dict(delta_p=dp, delta_q=dq, delta_v=dv, sum_dt=T.value, jacobian=jac, covariance=cov)
+
+    def evaluate(self, pose_i, sb_i, pose_j, sb_j):
+        r = np.zeros(15)
+        _check(self.lib.fvgs_preint_evaluate(self.h, _ptr(_d(pose_i, 7)), _ptr(_d(sb_i, 9)), _ptr(_d(pose_j, 7)),
+                                             _ptr(_d(sb_j, 9)), _ptr(r)), "fvgs_preint_evaluate")
+        return r
+
+    def predict(self, pose_i, v_i):
+        pj, vj = np.zeros(7), np.zeros(3)
+        _check(self.lib.fvgs_preint_predict(self.h, _ptr(_d(pose_i, 7)), _ptr(_d(v_i, 3)), _ptr(pj), _ptr(vj)),
+               "fvgs_preint_predict")
+        return pj, vj
+
+    def factor(self, pose_i, sb_i, pose_j, sb_j, jacobians=True):
+        """fvgs_imu_factor: whitened residual [15] and Jacobians (15x7, 15x9, 15x7, 15x9)."""
+        r = np.zeros(15)
+        J = [np.zeros((15, 7)), np.zeros((15, 9)), np.zeros((15, 7)), np.zeros((15, 9))] if jacobians else [None] * 4
+        _check(self.lib.fvgs_imu_factor(self.h, _ptr(_d(pose_i, 7)), _ptr(_d(sb_i, 9)), _ptr(_d(pose_j, 7)),
+                                        _ptr(_d(sb_j, 9)), _ptr(r), *(_ptr(j) for j in J)), "fvgs_imu_factor")
+        return (r, J) if jacobians else r
+
+
+def marginalize(A, b, m, eps=1e-8):
+    """fvgs_marginalize: prior (J [n x n], r [n]) of the kept n = dim - m dimensions."""
+    A = _d(A)
+    N = A.shape[0]
+    n = N - m
+    J, r = np.zeros((n, n)), np.zeros(n)
+    _check(load_library().fvgs_marginalize(_ptr(A), _ptr(_d(b, N)), C.c_int(m), C.c_int(n), C.c_double(eps),
+                                           _ptr(J), _ptr(r)), "fvgs_marginalize")
+    return J, r
+
+
+def marginal_prior_evaluate(J, r, blocks, x, x0, jacobians=True):
+    """fvgs_marginal_prior_evaluate: blocks = [(global size, local offset)]."""
+    J, r = _d(J), _d(r)
+    n = r.size
+    k = len(blocks)
+    sizes = (C.c_int * k)(*[b[0] for b in blocks])
+    idx = (C.c_int * k)(*[b[1] for b in blocks])
+    xs = [_d(v) for v in x]
+    x0s = [_d(v) for v in x0]
+    xp = (C.c_void_p * k)(*[v.ctypes.data for v in xs])
+    x0p = (C.c_void_p * k)(*[v.ctypes.data for v in x0s])
+    res = np.zeros(n)
+    jac = [np.zeros((n, b[0])) for b in blocks] if jacobians else []
+    jp = (C.c_void_p * k)(*[j.ctypes.data for j in jac]) if jacobians else None
+    _check(load_library().fvgs_marginal_prior_evaluate(_ptr(J), _ptr(r), C.c_int(n), C.c_int(k), sizes, idx, xp, x0p,
+                                                       _ptr(res), jp), "fvgs_marginal_prior_evaluate")
+    return (res, jac) if jacobians else res
