@@ -28,6 +28,10 @@ constexpr int kMaxLevels = 3;
 struct FrameLevel {
     int W = 0, H = 0;
     size_t cap_px = 0;
+    // launch variant of the Jacobian kernel chosen by the autotuner for
+    // frames of tuned_w x tuned_h (0 until tuned)
+    int track_variant = 0, tuned_w = 0, tuned_h = 0;
+    float tuned_ms[kTrackVariants] = {};
     float* rgb = nullptr;
     float* depth = nullptr;
     float* gx = nullptr;
@@ -191,6 +195,7 @@ struct fvgs_session {
     // colour/opacity that the projection reads; the float4 planes stay the
     // master copy (mapping updates both)
     int precision = FVGS_PRECISION_FP32;
+    bool autotune = true;  // tune the Jacobian kernel's launch variant on a frame shape's first frame
     uint4* attr_sr = nullptr;
     uint2* attr_c = nullptr;
 
@@ -581,6 +586,7 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
         ta.img_nc = s->img_nc;
     }
     ta.render_only = render_only ? 1 : 0;
+    ta.variant = (f.tuned_w == f.W && f.tuned_h == f.H) ? f.track_variant : 0;
     KScope k(s, render_only ? FVGS_K_RENDER : FVGS_K_TRACK, 1);
     FV_CK(launch_track(ta, s->stream));
     return FVGS_OK;
@@ -1235,12 +1241,119 @@ int fvgs_download_track_images(fvgs_session* s, float* color, float* depth, floa
     return FVGS_OK;
 }
 
+namespace {
+
+// Launch-variant autotuner of the Jacobian kernel: bin the level's frame at
+// `pose`, run every variant `reps` times in turn on that binning (timed with
+// CUDA events on the session's stream), keep the fastest median for frames
+// of this shape.  Every variant computes the same values in the same order,
+// so the choice changes only the time.
+int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int reps) {
+    FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    reps = std::max(1, std::min(reps, 16));
+    for (int attempt = 0;; ++attempt) {
+        if (attempt == 4) return FVGS_E_CAPACITY;
+        FV_TRY(reset_status(s));
+        FV_TRY(set_pose(s, pose));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (!retry) break;
+    }
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps * kTrackVariants, nullptr);
+    int rc = FVGS_OK;
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) rc = FVGS_E_CUDA;
+    FrameLevel saved = f;
+    if (rc == FVGS_OK) {
+        f.tuned_w = f.W;
+        f.tuned_h = f.H;
+        for (int r = 0; r < reps && rc == FVGS_OK; ++r)
+            for (int v = 0; v < kTrackVariants && rc == FVGS_OK; ++v) {
+                f.track_variant = v;
+                const size_t k = 2 * ((size_t)r * kTrackVariants + v);
+                if (cudaEventRecord(ev[k], s->stream) != cudaSuccess) rc = FVGS_E_CUDA;
+                if (rc == FVGS_OK) rc = enqueue_track(s, K, f, false, false);
+                if (rc == FVGS_OK && cudaEventRecord(ev[k + 1], s->stream) != cudaSuccess) rc = FVGS_E_CUDA;
+            }
+        if (rc == FVGS_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = FVGS_E_CUDA;
+    }
+    float med[kTrackVariants] = {};
+    if (rc == FVGS_OK) {
+        for (int v = 0; v < kTrackVariants; ++v) {
+            std::vector<float> t(reps);
+            for (int r = 0; r < reps; ++r) {
+                const size_t k = 2 * ((size_t)r * kTrackVariants + v);
+                cudaEventElapsedTime(&t[r], ev[k], ev[k + 1]);
+            }
+            std::sort(t.begin(), t.end());
+            med[v] = t[reps / 2];
+        }
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc != FVGS_OK) {
+        cudaGetLastError();
+        f = saved;
+        return rc;
+    }
+    int best = 0;
+    for (int v = 1; v < kTrackVariants; ++v)
+        if (med[v] < med[best]) best = v;
+    f.track_variant = best;
+    for (int v = 0; v < kTrackVariants; ++v) f.tuned_ms[v] = med[v];
+    ++s->gen;  // captured frame graphs hold the previous kernel
+    return FVGS_OK;
+}
+
+static_assert(kTrackVariants == FVGS_TRACK_VARIANTS, "launch variants of the Jacobian kernel");
+
+bool needs_tuning(const fvgs_session* s, int level) {
+    const FrameLevel& f = s->lv[level];
+    return s->autotune && (f.tuned_w != f.W || f.tuned_h != f.H);
+}
+
+}  // namespace
+
+int fvgs_session_autotune(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int reps,
+                          int* variant, float* ms) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    FV_TRY(autotune_track(s, pose, K, level, reps));
+    if (variant) *variant = s->lv[level].track_variant;
+    if (ms)
+        for (int v = 0; v < kTrackVariants; ++v) ms[v] = s->lv[level].tuned_ms[v];
+    return FVGS_OK;
+}
+
+int fvgs_session_set_autotune(fvgs_session* s, int enabled) {
+    if (!s) return FVGS_E_INVALID;
+    s->autotune = enabled != 0;
+    return FVGS_OK;
+}
+
+int fvgs_session_set_track_variant(fvgs_session* s, int level, int variant) {
+    if (!s || level < 0 || level >= kMaxLevels || variant < 0 || variant >= kTrackVariants) return FVGS_E_INVALID;
+    FrameLevel& f = s->lv[level];
+    if (!f.rgb) return FVGS_E_STATE;
+    f.track_variant = variant;
+    f.tuned_w = f.W;
+    f.tuned_h = f.H;
+    ++s->gen;
+    return FVGS_OK;
+}
+
 int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
                      double* last_step) {
     if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0) return FVGS_E_INVALID;
     const FrameLevel& f = s->lv[level];
     if (!f.rgb) return FVGS_E_STATE;
     FV_CK(cudaSetDevice(s->device));
+    if (iterations > 0 && needs_tuning(s, level)) FV_TRY(autotune_track(s, pose, K, level, 5));
     const fvgs_pose start = *pose;
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
@@ -1428,6 +1541,7 @@ int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrins
     if (!f.rgb || s->n_g == 0) return FVGS_E_STATE;
     FV_CK(cudaSetDevice(s->device));
     if (map_eta >= 0.f) FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
+    if (iterations > 0 && needs_tuning(s, level)) FV_TRY(autotune_track(s, pose, K, level, 5));
     s->req.pose = *pose;
     s->req.K = *K;
     s->req.level = level;

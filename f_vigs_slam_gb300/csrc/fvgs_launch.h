@@ -203,7 +203,12 @@ struct TrackArgs {
     const float* ref_col;
     const float* ref_opa;
     uint32_t quirks;
+    // launch variant of the Jacobian kernel (the autotuner's choice): 0 = four
+    // CTAs per SM (64 registers), 1 = three CTAs per SM (85 registers); the
+    // arithmetic and its order are the same in both
+    int variant;
 };
+constexpr int kTrackVariants = 2;
 cudaError_t launch_track(const TrackArgs& a, cudaStream_t s);
 // The tracking kernel reading the reference's separate screen-space buffers
 // instead of the packed record planes.

@@ -137,6 +137,7 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     ta.ref_col = colors;
     ta.ref_opa = opacities;
     ta.quirks = P.quirks;
+    ta.variant = 0;
     if (fvgs::launch_track_ref_layout(ta, s) != cudaSuccess) return FVGS_E_CUDA;
     if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), dpose, out, s) != cudaSuccess) return FVGS_E_CUDA;
     if (cudaMemcpyAsync(JtJ, out, sizeof(double) * 36, cudaMemcpyDefault, s) != cudaSuccess ||

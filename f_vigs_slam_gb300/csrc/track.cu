@@ -205,8 +205,8 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
     return total;
 }
 
-template <bool RENDER_ONLY, bool REF_LAYOUT = false>
-__global__ void __launch_bounds__(kPix, 4) track_tile_kernel(TrackArgs a) {
+template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4>
+__global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a) {
     pdl_begin();
     __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
@@ -838,6 +838,7 @@ cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
     const int T = a.ntx * a.nty;
     if (T <= 0) return cudaSuccess;
     if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a);
+    if (a.variant == 1) return launch_chained(track_tile_kernel<false, false, 3>, dim3(T), dim3(kPix), 0, s, a);
     return launch_chained(track_tile_kernel<false>, dim3(T), dim3(kPix), 0, s, a);
 }
 

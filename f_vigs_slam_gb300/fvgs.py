@@ -182,6 +182,21 @@ class Session:
         """Precision form (fvgs_session_set_precision): PRECISION_FP32 or PRECISION_REDUCED."""
         _check(self.lib.fvgs_session_set_precision(self.h, C.c_int(precision)), "fvgs_session_set_precision")
 
+    def autotune(self, pose, K, level: int = 0, reps: int = 5):
+        """fvgs_session_autotune: (chosen variant, median ms per variant)."""
+        v = C.c_int()
+        ms = np.zeros(2, np.float32)
+        _check(self.lib.fvgs_session_autotune(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
+                                              C.c_int(reps), C.byref(v), _ptr(ms)), "fvgs_session_autotune")
+        return int(v.value), ms
+
+    def set_autotune(self, enabled: bool):
+        _check(self.lib.fvgs_session_set_autotune(self.h, C.c_int(int(enabled))), "fvgs_session_set_autotune")
+
+    def set_track_variant(self, level: int, variant: int):
+        _check(self.lib.fvgs_session_set_track_variant(self.h, C.c_int(level), C.c_int(variant)),
+               "fvgs_session_set_track_variant")
+
     def footprint(self) -> int:
         b = C.c_uint64()
         _check(self.lib.fvgs_session_footprint(self.h, C.byref(b)), "fvgs_session_footprint")

@@ -98,6 +98,26 @@ int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes);
 int fvgs_session_set_precision(fvgs_session* s, int precision);
 
 /*
+ * Launch autotuner of the Jacobian kernel (batching form).  The kernel has
+ * two launch variants with the same arithmetic in the same order (four CTAs
+ * of 256 threads per SM at 64 registers, or three at 80); which is faster
+ * depends on the map and frame.  On the first frame of a new frame shape of a
+ * pyramid level (fvgs_track_frame, fvgs_frame_submit) the session bins the
+ * frame at the request's pose, times every variant on that binning and keeps
+ * the fastest for that level and shape; results do not depend on the choice.
+ * fvgs_session_autotune runs the tuning explicitly (reps timed launches per
+ * variant; variant and per-variant median ms (FVGS_TRACK_VARIANTS floats) may
+ * be null); fvgs_session_set_autotune(s, 0) keeps variant 0 for untuned
+ * shapes; fvgs_session_set_track_variant restores a known choice.  No
+ * reference counterpart.
+ */
+#define FVGS_TRACK_VARIANTS 2
+int fvgs_session_autotune(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int reps,
+                          int* variant, float* ms);
+int fvgs_session_set_autotune(fvgs_session* s, int enabled);
+int fvgs_session_set_track_variant(fvgs_session* s, int level, int variant);
+
+/*
  * Gaussians in the reference's SoA layout (Gaussians,
  * include/f_vigs_slam/RepresentationClasses.hpp:53-99): positions[3n],
  * scales[3n], orientations[4n] as (x,y,z,w), colors[3n], opacities[n].
