@@ -22,7 +22,10 @@ request per session.
    arrivals, 30 Hz per session or 70% of the measured capacity if lower.
 The large plain-method workload (one session, N = 1 M room, 1280x720, 20 GN
 iterations + 1 mapping step per frame) is reported under `large_plain`; the
-roofline entry is its dominant kernel.
+roofline entry is its dominant kernel.  Beside it: `batching` (64 keyframes,
+N log-uniform in [20k, 2M], one fvgs_frames_run call against sequential
+frames), `precision` (N = 2 M with BF16/FP16 attributes against FP32) and
+`maintenance` (outlier removal, covisibility, prune on the 1 M map).
 
 Multi-GPU: replicas only (every GPU serves its own sessions; no collective on
 the data path); the elapsed time is the max over ranks.
@@ -56,6 +59,8 @@ SERVE_FRAMES = 2         # distinct frames per session
 SERVE_BUDGET = 150 * 10**9
 MAP_EVERY = 10
 PREC_N = 2_000_000       # precision-form workload: N = 2 M room, 1280x720
+BATCH_SESSIONS = 64      # batching workload: keyframes with N log-uniform in [20k, 2M]
+BATCH_N_MIN, BATCH_N_MAX = 20_000, 2_000_000
 
 
 def parse():
@@ -70,6 +75,7 @@ def parse():
     ap.add_argument("--plain-only", action="store_true",
                     help="only the large plain workload (for profiling runs; not the benchmark line)")
     ap.add_argument("--prec-n", type=int, default=PREC_N, help="Gaussians of the precision-form workload")
+    ap.add_argument("--batch-sessions", type=int, default=BATCH_SESSIONS, help="keyframes of the batching workload")
     return ap.parse_args()
 
 
@@ -518,6 +524,79 @@ def run_precision(args, fvgs, S, torch, dev, stream, world):
     return out
 
 
+def run_batching(args, fvgs, S, torch, dev, world):
+    """The batching workload: 64 keyframes (sessions) with maps of N
+    log-uniform in [20k, 2M], 640x480 and 1280x720 alternately; one step =
+    one tracking frame (20 GN iterations) of every keyframe, either as 64
+    sequential plain frames (fvgs_track_frame) or as one fvgs_frames_run call
+    (all frames in flight together, each replayed from its captured graph)."""
+    rng = np.random.default_rng(41)
+    ns = np.exp(rng.uniform(np.log(BATCH_N_MIN), np.log(BATCH_N_MAX), args.batch_sessions)).astype(int)
+    ws = []
+    for i in range(args.batch_sessions):
+        cam = S.CAM_VGA if i % 2 == 0 else S.CAM_HD
+        W, H, K = cam.width, cam.height, cam.intrinsics
+        sess = fvgs.Session(int(ns[i]), W, H, device=dev.index or 0)
+        sess.upload(S.room(int(ns[i]), seed=5000 + i))
+        traj = S.trajectory(3, seed=6000 + i)
+        frames = []
+        for k in range(2):
+            col, dep, _, _ = sess.render(traj[k + 1], K, W, H)
+            rgb, d = S.add_noise(col, dep, rng)
+            gx, gy = S.sobel3(rgb)
+            frames.append({"prev": traj[k], "pose": traj[k + 1],
+                           "dev": {k2: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+                                   for k2, v in (("rgb", rgb), ("depth", d), ("gx", gx), ("gy", gy))}})
+        ws.append({"sess": sess, "W": W, "H": H, "K": K, "frames": frames})
+    torch.cuda.synchronize()
+
+    def load(k):
+        for w in ws:
+            set_frame_tensors(fvgs, w["sess"], 0, w["frames"][k % 2]["dev"], w["W"], w["H"])
+
+    def batched(k):
+        load(k)
+        return fvgs.frames_run([w["sess"] for w in ws], [w["frames"][k % 2]["prev"] for w in ws],
+                               [w["K"] for w in ws], iterations=ITERS)
+
+    def sequential(k):
+        out = []
+        for w in ws:
+            set_frame_tensors(fvgs, w["sess"], 0, w["frames"][k % 2]["dev"], w["W"], w["H"])
+            out.append(w["sess"].track_frame(w["frames"][k % 2]["prev"], w["K"], iterations=ITERS)[0])
+        return out
+
+    for k in range(max(4, args.warmup + 1)):  # both buffer parities of both frames captured
+        batched(k)
+    sequential(0)
+    steps = max(1, args.steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        seq = sequential(k)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        bat = batched(k)
+    torch.cuda.synchronize()
+    bat_s = time.perf_counter() - t0
+    same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(seq, bat))
+    graphed = sum(w["sess"].frame_stats()["graphed"] for w in ws)
+    for w in ws:
+        w["sess"].close()
+    seq_s, bat_s = max_over_ranks([seq_s, bat_s], dev, world)
+    n = steps * len(ws)
+    return {"workload": "%d keyframes, N log-uniform in [20k, 2M] (%d Gaussians in total), 640x480 / 1280x720, "
+                        "20 GN iterations per frame; one step = one frame of every keyframe"
+                        % (len(ws), int(ns.sum())),
+            "batched_frames_per_s": world * n / bat_s, "sequential_frames_per_s": world * n / seq_s,
+            "speedup_batched_over_sequential": seq_s / bat_s, "poses_identical": bool(same),
+            "graphed_frames": graphed,
+            "form": "fvgs_frames_run: every keyframe's frame on its own stream from its captured graph, "
+                    "against fvgs_track_frame one keyframe after the other"}
+
+
 def set_frame_tensors(fvgs, sess, level, fr, W, H):
     st = sess.lib.fvgs_set_frame(sess.h, level, *(fvgs.C.c_void_p(fr[k].data_ptr()) for k in ("rgb", "depth", "gx", "gy")),
                                  W, H)
@@ -740,6 +819,7 @@ def run_ours(args):
             print(json.dumps({"metric": "large plain workload only (profiling run)", "large_plain": large}), flush=True)
         return 0
     prec = run_precision(args, fvgs, S, torch, dev, stream, world)
+    batch = run_batching(args, fvgs, S, torch, dev, world)
     srv = run_serving(args, fvgs, S, torch, dev)
     srv_fps, plain_fps, e2e_fps = max_over_ranks_rate([srv["served_frames_per_s"], srv["plain_frames_per_s"],
                                                        srv["e2e_frames_per_s"]], dev, world)
@@ -784,6 +864,7 @@ def run_ours(args):
             "large_plain": {k: v for k, v in large.items() if k not in ("roofline", "maintenance")},
             "maintenance": large["maintenance"],
             "precision": prec,
+            "batching": batch,
             "clocks": srv["clocks"],
             "cpu_baseline": cpu,
         }
