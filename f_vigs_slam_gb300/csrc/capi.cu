@@ -15,6 +15,8 @@
 #include <new>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/fvgs.h"
 #include "fvgs_device.cuh"
 #include "fvgs_launch.h"
@@ -194,6 +196,10 @@ struct fvgs_session {
     // precision form: reduced-precision copies of scale/rotation and
     // colour/opacity that the projection reads; the float4 planes stay the
     // master copy (mapping updates both)
+    // tensor maps of the record planes (TMA-staged Jacobian variant)
+    RecMaps rec_maps{};
+    bool rec_maps_ok = false;
+
     int precision = FVGS_PRECISION_FP32;
     bool autotune = true;  // tune the Jacobian kernel's launch variant on a frame shape's first frame
     uint4* attr_sr = nullptr;
@@ -298,6 +304,37 @@ void dev_free(fvgs_session* s, T*& p, size_t count) {
         int r_ = (expr);        \
         if (r_ != FVGS_OK) return r_; \
     } while (0)
+
+// Tensor maps of the three record planes for the TMA-staged Jacobian kernel:
+// 2-D, 4 floats x capacity rows of 16 bytes, one-row boxes (gather4 loads).
+// The encoder comes from the driver through the runtime; without it the
+// variant is simply not offered.
+bool encode_record_maps(fvgs_session* s) {
+    static PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        cudaDriverEntryPointQueryResult q{};
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        cudaGetLastError();
+    }
+    if (!enc) return false;
+    float4* planes[3] = {s->rec0, s->rec1, s->rec2};
+    const cuuint64_t dims[2] = {4, (cuuint64_t)s->cap_g};
+    const cuuint64_t strides[1] = {sizeof(float4)};
+    const cuuint32_t box[2] = {4, 1};
+    const cuuint32_t elem[2] = {1, 1};
+    for (int p = 0; p < 3; ++p)
+        if (enc(&s->rec_maps.rec[p], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, planes[p], dims, strides, box, elem,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    return true;
+}
 
 // Bring the reduced-precision planes up to date with the master planes after
 // a host-side map change (upload, removal, seeding).
@@ -587,8 +624,10 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
     }
     ta.render_only = render_only ? 1 : 0;
     ta.variant = (f.tuned_w == f.W && f.tuned_h == f.H) ? f.track_variant : 0;
+    if (ta.variant == 2 && !s->rec_maps_ok) ta.variant = 0;
+    ta.st_flags = &s->st->flags;
     KScope k(s, render_only ? FVGS_K_RENDER : FVGS_K_TRACK, 1);
-    FV_CK(launch_track(ta, s->stream));
+    FV_CK(launch_track(ta, s->rec_maps_ok ? &s->rec_maps : nullptr, s->stream));
     return FVGS_OK;
 }
 
@@ -881,6 +920,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
         return fail(FVGS_E_NOMEM);
     if (cudaEventCreateWithFlags(&s->frame_done, cudaEventDisableTiming) != cudaSuccess) return fail(FVGS_E_CUDA);
     if (sort_init(&s->sort, device) != cudaSuccess) return fail(FVGS_E_CUDA);
+    s->rec_maps_ok = encode_record_maps(s);
     const uint64_t cap0 = std::max<uint64_t>(1u << 20, 8ull * N);
     if ((rc = alloc_instances(s, std::min<uint64_t>(cap0, 0xffffffffull))) != FVGS_OK) return fail(rc);
     if (cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
@@ -1274,6 +1314,7 @@ int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics
         f.tuned_h = f.H;
         for (int r = 0; r < reps && rc == FVGS_OK; ++r)
             for (int v = 0; v < kTrackVariants && rc == FVGS_OK; ++v) {
+                if (v == 2 && !s->rec_maps_ok) continue;
                 f.track_variant = v;
                 const size_t k = 2 * ((size_t)r * kTrackVariants + v);
                 if (cudaEventRecord(ev[k], s->stream) != cudaSuccess) rc = FVGS_E_CUDA;
@@ -1303,7 +1344,7 @@ int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics
     }
     int best = 0;
     for (int v = 1; v < kTrackVariants; ++v)
-        if (med[v] < med[best]) best = v;
+        if ((v != 2 || s->rec_maps_ok) && med[v] < med[best]) best = v;
     f.track_variant = best;
     for (int v = 0; v < kTrackVariants; ++v) f.tuned_ms[v] = med[v];
     ++s->gen;  // captured frame graphs hold the previous kernel
@@ -1339,7 +1380,7 @@ int fvgs_session_set_autotune(fvgs_session* s, int enabled) {
 int fvgs_session_set_track_variant(fvgs_session* s, int level, int variant) {
     if (!s || level < 0 || level >= kMaxLevels || variant < 0 || variant >= kTrackVariants) return FVGS_E_INVALID;
     FrameLevel& f = s->lv[level];
-    if (!f.rgb) return FVGS_E_STATE;
+    if (!f.rgb || (variant == 2 && !s->rec_maps_ok)) return FVGS_E_STATE;
     f.track_variant = variant;
     f.tuned_w = f.W;
     f.tuned_h = f.H;

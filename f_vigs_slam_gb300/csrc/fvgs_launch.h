@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/fvgs_types.h"
@@ -204,12 +205,19 @@ struct TrackArgs {
     const float* ref_opa;
     uint32_t quirks;
     // launch variant of the Jacobian kernel (the autotuner's choice): 0 = four
-    // CTAs per SM (64 registers), 1 = three CTAs per SM (85 registers); the
-    // arithmetic and its order are the same in both
+    // CTAs per SM (64 registers), 1 = three CTAs per SM (80 registers), 2 =
+    // four CTAs per SM with the record batches gathered by TMA (needs the
+    // record tensor maps); the arithmetic and its order are the same in all
     int variant;
+    uint32_t* st_flags;  // status word for bounded-wait timeouts (variant 2)
 };
-constexpr int kTrackVariants = 2;
-cudaError_t launch_track(const TrackArgs& a, cudaStream_t s);
+constexpr int kTrackVariants = 3;
+// Tensor maps of the three record planes (2-D: 4 floats x capacity rows,
+// 16-byte rows, one-row boxes) for the TMA-staged variant.
+struct RecMaps {
+    CUtensorMap rec[3];
+};
+cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s);
 // The tracking kernel reading the reference's separate screen-space buffers
 // instead of the packed record planes.
 cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s);

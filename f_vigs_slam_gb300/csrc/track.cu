@@ -205,12 +205,184 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
     return total;
 }
 
-template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4>
-__global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a) {
+// ---------------------------------------------------------------------------
+// TMA staging (launch variant 2).  The records of a batch are gathered into
+// shared memory by tile::gather4 tensor copies -- four Gaussians' 16-byte rows
+// of one record plane per copy, 192 copies per batch -- completing on an
+// mbarrier.  The next batch is gathered while the current one is blended, so
+// the records' load latency leaves the blending warps.  The staging itself
+// (rejection test, compaction into TrackBatch) is the same as stage_batch's.
+// Row indices outside the map (past the list, or defensive out-of-range
+// values) are replaced by row 0 and the row is not staged, so every copy
+// reads inside the record planes and transfers exactly 64 bytes.
+constexpr int kGroups = kBatch / 4;
+constexpr uint32_t kTmaBatchBytes = 3u * kGroups * 64u;
+
+struct TmaStage {
+    float4 raw[3][kGroups][8];  // plane, group of 4 Gaussians (128-byte slots, first 64 bytes used)
+    uint32_t gid[kBatch];       // the batch's Gaussian indices (0xffffffff past the list)
+    unsigned long long bar;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_bar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_bar_expect(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the completion of the phase with the given parity.
+__device__ __forceinline__ bool tma_bar_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kSpinLimit && !done; ++it)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void tma_gather4(float4* dst, const CUtensorMap* map, uint32_t r0, uint32_t r1,
+                                            uint32_t r2, uint32_t r3, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Issue the gathers of entries [base, base + kBatch) of the tile's list (the
+// expected bytes were announced before the preceding barrier).
+__device__ __forceinline__ void tma_issue(const TrackArgs& a, const RecMaps& maps, TmaStage& ts, uint32_t list0,
+                                          int base, int limit) {
+    const int tid = threadIdx.x;
+    {
+        const int li = base + tid;
+        ts.gid[tid] = li < limit ? a.indices[list0 + li] : 0xffffffffu;
+    }
+    if (tid < 3 * kGroups) {
+        // the rows of the previous batch were read through the generic proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int plane = tid / kGroups, grp = tid % kGroups;
+        uint32_t r[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int li = base + 4 * grp + j;
+            const uint32_t g = li < limit ? a.indices[list0 + li] : 0u;
+            r[j] = g < a.n_gauss ? g : 0u;
+        }
+        tma_gather4(&ts.raw[plane][grp][0], &maps.rec[plane], r[0], r[1], r[2], r[3], &ts.bar);
+    }
+}
+
+// stage_batch with the records taken from the gathered batch; also announces
+// and issues the gathers of the next batch once this one is consumed.
+// parity / pending / broken track the mbarrier (uniform across the CTA).  A
+// wait that gives up flags kErrTimeout and leaves the copy pending: nothing
+// more is staged or issued, and the end of the pass waits for it once more.
+struct TmaState {
+    uint32_t parity = 0;
+    bool pending = false;
+    bool broken = false;
+};
+
+template <bool FORWARD>
+__device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps& maps, TrackBatch& sb, TmaStage& ts,
+                                               uint32_t list0, int base, int limit, float x0, float y0,
+                                               TmaState& tm) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    bool ready = !tm.broken;
+    if (ready && tm.pending) {
+        ready = tma_bar_wait(&ts.bar, tm.parity);
+        if (ready) {
+            tm.parity ^= 1u;
+            tm.pending = false;
+        } else {
+            tm.broken = true;
+            if (tid == 0) atomicOr(&a.st_flags[0], kErrTimeout);
+        }
+    }
+    const int li = base + tid;
+    bool keep = false;
+    float4 r0, r1, r2;
+    float vrej = 0.f;
+    const uint32_t g = ts.gid[tid];
+    if (ready && li < limit && g < a.n_gauss) {
+        r0 = ts.raw[0][tid >> 2][tid & 3];
+        r1 = ts.raw[1][tid >> 2][tid & 3];
+        r2 = ts.raw[2][tid >> 2][tid & 3];
+        vrej = reject_bound(r0.w);
+        keep = !tile_prunable<FORWARD>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+    }
+    const uint32_t bal = __ballot_sync(kFullMask, keep);
+    if (lane == 0) sb.wcnt[w] = __popc(bal);
+    __syncthreads();  // the batch's raw rows and indices are consumed
+    int wbase = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < kPix / 32; ++k) {
+        const int c = sb.wcnt[k];
+        wbase += (k < w) ? c : 0;
+        total += c;
+    }
+    if (keep) {
+        const int pos = wbase + __popc(bal & lanemask_lt());
+        sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
+        sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
+        sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
+        sb.D[pos] = r2.w;
+        sb.orig[pos] = li;
+    }
+    const bool next = ready && base + kBatch < limit;
+    if (next && tid == 0) tma_bar_expect(&ts.bar, kTmaBatchBytes);
+    __syncthreads();
+    if (next) {
+        tma_issue(a, maps, ts, list0, base + kBatch, limit);
+        tm.pending = true;
+    }
+    return total;
+}
+
+// Start a pass: announce and gather its first batch.
+__device__ __forceinline__ void tma_begin(const TrackArgs& a, const RecMaps& maps, TmaStage& ts, uint32_t list0,
+                                          int limit, TmaState& tm) {
+    if (limit <= 0 || tm.broken) return;
+    if (threadIdx.x == 0) tma_bar_expect(&ts.bar, kTmaBatchBytes);
+    __syncthreads();
+    tma_issue(a, maps, ts, list0, 0, limit);
+    tm.pending = true;
+}
+
+// End a pass: wait (bounded) for a gather still in flight, since the buffer
+// is reused or the CTA exits.
+__device__ __forceinline__ void tma_drain(const TrackArgs& a, TmaStage& ts, TmaState& tm) {
+    if (!tm.pending) return;
+    if (tma_bar_wait(&ts.bar, tm.parity)) {
+        tm.parity ^= 1u;
+        tm.pending = false;
+    } else {
+        tm.broken = true;
+        if (threadIdx.x == 0) atomicOr(&a.st_flags[0], kErrTimeout);
+    }
+}
+
+template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4, bool TMA = false>
+__global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a, const __grid_constant__ RecMaps maps) {
     pdl_begin();
     __shared__ TrackBatch sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
+    extern __shared__ __align__(128) unsigned char s_dyn[];  // TMA variant: the gathered batch
+    TmaStage& ts = *reinterpret_cast<TmaStage*>((reinterpret_cast<uintptr_t>(s_dyn) + 127) & ~uintptr_t(127));
+    TmaState tm;
+    if (TMA) {
+        if (threadIdx.x == 0) tma_bar_init(&ts.bar);
+        __syncthreads();
+    }
 
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
@@ -237,9 +409,11 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a)
     float final_T = 1.f;
     uint32_t n_contrib = 0;
     if (n > 0) {
+        if (TMA) tma_begin(a, maps, ts, range.x, n, tm);
         for (int base = 0; base < n; base += kBatch) {
             if (__syncthreads_and(done)) break;
-            const int cnt = stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
+            const int cnt = TMA ? stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm)
+                                : stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
                 int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
@@ -290,6 +464,7 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a)
                 if (last_j >= 0) last = (uint32_t)sb.orig[last_j] + 1u;
             }
         }
+        if (TMA) tma_drain(a, ts, tm);
         if (inside) {
             final_T = T;
             n_contrib = last;
@@ -378,9 +553,11 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a)
     float prod_alpha = 1.f, Tm = 1.f, acr = 0.f, acg = 0.f, acb = 0.f;
     bool done2 = !do_jac;
     const float inv_fx = __frcp_rn(fx), inv_fy = __frcp_rn(fy);
+    if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
-        const int cnt = stage_batch<REF_LAYOUT, false>(a, sb, range.x, base, nmax, x0, y0);
+        const int cnt = TMA ? stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm)
+                            : stage_batch<REF_LAYOUT, false>(a, sb, range.x, base, nmax, x0, y0);
         if (!done2) {
             for (int j = 0; j < cnt; ++j) {
                 if (sb.orig[j] >= (int)n_contrib) {
@@ -445,6 +622,8 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a)
             }
         }
     }
+
+    if (TMA) tma_drain(a, ts, tm);
 
     // --------------------------- tile reduction ------------------------------
     float vals[32];
@@ -834,18 +1013,25 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
         for (int k = 0; k < 6; ++k) step_out[k] = delta[k];
 }
 
-cudaError_t launch_track(const TrackArgs& a, cudaStream_t s) {
+cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s) {
     const int T = a.ntx * a.nty;
     if (T <= 0) return cudaSuccess;
-    if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a);
-    if (a.variant == 1) return launch_chained(track_tile_kernel<false, false, 3>, dim3(T), dim3(kPix), 0, s, a);
-    return launch_chained(track_tile_kernel<false>, dim3(T), dim3(kPix), 0, s, a);
+    RecMaps m{};
+    if (maps) m = *maps;
+    if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a, m);
+    if (a.variant == 1) return launch_chained(track_tile_kernel<false, false, 3>, dim3(T), dim3(kPix), 0, s, a, m);
+    if (a.variant == 2) {
+        if (!maps || !a.st_flags) return cudaErrorInvalidValue;
+        return launch_chained(track_tile_kernel<false, false, 4, true>, dim3(T), dim3(kPix), sizeof(TmaStage) + 128,
+                              s, a, m);
+    }
+    return launch_chained(track_tile_kernel<false>, dim3(T), dim3(kPix), 0, s, a, m);
 }
 
 cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s) {
     const int T = a.ntx * a.nty;
     if (T <= 0) return cudaSuccess;
-    return launch_chained(track_tile_kernel<false, true>, dim3(T), dim3(kPix), 0, s, a);
+    return launch_chained(track_tile_kernel<false, true>, dim3(T), dim3(kPix), 0, s, a, RecMaps{});
 }
 
 cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,

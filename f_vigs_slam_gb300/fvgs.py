@@ -185,7 +185,7 @@ class Session:
     def autotune(self, pose, K, level: int = 0, reps: int = 5):
         """fvgs_session_autotune: (chosen variant, median ms per variant)."""
         v = C.c_int()
-        ms = np.zeros(2, np.float32)
+        ms = np.zeros(3, np.float32)
         _check(self.lib.fvgs_session_autotune(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
                                               C.c_int(reps), C.byref(v), _ptr(ms)), "fvgs_session_autotune")
         return int(v.value), ms
