@@ -26,7 +26,10 @@ Q_INVSIGMA_SWAP = 0x4
 Q_MAP_CAP256 = 0x8
 Q_VIS_CAP256 = 0x10
 Q_ADAM_STAY = 0x20
-QUIRKS_DEFAULT = Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY
+Q_POSE_WXYZ = 0x40
+Q_COLOR_RESCALE = 0x80
+QUIRKS_DEFAULT = (Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY | Q_POSE_WXYZ
+                  | Q_COLOR_RESCALE)
 
 PRECISION_FP32 = 0
 PRECISION_REDUCED = 1

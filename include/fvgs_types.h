@@ -64,6 +64,12 @@ typedef enum fvgs_status {
  *                surviving Gaussian that moves down inherits the optimiser
  *                moments of the one that held its new index.  Clear: the
  *                moments move with their Gaussian.
+ *  POSE_WXYZ     (host mirror, include/f_vigs_slam) GSSlam builds the camera
+ *                orientation as make_float4(w, x, y, z) (src/GSSlam.cu:2121)
+ *                for kernels that read (x, y, z, w).  Clear: (x, y, z, w).
+ *  COLOR_RESCALE (host mirror) computeRgbdPoseJacobians scales the [0, 1]
+ *                colour pyramid by 1/255 once more (src/GSSlam.cu:2158).
+ *                Clear: the pyramid colour as is.
  */
 #define FVGS_Q_CULLED_SLOTS  0x1u
 #define FVGS_Q_RANGE_LAUNCH  0x2u
@@ -71,10 +77,14 @@ typedef enum fvgs_status {
 #define FVGS_Q_MAP_CAP256    0x8u
 #define FVGS_Q_VIS_CAP256    0x10u
 #define FVGS_Q_ADAM_STAY     0x20u
+#define FVGS_Q_POSE_WXYZ     0x40u
+#define FVGS_Q_COLOR_RESCALE 0x80u
 /* Default: the reference's arithmetic (swap, caps, optimiser state left in
- * place) with the two launch/slot defects that make its outputs degenerate
- * (NaN tile 0, empty ranges) off. */
-#define FVGS_QUIRKS_DEFAULT  (FVGS_Q_INVSIGMA_SWAP | FVGS_Q_MAP_CAP256 | FVGS_Q_VIS_CAP256 | FVGS_Q_ADAM_STAY)
+ * place, the host's pose order and colour rescale) with the two launch/slot
+ * defects that make its outputs degenerate (NaN tile 0, empty ranges) off. */
+#define FVGS_QUIRKS_DEFAULT                                                                          \
+    (FVGS_Q_INVSIGMA_SWAP | FVGS_Q_MAP_CAP256 | FVGS_Q_VIS_CAP256 | FVGS_Q_ADAM_STAY | FVGS_Q_POSE_WXYZ | \
+     FVGS_Q_COLOR_RESCALE)
 
 typedef struct fvgs_pose {
     float position[3];     /* camera centre in world frame */
