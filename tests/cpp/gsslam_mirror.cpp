@@ -9,7 +9,11 @@
 //         q_imu_cam[4] (x,y,z,w) imu_pose[7] (p, q x,y,z,w)
 // output: int32 status; float32 camera position[3] orientation[4] (raw);
 //         float64 JtJ[36] Jtr[6] (IMU frame); int32 evaluate_ok;
-//         float64 residuals[6] jacobian[42]; uint32 n_gaussians
+//         float64 residuals[6] jacobian[42]; uint32 n_gaussians;
+//         then the map maintenance at the camera pose: int32 status after
+//         each of removeOutliers, computeCovisibilityRatio, prune, densify,
+//         optimizeGaussiansKeyframe, renderView; uint32 count after
+//         removeOutliers, prune, densify; float32 covisibility ratio
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -76,6 +80,31 @@ int main(int argc, char** argv) {
     wr(out, jac, 42);
     const uint32_t count = slam.getGaussiansCount();
     wr(out, &count, 1);
+
+    // map maintenance as the reference's loop runs it after tracking
+    slam.setCurrentPose(cam);
+    slam.addKeyframe();
+    int32_t st[6];
+    uint32_t counts[3];
+    slam.removeOutliers();
+    st[0] = slam.lastStatus();
+    counts[0] = slam.getGaussiansCount();
+    const float ratio = slam.computeCovisibilityRatio();
+    st[1] = slam.lastStatus();
+    slam.prune();
+    st[2] = slam.lastStatus();
+    counts[1] = slam.getGaussiansCount();
+    slam.densify(slam.keyframes()[0]);
+    st[3] = slam.lastStatus();
+    counts[2] = slam.getGaussiansCount();
+    slam.optimizeGaussiansKeyframe(slam.keyframes()[0]);
+    st[4] = slam.lastStatus();
+    std::vector<float> img_rgb(3 * (size_t)W * H), img_d((size_t)W * H);
+    slam.renderView(cam, intr, W, H, img_rgb.data(), img_d.data());
+    st[5] = slam.lastStatus();
+    wr(out, st, 6);
+    wr(out, counts, 3);
+    wr(out, &ratio, 1);
     fclose(out);
     printf("gsslam mirror: status %d evaluate %d gaussians %u\n", status, eval_ok, count);
     return 0;

@@ -134,3 +134,18 @@ def test_mirror_evaluate_matches_reference_host_path(oracle, fvgs_lib, tmp_path)
     Hk, Pk = E.thresholded(JtJ, 1e-4)
     np.testing.assert_allclose(Jstar.T @ Jstar, Hk, rtol=0, atol=1e-9 * np.abs(Hk).max())
     np.testing.assert_allclose(Jstar.T @ res, Pk @ Jtr, rtol=0, atol=1e-6 * max(1.0, np.abs(Pk @ Jtr).max()))
+
+    # map maintenance through the mirror (removeOutliers at the camera pose
+    # on the level-0 depth, covisibility of a keyframe taken at that pose,
+    # prune, densify against it, a keyframe mapping step, renderView)
+    st = take(np.int32, 6)
+    counts = take(np.uint32, 3)
+    ratio = take(np.float32, 1)[0]
+    assert np.all(st == 0), st
+    b0 = oracle.prepare(scene, pose_raw, K, W, H, P)
+    ta, op = oracle.outlier_scores(b0, depth, W, H, P)
+    marked = int((oracle.outlier_states(ta, op, 0.6) != 0).sum())
+    removed = scene.n - int(counts[0])
+    assert abs(removed - marked) <= max(2, scene.n // 1000), (removed, marked)
+    assert ratio == 1.0  # the keyframe was taken at the current pose
+    assert counts[1] <= counts[0] and counts[2] >= counts[1]
