@@ -15,7 +15,12 @@
 //  * every per-Gaussian colour term is rank one (Jt_cam = jt_dl (x) alpha*dC),
 //    so J_pose * JtJ_cam * J_pose^T becomes one 21-FMA update with
 //    u = (jt_dl, d * (ray x jt_dl)) instead of the reference's 3x3 and 6x3
-//    products;
+//    products; with jt_dl = g / d that is u = (g / d, ray x g), so the
+//    per-pixel depth enters through one reciprocal;
+//  * per-Gaussian factors of u (the mean's ray, -f * ray) are computed once
+//    per staged batch; the per-pixel depth takes the compensated evaluation
+//    only where its two-FMA value may have cancelled; reciprocals are the
+//    one-ulp rcp.approx;
 //  * terms are accumulated in the camera frame (translation rows without R)
 //    and rotated once per frame, in FP64, by diag(R, I);
 //  * the 27 per-thread sums are reduced by a 31-shuffle butterfly
@@ -50,6 +55,25 @@ __device__ __forceinline__ float depth_at(float z, float dx, float phx, float dy
     const float b2 = __fsub_rn(s2, s1);
     const float r2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(p2, b2));
     return __fadd_rn(s2, __fadd_rn(__fadd_rn(r1, r2), __fadd_rn(e1, e2)));
+}
+
+// z + dx*phx + dy*phy by two FMAs when that is accurate, else depth_at.  Each
+// FMA rounds once, so the error is at most 2^-24 (|t| + |s|) with t the first
+// FMA's result and s the second's; when |t| <= 8 |s| that is under 6e-7 |s|.
+// Cancellation (|s| small against |t|) and non-finite values take the
+// compensated path.
+__device__ __forceinline__ float depth_fast(float z, float dx, float phx, float dy, float phy) {
+    const float t = __fmaf_rn(dx, phx, z);
+    const float s = __fmaf_rn(dy, phy, t);
+    if (fabsf(t) <= 8.0f * fabsf(s)) return s;
+    return depth_at(z, dx, phx, dy, phy);
+}
+
+// PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 __device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
@@ -155,15 +179,32 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
 
 // Shared-memory batch of Gaussians, repacked so a rejected pair needs two
 // loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, opacity, z),
-// sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list.
+// sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list;
+// for the Jacobian pass also sE = (rgx, rgy, -fx rgx, -fy rgy), the mean's
+// normalised ray and the third row of the projection Jacobian without 1/d.
 struct TrackBatch {
     float4 A[kBatch];
     float4 B[kBatch];
     float4 C[kBatch];
+    float4 E[kBatch];
     float D[kBatch];
     int orig[kBatch];
     int wcnt[kPix / 32];
 };
+
+template <bool FORWARD>
+__device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch& sb, int pos, const float4& r0,
+                                           const float4& r1, const float4& r2, float vrej, int li) {
+    sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
+    sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
+    sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
+    sb.D[pos] = r2.w;
+    sb.orig[pos] = li;
+    if (!FORWARD) {
+        const float rgx = (r0.x - a.K.cx) * __frcp_rn(a.K.fx), rgy = (r0.y - a.K.cy) * __frcp_rn(a.K.fy);
+        sb.E[pos] = make_float4(rgx, rgy, -a.K.fx * rgx, -a.K.fy * rgy);
+    }
+}
 
 // Stage entries [base, min(base+256, limit)) of the tile's list, dropping the
 // ones tile_prunable rejects; returns the number kept.  Ends with a barrier.
@@ -193,14 +234,7 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, u
         wbase += (k < w) ? c : 0;
         total += c;
     }
-    if (keep) {
-        const int pos = wbase + __popc(bal & lanemask_lt());
-        sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
-        sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
-        sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
-        sb.D[pos] = r2.w;
-        sb.orig[pos] = li;
-    }
+    if (keep) put_staged<FORWARD>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li);
     __syncthreads();
     return total;
 }
@@ -329,14 +363,7 @@ __device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps
         wbase += (k < w) ? c : 0;
         total += c;
     }
-    if (keep) {
-        const int pos = wbase + __popc(bal & lanemask_lt());
-        sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
-        sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
-        sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
-        sb.D[pos] = r2.w;
-        sb.orig[pos] = li;
-    }
+    if (keep) put_staged<FORWARD>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li);
     const bool next = ready && base + kBatch < limit;
     if (next && tid == 0) tma_bar_expect(&ts.bar, kTmaBatchBytes);
     __syncthreads();
@@ -424,9 +451,10 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                     const float test_T = T * (1.0f - alpha);
                     if (test_T < 0.0001f) return false;
                     const float4 rC = sb.C[j];
-                    cr += rC.z * alpha * T;
-                    cg += rC.w * alpha * T;
-                    cb += sb.D[j] * alpha * T;
+                    const float aT = alpha * T;
+                    cr += rC.z * aT;
+                    cg += rC.w * aT;
+                    cb += sb.D[j] * aT;
                     if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, dx, rC.x, dy, rC.y);
                     T = test_T;
                     last_j = j;
@@ -550,9 +578,10 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
     if (do_jac && n_contrib > 0) atomicMax(&s_nmax, n_contrib);
     __syncthreads();
     const int nmax = (int)min((uint32_t)n, s_nmax);
-    float prod_alpha = 1.f, Tm = 1.f, acr = 0.f, acg = 0.f, acb = 0.f;
+    // rem = final colour minus the colour accumulated so far (running)
+    float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
+    bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
     bool done2 = !do_jac;
-    const float inv_fx = __frcp_rn(fx), inv_fy = __frcp_rn(fy);
     if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
     for (int base = 0; base < nmax; base += kBatch) {
         if (__syncthreads_and(done2)) break;
@@ -572,30 +601,48 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
                 if (alpha < kInv255) continue;
                 const float4 rC = sb.C[j];
-                const float d = depth_at(rB.w, dx, rC.x, dy, rC.y);
+                const float4 rE = sb.E[j];
+                const float d = depth_fast(rB.w, dx, rC.x, dy, rC.y);
                 float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
-                acr += alpha * da0;
-                acg += alpha * da1;
-                acb += alpha * da2;
-                const float inv1m = __frcp_rn(1.0f - alpha);  // == 1.0f / x, correctly rounded
-                da0 -= (cr - acr) * inv1m;
-                da1 -= (cg - acg) * inv1m;
-                da2 -= (cb - acb) * inv1m;
+                remr -= alpha * da0;
+                remg -= alpha * da1;
+                remb -= alpha * da2;
+                const float inv1m = rcp_approx(1.0f - alpha);
+                da0 -= remr * inv1m;
+                da1 -= remg * inv1m;
+                da2 -= remb * inv1m;
                 const float dl0 = rA.z * dx + rA.w * dy;
                 const float dl1 = rA.w * dx + rB.x * dy;
-                const float rgx = (rA.x - cx) * inv_fx, rgy = (rA.y - cy) * inv_fy;
-                const float inv_d = __frcp_rn(d);
-                const float jt0 = fx * inv_d * dl0;
-                const float jt1 = fy * inv_d * dl1;
-                const float jt2 = (-fx * rgx * inv_d) * dl0 + (-fy * rgy * inv_d) * dl1;
+                // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
+                // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
+                // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
+                const float g0 = fx * dl0, g1 = fy * dl1, g2 = rE.z * dl0 + rE.w * dl1;
+                const float inv_d = rcp_approx(d);
+                const float u0 = g0 * inv_d, u1 = g1 * inv_d, u2 = g2 * inv_d;
+                const float u3 = rE.y * g2 - g1, u4 = g0 - rE.x * g2, u5 = rE.x * g1 - rE.y * g0;
                 const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
-                rank1_update(A, w, jt0, jt1, jt2, d, rgx, rgy, 1.0f);
+                {
+                    const float u[6] = {u0, u1, u2, u3, u4, u5};
+                    int idx = 0;
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) {
+                        const float wu = w * u[i];
+#pragma unroll
+                        for (int k = i; k < 6; ++k) A[idx++] += wu * u[k];
+                    }
+                }
                 const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
-                float Jr0 = coef * jt0, Jr1 = coef * jt1, Jr2 = coef * jt2;
+                bv[0] += coef * u0;
+                bv[1] += coef * u1;
+                bv[2] += coef * u2;
+                bv[3] += coef * u3;
+                bv[4] += coef * u4;
+                bv[5] += coef * u5;
                 prod_alpha *= (1.0f - alpha);
-                if (Tm > 0.5f && prod_alpha <= 0.5f && img_depth > 0.5f) {
-                    Tm = prod_alpha;
-                    const float r[3] = {rgx, rgy, 1.0f};
+                if (depth_pending && prod_alpha <= 0.5f) {
+                    // the depth term wd * derr * r: its rotation part d (r x r) is zero
+                    depth_pending = false;
+                    const float r[3] = {rE.x, rE.y, 1.0f};
                     int idx = 0;
 #pragma unroll
                     for (int i = 0; i < 3; ++i) {
@@ -605,16 +652,10 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                             ++idx;
                         }
                     }
-                    Jr0 += wd * derr * rgx;
-                    Jr1 += wd * derr * rgy;
-                    Jr2 += wd * derr;
+                    bv[0] += wd * derr * rE.x;
+                    bv[1] += wd * derr * rE.y;
+                    bv[2] += wd * derr;
                 }
-                bv[0] += Jr0;
-                bv[1] += Jr1;
-                bv[2] += Jr2;
-                bv[3] += d * (rgy * Jr2 - Jr1);
-                bv[4] += d * (Jr0 - rgx * Jr2);
-                bv[5] += d * (rgx * Jr1 - rgy * Jr0);
                 if (prod_alpha < 0.001f) {
                     done2 = true;
                     break;
