@@ -69,6 +69,16 @@ __device__ __forceinline__ float depth_fast(float z, float dx, float phx, float 
     return depth_at(z, dx, phx, dy, phy);
 }
 
+// The conic's quadratic form v = a dx^2 + 2 b dx dy + c dy^2, evaluated as
+// dx * dl0 + dy * dl1 with dl0 = a dx + b dy, dl1 = b dx + c dy: the
+// gradient terms the Jacobian pass needs come for free.  Both passes use this
+// one expression, so their per-pixel accept / reject decisions agree.
+__device__ __forceinline__ float conic_form(float a, float b, float c, float dx, float dy, float& dl0, float& dl1) {
+    dl0 = __fmaf_rn(a, dx, __fmul_rn(b, dy));
+    dl1 = __fmaf_rn(b, dx, __fmul_rn(c, dy));
+    return __fmaf_rn(dx, dl0, __fmul_rn(dy, dl1));
+}
+
 // PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
@@ -469,8 +479,9 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                     const float2 rB1 = *reinterpret_cast<const float2*>(&sb.B[j + 1]);
                     const float dx0 = rA0.x - xf, dy0 = rA0.y - yf;
                     const float dx1 = rA1.x - xf, dy1 = rA1.y - yf;
-                    const float v0 = rA0.z * dx0 * dx0 + 2.0f * rA0.w * dx0 * dy0 + rB0.x * dy0 * dy0;
-                    const float v1 = rA1.z * dx1 * dx1 + 2.0f * rA1.w * dx1 * dy1 + rB1.x * dy1 * dy1;
+                    float q0, q1;
+                    const float v0 = conic_form(rA0.z, rA0.w, rB0.x, dx0, dy0, q0, q1);
+                    const float v1 = conic_form(rA1.z, rA1.w, rB1.x, dx1, dy1, q0, q1);
                     const bool k0 = !(v0 > rB0.y || v0 <= 0.0f);
                     const bool k1 = !(v1 > rB1.y || v1 <= 0.0f);
                     if (k0 && !blend(j, dx0, dy0, v0)) {
@@ -486,7 +497,8 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                     const float4 rA = sb.A[j];
                     const float2 rB = *reinterpret_cast<const float2*>(&sb.B[j]);
                     const float dx = rA.x - xf, dy = rA.y - yf;
-                    const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
+                    float q0, q1;
+                    const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, q0, q1);
                     if (!(v > rB.y || v <= 0.0f) && !blend(j, dx, dy, v)) done = true;
                 }
                 if (last_j >= 0) last = (uint32_t)sb.orig[last_j] + 1u;
@@ -596,7 +608,8 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 const float4 rA = sb.A[j];
                 const float4 rB = sb.B[j];
                 const float dx = rA.x - xf, dy = rA.y - yf;
-                const float v = rA.z * dx * dx + 2.0f * rA.w * dx * dy + rB.x * dy * dy;
+                float dl0, dl1;
+                const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
                 if (v > rB.y) continue;
                 const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
                 if (alpha < kInv255) continue;
@@ -611,8 +624,6 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 da0 -= remr * inv1m;
                 da1 -= remg * inv1m;
                 da2 -= remb * inv1m;
-                const float dl0 = rA.z * dx + rA.w * dy;
-                const float dl1 = rA.w * dx + rB.x * dy;
                 // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
                 // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
                 // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
