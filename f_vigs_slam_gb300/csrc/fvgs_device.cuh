@@ -189,6 +189,24 @@ __device__ __forceinline__ float reject_bound(float o) {
     return b + 1e-3f + 1e-4f * fabsf(b);
 }
 
+// The conic's quadratic form v = a dx^2 + 2 b dx dy + c dy^2, evaluated as
+// dx * dl0 + dy * dl1 with dl0 = a dx + b dy, dl1 = b dx + c dy: the
+// gradient terms the backward passes need come for free.  A pass that
+// re-derives another pass's per-pixel accept / reject decisions uses the same
+// expression (the tracking passes, the mapping forward and backward).
+__device__ __forceinline__ float conic_form(float a, float b, float c, float dx, float dy, float& dl0, float& dl1) {
+    dl0 = __fmaf_rn(a, dx, __fmul_rn(b, dy));
+    dl1 = __fmaf_rn(b, dx, __fmul_rn(c, dy));
+    return __fmaf_rn(dx, dl0, __fmul_rn(dy, dl1));
+}
+
+// PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Reduced-precision attribute words (round to nearest even).
 __device__ __forceinline__ uint32_t bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float bf16_val(uint32_t b) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)b)); }

@@ -69,7 +69,8 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
                 const float4 r0 = s0[j];
                 const float4 r1 = s1[j];
                 const float dx = xf - r0.x, dy = yf - r0.y;
-                const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+                float dl0, dl1;
+                const float v = conic_form(r1.x, r1.y, r1.z, dx, dy, dl0, dl1);
                 const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
                 if (alpha < kMInv255 || v <= 0.0f) continue;
                 const float4 r2 = s2[j];
@@ -177,7 +178,8 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             if (j >= nc) continue;
             const float pxf = (float)(tx * 16 + (idx & 15)), pyf = (float)(ty * 16 + (idx >> 4));
             const float dx = r0.x - pxf, dy = r0.y - pyf;
-            const float v = r1.x * dx * dx + 2.0f * r1.y * dx * dy + r1.z * dy * dy;
+            float dl0, dl1;  // the forward pass's conic form ((dx, dy) negated: same value)
+            const float v = conic_form(r1.x, r1.y, r1.z, dx, dy, dl0, dl1);
             const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
             if (alpha < kMInv255) continue;
             const float4 pc = s_pc[idx];
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             a0 += d0 * alpha;
             a1 += d1 * alpha;
             a2 += d2 * alpha;
-            const float inv1m = 1.0f / (1.0f - alpha);
+            const float inv1m = rcp_approx(1.0f - alpha);
             d0 = (d0 - (pc.x - a0) * inv1m) * -pe.x;
             d1 = (d1 - (pc.y - a1) * inv1m) * -pe.y;
             d2 = (d2 - (pc.z - a2) * inv1m) * -pe.z;
@@ -197,11 +199,12 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             dcg -= aT * pe.y;
             dcb -= aT * pe.z;
             dal -= aG;
-            dmx -= aG * (r1.x * dx + r1.y * dy);
-            dmy -= aG * (r1.y * dx + r1.z * dy);
-            dix -= 0.5f * aG * dx * dx;
-            diy -= 0.5f * aG * dx * dy;
-            diz -= 0.5f * aG * dy * dy;
+            dmx -= aG * dl0;
+            dmy -= aG * dl1;
+            const float haG = 0.5f * aG;
+            dix -= haG * dx * dx;
+            diy -= haG * dx * dy;
+            diz -= haG * dy * dy;
             const float test_T = T * (1.0f - alpha);
             const float phx = r1.w, phy = r2.x;
             if (T > 0.5f && test_T <= 0.5f) {

@@ -69,23 +69,6 @@ __device__ __forceinline__ float depth_fast(float z, float dx, float phx, float 
     return depth_at(z, dx, phx, dy, phy);
 }
 
-// The conic's quadratic form v = a dx^2 + 2 b dx dy + c dy^2, evaluated as
-// dx * dl0 + dy * dl1 with dl0 = a dx + b dy, dl1 = b dx + c dy: the
-// gradient terms the Jacobian pass needs come for free.  Both passes use this
-// one expression, so their per-pixel accept / reject decisions agree.
-__device__ __forceinline__ float conic_form(float a, float b, float c, float dx, float dy, float& dl0, float& dl1) {
-    dl0 = __fmaf_rn(a, dx, __fmul_rn(b, dy));
-    dl1 = __fmaf_rn(b, dx, __fmul_rn(c, dy));
-    return __fmaf_rn(dx, dl0, __fmul_rn(dy, dl1));
-}
-
-// PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 __device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
                                              float r0, float r1, float r2) {
     // u = (a, d * (r x a))
