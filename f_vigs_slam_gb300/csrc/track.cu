@@ -709,7 +709,7 @@ __device__ __forceinline__ bool chol6(const double A[6][6], double L[6][6]) {
 // (src/RgbdPoseCost.cu:57-78).  When H - eps*I is positive definite every
 // eigenvalue is kept and the step is exactly -H^-1 g (Cholesky); otherwise a
 // cyclic Jacobi eigen-decomposition drops the small eigenvalues.
-__device__ void pseudo_step(const double H[6][6], const double g[6], double eps, double delta[6]) {
+__device__ __noinline__ void pseudo_step(const double H[6][6], const double g[6], double eps, double delta[6]) {
     double L[6][6];
     double He[6][6];
 #pragma unroll
@@ -801,6 +801,18 @@ __device__ void pseudo_step(const double H[6][6], const double g[6], double eps,
 
 __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(kFullMask, v, src); }
 
+// 1/x for finite positive x: the PTX rcp.approx.ftz.f64 estimate refined by
+// two Newton steps r += r (1 - x r), each doubling the correct bits, to within
+// an ulp or two of the correctly rounded reciprocal.  FP64 division is a long
+// dependent sequence on this part, and the factorisation and pose step below
+// are latency chains.
+__device__ __forceinline__ double rcp_newton(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    r = fma(r, fma(-x, r, 1.0), r);
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
 // Lower-triangle lane map: lane l < 21 holds entry (i, j), i >= j,
 // l = i (i + 1) / 2 + j.
 __device__ __forceinline__ int tri_index(int i, int j) { return i * (i + 1) / 2 + j; }
@@ -809,15 +821,17 @@ __device__ __forceinline__ int tri_index(int i, int j) { return i * (i + 1) / 2 
 // lower-triangle entry per lane (lanes >= 21 idle), without square roots: on
 // return lane tri_index(i, j) holds L[i][j] (i > j, unit diagonal implied) or
 // D[i] (i == j).  Returns false (uniformly) when a pivot is not positive, i.e.
-// the matrix is not positive definite.
-__device__ __forceinline__ bool warp_ldl6(double& m, int li, int lj) {
+// the matrix is not positive definite.  Lane k < 6 also ends with 1 / D[k]
+// in inv_d.
+__device__ __forceinline__ bool warp_ldl6(double& m, int li, int lj, double& inv_d) {
     const int lane = threadIdx.x & 31;
     const bool act = lane < 21;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const double dk = shfl_d(m, tri_index(k, k));
-        if (!(dk > 0.0)) return false;
-        const double inv = __drcp_rn(dk);
+        if (!(dk > 0.0 && dk <= 1e300)) return false;
+        const double inv = rcp_newton(dk);
+        if (lane == k) inv_d = inv;
         // entries still holding L(i, k) D(k) for i > k
         const double lik = shfl_d(m, (act && li > k) ? tri_index(li, k) : 0);
         const double ljk = shfl_d(m, (act && lj > k) ? tri_index(lj, k) : 0);
@@ -843,7 +857,7 @@ __device__ __forceinline__ bool warp_ldl6(double& m, int li, int lj) {
 // H and solves; only a failed test falls back to a one-thread Jacobi
 // eigen-decomposition that drops the small eigenvalues.
 constexpr int kRedCtas = 8;
-constexpr int kRedUnroll = 8;
+constexpr int kRedUnroll = 28;
 template <bool DO_GN>
 __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles, DevPose* pose, double* out,
@@ -859,25 +873,36 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int col = lane < FVGS_POSEDATA_FLOATS ? lane : 0;
     const int stride = kRedCtas * 8;
+    // the pose the step is applied to, loaded now so its latency overlaps the sums
+    float pq[4] = {0.f, 0.f, 0.f, 0.f};
+    double pqd[4] = {0.0, 0.0, 0.0, 0.0}, ptd[3] = {0.0, 0.0, 0.0};
+    if (DO_GN && rank == 0 && w == 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            pq[k] = pose->q[k];
+            pqd[k] = pose->qd[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ptd[k] = pose->td[k];
+    }
+    // every load of a round is issued before the (ordered) compensated adds
     float sum = 0.f, comp = 0.f;
-    int t = (int)rank * 8 + w;
-    for (; t + (kRedUnroll - 1) * stride < num_tiles; t += kRedUnroll * stride) {
+    for (int t0 = (int)rank * 8 + w; t0 < num_tiles; t0 += kRedUnroll * stride) {
         float x[kRedUnroll];
 #pragma unroll
-        for (int u = 0; u < kRedUnroll; ++u) x[u] = tile_out[(size_t)(t + u * stride) * FVGS_POSEDATA_FLOATS + col];
+        for (int u = 0; u < kRedUnroll; ++u) {
+            const int t = t0 + u * stride;
+            x[u] = t < num_tiles ? tile_out[(size_t)t * FVGS_POSEDATA_FLOATS + col] : 0.f;
+        }
 #pragma unroll
         for (int u = 0; u < kRedUnroll; ++u) {
-            const float y = __fsub_rn(x[u], comp);
-            const float s = __fadd_rn(sum, y);
-            comp = __fsub_rn(__fsub_rn(s, sum), y);
-            sum = s;
+            if (t0 + u * stride < num_tiles) {
+                const float y = __fsub_rn(x[u], comp);
+                const float s = __fadd_rn(sum, y);
+                comp = __fsub_rn(__fsub_rn(s, sum), y);
+                sum = s;
+            }
         }
-    }
-    for (; t < num_tiles; t += stride) {
-        const float y = __fsub_rn(tile_out[(size_t)t * FVGS_POSEDATA_FLOATS + col], comp);
-        const float s = __fadd_rn(sum, y);
-        comp = __fsub_rn(__fsub_rn(s, sum), y);
-        sum = s;
     }
     s_w[w][lane] = lane < FVGS_POSEDATA_FLOATS ? (double)sum - (double)comp : 0.0;
     __syncthreads();
@@ -961,13 +986,15 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     double m = lane < 21 ? Ac(li, lj) : 0.0;
     if (w == 0) {
         if (lane < 21 && li == lj) m -= eig_eps;
-        const bool pd = warp_ldl6(m, li, lj);
+        double inv_d;
+        const bool pd = warp_ldl6(m, li, lj, inv_d);
         if (lane == 0) s_pd = pd ? 1 : 0;
         asm volatile("bar.sync 1, 64;" ::: "memory");
         return;
     }
     // warp 1
-    const bool pdh = warp_ldl6(m, li, lj);
+    double inv_d = 0.0;
+    const bool pdh = warp_ldl6(m, li, lj, inv_d);
     asm volatile("bar.sync 1, 64;" ::: "memory");
     double xv = lane < 6 ? s_tot[lane] : 0.0;  // lane k < 6 ends with x[k]
     if (s_pd && pdh) {
@@ -979,8 +1006,7 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
             if (lane < 6 && lane > k) xv = fma(-lik, yk, xv);
         }
         // D z = y
-        const double dl = shfl_d(m, lane < 6 ? tri_index(lane, lane) : 0);
-        if (lane < 6) xv = xv / dl;
+        if (lane < 6) xv *= inv_d;
         // L^T x = z (unit upper)
 #pragma unroll
         for (int k = 5; k >= 0; --k) {
@@ -1010,7 +1036,7 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     for (int k = 0; k < 6; ++k) x[k] = shfl_d(xv, k);
     if (lane != 0) return;
     // delta = (R x_t, x_r), R of the pose the Jacobians were taken at
-    const double qx = pose->q[0], qy = pose->q[1], qz = pose->q[2], qw = pose->q[3];
+    const double qx = pq[0], qy = pq[1], qz = pq[2], qw = pq[3];
     const double R[3][3] = {
         {1.0 - 2.0 * (qy * qy + qz * qz), 2.0 * (qx * qy - qw * qz), 2.0 * (qx * qz + qw * qy)},
         {2.0 * (qx * qy + qw * qz), 1.0 - 2.0 * (qx * qx + qz * qz), 2.0 * (qy * qz - qw * qx)},
@@ -1021,14 +1047,23 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
 #pragma unroll
     for (int i = 3; i < 6; ++i) delta[i] = x[i];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) pose->td[k] += delta[k];
-    const double ax = pose->qd[0], ay = pose->qd[1], az = pose->qd[2], aw = pose->qd[3];
+    for (int k = 0; k < 3; ++k) {
+        ptd[k] += delta[k];
+        pose->td[k] = ptd[k];
+    }
+    const double ax = pqd[0], ay = pqd[1], az = pqd[2], aw = pqd[3];
     const double bx = 0.5 * delta[3], by = 0.5 * delta[4], bz = 0.5 * delta[5];
     double nx = aw * bx + ax + (ay * bz - az * by);
     double ny = aw * by + ay + (az * bx - ax * bz);
     double nz = aw * bz + az + (ax * by - ay * bx);
     double nw = aw - (ax * bx + ay * by + az * bz);
-    const double inn = 1.0 / sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+    // 1 / |n| by the FP32 estimate and two Newton steps r *= (3 - n2 r^2) / 2
+    // (about 2^-22, 2^-44, then rounding): the quaternion is within O(|delta|^2)
+    // of unit length, and FP64 square root and division are long chains here
+    const double n2 = nx * nx + ny * ny + nz * nz + nw * nw;
+    double inn = (double)rsqrtf((float)n2);
+    inn = inn * fma(-0.5 * n2, inn * inn, 1.5);
+    inn = inn * fma(-0.5 * n2, inn * inn, 1.5);
     nx *= inn;
     ny *= inn;
     nz *= inn;
@@ -1038,7 +1073,7 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     pose->qd[2] = nz;
     pose->qd[3] = nw;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) pose->t[k] = (float)pose->td[k];
+    for (int k = 0; k < 3; ++k) pose->t[k] = (float)ptd[k];
     pose->q[0] = (float)nx;
     pose->q[1] = (float)ny;
     pose->q[2] = (float)nz;
