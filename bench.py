@@ -517,10 +517,74 @@ def run_precision(args, fvgs, S, torch, dev, stream, world):
                                            "m": float(np.median([e[1] for e in errs]))},
                      "footprint_gb": sess.footprint() / 1e9}
     d = [S.pose_error(a, b) for a, b in zip(poses["reduced"], poses["fp32"])]
-    sess.close()
     out["workload"] = "room N=%d, 1280x720, 20 GN iterations per frame, map fixed" % n
     out["pose_difference_max"] = {"rad": float(max(e[0] for e in d)), "m": float(max(e[1] for e in d))}
     out["speedup_reduced_over_fp32"] = out["reduced"]["frames_per_s"] / out["fp32"]["frames_per_s"]
+    out["visual_inertial"] = run_visual_inertial(args, fvgs, S, torch, dev, stream, world, sess, K, W, H)
+    sess.close()
+    return out
+
+
+def run_visual_inertial(args, fvgs, S, torch, dev, stream, world, sess, K, W, H):
+    """The precision form's visual-inertial solve on the same map: a smooth
+    trajectory with 200 Hz IMU samples (gyroscope 1.7e-4 rad/s/sqrt(Hz),
+    accelerometer 2e-3 m/s^2/sqrt(Hz) white noise, constant sensor biases),
+    camera frames every 6 samples rendered at the true camera poses (+ the
+    colour / depth noise of the other workloads).  Per frame: preintegration,
+    prediction, 20 Gauss-Newton steps of the RGB-D factor + IMU factor +
+    marginalization prior (each on the GPU Jacobian at the current pose, the
+    15 / 30-dim normal equations in FP64 on the host), then marginalization.
+    Frames/s and the errors against the true trajectory, FP32 and reduced."""
+    from f_vigs_slam_gb300.vi import VisualInertialTracker
+
+    n_frames = args.warmup + args.steps + 1
+    ba, bg = np.array([0.05, -0.03, 0.04]), np.array([0.002, -0.001, 0.0015])
+    tr = S.imu_trajectory(n_frames, seed=31, acc_bias=ba, gyr_bias=bg,
+                          camera0=S.trajectory(1, seed=29)[0])
+    rng = np.random.default_rng(37)
+    sess.set_precision(fvgs.PRECISION_FP32)
+    dframes = []
+    for k in range(1, n_frames):
+        col, dep, _, _ = sess.render(tr["cam_pose"][k], K, W, H)
+        rgb, dd = S.add_noise(col, dep, rng)
+        gx, gy = S.sobel3(rgb)
+        dframes.append({k2: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+                        for k2, v in (("rgb", rgb), ("depth", dd), ("gx", gx), ("gy", gy))})
+    torch.cuda.synchronize()
+    M = tr["imu_per_frame"]
+    out, poses = {}, {}
+    for name, prec in (("fp32", fvgs.PRECISION_FP32), ("reduced", fvgs.PRECISION_REDUCED)):
+        sess.set_precision(prec)
+        vt = VisualInertialTracker(lambda cp: sess.track_jacobian(cp, K, 0), tr["t_imu_cam"], tr["q_imu_cam"],
+                                   tr["acc_sd"], tr["gyr_sd"], iterations=ITERS)
+        vt.start(tr["imu_pose"][0], np.concatenate([tr["imu_vel"][0], np.zeros(6)]), tr["acc"][0], tr["gyr"][0])
+        got, t_frames = [], []
+        for k in range(1, n_frames):
+            set_frame_tensors(fvgs, sess, 0, dframes[k - 1], W, H)
+            sl = slice((k - 1) * M + 1, k * M + 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pose, sb, _ = vt.track(tr["dt"], tr["acc"][sl], tr["gyr"][sl])
+            t_frames.append(time.perf_counter() - t0)
+            got.append((pose.copy(), sb.copy()))
+        timed = t_frames[args.warmup:]
+        ms = max_over_ranks([1e3 * float(np.sum(timed))], dev, world)[0]
+        errs = [S.pose_error((p[:3], p[3:]), (tr["imu_pose"][k][:3], tr["imu_pose"][k][3:]))
+                for k, (p, _) in enumerate(got, start=1)]
+        v_err = [float(np.linalg.norm(sb[:3] - tr["imu_vel"][k])) for k, (_, sb) in enumerate(got, start=1)]
+        poses[name] = got
+        out[name] = {"frames_per_s": replica_throughput(len(timed), world, ms), "ms_per_frame": ms / len(timed),
+                     "pose_error_median": {"rad": float(np.median([e[0] for e in errs])),
+                                           "m": float(np.median([e[1] for e in errs]))},
+                     "velocity_error_median_m_s": float(np.median(v_err)),
+                     "bias_error_last": {"acc": float(np.linalg.norm(got[-1][1][3:6] - ba)),
+                                         "gyr": float(np.linalg.norm(got[-1][1][6:9] - bg))}}
+    d = [S.pose_error((a[0][:3], a[0][3:]), (b[0][:3], b[0][3:])) for a, b in zip(poses["reduced"], poses["fp32"])]
+    out["pose_difference_max"] = {"rad": float(max(e[0] for e in d)), "m": float(max(e[1] for e in d))}
+    out["workload"] = ("same map; %d frames of a smooth trajectory, IMU 200 Hz (gyro 1.7e-4 rad/s/sqrt(Hz), "
+                       "accel 2e-3 m/s^2/sqrt(Hz), biases %s / %s), a frame every 6 samples; 20 GN steps of "
+                       "RGB-D + IMU + marginalization prior per frame, 15 / 30-dim FP64 solve on the host"
+                       % (n_frames - 1, ba.tolist(), bg.tolist()))
     return out
 
 

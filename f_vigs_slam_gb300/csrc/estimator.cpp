@@ -14,6 +14,9 @@
 //   MarginalizationInfo::marginalize / MarginalizationFactor::Evaluate,
 //     src/MarginalizationFactor.cpp:278-360,398-470 (eigen-thresholded Schur
 //     complement, prior residual with the quaternion local difference)
+//   the Ceres problem of GSSlam (src/GSSlam.cu:150-185, 2246-2290) and the
+//     end-of-frame marginalization (958-973), as Gauss-Newton steps over the
+//     15 / 30 local dimensions of the two states
 //
 // All of it stays FP64 on the host: these are the small dense solves the GPU
 // path hands its 6x6 system to.  Quaternions are (x, y, z, w) arrays, the
@@ -699,6 +702,200 @@ int fvgs_marginal_prior_evaluate(const double* J, const double* r, int n, int n_
             for (int i = 0; i < n; ++i)
                 for (int c = 0; c < size; ++c) Jb[i * size + c] = c < local ? J[i * n + idx + c] : 0.0;
         }
+    return FVGS_OK;
+}
+
+// --------------------------------------------------------------------------
+// Visual-inertial normal equations
+// --------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// The linearised factors of the two-state problem as one system over the 30
+// local dimensions [pose_i 6 | speedbias_i 9 | pose_j 6 | speedbias_j 9]:
+// A = sum J^T J, b = sum J^T r; the cost 0.5 sum |r|^2.
+int vi_system(fvgs_preint* P, const double* JtJ_imu, const double* Jtr_imu, double eps, const double* prior_J,
+              const double* prior_r, const double* prior_x0, const double* pose_i, const double* sb_i,
+              const double* pose_j, const double* sb_j, double A[900], double b[30], double* cost) {
+    const int N = 30;
+    for (int i = 0; i < N * N; ++i) A[i] = 0.0;
+    for (int i = 0; i < N; ++i) b[i] = 0.0;
+    double c = 0.0;
+    // rows of one factor: residual r (m) and its Jacobian over the 30 dims
+    auto add = [&](const double* r, const double* J, int m) {
+        for (int a = 0; a < N; ++a) {
+            double s = 0.0;
+            for (int k = 0; k < m; ++k) s += J[k * N + a] * r[k];
+            b[a] += s;
+            for (int d = a; d < N; ++d) {
+                double t = 0.0;
+                for (int k = 0; k < m; ++k) t += J[k * N + a] * J[k * N + d];
+                A[a * N + d] += t;
+                if (d != a) A[d * N + a] += t;
+            }
+        }
+        for (int k = 0; k < m; ++k) c += r[k] * r[k];
+    };
+    // RGB-D pseudo factor on pose_j
+    {
+        double rs[6], Js[36];
+        const int st = fvgs_pseudo_factor(JtJ_imu, Jtr_imu, eps, rs, Js);
+        if (st != FVGS_OK) return st;
+        std::vector<double> J(6 * N, 0.0);
+        for (int k = 0; k < 6; ++k)
+            for (int d = 0; d < 6; ++d) J[k * N + 15 + d] = Js[k * 6 + d];
+        add(rs, J.data(), 6);
+    }
+    // IMU factor between i and j
+    {
+        double r[15], Jpi[105], Jsi[135], Jpj[105], Jsj[135];
+        const int st = fvgs_imu_factor(P, pose_i, sb_i, pose_j, sb_j, r, Jpi, Jsi, Jpj, Jsj);
+        if (st != FVGS_OK) return st;
+        std::vector<double> J(15 * N, 0.0);
+        for (int k = 0; k < 15; ++k) {
+            for (int d = 0; d < 6; ++d) {
+                J[k * N + d] = Jpi[k * 7 + d];
+                J[k * N + 15 + d] = Jpj[k * 7 + d];
+            }
+            for (int d = 0; d < 9; ++d) {
+                J[k * N + 6 + d] = Jsi[k * 9 + d];
+                J[k * N + 21 + d] = Jsj[k * 9 + d];
+            }
+        }
+        add(r, J.data(), 15);
+    }
+    // marginalization prior on state i
+    if (prior_J) {
+        const int bs[2] = {7, 9}, bi[2] = {0, 6};
+        const double* x[2] = {pose_i, sb_i};
+        const double* x0[2] = {prior_x0, prior_x0 + 7};
+        double r[15], Jp[105], Js[135];
+        double* jac[2] = {Jp, Js};
+        const int st = fvgs_marginal_prior_evaluate(prior_J, prior_r, 15, 2, bs, bi, x, x0, r, jac);
+        if (st != FVGS_OK) return st;
+        std::vector<double> J(15 * N, 0.0);
+        for (int k = 0; k < 15; ++k) {
+            for (int d = 0; d < 6; ++d) J[k * N + d] = Jp[k * 7 + d];
+            for (int d = 0; d < 9; ++d) J[k * N + 6 + d] = Js[k * 9 + d];
+        }
+        add(r, J.data(), 15);
+    }
+    if (cost) *cost = 0.5 * c;
+    return FVGS_OK;
+}
+
+// x = -A^-1 b for symmetric A (n x n): Cholesky, or the eigen-thresholded
+// pseudo-inverse (eigenvalues above 1e-12 of the largest) if A is not
+// positive definite.
+void solve_spd(const double* A, const double* b, int n, double* x) {
+    std::vector<double> L((size_t)n * n, 0.0);
+    bool pd = true;
+    for (int j = 0; j < n && pd; ++j) {
+        double s = A[j * n + j];
+        for (int k = 0; k < j; ++k) s -= L[j * n + k] * L[j * n + k];
+        if (!(s > 0.0)) {
+            pd = false;
+            break;
+        }
+        const double ljj = std::sqrt(s);
+        L[j * n + j] = ljj;
+        for (int i = j + 1; i < n; ++i) {
+            double t = A[i * n + j];
+            for (int k = 0; k < j; ++k) t -= L[i * n + k] * L[j * n + k];
+            L[i * n + j] = t / ljj;
+        }
+    }
+    if (pd) {
+        std::vector<double> y(n);
+        for (int i = 0; i < n; ++i) {
+            double s = b[i];
+            for (int k = 0; k < i; ++k) s -= L[i * n + k] * y[k];
+            y[i] = s / L[i * n + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double s = y[i];
+            for (int k = i + 1; k < n; ++k) s -= L[k * n + i] * x[k];
+            x[i] = s / L[i * n + i];
+        }
+        for (int i = 0; i < n; ++i) x[i] = -x[i];
+        return;
+    }
+    std::vector<double> w(n), V((size_t)n * n);
+    sym_eig(A, n, w.data(), V.data());
+    const double wmax = w[n - 1];
+    for (int i = 0; i < n; ++i) x[i] = 0.0;
+    for (int k = 0; k < n; ++k) {
+        if (!(w[k] > 1e-12 * wmax)) continue;
+        double proj = 0.0;
+        for (int i = 0; i < n; ++i) proj += V[i * n + k] * b[i];
+        for (int i = 0; i < n; ++i) x[i] -= V[i * n + k] * proj / w[k];
+    }
+}
+
+// PoseLocalParameterization::Plus: p + dp, (q (x) [dtheta / 2, 1]) normalised.
+void pose_plus(double* pose, const double* d) {
+    for (int k = 0; k < 3; ++k) pose[k] += d[k];
+    const Quat q = q4(pose + 3);
+    const Quat dq = {0.5 * d[3], 0.5 * d[4], 0.5 * d[5], 1.0};
+    const Quat n = qnormalized(qmul(q, dq));
+    pose[3] = n.x, pose[4] = n.y, pose[5] = n.z, pose[6] = n.w;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fvgs_vi_step(fvgs_preint* P, const double JtJ_imu[36], const double Jtr_imu[6], double eps,
+                 const double* prior_J, const double* prior_r, const double* prior_x0, double pose_i[7],
+                 double speedbias_i[9], double pose_j[7], double speedbias_j[9], double* cost, double delta[30]) {
+    if (!P || !JtJ_imu || !Jtr_imu || !pose_i || !speedbias_i || !pose_j || !speedbias_j) return FVGS_E_INVALID;
+    if (prior_J && (!prior_r || !prior_x0)) return FVGS_E_INVALID;
+    double A[900], b[30];
+    const int st = vi_system(P, JtJ_imu, Jtr_imu, eps, prior_J, prior_r, prior_x0, pose_i, speedbias_i, pose_j,
+                             speedbias_j, A, b, cost);
+    if (st != FVGS_OK) return st;
+    double d[30] = {};
+    if (prior_J) {
+        solve_spd(A, b, 30, d);
+    } else {
+        // state i fixed: the 15-dim system of state j
+        double Aj[225], bj[15], dj[15];
+        for (int r = 0; r < 15; ++r) {
+            bj[r] = b[15 + r];
+            for (int c = 0; c < 15; ++c) Aj[r * 15 + c] = A[(15 + r) * 30 + 15 + c];
+        }
+        solve_spd(Aj, bj, 15, dj);
+        for (int k = 0; k < 15; ++k) d[15 + k] = dj[k];
+    }
+    for (int k = 0; k < 30; ++k)
+        if (!std::isfinite(d[k])) return FVGS_E_STATE;
+    if (prior_J) {
+        pose_plus(pose_i, d);
+        for (int k = 0; k < 9; ++k) speedbias_i[k] += d[6 + k];
+    }
+    pose_plus(pose_j, d + 15);
+    for (int k = 0; k < 9; ++k) speedbias_j[k] += d[21 + k];
+    if (delta) std::memcpy(delta, d, sizeof(d));
+    return FVGS_OK;
+}
+
+int fvgs_vi_marginalize(fvgs_preint* P, const double JtJ_imu[36], const double Jtr_imu[6], double eps,
+                        const double* prior_J, const double* prior_r, const double* prior_x0,
+                        const double pose_i[7], const double speedbias_i[9], const double pose_j[7],
+                        const double speedbias_j[9], double new_J[225], double new_r[15], double new_x0[16]) {
+    if (!P || !JtJ_imu || !Jtr_imu || !pose_i || !speedbias_i || !pose_j || !speedbias_j || !new_J || !new_r ||
+        !new_x0)
+        return FVGS_E_INVALID;
+    if (prior_J && (!prior_r || !prior_x0)) return FVGS_E_INVALID;
+    double A[900], b[30];
+    const int st = vi_system(P, JtJ_imu, Jtr_imu, eps, prior_J, prior_r, prior_x0, pose_i, speedbias_i, pose_j,
+                             speedbias_j, A, b, nullptr);
+    if (st != FVGS_OK) return st;
+    const int ms = fvgs_marginalize(A, b, 15, 15, 1e-8, new_J, new_r);
+    if (ms != FVGS_OK) return ms;
+    std::memcpy(new_x0, pose_j, 7 * sizeof(double));
+    std::memcpy(new_x0 + 7, speedbias_j, 9 * sizeof(double));
     return FVGS_OK;
 }
 

@@ -711,3 +711,41 @@ def marginal_prior_evaluate(J, r, blocks, x, x0, jacobians=True):
     _check(load_library().fvgs_marginal_prior_evaluate(_ptr(J), _ptr(r), C.c_int(n), C.c_int(k), sizes, idx, xp, x0p,
                                                        _ptr(res), jp), "fvgs_marginal_prior_evaluate")
     return (res, jac) if jacobians else res
+
+
+def _prior_args(prior):
+    if prior is None:
+        return None, None, None, ()
+    J, r, x0 = _d(prior[0], 225), _d(prior[1], 15), _d(prior[2], 16)
+    return _ptr(J), _ptr(r), _ptr(x0), (J, r, x0)
+
+
+def vi_step(preint, JtJ_imu, Jtr_imu, state_i, state_j, prior=None, eps=1e-4):
+    """fvgs_vi_step: one Gauss-Newton step of the visual-inertial problem.
+
+    state_* = (pose [7: p, q x y z w], speedbias [9]); prior = (J 15x15, r 15,
+    x0 16) on state i or None (state i fixed).  Returns the updated
+    (state_i, state_j), the cost before the step and the 30 local increments."""
+    pi, si = _d(state_i[0], 7).copy(), _d(state_i[1], 9).copy()
+    pj, sj = _d(state_j[0], 7).copy(), _d(state_j[1], 9).copy()
+    Jp, rp, xp, keep = _prior_args(prior)
+    cost = C.c_double()
+    delta = np.zeros(30)
+    _check(load_library().fvgs_vi_step(preint.h, _ptr(_d(JtJ_imu, 36)), _ptr(_d(Jtr_imu, 6)), C.c_double(eps), Jp,
+                                       rp, xp, _ptr(pi), _ptr(si), _ptr(pj), _ptr(sj), C.byref(cost), _ptr(delta)),
+           "fvgs_vi_step")
+    del keep
+    return (pi, si), (pj, sj), cost.value, delta
+
+
+def vi_marginalize(preint, JtJ_imu, Jtr_imu, state_i, state_j, prior=None, eps=1e-4):
+    """fvgs_vi_marginalize: the prior (J 15x15, r 15, x0 16) on state j for the next frame."""
+    Jp, rp, xp, keep = _prior_args(prior)
+    J, r, x0 = np.zeros((15, 15)), np.zeros(15), np.zeros(16)
+    _check(load_library().fvgs_vi_marginalize(preint.h, _ptr(_d(JtJ_imu, 36)), _ptr(_d(Jtr_imu, 6)),
+                                              C.c_double(eps), Jp, rp, xp, _ptr(_d(state_i[0], 7)),
+                                              _ptr(_d(state_i[1], 9)), _ptr(_d(state_j[0], 7)),
+                                              _ptr(_d(state_j[1], 9)), _ptr(J), _ptr(r), _ptr(x0)),
+           "fvgs_vi_marginalize")
+    del keep
+    return J, r, x0

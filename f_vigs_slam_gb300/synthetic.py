@@ -159,6 +159,101 @@ def trajectory(n_poses: int, seed: int = 0, step_cm: float = 1.0, step_deg: floa
     return out
 
 
+def qlog(q):
+    """Rotation vector of the unit quaternion q = (x, y, z, w)."""
+    q = np.asarray(q, np.float64)
+    if q[3] < 0:
+        q = -q
+    s = float(np.linalg.norm(q[:3]))
+    if s < 1e-15:
+        return 2.0 * q[:3]
+    return q[:3] * (2.0 * np.arctan2(s, q[3]) / s)
+
+
+GRAVITY = np.array([0.0, 0.0, 9.81])
+
+
+def imu_trajectory(n_frames: int, seed: int = 0, imu_rate: float = 200.0, imu_per_frame: int = 6,
+                   t_imu_cam=(0.02, -0.01, 0.005), q_imu_cam=(0.0, 0.0, 0.0, 1.0), acc_n: float = 2e-3,
+                   gyr_n: float = 1.7e-4, noise: bool = True, camera0=None, acc_bias=(0.0, 0.0, 0.0),
+                   gyr_bias=(0.0, 0.0, 0.0)):
+    """A smooth visual-inertial trajectory with IMU samples.
+
+    The IMU body moves as P(t) = P0 + a_p sin(2 pi f_p t + phi_p) and
+    Q(t) = Q0 exp(a_r sin(2 pi f_r t + phi_r)) (per-axis amplitudes and
+    frequencies drawn from the seed).  Samples come at `imu_rate` Hz: the
+    gyroscope reads the body angular rate (central difference of Q), the
+    accelerometer R(t)^T (P''(t) + g) with g = (0, 0, 9.81), the
+    preintegration's convention, both plus constant biases; with `noise`,
+    white noise of the given densities (std density * sqrt(rate)) is added.  Camera frames come every
+    `imu_per_frame` samples; the camera pose is P + Q t_imu_cam,
+    Q q_imu_cam, starting at `camera0` (t, q) (default: the origin, identity).
+
+    Returns a dict: frame times, IMU poses (7 doubles: p, q x y z w) and
+    velocities at the frames, camera poses (float32 t, q) at the frames, the
+    IMU sample times, accelerometer and gyroscope arrays, and the discrete
+    noise standard deviations."""
+    rng = np.random.default_rng(seed + 4241)
+    t_ic = np.asarray(t_imu_cam, np.float64)
+    q_ic = np.asarray(q_imu_cam, np.float64)
+    q_ic_inv = np.array([-q_ic[0], -q_ic[1], -q_ic[2], q_ic[3]])
+    if camera0 is None:
+        camera0 = (np.zeros(3), IDENTITY_Q)
+    Qc0 = np.asarray(camera0[1], np.float64)
+    Q0 = qmul(Qc0, q_ic_inv)
+    P0 = np.asarray(camera0[0], np.float64) - qrot(Q0) @ t_ic
+    a_p = rng.uniform(0.02, 0.06, 3)
+    f_p = rng.uniform(0.3, 0.8, 3)
+    ph_p = rng.uniform(0, 2 * np.pi, 3)
+    a_r = rng.uniform(0.01, 0.04, 3)
+    f_r = rng.uniform(0.3, 0.8, 3)
+    ph_r = rng.uniform(0, 2 * np.pi, 3)
+
+    def pos(t):
+        return P0 + a_p * np.sin(2 * np.pi * f_p * t + ph_p)
+
+    def vel(t):
+        return a_p * 2 * np.pi * f_p * np.cos(2 * np.pi * f_p * t + ph_p)
+
+    def accel(t):
+        return -a_p * (2 * np.pi * f_p) ** 2 * np.sin(2 * np.pi * f_p * t + ph_p)
+
+    def rot(t):
+        q = qmul(Q0, qexp(a_r * np.sin(2 * np.pi * f_r * t + ph_r)))
+        return q / np.linalg.norm(q)
+
+    def omega(t, h=1e-5):
+        qa, qb = rot(t - h), rot(t + h)
+        return qlog(qmul(np.array([-qa[0], -qa[1], -qa[2], qa[3]]), qb)) / (2 * h)
+
+    dt = 1.0 / imu_rate
+    n_imu = (n_frames - 1) * imu_per_frame + 1
+    imu_t = np.arange(n_imu) * dt
+    acc = np.zeros((n_imu, 3))
+    gyr = np.zeros((n_imu, 3))
+    for k, t in enumerate(imu_t):
+        acc[k] = qrot(rot(t)).T @ (accel(t) + GRAVITY)
+        gyr[k] = omega(t)
+    acc += np.asarray(acc_bias, np.float64)
+    gyr += np.asarray(gyr_bias, np.float64)
+    acc_sd, gyr_sd = acc_n * np.sqrt(imu_rate), gyr_n * np.sqrt(imu_rate)
+    if noise:
+        acc += rng.normal(0.0, acc_sd, acc.shape)
+        gyr += rng.normal(0.0, gyr_sd, gyr.shape)
+    frame_t = imu_t[::imu_per_frame]
+    imu_pose, imu_vel, cam_pose = [], [], []
+    for t in frame_t:
+        P, Q = pos(t), rot(t)
+        imu_pose.append(np.concatenate([P, Q]))
+        imu_vel.append(vel(t))
+        Pc = P + qrot(Q) @ t_ic
+        Qc = qmul(Q, q_ic)
+        cam_pose.append((Pc.astype(np.float32), (Qc / np.linalg.norm(Qc)).astype(np.float32)))
+    return dict(frame_t=frame_t, imu_pose=imu_pose, imu_vel=imu_vel, cam_pose=cam_pose, imu_t=imu_t, acc=acc,
+                gyr=gyr, imu_per_frame=imu_per_frame, dt=dt, acc_sd=acc_sd, gyr_sd=gyr_sd, t_imu_cam=t_ic,
+                q_imu_cam=q_ic)
+
+
 def sobel3(img: np.ndarray):
     """3x3 Sobel derivatives of an (H, W, C) float image with reflect-101
     borders, as cv::Sobel(src, dst, CV_32F, 1, 0, 3) / (0, 1, 3) computes them

@@ -96,6 +96,40 @@ int fvgs_marginal_prior_evaluate(const double* J, const double* r, int n, int n_
                                  const int* block_idx, const double* const* x, const double* const* x0,
                                  double* residual, double* const* jacobians);
 
+/*
+ * One Gauss-Newton step of the visual-inertial problem the reference gives
+ * Ceres (GSSlam constructor, src/GSSlam.cu:150-185; optimizeWithCeres,
+ * src/GSSlam.cu:2246-2290): the RGB-D pseudo factor on pose_j (from the
+ * IMU-frame JtJ / Jtr of fvgs_jacobian_cam_to_imu, eigenvalues above eps
+ * kept), the IMU factor between states i and j, and, when prior_J is given,
+ * the marginalization prior on state i (prior_J 15x15, prior_r 15, its
+ * linearisation point prior_x0 = pose 7 + speed-bias 9).  Without a prior
+ * state i is held fixed and the normal equations are the 15-dim ones of
+ * state j; with it both states move (30 dims: pose_i, speedbias_i, pose_j,
+ * speedbias_j in local coordinates).  The system is solved in FP64
+ * (Cholesky; an eigen-thresholded pseudo-inverse if it is not positive
+ * definite) and the step applied as PoseLocalParameterization::Plus
+ * (src/PoseLocalParameterization.cpp:22-44: p + dp, (q (x) [dtheta/2, 1])
+ * normalised) and additively for the speed-bias blocks.  cost (may be null)
+ * receives 0.5 (|r*|^2 + |r_imu|^2 + |r_prior|^2) before the step; delta (may
+ * be null) the 30 local increments (zeros for a fixed state i).
+ */
+int fvgs_vi_step(fvgs_preint* p, const double JtJ_imu[36], const double Jtr_imu[6], double eps,
+                 const double* prior_J, const double* prior_r, const double* prior_x0, double pose_i[7],
+                 double speedbias_i[9], double pose_j[7], double speedbias_j[9], double* cost, double delta[30]);
+/*
+ * The prior the next frame starts from (the marginalization at the end of a
+ * tracked frame, src/GSSlam.cu:958-973 with MarginalizationInfo): every
+ * factor of fvgs_vi_step linearised at the given states, state i (15 local
+ * dims) marginalised by fvgs_marginalize (threshold 1e-8): new_J 15x15,
+ * new_r 15 on state j, new_x0 = (pose_j, speedbias_j).  The outputs may
+ * alias the prior inputs: those are read before any output is written.
+ */
+int fvgs_vi_marginalize(fvgs_preint* p, const double JtJ_imu[36], const double Jtr_imu[6], double eps,
+                        const double* prior_J, const double* prior_r, const double* prior_x0,
+                        const double pose_i[7], const double speedbias_i[9], const double pose_j[7],
+                        const double speedbias_j[9], double new_J[225], double new_r[15], double new_x0[16]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -270,3 +270,169 @@ def test_marginal_prior_evaluate(fv):
     _close(jac[0][:, :6], J[:, :6])
     assert np.all(jac[0][:, 6] == 0.0)
     _close(jac[1], J[:, 6:])
+
+
+# ---------------------------------------------------------------------------
+# visual-inertial normal equations (fvgs_vi_step / fvgs_vi_marginalize)
+# ---------------------------------------------------------------------------
+def _local_error(pose, ref):
+    """(p - p_ref, 2 vec(q_ref^-1 q)): the local coordinates of the pose Plus."""
+    d = E.qmul(E.qinv(ref[3:]), pose[3:])
+    s = 2.0 if d[3] >= 0 else -2.0
+    return np.concatenate([pose[:3] - ref[:3], s * d[:3]])
+
+
+def _vi_case(fv, seed, noise=True):
+    from f_vigs_slam_gb300 import synthetic as S
+
+    tr = S.imu_trajectory(4, seed=seed, noise=noise)
+    M = tr["imu_per_frame"]
+    pre = fv.Preintegration(tr["acc"][0], tr["gyr"][0], np.zeros(3), np.zeros(3), tr["acc_sd"], tr["gyr_sd"], 1e-4,
+                            1e-5)
+    for m in range(1, M + 1):
+        pre.add(tr["dt"], tr["acc"][m], tr["gyr"][m])
+    rng = np.random.default_rng(seed)
+    sb_i = np.concatenate([tr["imu_vel"][0], rng.normal(0, 0.01, 3), rng.normal(0, 0.001, 3)])
+    pose_j, vj = pre.predict(tr["imu_pose"][0], tr["imu_vel"][0])
+    pose_j[:3] += rng.normal(0, 0.01, 3)
+    sb_j = np.concatenate([vj + rng.normal(0, 0.02, 3), sb_i[3:]])
+    # a visual system pulling pose_j to the true pose: JtJ SPD, Jtr = JtJ e
+    Q, _ = np.linalg.qr(rng.normal(size=(6, 6)))
+    JtJ = Q @ np.diag(10.0 ** rng.uniform(4, 8, 6)) @ Q.T
+    Jtr = JtJ @ _local_error(pose_j, tr["imu_pose"][1])
+    return tr, pre, (tr["imu_pose"][0].copy(), sb_i), (pose_j, sb_j), JtJ, Jtr
+
+
+def _prior(fv, seed):
+    rng = np.random.default_rng(seed + 5)
+    A = rng.normal(size=(30, 30))
+    A = A @ A.T + 30 * np.eye(30)
+    J, r = fv.marginalize(A, rng.normal(size=30), 15)
+    return J, r
+
+
+def _expected_step(fv, pre, JtJ, Jtr, si, sj, prior):
+    """The normal equations assembled in NumPy from the library's own factor
+    evaluations: H = sum J^T J, g = sum J^T r over the free local dims."""
+    cols = []
+    rs, Js = fv.pseudo_factor(JtJ, Jtr, 1e-4)
+    Jv = np.zeros((6, 30))
+    Jv[:, 15:21] = Js
+    r_imu, (Jpi, Jsi, Jpj, Jsj) = pre.factor(si[0], si[1], sj[0], sj[1])
+    Ji = np.zeros((15, 30))
+    Ji[:, 0:6], Ji[:, 6:15], Ji[:, 15:21], Ji[:, 21:30] = Jpi[:, :6], Jsi, Jpj[:, :6], Jsj
+    rows = [(rs, Jv), (r_imu, Ji)]
+    if prior is not None:
+        res, (Jp, Jb) = fv.marginal_prior_evaluate(prior[0], prior[1], [(7, 0), (9, 6)], [si[0], si[1]],
+                                                   [prior[2][:7], prior[2][7:]])
+        Jr = np.zeros((15, 30))
+        Jr[:, 0:6], Jr[:, 6:15] = Jp[:, :6], Jb
+        rows.append((res, Jr))
+    H = sum(J.T @ J for _, J in rows)
+    g = sum(J.T @ r for r, J in rows)
+    cost = 0.5 * sum(float(r @ r) for r, _ in rows)
+    free = np.arange(30) if prior is not None else np.arange(15, 30)
+    d = np.zeros(30)
+    Hf, gf = H[np.ix_(free, free)], g[free]
+    d[free] = -np.linalg.solve(Hf, gf)
+    return d, cost, (free, Hf, gf)
+
+
+def _plus(pose, d):
+    q = E.qmul(pose[3:], np.array([0.5 * d[3], 0.5 * d[4], 0.5 * d[5], 1.0]))
+    return np.concatenate([pose[:3] + d[:3], q / np.linalg.norm(q)])
+
+
+@pytest.mark.parametrize("with_prior", [False, True])
+def test_vi_step_solves_the_normal_equations(fv, with_prior):
+    """fvgs_vi_step = the Gauss-Newton step of {RGB-D pseudo factor, IMU
+    factor, marginalization prior}: 15 free dims (state i fixed) or 30."""
+    tr, pre, si, sj, JtJ, Jtr = _vi_case(fv, 11)
+    prior = None
+    if with_prior:
+        J, r = _prior(fv, 11)
+        x0 = np.concatenate([si[0], si[1]]).copy()
+        x0[:3] += 0.003  # linearised away from the current state
+        prior = (J, r, x0)
+    want, want_cost, (free, Hf, gf) = _expected_step(fv, pre, JtJ, Jtr, si, sj, prior)
+    (pi2, si2), (pj2, sj2), cost, d = fv.vi_step(pre, JtJ, Jtr, si, sj, prior)
+    # the step solves the normal equations (relative residual at FP64 level),
+    # and equals NumPy's solution to the system's conditioning
+    assert np.linalg.norm(Hf @ d[free] + gf) <= 1e-9 * np.linalg.norm(gf)
+    cond = np.linalg.cond(Hf)
+    np.testing.assert_allclose(d, want, rtol=0, atol=max(1e-12, 1e-15 * cond) * np.abs(want).max())
+    assert abs(cost - want_cost) <= 1e-10 * want_cost
+    np.testing.assert_allclose(pj2, _plus(sj[0], d[15:21]), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sj2, sj[1] + d[21:30], rtol=0, atol=1e-12)
+    if with_prior:
+        np.testing.assert_allclose(pi2, _plus(si[0], d[0:6]), rtol=0, atol=1e-12)
+        np.testing.assert_allclose(si2, si[1] + d[6:15], rtol=0, atol=1e-12)
+    else:
+        assert np.all(d[:15] == 0) and np.array_equal(pi2, si[0]) and np.array_equal(si2, si[1])
+
+
+def test_vi_marginalize_is_the_schur_complement(fv):
+    tr, pre, si, sj, JtJ, Jtr = _vi_case(fv, 12)
+    J0, r0 = _prior(fv, 12)
+    prior = (J0, r0, np.concatenate([si[0], si[1]]))
+    J, r, x0 = fv.vi_marginalize(pre, JtJ, Jtr, si, sj, prior)
+    # expected: the same linearised system, state i marginalised
+    rows = []
+    rs, Js = fv.pseudo_factor(JtJ, Jtr, 1e-4)
+    Jv = np.zeros((6, 30))
+    Jv[:, 15:21] = Js
+    r_imu, (Jpi, Jsi, Jpj, Jsj) = pre.factor(si[0], si[1], sj[0], sj[1])
+    Ji = np.zeros((15, 30))
+    Ji[:, 0:6], Ji[:, 6:15], Ji[:, 15:21], Ji[:, 21:30] = Jpi[:, :6], Jsi, Jpj[:, :6], Jsj
+    res, (Jp, Jb) = fv.marginal_prior_evaluate(J0, r0, [(7, 0), (9, 6)], [si[0], si[1]], [prior[2][:7], prior[2][7:]])
+    Jr = np.zeros((15, 30))
+    Jr[:, 0:6], Jr[:, 6:15] = Jp[:, :6], Jb
+    for rr, JJ in ((rs, Jv), (r_imu, Ji), (res, Jr)):
+        rows.append((rr, JJ))
+    A = sum(JJ.T @ JJ for _, JJ in rows)
+    b = sum(JJ.T @ rr for rr, JJ in rows)
+    As = A[15:, 15:] - A[15:, :15] @ np.linalg.solve(A[:15, :15], A[:15, 15:])
+    bs = b[15:] - A[15:, :15] @ np.linalg.solve(A[:15, :15], b[:15])
+    np.testing.assert_allclose(J.T @ J, As, rtol=0, atol=1e-8 * np.abs(As).max())
+    np.testing.assert_allclose(J.T @ r, bs, rtol=0, atol=1e-8 * max(1.0, np.abs(bs).max()))
+    np.testing.assert_array_equal(x0, np.concatenate([sj[0], sj[1]]))
+
+
+def test_vi_tracker_converges_on_a_synthetic_trajectory(fv):
+    """The tracking loop (preintegrate, predict, 20 Gauss-Newton steps,
+    marginalise) on noisy 200 Hz IMU data with constant sensor biases and a
+    visual system of the RGB-D system's magnitude pinning the camera pose: the
+    IMU-frame pose follows the truth, the velocity stays on it, and the bias
+    estimates (started at zero) converge towards the true biases."""
+    from f_vigs_slam_gb300 import synthetic as S
+    from f_vigs_slam_gb300.vi import VisualInertialTracker
+
+    ba, bg = np.array([0.05, -0.03, 0.04]), np.array([0.002, -0.001, 0.0015])
+    tr = S.imu_trajectory(16, seed=3, acc_bias=ba, gyr_bias=bg)
+    truth = {}
+
+    def visual(cam_pose):
+        # camera-frame system pulling the camera to the frame's true camera pose
+        t_true, q_true = truth["cam"]
+        e = np.concatenate([np.asarray(cam_pose[0], np.float64) - t_true,
+                            _local_error(np.concatenate([[0, 0, 0], np.asarray(cam_pose[1], np.float64)]),
+                                         np.concatenate([[0, 0, 0], np.asarray(q_true, np.float64)]))[3:]])
+        JtJ = np.diag([1e12, 1e12, 1e12, 1e11, 1e11, 1e11])
+        return JtJ, JtJ @ e
+
+    vt = VisualInertialTracker(visual, tr["t_imu_cam"], tr["q_imu_cam"], tr["acc_sd"], tr["gyr_sd"])
+    M = tr["imu_per_frame"]
+    vt.start(tr["imu_pose"][0], np.concatenate([tr["imu_vel"][0], np.zeros(6)]), tr["acc"][0], tr["gyr"][0])
+    ba_err, bg_err = [], []
+    for k in range(1, len(tr["frame_t"])):
+        t_c, q_c = tr["cam_pose"][k]
+        truth["cam"] = (np.asarray(t_c, np.float64), np.asarray(q_c, np.float64))
+        sl = slice((k - 1) * M + 1, k * M + 1)
+        pose, sb, costs = vt.track(tr["dt"], tr["acc"][sl], tr["gyr"][sl])
+        ang, dist = S.pose_error((pose[:3], pose[3:]), (tr["imu_pose"][k][:3], tr["imu_pose"][k][3:]))
+        assert ang < 1e-5 and dist < 1e-5, (k, ang, dist)
+        assert np.linalg.norm(sb[:3] - tr["imu_vel"][k]) < 5e-3
+        assert costs[-1] < costs[0]
+        ba_err.append(float(np.linalg.norm(sb[3:6] - ba)))
+        bg_err.append(float(np.linalg.norm(sb[6:9] - bg)))
+    assert ba_err[-1] < 0.2 * ba_err[0] and bg_err[-1] < 0.3 * bg_err[0], (ba_err, bg_err)
