@@ -211,7 +211,7 @@ struct TrackArgs {
     int variant;
     uint32_t* st_flags;  // status word for bounded-wait timeouts (variant 2)
 };
-constexpr int kTrackVariants = 3;
+constexpr int kTrackVariants = 5;
 // Tensor maps of the three record planes (2-D: 4 floats x capacity rows,
 // 16-byte rows, one-row boxes) for the TMA-staged variant.
 struct RecMaps {

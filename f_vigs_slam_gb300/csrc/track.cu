@@ -175,18 +175,19 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
 // sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list;
 // for the Jacobian pass also sE = (rgx, rgy, -fx rgx, -fy rgy), the mean's
 // normalised ray and the third row of the projection Jacobian without 1/d.
+template <int BATCH = kBatch>
 struct TrackBatch {
-    float4 A[kBatch];
-    float4 B[kBatch];
-    float4 C[kBatch];
-    float4 E[kBatch];
-    float D[kBatch];
-    int orig[kBatch];
+    float4 A[BATCH];
+    float4 B[BATCH];
+    float4 C[BATCH];
+    float4 E[BATCH];
+    float D[BATCH];
+    int orig[BATCH];
     int wcnt[kPix / 32];
 };
 
-template <bool FORWARD>
-__device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch& sb, int pos, const float4& r0,
+template <bool FORWARD, int BATCH>
+__device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH>& sb, int pos, const float4& r0,
                                            const float4& r1, const float4& r2, float vrej, int li) {
     sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
     sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
@@ -199,36 +200,44 @@ __device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch& sb, i
     }
 }
 
-// Stage entries [base, min(base+256, limit)) of the tile's list, dropping the
-// ones tile_prunable rejects; returns the number kept.  Ends with a barrier.
-template <bool REF_LAYOUT, bool FORWARD>
-__device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch& sb, uint32_t list0, int base, int limit,
-                                           float x0, float y0) {
+// Stage entries [base, min(base+BATCH, limit)) of the tile's list, dropping
+// the ones tile_prunable rejects; returns the number kept.  The CTA takes the
+// entries 256 at a time (one per thread; BATCH = 128 uses half the threads),
+// each round compacted after the previous one, so the staged order is the
+// list order.  Ends with a barrier.
+template <bool REF_LAYOUT, bool FORWARD, int BATCH = kBatch>
+__device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH>& sb, uint32_t list0, int base,
+                                           int limit, float x0, float y0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int li = base + tid;
-    bool keep = false;
-    float4 r0, r1, r2;
-    float vrej = 0.f;
-    if (li < limit) {
-        const uint32_t g = a.indices[list0 + li];
-        if (g < a.n_gauss) {
-            load_record<REF_LAYOUT>(a, g, r0, r1, r2);
-            vrej = reject_bound(r0.w);
-            keep = !tile_prunable<FORWARD>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
-        }
-    }
-    const uint32_t bal = __ballot_sync(kFullMask, keep);
-    if (lane == 0) sb.wcnt[w] = __popc(bal);
-    __syncthreads();
-    int wbase = 0, total = 0;
+    int total = 0;
 #pragma unroll
-    for (int k = 0; k < kPix / 32; ++k) {
-        const int c = sb.wcnt[k];
-        wbase += (k < w) ? c : 0;
-        total += c;
+    for (int r0 = 0; r0 < BATCH; r0 += kPix) {
+        const int li = base + r0 + tid;
+        bool keep = false;
+        float4 r0v, r1, r2;
+        float vrej = 0.f;
+        if (r0 + tid < BATCH && li < limit) {
+            const uint32_t g = a.indices[list0 + li];
+            if (g < a.n_gauss) {
+                load_record<REF_LAYOUT>(a, g, r0v, r1, r2);
+                vrej = reject_bound(r0v.w);
+                keep = !tile_prunable<FORWARD>(r0v.x, r0v.y, r1.x, r1.y, r1.z, vrej, x0, y0);
+            }
+        }
+        const uint32_t bal = __ballot_sync(kFullMask, keep);
+        if (lane == 0) sb.wcnt[w] = __popc(bal);
+        __syncthreads();
+        int wbase = 0, round_total = 0;
+#pragma unroll
+        for (int k = 0; k < kPix / 32; ++k) {
+            const int c = sb.wcnt[k];
+            wbase += (k < w) ? c : 0;
+            round_total += c;
+        }
+        if (keep) put_staged<FORWARD>(a, sb, total + wbase + __popc(bal & lanemask_lt()), r0v, r1, r2, vrej, li);
+        total += round_total;
+        __syncthreads();
     }
-    if (keep) put_staged<FORWARD>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li);
-    __syncthreads();
     return total;
 }
 
@@ -319,7 +328,7 @@ struct TmaState {
 };
 
 template <bool FORWARD>
-__device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps& maps, TrackBatch& sb, TmaStage& ts,
+__device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps& maps, TrackBatch<>& sb, TmaStage& ts,
                                                uint32_t list0, int base, int limit, float x0, float y0,
                                                TmaState& tm) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -390,10 +399,12 @@ __device__ __forceinline__ void tma_drain(const TrackArgs& a, TmaStage& ts, TmaS
     }
 }
 
-template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4, bool TMA = false>
+template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4, bool TMA = false, int BATCH = kBatch>
 __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a, const __grid_constant__ RecMaps maps) {
+    static_assert(!TMA || BATCH == kBatch, "the TMA staging gathers batches of kBatch records");
+    static_assert(BATCH % 128 == 0 && BATCH <= 2 * kPix, "batch of 128, 256 or 512 Gaussians");
     pdl_begin();
-    __shared__ TrackBatch sb;
+    __shared__ TrackBatch<BATCH> sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
     extern __shared__ __align__(128) unsigned char s_dyn[];  // TMA variant: the gathered batch
@@ -430,10 +441,13 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
     uint32_t n_contrib = 0;
     if (n > 0) {
         if (TMA) tma_begin(a, maps, ts, range.x, n, tm);
-        for (int base = 0; base < n; base += kBatch) {
+        for (int base = 0; base < n; base += BATCH) {
             if (__syncthreads_and(done)) break;
-            const int cnt = TMA ? stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm)
-                                : stage_batch<REF_LAYOUT, true>(a, sb, range.x, base, n, x0, y0);
+            int cnt;
+            if constexpr (TMA)
+                cnt = stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm);
+            else
+                cnt = stage_batch<REF_LAYOUT, true, BATCH>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
                 int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
@@ -578,10 +592,13 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
     bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
     bool done2 = !do_jac;
     if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
-    for (int base = 0; base < nmax; base += kBatch) {
+    for (int base = 0; base < nmax; base += BATCH) {
         if (__syncthreads_and(done2)) break;
-        const int cnt = TMA ? stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm)
-                            : stage_batch<REF_LAYOUT, false>(a, sb, range.x, base, nmax, x0, y0);
+        int cnt;
+        if constexpr (TMA)
+            cnt = stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm);
+        else
+            cnt = stage_batch<REF_LAYOUT, false, BATCH>(a, sb, range.x, base, nmax, x0, y0);
         if (!done2) {
             for (int j = 0; j < cnt; ++j) {
                 if (sb.orig[j] >= (int)n_contrib) {
@@ -1090,6 +1107,10 @@ cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s
     if (maps) m = *maps;
     if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a, m);
     if (a.variant == 1) return launch_chained(track_tile_kernel<false, false, 3>, dim3(T), dim3(kPix), 0, s, a, m);
+    if (a.variant == 3)
+        return launch_chained(track_tile_kernel<false, false, 4, false, 128>, dim3(T), dim3(kPix), 0, s, a, m);
+    if (a.variant == 4)
+        return launch_chained(track_tile_kernel<false, false, 4, false, 512>, dim3(T), dim3(kPix), 0, s, a, m);
     if (a.variant == 2) {
         if (!maps || !a.st_flags) return cudaErrorInvalidValue;
         return launch_chained(track_tile_kernel<false, false, 4, true>, dim3(T), dim3(kPix), sizeof(TmaStage) + 128,

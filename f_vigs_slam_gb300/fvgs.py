@@ -39,6 +39,7 @@ DEBUG_IMAGES = 0x2
 DEBUG_MAPPING = 0x4
 DEBUG_RADIX_SORT = 0x8
 
+TRACK_VARIANTS = 5  # FVGS_TRACK_VARIANTS
 KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
                   "map_update", "render", "maint"]
 K = {name: i for i, name in enumerate(KERNEL_CLASSES)}
@@ -188,7 +189,7 @@ class Session:
     def autotune(self, pose, K, level: int = 0, reps: int = 5):
         """fvgs_session_autotune: (chosen variant, median ms per variant)."""
         v = C.c_int()
-        ms = np.zeros(3, np.float32)
+        ms = np.zeros(TRACK_VARIANTS, np.float32)
         _check(self.lib.fvgs_session_autotune(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K)), C.c_int(level),
                                               C.c_int(reps), C.byref(v), _ptr(ms)), "fvgs_session_autotune")
         return int(v.value), ms
