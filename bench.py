@@ -307,6 +307,91 @@ def run_reference(args):
 # ----------------------------------------------------------------------------
 # GPU arm
 # ----------------------------------------------------------------------------
+def small_case(S):
+    """The small plain-method workload: N = 50,000 Gaussians in the camera
+    frame box, 640x480 (fx = fy = 525), target rendered at a pose 1 deg / 2 cm
+    from the start pose plus colour / depth noise, Sobel gradients."""
+    cam = S.CAM_VGA
+    scene = S.cam_box(50_000, seed=0)
+    rng = np.random.default_rng(1)
+    start = (np.zeros(3, np.float32), S.IDENTITY_Q.copy())
+    true_pose = S.perturb(start, 1.0, 2.0, rng)
+    return cam, scene, start, true_pose, rng
+
+
+def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
+    """The small plain-method configuration, as the reference's plain path
+    runs it: one mapping forward + backward step, then 20 Gauss-Newton pose
+    iterations (fvgs_map_step + fvgs_track_frame), on the GPU and, whole, in
+    the FP64 CPU restatement on all host cores.  The map is uploaded again
+    before every run (outside the timed region), so every run is the same."""
+    cam, scene, start, true_pose, rng = small_case(S)
+    W, H, K = cam.width, cam.height, cam.intrinsics
+    sess = fvgs.Session(scene.n, W, H, device=dev.index or 0)
+    sess.set_stream(stream.cuda_stream)
+    sess.upload(scene)
+    col, dep, _, _ = sess.render(true_pose, K, W, H)
+    rgb, d = S.add_noise(col, dep, rng)
+    gx, gy = S.sobel3(rgb)
+    sess.set_frame(0, rgb, d, gx, gy)
+    ms, poses = [], []
+    for i in range(args.warmup + args.steps):
+        sess.upload(scene)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sess.map_step(start, K, ETA)
+        pose, _ = sess.track_frame(start, K, iterations=ITERS)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ms.append(e0.elapsed_time(e1))
+            poses.append(pose)
+    sess.close()
+    ms_run = max_over_ranks([float(np.median(ms))], dev, world)[0]
+    err = S.pose_error(poses[-1], true_pose)
+    out = {"workload": "cam-frame box N=50000, 640x480, target 1 deg / 2 cm away + noise; one mapping forward + "
+                       "backward step, then 20 GN iterations (fvgs_map_step + fvgs_track_frame)",
+           "gpu_ms_per_run": ms_run, "runs_per_s": replica_throughput(1, world, ms_run),
+           "pose_error": {"rad": err[0], "m": err[1]}}
+    if with_cpu:
+        cpu = cpu_small_run(S, scene, start, rgb, d, gx, gy, K, W, H)
+        out["cpu"] = cpu
+        out["cpu_s_per_run"] = cpu["s_per_run"]
+        out["speedup_gpu_over_cpu"] = 1e3 * cpu["s_per_run"] / ms_run
+        dq = S.pose_error(poses[-1], cpu["pose"])
+        out["pose_difference_gpu_vs_cpu"] = {"rad": dq[0], "m": dq[1]}
+        del cpu["pose"]
+    return out
+
+
+def cpu_small_run(S, scene, start, rgb, d, gx, gy, K, W, H):
+    """The whole small configuration in the CPU restatement (FP64 blending
+    and Jacobians on the FP32-exact binning, OpenMP over tiles): the mapping
+    step at the start pose, then 20 iterations of binning + Jacobian +
+    pseudo-factor step on the host."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    P = O.default_params()
+    sc = S.Scene(*[np.array(a, copy=True) for a in (scene.positions, scene.scales, scene.orientations,
+                                                      scene.colors, scene.opacities)])
+    t0 = time.perf_counter()
+    b = O.prepare(sc, start, K, W, H, P)
+    m = O.map_step(sc, b, rgb, d, start, K, W, H, P, ETA)
+    sc = S.Scene(*[np.asarray(a, np.float32) for a in (m.pos, m.scl, m.rot, m.col, m.opa)])
+    pose = (np.asarray(start[0], np.float64), np.asarray(start[1], np.float64))
+    for _ in range(ITERS):
+        pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
+        b = O.prepare(sc, pf, K, W, H, P)
+        r = O.track(b, (rgb, d, gx, gy), pf, K, W, H, P, images=False)
+        pose = O.pose_plus(pose, O.gn_delta(r.JtJ, r.Jtr))
+    t = time.perf_counter() - t0
+    return {"s_per_run": t, "cores": os.cpu_count() or 1, "kind": "port", "pose": pose,
+            "sample": "the whole run (1 mapping step + 20 binnings, Jacobians and GN steps), FP64 restatement"}
+
+
 def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     """The large plain-method workload: one session, N = 1 M room, 1280x720,
     frames through the synchronous per-frame path (fvgs_track_frame +
@@ -882,6 +967,8 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": "large plain workload only (profiling run)", "large_plain": large}), flush=True)
         return 0
+    small = run_small(args, fvgs, S, torch, dev, stream, world,
+                      with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
     prec = run_precision(args, fvgs, S, torch, dev, stream, world)
     batch = run_batching(args, fvgs, S, torch, dev, world)
     srv = run_serving(args, fvgs, S, torch, dev)
@@ -925,6 +1012,7 @@ def run_ours(args):
             "gpu_launches": srv["launches"],
             "graphed_frames": srv["graphed_frames"],
             "roofline": large["roofline"],
+            "small_plain": small,
             "large_plain": {k: v for k, v in large.items() if k not in ("roofline", "maintenance")},
             "maintenance": large["maintenance"],
             "precision": prec,
