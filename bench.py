@@ -199,6 +199,32 @@ def load_traffic():
     return {}
 
 
+def issue_roofline(kernel, per_launch_ms, dev):
+    """The instruction-issue roofline of an issue-bound kernel: warp
+    instructions per launch (smsp__inst_executed.sum of the ncu capture of
+    the same workload, profiles/ncu_traffic.json) over the live per-launch
+    time, against one warp instruction per cycle per SM sub-partition (4 per
+    SM) at the maximum SM clock."""
+    inst = load_traffic().get(kernel + "_warp_inst")
+    if not inst:
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", str(dev.index or 0), "--query-gpu=clocks.max.sm",
+                              "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+        mhz = float(out.stdout.strip().splitlines()[0])
+    except Exception:
+        pass
+    achieved = inst / (per_launch_ms / 1000.0)
+    peak = sms * 4 * mhz * 1e6
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "warp_inst_per_launch": inst, "sms": sms, "sm_max_mhz": mhz,
+            "source": "instructions per launch from the ncu capture of this workload; time live (CUDA events)"}
+
+
 def max_over_ranks(values, device, world):
     """Elapsed times are the max over ranks (the slowest replica bounds the job)."""
     if world <= 1:
@@ -475,6 +501,17 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
 
     dominant = max((c for c in timing if timing[c]["timed"]), key=lambda c: timing[c]["ms"])
     peak, peak_kind = load_peaks()
+    # every kernel class with algorithmic bytes: live GB/s against the HBM peak
+    # (not the key emission: 20 of a frame's 21 binnings are incremental and
+    # emit only the entering instances, so its full-binning bytes do not apply)
+    per_class = {}
+    for c, t in timing.items():
+        algo_c = algorithmic_bytes(c, args.n, n_inst, W, H)
+        if not t["timed"] or algo_c is None or c == "emit":
+            continue
+        ms_c = t["ms"] / t["timed"]
+        per_class[c] = {"ms_per_launch": ms_c, "algorithmic_bytes_per_launch": algo_c,
+                        "achieved_gbs": algo_c / (ms_c / 1000.0) / 1e9, "frac": algo_c / (ms_c / 1000.0) / 1e9 / peak}
     per_launch_ms = timing[dominant]["ms"] / max(1, timing[dominant]["timed"])
     algo = algorithmic_bytes(dominant, args.n, n_inst, W, H)
     achieved = algo / (per_launch_ms / 1000.0) / 1e9
@@ -493,7 +530,9 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
                          for c, v in timing.items() if v["ms"] > 0},
         "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": load_traffic().get(dominant), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": per_launch_ms},
+                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": per_launch_ms,
+                     "issue": issue_roofline(dominant, per_launch_ms, dev)},
+        "kernel_rooflines": per_class,
         "maintenance": maint,
     }
 
