@@ -356,3 +356,69 @@ def test_kat_compaction_order_and_covisibility(oracle):
     np.testing.assert_array_equal(oracle.compact_order([0, 0xff, 0, 0xff, 0]), [0, 2, 4, 1, 3])
     assert oracle.covisibility([1, 1, 0, 1, 0], [0, 1, 1, 1, 0]) == (2, 4, np.float32(0.5))
     assert oracle.covisibility([0, 0], [0, 0]) == (0, 0, np.float32(0.0))
+
+
+def test_backward_colour_terms_are_loss_gradients(oracle):
+    """optimizeGaussiansPerGaussianPass (src/GSCudaKernels.cu:2265-2502), colour
+    part (depth and distortion weights 0), in the intended semantics (quirks
+    off: consumed conic = true inverse covariance, no 256 cap): with
+    L = 0.5 sum_p |C_p - obs_p|^2 and C the forward blend, the per-Gaussian 2D
+    accumulations are
+      dmx, dmy = -dL/du, -dL/dv;  dix, diz = -dL/da, -dL/dc and
+      diy = -dL/db / 2 for the consumed conic (a, b, c);
+      dcr, dcg, dcb = -dL/d colour;  dal = +o dL/do (the opposite sign)
+    checked against central differences of the oracle's FP64 forward blend on
+    the same tile lists (records perturbed in place).  With the reference's
+    conic-layout quirk the quadratic form can be indefinite and alpha clamped
+    at 0.99, where the backward (which ignores the clamp) is no longer the
+    loss gradient."""
+    rng = np.random.default_rng(5)
+    n, W, H = 6, 32, 32
+    K = (40.0, 40.0, 15.5, 15.5)
+    pos = np.column_stack([rng.uniform(-0.5, 0.5, n), rng.uniform(-0.5, 0.5, n), rng.uniform(1.5, 2.5, n)])
+    scene = S.Scene(pos.astype(np.float32), np.full((n, 3), 0.12, np.float32),
+                    np.tile(np.array([0, 0, 0, 1], np.float32), (n, 1)), rng.uniform(0.2, 0.8, (n, 3)).astype(np.float32),
+                    np.full(n, 0.45, np.float32))
+    P = oracle.default_params(0)
+    P.w_depth = 0.0
+    P.w_dist = 0.0
+    b = oracle.prepare(scene, IDENT, K, W, H, P)
+    obs = rng.uniform(0, 1, (H, W, 3)).astype(np.float32)
+    depth = np.ones((H, W), np.float32)
+    m = oracle.map_step(scene, b, obs, depth, IDENT, K, W, H, P, 0.0)
+    rec0 = b.rec.copy()
+
+    def loss(g, col, h):
+        b.rec = rec0.copy()
+        b.rec[g, col] = np.float32(rec0[g, col] + h)
+        c, _, _, _ = oracle.render(b, IDENT, K, W, H, P)
+        return 0.5 * float(np.sum((np.asarray(c).reshape(H, W, 3) - obs) ** 2))
+
+    def fd(g, col, h):
+        """Central, forward and backward differences: a pixel whose alpha
+        crosses the 1/255 cut inside the step makes one side jump; the
+        gradient must match the central difference or a one-sided one."""
+        hp = float(np.float32(rec0[g, col] + h) - rec0[g, col])
+        hm = float(rec0[g, col] - np.float32(rec0[g, col] - h))
+        l0, lp, lm = loss(g, col, 0.0), loss(g, col, hp), loss(g, col, -hm)
+        return np.array([(lp - lm) / (hp + hm), (lp - l0) / hp, (l0 - lm) / hm])
+
+    def check(got, cands, name):
+        scale = np.abs(cands[:, 0]).max()
+        for i, (gv, c) in enumerate(zip(got, cands)):
+            err = np.abs(c - gv)
+            # central differences agree to 1e-3; one-sided ones to first order in h
+            ok = err[0] <= 1e-3 * max(abs(c[0]), scale) or min(err[1:]) <= 2e-2 * max(abs(gv), scale)
+            assert ok, (name, i, gv, c)
+
+    # record columns: u v z o | c.x c.y c.z | phat | r g b
+    # delta2d: dmx dmy dix diy diz dcr dcg dcb dz dal dpx dpy n
+    checks = [(0, 0, -1.0, 1e-3), (1, 1, -1.0, 1e-3), (4, 2, -1.0, 1e-4), (5, 3, -0.5, 1e-4), (6, 4, -1.0, 1e-4),
+              (9, 5, -1.0, 1e-3), (10, 6, -1.0, 1e-3), (11, 7, -1.0, 1e-3)]
+    active = [g for g in range(n) if m.delta2d[g, 12] > 0]
+    assert len(active) >= 4
+    for col, k, sgn, h in checks:
+        check(m.delta2d[active, k], np.array([sgn * fd(g, col, h) for g in active]), "record column %d" % col)
+    o = rec0[active, 3].astype(np.float64)
+    check(m.delta2d[active, 9], o[:, None] * np.array([fd(g, 3, 1e-4) for g in active]), "opacity")
+    b.rec = rec0
