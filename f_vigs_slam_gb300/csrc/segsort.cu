@@ -28,18 +28,20 @@ namespace fvgs {
 constexpr int kSegThreads = 256;
 constexpr int kSegItems = 16;
 constexpr int kSegCap = kSegThreads * kSegItems;  // 4096
+constexpr int kSmallItems = 8;                     // lists of up to 2048 keys
 constexpr uint64_t kKeyInf = ~0ull;
 
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }  // one pad word per 16 keys
 
-// Sort kSegItems keys in registers (bitonic network, ascending).
-__device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
+// Sort ITEMS keys in registers (bitonic network, ascending).
+template <int ITEMS>
+__device__ __forceinline__ void sort_items(uint64_t (&k)[ITEMS]) {
 #pragma unroll
-    for (int sz = 2; sz <= kSegItems; sz <<= 1)
+    for (int sz = 2; sz <= ITEMS; sz <<= 1)
 #pragma unroll
         for (int j = sz >> 1; j > 0; j >>= 1)
 #pragma unroll
-            for (int i = 0; i < kSegItems; ++i) {
+            for (int i = 0; i < ITEMS; ++i) {
                 const int l = i ^ j;
                 if (l > i) {
                     const bool up = (i & sz) == 0;
@@ -52,15 +54,17 @@ __device__ __forceinline__ void sort_items(uint64_t (&k)[kSegItems]) {
             }
 }
 
-// One merge-path round over runs of length L of s[0..m) (m a multiple of 16):
-// thread t produces outputs [16t, 16t+16) of the pair of runs containing them.
+// One merge-path round over runs of length L of s[0..m) (m a multiple of
+// ITEMS): thread t produces outputs [ITEMS t, ITEMS (t + 1)) of the pair of runs
+// containing them.
 // Returns false when the pair is already in order (nothing to write).  Both
 // run heads are re-read from shared memory each step (register-held heads
 // measured slower: more registers, fewer resident CTAs).
-__device__ __forceinline__ bool merge_round(const uint64_t* s, int t, int m, int L, uint64_t (&k)[kSegItems]) {
-    const int per_pair = (2 * L) / kSegItems;
+template <int ITEMS>
+__device__ __forceinline__ bool merge_round(const uint64_t* s, int t, int m, int L, uint64_t (&k)[ITEMS]) {
+    const int per_pair = (2 * L) / ITEMS;
     const int ps = (t / per_pair) * 2 * L;
-    const int d = (t % per_pair) * kSegItems;
+    const int d = (t % per_pair) * ITEMS;
     const int la = min(L, m - ps);
     const int lb = min(L, max(0, m - ps - L));
     if (lb == 0 || s[spad(ps + la - 1)] <= s[spad(ps + la)]) return false;
@@ -74,7 +78,7 @@ __device__ __forceinline__ bool merge_round(const uint64_t* s, int t, int m, int
     }
     int ai = lo, bj = d - lo;
 #pragma unroll
-    for (int r = 0; r < kSegItems; ++r) {
+    for (int r = 0; r < ITEMS; ++r) {
         const uint64_t a = ai < la ? s[spad(ps + ai)] : kKeyInf;
         const uint64_t b = bj < lb ? s[spad(ps + la + bj)] : kKeyInf;
         const bool ta = a <= b;
@@ -85,31 +89,34 @@ __device__ __forceinline__ bool merge_round(const uint64_t* s, int t, int m, int
     return true;
 }
 
-// Sort s[0..m) (padded layout, m a multiple of kSegItems, <= 4096) in shared
-// memory with the CTA.  Threads >= m/kSegItems only take part in the
-// barriers.  While a merged pair spans at most one warp's 512 keys the round
-// touches only that warp's slice, so it synchronises the warp, not the CTA.
+// Sort s[0..m) (padded layout, m a multiple of ITEMS, <= 256 ITEMS) in shared
+// memory with the CTA.  Threads >= m/ITEMS only take part in the barriers.
+// Lists of up to 2048 keys use ITEMS = 8, so every thread of the CTA sorts
+// and merges instead of at most half of them.  While a merged pair spans at
+// most one warp's 32 ITEMS keys the round touches only that warp's slice, so
+// it synchronises the warp, not the CTA.
+template <int ITEMS = kSegItems>
 __device__ void block_merge_sort(uint64_t* s, int m) {
     const int t = threadIdx.x;
-    const int active = m / kSegItems;
-    uint64_t k[kSegItems];
+    const int active = m / ITEMS;
+    uint64_t k[ITEMS];
     if (t < active) {
 #pragma unroll
-        for (int j = 0; j < kSegItems; ++j) k[j] = s[spad(t * kSegItems + j)];
+        for (int j = 0; j < ITEMS; ++j) k[j] = s[spad(t * ITEMS + j)];
         bool sorted = true;
 #pragma unroll
-        for (int j = 0; j + 1 < kSegItems; ++j) sorted = sorted && k[j] <= k[j + 1];
+        for (int j = 0; j + 1 < ITEMS; ++j) sorted = sorted && k[j] <= k[j + 1];
         if (!sorted) {
             sort_items(k);
 #pragma unroll
-            for (int j = 0; j < kSegItems; ++j) s[spad(t * kSegItems + j)] = k[j];
+            for (int j = 0; j < ITEMS; ++j) s[spad(t * ITEMS + j)] = k[j];
         }
     }
     __syncthreads();
-    const bool desc = t + 1 < active && s[spad(t * kSegItems + kSegItems - 1)] > s[spad((t + 1) * kSegItems)];
+    const bool desc = t + 1 < active && s[spad(t * ITEMS + ITEMS - 1)] > s[spad((t + 1) * ITEMS)];
     if (!__syncthreads_or(desc)) return;  // every run boundary already in order
-    constexpr int kWarpSpan = 32 * kSegItems;
-    for (int L = kSegItems; L < m; L <<= 1) {
+    constexpr int kWarpSpan = 32 * ITEMS;
+    for (int L = ITEMS; L < m; L <<= 1) {
         const bool warp_local = 2 * L <= kWarpSpan;
         bool wrote = false;
         if (t < active) wrote = merge_round(s, t, m, L, k);
@@ -119,7 +126,7 @@ __device__ void block_merge_sort(uint64_t* s, int m) {
             __syncthreads();
         if (wrote) {
 #pragma unroll
-            for (int r = 0; r < kSegItems; ++r) s[spad(t * kSegItems + r)] = k[r];
+            for (int r = 0; r < ITEMS; ++r) s[spad(t * ITEMS + r)] = k[r];
         }
         if (4 * L <= kWarpSpan)
             __syncwarp();
@@ -317,7 +324,10 @@ __global__ void __launch_bounds__(kSegThreads) segsort_kernel(uint64_t* comp, co
         for (int i = threadIdx.x; i < m; i += kSegThreads) s[spad(i)] = i < n ? comp[r.x + i] : kKeyInf;
     }
     __syncthreads();
-    block_merge_sort(s, m);
+    if (m <= kSegThreads * kSmallItems)
+        block_merge_sort<kSmallItems>(s, (n + kSmallItems - 1) / kSmallItems * kSmallItems);
+    else
+        block_merge_sort<kSegItems>(s, m);
     for (int i = threadIdx.x; i < n; i += kSegThreads) write_sorted(s[spad(i)], r.x + i, vals);
 }
 
