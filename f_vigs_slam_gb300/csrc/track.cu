@@ -69,6 +69,16 @@ __device__ __forceinline__ float depth_fast(float z, float dx, float phx, float 
     return depth_at(z, dx, phx, dy, phy);
 }
 
+// alpha = min(0.99, o exp(-v / 2)) from log2(o), staged per Gaussian:
+// o exp(-v/2) = 2^(log2 o - v log2(e) / 2), one FMA and the PTX ex2.approx
+// (about 2 ulp; the FP32 rounding of the exponent adds under 7e-7 relative
+// where alpha >= 1/255).  Both passes use it, so their decisions agree.
+__device__ __forceinline__ float gauss_alpha(float log2_o, float v) {
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(__fmaf_rn(v, -0.72134752044448170368f, log2_o)));
+    return fminf(0.99f, e);
+}
+
 __device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
                                              float r0, float r1, float r2) {
     // u = (a, d * (r x a))
@@ -171,7 +181,7 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
 }
 
 // Shared-memory batch of Gaussians, repacked so a rejected pair needs two
-// loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, opacity, z),
+// loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, log2(opacity), z),
 // sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list;
 // for the Jacobian pass also sE = (rgx, rgy, -fx rgx, -fy rgy), the mean's
 // normalised ray and the third row of the projection Jacobian without 1/d.
@@ -190,7 +200,7 @@ template <bool FORWARD, int BATCH>
 __device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH>& sb, int pos, const float4& r0,
                                            const float4& r1, const float4& r2, float vrej, int li) {
     sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
-    sb.B[pos] = make_float4(r1.z, vrej, r0.w, r0.z);
+    sb.B[pos] = make_float4(r1.z, vrej, log2f(r0.w), r0.z);
     sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
     sb.D[pos] = r2.w;
     sb.orig[pos] = li;
@@ -453,7 +463,7 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 // one staged Gaussian: returns false when the pixel terminates
                 auto blend = [&](int j, float dx, float dy, float v) -> bool {
                     const float4 rB = sb.B[j];
-                    const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
+                    const float alpha = gauss_alpha(rB.z, v);
                     if (alpha < kInv255) return true;
                     const float test_T = T * (1.0f - alpha);
                     if (test_T < 0.0001f) return false;
@@ -611,7 +621,7 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 float dl0, dl1;
                 const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
                 if (v > rB.y) continue;
-                const float alpha = fminf(0.99f, rB.z * expf(-0.5f * v));
+                const float alpha = gauss_alpha(rB.z, v);
                 if (alpha < kInv255) continue;
                 const float4 rC = sb.C[j];
                 const float4 rE = sb.E[j];
