@@ -200,6 +200,17 @@ __device__ __forceinline__ float conic_form(float a, float b, float c, float dx,
     return __fmaf_rn(dx, dl0, __fmul_rn(dy, dl1));
 }
 
+// alpha = min(0.99, o exp(-v / 2)) from log2(o), computed once per Gaussian:
+// o exp(-v/2) = 2^(log2 o - v log2(e) / 2), one FMA and the PTX ex2.approx
+// (about 2 ulp; the FP32 rounding of the exponent adds under 7e-7 relative
+// where alpha >= 1/255).  A pass that re-derives another pass's alphas uses
+// it too (the tracking passes; the mapping forward and backward).
+__device__ __forceinline__ float gauss_alpha(float log2_o, float v) {
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(__fmaf_rn(v, -0.72134752044448170368f, log2_o)));
+    return fminf(0.99f, e);
+}
+
 // PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;

@@ -54,7 +54,9 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
         if (li < n) {
             const uint32_t g = a.indices[range.x + li];
             const bool ok = g < a.n_gauss;  // zero opacity otherwise: never blends
-            s0[tid] = ok ? a.rec0[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 r0 = ok ? a.rec0[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+            r0.w = log2f(r0.w);  // staged as log2(opacity) for gauss_alpha
+            s0[tid] = r0;
             s1[tid] = ok ? a.rec1[g] : make_float4(0.f, 0.f, 0.f, 0.f);
             s2[tid] = ok ? a.rec2[g] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
                 const float dx = xf - r0.x, dy = yf - r0.y;
                 float dl0, dl1;
                 const float v = conic_form(r1.x, r1.y, r1.z, dx, dy, dl0, dl1);
-                const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
+                const float alpha = gauss_alpha(r0.w, v);
                 if (alpha < kMInv255 || v <= 0.0f) continue;
                 const float4 r2 = s2[j];
                 cr += T * alpha * r2.y;
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             r1 = a.rec1[gid];
             r2 = a.rec2[gid];
         }
+        const float lo2 = log2f(r0.w);  // the forward pass's alpha from log2(opacity)
         float dmx = 0.f, dmy = 0.f, dix = 0.f, diy = 0.f, diz = 0.f, dcr = 0.f, dcg = 0.f, dcb = 0.f;
         float dz = 0.f, dal = 0.f, dpx = 0.f, dpy = 0.f;
         uint32_t dn = 0;
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             const float dx = r0.x - pxf, dy = r0.y - pyf;
             float dl0, dl1;  // the forward pass's conic form ((dx, dy) negated: same value)
             const float v = conic_form(r1.x, r1.y, r1.z, dx, dy, dl0, dl1);
-            const float alpha = fminf(0.99f, r0.w * expf(-0.5f * v));
+            const float alpha = gauss_alpha(lo2, v);
             if (alpha < kMInv255) continue;
             const float4 pc = s_pc[idx];
             const float4 pe = s_pe[idx];

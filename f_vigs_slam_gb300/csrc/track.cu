@@ -69,16 +69,6 @@ __device__ __forceinline__ float depth_fast(float z, float dx, float phx, float 
     return depth_at(z, dx, phx, dy, phy);
 }
 
-// alpha = min(0.99, o exp(-v / 2)) from log2(o), staged per Gaussian:
-// o exp(-v/2) = 2^(log2 o - v log2(e) / 2), one FMA and the PTX ex2.approx
-// (about 2 ulp; the FP32 rounding of the exponent adds under 7e-7 relative
-// where alpha >= 1/255).  Both passes use it, so their decisions agree.
-__device__ __forceinline__ float gauss_alpha(float log2_o, float v) {
-    float e;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(__fmaf_rn(v, -0.72134752044448170368f, log2_o)));
-    return fminf(0.99f, e);
-}
-
 __device__ __forceinline__ void rank1_update(float A[21], float w, float a0, float a1, float a2, float d,
                                              float r0, float r1, float r2) {
     // u = (a, d * (r x a))
