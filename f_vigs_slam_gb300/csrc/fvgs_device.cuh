@@ -205,11 +205,12 @@ __device__ __forceinline__ float conic_form(float a, float b, float c, float dx,
 // (about 2 ulp; the FP32 rounding of the exponent adds under 7e-7 relative
 // where alpha >= 1/255).  A pass that re-derives another pass's alphas uses
 // it too (the tracking passes; the mapping forward and backward).
-__device__ __forceinline__ float gauss_alpha(float log2_o, float v) {
+__device__ __forceinline__ float gauss_weight(float log2_o, float v) {
     float e;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(__fmaf_rn(v, -0.72134752044448170368f, log2_o)));
-    return fminf(0.99f, e);
+    return e;
 }
+__device__ __forceinline__ float gauss_alpha(float log2_o, float v) { return fminf(0.99f, gauss_weight(log2_o, v)); }
 
 // PTX rcp.approx.f32 (at most one ulp from 1/x; subnormals kept).
 __device__ __forceinline__ float rcp_approx(float x) {

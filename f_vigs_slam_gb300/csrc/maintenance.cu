@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
         if (g >= a.n_gauss) continue;
         const float4 r0 = a.rec0[g], r1 = a.rec1[g];
         const float phy = a.rec2[g].x;
+        const float lo2 = log2f(r0.w);  // alpha = o exp(-q/2) = 2^(log2 o - q log2(e) / 2)
         float ta = 0.f, to = 0.f;
         for (int yy = 0; yy < h; ++yy) {
             const float dy = (float)(y0 + yy) - r0.y;
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
             for (int xx = 0; xx < w; ++xx) {
                 const float dx = (float)(x0 + xx) - r0.x;
                 const float q = (r1.x * dx + b_row) * dx + q_row;
-                const float alpha = r0.w * expf(-0.5f * q);
+                const float alpha = gauss_weight(lo2, q);
                 const float dr = dr_row + r1.w * dx;
                 if (alpha < 1.0f / 255.0f || dr <= 0.0f) continue;
                 ta += alpha;
