@@ -295,6 +295,39 @@ def cpu_sample(n, band_rows=720, seed=0, cam=None, maps_per_frame=1.0):
                 band_rows=band_rows, threads=os.cpu_count() or 1)
 
 
+def cpu_frame_run(n, cam, seed=0, maps_per_frame=1.0):
+    """Time the oracle on one whole tracking frame of a session: 20
+    iterations of binning + Jacobian + pseudo-factor Gauss-Newton step at
+    the moving pose (as fvgs_track_frame), plus one mapping step, weighted
+    by maps_per_frame.  Returns the frame's CPU seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from f_vigs_slam_gb300 import synthetic as S
+
+    O.build()
+    W, H, K = cam.width, cam.height, cam.intrinsics
+    scene = S.room(n, seed=seed)
+    traj = S.trajectory(3, seed=seed)
+    P = O.default_params()
+    b_true = O.prepare(scene, traj[1], K, W, H, P)
+    col, dep, _, _ = O.render(b_true, traj[1], K, W, H, P)
+    rng = np.random.default_rng(seed + 1)
+    rgb, d = S.add_noise(col.astype(np.float32), dep.astype(np.float32), rng)
+    gx, gy = S.sobel3(rgb)
+    pose = (np.asarray(traj[0][0], np.float64), np.asarray(traj[0][1], np.float64))
+    t0 = time.perf_counter()
+    for _ in range(ITERS):
+        pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
+        b = O.prepare(scene, pf, K, W, H, P)
+        r = O.track(b, (rgb, d, gx, gy), pf, K, W, H, P, images=False)
+        pose = O.pose_plus(pose, O.gn_delta(r.JtJ, r.Jtr))
+    t_iters = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.map_step(scene, b, rgb, d, pf, K, W, H, P, ETA)
+    t_map = time.perf_counter() - t0
+    return dict(frame_s=t_iters + maps_per_frame * t_map, wall_s=t_iters + t_map, threads=os.cpu_count() or 1)
+
+
 def run_reference(args):
     """CPU arm: the CPU restatement of the reference's path (FP64, all host
     threads) on the serving configuration's request mix, one bounded sample
@@ -958,8 +991,9 @@ def run_serving(args, fvgs, S, torch, dev):
 
 def cpu_serving_sample(args):
     """CPU restatement on a bounded sample of the serving mix: the median-N
-    session of each frame size, timed on a band of rows and extrapolated to a
-    frame (see cpu_sample), then to the mix in proportion to N."""
+    session of each frame size, one whole frame (20 Gauss-Newton iterations
+    and a mapping step, see cpu_frame_run), scaled to the mix in proportion
+    to N."""
     rng = np.random.default_rng(5)
     ns = np.exp(rng.uniform(np.log(SERVE_N_MIN), np.log(SERVE_N_MAX), args.sessions)).astype(int)
     from f_vigs_slam_gb300 import synthetic as S
@@ -970,17 +1004,16 @@ def cpu_serving_sample(args):
     for parity, cam in ((0, S.CAM_VGA), (1, S.CAM_HD)):
         group = sorted(int(n) for i, n in enumerate(ns) if i % 2 == parity)
         n_med = group[len(group) // 2]
-        rows = 96 if cam is S.CAM_HD else 64
-        r = cpu_sample(n_med, band_rows=rows, seed=0, cam=cam, maps_per_frame=1.0 / MAP_EVERY)
+        r = cpu_frame_run(n_med, cam, seed=0, maps_per_frame=1.0 / MAP_EVERY)
         wall += r["wall_s"]
         threads = r["threads"]
         per += [r["frame_s"] * n / n_med for n in group]
     frame_s = float(np.mean(per))
     return {"value": 1.0 / frame_s, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": ("median-N session of each frame size (one binning + one Jacobian + one mapping step on a band "
-                       "of rows, %.1f s of CPU work), extrapolated to 20 binnings + 20 Jacobians per frame plus a "
-                       "mapping step every %d-th frame, and to the %d sessions in proportion to N"
-                       % (wall, MAP_EVERY, args.sessions))}
+            "sample": ("median-N session of each frame size, one whole frame each (20 binnings + Jacobians + GN "
+                       "steps and one mapping step, weighted 1/%d; %.1f s of CPU work), scaled to the %d sessions in "
+                       "proportion to N"
+                       % (MAP_EVERY, wall, args.sessions))}
 
 
 def run_ours(args):
