@@ -245,56 +245,6 @@ def replica_throughput(steps, world, max_ms):
 # ----------------------------------------------------------------------------
 # CPU baseline (the CPU restatement of the reference, FP64, all host threads)
 # ----------------------------------------------------------------------------
-def cpu_sample(n, band_rows=720, seed=0, cam=None, maps_per_frame=1.0):
-    """Time the oracle on a bounded sample of one frame: projection + tile
-    counts of all N Gaussians, then keys / sort / tracking Jacobian / mapping
-    step on a horizontal band of `band_rows` pixel rows through the image
-    centre (intrinsics shifted so the band is the same pixels of the full
-    frame).  Extrapolates one frame = 21 binnings + 20 Jacobians + 1 mapping
-    step, with band costs scaled by H / band_rows."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    from f_vigs_slam_gb300 import synthetic as S
-
-    O.build()
-    cam = cam or S.CAM_HD
-    W, H = cam.width, cam.height
-    scene = S.room(n, seed=seed)
-    traj = S.trajectory(3, seed=seed)
-    pose, prev = traj[1], traj[0]
-    P = O.default_params()
-    band_rows = max(16, min(H, (band_rows // 16) * 16))
-    y0 = ((H - band_rows) // 2 // 16) * 16
-    K_band = (cam.fx, cam.fy, cam.cx, cam.cy - y0)
-    # observed band: oracle render at the true pose over the band only
-    b_true = O.prepare(scene, pose, K_band, W, band_rows, P)
-    col, dep, _, _ = O.render(b_true, pose, K_band, W, band_rows, P)
-    rng = np.random.default_rng(seed + 1)
-    rgb, d = S.add_noise(col.astype(np.float32), dep.astype(np.float32), rng)
-    gx, gy = S.sobel3(rgb)
-    t0 = time.perf_counter()
-    proj = O.project(scene, prev, cam.intrinsics, W, H)
-    O.count(proj, W, H, P)
-    t_proj = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    b = O.prepare(scene, prev, K_band, W, band_rows, P)
-    t_bin_band_all = time.perf_counter() - t0
-    t_bin_band = max(t_bin_band_all - t_proj, 0.0)
-    t0 = time.perf_counter()
-    O.track(b, (rgb, d, gx, gy), prev, K_band, W, band_rows, P, images=False)
-    t_track = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.map_step(scene, b, rgb, d, prev, K_band, W, band_rows, P, ETA)
-    t_map_all = time.perf_counter() - t0
-    t_map = max(t_map_all - 0.0, 0.0)
-    scale = H / band_rows
-    bins = ITERS + maps_per_frame
-    frame_s = bins * t_proj + scale * (bins * t_bin_band + ITERS * t_track + maps_per_frame * t_map)
-    wall = t_proj + t_bin_band_all + t_track + t_map_all
-    return dict(frame_s=frame_s, wall_s=wall, t_proj=t_proj, t_bin_band=t_bin_band, t_track=t_track, t_map=t_map,
-                band_rows=band_rows, threads=os.cpu_count() or 1)
-
-
 def cpu_frame_run(n, cam, seed=0, maps_per_frame=1.0):
     """Time the oracle on one whole tracking frame of a session: 20
     iterations of binning + Jacobian + pseudo-factor Gauss-Newton step at
