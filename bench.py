@@ -22,10 +22,14 @@ request per session.
    arrivals, 30 Hz per session or 70% of the measured capacity if lower.
 The large plain-method workload (one session, N = 1 M room, 1280x720, 20 GN
 iterations + 1 mapping step per frame) is reported under `large_plain`; the
-roofline entry is its dominant kernel.  Beside it: `batching` (64 keyframes,
-N log-uniform in [20k, 2M], one fvgs_frames_run call against sequential
-frames), `precision` (N = 2 M with BF16/FP16 attributes against FP32) and
-`maintenance` (outlier removal, covisibility, prune on the 1 M map).
+roofline entry is its dominant kernel (HBM, plus the instruction-issue
+roofline that bounds it), and `large_plain.kernel_rooflines` has every kernel
+class's HBM fraction.  Beside it: `small_plain` (N = 50k, 640x480, a mapping
+step + 20 GN iterations, also run whole in the CPU restatement), `batching`
+(64 keyframes, N log-uniform in [20k, 2M], one fvgs_frames_run call against
+sequential frames), `precision` (N = 2 M with BF16/FP16 attributes against
+FP32, and the visual-inertial solve with 200 Hz IMU data) and `maintenance`
+(outlier removal, covisibility, prune on the 1 M map).
 
 Multi-GPU: replicas only (every GPU serves its own sessions; no collective on
 the data path); the elapsed time is the max over ranks.
