@@ -1,6 +1,6 @@
 """GPU parity of the fused tracking kernel against the FP64 oracle.
 
-Tolerances (from the spec contract): rendered colour and depth within
+Tolerances: rendered colour and depth within
 1e-5 relative; JtJ and Jtr within 1e-5 relative (Frobenius / 2-norm) of the
 FP64 oracle.  The GPU blends in FP32, so a pixel whose FP32 and FP64 values
 fall on opposite sides of a discrete threshold (alpha < 1/255, T < 1e-4,
