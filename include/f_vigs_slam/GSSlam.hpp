@@ -8,8 +8,8 @@
  * initAndCopyImgs, initializeGaussiansFromRgbd, prepareRasterization,
  * renderView, computeRgbdPoseJacobians, optimizeGaussiansKeyframe,
  * removeOutliers, computeCovisibilityRatio, addKeyframe, prune, densify,
- * getGaussiansCount, getGaussianData.  Differences, all forced by the
- * absence of OpenCV, Eigen and Ceres in this build:
+ * getGaussiansCount, getGaussianData.  Differences, all forced by working
+ * without OpenCV, Eigen and Ceres:
  *  - images are raw host buffers (8-bit colour, 3 bytes per pixel in the
  *    camera's (b, g, r) order; depth float metres or uint16 millimetres)
  *    instead of cv::Mat;
@@ -263,7 +263,7 @@ public:
     }
     const std::vector<KeyframeData>& keyframes() const { return keyframes_; }
 
-    // ---- this build
+    // ---- additions of this interface (status, session, diagnostics)
     int lastStatus() const { return status_; }
     fvgs_session* session() { return s_; }
     uint32_t lastInstanceCount() const { return last_nb_instances_; }

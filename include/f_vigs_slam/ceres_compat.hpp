@@ -1,7 +1,7 @@
 /*
  * f_vigs_slam/ceres_compat.hpp -- the Ceres cost-function interface the
  * reference's RgbdPoseCostFunction derives from.  With Ceres installed this
- * includes it; without it (this build's image has no Ceres) it declares the
+ * includes it; without it (no Ceres installed) it declares the
  * two classes with Ceres's shape -- CostFunction with the virtual
  * Evaluate(parameters, residuals, jacobians) and the residual / parameter
  * block sizes, SizedCostFunction<num_residuals, block sizes...> -- so the

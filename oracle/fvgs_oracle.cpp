@@ -3,7 +3,7 @@
  * path (jcevasco2003/f_vigs_slam, src/GSCudaKernels.cu + src/GSSlam.cu +
  * src/RgbdPoseCost.cu).
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA library is
+ * TEST INFRASTRUCTURE ONLY.  This file is the restatement the CUDA library is
  * compared against, and the timed CPU baseline.  No product code path may
  * call it.
  *
