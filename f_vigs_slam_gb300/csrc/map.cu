@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
     __shared__ float4 s_pc[kMPix];  // final colour (incl. background), median depth
     __shared__ float4 s_pe[kMPix];  // colour error, observed depth
     __shared__ uint32_t s_nc[kMPix];
+    __shared__ uint16_t s_act[kMPix / 32][kMPix];  // per warp: the pixels its bucket can reach
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -163,13 +164,26 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
         uint32_t dn = 0;
         float T = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
         const float4* samp = a.sampled + (size_t)(base_slot + b) * kMPix;
-        for (int i = 0; i < kMPix + 31; ++i) {
+        // Only pixels whose contributor count exceeds the bucket's first list
+        // position can receive anything from it; the pipeline walks those, in
+        // pixel order (each starts from its own checkpoint, so skipping the
+        // others changes no sum).
+        int n_act = 0;
+        for (int c = 0; c < kMPix; c += 32) {
+            const bool act = s_nc[c + lane] > b * 32;
+            const unsigned m = __ballot_sync(kFullMask, act);
+            if (act) s_act[warp][n_act + __popc(m & lanemask_lt())] = (uint16_t)(c + lane);
+            n_act += __popc(m);
+        }
+        __syncwarp();
+        for (int i = 0; i < n_act + 31; ++i) {
             T = __shfl_up_sync(kFullMask, T, 1);
             a0 = __shfl_up_sync(kFullMask, a0, 1);
             a1 = __shfl_up_sync(kFullMask, a1, 1);
             a2 = __shfl_up_sync(kFullMask, a2, 1);
-            const int idx = i - lane;
-            if (!valid_splat || idx < 0 || idx >= kMPix) continue;
+            const int pos = i - lane;
+            if (!valid_splat || pos < 0 || pos >= n_act) continue;
+            const int idx = s_act[warp][pos];
             const uint32_t nc = s_nc[idx];
             if (lane == 0 && nc != 0) {
                 const float4 sv = samp[idx];
