@@ -205,6 +205,11 @@ __device__ __forceinline__ float conic_form(float a, float b, float c, float dx,
 // (about 2 ulp; the FP32 rounding of the exponent adds under 7e-7 relative
 // where alpha >= 1/255).  A pass that re-derives another pass's alphas uses
 // it too (the tracking passes; the mapping forward and backward).
+// log2 of an opacity for gauss_weight / gauss_alpha.  A non-positive (or
+// NaN) opacity maps to -inf, i.e. weight 0: such a Gaussian never reaches
+// alpha 1/255, as o exp(-v/2) <= 0 never does.
+__device__ __forceinline__ float log2_opacity(float o) { return log2f(fmaxf(o, 0.0f)); }
+
 __device__ __forceinline__ float gauss_weight(float log2_o, float v) {
     float e;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(__fmaf_rn(v, -0.72134752044448170368f, log2_o)));

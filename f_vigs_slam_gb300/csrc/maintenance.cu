@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
         if (g >= a.n_gauss) continue;
         const float4 r0 = a.rec0[g], r1 = a.rec1[g];
         const float phy = a.rec2[g].x;
-        const float lo2 = log2f(r0.w);  // alpha = o exp(-q/2) = 2^(log2 o - q log2(e) / 2)
+        const float lo2 = log2_opacity(r0.w);  // alpha = o exp(-q/2) = 2^(log2 o - q log2(e) / 2)
         float ta = 0.f, to = 0.f;
         for (int yy = 0; yy < h; ++yy) {
             const float dy = (float)(y0 + yy) - r0.y;

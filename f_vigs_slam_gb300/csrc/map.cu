@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
             const uint32_t g = a.indices[range.x + li];
             const bool ok = g < a.n_gauss;  // zero opacity otherwise: never blends
             float4 r0 = ok ? a.rec0[g] : make_float4(0.f, 0.f, 0.f, 0.f);
-            r0.w = log2f(r0.w);  // staged as log2(opacity) for gauss_alpha
+            r0.w = log2_opacity(r0.w);  // staged as log2(opacity) for gauss_alpha
             s0[tid] = r0;
             s1[tid] = ok ? a.rec1[g] : make_float4(0.f, 0.f, 0.f, 0.f);
             s2[tid] = ok ? a.rec2[g] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
             r1 = a.rec1[gid];
             r2 = a.rec2[gid];
         }
-        const float lo2 = log2f(r0.w);  // the forward pass's alpha from log2(opacity)
+        const float lo2 = log2_opacity(r0.w);  // the forward pass's alpha from log2(opacity)
         float dmx = 0.f, dmy = 0.f, dix = 0.f, diy = 0.f, diz = 0.f, dcr = 0.f, dcg = 0.f, dcb = 0.f;
         float dz = 0.f, dal = 0.f, dpx = 0.f, dpy = 0.f;
         uint32_t dn = 0;

@@ -190,7 +190,7 @@ template <bool FORWARD, int BATCH>
 __device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH>& sb, int pos, const float4& r0,
                                            const float4& r1, const float4& r2, float vrej, int li) {
     sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
-    sb.B[pos] = make_float4(r1.z, vrej, log2f(r0.w), r0.z);
+    sb.B[pos] = make_float4(r1.z, vrej, log2_opacity(r0.w), r0.z);
     sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
     sb.D[pos] = r2.w;
     sb.orig[pos] = li;

@@ -23,9 +23,14 @@ GROUPS_3D = {"position": [0, 1, 2], "scale": [3, 4, 5], "orientation": [6, 7, 8]
              "alpha": [12]}
 
 
-def _run(oracle, fv, quirks, n=8000, scale=0.5, seed=21):
+def _run(oracle, fv, quirks, n=8000, scale=0.5, seed=21, bad_opacity=False):
     W, H, K = scaled_camera(scale)
     scene = S.cam_box(n, seed=seed)
+    if bad_opacity:
+        # every 20th Gaussian transparent, every 20th (offset) with a negative
+        # opacity: neither may ever reach alpha 1/255
+        scene.opacities[::20] = 0.0
+        scene.opacities[7::20] = -0.3
     P = oracle.default_params(quirks)
     rng = np.random.default_rng(seed)
     true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
@@ -44,9 +49,11 @@ def _run(oracle, fv, quirks, n=8000, scale=0.5, seed=21):
     return W, H, scene, g, params, o
 
 
-@pytest.mark.parametrize("quirks", [0x4 | 0x8, 0x4])
-def test_map_step_parity(oracle, fvgs_lib, quirks):
-    W, H, scene, g, params, o = _run(oracle, fvgs_lib, quirks)
+@pytest.mark.parametrize("quirks,bad_opacity", [(0x4 | 0x8, False), (0x4, False), (0x4 | 0x8, True)])
+def test_map_step_parity(oracle, fvgs_lib, quirks, bad_opacity):
+    W, H, scene, g, params, o = _run(oracle, fvgs_lib, quirks, bad_opacity=bad_opacity)
+    if bad_opacity:
+        assert np.all(g["delta2d"][::20, 12] == 0) and np.all(g["delta2d"][7::20, 12] == 0)
     # forward images
     m = o.final_T.reshape(H, W)
     assert np.mean(g["n_contrib"] == o.n_contrib.reshape(H, W)) > 0.999
