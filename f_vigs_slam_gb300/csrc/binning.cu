@@ -132,10 +132,12 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
     const float bx1 = fminf((float)(a.W - 1), __fadd_rn(u, rx));
     const float by0 = fmaxf(0.0f, __fsub_rn(v, ry));
     const float by1 = fminf((float)(a.H - 1), __fadd_rn(v, ry));
-    int x0 = __float2int_rz(__fdiv_rn(bx0, (float)a.tw));
-    int x1 = __float2int_rz(__fdiv_rn(bx1, (float)a.tw));
-    int y0 = __float2int_rz(__fdiv_rn(by0, (float)a.th));
-    int y1 = __float2int_rz(__fdiv_rn(by1, (float)a.th));
+    // bx / tw of the reference; a multiplication by 2^-k when tw = 2^k (exact)
+    auto tdiv = [](float x, int t, float inv) { return inv != 0.0f ? __fmul_rn(x, inv) : __fdiv_rn(x, (float)t); };
+    int x0 = __float2int_rz(tdiv(bx0, a.tw, a.inv_tw));
+    int x1 = __float2int_rz(tdiv(bx1, a.tw, a.inv_tw));
+    int y0 = __float2int_rz(tdiv(by0, a.th, a.inv_th));
+    int y1 = __float2int_rz(tdiv(by1, a.th, a.inv_th));
     x0 = max(0, min(x0, a.ntx - 1));
     x1 = max(0, min(x1, a.ntx - 1));
     y0 = max(0, min(y0, a.nty - 1));

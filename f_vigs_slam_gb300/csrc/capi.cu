@@ -473,6 +473,8 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     pa.H = H;
     pa.tw = P.tile_w;
     pa.th = P.tile_h;
+    pa.inv_tw = (P.tile_w > 0 && (P.tile_w & (P.tile_w - 1)) == 0) ? 1.0f / (float)P.tile_w : 0.0f;
+    pa.inv_th = (P.tile_h > 0 && (P.tile_h & (P.tile_h - 1)) == 0) ? 1.0f / (float)P.tile_h : 0.0f;
     pa.ntx = ntx;
     pa.nty = nty;
     pa.radius_sigma = P.radius_sigma;

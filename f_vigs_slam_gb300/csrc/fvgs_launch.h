@@ -55,6 +55,9 @@ struct ProjectArgs {
     const DevPose* pose;
     fvgs_intrinsics K;
     int W, H, tw, th, ntx, nty;
+    // 1/tw and 1/th when the tile sides are powers of two (x / 2^k == x * 2^-k
+    // exactly in IEEE arithmetic), else 0 (divide)
+    float inv_tw, inv_th;
     float radius_sigma;
     uint32_t quirks;
     float4* rec0;
