@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
             const float dy = (float)(y0 + yy) - r0.y;
             const float q_row = r1.z * dy * dy, b_row = 2.0f * r1.y * dy;
             const float dr_row = r0.z + phy * dy;
+            float pxf = (float)x0;  // the pixel's x as a float, stepped exactly (integers < 2^24)
 #pragma unroll 4
-            for (int xx = 0; xx < w; ++xx) {
-                const float dx = (float)(x0 + xx) - r0.x;
+            for (int xx = 0; xx < w; ++xx, pxf += 1.0f) {
+                const float dx = pxf - r0.x;
                 const float q = (r1.x * dx + b_row) * dx + q_row;
                 const float alpha = gauss_weight(lo2, q);
                 const float dr = dr_row + r1.w * dx;
