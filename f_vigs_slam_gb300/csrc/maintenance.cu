@@ -89,14 +89,16 @@ __global__ void __launch_bounds__(kMPix) visibility_kernel(VisArgs a) {
 
 __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
     pdl_begin();
-    __shared__ float sD[kMPix];  // observed depth of the tile's pixels
+    __shared__ float sD[kMPix];  // per pixel: 0.8 x observed depth where it is > 0.1, else -inf
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * 16, y0 = ty * 16;
     const int tid = threadIdx.x;
     {
         const int x = x0 + (tid & 15), y = y0 + (tid >> 4);
-        sD[tid] = (x < a.W && y < a.H) ? a.obs_depth[(size_t)y * a.W + x] : 0.f;
+        const float d_obs = (x < a.W && y < a.H) ? a.obs_depth[(size_t)y * a.W + x] : 0.f;
+        // a pair counts as an outlier where d_obs > 0.1 and dr < 0.8 d_obs: one compare per pair
+        sD[tid] = d_obs > 0.1f ? 0.8f * d_obs : -INFINITY;
     }
     uint2 range = a.ranges[tile];
     range.y = min(range.y, a.n_list);
@@ -126,8 +128,7 @@ __global__ void __launch_bounds__(kMPix) outliers_kernel(OutlierArgs a) {
                 const float dr = dr_row + r1.w * dx;
                 if (alpha < 1.0f / 255.0f || dr <= 0.0f) continue;
                 ta += alpha;
-                const float d_obs = sD[yy * 16 + xx];
-                if (d_obs > 0.1f && dr < 0.8f * d_obs) to += alpha;
+                if (dr < sD[yy * 16 + xx]) to += alpha;
             }
         }
         if (ta != 0.f) atomicAdd(a.total_alpha + g, ta);
