@@ -39,6 +39,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
 
     float u = 0.f, v = 0.f, z = 0.f, cxx = 0.f, cyy = 0.f, cxy = 0.f;
     float ixx = 0.f, iyy = 0.f, ixy = 0.f, phx = 0.f, phy = 0.f;
+    float4 geo0 = make_float4(0.f, 0.f, 0.f, 0.f), geo1 = geo0;  // camera-frame covariance and mean
     bool visible = false;
     {
         const float d0 = __fsub_rn(p.x, tw[0]);
@@ -121,6 +122,8 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
                 }
                 phx = __fmul_rn(__fmul_rn(pcx, inv_z), inv_z);
                 phy = __fmul_rn(__fmul_rn(pcy, inv_z), inv_z);
+                geo0 = make_float4(C[0][0], C[0][1], C[0][2], C[1][1]);
+                geo1 = make_float4(C[1][2], C[2][2], pcx, pcy);
             }
         }
     }
@@ -161,6 +164,10 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
         a.rec1[i] = make_float4(ixx, swap ? iyy : ixy, swap ? ixy : iyy, phx);
         a.rec2[i] = make_float4(phy, co.x, co.y, co.z);
         a.bins[i].p = make_float4(u, v, z, phx);
+        if (a.geo0) {
+            a.geo0[i] = geo0;
+            a.geo1[i] = geo1;
+        }
     }
     // bins[i].r.z == counts[i] after every binning; a Gaussian without
     // instances before and now needs no write (most of a large map).

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <vector>
 
@@ -25,7 +26,7 @@ using namespace fvgs;
 
 namespace {
 
-constexpr int kMaxLevels = 3;
+constexpr int kMaxLevels = 4;
 
 struct FrameLevel {
     int W = 0, H = 0;
@@ -112,6 +113,9 @@ struct fvgs_session {
 
     float4 *pos = nullptr, *scale = nullptr, *rot = nullptr, *col = nullptr;
     float4 *rec0 = nullptr, *rec1 = nullptr, *rec2 = nullptr;
+    // geometry records of the analytic pose Jacobian (sessions whose quirks
+    // clear FVGS_Q_POSE_JAC_APPROX): camera-frame covariance and mean
+    float4 *geo0 = nullptr, *geo1 = nullptr;
     BinRec* bins = nullptr;  // binning records; bins[i].r.z == counts[i] after every binning
     uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
     float *dbg_cov = nullptr, *dbg_inv = nullptr;
@@ -228,11 +232,15 @@ struct fvgs_session {
     // with every device allocation (a graph holds buffer addresses).
     struct FrameGraph {
         bool valid = false;
-        int level = 0, iterations = 0, W = 0, H = 0;
+        int iters[kMaxLevels] = {}, W[kMaxLevels] = {}, H[kMaxLevels] = {};
+        int map_level = 0;
+        bool entry_incremental = false;  // the frame's first binning continues the previous one
         uint32_t n_g = 0;  // launch shapes and kernel arguments depend on the Gaussian count
-        fvgs_intrinsics K{};
+        fvgs_intrinsics K[kMaxLevels] = {};
         float eta = -1.f;
         uint64_t gen = 0;
+        // host-side binning state the frame leaves (the tile grid of its last binning)
+        int exit_ntx = 0, exit_nty = 0, exit_W = 0, exit_H = 0, exit_T = 0;
         uint32_t *vals_in = nullptr, *vals_out = nullptr, *vals_alt_out = nullptr;
         uint2 *ranges_in = nullptr, *ranges_out = nullptr, *ranges_prev_out = nullptr;
         uint64_t launches[FVGS_K_COUNT] = {};
@@ -247,10 +255,15 @@ struct fvgs_session {
     fvgs_pose* d_pose_in = nullptr;
     cudaEvent_t frame_done = nullptr;
     bool frame_pending = false;
+    // A frame: iters[l] Gauss-Newton iterations at pyramid level l with
+    // intrinsics K[l], from the coarsest level down to level 0 (the loop of
+    // GSSlam::optimizeWithCeres, src/GSSlam.cu:2269-2272), then optionally a
+    // mapping step at map_level.
     struct FrameRequest {
         fvgs_pose pose{};
-        fvgs_intrinsics K{};
-        int level = 0, iterations = 0;
+        fvgs_intrinsics K[kMaxLevels] = {};
+        int iters[kMaxLevels] = {};
+        int map_level = 0;
         float eta = -1.f;
     } req;
     uint64_t frames_graphed = 0, frames_eager = 0;
@@ -484,6 +497,8 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     pa.rec2 = s->rec2;
     pa.bins = s->bins;
     pa.counts = s->counts;
+    pa.geo0 = s->geo0;
+    pa.geo1 = s->geo1;
     if (s->debug & FVGS_DEBUG_PROJECTION) {
         pa.dbg_cov = s->dbg_cov;
         pa.dbg_inv = s->dbg_inv;
@@ -625,6 +640,9 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
         ta.img_nc = s->img_nc;
     }
     ta.render_only = render_only ? 1 : 0;
+    ta.quirks = P.quirks;
+    ta.geo0 = s->geo0;
+    ta.geo1 = s->geo1;
     ta.variant = (f.tuned_w == f.W && f.tuned_h == f.H) ? f.track_variant : 0;
     if (ta.variant == 2 && !s->rec_maps_ok) ta.variant = 0;
     ta.st_flags = &s->st->flags;
@@ -868,6 +886,10 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->rec0, N);
     FV_A(s->rec1, N);
     FV_A(s->rec2, N);
+    if (!(P.quirks & FVGS_Q_POSE_JAC_APPROX)) {
+        FV_A(s->geo0, N);
+        FV_A(s->geo1, N);
+    }
     FV_A(s->bins, N);
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
@@ -1390,64 +1412,31 @@ int fvgs_session_set_track_variant(fvgs_session* s, int level, int variant) {
     return FVGS_OK;
 }
 
-int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
-                     double* last_step) {
-    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0) return FVGS_E_INVALID;
-    const FrameLevel& f = s->lv[level];
-    if (!f.rgb) return FVGS_E_STATE;
-    FV_CK(cudaSetDevice(s->device));
-    if (iterations > 0 && needs_tuning(s, level)) FV_TRY(autotune_track(s, pose, K, level, 5));
-    const fvgs_pose start = *pose;
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        FV_TRY(reset_status(s));
-        FV_TRY(set_pose(s, &start));
-        for (int it = 0; it < iterations; ++it) {
-            FV_TRY(enqueue_bin(s, K, f.W, f.H));
-            FV_TRY(enqueue_track(s, K, f, false, false));
-            {
-                KScope k(s, FVGS_K_GN, 1);
-                FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step,
-                                             s->stream));
-            }
-        }
-        FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
-        FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
-        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
-        FV_CK(cudaStreamSynchronize(s->stream));
-        collect_timing(s);
-        int retry = 0;
-        FV_TRY(check_status(s, &retry));
-        if (retry) continue;
-        for (int k = 0; k < 3; ++k) pose->position[k] = s->h_devpose->t[k];
-        for (int k = 0; k < 4; ++k) pose->orientation[k] = s->h_devpose->q[k];
-        if (last_step) std::memcpy(last_step, s->h_jj + 42, sizeof(double) * 6);
-        s->has_track = iterations > 0;
-        return FVGS_OK;
-    }
-    return FVGS_E_CAPACITY;
-}
-
 namespace {
 
 // One frame on the session's stream: the request's pose (already in the
-// pinned staging s->h_pose) to the device, `iterations` Gauss-Newton steps,
-// optionally a mapping step at the tracked pose, then the result pose, last
-// step and status back to pinned host memory.
+// pinned staging s->h_pose) to the device, the Gauss-Newton steps of every
+// level from the coarsest down, optionally a mapping step at the tracked
+// pose, then the result pose, last step and status back to pinned host memory.
 int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
-    const FrameLevel& f = s->lv[r.level];
     FV_TRY(reset_status(s));
     FV_CK(cudaMemcpyAsync(s->d_pose_in, s->h_pose, sizeof(fvgs_pose), cudaMemcpyHostToDevice, s->stream));
     FV_CK(launch_chained(set_pose_dev_kernel, dim3(1), dim3(1), 0, s->stream, s->pose,
                          static_cast<const fvgs_pose*>(s->d_pose_in)));
-    for (int it = 0; it < r.iterations; ++it) {
-        FV_TRY(enqueue_bin(s, &r.K, f.W, f.H));
-        FV_TRY(enqueue_track(s, &r.K, f, false, false));
-        KScope k(s, FVGS_K_GN, 1);
-        FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step, s->stream));
+    for (int l = kMaxLevels - 1; l >= 0; --l) {
+        const FrameLevel& f = s->lv[l];
+        for (int it = 0; it < r.iters[l]; ++it) {
+            FV_TRY(enqueue_bin(s, &r.K[l], f.W, f.H));
+            FV_TRY(enqueue_track(s, &r.K[l], f, false, false));
+            KScope k(s, FVGS_K_GN, 1);
+            FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step,
+                                         s->stream));
+        }
     }
     if (r.eta >= 0.f) {
-        FV_TRY(enqueue_bin(s, &r.K, f.W, f.H));
-        FV_TRY(enqueue_map(s, &r.K, f, r.eta));
+        const FrameLevel& f = s->lv[r.map_level];
+        FV_TRY(enqueue_bin(s, &r.K[r.map_level], f.W, f.H));
+        FV_TRY(enqueue_map(s, &r.K[r.map_level], f, r.eta));
     }
     FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
     FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
@@ -1455,24 +1444,50 @@ int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
     return FVGS_OK;
 }
 
-bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
-                       const fvgs_session::FrameRequest& r) {
-    const FrameLevel& f = s->lv[r.level];
-    return g.valid && g.gen == s->gen && g.level == r.level && g.iterations == r.iterations && g.W == f.W &&
-           g.H == f.H && g.eta == r.eta && g.K.fx == r.K.fx && g.K.fy == r.K.fy && g.K.cx == r.K.cx &&
-           g.K.cy == r.K.cy && g.n_g == s->n_g && g.vals_in == s->vals && g.ranges_in == s->ranges;
+// Level of the frame's first binning (-1: none).
+int first_level(const fvgs_session::FrameRequest& r) {
+    for (int l = kMaxLevels - 1; l >= 0; --l)
+        if (r.iters[l] > 0) return l;
+    return r.eta >= 0.f ? r.map_level : -1;
 }
 
-// Whether a frame may run from a captured graph: the binning history must be
-// valid (every binning of the frame is then incremental and needs no
-// host-side memset), and no per-call host work may be involved.
+// Whether the frame's first binning continues the session's last one
+// (incremental binning on the same tile grid).
+bool entry_incremental(const fvgs_session* s, const fvgs_session::FrameRequest& r) {
+    const int l0 = first_level(r);
+    if (l0 < 0 || !s->hist_ok) return false;
+    const FrameLevel& f = s->lv[l0];
+    return s->hist_ntx == (f.W + s->params.tile_w - 1) / s->params.tile_w &&
+           s->hist_nty == (f.H + s->params.tile_h - 1) / s->params.tile_h;
+}
+
+bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
+                       const fvgs_session::FrameRequest& r) {
+    if (!(g.valid && g.gen == s->gen && g.map_level == r.map_level && g.eta == r.eta && g.n_g == s->n_g &&
+          g.vals_in == s->vals && g.ranges_in == s->ranges && g.entry_incremental == entry_incremental(s, r)))
+        return false;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        const bool used = r.iters[l] > 0 || (r.eta >= 0.f && l == r.map_level);
+        if (g.iters[l] != r.iters[l]) return false;
+        if (!used) continue;
+        const FrameLevel& f = s->lv[l];
+        if (g.W[l] != f.W || g.H[l] != f.H || g.K[l].fx != r.K[l].fx || g.K[l].fy != r.K[l].fy ||
+            g.K[l].cx != r.K[l].cx || g.K[l].cy != r.K[l].cy)
+            return false;
+    }
+    return true;
+}
+
+// Whether a frame may run from a captured graph: no per-call host work may
+// be involved (the binning scratch is clean, so no binning needs a host-side
+// memset; no event timing; the tile-bucket binning without the reference's
+// literal range / culled-slot behaviours).  A captured frame holds the
+// binning decisions of its capture, so the graph key records whether its
+// first binning continued the previous one.
 bool frame_graphable(const fvgs_session* s, const fvgs_session::FrameRequest& r) {
-    const FrameLevel& f = s->lv[r.level];
-    const int ntx = (f.W + s->params.tile_w - 1) / s->params.tile_w;
-    const int nty = (f.H + s->params.tile_h - 1) / s->params.tile_h;
     const bool literal = (s->params.quirks & (FVGS_Q_CULLED_SLOTS | FVGS_Q_RANGE_LAUNCH)) != 0;
-    return s->hist_ok && s->diff_clean && s->hist_ntx == ntx && s->hist_nty == nty && s->timing_mask == 0 &&
-           !(s->debug & FVGS_DEBUG_RADIX_SORT) && !literal;
+    return first_level(r) >= 0 && s->diff_clean && s->timing_mask == 0 && !(s->debug & FVGS_DEBUG_RADIX_SORT) &&
+           !literal;
 }
 
 int launch_frame(fvgs_session* s) {
@@ -1491,6 +1506,13 @@ int launch_frame(fvgs_session* s) {
         s->ranges = g.ranges_out;
         s->ranges_prev = g.ranges_prev_out;
         for (int c = 0; c < FVGS_K_COUNT; ++c) s->launches[c] += g.launches[c];
+        s->hist_ok = true;
+        s->hist_ntx = g.exit_ntx;
+        s->hist_nty = g.exit_nty;
+        s->last_W = g.exit_W;
+        s->last_H = g.exit_H;
+        s->last_T = g.exit_T;
+        s->keys_valid = false;
         s->has_binning = true;
         ++s->frames_graphed;
         return FVGS_OK;
@@ -1523,6 +1545,7 @@ int launch_frame(fvgs_session* s) {
     g.vals_in = s->vals;
     g.ranges_in = s->ranges;
     g.n_g = s->n_g;
+    g.entry_incremental = entry_incremental(s, r);
     cudaGraph_t graph = nullptr;
     int rc = FVGS_OK;
     cudaError_t ec = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
@@ -1553,14 +1576,20 @@ int launch_frame(fvgs_session* s) {
         ++s->frames_eager;
         return enqueue_frame(s, r);
     }
-    const FrameLevel& f = s->lv[r.level];
-    g.level = r.level;
-    g.iterations = r.iterations;
-    g.W = f.W;
-    g.H = f.H;
-    g.K = r.K;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        g.iters[l] = r.iters[l];
+        g.W[l] = s->lv[l].W;
+        g.H[l] = s->lv[l].H;
+        g.K[l] = r.K[l];
+    }
+    g.map_level = r.map_level;
     g.eta = r.eta;
     g.gen = s->gen;
+    g.exit_ntx = s->hist_ntx;
+    g.exit_nty = s->hist_nty;
+    g.exit_W = s->last_W;
+    g.exit_H = s->last_H;
+    g.exit_T = s->last_T;
     g.vals_out = s->vals;
     g.vals_alt_out = s->sort.vals_alt;
     g.ranges_out = s->ranges;
@@ -1575,25 +1604,137 @@ int launch_frame(fvgs_session* s) {
 
 }  // namespace
 
-int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
-                      float map_eta) {
-    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0 || !(map_eta == map_eta))
+namespace {
+
+// Intrinsics of pyramid level l from those of level 0: focal lengths and
+// principal point scaled by 2^-l (GSSlam::computeRgbdPoseJacobians,
+// src/GSSlam.cu:2133-2138).
+fvgs_intrinsics level_intrinsics(const fvgs_intrinsics& K0, int l) {
+    const float sc = 1.0f / (float)(1 << l);
+    fvgs_intrinsics K = K0;
+    K.fx *= sc;
+    K.fy *= sc;
+    K.cx *= sc;
+    K.cy *= sc;
+    return K;
+}
+
+using Request = fvgs_session::FrameRequest;
+
+Request single_level_request(const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                             float map_eta) {
+    Request r;
+    r.pose = *pose;
+    r.K[level] = *K;
+    r.iters[level] = iterations;
+    r.map_level = level;
+    r.eta = map_eta >= 0.f ? map_eta : -1.f;
+    return r;
+}
+
+int pyramid_request(const fvgs_pose* pose, const fvgs_intrinsics* K0, const int* iterations, int levels,
+                    float map_eta, Request* r) {
+    if (!pose || !K0 || !iterations || levels < 1 || levels > kMaxLevels || !(map_eta == map_eta))
         return FVGS_E_INVALID;
+    *r = Request{};
+    r->pose = *pose;
+    for (int l = 0; l < levels; ++l) {
+        if (iterations[l] < 0) return FVGS_E_INVALID;
+        r->K[l] = level_intrinsics(*K0, l);
+        r->iters[l] = iterations[l];
+    }
+    r->map_level = 0;
+    r->eta = map_eta >= 0.f ? map_eta : -1.f;
+    return FVGS_OK;
+}
+
+// Checks and one-time preparations of a frame: every level it uses holds an
+// observed frame, mapping buffers exist, launch variants are tuned.
+int prepare_request(fvgs_session* s, const Request& r) {
+    if (s->n_g == 0) return FVGS_E_STATE;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        const bool used = r.iters[l] > 0 || (r.eta >= 0.f && l == r.map_level);
+        if (used && !s->lv[l].rgb) return FVGS_E_STATE;
+    }
+    if (r.eta >= 0.f) {
+        const FrameLevel& f = s->lv[r.map_level];
+        FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
+    }
+    for (int l = kMaxLevels - 1; l >= 0; --l)
+        if (r.iters[l] > 0 && needs_tuning(s, l)) FV_TRY(autotune_track(s, &r.pose, &r.K[l], l, 5));
+    return FVGS_OK;
+}
+
+int total_iterations(const Request& r) {
+    int n = 0;
+    for (int l = 0; l < kMaxLevels; ++l) n += r.iters[l];
+    return n;
+}
+
+// The plain per-frame path: the frame enqueued eagerly, then waited for.
+int run_request_eager(fvgs_session* s, const Request& r, fvgs_pose* pose, double* last_step) {
+    FV_TRY(prepare_request(s, r));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        *s->h_pose = r.pose;
+        FV_TRY(enqueue_frame(s, r));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        collect_timing(s);
+        int retry = 0;
+        FV_TRY(check_status(s, &retry));
+        if (retry) continue;
+        for (int k = 0; k < 3; ++k) pose->position[k] = s->h_devpose->t[k];
+        for (int k = 0; k < 4; ++k) pose->orientation[k] = s->h_devpose->q[k];
+        if (last_step) std::memcpy(last_step, s->h_jj + 42, sizeof(double) * 6);
+        s->has_track = total_iterations(r) > 0;
+        if (r.eta >= 0.f) s->has_map = true;
+        return FVGS_OK;
+    }
+    return FVGS_E_CAPACITY;
+}
+
+int submit_request(fvgs_session* s, const Request& r) {
     if (s->frame_pending) return FVGS_E_STATE;
-    const FrameLevel& f = s->lv[level];
-    if (!f.rgb || s->n_g == 0) return FVGS_E_STATE;
     FV_CK(cudaSetDevice(s->device));
-    if (map_eta >= 0.f) FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
-    if (iterations > 0 && needs_tuning(s, level)) FV_TRY(autotune_track(s, pose, K, level, 5));
-    s->req.pose = *pose;
-    s->req.K = *K;
-    s->req.level = level;
-    s->req.iterations = iterations;
-    s->req.eta = map_eta >= 0.f ? map_eta : -1.f;
+    FV_TRY(prepare_request(s, r));
+    s->req = r;
     FV_TRY(launch_frame(s));
     FV_CK(cudaEventRecord(s->frame_done, s->stream));
     s->frame_pending = true;
     return FVGS_OK;
+}
+
+}  // namespace
+
+int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                     double* last_step) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0) return FVGS_E_INVALID;
+    if (!s->lv[level].rgb) return FVGS_E_STATE;
+    FV_CK(cudaSetDevice(s->device));
+    return run_request_eager(s, single_level_request(pose, K, level, iterations, -1.f), pose, last_step);
+}
+
+int fvgs_track_frame_pyramid(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K0, const int* iterations,
+                             int levels, double* last_step) {
+    if (!s) return FVGS_E_INVALID;
+    Request r;
+    FV_TRY(pyramid_request(pose, K0, iterations, levels, -1.f, &r));
+    FV_CK(cudaSetDevice(s->device));
+    return run_request_eager(s, r, pose, last_step);
+}
+
+int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
+                      float map_eta) {
+    if (!s || !valid_pose(pose) || !K || level < 0 || level >= kMaxLevels || iterations < 0 || !(map_eta == map_eta))
+        return FVGS_E_INVALID;
+    return submit_request(s, single_level_request(pose, K, level, iterations, map_eta));
+}
+
+int fvgs_frame_submit_pyramid(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K0,
+                              const int* iterations, int levels, float map_eta) {
+    if (!s) return FVGS_E_INVALID;
+    Request r;
+    FV_TRY(pyramid_request(pose, K0, iterations, levels, map_eta, &r));
+    return submit_request(s, r);
 }
 
 int fvgs_frame_poll(fvgs_session* s, int* done) {
@@ -1621,9 +1762,10 @@ int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step) {
     // An instance overflow (the buffers have grown) or an inconsistent
     // incremental binning: run the frame again, eagerly, from the same pose.
     for (int attempt = 0; retry && attempt < 4; ++attempt) {
-        const FrameLevel& f = s->lv[s->req.level];
-        if (s->req.eta >= 0.f)
+        if (s->req.eta >= 0.f) {
+            const FrameLevel& f = s->lv[s->req.map_level];
             FV_TRY(ensure_map_buffers(s, (size_t)f.W * f.H, (s->params.quirks & FVGS_Q_MAP_CAP256) != 0));
+        }
         *s->h_pose = s->req.pose;
         ++s->frames_eager;
         FV_TRY(enqueue_frame(s, s->req));
@@ -1637,20 +1779,19 @@ int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step) {
         for (int k = 0; k < 4; ++k) pose->orientation[k] = s->h_devpose->q[k];
     }
     if (last_step) std::memcpy(last_step, s->h_jj + 42, sizeof(double) * 6);
-    s->has_track = s->req.iterations > 0;
+    s->has_track = total_iterations(s->req) > 0;
     if (s->req.eta >= 0.f) s->has_map = true;
     return FVGS_OK;
 }
 
-int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K, const int* levels,
-                    int iterations, const float* map_etas, int n) {
-    if (!sessions || !poses || !K || n < 0) return FVGS_E_INVALID;
+namespace {
+
+// Submit every session's frame (each on its own stream), then wait for all.
+int run_batched(fvgs_session* const* sessions, fvgs_pose* poses, int n, const std::function<int(int)>& submit) {
     int first_error = FVGS_OK;
     int submitted = 0;
     for (; submitted < n; ++submitted) {
-        const int rc = fvgs_frame_submit(sessions[submitted], &poses[submitted], &K[submitted],
-                                         levels ? levels[submitted] : 0, iterations,
-                                         map_etas ? map_etas[submitted] : -1.f);
+        const int rc = submit(submitted);
         if (rc != FVGS_OK) {
             first_error = rc;
             break;
@@ -1661,6 +1802,26 @@ int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_
         if (rc != FVGS_OK && first_error == FVGS_OK) first_error = rc;
     }
     return first_error;
+}
+
+}  // namespace
+
+int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K, const int* levels,
+                    int iterations, const float* map_etas, int n) {
+    if (!sessions || !poses || !K || n < 0) return FVGS_E_INVALID;
+    return run_batched(sessions, poses, n, [&](int i) {
+        return fvgs_frame_submit(sessions[i], &poses[i], &K[i], levels ? levels[i] : 0, iterations,
+                                 map_etas ? map_etas[i] : -1.f);
+    });
+}
+
+int fvgs_frames_run_pyramid(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K0,
+                            const int* iterations, int levels, const float* map_etas, int n) {
+    if (!sessions || !poses || !K0 || !iterations || n < 0) return FVGS_E_INVALID;
+    return run_batched(sessions, poses, n, [&](int i) {
+        return fvgs_frame_submit_pyramid(sessions[i], &poses[i], &K0[i], iterations, levels,
+                                         map_etas ? map_etas[i] : -1.f);
+    });
 }
 
 int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager) {

@@ -76,6 +76,11 @@ struct ProjectArgs {
     float* dbg_cov;    // optional: 3N Sigma2D (xx, yy, xy)
     float* dbg_inv;    // optional: 3N inverse, stored order (xx, yy, xy)
     uint8_t* dbg_vis;  // optional: N visibility
+    // optional (analytic pose Jacobian): geometry record of every Gaussian
+    // with instances, geo0 = (Sxx, Sxy, Sxz, Syy), geo1 = (Syz, Szz, x, y) --
+    // the camera-frame 3D covariance and mean (z is rec0.z)
+    float4* geo0;
+    float4* geo1;
 };
 
 struct EmitArgs {
@@ -213,6 +218,10 @@ struct TrackArgs {
     // record tensor maps); the arithmetic and its order are the same in all
     int variant;
     uint32_t* st_flags;  // status word for bounded-wait timeouts (variant 2)
+    // analytic pose Jacobian (FVGS_Q_POSE_JAC_APPROX clear): the geometry
+    // records written by the projection (ProjectArgs::geo0 / geo1)
+    const float4* geo0;
+    const float4* geo1;
 };
 constexpr int kTrackVariants = 5;
 // Tensor maps of the three record planes (2-D: 4 floats x capacity rows,

@@ -136,7 +136,9 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     ta.ref_phat = p_hats;
     ta.ref_col = colors;
     ta.ref_opa = opacities;
-    ta.quirks = P.quirks;
+    // the reference's buffers hold no camera-frame geometry: always the
+    // reference's approximate Jacobian
+    ta.quirks = P.quirks | FVGS_Q_POSE_JAC_APPROX;
     ta.variant = 0;
     if (fvgs::launch_track_ref_layout(ta, s) != cudaSuccess) return FVGS_E_CUDA;
     if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), dpose, out, s) != cudaSuccess) return FVGS_E_CUDA;

@@ -86,7 +86,10 @@ struct fvgs_server {
                         rc = fvgs_preprocess_frame(sl.session, r.raw_color, r.raw_depth, r.raw_depth_u16_mm, r.width,
                                                    r.height, r.raw_levels > 0 ? r.raw_levels : 1, r.raw_double_scale);
                     if (rc == FVGS_OK)
-                        rc = fvgs_frame_submit(sl.session, &r.pose, &r.K, r.level, r.iterations, r.map_eta);
+                        rc = r.pyr_levels > 0
+                                 ? fvgs_frame_submit_pyramid(sl.session, &r.pose, &r.K, r.pyr_iterations,
+                                                             r.pyr_levels, r.map_eta)
+                                 : fvgs_frame_submit(sl.session, &r.pose, &r.K, r.level, r.iterations, r.map_eta);
                     sl.t_launch = now_s();
                     if (rc != FVGS_OK) {
                         fvgs_server_result res{};

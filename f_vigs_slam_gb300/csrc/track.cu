@@ -173,30 +173,110 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
 // Shared-memory batch of Gaussians, repacked so a rejected pair needs two
 // loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, log2(opacity), z),
 // sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list;
-// for the Jacobian pass also sE = (rgx, rgy, -fx rgx, -fy rgy), the mean's
-// normalised ray and the third row of the projection Jacobian without 1/d.
-template <int BATCH = kBatch>
+// for the Jacobian pass also NX planes sX: the reference Jacobian stages
+// sX[0] = (rgx, rgy, -fx rgx, -fy rgy), the mean's normalised ray and the
+// third row of the projection Jacobian without 1/d; the analytic Jacobian
+// stages eight planes with the derivatives of (u, v, a, b, c) with respect to
+// the camera-frame pose update and the mean's (x, y) (see stage_deriv).
+template <int BATCH = kBatch, int NX = 1>
 struct TrackBatch {
     float4 A[BATCH];
     float4 B[BATCH];
     float4 C[BATCH];
-    float4 E[BATCH];
+    float4 X[NX][BATCH];
     float D[BATCH];
     int orig[BATCH];
     int wcnt[kPix / 32];
 };
 
-template <bool FORWARD, int BATCH>
-__device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH>& sb, int pos, const float4& r0,
-                                           const float4& r1, const float4& r2, float vrej, int li) {
+// What a staging round stores besides the blending record.
+enum StageExtra { kStageNone = 0, kStageRay = 1, kStageDeriv = 2 };
+
+// Derivatives of one Gaussian's screen mean (u, v) and consumed conic slots
+// (a, b, c) with respect to the camera-frame pose update delta = (dp_c,
+// dtheta): t' = t + R dp_c, R' = R exp(dtheta), so d p_cam / d dp_c = -I,
+// d p_cam / d dtheta = [p_cam]x and d Sigma_cam / d dtheta_j =
+// -[e_j]x Sigma_cam + Sigma_cam [e_j]x.  With J the projection's Jacobian
+// (rows J0, J1), M = Sigma_cam J^T and Q = Sigma2D^-1:
+//   d Sigma2D = dJ M + (dJ M)^T (+ the rotated-covariance terms
+//   2 J0 x M0, J0 x M1 + J1 x M0, 2 J1 x M1 for dtheta), dQ = -Q dSigma2D Q.
+// r0, r1: the blending record; g0, g1: the geometry record (camera-frame
+// covariance and mean).  out: du[6], dv[6], da[6], db[6], dc[6], x, y.
+__device__ __forceinline__ void stage_deriv(const TrackArgs& a, const float4& r0, const float4& r1, const float4& g0,
+                                            const float4& g1, float4 (&out)[8]) {
+    const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+    const float fx = a.K.fx, fy = a.K.fy;
+    const float z = r0.z, x = g1.z, y = g1.w;
+    const float sxx = g0.x, sxy = g0.y, sxz = g0.z, syy = g0.w, syz = g1.x, szz = g1.y;
+    const float q00 = r1.x, q01 = swap ? r1.z : r1.y, q11 = swap ? r1.y : r1.z;
+    const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
+    // J0 = (j00, 0, j02), J1 = (0, j11, j12)
+    const float j00 = fx * iz, j02 = -fx * x * iz2, j11 = fy * iz, j12 = -fy * y * iz2;
+    const float m0x = sxx * j00 + sxz * j02, m0y = sxy * j00 + syz * j02, m0z = sxz * j00 + szz * j02;
+    const float m1x = sxy * j11 + sxz * j12, m1y = syy * j11 + syz * j12, m1z = syz * j11 + szz * j12;
+    // rotated-covariance terms: w00 = 2 J0 x M0, w01 = J0 x M1 + J1 x M0, w11 = 2 J1 x M1
+    const float w00[3] = {2.f * (-j02 * m0y), 2.f * (j02 * m0x - j00 * m0z), 2.f * (j00 * m0y)};
+    const float w01[3] = {-j02 * m1y + (j11 * m0z - j12 * m0y), (j02 * m1x - j00 * m1z) + j12 * m0x,
+                          j00 * m1y - j11 * m0x};
+    const float w11[3] = {2.f * (j11 * m1z - j12 * m1y), 2.f * (j12 * m1x), 2.f * (-j11 * m1x)};
+    const float qa = q00 * q00, qb = 2.f * q00 * q01, qc = q01 * q01;
+    const float qd = q00 * q01, qe = q00 * q11 + q01 * q01, qf = q01 * q11;
+    const float qg = 2.f * q01 * q11, qh = q11 * q11;
+    float du[6], dv[6], da[6], db[6], dc[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        // d p_cam for tangent direction k
+        const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
+        const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
+        const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
+        const float dj00 = -fx * iz2 * dpz;
+        const float dj02 = -fx * iz2 * dpx + 2.f * fx * x * iz3 * dpz;
+        const float dj11 = -fy * iz2 * dpz;
+        const float dj12 = -fy * iz2 * dpy + 2.f * fy * y * iz3 * dpz;
+        float ds00 = 2.f * (dj00 * m0x + dj02 * m0z);
+        float ds01 = (dj00 * m1x + dj02 * m1z) + (dj11 * m0y + dj12 * m0z);
+        float ds11 = 2.f * (dj11 * m1y + dj12 * m1z);
+        if (k >= 3) {
+            ds00 += w00[k - 3];
+            ds01 += w01[k - 3];
+            ds11 += w11[k - 3];
+        }
+        const float dq00 = -(qa * ds00 + qb * ds01 + qc * ds11);
+        const float dq01 = -(qd * ds00 + qe * ds01 + qf * ds11);
+        const float dq11 = -(qc * ds00 + qg * ds01 + qh * ds11);
+        du[k] = j00 * dpx + j02 * dpz;
+        dv[k] = j11 * dpy + j12 * dpz;
+        da[k] = dq00;
+        db[k] = swap ? dq11 : dq01;
+        dc[k] = swap ? dq01 : dq11;
+    }
+    out[0] = make_float4(du[0], du[1], du[2], du[3]);
+    out[1] = make_float4(du[4], du[5], dv[0], dv[1]);
+    out[2] = make_float4(dv[2], dv[3], dv[4], dv[5]);
+    out[3] = make_float4(da[0], da[1], da[2], da[3]);
+    out[4] = make_float4(da[4], da[5], db[0], db[1]);
+    out[5] = make_float4(db[2], db[3], db[4], db[5]);
+    out[6] = make_float4(dc[0], dc[1], dc[2], dc[3]);
+    out[7] = make_float4(dc[4], dc[5], x, y);
+}
+
+template <int STAGE, int BATCH, int NX>
+__device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH, NX>& sb, int pos, const float4& r0,
+                                           const float4& r1, const float4& r2, float vrej, int li, uint32_t g) {
     sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
     sb.B[pos] = make_float4(r1.z, vrej, log2_opacity(r0.w), r0.z);
     sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
     sb.D[pos] = r2.w;
     sb.orig[pos] = li;
-    if (!FORWARD) {
+    if constexpr (STAGE == kStageRay) {
         const float rgx = (r0.x - a.K.cx) * __frcp_rn(a.K.fx), rgy = (r0.y - a.K.cy) * __frcp_rn(a.K.fy);
-        sb.E[pos] = make_float4(rgx, rgy, -a.K.fx * rgx, -a.K.fy * rgy);
+        sb.X[0][pos] = make_float4(rgx, rgy, -a.K.fx * rgx, -a.K.fy * rgy);
+    } else if constexpr (STAGE == kStageDeriv) {
+        static_assert(NX == 8, "the analytic Jacobian stages eight derivative planes");
+        float4 d[8];
+        stage_deriv(a, r0, r1, a.geo0[g], a.geo1[g], d);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sb.X[k][pos] = d[k];
     }
 }
 
@@ -205,8 +285,8 @@ __device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH>
 // entries 256 at a time (one per thread; BATCH = 128 uses half the threads),
 // each round compacted after the previous one, so the staged order is the
 // list order.  Ends with a barrier.
-template <bool REF_LAYOUT, bool FORWARD, int BATCH = kBatch>
-__device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH>& sb, uint32_t list0, int base,
+template <bool REF_LAYOUT, bool FORWARD, int STAGE, int BATCH, int NX>
+__device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH, NX>& sb, uint32_t list0, int base,
                                            int limit, float x0, float y0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     int total = 0;
@@ -216,8 +296,9 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH>
         bool keep = false;
         float4 r0v, r1, r2;
         float vrej = 0.f;
+        uint32_t g = 0;
         if (r0 + tid < BATCH && li < limit) {
-            const uint32_t g = a.indices[list0 + li];
+            g = a.indices[list0 + li];
             if (g < a.n_gauss) {
                 load_record<REF_LAYOUT>(a, g, r0v, r1, r2);
                 vrej = reject_bound(r0v.w);
@@ -234,7 +315,8 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH>
             wbase += (k < w) ? c : 0;
             round_total += c;
         }
-        if (keep) put_staged<FORWARD>(a, sb, total + wbase + __popc(bal & lanemask_lt()), r0v, r1, r2, vrej, li);
+        if (keep)
+            put_staged<STAGE>(a, sb, total + wbase + __popc(bal & lanemask_lt()), r0v, r1, r2, vrej, li, g);
         total += round_total;
         __syncthreads();
     }
@@ -365,7 +447,7 @@ __device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps
         wbase += (k < w) ? c : 0;
         total += c;
     }
-    if (keep) put_staged<FORWARD>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li);
+    if (keep) put_staged<FORWARD ? kStageNone : kStageRay>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li, g);
     const bool next = ready && base + kBatch < limit;
     if (next && tid == 0) tma_bar_expect(&ts.bar, kTmaBatchBytes);
     __syncthreads();
@@ -399,12 +481,30 @@ __device__ __forceinline__ void tma_drain(const TrackArgs& a, TmaStage& ts, TmaS
     }
 }
 
-template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4, bool TMA = false, int BATCH = kBatch>
+// Depth weight of a pixel's depth residual: the reference's
+// (|e| < thr ? 1 : thr / |e|) / z_obs (src/GSCudaKernels.cu:1120-1121) with
+// FVGS_Q_DEPTH_HUBER, else Tukey's biweight (1 - (e / thr)^2)^2 / z_obs, zero
+// beyond thr.
+__device__ __forceinline__ float depth_weight(float derr, float thr, float z_obs, bool huber) {
+    const float ld = fabsf(derr);
+    float w;
+    if (huber) {
+        w = (ld < thr) ? 1.0f : thr / ld;
+    } else {
+        const float r = ld / thr, t = 1.0f - r * r;
+        w = (ld < thr) ? t * t : 0.0f;
+    }
+    return w / z_obs;
+}
+
+template <bool RENDER_ONLY, bool REF_LAYOUT = false, int MIN_CTAS = 4, bool TMA = false, int BATCH = kBatch,
+          bool ANALYTIC = false>
 __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a, const __grid_constant__ RecMaps maps) {
     static_assert(!TMA || BATCH == kBatch, "the TMA staging gathers batches of kBatch records");
     static_assert(BATCH % 128 == 0 && BATCH <= 2 * kPix, "batch of 128, 256 or 512 Gaussians");
+    static_assert(!ANALYTIC || (!TMA && !REF_LAYOUT && BATCH <= kBatch), "analytic Jacobian: packed records, plain staging");
     pdl_begin();
-    __shared__ TrackBatch<BATCH> sb;
+    __shared__ TrackBatch<BATCH, ANALYTIC ? 8 : 1> sb;
     __shared__ float s_red[kPix / 32][32];
     __shared__ uint32_t s_nmax;
     extern __shared__ __align__(128) unsigned char s_dyn[];  // TMA variant: the gathered batch
@@ -447,7 +547,7 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
             if constexpr (TMA)
                 cnt = stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm);
             else
-                cnt = stage_batch<REF_LAYOUT, true, BATCH>(a, sb, range.x, base, n, x0, y0);
+                cnt = stage_batch<REF_LAYOUT, true, kStageNone>(a, sb, range.x, base, n, x0, y0);
             if (!done) {
                 int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
@@ -529,8 +629,18 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
 #pragma unroll
     for (int k = 0; k < 6; ++k) bv[k] = 0.f;
     const float fx = a.K.fx, fy = a.K.fy, cx = a.K.cx, cy = a.K.cy;
+    const bool huber = (a.quirks & FVGS_Q_DEPTH_HUBER) != 0;
     float e0 = 0.f, e1 = 0.f, e2 = 0.f, wc = 0.f, derr = 0.f, wd = 0.f;
-    if (do_jac) {
+    if (ANALYTIC && do_jac) {
+        e0 = cr - a.obs_rgb[3 * p];
+        e1 = cg - a.obs_rgb[3 * p + 1];
+        e2 = cb - a.obs_rgb[3 * p + 2];
+        derr = depth - img_depth;
+        const float closs = sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+        wc = (closs < a.color_thresh) ? 1.0f : a.color_thresh / closs;
+        wd = depth_weight(derr, a.depth_thresh, img_depth, huber);
+    }
+    if (!ANALYTIC && do_jac) {
         e0 = cr - a.obs_rgb[3 * p];
         e1 = cg - a.obs_rgb[3 * p + 1];
         e2 = cb - a.obs_rgb[3 * p + 2];
@@ -555,8 +665,7 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
         Jr0 *= -wc;
         Jr1 *= -wc;
         Jr2 *= -wc;
-        const float ld = fabsf(derr);
-        wd = ((ld < a.depth_thresh) ? 1.0f : a.depth_thresh / ld) / img_depth;
+        wd = depth_weight(derr, a.depth_thresh, img_depth, huber);
         // wd * ray ray^T: the rotation block gets ray x ray = 0
         {
             const float r[3] = {rx, ry, 1.0f};
@@ -587,19 +696,26 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
     if (do_jac && n_contrib > 0) atomicMax(&s_nmax, n_contrib);
     __syncthreads();
     const int nmax = (int)min((uint32_t)n, s_nmax);
-    // rem = final colour minus the colour accumulated so far (running)
-    float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
-    bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
-    bool done2 = !do_jac;
-    if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
-    for (int base = 0; base < nmax; base += BATCH) {
-        if (__syncthreads_and(done2)) break;
-        int cnt;
-        if constexpr (TMA)
-            cnt = stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm);
-        else
-            cnt = stage_batch<REF_LAYOUT, false, BATCH>(a, sb, range.x, base, nmax, x0, y0);
-        if (!done2) {
+    if constexpr (ANALYTIC) {
+        // Colour Jacobian jc (3 x 6) and depth Jacobian jd of the pixel over
+        // the Gaussians the forward pass blended, in its order: for each,
+        // dC/dalpha = c T - (C - A) / (1 - alpha) (A: colour accumulated up
+        // to and including it, C: final colour with background), dalpha/dv =
+        // -alpha / 2 (0 where alpha is clamped at 0.99) and dv/ddelta from
+        // the staged derivatives; jd is the derivative of
+        // d = z + dx phat.x + dy phat.y of the Gaussian where T crosses 0.5.
+        float jc[3][6], jd[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            jc[0][k] = jc[1][k] = jc[2][k] = 0.f;
+            jd[k] = 0.f;
+        }
+        float prod = 1.f, remr = cr, remg = cg, remb = cb;
+        bool done2 = !do_jac;
+        for (int base = 0; base < nmax; base += BATCH) {
+            if (__syncthreads_and(done2)) break;
+            const int cnt = stage_batch<false, true, kStageDeriv>(a, sb, range.x, base, nmax, x0, y0);
+            if (done2) continue;
             for (int j = 0; j < cnt; ++j) {
                 if (sb.orig[j] >= (int)n_contrib) {
                     done2 = true;
@@ -610,71 +726,153 @@ __global__ void __launch_bounds__(kPix, MIN_CTAS) track_tile_kernel(TrackArgs a,
                 const float dx = rA.x - xf, dy = rA.y - yf;
                 float dl0, dl1;
                 const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
-                if (v > rB.y) continue;
-                const float alpha = gauss_alpha(rB.z, v);
+                if (v > rB.y || v <= 0.0f) continue;
+                const float raw = gauss_weight(rB.z, v);
+                const float alpha = fminf(0.99f, raw);
                 if (alpha < kInv255) continue;
                 const float4 rC = sb.C[j];
-                const float4 rE = sb.E[j];
-                const float d = depth_fast(rB.w, dx, rC.x, dy, rC.y);
-                float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
-                remr -= alpha * da0;
-                remg -= alpha * da1;
-                remb -= alpha * da2;
+                float d0 = rC.z * prod, d1 = rC.w * prod, d2 = sb.D[j] * prod;
+                remr -= alpha * d0;
+                remg -= alpha * d1;
+                remb -= alpha * d2;
                 const float inv1m = rcp_approx(1.0f - alpha);
-                da0 -= remr * inv1m;
-                da1 -= remg * inv1m;
-                da2 -= remb * inv1m;
-                // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
-                // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
-                // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
-                const float g0 = fx * dl0, g1 = fy * dl1, g2 = rE.z * dl0 + rE.w * dl1;
-                const float inv_d = rcp_approx(d);
-                const float u0 = g0 * inv_d, u1 = g1 * inv_d, u2 = g2 * inv_d;
-                const float u3 = rE.y * g2 - g1, u4 = g0 - rE.x * g2, u5 = rE.x * g1 - rE.y * g0;
-                const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
-                {
-                    const float u[6] = {u0, u1, u2, u3, u4, u5};
-                    int idx = 0;
+                const float kf = (raw > 0.99f) ? 0.0f : -0.5f * alpha;
+                const float k0 = kf * (d0 - remr * inv1m), k1 = kf * (d1 - remg * inv1m),
+                            k2 = kf * (d2 - remb * inv1m);
+                const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
+                const float4 X0 = sb.X[0][j], X1 = sb.X[1][j], X2 = sb.X[2][j], X3 = sb.X[3][j];
+                const float4 X4 = sb.X[4][j], X5 = sb.X[5][j], X6 = sb.X[6][j], X7 = sb.X[7][j];
+                const float du[6] = {X0.x, X0.y, X0.z, X0.w, X1.x, X1.y};
+                const float dv[6] = {X1.z, X1.w, X2.x, X2.y, X2.z, X2.w};
+                const float da[6] = {X3.x, X3.y, X3.z, X3.w, X4.x, X4.y};
+                const float db[6] = {X4.z, X4.w, X5.x, X5.y, X5.z, X5.w};
+                const float dc[6] = {X6.x, X6.y, X6.z, X6.w, X7.x, X7.y};
+                float gv[6];
 #pragma unroll
-                    for (int i = 0; i < 6; ++i) {
-                        const float wu = w * u[i];
+                for (int k = 0; k < 6; ++k) {
+                    gv[k] = cu * du[k] + cv * dv[k] + ca * da[k] + cb2 * db[k] + cc * dc[k];
+                    jc[0][k] += k0 * gv[k];
+                    jc[1][k] += k1 * gv[k];
+                    jc[2][k] += k2 * gv[k];
+                }
+                const float np = prod * (1.0f - alpha);
+                if (prod > 0.5f && np < 0.5f) {
+                    // d phat = (dp_x / z^2 - 2 x dp_z / z^3, dp_y / z^2 - 2 y dp_z / z^3)
+                    const float z = rB.w, x = X7.z, y = X7.w;
+                    const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
 #pragma unroll
-                        for (int k = i; k < 6; ++k) A[idx++] += wu * u[k];
+                    for (int k = 0; k < 6; ++k) {
+                        const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
+                        const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
+                        const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
+                        const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
+                        const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
+                        jd[k] = dpz + rC.x * du[k] + dx * dphx + rC.y * dv[k] + dy * dphy;
                     }
                 }
-                const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
-                bv[0] += coef * u0;
-                bv[1] += coef * u1;
-                bv[2] += coef * u2;
-                bv[3] += coef * u3;
-                bv[4] += coef * u4;
-                bv[5] += coef * u5;
-                prod_alpha *= (1.0f - alpha);
-                if (depth_pending && prod_alpha <= 0.5f) {
-                    // the depth term wd * derr * r: its rotation part d (r x r) is zero
-                    depth_pending = false;
-                    const float r[3] = {rE.x, rE.y, 1.0f};
-                    int idx = 0;
+                prod = np;
+            }
+        }
+        if (do_jac) {
+            int idx = 0;
 #pragma unroll
-                    for (int i = 0; i < 3; ++i) {
+            for (int i = 0; i < 6; ++i) {
 #pragma unroll
-                        for (int jj = i; jj < 6; ++jj) {
-                            if (jj < 3) A[idx] += wd * r[i] * r[jj];
-                            ++idx;
+                for (int k = i; k < 6; ++k)
+                    A[idx++] = wc * (jc[0][i] * jc[0][k] + jc[1][i] * jc[1][k] + jc[2][i] * jc[2][k]) +
+                               wd * jd[i] * jd[k];
+                bv[i] = -(wc * (jc[0][i] * e0 + jc[1][i] * e1 + jc[2][i] * e2) + wd * jd[i] * derr);
+            }
+        }
+    } else {
+        // rem = final colour minus the colour accumulated so far (running)
+        float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
+        bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
+        bool done2 = !do_jac;
+        if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
+        for (int base = 0; base < nmax; base += BATCH) {
+            if (__syncthreads_and(done2)) break;
+            int cnt;
+            if constexpr (TMA)
+                cnt = stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm);
+            else
+                cnt = stage_batch<REF_LAYOUT, false, kStageRay>(a, sb, range.x, base, nmax, x0, y0);
+            if (!done2) {
+                for (int j = 0; j < cnt; ++j) {
+                    if (sb.orig[j] >= (int)n_contrib) {
+                        done2 = true;
+                        break;
+                    }
+                    const float4 rA = sb.A[j];
+                    const float4 rB = sb.B[j];
+                    const float dx = rA.x - xf, dy = rA.y - yf;
+                    float dl0, dl1;
+                    const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
+                    if (v > rB.y) continue;
+                    const float alpha = gauss_alpha(rB.z, v);
+                    if (alpha < kInv255) continue;
+                    const float4 rC = sb.C[j];
+                    const float4 rE = sb.X[0][j];
+                    const float d = depth_fast(rB.w, dx, rC.x, dy, rC.y);
+                    float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
+                    remr -= alpha * da0;
+                    remg -= alpha * da1;
+                    remb -= alpha * da2;
+                    const float inv1m = rcp_approx(1.0f - alpha);
+                    da0 -= remr * inv1m;
+                    da1 -= remg * inv1m;
+                    da2 -= remb * inv1m;
+                    // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
+                    // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
+                    // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
+                    const float g0 = fx * dl0, g1 = fy * dl1, g2 = rE.z * dl0 + rE.w * dl1;
+                    const float inv_d = rcp_approx(d);
+                    const float u0 = g0 * inv_d, u1 = g1 * inv_d, u2 = g2 * inv_d;
+                    const float u3 = rE.y * g2 - g1, u4 = g0 - rE.x * g2, u5 = rE.x * g1 - rE.y * g0;
+                    const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
+                    {
+                        const float u[6] = {u0, u1, u2, u3, u4, u5};
+                        int idx = 0;
+    #pragma unroll
+                        for (int i = 0; i < 6; ++i) {
+                            const float wu = w * u[i];
+    #pragma unroll
+                            for (int k = i; k < 6; ++k) A[idx++] += wu * u[k];
                         }
                     }
-                    bv[0] += wd * derr * rE.x;
-                    bv[1] += wd * derr * rE.y;
-                    bv[2] += wd * derr;
-                }
-                if (prod_alpha < 0.001f) {
-                    done2 = true;
-                    break;
+                    const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
+                    bv[0] += coef * u0;
+                    bv[1] += coef * u1;
+                    bv[2] += coef * u2;
+                    bv[3] += coef * u3;
+                    bv[4] += coef * u4;
+                    bv[5] += coef * u5;
+                    prod_alpha *= (1.0f - alpha);
+                    if (depth_pending && prod_alpha <= 0.5f) {
+                        // the depth term wd * derr * r: its rotation part d (r x r) is zero
+                        depth_pending = false;
+                        const float r[3] = {rE.x, rE.y, 1.0f};
+                        int idx = 0;
+    #pragma unroll
+                        for (int i = 0; i < 3; ++i) {
+    #pragma unroll
+                            for (int jj = i; jj < 6; ++jj) {
+                                if (jj < 3) A[idx] += wd * r[i] * r[jj];
+                                ++idx;
+                            }
+                        }
+                        bv[0] += wd * derr * rE.x;
+                        bv[1] += wd * derr * rE.y;
+                        bv[2] += wd * derr;
+                    }
+                    if (prod_alpha < 0.001f) {
+                        done2 = true;
+                        break;
+                    }
                 }
             }
         }
     }
-
     if (TMA) tma_drain(a, ts, tm);
 
     // --------------------------- tile reduction ------------------------------
@@ -1106,6 +1304,19 @@ cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s
     RecMaps m{};
     if (maps) m = *maps;
     if (a.render_only) return launch_chained(track_tile_kernel<true>, dim3(T), dim3(kPix), 0, s, a, m);
+    if (!(a.quirks & FVGS_Q_POSE_JAC_APPROX)) {
+        // analytic Jacobian: plain staging of up to 256 Gaussians per batch
+        // (the derivative planes fill the rest of the shared memory)
+        if (!a.geo0 || !a.geo1) return cudaErrorInvalidValue;
+        if (a.variant == 1)
+            return launch_chained(track_tile_kernel<false, false, 3, false, kBatch, true>, dim3(T), dim3(kPix), 0, s,
+                                  a, m);
+        if (a.variant == 3)
+            return launch_chained(track_tile_kernel<false, false, 4, false, 128, true>, dim3(T), dim3(kPix), 0, s, a,
+                                  m);
+        return launch_chained(track_tile_kernel<false, false, 4, false, kBatch, true>, dim3(T), dim3(kPix), 0, s, a,
+                              m);
+    }
     if (a.variant == 1) return launch_chained(track_tile_kernel<false, false, 3>, dim3(T), dim3(kPix), 0, s, a, m);
     if (a.variant == 3)
         return launch_chained(track_tile_kernel<false, false, 4, false, 128>, dim3(T), dim3(kPix), 0, s, a, m);

@@ -28,8 +28,13 @@ Q_VIS_CAP256 = 0x10
 Q_ADAM_STAY = 0x20
 Q_POSE_WXYZ = 0x40
 Q_COLOR_RESCALE = 0x80
+Q_POSE_JAC_APPROX = 0x100
+Q_DEPTH_HUBER = 0x200
 QUIRKS_DEFAULT = (Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY | Q_POSE_WXYZ
-                  | Q_COLOR_RESCALE)
+                  | Q_COLOR_RESCALE | Q_POSE_JAC_APPROX | Q_DEPTH_HUBER)
+# every reference behaviour off: the analytic pose Jacobian, Tukey depth weight
+QUIRKS_INTENDED = 0
+MAX_LEVELS = 4  # FVGS_MAX_LEVELS
 
 PRECISION_FP32 = 0
 PRECISION_REDUCED = 1
@@ -328,6 +333,17 @@ class Session:
         )
         return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
 
+    def track_frame_pyramid(self, pose, K0, iterations=(4, 4, 6, 6)):
+        """Coarse-to-fine frame (fvgs_track_frame_pyramid): iterations[l] Gauss-Newton steps at level l,
+        from the coarsest level down; K0 are the level-0 intrinsics."""
+        p = make_pose(pose)
+        step = np.zeros(6, np.float64)
+        it = (C.c_int * len(iterations))(*iterations)
+        _check(self.lib.fvgs_track_frame_pyramid(self.h, C.byref(p), C.byref(make_intr(K0)), it,
+                                                 C.c_int(len(iterations)), _ptr(step)),
+               "fvgs_track_frame_pyramid")
+        return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
+
     def render_view(self, pose, K, W, H, rgb8: bool = False):
         """Render-form image (fvgs_render_view): float rgb (H,W,3), depth (H,W), optional 8-bit rgb."""
         col = np.zeros((H, W, 3), np.float32)
@@ -480,6 +496,13 @@ class Session:
                                           C.c_int(iterations), C.c_float(-1.0 if map_eta is None else map_eta)),
                "fvgs_frame_submit")
 
+    def frame_submit_pyramid(self, pose, K0, iterations=(4, 4, 6, 6), map_eta: float | None = None):
+        it = (C.c_int * len(iterations))(*iterations)
+        _check(self.lib.fvgs_frame_submit_pyramid(self.h, C.byref(make_pose(pose)), C.byref(make_intr(K0)), it,
+                                                  C.c_int(len(iterations)),
+                                                  C.c_float(-1.0 if map_eta is None else map_eta)),
+               "fvgs_frame_submit_pyramid")
+
     def frame_poll(self) -> bool:
         d = C.c_int()
         _check(self.lib.fvgs_frame_poll(self.h, C.byref(d)), "fvgs_frame_poll")
@@ -510,13 +533,28 @@ def frames_run(sessions, poses, Ks, iterations: int = 20, levels=None, map_etas=
     return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
 
 
+def frames_run_pyramid(sessions, poses, K0s, iterations=(4, 4, 6, 6), map_etas=None):
+    """One coarse-to-fine frame on each session, overlapped on the device (fvgs_frames_run_pyramid)."""
+    lib = load_library()
+    n = len(sessions)
+    hs = (C.c_void_p * n)(*[s.h for s in sessions])
+    ps = (Pose * n)(*[make_pose(p) for p in poses])
+    ks = (Intrinsics * n)(*[make_intr(k) for k in K0s])
+    it = (C.c_int * len(iterations))(*iterations)
+    et = None if map_etas is None else (C.c_float * n)(*[(-1.0 if e is None else e) for e in map_etas])
+    _check(lib.fvgs_frames_run_pyramid(hs, ps, ks, it, C.c_int(len(iterations)), et, C.c_int(n)),
+           "fvgs_frames_run_pyramid")
+    return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
+
+
 # ---- serving (include/fvgs_server.h) ----
 class ServerRequest(C.Structure):
     _fields_ = [("pose", Pose), ("K", Intrinsics), ("level", C.c_int), ("iterations", C.c_int),
                 ("map_eta", C.c_float), ("tag", C.c_uint64), ("t_arrival", C.c_double),
                 ("rgb", C.c_void_p), ("depth", C.c_void_p), ("grad_x", C.c_void_p), ("grad_y", C.c_void_p),
                 ("width", C.c_int), ("height", C.c_int), ("raw_color", C.c_void_p), ("raw_depth", C.c_void_p),
-                ("raw_depth_u16_mm", C.c_int), ("raw_levels", C.c_int), ("raw_double_scale", C.c_int)]
+                ("raw_depth_u16_mm", C.c_int), ("raw_levels", C.c_int), ("raw_double_scale", C.c_int),
+                ("pyr_levels", C.c_int), ("pyr_iterations", C.c_int * MAX_LEVELS)]
 
 
 class ServerResult(C.Structure):
@@ -560,14 +598,19 @@ class Server:
         return float(t.value)
 
     def submit(self, slot: int, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None,
-               tag: int = 0, t_arrival: float = 0.0, frame=None, raw=None):
+               tag: int = 0, t_arrival: float = 0.0, frame=None, raw=None, pyramid=None):
         """frame: optional (rgb_ptr, depth_ptr, gx_ptr, gy_ptr, W, H) of memory that stays valid (pinned
-        host or device) until the result is back; raw: optional (color_u8_ptr, depth_ptr, W, H[, depth_u16])
-        camera frame, preprocessed on the device (level 0)."""
+        host or device) until the result is back, for `level`; raw: optional (color_u8_ptr, depth_ptr, W,
+        H[, depth_u16]) camera frame, preprocessed on the device (level 0); pyramid: optional per-level
+        iteration counts of a coarse-to-fine frame (K is then the level-0 intrinsics)."""
         r = ServerRequest()
         r.pose = make_pose(pose)
         r.K = make_intr(K)
         r.level, r.iterations = level, iterations
+        if pyramid is not None:
+            r.pyr_levels = len(pyramid)
+            for i, v in enumerate(pyramid):
+                r.pyr_iterations[i] = int(v)
         r.map_eta = -1.0 if map_eta is None else map_eta
         r.tag, r.t_arrival = tag, t_arrival
         if frame is not None:

@@ -132,8 +132,12 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
 int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, float* orientations,
                             float* colors, float* opacities, uint32_t n);
 
+/* Pyramid levels a session holds frames for (the reference uses three,
+ * nb_pyr_levels_ = 3, include/f_vigs_slam/GSSlam.cuh:275). */
+#define FVGS_MAX_LEVELS 4
+
 /*
- * Observed frame of pyramid level `level` (0..2): rgb[3P], depth[P],
+ * Observed frame of pyramid level `level` (0..FVGS_MAX_LEVELS-1): rgb[3P], depth[P],
  * grad_x[3P], grad_y[3P], dense row-major (the pyr_color_ / pyr_depth_ /
  * pyr_dx_ / pyr_dy_ images of GSSlam::initAndCopyImgs, src/GSSlam.cu:1913-1969).
  */
@@ -193,15 +197,25 @@ int fvgs_download_track_images(fvgs_session* s, float* color, float* depth, floa
  */
 int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
                      double* last_step);
+/*
+ * A coarse-to-fine tracking frame, the level loop of
+ * GSSlam::optimizeWithCeres (src/GSSlam.cu:2267-2297): for level = levels-1
+ * down to 0, iterations[level] Gauss-Newton steps against that level's frame,
+ * with the level's intrinsics K0 scaled by 2^-level as
+ * GSSlam::computeRgbdPoseJacobians scales them (src/GSSlam.cu:2133-2138).
+ * K0 are the level-0 intrinsics; levels <= FVGS_MAX_LEVELS.
+ */
+int fvgs_track_frame_pyramid(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K0, const int* iterations,
+                             int levels, double* last_step);
 
 /*
  * Asynchronous frames, for serving and batching many sessions at once.
  * fvgs_frame_submit enqueues one frame on the session's stream and returns:
  * `iterations` Gauss-Newton steps from `pose` (as fvgs_track_frame), then,
  * when map_eta >= 0, one mapping step at the tracked pose (as fvgs_map_step).
- * Once the session's binning history is valid, a frame of a given shape
- * (level, iterations, intrinsics, mapping) is captured as a CUDA graph on
- * first use and replayed afterwards.  fvgs_frame_poll reports completion
+ * A frame of a given shape (levels, iterations, intrinsics, mapping, and
+ * whether its first binning continues the session's last one) is captured
+ * as a CUDA graph on first use and replayed afterwards.  fvgs_frame_poll reports completion
  * without blocking; fvgs_frame_wait completes the frame (repeating it
  * eagerly if the instance buffers had to grow) and returns the pose and last
  * step (both nullable).  One frame per session may be in flight.  The
@@ -209,6 +223,10 @@ int fvgs_track_frame(fvgs_session* s, fvgs_pose* pose, const fvgs_intrinsics* K,
  */
 int fvgs_frame_submit(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int iterations,
                       float map_eta);
+/* The same for a coarse-to-fine frame (as fvgs_track_frame_pyramid); the
+ * optional mapping step runs at level 0. */
+int fvgs_frame_submit_pyramid(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K0,
+                              const int* iterations, int levels, float map_eta);
 int fvgs_frame_poll(fvgs_session* s, int* done);
 int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step);
 /* Batched frames: submit one frame on each of n sessions (each on its own
@@ -217,6 +235,10 @@ int fvgs_frame_wait(fvgs_session* s, fvgs_pose* pose, double* last_step);
  * no mapping).  Returns the first error. */
 int fvgs_frames_run(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K, const int* levels,
                     int iterations, const float* map_etas, int n);
+/* Batched coarse-to-fine frames: the same level schedule (iterations[levels])
+ * on every session, K0[i] the level-0 intrinsics of session i. */
+int fvgs_frames_run_pyramid(fvgs_session* const* sessions, fvgs_pose* poses, const fvgs_intrinsics* K0,
+                            const int* iterations, int levels, const float* map_etas, int n);
 /* Frames of the session that ran from a captured graph / eagerly. */
 int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager);
 

@@ -48,6 +48,12 @@ typedef struct fvgs_server_request {
     int raw_depth_u16_mm;
     int raw_levels;
     int raw_double_scale;
+    /* Coarse-to-fine frame instead of one level: when pyr_levels > 0, K is
+     * the level-0 intrinsics and the frame runs pyr_iterations[l] steps at
+     * every level l < pyr_levels from the coarsest down (as
+     * fvgs_frame_submit_pyramid); level and iterations are then unused. */
+    int pyr_levels;
+    int pyr_iterations[FVGS_MAX_LEVELS];
 } fvgs_server_request;
 
 typedef struct fvgs_server_result {

@@ -70,6 +70,22 @@ typedef enum fvgs_status {
  *  COLOR_RESCALE (host mirror) computeRgbdPoseJacobians scales the [0, 1]
  *                colour pyramid by 1/255 once more (src/GSSlam.cu:2158).
  *                Clear: the pyramid colour as is.
+ *  POSE_JAC_APPROX getRgbdPoseJacobians' approximate pose Jacobian
+ *                (src/GSCudaKernels.cu:1043-1350): a per-pixel term from the
+ *                observed image's Sobel gradients at the observed depth plus,
+ *                per contributing Gaussian, the derivative through its screen
+ *                mean taken at the cancelling per-pixel depth
+ *                z + dx phat.x + dy phat.y.  Clear: the analytic derivative of
+ *                the rendered colour and median depth with respect to the pose
+ *                update, through every blended Gaussian's screen mean, conic
+ *                and depth (the gradient images are then not read).
+ *  DEPTH_HUBER   the tracking depth weight (|e| < 0.2 ? 1 : 0.2 / |e|) / z_obs
+ *                (src/GSCudaKernels.cu:1120-1121, 1283-1284; 0.2 is
+ *                depth_thresh).  Clear: Tukey's biweight
+ *                (1 - (e / depth_thresh)^2)^2 / z_obs, zero beyond
+ *                depth_thresh: a median depth jumps between the layers of a
+ *                map at occlusion edges, and those residuals would otherwise
+ *                pull the pose.
  */
 #define FVGS_Q_CULLED_SLOTS  0x1u
 #define FVGS_Q_RANGE_LAUNCH  0x2u
@@ -79,12 +95,18 @@ typedef enum fvgs_status {
 #define FVGS_Q_ADAM_STAY     0x20u
 #define FVGS_Q_POSE_WXYZ     0x40u
 #define FVGS_Q_COLOR_RESCALE 0x80u
+#define FVGS_Q_POSE_JAC_APPROX 0x100u
+#define FVGS_Q_DEPTH_HUBER   0x200u
 /* Default: the reference's arithmetic (swap, caps, optimiser state left in
- * place, the host's pose order and colour rescale) with the two launch/slot
- * defects that make its outputs degenerate (NaN tile 0, empty ranges) off. */
+ * place, the host's pose order and colour rescale, the approximate pose
+ * Jacobian and its depth weight) with the two launch/slot defects that make its outputs
+ * degenerate (NaN tile 0, empty ranges) off. */
 #define FVGS_QUIRKS_DEFAULT                                                                          \
     (FVGS_Q_INVSIGMA_SWAP | FVGS_Q_MAP_CAP256 | FVGS_Q_VIS_CAP256 | FVGS_Q_ADAM_STAY | FVGS_Q_POSE_WXYZ | \
-     FVGS_Q_COLOR_RESCALE)
+     FVGS_Q_COLOR_RESCALE | FVGS_Q_POSE_JAC_APPROX | FVGS_Q_DEPTH_HUBER)
+/* Every reference behaviour off: the intended semantics, and the analytic
+ * pose Jacobian with which Gauss-Newton tracking converges. */
+#define FVGS_QUIRKS_INTENDED 0u
 
 typedef struct fvgs_pose {
     float position[3];     /* camera centre in world frame */

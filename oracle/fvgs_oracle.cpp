@@ -196,6 +196,22 @@ const double k099 = (double)0.99f;
 const double k1em4 = (double)0.0001f;
 const double k1em3 = (double)0.001f;
 
+// Depth weight of the tracking residual: the reference's
+// (|e| < thr ? 1 : thr / |e|) / z_obs (src/GSCudaKernels.cu:1120-1121,
+// 1283-1284) with FVGS_Q_DEPTH_HUBER, else Tukey's biweight
+// (1 - (e / thr)^2)^2 / z_obs, zero beyond thr.
+inline double depth_w(double derr, double thr, double z_obs, bool huber) {
+    const double ld = std::fabs(derr);
+    double w;
+    if (huber) {
+        w = (ld < thr) ? 1.0 : thr / ld;
+    } else {
+        const double r = ld / thr, t = 1.0 - r * r;
+        w = (ld < thr) ? t * t : 0.0;
+    }
+    return w / z_obs;
+}
+
 struct Rec {  // one Gaussian's 2D record as the blending kernels consume it
     double u, v, z, o, cx, cy, cz, phx, phy, r, g, b;
 };
@@ -413,6 +429,7 @@ int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indic
     const double bg[3] = {P->bg[0], P->bg[1], P->bg[2]};
     const double alpha_thresh = P->alpha_thresh, color_thresh = P->color_thresh,
                  depth_thresh = P->depth_thresh;
+    const bool huber = (P->quirks & FVGS_Q_DEPTH_HUBER) != 0;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int t = 0; t < T; ++t) {
         const int tx = t % ntx, ty = t / ntx;
@@ -508,9 +525,7 @@ int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indic
                 for (int r = 0; r < 3; ++r)
                     Jr[r] = -wc * (Jc[r * 3] * e[0] + Jc[r * 3 + 1] * e[1] + Jc[r * 3 + 2] * e[2]);
                 {
-                    const double ld = std::fabs(depth_error);
-                    double wd = (ld < depth_thresh) ? 1.0 : depth_thresh / ld;
-                    wd /= imgd;
+                    const double wd = depth_w(depth_error, depth_thresh, imgd, huber);
                     for (int r = 0; r < 3; ++r)
                         for (int c = 0; c < 3; ++c) JJ[r * 3 + c] += wd * ray[r] * ray[c];
                     for (int r = 0; r < 3; ++r) Jr[r] += wd * depth_error * ray[r];
@@ -589,9 +604,7 @@ int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indic
                     prod_alpha *= (1.0 - a);
                     if (Tm > 0.5 && prod_alpha <= 0.5 && imgd > 0.5) {
                         Tm = prod_alpha;
-                        const double ld = std::fabs(depth_error);
-                        double wd = (ld < depth_thresh) ? 1.0 : depth_thresh / ld;
-                        wd /= imgd;
+                        const double wd = depth_w(depth_error, depth_thresh, imgd, huber);
                         for (int r = 0; r < 3; ++r)
                             for (int c = 0; c < 3; ++c) JJg[r * 3 + c] += wd * rg[r] * rg[c];
                         for (int r = 0; r < 3; ++r) Jrg[r] += wd * depth_error * rg[r];
@@ -620,6 +633,445 @@ int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indic
     return 0;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Analytic pose Jacobian (the tracking kernel with FVGS_Q_POSE_JAC_APPROX
+// clear).  The residuals are those of getRgbdPoseJacobians
+// (src/GSCudaKernels.cu:979-1052: rendered colour minus observed colour with
+// the colour weight, median depth minus observed depth with the depth
+// weight, pixels with observed depth > 0.1 and final T < alpha_thresh), but
+// the Jacobian is the exact derivative of the rendered colour and median depth
+// with respect to the pose update of PoseLocalParameterization::Plus
+// (src/PoseLocalParameterization.cpp:22-44): delta = (dp, dtheta) with
+// t' = t + dp, q' = q (x) exp(dtheta).  With p_cam = R^T (p - t):
+//   d p_cam / d dp = -R^T,   d p_cam / d dtheta = [p_cam]x,
+//   d Sigma_cam / d dtheta_j = -[e_j]x Sigma_cam + Sigma_cam [e_j]x.
+// Each contributor's screen mean (u, v), conic (the consumed slots a, b, c of
+// v = a dx^2 + 2 b dx dy + c dy^2), depth z and p_hat move with the pose; the
+// colour follows through alpha = o exp(-v/2) (zero where alpha is clamped at
+// 0.99) and the depth through d = z + dx phat.x + dy phat.y of the Gaussian
+// where T crosses 0.5.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct GeoD {  // derivatives of one Gaussian's screen quantities w.r.t. delta
+    double du[6], dv[6], da[6], db[6], dc[6], dz[6], dphx[6], dphy[6];
+};
+
+// c3 = (x, y, z, Sxx, Sxy, Sxz, Syy, Syz, Szz): camera-frame mean and 3D
+// covariance.  Tangent columns 0-2 are the translation, expressed in the
+// frame given by Tr (rows of Tr are the columns of d p_cam / d dp up to sign:
+// world frame Tr = R, camera frame Tr = I), 3-5 the rotation.
+void gauss_derivs(const double* c3, const double Tr[3][3], double fx, double fy, bool swap, GeoD& o) {
+    const double x = c3[0], y = c3[1], z = c3[2];
+    const double S[3][3] = {{c3[3], c3[4], c3[5]}, {c3[4], c3[6], c3[7]}, {c3[5], c3[7], c3[8]}};
+    const double iz = 1.0 / z, iz2 = iz * iz, iz3 = iz2 * iz;
+    const double J0[3] = {fx * iz, 0.0, -fx * x * iz2};
+    const double J1[3] = {0.0, fy * iz, -fy * y * iz2};
+    double M0[3], M1[3];
+    for (int i = 0; i < 3; ++i) {
+        M0[i] = S[i][0] * J0[0] + S[i][1] * J0[1] + S[i][2] * J0[2];
+        M1[i] = S[i][0] * J1[0] + S[i][1] * J1[1] + S[i][2] * J1[2];
+    }
+    const double s00 = J0[0] * M0[0] + J0[1] * M0[1] + J0[2] * M0[2];
+    const double s01 = J0[0] * M1[0] + J0[1] * M1[1] + J0[2] * M1[2];
+    const double s11 = J1[0] * M1[0] + J1[1] * M1[1] + J1[2] * M1[2];
+    const double det = s00 * s11 - s01 * s01;
+    const double q00 = s11 / det, q01 = -s01 / det, q11 = s00 / det;
+    for (int k = 0; k < 6; ++k) {
+        double dp[3];
+        double dS[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (k < 3) {
+            for (int i = 0; i < 3; ++i) dp[i] = -Tr[k][i];
+        } else {
+            const int j = k - 3;
+            const double e[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
+            // p x e
+            dp[0] = y * e[2] - z * e[1];
+            dp[1] = z * e[0] - x * e[2];
+            dp[2] = x * e[1] - y * e[0];
+            const double E[3][3] = {{0, -e[2], e[1]}, {e[2], 0, -e[0]}, {-e[1], e[0], 0}};
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    double s = 0.0;
+                    for (int m = 0; m < 3; ++m) s += -E[r][m] * S[m][c] + S[r][m] * E[m][c];
+                    dS[r][c] = s;
+                }
+        }
+        const double dJ0[3] = {-fx * iz2 * dp[2], 0.0, -fx * iz2 * dp[0] + 2.0 * fx * x * iz3 * dp[2]};
+        const double dJ1[3] = {0.0, -fy * iz2 * dp[2], -fy * iz2 * dp[1] + 2.0 * fy * y * iz3 * dp[2]};
+        double ds00 = 0, ds01 = 0, ds11 = 0;
+        for (int i = 0; i < 3; ++i) {
+            ds00 += 2.0 * dJ0[i] * M0[i];
+            ds01 += dJ0[i] * M1[i] + dJ1[i] * M0[i];
+            ds11 += 2.0 * dJ1[i] * M1[i];
+        }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                ds00 += J0[r] * dS[r][c] * J0[c];
+                ds01 += J0[r] * dS[r][c] * J1[c];
+                ds11 += J1[r] * dS[r][c] * J1[c];
+            }
+        // d(Sigma^-1) = -Q dSigma Q
+        const double dq00 = -(q00 * q00 * ds00 + 2.0 * q00 * q01 * ds01 + q01 * q01 * ds11);
+        const double dq01 = -(q00 * q01 * ds00 + (q00 * q11 + q01 * q01) * ds01 + q01 * q11 * ds11);
+        const double dq11 = -(q01 * q01 * ds00 + 2.0 * q01 * q11 * ds01 + q11 * q11 * ds11);
+        o.du[k] = J0[0] * dp[0] + J0[1] * dp[1] + J0[2] * dp[2];
+        o.dv[k] = J1[0] * dp[0] + J1[1] * dp[1] + J1[2] * dp[2];
+        o.da[k] = dq00;
+        o.db[k] = swap ? dq11 : dq01;
+        o.dc[k] = swap ? dq01 : dq11;
+        o.dz[k] = dp[2];
+        o.dphx[k] = dp[0] * iz2 - 2.0 * x * iz3 * dp[2];
+        o.dphy[k] = dp[1] * iz2 - 2.0 * y * iz3 * dp[2];
+    }
+}
+
+// FP64 camera-frame mean and covariance of one Gaussian (the projection's
+// formulas, src/GSCudaKernels.cu:366-433).
+void cam3d_one(const float* p, const float* s, const float* q, const double t[3], const double R[3][3], double* o) {
+    const double d[3] = {(double)p[0] - t[0], (double)p[1] - t[1], (double)p[2] - t[2]};
+    double pc[3];
+    for (int i = 0; i < 3; ++i) pc[i] = R[0][i] * d[0] + R[1][i] * d[1] + R[2][i] * d[2];
+    double Rg[3][3];
+    quat_to_R_f64(q, Rg);
+    double M[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[i][j] = Rg[i][j] * (double)s[j];
+    double Sg[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Sg[i][j] = M[i][0] * M[j][0] + M[i][1] * M[j][1] + M[i][2] * M[j][2];
+    double C[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) acc += R[k][i] * Sg[k][l] * R[l][j];
+            C[i][j] = acc;
+        }
+    o[0] = pc[0];
+    o[1] = pc[1];
+    o[2] = pc[2];
+    o[3] = C[0][0];
+    o[4] = C[0][1];
+    o[5] = C[0][2];
+    o[6] = C[1][1];
+    o[7] = C[1][2];
+    o[8] = C[2][2];
+}
+
+void quat_to_R_d(const double q[4], double R[3][3]) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    R[0][0] = 1.0 - 2.0 * (y * y + z * z);
+    R[0][1] = 2.0 * (x * y - w * z);
+    R[0][2] = 2.0 * (x * z + w * y);
+    R[1][0] = 2.0 * (x * y + w * z);
+    R[1][1] = 1.0 - 2.0 * (x * x + z * z);
+    R[1][2] = 2.0 * (y * z - w * x);
+    R[2][0] = 2.0 * (x * z - w * y);
+    R[2][1] = 2.0 * (y * z + w * x);
+    R[2][2] = 1.0 - 2.0 * (x * x + y * y);
+}
+
+}  // namespace
+
+extern "C" {
+
+/*
+ * FP64 camera-frame geometry of every Gaussian at a pose: cam3d[9N] =
+ * (x, y, z, Sxx, Sxy, Sxz, Syy, Syz, Szz), the inputs of the analytic pose
+ * Jacobian.
+ */
+int oracle_cam3d(const float* pos, const float* scl, const float* rot, int n, const fvgs_pose* pose,
+                 double* cam3d) {
+    double R[3][3];
+    quat_to_R_f64(pose->orientation, R);
+    const double t[3] = {pose->position[0], pose->position[1], pose->position[2]};
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i)
+        cam3d_one(pos + 3 * (size_t)i, scl + 3 * (size_t)i, rot + 4 * (size_t)i, t, R, cam3d + 9 * (size_t)i);
+    return 0;
+}
+
+/*
+ * The tracking forward blend (src/GSCudaKernels.cu:979-1041) entirely in FP64
+ * at an FP64 pose (t[3], q[4] (x, y, z, w)), over the given tile lists: the
+ * projection's formulas in FP64 (a Gaussian that this projection culls is
+ * skipped), the consumed conic as the quirk bits select.  Every pixel is
+ * treated as having valid observed depth.  Outputs colour (incl. background)
+ * and median depth per pixel; sig[3P] = (Gaussians blended, list position of
+ * the median-depth Gaussian + 1 (0: none), n_contrib), which identifies the
+ * piecewise-smooth branch a pixel is on.  For finite-difference checks of the
+ * analytic Jacobian.
+ */
+int oracle_forward64(const float* pos, const float* scl, const float* rot, const float* col, const float* opa, int n,
+                     const double* t, const double* q, const fvgs_intrinsics* K, const fvgs_params* P, int W, int H,
+                     const uint32_t* ranges, const uint32_t* indices, double* out_color, double* out_depth,
+                     uint32_t* sig) {
+    double R[3][3];
+    quat_to_R_d(q, R);
+    const double fx = K->fx, fy = K->fy, cx = K->cx, cy = K->cy;
+    const bool swap = (P->quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+    struct G64 {
+        bool ok;
+        double u, v, z, a, b, c, phx, phy;
+    };
+    std::vector<G64> g(n > 0 ? n : 1);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double c3[9];
+        cam3d_one(pos + 3 * (size_t)i, scl + 3 * (size_t)i, rot + 4 * (size_t)i, t, R, c3);
+        G64 o{};
+        const double x = c3[0], y = c3[1], z = c3[2];
+        if (z > 0.0) {
+            const double iz = 1.0 / z;
+            o.u = fx * x * iz + cx;
+            o.v = fy * y * iz + cy;
+            o.ok = !(o.u < 0.0 || o.u >= W || o.v < 0.0 || o.v >= H);
+            const double J0[3] = {fx * iz, 0.0, -fx * x * iz * iz};
+            const double J1[3] = {0.0, fy * iz, -fy * y * iz * iz};
+            const double S[3][3] = {{c3[3], c3[4], c3[5]}, {c3[4], c3[6], c3[7]}, {c3[5], c3[7], c3[8]}};
+            double s00 = 0, s01 = 0, s11 = 0;
+            for (int r = 0; r < 3; ++r)
+                for (int cc = 0; cc < 3; ++cc) {
+                    s00 += J0[r] * S[r][cc] * J0[cc];
+                    s01 += J0[r] * S[r][cc] * J1[cc];
+                    s11 += J1[r] * S[r][cc] * J1[cc];
+                }
+            const double det = s00 * s11 - s01 * s01;
+            const double q00 = s11 / det, q01 = -s01 / det, q11 = s00 / det;
+            o.a = q00;
+            o.b = swap ? q11 : q01;
+            o.c = swap ? q01 : q11;
+            o.z = z;
+            o.phx = x * iz * iz;
+            o.phy = y * iz * iz;
+        }
+        g[i] = o;
+    }
+    const int tw = P->tile_w, th = P->tile_h;
+    const int ntx = (W + tw - 1) / tw, nty = (H + th - 1) / th, T = ntx * nty;
+    const double bg[3] = {P->bg[0], P->bg[1], P->bg[2]};
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int tt = 0; tt < T; ++tt) {
+        const int tx = tt % ntx, ty = tt / ntx;
+        const uint32_t rs = ranges[2 * (size_t)tt], re = ranges[2 * (size_t)tt + 1];
+        for (int ly = 0; ly < th; ++ly)
+            for (int lx = 0; lx < tw; ++lx) {
+                const int x = tx * tw + lx, y = ty * th + ly;
+                if (x >= W || y >= H) continue;
+                const size_t p = (size_t)y * W + x;
+                double c[3] = {0, 0, 0}, depth = 0.0, Tr = 1.0;
+                uint32_t nbl = 0, med = 0, last = 0;
+                for (uint32_t i = rs; i < re; ++i) {
+                    const uint32_t gi = indices[i];
+                    if (gi >= (uint32_t)n || !g[gi].ok) continue;
+                    const G64& o = g[gi];
+                    const uint32_t ord = i - rs + 1;
+                    const double dx = o.u - x, dy = o.v - y;
+                    const double v = o.a * dx * dx + 2.0 * o.b * dx * dy + o.c * dy * dy;
+                    const double al = std::min(k099, (double)opa[gi] * std::exp(-0.5 * v));
+                    if (al < kInv255 || v <= 0.0) continue;
+                    const double test_T = Tr * (1.0 - al);
+                    if (test_T < k1em4) break;
+                    for (int k = 0; k < 3; ++k) c[k] += (double)col[3 * (size_t)gi + k] * al * Tr;
+                    if (Tr > 0.5 && test_T < 0.5) {
+                        depth = o.z + dx * o.phx + dy * o.phy;
+                        med = ord;
+                    }
+                    Tr = test_T;
+                    ++nbl;
+                    last = ord;
+                }
+                for (int k = 0; k < 3; ++k) out_color[3 * p + k] = c[k] + Tr * bg[k];
+                out_depth[p] = depth;
+                sig[3 * p] = nbl;
+                sig[3 * p + 1] = med;
+                sig[3 * p + 2] = last;
+            }
+    }
+    return 0;
+}
+
+/*
+ * The tracking kernel with the analytic pose Jacobian, in FP64, one pixel at
+ * a time: the forward blend of oracle_track (same records, lists and
+ * thresholds), then for every valid pixel the colour Jacobian
+ * J_C = sum_i dC/dalpha_i dalpha_i/dv_i dv_i/ddelta over the Gaussians the
+ * forward blended, dC/dalpha_i = c_i T_i - (C - A_i) / (1 - alpha_i) (A_i the
+ * colour accumulated up to and including i, C the final colour with the
+ * background), and the depth Jacobian J_D of the median-depth Gaussian.  A
+ * pixel adds wc J_C^T J_C + wd J_D^T J_D to JtJ and -(wc J_C^T e_c +
+ * wd J_D^T e_d) to the tile's Jtr sum (the reference's per-tile sign;
+ * src/GSSlam.cu:2225 negates it), with the reference's colour and depth
+ * weights.  cam3d (oracle_cam3d at the same pose) supplies the geometry.
+ * Outputs as oracle_track (world frame); optional per-pixel Jacobians
+ * pix_jc[18P] (3 x 6 row-major) and pix_jd[6P].
+ */
+int oracle_track_intended(const float* rec, const double* cam3d, const uint32_t* ranges, const uint32_t* indices,
+                          const float* obs_rgb, const float* obs_depth, const fvgs_pose* pose,
+                          const fvgs_intrinsics* Kf, const fvgs_params* P, int W, int H, double* tile_out,
+                          double* JtJ, double* Jtr, double* img_color, double* img_depth, double* img_T,
+                          uint32_t* img_nc, double* pix_jc, double* pix_jd) {
+    const int tw = P->tile_w, th = P->tile_h;
+    const int ntx = (W + tw - 1) / tw, nty = (H + th - 1) / th, T = ntx * nty;
+    double R[3][3];
+    quat_to_R_f64(pose->orientation, R);
+    const double fx = Kf->fx, fy = Kf->fy;
+    const bool swap = (P->quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
+    const double bg[3] = {P->bg[0], P->bg[1], P->bg[2]};
+    const double alpha_thresh = P->alpha_thresh, color_thresh = P->color_thresh,
+                 depth_thresh = P->depth_thresh;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < T; ++t) {
+        const int tx = t % ntx, ty = t / ntx;
+        double acc[27];
+        for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+        const uint32_t rs = ranges[2 * (size_t)t], re = ranges[2 * (size_t)t + 1];
+        const int n_total = (int)(re - rs);
+        std::vector<GeoD> dcache(n_total > 0 ? n_total : 1);
+        std::vector<char> have(n_total > 0 ? n_total : 1, 0);
+        for (int ly = 0; ly < th; ++ly)
+            for (int lx = 0; lx < tw; ++lx) {
+                const int x = tx * tw + lx, y = ty * th + ly;
+                const bool in_bounds = (x < W && y < H);
+                const size_t p = (size_t)y * W + x;
+                double imgd = 0.0;
+                if (in_bounds) imgd = obs_depth[p];
+                bool inside = in_bounds && imgd > (double)0.1f;
+                double col[3] = {0, 0, 0};
+                double depth = 0.0, final_T = 1.0;
+                uint32_t n_contrib = 0;
+                if (n_total > 0) {
+                    double Tr = 1.0;
+                    uint32_t contributor = 0, last = 0;
+                    bool done = !inside;
+                    for (int i = 0; i < n_total && !done; ++i) {
+                        contributor++;
+                        const Rec g = load_rec(rec, indices[rs + i]);
+                        const double dx = g.u - x, dy = g.v - y;
+                        const double v = g.cx * dx * dx + 2.0 * g.cy * dx * dy + g.cz * dy * dy;
+                        const double a = std::min(k099, g.o * std::exp(-0.5 * v));
+                        if (a < kInv255 || v <= 0.0) continue;
+                        const double test_T = Tr * (1.0 - a);
+                        if (test_T < k1em4) {
+                            done = true;
+                            continue;
+                        }
+                        col[0] += g.r * a * Tr;
+                        col[1] += g.g * a * Tr;
+                        col[2] += g.b * a * Tr;
+                        const double d = g.z + dx * g.phx + dy * g.phy;
+                        if (Tr > 0.5 && test_T < 0.5) depth = d;
+                        Tr = test_T;
+                        last = contributor;
+                    }
+                    if (inside) {
+                        final_T = Tr;
+                        n_contrib = last;
+                        col[0] += Tr * bg[0];
+                        col[1] += Tr * bg[1];
+                        col[2] += Tr * bg[2];
+                    }
+                }
+                if (in_bounds) {
+                    if (img_color) {
+                        img_color[3 * p] = col[0];
+                        img_color[3 * p + 1] = col[1];
+                        img_color[3 * p + 2] = col[2];
+                    }
+                    if (img_depth) img_depth[p] = depth;
+                    if (img_T) img_T[p] = final_T;
+                    if (img_nc) img_nc[p] = n_contrib;
+                    if (pix_jc)
+                        for (int k = 0; k < 18; ++k) pix_jc[18 * p + k] = 0.0;
+                    if (pix_jd)
+                        for (int k = 0; k < 6; ++k) pix_jd[6 * p + k] = 0.0;
+                }
+                inside = inside && (final_T < alpha_thresh);
+                if (!inside) continue;
+
+                double JC[3][6], JD[6];
+                for (int k = 0; k < 6; ++k) {
+                    JC[0][k] = JC[1][k] = JC[2][k] = 0.0;
+                    JD[k] = 0.0;
+                }
+                double prod = 1.0, rem[3] = {col[0], col[1], col[2]};
+                for (int i = 0; i < n_total && i < (int)n_contrib; ++i) {
+                    const uint32_t gi = indices[rs + i];
+                    const Rec g = load_rec(rec, gi);
+                    const double dx = g.u - x, dy = g.v - y;
+                    const double v = g.cx * dx * dx + 2.0 * g.cy * dx * dy + g.cz * dy * dy;
+                    const double raw = g.o * std::exp(-0.5 * v);
+                    const double a = std::min(k099, raw);
+                    if (a < kInv255 || v <= 0.0) continue;
+                    if (!have[i]) {
+                        gauss_derivs(cam3d + 9 * (size_t)gi, R, fx, fy, swap, dcache[i]);
+                        have[i] = 1;
+                    }
+                    const GeoD& D = dcache[i];
+                    const double gc[3] = {g.r, g.g, g.b};
+                    double dCda[3];
+                    for (int k = 0; k < 3; ++k) {
+                        rem[k] -= gc[k] * a * prod;
+                        dCda[k] = gc[k] * prod - rem[k] / (1.0 - a);
+                    }
+                    const double dadv = (raw > k099) ? 0.0 : -0.5 * a;
+                    const double cu = 2.0 * (g.cx * dx + g.cy * dy), cv = 2.0 * (g.cy * dx + g.cz * dy);
+                    const double ca = dx * dx, cb = 2.0 * dx * dy, cc = dy * dy;
+                    for (int k = 0; k < 6; ++k) {
+                        const double dvd = cu * D.du[k] + cv * D.dv[k] + ca * D.da[k] + cb * D.db[k] + cc * D.dc[k];
+                        for (int c = 0; c < 3; ++c) JC[c][k] += dCda[c] * dadv * dvd;
+                    }
+                    const double np = prod * (1.0 - a);
+                    if (prod > 0.5 && np < 0.5)
+                        for (int k = 0; k < 6; ++k)
+                            JD[k] = D.dz[k] + g.phx * D.du[k] + dx * D.dphx[k] + g.phy * D.dv[k] + dy * D.dphy[k];
+                    prod = np;
+                }
+                const double e[3] = {col[0] - obs_rgb[3 * p], col[1] - obs_rgb[3 * p + 1],
+                                     col[2] - obs_rgb[3 * p + 2]};
+                const double derr = depth - imgd;
+                const double closs = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+                const double wc = (closs < color_thresh) ? 1.0 : color_thresh / closs;
+                const double wd = depth_w(derr, depth_thresh, imgd, (P->quirks & FVGS_Q_DEPTH_HUBER) != 0);
+                int idx = 0;
+                for (int i = 0; i < 6; ++i)
+                    for (int j = i; j < 6; ++j) {
+                        double s = wd * JD[i] * JD[j];
+                        for (int c = 0; c < 3; ++c) s += wc * JC[c][i] * JC[c][j];
+                        acc[6 + idx] += s;
+                        ++idx;
+                    }
+                for (int i = 0; i < 6; ++i) {
+                    double s = wd * JD[i] * derr;
+                    for (int c = 0; c < 3; ++c) s += wc * JC[c][i] * e[c];
+                    acc[i] -= s;
+                }
+                if (pix_jc)
+                    for (int c = 0; c < 3; ++c)
+                        for (int k = 0; k < 6; ++k) pix_jc[18 * p + 6 * c + k] = JC[c][k];
+                if (pix_jd)
+                    for (int k = 0; k < 6; ++k) pix_jd[6 * p + k] = JD[k];
+            }
+        for (int k = 0; k < 27; ++k) tile_out[27 * (size_t)t + k] = acc[k];
+    }
+    double tot[27];
+    for (int k = 0; k < 27; ++k) tot[k] = 0.0;
+    for (int t = 0; t < T; ++t)
+        for (int k = 0; k < 27; ++k) tot[k] += tile_out[27 * (size_t)t + k];
+    int idx = 0;
+    for (int i = 0; i < 6; ++i) {
+        for (int j = i; j < 6; ++j) {
+            JtJ[i * 6 + j] = tot[6 + idx];
+            JtJ[j * 6 + i] = tot[6 + idx];
+            ++idx;
+        }
+        Jtr[i] = -tot[i];
+    }
+    return 0;
+}
 
 /*
  * Bucket bookkeeping of the mapping step: perTileBucketCount +

@@ -62,8 +62,11 @@ Q_VIS_CAP256 = 0x10
 Q_ADAM_STAY = 0x20
 Q_POSE_WXYZ = 0x40
 Q_COLOR_RESCALE = 0x80
+Q_POSE_JAC_APPROX = 0x100
+Q_DEPTH_HUBER = 0x200
 QUIRKS_DEFAULT = (Q_INVSIGMA_SWAP | Q_MAP_CAP256 | Q_VIS_CAP256 | Q_ADAM_STAY | Q_POSE_WXYZ
-                  | Q_COLOR_RESCALE)
+                  | Q_COLOR_RESCALE | Q_POSE_JAC_APPROX | Q_DEPTH_HUBER)
+QUIRKS_INTENDED = 0
 
 
 def default_params(quirks: int = QUIRKS_DEFAULT, tile=(16, 16)) -> Params:
@@ -185,13 +188,26 @@ def make_records(proj: Projection, scene, params: Params):
     return rec
 
 
-class Binning:
-    """Everything prepareRasterization produces (src/GSSlam.cu:408-646)."""
+def cam3d(scene, pose):
+    """FP64 camera-frame mean and 3D covariance of every Gaussian, (N, 9) =
+    (x, y, z, Sxx, Sxy, Sxz, Syy, Syz, Szz): the geometry the analytic pose
+    Jacobian differentiates."""
+    n = scene.n
+    out = np.zeros((max(n, 1), 9), np.float64)
+    pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
+    lib().oracle_cam3d(_p(pos), _p(scl), _p(rot), C.c_int(n), C.byref(make_pose(pose)), _p(out))
+    return out[:n]
 
-    def __init__(self, proj, cnt, rect, keys_gen, vals_gen, keys, vals, ranges, rec):
+
+class Binning:
+    """Everything prepareRasterization produces (src/GSSlam.cu:408-646), plus
+    the FP64 camera-frame geometry the analytic pose Jacobian needs."""
+
+    def __init__(self, proj, cnt, rect, keys_gen, vals_gen, keys, vals, ranges, rec, geo=None):
         self.proj, self.cnt, self.rect = proj, cnt, rect
         self.keys_gen, self.vals_gen = keys_gen, vals_gen
         self.keys, self.vals, self.ranges, self.rec = keys, vals, ranges, rec
+        self.geo = geo
 
 
 def prepare(scene, pose, K, W, H, params: Params) -> Binning:
@@ -200,7 +216,8 @@ def prepare(scene, pose, K, W, H, params: Params) -> Binning:
     kg, vg = emit_keys(proj, cnt, rect, W, params)
     ks, vs, ranges = sort_ranges(kg, vg, W, H, params)
     rec = make_records(proj, scene, params)
-    return Binning(proj, cnt, rect, kg, vg, ks, vs, ranges, rec)
+    geo = None if (params.quirks & Q_POSE_JAC_APPROX) else cam3d(scene, pose)
+    return Binning(proj, cnt, rect, kg, vg, ks, vs, ranges, rec, geo)
 
 
 class TrackResult:
@@ -209,8 +226,17 @@ class TrackResult:
         self.color, self.depth, self.final_T, self.n_contrib = color, depth, final_T, n_contrib
 
 
-def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True) -> TrackResult:
-    """frame = (rgb (H,W,3), depth (H,W), gx (H,W,3), gy (H,W,3)) float32."""
+def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True,
+          pixel_jacobians: bool = False) -> TrackResult:
+    """frame = (rgb (H,W,3), depth (H,W), gx (H,W,3), gy (H,W,3)) float32.
+
+    With Q_POSE_JAC_APPROX set in params.quirks this is the reference's
+    getRgbdPoseJacobians; clear, the analytic pose Jacobian
+    (oracle_track_intended; the gradient images are not read).  With
+    pixel_jacobians (analytic mode only) the result also carries the
+    per-pixel colour Jacobian jc (H, W, 3, 6) and depth Jacobian jd (H, W, 6)."""
+    if not (params.quirks & Q_POSE_JAC_APPROX):
+        return _track_intended(b, frame, pose, K, W, H, params, images, pixel_jacobians)
     rgb, depth, gx, gy = [_f32(a) for a in frame]
     T = num_tiles(W, H, params)
     tiles = np.zeros((T, 27), np.float64)
@@ -231,6 +257,53 @@ def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True)
         _p(tiles), _p(JtJ), _p(Jtr), *ptrs,
     )
     return TrackResult(JtJ, Jtr, tiles, col, dep, fT, nc)
+
+
+def _track_intended(b: Binning, frame, pose, K, W, H, params: Params, images: bool, pixel_jacobians: bool):
+    rgb, depth = _f32(frame[0]), _f32(frame[1])
+    if b.geo is None:
+        raise ValueError("binning was prepared without the geometry of the analytic Jacobian")
+    geo = np.ascontiguousarray(b.geo, np.float64)
+    T = num_tiles(W, H, params)
+    tiles = np.zeros((T, 27), np.float64)
+    JtJ = np.zeros((6, 6), np.float64)
+    Jtr = np.zeros(6, np.float64)
+    if images or pixel_jacobians:
+        col = np.zeros((H, W, 3), np.float64)
+        dep = np.zeros((H, W), np.float64)
+        fT = np.zeros((H, W), np.float64)
+        nc = np.zeros((H, W), np.uint32)
+        ptrs = (_p(col), _p(dep), _p(fT), _p(nc))
+    else:
+        col = dep = fT = nc = None
+        ptrs = (None, None, None, None)
+    jc = np.zeros((H, W, 3, 6), np.float64) if pixel_jacobians else None
+    jd = np.zeros((H, W, 6), np.float64) if pixel_jacobians else None
+    lib().oracle_track_intended(
+        _p(b.rec), _p(geo), _p(b.ranges), _p(b.vals), _p(rgb), _p(depth), C.byref(make_pose(pose)),
+        C.byref(make_intr(K)), C.byref(params), C.c_int(W), C.c_int(H), _p(tiles), _p(JtJ), _p(Jtr), *ptrs,
+        _p(jc) if jc is not None else None, _p(jd) if jd is not None else None,
+    )
+    r = TrackResult(JtJ, Jtr, tiles, col, dep, fT, nc)
+    r.jc, r.jd = jc, jd
+    return r
+
+
+def forward64(scene, b: Binning, pose64, K, W, H, params: Params):
+    """The tracking forward blend in FP64 at the FP64 pose (t, q (x,y,z,w))
+    over b's tile lists: colour (H,W,3), median depth (H,W) and the per-pixel
+    branch signature (H,W,3) (blended count, median position, n_contrib)."""
+    t, q = pose64
+    t = np.ascontiguousarray(t, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    col = np.zeros((H, W, 3), np.float64)
+    dep = np.zeros((H, W), np.float64)
+    sig = np.zeros((H, W, 3), np.uint32)
+    lib().oracle_forward64(
+        _p(_f32(scene.positions)), _p(_f32(scene.scales)), _p(_f32(scene.orientations)), _p(_f32(scene.colors)),
+        _p(_f32(scene.opacities)), C.c_int(scene.n), _p(t), _p(q), C.byref(make_intr(K)), C.byref(params),
+        C.c_int(W), C.c_int(H), _p(b.ranges), _p(b.vals), _p(col), _p(dep), _p(sig))
+    return col, dep, sig
 
 
 def render(b: Binning, pose, K, W, H, params: Params):

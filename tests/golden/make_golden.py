@@ -20,11 +20,17 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle as O  # noqa: E402
 from f_vigs_slam_gb300 import synthetic as S  # noqa: E402
 
+REF_JAC = O.Q_POSE_JAC_APPROX | O.Q_DEPTH_HUBER  # the reference's pose Jacobian and depth weight
+
 CASES = {
     # name: (n, W, H, K, scene seed, pose seed, quirks)
     "small_default": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 101, 7, O.QUIRKS_DEFAULT),
-    "small_intended": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 102, 8, 0),
-    "small_culled_slots": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 103, 9, O.Q_CULLED_SLOTS | O.Q_INVSIGMA_SWAP),
+    # every other reference behaviour off, the reference's Jacobian
+    "small_quirks_off_refjac": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 102, 8, REF_JAC),
+    # everything intended: the analytic pose Jacobian
+    "small_intended": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 104, 10, O.QUIRKS_INTENDED),
+    "small_culled_slots": (300, 64, 48, (52.5, 52.5, 31.95, 23.95), 103, 9,
+                           O.Q_CULLED_SLOTS | O.Q_INVSIGMA_SWAP | REF_JAC),
 }
 
 

@@ -11,16 +11,18 @@ from f_vigs_slam_gb300 import synthetic as S
 pytestmark = pytest.mark.gpu
 
 
-def test_variants_agree_bit_for_bit(oracle, fvgs_lib):
+@pytest.mark.parametrize("analytic", [False, True], ids=["ref_jacobian", "analytic_jacobian"])
+def test_variants_agree_bit_for_bit(oracle, fvgs_lib, analytic):
     fv = fvgs_lib
     W, H, K = scaled_camera(0.5)
     scene = S.cam_box(30_000, seed=71)
-    P = oracle.default_params()
+    quirks = fv.QUIRKS_INTENDED if analytic else fv.QUIRKS_DEFAULT
+    P = oracle.default_params(quirks)
     rng = np.random.default_rng(72)
     true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
     start = S.perturb(true_pose, 1.0, 2.0, rng)
     frame = make_frame(oracle, scene, true_pose, K, W, H, P)
-    with fv.Session(scene.n, W, H) as s:
+    with fv.Session(scene.n, W, H, fv.default_params(quirks)) as s:
         s.upload(scene)
         s.set_frame(0, *frame)
         v, ms = s.autotune(start, K, 0, reps=3)

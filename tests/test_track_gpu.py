@@ -1,10 +1,14 @@
-"""GPU parity of the fused tracking kernel against the FP64 oracle.
+"""GPU parity of the fused tracking kernel against the FP64 oracle, for the
+reference's approximate pose Jacobian (FVGS_Q_POSE_JAC_APPROX set) and the
+analytic one (clear).
 
 Tolerances: rendered colour and depth within
 1e-5 relative; JtJ and Jtr within 1e-5 relative (Frobenius / 2-norm) of the
 FP64 oracle.  The GPU blends in FP32, so a pixel whose FP32 and FP64 values
 fall on opposite sides of a discrete threshold (alpha < 1/255, T < 1e-4,
 T crossing 0.5) is a "flip"; flips are counted and must stay rare.
+Tracking with the analytic Jacobian must reach 1e-4 rad / 1e-4 m in 20
+Gauss-Newton iterations from a 1 deg / 2 cm perturbation.
 """
 import numpy as np
 import pytest
@@ -16,9 +20,14 @@ pytestmark = pytest.mark.gpu
 
 IMG_RTOL = 1e-5
 JAC_RTOL = 1e-5
+POSE_TOL = 1e-4  # rad and m after 20 Gauss-Newton iterations
+
+REF_JAC = 0x100 | 0x200  # FVGS_Q_POSE_JAC_APPROX | FVGS_Q_DEPTH_HUBER: the reference's Jacobian and depth weight
+REF = 0x4 | 0x8 | REF_JAC  # the reference's conic layout and mapping cap, its Jacobian
+INTENDED = 0x0  # every reference behaviour off: the analytic Jacobian
 
 
-def _setup(oracle, fv, n, scale, seed, quirks=0x4 | 0x8):
+def _setup(oracle, fv, n, scale, seed, quirks=REF):
     W, H, K = scaled_camera(scale)
     scene = S.cam_box(n, seed=seed)
     P = oracle.default_params(quirks)
@@ -60,7 +69,8 @@ def test_render_parity(oracle, fvgs_lib):
     s.close()
 
 
-@pytest.mark.parametrize("quirks", [0x4 | 0x8, 0x8])
+@pytest.mark.parametrize("quirks", [REF, 0x8 | REF_JAC, INTENDED, 0x4, 0x200],
+                         ids=["ref", "ref_noswap", "analytic", "analytic_swap", "analytic_huber"])
 def test_track_jacobian_parity(oracle, fvgs_lib, quirks):
     W, H, K, scene, P, frame, s = _setup(oracle, fvgs_lib, 20_000, 0.5, 3, quirks)
     pose = (np.zeros(3), S.IDENTITY_Q)
@@ -98,3 +108,109 @@ def test_track_frame_matches_host_loop(oracle, fvgs_lib):
     ang, tr = S.pose_error(dev_pose, pose)
     assert ang < 1e-6 and tr < 1e-6, (ang, tr)
     s.close()
+
+
+@pytest.mark.parametrize("quirks", [REF, INTENDED], ids=["ref", "analytic"])
+def test_track_jacobian_parity_vga_50k(oracle, fvgs_lib, quirks):
+    """The small plain-method workload whole: N = 50k at 640 x 480, tracked
+    from the identity against a frame rendered 1 deg / 2 cm away."""
+    W, H, K, scene, P, frame, s = _setup(oracle, fvgs_lib, 50_000, 1.0, 11, quirks)
+    pose = (np.zeros(3), S.IDENTITY_Q)
+    JtJ, Jtr = s.track_jacobian(pose, K, 0)
+    b = oracle.prepare(scene, pose, K, W, H, P)
+    r = oracle.track(b, frame, pose, K, W, H, P, images=False)
+    e1, e2 = rel_err(JtJ, r.JtJ), rel_err(Jtr, r.Jtr)
+    print("JtJ rel", e1, "Jtr rel", e2)
+    assert e1 <= JAC_RTOL, e1
+    assert e2 <= JAC_RTOL, e2
+    s.close()
+
+
+def _target_pyramid(oracle, scene, pose, K0, W, H, P, levels, seed):
+    """Observed frames of every pyramid level rendered at `pose` by the oracle
+    (a synthetic sensor at each resolution, intrinsics scaled by 2^-l), plus
+    N(0, 0.01) colour and N(0, 0.005 m) depth noise."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for lv in range(levels):
+        sc = 1.0 / (1 << lv)
+        K = tuple(np.float32(k * sc) for k in K0)
+        w, h = W >> lv, H >> lv
+        b = oracle.prepare(scene, pose, K, w, h, P)
+        col, dep, _, _ = oracle.render(b, pose, K, w, h, P)
+        rgb, d = S.add_noise(col.astype(np.float32), dep.astype(np.float32), rng)
+        gx, gy = S.sobel3(rgb)
+        out.append((rgb, d, gx, gy))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_intended_tracking_converges_vga_50k(oracle, fvgs_lib, seed):
+    """Analytic Jacobian, coarse-to-fine over four levels (4 + 4 + 6 + 6 = 20
+    Gauss-Newton iterations): from 1 deg / 2 cm the pose reaches 1e-4 rad /
+    1e-4 m, and it matches the oracle's own loop over the same frames."""
+    fv = fvgs_lib
+    W, H, K0 = scaled_camera(1.0)
+    scene = S.cam_box(50_000, seed=seed)
+    P = oracle.default_params(INTENDED)
+    rng = np.random.default_rng(seed + 1)
+    ident = (np.zeros(3, np.float32), S.IDENTITY_Q.copy())
+    true_pose = S.perturb(ident, 1.0, 2.0, rng)
+    iters = (4, 4, 6, 6)
+    frames = _target_pyramid(oracle, scene, true_pose, K0, W, H, P, len(iters), seed + 2)
+    with fv.Session(scene.n, W, H, fv.default_params(INTENDED)) as s:
+        s.upload(scene)
+        for lv, fr in enumerate(frames):
+            s.set_frame(lv, *fr)
+        gpu_pose, _ = s.track_frame_pyramid(ident, K0, iters)
+    err = S.pose_error(gpu_pose, true_pose)
+    print("GPU pose error rad %.3e m %.3e" % err)
+    assert err[0] <= POSE_TOL and err[1] <= POSE_TOL, err
+    # the oracle's loop: same levels, same pseudo-factor step, FP64 throughout
+    pose = (ident[0].astype(np.float64), ident[1].astype(np.float64))
+    for lv in reversed(range(len(iters))):
+        sc = 1.0 / (1 << lv)
+        K = tuple(np.float32(k * sc) for k in K0)
+        w, h = W >> lv, H >> lv
+        for _ in range(iters[lv]):
+            pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
+            b = oracle.prepare(scene, pf, K, w, h, P)
+            r = oracle.track(b, frames[lv], pf, K, w, h, P, images=False)
+            pose = oracle.pose_plus(pose, oracle.gn_delta(r.JtJ, r.Jtr))
+    d = S.pose_error(gpu_pose, pose)
+    print("GPU vs oracle loop rad %.3e m %.3e" % d)
+    assert d[0] <= 1e-5 and d[1] <= 1e-5, d
+
+
+def test_pyramid_frame_eager_graph_and_batched_agree(oracle, fvgs_lib):
+    """A coarse-to-fine frame gives the same pose eagerly
+    (fvgs_track_frame_pyramid), submitted (captured as a graph, then replayed)
+    and batched with another session (fvgs_frames_run_pyramid)."""
+    fv = fvgs_lib
+    W, H, K0 = scaled_camera(0.5)
+    scene = S.cam_box(20_000, seed=21)
+    P = oracle.default_params(INTENDED)
+    rng = np.random.default_rng(22)
+    ident = (np.zeros(3, np.float32), S.IDENTITY_Q.copy())
+    true_pose = S.perturb(ident, 1.0, 2.0, rng)
+    iters = (2, 3, 3)
+    frames = _target_pyramid(oracle, scene, true_pose, K0, W, H, P, len(iters), 23)
+    sessions = []
+    for _ in range(2):
+        s = fv.Session(scene.n, W, H, fv.default_params(INTENDED))
+        s.upload(scene)
+        for lv, fr in enumerate(frames):
+            s.set_frame(lv, *fr)
+        sessions.append(s)
+    a, _ = sessions[0].track_frame_pyramid(ident, K0, iters)
+    got = []
+    for _ in range(3):
+        sessions[0].frame_submit_pyramid(ident, K0, iters)
+        got.append(sessions[0].frame_wait()[0])
+    assert sessions[0].frame_stats()["graphed"] >= 2
+    got += fv.frames_run_pyramid(sessions, [ident, ident], [K0, K0], iters)
+    for p in got:
+        np.testing.assert_array_equal(p[0], a[0])
+        np.testing.assert_array_equal(p[1], a[1])
+    for s in sessions:
+        s.close()
