@@ -1,35 +1,50 @@
 #!/usr/bin/env python
 """Tracking benchmark of the GB300 Gaussian-splatting hot path: served +
-batched versus plain tracking frames/s, with p50/p99 latency.
+batched versus plain tracking frames/s, with p50/p99 latency and the pose
+error of every form.
+
+Every form tracks with the analytic pose Jacobian (all reference quirks off,
+FVGS_QUIRKS_INTENDED) and coarse-to-fine over four pyramid levels, the level
+loop of GSSlam::optimizeWithCeres: 6 + 6 + 4 + 4 = 20 Gauss-Newton
+iterations from level 3 down to level 0 (intrinsics scaled by 2^-level).
+The observed frame of every level is rendered at the true pose at that
+level's resolution, plus N(0,0.01) colour and N(0,0.005 m) depth noise
+(synthetic data; the reference names no dataset).  The pose error criterion
+is 1e-4 rad and 1e-4 m after the 20 iterations.
 
 Serving workload (the `value`): sessions, each its own map of N Gaussians
 (log-uniform in [100k, 3M], room scenes), 640x480 or 1280x720 frames (fx =
-fy = 525 / 1050), a random-walk trajectory with frames rendered at its true
-poses (+ N(0,0.01) colour / N(0,0.005 m) depth noise, Sobel gradients;
-synthetic data, the reference names no dataset).  A request = one frame of
-one session = 20 Gauss-Newton tracking iterations (binning + fused Jacobian
-kernel + on-device 6x6 pseudo-factor step), with a mapping step (forward,
-backward, 2D->3D, Adam) on every 10th frame of a session.  One step = one
-request per session.
+fy = 525 / 1050), a random-walk trajectory (1 cm / 0.5 deg per frame); each
+frame starts from its predicted pose (the true pose perturbed by 0.05 deg /
+1 mm: the reference seeds every frame with the IMU prediction).  A
+request = one frame of one session = the 20 coarse-to-fine iterations
+(binning + fused Jacobian kernel + on-device 6x6 pseudo-factor step each),
+with a mapping step (forward, backward, 2D->3D, Adam) on every 10th frame of
+a session.  One step = one request per session.
  * value: the continuous-batching server (fvgs_server) with every
    session's requests in flight together and frames replayed from captured
    CUDA graphs, frames in HBM;
  * plain: the same requests one at a time through the plain per-frame path
-   (fvgs_track_frame / fvgs_map_step);
- * e2e: the server with each request carrying its frame in pinned host
-   memory (host->device copies inside the timed region);
+   (fvgs_track_frame_pyramid / fvgs_map_step);
+ * e2e: the server with each request carrying its four-level frame in one
+   pinned host buffer (host->device copies inside the timed region);
  * p50/p99: request latency (arrival to result) of the server under Poisson
-   arrivals, 30 Hz per session or 70% of the measured capacity if lower.
-The large plain-method workload (one session, N = 1 M room, 1280x720, 20 GN
-iterations + 1 mapping step per frame) is reported under `large_plain`; the
-roofline entry is its dominant kernel (HBM, plus the instruction-issue
-roofline that bounds it), and `large_plain.kernel_rooflines` has every kernel
-class's HBM fraction.  Beside it: `small_plain` (N = 50k, 640x480, a mapping
-step + 20 GN iterations, also run whole in the CPU restatement), `batching`
-(64 keyframes, N log-uniform in [20k, 2M], one fvgs_frames_run call against
+   arrivals, 30 Hz per session or 70% of the measured capacity if lower;
+ * pose_error: per form, against the true poses.
+Beside it: `small_plain` (N = 50k camera-frame box, 640x480, target 1 deg /
+2 cm away: 20 iterations then a mapping step; also run whole in the CPU
+restatement, and with the reference's approximate Jacobian for contrast),
+`large_plain` (N = 1 M room, 1280x720, 20 iterations + a mapping step per
+frame; the roofline entry is its dominant kernel), `batching` (64 keyframes,
+N log-uniform in [20k, 2M], one fvgs_frames_run_pyramid call against
 sequential frames), `precision` (N = 2 M with BF16/FP16 attributes against
 FP32, and the visual-inertial solve with 200 Hz IMU data) and `maintenance`
 (outlier removal, covisibility, prune on the 1 M map).
+
+The CPU arm (--impl reference) and `cpu_baseline` time the CPU restatement
+(FP64, all host threads) on whole frames of the same serving mix, session
+after session, for a bounded time: `steps` is the frames it timed and
+`ms_per_step` their mean time.
 
 Multi-GPU: replicas only (every GPU serves its own sessions; no collective on
 the data path); the elapsed time is the max over ranks.
@@ -53,7 +68,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "tracking frames/s & p99 latency, served+batched vs plain, 1 GB300, same pose err"
 N_GAUSS = 1_000_000
-ITERS = 20
+QUIRKS = 0               # FVGS_QUIRKS_INTENDED: analytic pose Jacobian, every reference quirk off
+PYR = (4, 4, 6, 6)       # Gauss-Newton iterations at pyramid levels 0..3, run from level 3 down
+# Initial pose of a room frame: the reference seeds every frame with the IMU
+# prediction (GSSlam::compute, src/GSSlam.cu:880-897); modelled as the true
+# pose perturbed by 0.05 deg / 1 mm in random directions (a tenth of a
+# trajectory step, above the error of preintegrating the configured IMU noise
+# over one 33 ms frame interval).
+PRED_DEG, PRED_CM = 0.05, 0.1
+ITERS = sum(PYR)
+POSE_TOL = 1e-4          # rad and m
 ETA = 0.002
 # serving configuration
 SERVE_N_MIN, SERVE_N_MAX = 100_000, 3_000_000
@@ -61,10 +85,13 @@ SERVE_HZ = 30.0          # arrivals per session
 SERVE_SECONDS = 2.0      # Poisson arrival window of the latency run
 SERVE_FRAMES = 2         # distinct frames per session
 SERVE_BUDGET = 150 * 10**9
+SERVE_SEED = 5
 MAP_EVERY = 10
 PREC_N = 2_000_000       # precision-form workload: N = 2 M room, 1280x720
 BATCH_SESSIONS = 64      # batching workload: keyframes with N log-uniform in [20k, 2M]
 BATCH_N_MIN, BATCH_N_MAX = 20_000, 2_000_000
+CPU_ARM_BUDGET_S = 170.0   # --impl reference: timed CPU work, bounded so the run ends within a few minutes
+CPU_BASELINE_BUDGET_S = 20.0
 
 
 def parse():
@@ -91,21 +118,100 @@ def dist_info():
 # ----------------------------------------------------------------------------
 # workload
 # ----------------------------------------------------------------------------
-def make_workload(sess, n_frames, seed):
-    from f_vigs_slam_gb300 import synthetic as S
+def level_dims(W, H, levels=len(PYR)):
+    """Frame sizes of the pyramid levels (cv::pyrDown's (n + 1) / 2)."""
+    out, w, h = [], W, H
+    for _ in range(levels):
+        out.append((w, h))
+        w, h = (w + 1) // 2, (h + 1) // 2
+    return out
 
+
+def level_K(K0, level):
+    """Intrinsics of a pyramid level as the library derives them: all four
+    scaled by 2^-level in FP32 (src/GSSlam.cu:2133-2138)."""
+    sc = np.float32(1.0 / (1 << level))
+    return tuple(float(np.float32(k) * sc) for k in K0)
+
+
+def render_pyramid(S, sess, pose, K0, W, H, rng):
+    """Observed frames of every level: the session's render at `pose` at that
+    level's resolution, + N(0,0.01) colour / N(0,0.005 m) depth noise, Sobel
+    gradients.  Level 0 first."""
+    out = []
+    for lv, (w, h) in enumerate(level_dims(W, H)):
+        col, dep, _, _ = sess.render(pose, level_K(K0, lv), w, h)
+        rgb, d = S.add_noise(col, dep, rng)
+        gx, gy = S.sobel3(rgb)
+        out.append({"rgb": rgb, "depth": d, "gx": gx, "gy": gy})
+    return out
+
+
+def to_device(torch, dev, pyr):
+    return [{k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in lv.items()} for lv in pyr]
+
+
+def to_pinned(torch, pyr):
+    return [{k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in lv.items()} for lv in pyr]
+
+
+def set_frame_tensors(fvgs, sess, level, fr, W, H):
+    st = sess.lib.fvgs_set_frame(sess.h, level, *(fvgs.C.c_void_p(fr[k].data_ptr()) for k in ("rgb", "depth", "gx", "gy")),
+                                 W, H)
+    if st != 0:
+        raise fvgs.FvgsError(st, "fvgs_set_frame")
+
+
+def set_pyramid(fvgs, sess, pyr, W, H):
+    for lv, (w, h) in enumerate(level_dims(W, H)):
+        set_frame_tensors(fvgs, sess, lv, pyr[lv], w, h)
+
+
+def err_stats(errs):
+    """Pose errors (rad, m) of a form: medians, maxima and the share within the criterion."""
+    a = np.array(errs, np.float64).reshape(-1, 2)
+    return {"rad_median": float(np.median(a[:, 0])), "m_median": float(np.median(a[:, 1])),
+            "rad_max": float(a[:, 0].max()), "m_max": float(a[:, 1].max()),
+            "within_1e-4": float(np.mean((a[:, 0] <= POSE_TOL) & (a[:, 1] <= POSE_TOL))), "frames": int(a.shape[0])}
+
+
+def make_workload(S, sess, n_frames, seed):
+    """Frames of a random-walk trajectory through the room (1280x720): frame k
+    is observed at pose k + 1 and starts from its predicted pose."""
     cam = S.CAM_HD
     W, H, K = cam.width, cam.height, cam.intrinsics
     traj = S.trajectory(200, seed=seed)
     rng = np.random.default_rng(seed + 1)
     frames = []
     for k in range(n_frames):
-        pose = traj[(k + 1) % len(traj)]
-        col, dep, _, _ = sess.render(pose, K, W, H)
-        rgb, d = S.add_noise(col, dep, rng)
-        gx, gy = S.sobel3(rgb)
-        frames.append(dict(rgb=rgb, depth=d, gx=gx, gy=gy, pose=pose, prev=traj[k % len(traj)]))
+        true = traj[(k + 1) % len(traj)]
+        frames.append({"pyr": render_pyramid(S, sess, true, K, W, H, rng), "pose": true,
+                       "prev": S.perturb(true, PRED_DEG, PRED_CM, rng)})
     return W, H, K, frames
+
+
+def serving_sessions(n_sessions, seed=SERVE_SEED):
+    """Sizes of the serving sessions: N log-uniform in [100k, 3M], 640x480
+    and 1280x720 alternately, each with its own room map and trajectory."""
+    from f_vigs_slam_gb300 import synthetic as S
+
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(SERVE_N_MIN), np.log(SERVE_N_MAX), n_sessions)).astype(int)
+    return [{"n": int(ns[i]), "cam": S.CAM_VGA if i % 2 == 0 else S.CAM_HD, "map_seed": seed + 1000 + i,
+             "traj_seed": seed + 2000 + i} for i in range(n_sessions)]
+
+
+def serving_config(n_sessions):
+    return {"workload": ("serving: %d sessions, maps of 100k-3M Gaussians (log-uniform, room scenes), 640x480 / "
+                         "1280x720 frames; a request = one frame of one session = 20 Gauss-Newton iterations "
+                         "coarse-to-fine (levels 3..0: %d/%d/%d/%d) with the analytic pose Jacobian, plus a "
+                         "mapping step every %d-th frame; one step = one request per session"
+                         % ((n_sessions,) + tuple(reversed(PYR)) + (MAP_EVERY,))),
+            "quirks": "FVGS_QUIRKS_INTENDED (analytic pose Jacobian, Tukey depth weight, every reference quirk off)",
+            "initial_pose": "the predicted pose: the true pose perturbed by %.2f deg / %.1f mm (the reference seeds "
+                            "each frame with the IMU prediction)" % (PRED_DEG, 10 * PRED_CM),
+            "pose_error_criterion": "1e-4 rad and 1e-4 m after the 20 iterations",
+            "sessions": n_sessions}
 
 
 class ClockSampler:
@@ -161,29 +267,31 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_track_bytes(n_inst, W, H):
-    """Algorithmic HBM bytes of one fused tracking launch: every instance's
-    48-byte blending record read once, 40 B/pixel of observed rgb, depth and
-    the two gradient images, 108 B per tile written."""
-    T = ((W + 15) // 16) * ((H + 15) // 16)
-    return 48 * n_inst + 40 * W * H + 108 * T
-
-
-def algorithmic_bytes(cls, n_g, n_inst, W, H):
-    """Per-launch algorithmic bytes of each kernel class."""
+def algorithmic_bytes(cls, n_g, n_vis, n_inst, visited, W, H):
+    """Bytes one launch of a kernel class must move on the frame's level-0
+    binning, with the basis they are counted on; None where a class has no
+    meaningful byte count.  n_vis: Gaussians with instances; visited: the
+    instances the blending kernels must read (per tile, the list prefix up to
+    its deepest pixel's last blended Gaussian)."""
     P = W * H
     T = ((W + 15) // 16) * ((H + 15) // 16)
-    return {
-        "project": 64 * n_g + 84 * n_g,
-        "scan": 8 * n_g,
-        "emit": 36 * n_g + 12 * n_inst,
-        "sort": 24 * n_inst,
-        "ranges": 8 * n_inst + 8 * T,
-        "track": algorithmic_track_bytes(n_inst, W, H),
-        "map_fwd": 48 * n_inst + 16 * P + 40 * P,
-        "map_bwd": 48 * n_inst + 52 * P + 52 * n_g,
-        "map_update": (64 + 64 + 144) * n_g + (64 + 144) * n_g,
-    }.get(cls)
+    table = {
+        "project": (20 * n_g + 160 * n_vis,
+                    "20 B per Gaussian (position, previous count) + per visible Gaussian 48 B of attributes in and "
+                    "112 B out (blending 48, binning 32, geometry 32 records)"),
+        "sort": (8 * n_inst + 32 * n_vis,
+                 "incremental per-tile sort: 4 B in + 4 B out per instance + each visible Gaussian's 32-byte "
+                 "binning record"),
+        "track": (80 * visited + 16 * P + 108 * T,
+                  "48-byte blending + 32-byte geometry record per instance read (list prefixes the pixels reach), "
+                  "16 B per pixel of observed colour and depth, 108 B per tile out"),
+        "gn": (108 * T, "the tile partials"),
+        "map_fwd": (48 * visited + 52 * P, "48-byte record per instance read + 16 B in and 36 B out per pixel"),
+        "map_bwd": (48 * visited + 52 * P + 64 * n_vis,
+                    "48-byte record per instance read + 52 B per pixel + 64 B of gradients per visible Gaussian"),
+        "map_update": (480 * n_g, "parameters 64 + Adam state 144 in and out, 2D gradients 64 in, per Gaussian"),
+    }
+    return table.get(cls)
 
 
 def load_peaks():
@@ -249,69 +357,101 @@ def replica_throughput(steps, world, max_ms):
 # ----------------------------------------------------------------------------
 # CPU baseline (the CPU restatement of the reference, FP64, all host threads)
 # ----------------------------------------------------------------------------
-def cpu_frame_run(n, cam, seed=0, maps_per_frame=1.0):
-    """Time the oracle on one whole tracking frame of a session: 20
-    iterations of binning + Jacobian + pseudo-factor Gauss-Newton step at
-    the moving pose (as fvgs_track_frame), plus one mapping step, weighted
-    by maps_per_frame.  Returns the frame's CPU seconds."""
+def cpu_pyramid_frame(O, S, scene, start, frames, K0, W, H, P, map_eta=None):
+    """One whole frame in the CPU restatement: the 20 coarse-to-fine
+    iterations of binning + Jacobian + pseudo-factor Gauss-Newton step, then
+    optionally the mapping step at the tracked pose.  frames: per level
+    (rgb, depth, gx, gy).  Returns the tracked pose (FP64)."""
+    pose = (np.asarray(start[0], np.float64), np.asarray(start[1], np.float64))
+    dims = level_dims(W, H)
+    for lv in reversed(range(len(PYR))):
+        K = level_K(K0, lv)
+        w, h = dims[lv]
+        for _ in range(PYR[lv]):
+            pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
+            b = O.prepare(scene, pf, K, w, h, P)
+            r = O.track(b, frames[lv], pf, K, w, h, P, images=False)
+            pose = O.pose_plus(pose, O.gn_delta(r.JtJ, r.Jtr))
+    if map_eta is not None:
+        pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
+        b = O.prepare(scene, pf, K0, W, H, P)
+        O.map_step(scene, b, frames[0][0], frames[0][1], pf, K0, W, H, P, map_eta)
+    return pose
+
+
+def cpu_oracle_pyramid(O, S, scene, pose, K0, W, H, P, rng):
+    """Observed frames of every level rendered by the oracle at `pose` (+ noise)."""
+    out = []
+    for lv, (w, h) in enumerate(level_dims(W, H)):
+        K = level_K(K0, lv)
+        b = O.prepare(scene, pose, K, w, h, P)
+        col, dep, _, _ = O.render(b, pose, K, w, h, P)
+        rgb, d = S.add_noise(col.astype(np.float32), dep.astype(np.float32), rng)
+        gx, gy = S.sobel3(rgb)
+        out.append((rgb, d, gx, gy))
+    return out
+
+
+def cpu_serving_run(n_sessions, budget_s, wall_limit_s):
+    """The CPU restatement on whole frames of the serving mix: session 0, 1,
+    2, ... in turn (each its own map, frame size and trajectory, as the GPU
+    arm builds them), one frame each (a mapping step on every MAP_EVERY-th
+    frame timed), until `budget_s` of timed work or `wall_limit_s` of wall
+    time.  Inputs are built outside the timed region.  Returns per-frame
+    times and pose errors."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from f_vigs_slam_gb300 import synthetic as S
 
     O.build()
-    W, H, K = cam.width, cam.height, cam.intrinsics
-    scene = S.room(n, seed=seed)
-    traj = S.trajectory(3, seed=seed)
-    P = O.default_params()
-    b_true = O.prepare(scene, traj[1], K, W, H, P)
-    col, dep, _, _ = O.render(b_true, traj[1], K, W, H, P)
-    rng = np.random.default_rng(seed + 1)
-    rgb, d = S.add_noise(col.astype(np.float32), dep.astype(np.float32), rng)
-    gx, gy = S.sobel3(rgb)
-    pose = (np.asarray(traj[0][0], np.float64), np.asarray(traj[0][1], np.float64))
-    t0 = time.perf_counter()
-    for _ in range(ITERS):
-        pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
-        b = O.prepare(scene, pf, K, W, H, P)
-        r = O.track(b, (rgb, d, gx, gy), pf, K, W, H, P, images=False)
-        pose = O.pose_plus(pose, O.gn_delta(r.JtJ, r.Jtr))
-    t_iters = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.map_step(scene, b, rgb, d, pf, K, W, H, P, ETA)
-    t_map = time.perf_counter() - t0
-    return dict(frame_s=t_iters + maps_per_frame * t_map, wall_s=t_iters + t_map, threads=os.cpu_count() or 1)
+    P = O.default_params(QUIRKS)
+    t_wall = time.perf_counter()
+    times, errs, desc = [], [], []
+    for j in range(10**6):
+        spec = serving_sessions(n_sessions)[j % n_sessions]
+        cam = spec["cam"]
+        W, H, K = cam.width, cam.height, cam.intrinsics
+        scene = S.room(spec["n"], seed=spec["map_seed"])
+        traj = S.trajectory(2, seed=spec["traj_seed"])
+        rng = np.random.default_rng(spec["traj_seed"])
+        frames = cpu_oracle_pyramid(O, S, scene, traj[1], K, W, H, P, rng)
+        start = S.perturb(traj[1], PRED_DEG, PRED_CM, rng)
+        eta = ETA if j % MAP_EVERY == MAP_EVERY - 1 else None
+        t0 = time.perf_counter()
+        pose = cpu_pyramid_frame(O, S, scene, start, frames, K, W, H, P, eta)
+        times.append(time.perf_counter() - t0)
+        errs.append(S.pose_error(pose, traj[1]))
+        desc.append("N=%d %dx%d%s" % (spec["n"], W, H, " +map" if eta else ""))
+        if sum(times) >= budget_s or time.perf_counter() - t_wall >= wall_limit_s:
+            break
+    return {"frame_s": times, "pose_errors": errs, "frames": desc, "cores": os.cpu_count() or 1}
 
 
 def run_reference(args):
     """CPU arm: the CPU restatement of the reference's path (FP64, all host
-    threads) on the serving configuration's request mix, one bounded sample
-    per step (see cpu_serving_sample), as frames/s."""
+    threads) on whole frames of the serving mix, session after session, for
+    a bounded time; `steps` = frames timed, `ms_per_step` = their mean time,
+    value = frames per second of timed work."""
     rank, _, world = dist_info()
     if rank != 0:
         return 0
-    samples = []
-    t_start = time.perf_counter()
-    for i in range(args.warmup + args.steps):
-        if i >= max(1, args.warmup) and time.perf_counter() - t_start > 240.0:
-            break  # keep the whole run within a few minutes
-        r = cpu_serving_sample(args)
-        if i >= args.warmup or args.warmup + args.steps == 1:
-            samples.append(r)
-    if not samples:
-        samples.append(r)
-    v = float(np.median([r["value"] for r in samples]))
+    r = cpu_serving_run(args.sessions, CPU_ARM_BUDGET_S, CPU_ARM_BUDGET_S + 60.0)
+    t = np.array(r["frame_s"])
+    v = len(t) / float(t.sum())
+    sample = ("the first %d frames of the serving mix (sessions 0..%d, one frame each: %s), FP64 restatement with "
+              "OpenMP, %.1f s of timed work" % (len(t), len(t) - 1, ", ".join(r["frames"]), t.sum()))
+    cfg = serving_config(args.sessions)
+    cfg["path"] = ("CPU restatement of the reference (FP64, OpenMP), one frame at a time; the reference itself "
+                   "cannot be built here (needs Eigen in device code, OpenCV-CUDA, Ceres, ROS 2)")
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 1, "steps": len(samples),
-        "warmup": args.warmup, "ms_per_step": 1000.0 * args.sessions / v,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": ("serving: %d sessions, maps of 100k-3M Gaussians, 640x480 / 1280x720 frames, 20 GN "
-                                "iterations per frame, a mapping step every %d-th frame; one step = one request per "
-                                "session" % (args.sessions, MAP_EVERY)),
-                   "path": "CPU restatement of the reference (FP64, OpenMP), one frame at a time; the reference "
-                           "itself cannot be built here (needs Eigen in device code, OpenCV-CUDA, Ceres, ROS 2)"},
-        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": samples[0]["cores"], "kind": "port",
-                         "sample": samples[0]["sample"]},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 1, "steps": len(t),
+        "warmup": 0, "ms_per_step": 1000.0 * float(t.mean()), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "pose_error": err_stats(r["pose_errors"]),
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": r["cores"], "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "steps = frames timed (a bounded sample of the serving mix), not the GPU arm's rounds of %d "
+                "requests; requested --steps %d --warmup %d" % (args.sessions, args.steps, args.warmup),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -323,7 +463,7 @@ def run_reference(args):
 def small_case(S):
     """The small plain-method workload: N = 50,000 Gaussians in the camera
     frame box, 640x480 (fx = fy = 525), target rendered at a pose 1 deg / 2 cm
-    from the start pose plus colour / depth noise, Sobel gradients."""
+    from the start pose plus colour / depth noise."""
     cam = S.CAM_VGA
     scene = S.cam_box(50_000, seed=0)
     rng = np.random.default_rng(1)
@@ -333,28 +473,28 @@ def small_case(S):
 
 
 def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
-    """The small plain-method configuration, as the reference's plain path
-    runs it: one mapping forward + backward step, then 20 Gauss-Newton pose
-    iterations (fvgs_map_step + fvgs_track_frame), on the GPU and, whole, in
-    the FP64 CPU restatement on all host cores.  The map is uploaded again
-    before every run (outside the timed region), so every run is the same."""
+    """The small plain-method configuration on the plain path: the 20
+    coarse-to-fine iterations from the start pose, then one mapping forward +
+    backward step at the tracked pose (fvgs_track_frame_pyramid +
+    fvgs_map_step), on the GPU and, whole, in the FP64 CPU restatement on all
+    host cores.  The map is uploaded again before every run (outside the timed
+    region), so every run is the same.  The same frame is also tracked with
+    the reference's approximate Jacobian (its quirk bits set) for contrast."""
     cam, scene, start, true_pose, rng = small_case(S)
     W, H, K = cam.width, cam.height, cam.intrinsics
-    sess = fvgs.Session(scene.n, W, H, device=dev.index or 0)
+    sess = fvgs.Session(scene.n, W, H, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    col, dep, _, _ = sess.render(true_pose, K, W, H)
-    rgb, d = S.add_noise(col, dep, rng)
-    gx, gy = S.sobel3(rgb)
-    sess.set_frame(0, rgb, d, gx, gy)
+    pyr = render_pyramid(S, sess, true_pose, K, W, H, rng)
+    set_pyramid(fvgs, sess, to_device(torch, dev, pyr), W, H)
     ms, poses = [], []
     for i in range(args.warmup + args.steps):
         sess.upload(scene)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        sess.map_step(start, K, ETA)
-        pose, _ = sess.track_frame(start, K, iterations=ITERS)
+        pose, _ = sess.track_frame_pyramid(start, K, PYR)
+        sess.map_step(pose, K, ETA)
         e1.record(stream)
         torch.cuda.synchronize()
         if i >= args.warmup:
@@ -363,70 +503,89 @@ def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
     sess.close()
     ms_run = max_over_ranks([float(np.median(ms))], dev, world)[0]
     err = S.pose_error(poses[-1], true_pose)
-    out = {"workload": "cam-frame box N=50000, 640x480, target 1 deg / 2 cm away + noise; one mapping forward + "
-                       "backward step, then 20 GN iterations (fvgs_map_step + fvgs_track_frame)",
+    # the reference's approximate Jacobian on the same frames and schedule
+    ref = fvgs.Session(scene.n, W, H, fvgs.default_params(fvgs.QUIRKS_DEFAULT), device=dev.index or 0)
+    ref.set_stream(stream.cuda_stream)
+    ref.upload(scene)
+    set_pyramid(fvgs, ref, to_device(torch, dev, pyr), W, H)
+    ref_pose, _ = ref.track_frame_pyramid(start, K, PYR)
+    ref.close()
+    ref_err = S.pose_error(ref_pose, true_pose)
+    out = {"workload": "cam-frame box N=50000, 640x480, target 1 deg / 2 cm away + noise; 20 GN iterations "
+                       "coarse-to-fine (levels 3..0: %d/%d/%d/%d), then one mapping forward + backward step "
+                       "(fvgs_track_frame_pyramid + fvgs_map_step)" % tuple(reversed(PYR)),
            "gpu_ms_per_run": ms_run, "runs_per_s": replica_throughput(1, world, ms_run),
-           "pose_error": {"rad": err[0], "m": err[1]}}
+           "pose_error": {"rad": err[0], "m": err[1]},
+           "reference_jacobian_pose_error": {"rad": ref_err[0], "m": ref_err[1],
+                                             "note": "FVGS_QUIRKS_DEFAULT (the reference's approximate Jacobian "
+                                                     "and depth weight, conic layout swap) on the same frames"}}
     if with_cpu:
-        cpu = cpu_small_run(S, scene, start, rgb, d, gx, gy, K, W, H)
+        cpu = cpu_small_run(S, scene, start, pyr, K, W, H)
         out["cpu"] = cpu
         out["cpu_s_per_run"] = cpu["s_per_run"]
         out["speedup_gpu_over_cpu"] = 1e3 * cpu["s_per_run"] / ms_run
         dq = S.pose_error(poses[-1], cpu["pose"])
         out["pose_difference_gpu_vs_cpu"] = {"rad": dq[0], "m": dq[1]}
+        ce = S.pose_error(cpu["pose"], true_pose)
+        out["cpu_pose_error"] = {"rad": ce[0], "m": ce[1]}
         del cpu["pose"]
     return out
 
 
-def cpu_small_run(S, scene, start, rgb, d, gx, gy, K, W, H):
+def cpu_small_run(S, scene, start, pyr, K, W, H):
     """The whole small configuration in the CPU restatement (FP64 blending
-    and Jacobians on the FP32-exact binning, OpenMP over tiles): the mapping
-    step at the start pose, then 20 iterations of binning + Jacobian +
-    pseudo-factor step on the host."""
+    and Jacobians on the FP32-exact binning, OpenMP over tiles), on the same
+    observed frames: the 20 coarse-to-fine iterations, then the mapping step."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     O.build()
-    P = O.default_params()
-    sc = S.Scene(*[np.array(a, copy=True) for a in (scene.positions, scene.scales, scene.orientations,
-                                                      scene.colors, scene.opacities)])
+    P = O.default_params(QUIRKS)
+    frames = [(lv["rgb"], lv["depth"], lv["gx"], lv["gy"]) for lv in pyr]
     t0 = time.perf_counter()
-    b = O.prepare(sc, start, K, W, H, P)
-    m = O.map_step(sc, b, rgb, d, start, K, W, H, P, ETA)
-    sc = S.Scene(*[np.asarray(a, np.float32) for a in (m.pos, m.scl, m.rot, m.col, m.opa)])
-    pose = (np.asarray(start[0], np.float64), np.asarray(start[1], np.float64))
-    for _ in range(ITERS):
-        pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
-        b = O.prepare(sc, pf, K, W, H, P)
-        r = O.track(b, (rgb, d, gx, gy), pf, K, W, H, P, images=False)
-        pose = O.pose_plus(pose, O.gn_delta(r.JtJ, r.Jtr))
+    pose = cpu_pyramid_frame(O, S, scene, start, frames, K, W, H, P, ETA)
     t = time.perf_counter() - t0
     return {"s_per_run": t, "cores": os.cpu_count() or 1, "kind": "port", "pose": pose,
-            "sample": "the whole run (1 mapping step + 20 binnings, Jacobians and GN steps), FP64 restatement"}
+            "sample": "the whole run (20 coarse-to-fine binnings, Jacobians and GN steps, 1 mapping step), FP64 "
+                      "restatement"}
+
+
+def visited_records(fvgs, sess, pose, K, W, H):
+    """Instances the tracking kernel must read at `pose` (level 0): per tile,
+    the list prefix up to the deepest pixel's last blended Gaussian
+    (max n_contrib), since a tile's pixels stop there."""
+    sess.set_debug(fvgs.DEBUG_IMAGES)
+    sess.track_jacobian(pose, K, 0)
+    _, _, _, nc = sess.download_track_images(W, H)
+    _, _, ranges = sess.download_binning(W, H)
+    sess.set_debug(0)
+    ntx, nty = (W + 15) // 16, (H + 15) // 16
+    pad = np.zeros((nty * 16, ntx * 16), np.int64)
+    pad[:H, :W] = nc.reshape(H, W)
+    mx = pad.reshape(nty, 16, ntx, 16).max(axis=(1, 3)).ravel()
+    n_tile = (ranges[:, 1].astype(np.int64) - ranges[:, 0].astype(np.int64))
+    return int(np.minimum(n_tile, mx + 1).sum()), int(n_tile.sum())
 
 
 def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     """The large plain-method workload: one session, N = 1 M room, 1280x720,
-    frames through the synchronous per-frame path (fvgs_track_frame +
-    fvgs_map_step).  Returns its measurements (frames/s, latency, e2e,
-    per-kernel-class roofline)."""
+    frames through the synchronous per-frame path (fvgs_track_frame_pyramid +
+    fvgs_map_step).  Returns its measurements (frames/s, latency, e2e, pose
+    error, per-kernel-class roofline)."""
     n_frames = args.warmup + args.steps
     scene = S.room(args.n, seed=0)
-    sess = fvgs.Session(args.n, 1280, 720, device=dev.index or 0)
+    sess = fvgs.Session(args.n, 1280, 720, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    W, H, K, frames = make_workload(sess, n_frames, seed=17 * rank)
+    W, H, K, frames = make_workload(S, sess, n_frames, seed=17 * rank)
     # device-resident frames for the `value` leg, pinned host frames for e2e
-    dframes, hframes = [], []
-    for f in frames:
-        dframes.append({k: torch.from_numpy(np.ascontiguousarray(f[k])).to(dev) for k in ("rgb", "depth", "gx", "gy")})
-        hframes.append({k: torch.from_numpy(np.ascontiguousarray(f[k])).pin_memory() for k in ("rgb", "depth", "gx", "gy")})
+    dframes = [to_device(torch, dev, f["pyr"]) for f in frames]
+    hframes = [to_pinned(torch, f["pyr"]) for f in frames]
     torch.cuda.synchronize()
 
     def step(k, src):
-        fr = src[k % len(src)]
-        set_frame_tensors(fvgs, sess, 0, fr, W, H)
-        pose, _ = sess.track_frame(frames[k % len(frames)]["prev"], K, iterations=ITERS)
+        set_pyramid(fvgs, sess, src[k % len(src)], W, H)
+        pose, _ = sess.track_frame_pyramid(frames[k % len(frames)]["prev"], K, PYR)
         sess.map_step(pose, K, ETA)
         return pose
 
@@ -467,57 +626,71 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     ms = ev0.elapsed_time(ev1)
     lat = sorted(a.elapsed_time(b) for a, b in step_ev)
     timed_launches = sess.get_timing(reset=True)
-    n_inst = int(sess.project_bin(frames[-1]["pose"], K, W, H))
 
     # e2e leg: pinned host frames through the C-ABI
     torch.cuda.synchronize()
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    e2e_errs = []
     e0.record(stream)
     for i in range(args.steps):
-        step(args.warmup + i, hframes)
+        k = args.warmup + i
+        pose = step(k, hframes)
+        e2e_errs.append(S.pose_error(pose, frames[k % len(frames)]["pose"]))
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
     e2e_ms = e0.elapsed_time(e1)
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], dev, world)
 
+    # the level-0 binning the frames end on: instances, visible Gaussians,
+    # records the tracking kernel must read
+    last = frames[-1]
+    n_inst = int(sess.project_bin(last["pose"], K, W, H))
+    proj = sess.download_projection(debug=False)
+    n_vis = int(np.count_nonzero(proj["counts"]))
+    visited, listed = visited_records(fvgs, sess, last["pose"], K, W, H)
+
     maint = measure_maintenance(fvgs, sess, frames, K, W, H, reps=max(3, args.steps),
                                 with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     dominant = max((c for c in timing if timing[c]["timed"]), key=lambda c: timing[c]["ms"])
     peak, peak_kind = load_peaks()
-    # every kernel class with algorithmic bytes: live GB/s against the HBM peak
-    # (not the key emission: 20 of a frame's 21 binnings are incremental and
-    # emit only the entering instances, so its full-binning bytes do not apply)
+    traffic = load_traffic()
     per_class = {}
     for c, t in timing.items():
-        algo_c = algorithmic_bytes(c, args.n, n_inst, W, H)
-        if not t["timed"] or algo_c is None or c == "emit":
+        ab = algorithmic_bytes(c, args.n, n_vis, n_inst, visited, W, H)
+        if not t["timed"] or ab is None:
             continue
+        algo_c, basis = ab
         ms_c = t["ms"] / t["timed"]
-        per_class[c] = {"ms_per_launch": ms_c, "algorithmic_bytes_per_launch": algo_c,
-                        "achieved_gbs": algo_c / (ms_c / 1000.0) / 1e9, "frac": algo_c / (ms_c / 1000.0) / 1e9 / peak}
+        e = {"ms_per_launch": ms_c, "algorithmic_bytes_per_launch": algo_c, "bytes_basis": basis,
+             "achieved_gbs": algo_c / (ms_c / 1000.0) / 1e9, "frac": algo_c / (ms_c / 1000.0) / 1e9 / peak}
+        if traffic.get(c):
+            e["ncu_dram_bytes_per_launch"] = traffic[c]
+            e["ncu_dram_gbs"] = traffic[c] / (ms_c / 1000.0) / 1e9
+        per_class[c] = e
     per_launch_ms = timing[dominant]["ms"] / max(1, timing[dominant]["timed"])
-    algo = algorithmic_bytes(dominant, args.n, n_inst, W, H)
+    algo, basis = algorithmic_bytes(dominant, args.n, n_vis, n_inst, visited, W, H)
     achieved = algo / (per_launch_ms / 1000.0) / 1e9
     sess.close()
     return {
-        "workload": "room N=%d, 1280x720, 16x16 tiles, 20 GN iterations + 1 mapping step per frame" % args.n,
-        "form": "plain per-frame GPU path (fvgs_track_frame + fvgs_map_step)",
+        "workload": "room N=%d, 1280x720, 16x16 tiles, 20 GN iterations coarse-to-fine + 1 mapping step per frame"
+                    % args.n,
+        "form": "plain per-frame GPU path (fvgs_track_frame_pyramid + fvgs_map_step)",
         "frames_per_s": replica_throughput(args.steps, world, ms), "ms_per_frame": ms / args.steps,
         "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
         "e2e_frames_per_s": replica_throughput(args.steps, world, e2e_ms),
-        "pose_error_median": {"rad": float(np.median([e[0] for e in errs])),
-                              "m": float(np.median([e[1] for e in errs]))},
-        "instances_per_binning": n_inst,
+        "pose_error": err_stats(errs), "e2e_pose_error": err_stats(e2e_errs),
+        "instances_per_binning": n_inst, "visible_gaussians": n_vis,
+        "track_records_read": visited, "track_records_listed": listed,
         "gpu_launches": int(sum(v["launches"] for v in timed_launches.values())),
         "kernel_share": {c: round(v["ms"] / max(1e-9, sum(x["ms"] for x in timing.values())), 4)
                          for c, v in timing.items() if v["ms"] > 0},
         "roofline": {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": load_traffic().get(dominant), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": per_launch_ms,
+                     "frac": achieved / peak, "traffic": traffic.get(dominant), "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": algo, "bytes_basis": basis, "ms_per_launch": per_launch_ms,
                      "issue": issue_roofline(dominant, per_launch_ms, dev)},
         "kernel_rooflines": per_class,
         "maintenance": maint,
@@ -565,7 +738,7 @@ def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
     removed = sess.prune()
     out["prune_compact"] = {"call_ms": 1000.0 * (time.perf_counter() - t0), "removed": removed}
     if with_cpu:
-        out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["depth"])
+        out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["pyr"][0]["depth"])
     return out
 
 
@@ -592,25 +765,24 @@ def cpu_outlier_sample(sess, pose, K, W, H, depth, band_rows=64):
 
 def run_precision(args, fvgs, S, torch, dev, stream, world):
     """The precision form on an N = 2 M room at 1280x720: the same tracking
-    frames (20 GN iterations, map fixed) with FP32 attributes and with BF16
-    scale/rotation + FP16 colour/opacity; frames/s of both, the pose
+    frames (20 coarse-to-fine iterations, map fixed) with FP32 attributes and
+    with BF16 scale/rotation + FP16 colour/opacity; frames/s of both, the pose
     difference between them and each one's error to the true pose."""
     n = args.prec_n
     scene = S.room(n, seed=3)
-    sess = fvgs.Session(n, 1280, 720, device=dev.index or 0)
+    sess = fvgs.Session(n, 1280, 720, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    W, H, K, frames = make_workload(sess, args.warmup + args.steps, seed=29)
-    dframes = [{k: torch.from_numpy(np.ascontiguousarray(f[k])).to(dev) for k in ("rgb", "depth", "gx", "gy")}
-               for f in frames]
+    W, H, K, frames = make_workload(S, sess, args.warmup + args.steps, seed=29)
+    dframes = [to_device(torch, dev, f["pyr"]) for f in frames]
     torch.cuda.synchronize()
     out, poses = {}, {}
     for name, prec in (("fp32", fvgs.PRECISION_FP32), ("reduced", fvgs.PRECISION_REDUCED)):
         sess.set_precision(prec)
 
         def step(k):
-            set_frame_tensors(fvgs, sess, 0, dframes[k], W, H)
-            return sess.track_frame(frames[k]["prev"], K, iterations=ITERS)[0]
+            set_pyramid(fvgs, sess, dframes[k], W, H)
+            return sess.track_frame_pyramid(frames[k]["prev"], K, PYR)[0]
 
         for k in range(args.warmup):
             step(k)
@@ -624,11 +796,9 @@ def run_precision(args, fvgs, S, torch, dev, stream, world):
         poses[name] = got
         errs = [S.pose_error(p, frames[args.warmup + i]["pose"]) for i, p in enumerate(got)]
         out[name] = {"frames_per_s": replica_throughput(args.steps, world, ms), "ms_per_frame": ms / args.steps,
-                     "pose_error_median": {"rad": float(np.median([e[0] for e in errs])),
-                                           "m": float(np.median([e[1] for e in errs]))},
-                     "footprint_gb": sess.footprint() / 1e9}
+                     "pose_error": err_stats(errs), "footprint_gb": sess.footprint() / 1e9}
     d = [S.pose_error(a, b) for a, b in zip(poses["reduced"], poses["fp32"])]
-    out["workload"] = "room N=%d, 1280x720, 20 GN iterations per frame, map fixed" % n
+    out["workload"] = "room N=%d, 1280x720, 20 GN iterations coarse-to-fine per frame, map fixed" % n
     out["pose_difference_max"] = {"rad": float(max(e[0] for e in d)), "m": float(max(e[1] for e in d))}
     out["speedup_reduced_over_fp32"] = out["reduced"]["frames_per_s"] / out["fp32"]["frames_per_s"]
     out["visual_inertial"] = run_visual_inertial(args, fvgs, S, torch, dev, stream, world, sess, K, W, H)
@@ -702,43 +872,40 @@ def run_visual_inertial(args, fvgs, S, torch, dev, stream, world, sess, K, W, H)
 def run_batching(args, fvgs, S, torch, dev, world):
     """The batching workload: 64 keyframes (sessions) with maps of N
     log-uniform in [20k, 2M], 640x480 and 1280x720 alternately; one step =
-    one tracking frame (20 GN iterations) of every keyframe, either as 64
-    sequential plain frames (fvgs_track_frame) or as one fvgs_frames_run call
-    (all frames in flight together, each replayed from its captured graph)."""
+    one coarse-to-fine tracking frame (20 GN iterations) of every keyframe,
+    either as 64 sequential plain frames (fvgs_track_frame_pyramid) or as one
+    fvgs_frames_run_pyramid call (all frames in flight together, each replayed
+    from its captured graph)."""
     rng = np.random.default_rng(41)
     ns = np.exp(rng.uniform(np.log(BATCH_N_MIN), np.log(BATCH_N_MAX), args.batch_sessions)).astype(int)
     ws = []
     for i in range(args.batch_sessions):
         cam = S.CAM_VGA if i % 2 == 0 else S.CAM_HD
         W, H, K = cam.width, cam.height, cam.intrinsics
-        sess = fvgs.Session(int(ns[i]), W, H, device=dev.index or 0)
+        sess = fvgs.Session(int(ns[i]), W, H, fvgs.default_params(QUIRKS), device=dev.index or 0)
         sess.upload(S.room(int(ns[i]), seed=5000 + i))
         traj = S.trajectory(3, seed=6000 + i)
         frames = []
         for k in range(2):
-            col, dep, _, _ = sess.render(traj[k + 1], K, W, H)
-            rgb, d = S.add_noise(col, dep, rng)
-            gx, gy = S.sobel3(rgb)
-            frames.append({"prev": traj[k], "pose": traj[k + 1],
-                           "dev": {k2: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
-                                   for k2, v in (("rgb", rgb), ("depth", d), ("gx", gx), ("gy", gy))}})
+            frames.append({"prev": S.perturb(traj[k + 1], PRED_DEG, PRED_CM, rng), "pose": traj[k + 1],
+                           "dev": to_device(torch, dev, render_pyramid(S, sess, traj[k + 1], K, W, H, rng))})
         ws.append({"sess": sess, "W": W, "H": H, "K": K, "frames": frames})
     torch.cuda.synchronize()
 
     def load(k):
         for w in ws:
-            set_frame_tensors(fvgs, w["sess"], 0, w["frames"][k % 2]["dev"], w["W"], w["H"])
+            set_pyramid(fvgs, w["sess"], w["frames"][k % 2]["dev"], w["W"], w["H"])
 
     def batched(k):
         load(k)
-        return fvgs.frames_run([w["sess"] for w in ws], [w["frames"][k % 2]["prev"] for w in ws],
-                               [w["K"] for w in ws], iterations=ITERS)
+        return fvgs.frames_run_pyramid([w["sess"] for w in ws], [w["frames"][k % 2]["prev"] for w in ws],
+                                       [w["K"] for w in ws], PYR)
 
     def sequential(k):
         out = []
         for w in ws:
-            set_frame_tensors(fvgs, w["sess"], 0, w["frames"][k % 2]["dev"], w["W"], w["H"])
-            out.append(w["sess"].track_frame(w["frames"][k % 2]["prev"], w["K"], iterations=ITERS)[0])
+            set_pyramid(fvgs, w["sess"], w["frames"][k % 2]["dev"], w["W"], w["H"])
+            out.append(w["sess"].track_frame_pyramid(w["frames"][k % 2]["prev"], w["K"], PYR)[0])
         return out
 
     for k in range(max(4, args.warmup + 1)):  # both buffer parities of both frames captured
@@ -757,59 +924,45 @@ def run_batching(args, fvgs, S, torch, dev, world):
     torch.cuda.synchronize()
     bat_s = time.perf_counter() - t0
     same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(seq, bat))
+    k_last = steps - 1
+    errs = [S.pose_error(p, w["frames"][k_last % 2]["pose"]) for p, w in zip(bat, ws)]
     graphed = sum(w["sess"].frame_stats()["graphed"] for w in ws)
     for w in ws:
         w["sess"].close()
     seq_s, bat_s = max_over_ranks([seq_s, bat_s], dev, world)
     n = steps * len(ws)
     return {"workload": "%d keyframes, N log-uniform in [20k, 2M] (%d Gaussians in total), 640x480 / 1280x720, "
-                        "20 GN iterations per frame; one step = one frame of every keyframe"
+                        "20 GN iterations coarse-to-fine per frame; one step = one frame of every keyframe"
                         % (len(ws), int(ns.sum())),
             "batched_frames_per_s": world * n / bat_s, "sequential_frames_per_s": world * n / seq_s,
             "speedup_batched_over_sequential": seq_s / bat_s, "poses_identical": bool(same),
-            "graphed_frames": graphed,
-            "form": "fvgs_frames_run: every keyframe's frame on its own stream from its captured graph, "
-                    "against fvgs_track_frame one keyframe after the other"}
+            "pose_error": err_stats(errs), "graphed_frames": graphed,
+            "form": "fvgs_frames_run_pyramid: every keyframe's frame on its own stream from its captured graph, "
+                    "against fvgs_track_frame_pyramid one keyframe after the other"}
 
 
-def set_frame_tensors(fvgs, sess, level, fr, W, H):
-    st = sess.lib.fvgs_set_frame(sess.h, level, *(fvgs.C.c_void_p(fr[k].data_ptr()) for k in ("rgb", "depth", "gx", "gy")),
-                                 W, H)
-    if st != 0:
-        raise fvgs.FvgsError(st, "fvgs_set_frame")
-
-
-def frame_ptrs(fvgs, fr, W, H):
-    return tuple(fvgs.C.c_void_p(fr[k].data_ptr()) for k in ("rgb", "depth", "gx", "gy")) + (W, H)
-
-
-def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session, seed):
-    """Sessions of the serving configuration: maps of N log-uniform in
-    [100k, 3M] Gaussians (room scenes), 640x480 and 1280x720 frames
-    alternately, each with a short random-walk trajectory and frames rendered
-    at its true poses (+ noise, Sobel gradients)."""
-    rng = np.random.default_rng(seed)
-    ns = np.exp(rng.uniform(np.log(SERVE_N_MIN), np.log(SERVE_N_MAX), n_sessions)).astype(int)
+def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session):
+    """Sessions of the serving configuration (serving_sessions): each with a
+    short random-walk trajectory, its frames' four-level pyramids rendered at
+    the true poses (+ noise) in HBM and packed in pinned host memory, and
+    each frame's predicted start pose."""
+    rng = np.random.default_rng(SERVE_SEED)
     out = []
-    for i in range(n_sessions):
-        cam = S.CAM_VGA if i % 2 == 0 else S.CAM_HD
+    for spec in serving_sessions(n_sessions):
+        cam = spec["cam"]
         W, H, K = cam.width, cam.height, cam.intrinsics
-        sess = fvgs.Session(int(ns[i]), W, H, device=dev.index or 0)
-        sess.upload(S.room(int(ns[i]), seed=seed + 1000 + i))
-        traj = S.trajectory(frames_per_session + 1, seed=seed + 2000 + i)
+        sess = fvgs.Session(spec["n"], W, H, fvgs.default_params(QUIRKS), device=dev.index or 0)
+        sess.upload(S.room(spec["n"], seed=spec["map_seed"]))
+        traj = S.trajectory(frames_per_session + 1, seed=spec["traj_seed"])
         frames = []
         for k in range(frames_per_session):
-            col, dep, _, _ = sess.render(traj[k + 1], K, W, H)
-            rgb, d = S.add_noise(col, dep, rng)
-            gx, gy = S.sobel3(rgb)
-            f = {"rgb": rgb, "depth": d, "gx": gx, "gy": gy}
-            raw_color = np.clip(np.rint(np.clip(rgb, 0.0, 1.0) * 255.0), 0, 255).astype(np.uint8)
-            frames.append({"pose": traj[k + 1], "prev": traj[k],
-                           "dev": {k2: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k2, v in f.items()},
-                           "host": {k2: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k2, v in f.items()},
-                           "raw": {"color": torch.from_numpy(raw_color).pin_memory(),
-                                   "depth": torch.from_numpy(np.ascontiguousarray(d)).pin_memory()}})
-        out.append({"sess": sess, "W": W, "H": H, "K": K, "n": int(ns[i]), "frames": frames})
+            pyr = render_pyramid(S, sess, traj[k + 1], K, W, H, rng)
+            packed = torch.from_numpy(fvgs.pack_pyramid([(lv["rgb"], lv["depth"], lv["gx"], lv["gy"]) for lv in pyr]))
+            frames.append({"pose": traj[k + 1], "prev": S.perturb(traj[k + 1], PRED_DEG, PRED_CM, rng),
+                           "dev": to_device(torch, dev, pyr),
+                           "packed": packed.pin_memory(), "packed_dev": packed.to(dev),
+                           "packed_bytes": int(packed.numel() * 4)})
+        out.append({"sess": sess, "W": W, "H": H, "K": K, "n": spec["n"], "frames": frames})
     torch.cuda.synchronize()
     return out
 
@@ -829,9 +982,9 @@ def run_serving(args, fvgs, S, torch, dev):
     """Serving configuration: the same request stream through (a) the plain
     per-frame path, one request at a time, and (b) the continuous-batching
     server (requests of all sessions in flight together, frames replayed from
-    captured graphs).  Returns frames/s of both, the server's latency under
-    Poisson arrivals, e2e with host frames, kernel launches."""
-    ws = make_serving_workload(fvgs, S, torch, dev, args.sessions, SERVE_FRAMES, seed=5)
+    captured graphs).  Returns frames/s and pose error of both, the server's
+    latency under Poisson arrivals, e2e with host frames, kernel launches."""
+    ws = make_serving_workload(fvgs, S, torch, dev, args.sessions, SERVE_FRAMES)
     total_bytes = sum(w["sess"].footprint() for w in ws)
     # warm-up: every session runs plain, plain, map, plain, plain, map, plain
     # frames (captures both frame shapes at both buffer parities)
@@ -839,21 +992,23 @@ def run_serving(args, fvgs, S, torch, dev):
     for w in ws:
         for j, eta in enumerate(warm):
             f = w["frames"][j % len(w["frames"])]
-            set_frame_tensors(fvgs, w["sess"], 0, f["dev"], w["W"], w["H"])
-            w["sess"].frame_submit(f["prev"], w["K"], iterations=ITERS, map_eta=eta)
+            set_pyramid(fvgs, w["sess"], f["dev"], w["W"], w["H"])
+            w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR, map_eta=eta)
             w["sess"].frame_wait()
     torch.cuda.synchronize()
     rounds = max(1, args.steps)
     reqs = serving_requests(ws, rounds, 0)
 
     # (a) plain per-frame path: one request after the other
+    plain_errs = []
     t0 = time.perf_counter()
     for i, r, f, eta in reqs:
         w = ws[i]
-        set_frame_tensors(fvgs, w["sess"], 0, f["dev"], w["W"], w["H"])
-        pose, _ = w["sess"].track_frame(f["prev"], w["K"], iterations=ITERS)
+        set_pyramid(fvgs, w["sess"], f["dev"], w["W"], w["H"])
+        pose, _ = w["sess"].track_frame_pyramid(f["prev"], w["K"], PYR)
         if eta is not None:
             w["sess"].map_step(pose, w["K"], eta)
+        plain_errs.append(S.pose_error(pose, f["pose"]))
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
 
@@ -863,27 +1018,22 @@ def run_serving(args, fvgs, S, torch, dev):
         with fvgs.Server(memory_budget_bytes=SERVE_BUDGET, max_inflight=args.sessions) as sv:
             slots = [sv.admit(w["sess"]) for w in ws]
             t_start = fvgs.Server.now()
-            if arrivals is None:
-                for j, (i, r, f, eta) in enumerate(reqs_):
-                    w = ws[i]
-                    if frames_key == "raw":
-                        sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
-                                  raw=(f["raw"]["color"].data_ptr(), f["raw"]["depth"].data_ptr(), w["W"], w["H"]))
-                    else:
-                        sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
-                                  frame=frame_ptrs(fvgs, f[frames_key], w["W"], w["H"]))
-            else:
-                order = sorted(range(len(reqs_)), key=lambda j: arrivals[j])
-                for j in order:
-                    i, r, f, eta = reqs_[j]
-                    w = ws[i]
+            order = range(len(reqs_)) if arrivals is None else sorted(range(len(reqs_)), key=lambda j: arrivals[j])
+            for j in order:
+                i, r, f, eta = reqs_[j]
+                w = ws[i]
+                kw = {}
+                if arrivals is not None:
                     while True:
                         now = fvgs.Server.now()
                         if now >= t_start + arrivals[j]:
                             break
                         time.sleep(min(1e-3, t_start + arrivals[j] - now))
-                    sv.submit(slots[i], f["prev"], w["K"], iterations=ITERS, map_eta=eta, tag=j,
-                              frame=frame_ptrs(fvgs, f[frames_key], w["W"], w["H"]), t_arrival=t_start + arrivals[j])
+                    kw["t_arrival"] = t_start + arrivals[j]
+                # the request's four-level frame: from HBM (device-to-device copies) or pinned host memory
+                src = f["packed"] if frames_key == "host" else f["packed_dev"]
+                sv.submit(slots[i], f["prev"], w["K"], map_eta=eta, tag=j, pyramid=PYR,
+                          pyramid_frames=(src.data_ptr(), w["W"], w["H"]), **kw)
             res = []
             while len(res) < len(reqs_):
                 res += sv.results(wait_for=len(reqs_) - len(res))
@@ -894,15 +1044,15 @@ def run_serving(args, fvgs, S, torch, dev):
         launches = sum(sum(v["launches"] for v in w["sess"].get_timing(reset=True).values()) for w in ws)
         span = max(x["t_done"] for x in res) - t_start
         lat = sorted(1000.0 * (x["t_done"] - x["t_arrival"]) for x in res)
+        errs = [S.pose_error(x["pose"], reqs_[x["tag"]][2]["pose"]) for x in res]
         return {"frames_per_s": len(res) / span, "span_s": span, "latency_ms": lat, "launches": launches,
-                "stats": stats, "results": res}
+                "stats": stats, "errs": errs}
 
     clocks = ClockSampler(dev.index or 0)
     clocks.start()
     sat = served("dev", reqs)
     clk = clocks.stop()
     e2e = served("host", reqs)
-    e2e_raw = served("raw", reqs)
     # latency under Poisson arrivals: 30 Hz per session, or 70% of the measured
     # capacity if the GPU cannot sustain that rate
     hz = min(SERVE_HZ, 0.7 * sat["frames_per_s"] / len(ws))
@@ -920,7 +1070,6 @@ def run_serving(args, fvgs, S, torch, dev):
             arrivals.append(t)
             r += 1
     poi = served("dev", preqs, arrivals)
-    frame_bytes = [40 * w["W"] * w["H"] for w in ws]
     out = {
         "sessions": len(ws), "footprint_gb": total_bytes / 1e9,
         "gaussians": [w["n"] for w in ws], "sizes": ["%dx%d" % (w["W"], w["H"]) for w in ws],
@@ -928,10 +1077,11 @@ def run_serving(args, fvgs, S, torch, dev):
         "served_frames_per_s": sat["frames_per_s"], "served_span_s": sat["span_s"],
         "plain_frames_per_s": len(reqs) / plain_s, "plain_span_s": plain_s,
         "e2e_frames_per_s": e2e["frames_per_s"],
-        "e2e_raw_frames_per_s": e2e_raw["frames_per_s"],
-        "h2d_raw_bytes_per_round": int(sum(7 * w["W"] * w["H"] for w in ws)),
-        "h2d_bytes_per_round": int(sum(frame_bytes)), "d2h_bytes_per_round": 160 * len(ws),
+        "h2d_bytes_per_round": int(sum(w["frames"][0]["packed_bytes"] for w in ws)),
+        "d2h_bytes_per_round": 160 * len(ws),
         "launches": sat["launches"], "clocks": clk,
+        "pose_error": {"plain": err_stats(plain_errs), "served": err_stats(sat["errs"]),
+                       "e2e": err_stats(e2e["errs"]), "poisson": err_stats(poi["errs"])},
         "poisson": {"hz_per_session": hz, "spec_hz_per_session": SERVE_HZ, "seconds": SERVE_SECONDS,
                     "requests": len(preqs), "frames_per_s": poi["frames_per_s"],
                     "p50_ms": poi["latency_ms"][len(poi["latency_ms"]) // 2],
@@ -941,33 +1091,6 @@ def run_serving(args, fvgs, S, torch, dev):
     for w in ws:
         w["sess"].close()
     return out
-
-
-def cpu_serving_sample(args):
-    """CPU restatement on a bounded sample of the serving mix: the median-N
-    session of each frame size, one whole frame (20 Gauss-Newton iterations
-    and a mapping step, see cpu_frame_run), scaled to the mix in proportion
-    to N."""
-    rng = np.random.default_rng(5)
-    ns = np.exp(rng.uniform(np.log(SERVE_N_MIN), np.log(SERVE_N_MAX), args.sessions)).astype(int)
-    from f_vigs_slam_gb300 import synthetic as S
-
-    per = []
-    wall = 0.0
-    threads = 1
-    for parity, cam in ((0, S.CAM_VGA), (1, S.CAM_HD)):
-        group = sorted(int(n) for i, n in enumerate(ns) if i % 2 == parity)
-        n_med = group[len(group) // 2]
-        r = cpu_frame_run(n_med, cam, seed=0, maps_per_frame=1.0 / MAP_EVERY)
-        wall += r["wall_s"]
-        threads = r["threads"]
-        per += [r["frame_s"] * n / n_med for n in group]
-    frame_s = float(np.mean(per))
-    return {"value": 1.0 / frame_s, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": ("median-N session of each frame size, one whole frame each (20 binnings + Jacobians + GN "
-                       "steps and one mapping step, weighted 1/%d; %.1f s of CPU work), scaled to the %d sessions in "
-                       "proportion to N"
-                       % (MAP_EVERY, wall, args.sessions))}
 
 
 def run_ours(args):
@@ -1003,38 +1126,36 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_serving_sample(args)
+        r = cpu_serving_run(args.sessions, CPU_BASELINE_BUDGET_S, 3 * CPU_BASELINE_BUDGET_S)
+        t = np.array(r["frame_s"])
+        cpu = {"value": len(t) / float(t.sum()), "unit": "frames/s", "cores": r["cores"], "kind": "port",
+               "sample": "the first %d frames of the serving mix (%s), FP64 restatement with OpenMP, %.1f s of "
+                         "timed work" % (len(t), ", ".join(r["frames"]), t.sum()),
+               "pose_error": err_stats(r["pose_errors"])}
 
     if rank == 0:
+        cfg = serving_config(srv["sessions"])
+        cfg.update({"form": "served + batched: continuous-batching server, all sessions' frames in flight "
+                            "together, frames replayed from per-session CUDA graphs",
+                    "parallelism": "replicas" if world > 1 else "single",
+                    "l2": "not flushed: the sessions' working sets (%.1f GB in HBM) exceed the 129 MB L2"
+                          % srv["footprint_gb"],
+                    "gaussians": srv["gaussians"], "sizes": srv["sizes"], "requests": srv["requests"]})
         line = {
             "metric": METRIC, "value": srv_fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * srv["served_span_s"] / srv["rounds"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": ("serving: %d sessions, maps of 100k-3M Gaussians (log-uniform, room scenes), "
-                                    "640x480 / 1280x720 frames, 20 GN iterations per frame, a mapping step every "
-                                    "%d-th frame; one step = one request per session" % (srv["sessions"], MAP_EVERY)),
-                       "form": "served + batched: continuous-batching server, all sessions' frames in flight "
-                               "together, frames replayed from per-session CUDA graphs",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "not flushed: the sessions' working sets (%.1f GB in HBM) exceed the 129 MB L2"
-                             % srv["footprint_gb"],
-                       "sessions": srv["sessions"], "gaussians": srv["gaussians"], "sizes": srv["sizes"],
-                       "requests": srv["requests"]},
+            "config": cfg,
             "plain": {"value": plain_fps, "unit": "frames/s",
-                      "form": "the same requests one at a time through the plain per-frame path",
-                      "speedup_served_over_plain": srv_fps / plain_fps},
+                      "form": "the same requests one at a time through the plain per-frame path"},
+            "speedup_served_over_plain": srv_fps / plain_fps,
+            "pose_error": srv["pose_error"],
             "p50_ms": srv["poisson"]["p50_ms"], "p99_ms": srv["poisson"]["p99_ms"],
             "latency": srv["poisson"],
-            "pose_error": "the served frames return the same poses as the plain path (tracking results are bit-"
-                          "identical; tests/test_serving_gpu.py), so pose error is equal by construction",
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": srv["h2d_bytes_per_round"],
                     "d2h_bytes_per_step": srv["d2h_bytes_per_round"],
-                    "path": "server requests carrying pinned host frames (fvgs_server_submit), copies inside",
-                    "raw_camera_frames": {"value": srv["e2e_raw_frames_per_s"], "unit": "frames/s",
-                                          "h2d_bytes_per_step": srv["h2d_raw_bytes_per_round"],
-                                          "path": "requests carrying 8-bit colour + float depth camera frames, "
-                                                  "pyramid level, colour scaling and Sobel gradients built on the "
-                                                  "device (fvgs_preprocess_frame)"}},
+                    "path": "server requests carrying each frame's four pyramid levels in one pinned host buffer "
+                            "(fvgs_server_submit), copies inside the timed region"},
             "gpu_launches": srv["launches"],
             "graphed_frames": srv["graphed_frames"],
             "roofline": large["roofline"],

@@ -79,7 +79,17 @@ struct fvgs_server {
                     sl.queue.pop_front();
                     const fvgs_server_request& r = sl.running;
                     int rc = FVGS_OK;
-                    if (r.rgb)
+                    if (r.pyr_levels > 0 && r.pyr_frames) {
+                        int w = r.width, h = r.height;
+                        const float* p = r.pyr_frames;
+                        for (int l = 0; l < r.pyr_levels && rc == FVGS_OK; ++l) {
+                            const size_t px = (size_t)w * h;
+                            rc = fvgs_set_frame(sl.session, l, p, p + 3 * px, p + 4 * px, p + 7 * px, w, h);
+                            p += 10 * px;
+                            w = (w + 1) / 2;
+                            h = (h + 1) / 2;
+                        }
+                    } else if (r.rgb)
                         rc = fvgs_set_frame(sl.session, r.level, r.rgb, r.depth, r.grad_x, r.grad_y, r.width,
                                             r.height);
                     else if (r.raw_color)

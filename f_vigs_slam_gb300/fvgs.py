@@ -547,6 +547,15 @@ def frames_run_pyramid(sessions, poses, K0s, iterations=(4, 4, 6, 6), map_etas=N
     return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
 
 
+def pack_pyramid(levels):
+    """Pack per-level frames [(rgb, depth, gx, gy), ...] (level 0 first) into one float32 array in the
+    layout of fvgs_server_request.pyr_frames: per level rgb[3P], depth[P], grad_x[3P], grad_y[3P]."""
+    parts = []
+    for rgb, d, gx, gy in levels:
+        parts += [np.ravel(_f32(rgb)), np.ravel(_f32(d)), np.ravel(_f32(gx)), np.ravel(_f32(gy))]
+    return np.concatenate(parts)
+
+
 # ---- serving (include/fvgs_server.h) ----
 class ServerRequest(C.Structure):
     _fields_ = [("pose", Pose), ("K", Intrinsics), ("level", C.c_int), ("iterations", C.c_int),
@@ -554,7 +563,7 @@ class ServerRequest(C.Structure):
                 ("rgb", C.c_void_p), ("depth", C.c_void_p), ("grad_x", C.c_void_p), ("grad_y", C.c_void_p),
                 ("width", C.c_int), ("height", C.c_int), ("raw_color", C.c_void_p), ("raw_depth", C.c_void_p),
                 ("raw_depth_u16_mm", C.c_int), ("raw_levels", C.c_int), ("raw_double_scale", C.c_int),
-                ("pyr_levels", C.c_int), ("pyr_iterations", C.c_int * MAX_LEVELS)]
+                ("pyr_levels", C.c_int), ("pyr_iterations", C.c_int * MAX_LEVELS), ("pyr_frames", C.c_void_p)]
 
 
 class ServerResult(C.Structure):
@@ -598,11 +607,12 @@ class Server:
         return float(t.value)
 
     def submit(self, slot: int, pose, K, iterations: int = 20, level: int = 0, map_eta: float | None = None,
-               tag: int = 0, t_arrival: float = 0.0, frame=None, raw=None, pyramid=None):
+               tag: int = 0, t_arrival: float = 0.0, frame=None, raw=None, pyramid=None, pyramid_frames=None):
         """frame: optional (rgb_ptr, depth_ptr, gx_ptr, gy_ptr, W, H) of memory that stays valid (pinned
         host or device) until the result is back, for `level`; raw: optional (color_u8_ptr, depth_ptr, W,
         H[, depth_u16]) camera frame, preprocessed on the device (level 0); pyramid: optional per-level
-        iteration counts of a coarse-to-fine frame (K is then the level-0 intrinsics)."""
+        iteration counts of a coarse-to-fine frame (K is then the level-0 intrinsics); pyramid_frames:
+        optional (ptr, W, H) of every level's frame packed in one buffer (pack_pyramid's layout)."""
         r = ServerRequest()
         r.pose = make_pose(pose)
         r.K = make_intr(K)
@@ -611,6 +621,8 @@ class Server:
             r.pyr_levels = len(pyramid)
             for i, v in enumerate(pyramid):
                 r.pyr_iterations[i] = int(v)
+            if pyramid_frames is not None:
+                r.pyr_frames, r.width, r.height = pyramid_frames
         r.map_eta = -1.0 if map_eta is None else map_eta
         r.tag, r.t_arrival = tag, t_arrival
         if frame is not None:

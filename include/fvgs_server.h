@@ -54,6 +54,13 @@ typedef struct fvgs_server_request {
      * fvgs_frame_submit_pyramid); level and iterations are then unused. */
     int pyr_levels;
     int pyr_iterations[FVGS_MAX_LEVELS];
+    /* Optional observed frames of levels 0..pyr_levels-1 (with pyr_levels >
+     * 0; used instead of rgb / raw_color), packed one level after the other,
+     * each as rgb[3P], depth[P], grad_x[3P], grad_y[3P] with P = W_l H_l,
+     * W_0 = width, H_0 = height, W_{l+1} = (W_l + 1) / 2, H_{l+1} =
+     * (H_l + 1) / 2: one host buffer (pinned, so the copies overlap) copied to
+     * the device on the session's stream right before the frame. */
+    const float* pyr_frames;
 } fvgs_server_request;
 
 typedef struct fvgs_server_result {
