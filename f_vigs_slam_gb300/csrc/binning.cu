@@ -45,9 +45,10 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
         const float d0 = __fsub_rn(p.x, tw[0]);
         const float d1 = __fsub_rn(p.y, tw[1]);
         const float d2 = __fsub_rn(p.z, tw[2]);
-        const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[1][0], d1, __fmul_rn(R[0][0], d0)));
-        const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[1][1], d1, __fmul_rn(R[0][1], d0)));
-        const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[1][2], d1, __fmul_rn(R[0][2], d0)));
+        // a*b + c*d + e*f as nvcc contracts the reference's expression
+        const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[0][0], d0, __fmul_rn(R[1][0], d1)));
+        const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[0][1], d0, __fmul_rn(R[1][1], d1)));
+        const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[0][2], d0, __fmul_rn(R[1][2], d1)));
         if (pcz > 0.0f) {
             const float inv_z = __fdiv_rn(1.0f, pcz);
             const float uu = __fmaf_rn(K.fx, __fmul_rn(pcx, inv_z), K.cx);
@@ -79,36 +80,42 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
                     for (int c = r; c < 3; ++c) {
-                        S[r][c] = __fmaf_rn(M[r][2], M[c][2], __fmaf_rn(M[r][1], M[c][1], __fmul_rn(M[r][0], M[c][0])));
+                        S[r][c] = __fmaf_rn(M[r][2], M[c][2], __fmaf_rn(M[r][0], M[c][0], __fmul_rn(M[r][1], M[c][1])));
                         S[c][r] = S[r][c];
                     }
-                float A[3][3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        A[k][c] = __fmaf_rn(S[k][2], R[2][c], __fmaf_rn(S[k][1], R[1][c], __fmul_rn(S[k][0], R[0][c])));
+                // Sigma_cam[r][c] = sum_k sum_l R[k][r] Sigma[k][l] R[l][c]: every entry by the
+                // reference's own 9-term accumulation (src/GSCudaKernels.cu:423-433)
                 float C[3][3];
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
-                    for (int c = r; c < 3; ++c) {
-                        C[r][c] = __fmaf_rn(R[2][r], A[2][c], __fmaf_rn(R[1][r], A[1][c], __fmul_rn(R[0][r], A[0][c])));
-                        C[c][r] = C[r][c];
+                    for (int c = 0; c < 3; ++c) {
+                        float acc = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k)
+#pragma unroll
+                            for (int l = 0; l < 3; ++l) acc = __fmaf_rn(__fmul_rn(R[k][r], S[k][l]), R[l][c], acc);
+                        C[r][c] = acc;
                     }
-                const float j00 = __fmul_rn(K.fx, inv_z);
-                const float j02 = __fmul_rn(__fmul_rn(__fmul_rn(-K.fx, pcx), inv_z), inv_z);
-                const float j11 = __fmul_rn(K.fy, inv_z);
-                const float j12 = __fmul_rn(__fmul_rn(__fmul_rn(-K.fy, pcy), inv_z), inv_z);
-                const float t0 = __fmaf_rn(j02, C[0][2], __fmul_rn(j00, C[0][0]));
-                const float t2 = __fmaf_rn(j02, C[2][2], __fmul_rn(j00, C[0][2]));
-                cxx = __fmaf_rn(j02, t2, __fmul_rn(j00, t0));
-                const float s1 = __fmaf_rn(j12, C[1][2], __fmul_rn(j11, C[1][1]));
-                const float s2 = __fmaf_rn(j12, C[2][2], __fmul_rn(j11, C[1][2]));
-                cyy = __fmaf_rn(j12, s2, __fmul_rn(j11, s1));
-                const float a0 = __fmaf_rn(C[0][2], j12, __fmul_rn(C[0][1], j11));
-                const float a2 = __fmaf_rn(C[2][2], j12, __fmul_rn(C[1][2], j11));
-                cxy = __fmaf_rn(j02, a2, __fmul_rn(j00, a0));
+                const float Jm[2][3] = {
+                    {__fmul_rn(K.fx, inv_z), 0.0f, __fmul_rn(__fmul_rn(__fmul_rn(-K.fx, pcx), inv_z), inv_z)},
+                    {0.0f, __fmul_rn(K.fy, inv_z), __fmul_rn(__fmul_rn(__fmul_rn(-K.fy, pcy), inv_z), inv_z)}};
+                // Sigma_2d = J Sigma_cam J^T by the same 9-term accumulation, zero entries of J included
+                float S2[2][2];
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int c = r; c < 2; ++c) {
+                        float acc = 0.0f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k)
+#pragma unroll
+                            for (int l = 0; l < 3; ++l) acc = __fmaf_rn(__fmul_rn(Jm[r][k], C[k][l]), Jm[c][l], acc);
+                        S2[r][c] = acc;
+                    }
+                cxx = S2[0][0];
+                cyy = S2[1][1];
+                cxy = S2[0][1];
                 const float det = __fmaf_rn(cxx, cyy, -__fmul_rn(cxy, cxy));
                 if (det == 0.0f) {
                     ixx = 1.0f;

@@ -39,20 +39,34 @@ namespace {
 // FP32 projection (src/GSCudaKernels.cu:319-334 quaternionToMatrix,
 // 345-476 projectGaussiansWorldToScreen_kernel, 1411-1437 invert2x2).
 // ---------------------------------------------------------------------------
+// Contraction policy.  The reference's kernels are compiled by nvcc with its
+// default --fmad=true: a multiply feeding an add becomes one FMA, and in a sum
+// of two products the first product is fused: a*b + c*d = fma(a, b, c*d),
+// a*b - c*d = fma(a, b, -(c*d)), a*b + c*d + e*f = fma(e, f, fma(a, b, c*d)),
+// acc += a*b*c = fma(a*b, c, acc).  Built with FVGS_ORACLE_NO_FMA every
+// product and sum rounds on its own instead (what the reference's source
+// gives compiled with contraction off; oracle/ref_host.cpp).
+#ifndef FVGS_ORACLE_NO_FMA
 inline float f_fma(float a, float b, float c) { return std::fmaf(a, b, c); }
+#else
+inline float f_fma(float a, float b, float c) { return a * b + c; }
+#endif
+inline float dot2(float a, float b, float c, float d) { return f_fma(a, b, c * d); }    // a*b + c*d
+inline float diff2(float a, float b, float c, float d) { return f_fma(a, b, -(c * d)); }  // a*b - c*d
+inline float dot3(float a, float b, float c, float d, float e, float f) { return f_fma(e, f, dot2(a, b, c, d)); }
 
 // quaternionToMatrix: q read as (x,y,z,w) = (.x,.y,.z,.w); no normalisation.
 inline void quat_to_R_f32(const float q[4], float R[3][3]) {
     const float x = q[0], y = q[1], z = q[2], w = q[3];
-    R[0][0] = f_fma(-2.f, f_fma(y, y, z * z), 1.f);
-    R[0][1] = 2.f * f_fma(x, y, -(w * z));
-    R[0][2] = 2.f * f_fma(x, z, w * y);
-    R[1][0] = 2.f * f_fma(x, y, w * z);
-    R[1][1] = f_fma(-2.f, f_fma(x, x, z * z), 1.f);
-    R[1][2] = 2.f * f_fma(y, z, -(w * x));
-    R[2][0] = 2.f * f_fma(x, z, -(w * y));
-    R[2][1] = 2.f * f_fma(y, z, w * x);
-    R[2][2] = f_fma(-2.f, f_fma(x, x, y * y), 1.f);
+    R[0][0] = f_fma(-2.f, dot2(y, y, z, z), 1.f);
+    R[0][1] = 2.f * diff2(x, y, w, z);
+    R[0][2] = 2.f * dot2(x, z, w, y);
+    R[1][0] = 2.f * dot2(x, y, w, z);
+    R[1][1] = f_fma(-2.f, dot2(x, x, z, z), 1.f);
+    R[1][2] = 2.f * diff2(y, z, w, x);
+    R[2][0] = 2.f * diff2(x, z, w, y);
+    R[2][1] = 2.f * dot2(y, z, w, x);
+    R[2][2] = f_fma(-2.f, dot2(x, x, y, y), 1.f);
 }
 
 struct Proj32 {
@@ -63,16 +77,19 @@ struct Proj32 {
     float phx, phy;
 };
 
+// projectGaussiansWorldToScreen_kernel (src/GSCudaKernels.cu:345-476), every
+// expression in the kernel's own order: the 3x3 products Sigma_cam and
+// Sigma_2d as its 9-term accumulation loops (zero Jacobian entries included).
 inline Proj32 project_one_f32(const float p[3], const float s[3], const float q[4],
                               const float cam_t[3], const float R[3][3],
                               const fvgs_intrinsics& K, int W, int H) {
     Proj32 o;
     std::memset(&o, 0, sizeof(o));
     const float d0 = p[0] - cam_t[0], d1 = p[1] - cam_t[1], d2 = p[2] - cam_t[2];
-    // pos_cam = R^T (p - t)  (src/GSCudaKernels.cu:372-378)
-    const float pcx = f_fma(R[2][0], d2, f_fma(R[1][0], d1, R[0][0] * d0));
-    const float pcy = f_fma(R[2][1], d2, f_fma(R[1][1], d1, R[0][1] * d0));
-    const float pcz = f_fma(R[2][2], d2, f_fma(R[1][2], d1, R[0][2] * d0));
+    // pos_cam = R^T (p - t)  (:372-378)
+    const float pcx = dot3(R[0][0], d0, R[1][0], d1, R[2][0], d2);
+    const float pcy = dot3(R[0][1], d0, R[1][1], d1, R[2][1], d2);
+    const float pcz = dot3(R[0][2], d0, R[1][2], d1, R[2][2], d2);
     if (pcz <= 0.0f) return o;  // :381
     const float inv_z = 1.0f / pcz;
     const float u = f_fma(K.fx, pcx * inv_z, K.cx);
@@ -94,39 +111,36 @@ inline Proj32 project_one_f32(const float p[3], const float s[3], const float q[
     float S[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = i; j < 3; ++j) {
-            S[i][j] = f_fma(M[i][2], M[j][2], f_fma(M[i][1], M[j][1], M[i][0] * M[j][0]));
+            S[i][j] = dot3(M[i][0], M[j][0], M[i][1], M[j][1], M[i][2], M[j][2]);
             S[j][i] = S[i][j];
         }
-    // Sigma_cam = R^T Sigma R (:423-433), upper triangle mirrored.
-    float A[3][3];  // A = Sigma R
-    for (int k = 0; k < 3; ++k)
-        for (int j = 0; j < 3; ++j)
-            A[k][j] = f_fma(S[k][2], R[2][j], f_fma(S[k][1], R[1][j], S[k][0] * R[0][j]));
+    // Sigma_cam[i][j] = sum_k sum_l R[k][i] Sigma[k][l] R[l][j], every entry (:423-433)
     float C[3][3];
     for (int i = 0; i < 3; ++i)
-        for (int j = i; j < 3; ++j) {
-            C[i][j] = f_fma(R[2][i], A[2][j], f_fma(R[1][i], A[1][j], R[0][i] * A[0][j]));
-            C[j][i] = C[i][j];
+        for (int j = 0; j < 3; ++j) {
+            float acc = 0.0f;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) acc = f_fma(R[k][i] * S[k][l], R[l][j], acc);
+            C[i][j] = acc;
         }
     // EWA: J = [fx/z 0 -fx x/z^2; 0 fy/z -fy y/z^2]  (:438-460)
-    const float j00 = K.fx * inv_z;
-    const float j02 = (((-K.fx) * pcx) * inv_z) * inv_z;
-    const float j11 = K.fy * inv_z;
-    const float j12 = (((-K.fy) * pcy) * inv_z) * inv_z;
-    const float t0 = f_fma(j02, C[0][2], j00 * C[0][0]);
-    const float t2 = f_fma(j02, C[2][2], j00 * C[0][2]);
-    const float sxx = f_fma(j02, t2, j00 * t0);
-    const float s1 = f_fma(j12, C[1][2], j11 * C[1][1]);
-    const float s2 = f_fma(j12, C[2][2], j11 * C[1][2]);
-    const float syy = f_fma(j12, s2, j11 * s1);
-    const float a0 = f_fma(C[0][2], j12, C[0][1] * j11);
-    const float a2 = f_fma(C[2][2], j12, C[1][2] * j11);
-    const float sxy = f_fma(j02, a2, j00 * a0);
+    const float J[2][3] = {{K.fx * inv_z, 0.0f, (((-K.fx) * pcx) * inv_z) * inv_z},
+                           {0.0f, K.fy * inv_z, (((-K.fy) * pcy) * inv_z) * inv_z}};
+    float S2[2][2];
+    for (int i = 0; i < 2; ++i)
+        for (int j = i; j < 2; ++j) {
+            float acc = 0.0f;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) acc = f_fma(J[i][k] * C[k][l], J[j][l], acc);
+            S2[i][j] = acc;
+            S2[j][i] = acc;
+        }
+    const float sxx = S2[0][0], syy = S2[1][1], sxy = S2[0][1];
     o.cxx = sxx;
     o.cyy = syy;
     o.cxy = sxy;
     // invert2x2 (:1411-1437): det == 0 -> identity.
-    const float det = f_fma(sxx, syy, -(sxy * sxy));
+    const float det = diff2(sxx, syy, sxy, sxy);
     if (det == 0.0f) {
         o.ixx = 1.0f;
         o.iyy = 1.0f;
@@ -312,7 +326,7 @@ int64_t oracle_emit_keys(const float* uv, const float* depth, const float* phat,
                 const float tcx = ((float)tx + 0.5f) * (float)tw;
                 const float tcy = ((float)ty + 0.5f) * (float)th;
                 const float dx = tcx - u, dy = tcy - v;
-                const float d = std::fmaf(phy, dy, std::fmaf(phx, dx, z));
+                const float d = f_fma(phy, dy, f_fma(phx, dx, z));
                 const uint32_t tile = (uint32_t)(ty * ntx + tx);
                 keys[w] = ((uint64_t)tile << 32) | (uint64_t)f2u(d);
                 vals[w] = (uint32_t)i;

@@ -21,19 +21,26 @@ LIB = os.path.join(BUILD, "liboracle.so")
 SRC = os.path.join(HERE, "fvgs_oracle.cpp")
 
 
-def build(force: bool = False) -> str:
-    """Compile the oracle with -ffp-contract=off (bit-exact FP32 keys) and OpenMP."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
-        return LIB
+LIB_NOFMA = os.path.join(BUILD, "liboracle_nofma.so")
+
+
+def build(force: bool = False, nofma: bool = False) -> str:
+    """Compile the oracle with -ffp-contract=off (bit-exact FP32 keys) and OpenMP.
+    nofma: the variant without the reference's FMA contractions (every product
+    and sum rounded on its own), compared with the reference's source compiled
+    the same way."""
+    lib = LIB_NOFMA if nofma else LIB
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= os.path.getmtime(SRC):
+        return lib
     os.makedirs(BUILD, exist_ok=True)
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib + ".tmp%d" % os.getpid()
     cmd = [
         "g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
         "-fPIC", "-shared", "-o", tmp, SRC,
-    ]
+    ] + (["-DFVGS_ORACLE_NO_FMA"] if nofma else [])
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 class Pose(C.Structure):
@@ -96,16 +103,16 @@ def make_intr(K) -> Intr:
     return i
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        _lib = C.CDLL(build())
-        _lib.oracle_emit_keys.restype = C.c_int64
-        _lib.oracle_buckets.restype = C.c_int64
-    return _lib
+def lib(nofma: bool = False):
+    if nofma not in _libs:
+        L = C.CDLL(build(nofma=nofma))
+        L.oracle_emit_keys.restype = C.c_int64
+        L.oracle_buckets.restype = C.c_int64
+        _libs[nofma] = L
+    return _libs[nofma]
 
 
 def _p(a):
@@ -122,7 +129,7 @@ class Projection:
         self.depth, self.phat, self.visible = depth, phat, visible
 
 
-def project(scene, pose, K, W, H) -> Projection:
+def project(scene, pose, K, W, H, nofma: bool = False) -> Projection:
     n = scene.n
     uv = np.zeros((n, 2), np.float32)
     cov = np.zeros((n, 3), np.float32)
@@ -131,18 +138,18 @@ def project(scene, pose, K, W, H) -> Projection:
     ph = np.zeros((n, 2), np.float32)
     vis = np.zeros(n, np.uint8)
     pos, scl, rot = _f32(scene.positions), _f32(scene.scales), _f32(scene.orientations)
-    lib().oracle_project(
+    lib(nofma).oracle_project(
         _p(pos), _p(scl), _p(rot), C.c_int(n), C.byref(make_pose(pose)), C.byref(make_intr(K)),
         C.c_int(W), C.c_int(H), _p(uv), _p(cov), _p(inv), _p(dep), _p(ph), _p(vis),
     )
     return Projection(uv, cov, inv, dep, ph, vis)
 
 
-def count(proj: Projection, W, H, params: Params):
+def count(proj: Projection, W, H, params: Params, nofma: bool = False):
     n = proj.uv.shape[0]
     cnt = np.zeros(n, np.uint32)
     rect = np.zeros((n, 4), np.int32)
-    lib().oracle_count(
+    lib(nofma).oracle_count(
         _p(proj.uv), _p(proj.cov2d), _p(proj.visible), C.c_int(n), C.c_int(W), C.c_int(H),
         C.c_int(params.tile_w), C.c_int(params.tile_h), C.c_float(params.radius_sigma),
         C.c_uint32(params.quirks), _p(cnt), _p(rect),
@@ -150,12 +157,12 @@ def count(proj: Projection, W, H, params: Params):
     return cnt, rect
 
 
-def emit_keys(proj: Projection, cnt, rect, W, params: Params):
+def emit_keys(proj: Projection, cnt, rect, W, params: Params, nofma: bool = False):
     n = proj.uv.shape[0]
     total = int(cnt.astype(np.int64).sum())
     keys = np.zeros(max(total, 1), np.uint64)
     vals = np.zeros(max(total, 1), np.uint32)
-    got = lib().oracle_emit_keys(
+    got = lib(nofma).oracle_emit_keys(
         _p(proj.uv), _p(proj.depth), _p(proj.phat), _p(cnt), _p(rect), C.c_int(n), C.c_int(W),
         C.c_int(params.tile_w), C.c_int(params.tile_h), C.c_int64(total), _p(keys), _p(vals),
     )
@@ -210,10 +217,11 @@ class Binning:
         self.geo = geo
 
 
-def prepare(scene, pose, K, W, H, params: Params) -> Binning:
-    proj = project(scene, pose, K, W, H)
-    cnt, rect = count(proj, W, H, params)
-    kg, vg = emit_keys(proj, cnt, rect, W, params)
+def prepare(scene, pose, K, W, H, params: Params, nofma: bool = False) -> Binning:
+    """nofma: the binning without the reference's FMA contractions (see build)."""
+    proj = project(scene, pose, K, W, H, nofma)
+    cnt, rect = count(proj, W, H, params, nofma)
+    kg, vg = emit_keys(proj, cnt, rect, W, params, nofma)
     ks, vs, ranges = sort_ranges(kg, vg, W, H, params)
     rec = make_records(proj, scene, params)
     geo = None if (params.quirks & Q_POSE_JAC_APPROX) else cam3d(scene, pose)
