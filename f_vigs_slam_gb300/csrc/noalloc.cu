@@ -15,8 +15,12 @@
 //
 // Rules of use:
 //  * The first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that
-//    first call before any stream capture.
+//    cudaGetSymbolAddress (with that device current) and caches it per device
+//    ordinal, so only the device's primary context (the one the CUDA runtime
+//    uses) is supported.
+//  * The call waits for its stream and copies the result to the caller's
+//    (possibly pageable) memory, so it cannot be called while the stream is
+//    being captured into a CUDA graph.
 //  * All calls share the array and it keeps the last call's contents.  Every
 //    word a call reads is first written by the same call (all tile partials of
 //    the frame, the pose, the reduced system), so nothing needs clearing.
@@ -83,12 +87,19 @@ __global__ void noalloc_set_pose_kernel(DevPose* dst, fvgs_pose p) {
 
 }  // namespace
 
+// A failed CUDA call: clear the error the runtime keeps, so the caller's next
+// CUDA check does not report it against another operation.
+int cuda_failed() {
+    cudaGetLastError();
+    return FVGS_E_CUDA;
+}
+
 extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     const uint32_t* ranges, const uint32_t* indices, const float* positions_2d, const float* depths,
     const float* inv_covariances_2d, const float* p_hats, const float* colors, const float* opacities,
     const float* grad_x, const float* grad_y, const float* observed_rgb, const float* observed_depth,
     const fvgs_pose* pose, const fvgs_intrinsics* K, const fvgs_params* params, int width, int height,
-    double* JtJ, double* Jtr, void* cuda_stream) {
+    uint32_t n_gaussians, uint32_t n_instances, double* JtJ, double* Jtr, void* cuda_stream) {
     if (!ranges || !indices || !positions_2d || !depths || !inv_covariances_2d || !p_hats || !colors ||
         !opacities || !grad_x || !grad_y || !observed_rgb || !observed_depth || !pose || !K || !JtJ || !Jtr)
         return FVGS_E_INVALID;
@@ -107,12 +118,15 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     DevPose* dpose = reinterpret_cast<DevPose*>(base + kOffPose);
 
     noalloc_set_pose_kernel<<<1, 1, 0, s>>>(dpose, *pose);
+    if (cudaGetLastError() != cudaSuccess) return cuda_failed();
     fvgs::TrackArgs ta;
     std::memset(&ta, 0, sizeof(ta));
     ta.ranges = reinterpret_cast<const uint2*>(ranges);
     ta.indices = indices;
-    ta.n_list = 0xffffffffu;   // the caller's buffers: sizes are not passed (as in the reference)
-    ta.n_gauss = 0xffffffffu;
+    // list entries at or past n_instances and indices at or above n_gaussians
+    // are skipped, as for the library's own buffers; 0 = not checked
+    ta.n_list = n_instances ? n_instances : 0xffffffffu;
+    ta.n_gauss = n_gaussians ? n_gaussians : 0xffffffffu;
     ta.obs_rgb = observed_rgb;
     ta.obs_depth = observed_depth;
     ta.gx = grad_x;
@@ -140,13 +154,11 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     // reference's approximate Jacobian
     ta.quirks = P.quirks | FVGS_Q_POSE_JAC_APPROX;
     ta.variant = 0;
-    if (fvgs::launch_track_ref_layout(ta, s) != cudaSuccess) return FVGS_E_CUDA;
-    if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), dpose, out, s) != cudaSuccess) return FVGS_E_CUDA;
+    if (fvgs::launch_track_ref_layout(ta, s) != cudaSuccess) return cuda_failed();
+    if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), dpose, out, s) != cudaSuccess) return cuda_failed();
     if (cudaMemcpyAsync(JtJ, out, sizeof(double) * 36, cudaMemcpyDefault, s) != cudaSuccess ||
         cudaMemcpyAsync(Jtr, out + 36, sizeof(double) * 6, cudaMemcpyDefault, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
-        return FVGS_E_CUDA;
-    }
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return cuda_failed();
     return FVGS_OK;
 }

@@ -407,15 +407,22 @@ int fvgs_densify(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* 
  * (tile_ranges_), indices (sorted gaussian_indices_), positions_2d[2N],
  * depths[N], inv_covariances_2d[3N] stored (xx, yy, xy), p_hats[2N],
  * colors[3N], opacities[N], and the frame's grad_x / grad_y / observed_rgb
- * [3P] and observed_depth [P].  params may be null (defaults).  JtJ[36] and
- * Jtr[6] may be host or device pointers; the call returns after the stream
- * (a cudaStream_t, NULL = legacy default stream) has finished the work.
+ * [3P] and observed_depth [P].  n_gaussians and n_instances are the lengths
+ * of the per-Gaussian buffers and of indices: list entries past them are
+ * skipped, as for the library's own buffers (0: not checked).  params may be
+ * null (defaults); the Jacobian is the reference's approximate one whatever
+ * its quirk bits (the screen-space buffers carry no camera-frame geometry for
+ * the analytic one).  JtJ[36] and Jtr[6] may be host or device pointers; the
+ * call returns after the stream (a cudaStream_t, NULL = legacy default
+ * stream) has finished the work, so it cannot be called while that stream is
+ * being captured into a CUDA graph.
  *
  * Its scratch is one static device array for at most FVGS_NOALLOC_MAX_TILES
  * 16x16 tiles (about 1.8 MB, held by every GPU that loads the library until
  * exit); larger frames return FVGS_E_CAPACITY.  The first call on a device
- * resolves that array's address (make it before any stream capture).  Calls
- * share the array: calls that overlap on the GPU race.
+ * resolves that array's address in the device's primary context (the only
+ * context supported).  Calls share the array: calls that overlap on the GPU
+ * race.
  */
 #define FVGS_NOALLOC_MAX_TILES 16384
 int fvgs_rgbd_pose_jacobians_noalloc(const uint32_t* ranges, const uint32_t* indices, const float* positions_2d,
@@ -423,7 +430,8 @@ int fvgs_rgbd_pose_jacobians_noalloc(const uint32_t* ranges, const uint32_t* ind
                                      const float* colors, const float* opacities, const float* grad_x,
                                      const float* grad_y, const float* observed_rgb, const float* observed_depth,
                                      const fvgs_pose* pose, const fvgs_intrinsics* K, const fvgs_params* params,
-                                     int width, int height, double* JtJ, double* Jtr, void* cuda_stream);
+                                     int width, int height, uint32_t n_gaussians, uint32_t n_instances, double* JtJ,
+                                     double* Jtr, void* cuda_stream);
 
 #ifdef __cplusplus
 }

@@ -428,13 +428,15 @@ int oracle_make_records(const float* uv, const float* inv2d, const float* depth,
  * Outputs: tile_out[27T] (Jtr[6], JtJ upper[21]) per tile; JtJ[36] symmetric
  * and Jtr[6] = -sum (camera frame, before the IMU extrinsic transform);
  * optional per-pixel images (colour incl. background, depth, final T,
- * n_contrib) of the forward blend -- pass null to skip.
+ * n_contrib) of the forward blend -- pass null to skip.  tile_mask (T bytes,
+ * nullable): only tiles with a non-zero byte are evaluated, the others get
+ * zero partials.
  */
 int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indices, const float* obs_rgb,
                  const float* obs_depth, const float* gx, const float* gy, const fvgs_pose* pose,
                  const fvgs_intrinsics* Kf, const fvgs_params* P, int W, int H, double* tile_out,
                  double* JtJ, double* Jtr, double* img_color, double* img_depth, double* img_T,
-                 uint32_t* img_nc) {
+                 uint32_t* img_nc, const uint8_t* tile_mask) {
     const int tw = P->tile_w, th = P->tile_h;
     const int ntx = (W + tw - 1) / tw, nty = (H + th - 1) / th, T = ntx * nty;
     double R[3][3];
@@ -449,6 +451,10 @@ int oracle_track(const float* rec, const uint32_t* ranges, const uint32_t* indic
         const int tx = t % ntx, ty = t / ntx;
         double acc[27];
         for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+        if (tile_mask && !tile_mask[t]) {  // not evaluated: zero partials, images untouched
+            for (int k = 0; k < 27; ++k) tile_out[27 * (size_t)t + k] = 0.0;
+            continue;
+        }
         const uint32_t rs = ranges[2 * (size_t)t], re = ranges[2 * (size_t)t + 1];
         const int n_total = (int)(re - rs);
         for (int ly = 0; ly < th; ++ly)
@@ -927,7 +933,7 @@ int oracle_track_intended(const float* rec, const double* cam3d, const uint32_t*
                           const float* obs_rgb, const float* obs_depth, const fvgs_pose* pose,
                           const fvgs_intrinsics* Kf, const fvgs_params* P, int W, int H, double* tile_out,
                           double* JtJ, double* Jtr, double* img_color, double* img_depth, double* img_T,
-                          uint32_t* img_nc, double* pix_jc, double* pix_jd) {
+                          uint32_t* img_nc, double* pix_jc, double* pix_jd, const uint8_t* tile_mask) {
     const int tw = P->tile_w, th = P->tile_h;
     const int ntx = (W + tw - 1) / tw, nty = (H + th - 1) / th, T = ntx * nty;
     double R[3][3];
@@ -942,6 +948,10 @@ int oracle_track_intended(const float* rec, const double* cam3d, const uint32_t*
         const int tx = t % ntx, ty = t / ntx;
         double acc[27];
         for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+        if (tile_mask && !tile_mask[t]) {  // not evaluated: zero partials, images untouched
+            for (int k = 0; k < 27; ++k) tile_out[27 * (size_t)t + k] = 0.0;
+            continue;
+        }
         const uint32_t rs = ranges[2 * (size_t)t], re = ranges[2 * (size_t)t + 1];
         const int n_total = (int)(re - rs);
         std::vector<GeoD> dcache(n_total > 0 ? n_total : 1);

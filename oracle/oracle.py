@@ -235,16 +235,22 @@ class TrackResult:
 
 
 def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True,
-          pixel_jacobians: bool = False) -> TrackResult:
+          pixel_jacobians: bool = False, tiles=None) -> TrackResult:
     """frame = (rgb (H,W,3), depth (H,W), gx (H,W,3), gy (H,W,3)) float32.
 
     With Q_POSE_JAC_APPROX set in params.quirks this is the reference's
     getRgbdPoseJacobians; clear, the analytic pose Jacobian
     (oracle_track_intended; the gradient images are not read).  With
     pixel_jacobians (analytic mode only) the result also carries the
-    per-pixel colour Jacobian jc (H, W, 3, 6) and depth Jacobian jd (H, W, 6)."""
+    per-pixel colour Jacobian jc (H, W, 3, 6) and depth Jacobian jd (H, W, 6).
+    tiles: optional tile ids to evaluate (the others get zero partials; JtJ
+    and Jtr then sum the evaluated tiles only)."""
+    mask = None
+    if tiles is not None:
+        mask = np.zeros(num_tiles(W, H, params), np.uint8)
+        mask[np.asarray(tiles, np.int64)] = 1
     if not (params.quirks & Q_POSE_JAC_APPROX):
-        return _track_intended(b, frame, pose, K, W, H, params, images, pixel_jacobians)
+        return _track_intended(b, frame, pose, K, W, H, params, images, pixel_jacobians, mask)
     rgb, depth, gx, gy = [_f32(a) for a in frame]
     T = num_tiles(W, H, params)
     tiles = np.zeros((T, 27), np.float64)
@@ -262,12 +268,13 @@ def track(b: Binning, frame, pose, K, W, H, params: Params, images: bool = True,
     lib().oracle_track(
         _p(b.rec), _p(b.ranges), _p(b.vals), _p(rgb), _p(depth), _p(gx), _p(gy),
         C.byref(make_pose(pose)), C.byref(make_intr(K)), C.byref(params), C.c_int(W), C.c_int(H),
-        _p(tiles), _p(JtJ), _p(Jtr), *ptrs,
+        _p(tiles), _p(JtJ), _p(Jtr), *ptrs, _p(mask) if mask is not None else None,
     )
     return TrackResult(JtJ, Jtr, tiles, col, dep, fT, nc)
 
 
-def _track_intended(b: Binning, frame, pose, K, W, H, params: Params, images: bool, pixel_jacobians: bool):
+def _track_intended(b: Binning, frame, pose, K, W, H, params: Params, images: bool, pixel_jacobians: bool,
+                    mask=None):
     rgb, depth = _f32(frame[0]), _f32(frame[1])
     if b.geo is None:
         raise ValueError("binning was prepared without the geometry of the analytic Jacobian")
@@ -291,6 +298,7 @@ def _track_intended(b: Binning, frame, pose, K, W, H, params: Params, images: bo
         _p(b.rec), _p(geo), _p(b.ranges), _p(b.vals), _p(rgb), _p(depth), C.byref(make_pose(pose)),
         C.byref(make_intr(K)), C.byref(params), C.c_int(W), C.c_int(H), _p(tiles), _p(JtJ), _p(Jtr), *ptrs,
         _p(jc) if jc is not None else None, _p(jd) if jd is not None else None,
+        _p(mask) if mask is not None else None,
     )
     r = TrackResult(JtJ, Jtr, tiles, col, dep, fT, nc)
     r.jc, r.jd = jc, jd

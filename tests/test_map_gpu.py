@@ -86,3 +86,24 @@ def test_map_step_parity(oracle, fvgs_lib, quirks, bad_opacity):
         assert bad[upd].mean() < 0.01, name
     untouched = n_o == 0
     np.testing.assert_array_equal(pos[untouched & same], scene.positions[untouched & same])
+
+
+@pytest.mark.parametrize("quirks", [0x4 | 0x8, 0x0], ids=["ref", "intended"])
+def test_map_step_parity_vga_50k(oracle, fvgs_lib, quirks):
+    """The small plain-method workload whole: N = 50k at 640 x 480."""
+    W, H, scene, g, params, o = _run(oracle, fvgs_lib, quirks, n=50_000, scale=1.0, seed=23)
+    n_g = g["delta2d"][:, 12]
+    n_o = o.delta2d[:, 12]
+    same = n_g == n_o
+    assert same.mean() > 0.99, same.mean()
+    assert (n_o > 0).sum() > 10_000
+    err_c = np.abs(g["color"] - o.color.reshape(H, W, 3)) / np.maximum(np.abs(o.color.reshape(H, W, 3)), 1e-3)
+    assert np.mean(err_c <= 1e-5) > 0.999
+    for name, cols in GROUPS_2D.items():
+        e = rel_err(g["delta2d"][same][:, cols], o.delta2d[same][:, cols])
+        print("delta2d", name, e)
+        assert e <= GRAD_RTOL, (name, e)
+    for name, cols in GROUPS_3D.items():
+        e = rel_err(g["delta3d"][same][:, cols], o.delta3d[same][:, cols])
+        print("delta3d", name, e)
+        assert e <= GRAD_RTOL, (name, e)

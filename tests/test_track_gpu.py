@@ -214,3 +214,64 @@ def test_pyramid_frame_eager_graph_and_batched_agree(oracle, fvgs_lib):
         np.testing.assert_array_equal(p[1], a[1])
     for s in sessions:
         s.close()
+
+
+def _tiles_to_world(tiles, q):
+    """Camera-frame tile partials (translation rows without R) to the world
+    frame the oracle reports: b = (R b_t, b_r), A = D A D^T, D = diag(R, I)."""
+    R = S.qrot(np.asarray(q, np.float64))
+    D = np.eye(6)
+    D[:3, :3] = R
+    iu = np.triu_indices(6)
+    out = np.zeros_like(tiles, dtype=np.float64)
+    for t in range(tiles.shape[0]):
+        A = np.zeros((6, 6))
+        A[iu] = tiles[t, 6:]
+        A = A + A.T - np.diag(np.diag(A))
+        Aw = D @ A @ D.T
+        out[t, :6] = D @ tiles[t, :6]
+        out[t, 6:] = Aw[iu]
+    return out
+
+
+@pytest.mark.parametrize("quirks", [REF, INTENDED], ids=["ref", "analytic"])
+def test_track_tiles_room_1m_hd(oracle, fvgs_lib, quirks):
+    """The large plain-method workload (N = 1 M room, 1280 x 720): per-tile
+    partials of 200 tiles spread over the frame against the oracle, after a
+    full binning and after an incremental one (the second evaluation, at a
+    pose one Gauss-Newton-sized step away, continues the first binning)."""
+    fv = fvgs_lib
+    cam = S.CAM_HD
+    W, H, K = cam.width, cam.height, cam.intrinsics
+    scene = S.room(1_000_000, seed=0)
+    traj = S.trajectory(2, seed=3)
+    true_pose = traj[1]
+    rng = np.random.default_rng(5)
+    pose_a = S.perturb(true_pose, 0.05, 0.1, rng)
+    pose_b = S.perturb(pose_a, 0.01, 0.02, rng)
+    P = oracle.default_params(quirks)
+    T = ((W + 15) // 16) * ((H + 15) // 16)
+    sel = np.arange(0, T, T // 200)[:200]
+    with fv.Session(scene.n, W, H, fv.default_params(quirks)) as s:
+        s.upload(scene)
+        col, dep, _, _ = s.render(true_pose, K, W, H)
+        rgb, d = S.add_noise(col, dep, rng)
+        gx, gy = S.sobel3(rgb)
+        s.set_frame(0, rgb, d, gx, gy)
+        got = {}
+        for name, pose in (("full", pose_a), ("incremental", pose_b)):
+            s.track_jacobian(pose, K, 0)
+            got[name] = (pose, s.download_tile_partials(T), s.binning_info()["incremental"])
+    assert not got["full"][2] and got["incremental"][2]
+    for name, (pose, tiles_gpu, _) in got.items():
+        b = oracle.prepare(scene, pose, K, W, H, P)
+        r = oracle.track(b, (rgb, d, gx, gy), pose, K, W, H, P, images=False, tiles=sel)
+        g = _tiles_to_world(tiles_gpu[sel].astype(np.float64), pose[1])
+        o = r.tiles[sel]
+        e_sum_jtj = rel_err(g[:, 6:].sum(0), o[:, 6:].sum(0))
+        e_sum_jtr = rel_err(g[:, :6].sum(0), o[:, :6].sum(0))
+        per = np.array([rel_err(g[t], o[t]) for t in range(len(sel)) if np.linalg.norm(o[t]) > 0])
+        print(name, "sum JtJ rel %.2e Jtr rel %.2e, tiles within 1e-4: %.3f (%d)" %
+              (e_sum_jtj, e_sum_jtr, np.mean(per <= 1e-4), per.size))
+        assert e_sum_jtj <= JAC_RTOL and e_sum_jtr <= JAC_RTOL, (name, e_sum_jtj, e_sum_jtr)
+        assert per.size > 150 and np.mean(per <= 1e-4) > 0.97, (name, np.sort(per)[-5:])
