@@ -9,8 +9,12 @@ loop of GSSlam::optimizeWithCeres: 6 + 6 + 4 + 4 = 20 Gauss-Newton
 iterations from level 3 down to level 0 (intrinsics scaled by 2^-level).
 The observed frame of every level is rendered at the true pose at that
 level's resolution, plus N(0,0.01) colour and N(0,0.005 m) depth noise
-(synthetic data; the reference names no dataset).  The pose error criterion
-is 1e-4 rad and 1e-4 m after the 20 iterations.
+(synthetic data; the reference names no dataset).  Where mapping steps
+change a map (the serving and large plain workloads), the frames a request
+tracks are rendered from the map as it stands at that request (replayed
+outside the timed region), so the observations follow the map the tracker
+sees.  The pose error criterion is 1e-4 rad and 1e-4 m after the 20
+iterations.
 
 Serving workload (the `value`): sessions, each its own map of N Gaussians
 (log-uniform in [100k, 3M], room scenes), 640x480 or 1280x720 frames (fx =
@@ -167,6 +171,19 @@ def set_pyramid(fvgs, sess, pyr, W, H):
         set_frame_tensors(fvgs, sess, lv, pyr[lv], w, h)
 
 
+def packed_levels(packed, W, H):
+    """Per-level views {rgb, depth, gx, gy} of a pack_pyramid buffer (level 0 first)."""
+    out, off = [], 0
+    for w, h in level_dims(W, H):
+        P = w * h
+        lv = {}
+        for k, n in (("rgb", 3 * P), ("depth", P), ("gx", 3 * P), ("gy", 3 * P)):
+            lv[k] = packed[off:off + n]
+            off += n
+        out.append(lv)
+    return out
+
+
 def err_stats(errs):
     """Pose errors (rad, m) of a form: medians, maxima and the share within the criterion."""
     a = np.array(errs, np.float64).reshape(-1, 2)
@@ -175,18 +192,36 @@ def err_stats(errs):
             "within_1e-4": float(np.mean((a[:, 0] <= POSE_TOL) & (a[:, 1] <= POSE_TOL))), "frames": int(a.shape[0])}
 
 
-def make_workload(S, sess, n_frames, seed):
+def make_workload(fvgs, S, torch, dev, sess, n_frames, seed, map_eta=None, world=None):
     """Frames of a random-walk trajectory through the room (1280x720): frame k
-    is observed at pose k + 1 and starts from its predicted pose."""
+    is observed at pose k + 1 and starts from its predicted pose.  With
+    map_eta, every frame is followed by a mapping step at its tracked pose,
+    and frame k is rendered from the map as the k mapping steps before it
+    left it (the session is reset to `world` first and at the end): the
+    observations follow the map the tracker sees, so the pose error measures
+    the tracking and not the drift of the mapping objective on a map that is
+    already the world.  Frames are on the device ("dev") and in pinned host
+    memory ("host")."""
     cam = S.CAM_HD
     W, H, K = cam.width, cam.height, cam.intrinsics
     traj = S.trajectory(200, seed=seed)
     rng = np.random.default_rng(seed + 1)
+    if map_eta is not None:
+        sess.upload(world)
     frames = []
     for k in range(n_frames):
         true = traj[(k + 1) % len(traj)]
-        frames.append({"pyr": render_pyramid(S, sess, true, K, W, H, rng), "pose": true,
-                       "prev": S.perturb(true, PRED_DEG, PRED_CM, rng)})
+        pyr = render_pyramid(S, sess, true, K, W, H, rng)
+        f = {"pose": true, "prev": S.perturb(true, PRED_DEG, PRED_CM, rng), "dev": to_device(torch, dev, pyr),
+             "host": to_pinned(torch, pyr)}
+        frames.append(f)
+        if map_eta is not None:
+            set_pyramid(fvgs, sess, f["dev"], W, H)
+            pose, _ = sess.track_frame_pyramid(f["prev"], K, PYR)
+            sess.map_step(pose, K, map_eta)
+    if map_eta is not None:
+        sess.upload(world)
+    torch.cuda.synchronize()
     return W, H, K, frames
 
 
@@ -211,6 +246,10 @@ def serving_config(n_sessions):
             "initial_pose": "the predicted pose: the true pose perturbed by %.2f deg / %.1f mm (the reference seeds "
                             "each frame with the IMU prediction)" % (PRED_DEG, 10 * PRED_CM),
             "pose_error_criterion": "1e-4 rad and 1e-4 m after the 20 iterations",
+            "observed_frames": "rendered at the true poses (+ N(0,0.01) colour, N(0,0.005 m) depth noise) from "
+                               "the session's map as its mapping steps left it: round r tracks frame r mod %d of "
+                               "map epoch r // %d (epochs replayed outside the timed region)"
+                               % (SERVE_FRAMES, MAP_EVERY),
             "sessions": n_sessions}
 
 
@@ -577,11 +616,11 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     sess = fvgs.Session(args.n, 1280, 720, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    W, H, K, frames = make_workload(S, sess, n_frames, seed=17 * rank)
+    # frame k is rendered from the map after the k mapping steps before it
+    W, H, K, frames = make_workload(fvgs, S, torch, dev, sess, n_frames, seed=17 * rank, map_eta=ETA, world=scene)
     # device-resident frames for the `value` leg, pinned host frames for e2e
-    dframes = [to_device(torch, dev, f["pyr"]) for f in frames]
-    hframes = [to_pinned(torch, f["pyr"]) for f in frames]
-    torch.cuda.synchronize()
+    dframes = [f["dev"] for f in frames]
+    hframes = [f["host"] for f in frames]
 
     def step(k, src):
         set_pyramid(fvgs, sess, src[k % len(src)], W, H)
@@ -589,14 +628,20 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         sess.map_step(pose, K, ETA)
         return pose
 
+    def rewind():
+        """The map as it stands before frame `warmup`: the world again, then
+        the warm-up frames with their mapping steps (untimed)."""
+        sess.upload(scene)
+        for k in range(args.warmup):
+            step(k, dframes)
+        torch.cuda.synchronize()
+
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
     # warm-up (also grows the instance buffers to the workload's size)
-    for k in range(args.warmup):
-        step(k, dframes)
-    torch.cuda.synchronize()
+    rewind()
     # per-kernel-class CUDA-event times for the roofline and the shares, from
     # separate untimed frames (the events would otherwise sit in the timed region)
     sess.set_timing(fvgs.KERNEL_CLASSES)
@@ -606,6 +651,8 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     torch.cuda.synchronize()
     timing = sess.get_timing(reset=True)
     sess.set_timing(())
+    rewind()
+    sess.get_timing(reset=True)
 
     barrier()
     torch.cuda.synchronize()
@@ -627,8 +674,8 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     lat = sorted(a.elapsed_time(b) for a, b in step_ev)
     timed_launches = sess.get_timing(reset=True)
 
-    # e2e leg: pinned host frames through the C-ABI
-    torch.cuda.synchronize()
+    # e2e leg: pinned host frames through the C-ABI, from the same map state
+    rewind()
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -738,7 +785,7 @@ def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
     removed = sess.prune()
     out["prune_compact"] = {"call_ms": 1000.0 * (time.perf_counter() - t0), "removed": removed}
     if with_cpu:
-        out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["pyr"][0]["depth"])
+        out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["host"][0]["depth"].numpy())
     return out
 
 
@@ -773,9 +820,8 @@ def run_precision(args, fvgs, S, torch, dev, stream, world):
     sess = fvgs.Session(n, 1280, 720, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    W, H, K, frames = make_workload(S, sess, args.warmup + args.steps, seed=29)
-    dframes = [to_device(torch, dev, f["pyr"]) for f in frames]
-    torch.cuda.synchronize()
+    W, H, K, frames = make_workload(fvgs, S, torch, dev, sess, args.warmup + args.steps, seed=29)
+    dframes = [f["dev"] for f in frames]
     out, poses = {}, {}
     for name, prec in (("fp32", fvgs.PRECISION_FP32), ("reduced", fvgs.PRECISION_REDUCED)):
         sess.set_precision(prec)
@@ -942,39 +988,88 @@ def run_batching(args, fvgs, S, torch, dev, world):
 
 
 def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session):
-    """Sessions of the serving configuration (serving_sessions): each with a
-    short random-walk trajectory, its frames' four-level pyramids rendered at
-    the true poses (+ noise) in HBM and packed in pinned host memory, and
-    each frame's predicted start pose."""
-    rng = np.random.default_rng(SERVE_SEED)
+    """Sessions of the serving configuration (serving_sessions): each with its
+    world map, a short random-walk trajectory and the observed frames of its
+    first map epoch (serving_epochs)."""
     out = []
     for spec in serving_sessions(n_sessions):
         cam = spec["cam"]
         W, H, K = cam.width, cam.height, cam.intrinsics
         sess = fvgs.Session(spec["n"], W, H, fvgs.default_params(QUIRKS), device=dev.index or 0)
-        sess.upload(S.room(spec["n"], seed=spec["map_seed"]))
-        traj = S.trajectory(frames_per_session + 1, seed=spec["traj_seed"])
-        frames = []
-        for k in range(frames_per_session):
-            pyr = render_pyramid(S, sess, traj[k + 1], K, W, H, rng)
-            packed = torch.from_numpy(fvgs.pack_pyramid([(lv["rgb"], lv["depth"], lv["gx"], lv["gy"]) for lv in pyr]))
-            frames.append({"pose": traj[k + 1], "prev": S.perturb(traj[k + 1], PRED_DEG, PRED_CM, rng),
-                           "dev": to_device(torch, dev, pyr),
-                           "packed": packed.pin_memory(), "packed_dev": packed.to(dev),
-                           "packed_bytes": int(packed.numel() * 4)})
-        out.append({"sess": sess, "W": W, "H": H, "K": K, "n": spec["n"], "frames": frames})
-    torch.cuda.synchronize()
+        world = S.room(spec["n"], seed=spec["map_seed"])
+        sess.upload(world)
+        out.append({"sess": sess, "world": world, "W": W, "H": H, "K": K, "n": spec["n"],
+                    "traj": S.trajectory(frames_per_session + 1, seed=spec["traj_seed"]),
+                    "seed": spec["traj_seed"], "epochs": []})
+    serving_epochs(fvgs, S, torch, dev, out, 1)
     return out
 
 
+def serving_epochs(fvgs, S, torch, dev, ws, n_epochs):
+    """Observed frames of every session's map epochs 0..n_epochs-1.  Round r
+    of a session tracks frame r mod F of epoch r // MAP_EVERY, and the
+    request of round r = MAP_EVERY e + MAP_EVERY - 1 ends with a mapping step
+    at its tracked pose, which starts epoch e + 1.  Frames of epoch e are
+    rendered (+ noise) at the true poses from the map as epoch e's requests
+    find it, obtained here by replaying the mapping requests of the epochs
+    before (untimed), so the observations follow the map the tracker sees;
+    rendered from the untouched world instead, the frames after a mapping
+    step would measure how far the mapping objective (photometric, depth,
+    distortion and isotropy terms, Adam) moves a map that already is the
+    world.  Each frame's four levels are packed in one buffer in HBM and one
+    in pinned host memory.  Sessions end reset to their world."""
+    for w in ws:
+        if len(w["epochs"]) >= n_epochs:
+            continue
+        sess, W, H, K = w["sess"], w["W"], w["H"], w["K"]
+        F = len(w["traj"]) - 1
+        sess.upload(w["world"])
+        for e in range(n_epochs):
+            if e == len(w["epochs"]):
+                rng = np.random.default_rng([w["seed"], e])
+                frames = []
+                for k in range(F):
+                    true = w["traj"][k + 1]
+                    pyr = render_pyramid(S, sess, true, K, W, H, rng)
+                    packed = torch.from_numpy(fvgs.pack_pyramid([(lv["rgb"], lv["depth"], lv["gx"], lv["gy"])
+                                                                 for lv in pyr]))
+                    frames.append({"pose": true, "prev": S.perturb(true, PRED_DEG, PRED_CM, rng), "epoch": e,
+                                   "packed": packed.pin_memory(), "packed_dev": packed.to(dev),
+                                   "packed_bytes": int(packed.numel() * 4)})
+                w["epochs"].append(frames)
+            if e + 1 < n_epochs:
+                f = w["epochs"][e][(MAP_EVERY * e + MAP_EVERY - 1) % F]
+                set_pyramid(fvgs, sess, packed_levels(f["packed_dev"], W, H), W, H)
+                pose, _ = sess.track_frame_pyramid(f["prev"], K, PYR)
+                sess.map_step(pose, K, ETA)
+        sess.upload(w["world"])
+    torch.cuda.synchronize()
+
+
+def serving_reset(fvgs, ws):
+    """Every session back to its world map (parameters as generated, Adam
+    state zero), then two tracking-only frames of epoch 0 through the
+    asynchronous frame path (untimed): they rebuild the binning history, so
+    the next frames replay their captured graphs."""
+    for w in ws:
+        w["sess"].upload(w["world"])
+    for j in range(2):
+        for w in ws:
+            f = w["epochs"][0][j % len(w["epochs"][0])]
+            set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
+            w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR)
+        for w in ws:
+            w["sess"].frame_wait()
+
+
 def serving_requests(ws, rounds, start_round):
-    """Round r holds one request per session: frame r mod F of the session,
-    a mapping step on every MAP_EVERY-th round."""
+    """Round r holds one request per session: frame r mod F of the session's
+    map epoch r // MAP_EVERY, a mapping step on every MAP_EVERY-th round."""
     reqs = []
     for r in range(start_round, start_round + rounds):
         for i, w in enumerate(ws):
-            f = w["frames"][r % len(w["frames"])]
-            reqs.append((i, r, f, ETA if r % MAP_EVERY == MAP_EVERY - 1 else None))
+            fr = w["epochs"][r // MAP_EVERY]
+            reqs.append((i, r, fr[r % len(fr)], ETA if r % MAP_EVERY == MAP_EVERY - 1 else None))
     return reqs
 
 
@@ -985,26 +1080,29 @@ def run_serving(args, fvgs, S, torch, dev):
     captured graphs).  Returns frames/s and pose error of both, the server's
     latency under Poisson arrivals, e2e with host frames, kernel launches."""
     ws = make_serving_workload(fvgs, S, torch, dev, args.sessions, SERVE_FRAMES)
+    rounds = max(1, args.steps)
+    serving_epochs(fvgs, S, torch, dev, ws, (rounds - 1) // MAP_EVERY + 1)
     total_bytes = sum(w["sess"].footprint() for w in ws)
     # warm-up: every session runs plain, plain, map, plain, plain, map, plain
     # frames (captures both frame shapes at both buffer parities)
     warm = [None, None, ETA, None, None, ETA, None][:max(1, args.warmup + 4)]
     for w in ws:
         for j, eta in enumerate(warm):
-            f = w["frames"][j % len(w["frames"])]
-            set_pyramid(fvgs, w["sess"], f["dev"], w["W"], w["H"])
+            f = w["epochs"][0][j % SERVE_FRAMES]
+            set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
             w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR, map_eta=eta)
             w["sess"].frame_wait()
     torch.cuda.synchronize()
-    rounds = max(1, args.steps)
     reqs = serving_requests(ws, rounds, 0)
 
     # (a) plain per-frame path: one request after the other
+    serving_reset(fvgs, ws)
+    torch.cuda.synchronize()
     plain_errs = []
     t0 = time.perf_counter()
     for i, r, f, eta in reqs:
         w = ws[i]
-        set_pyramid(fvgs, w["sess"], f["dev"], w["W"], w["H"])
+        set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
         pose, _ = w["sess"].track_frame_pyramid(f["prev"], w["K"], PYR)
         if eta is not None:
             w["sess"].map_step(pose, w["K"], eta)
@@ -1013,6 +1111,7 @@ def run_serving(args, fvgs, S, torch, dev):
     plain_s = time.perf_counter() - t0
 
     def served(frames_key, reqs_, arrivals=None):
+        serving_reset(fvgs, ws)
         for w in ws:
             w["sess"].get_timing(reset=True)
         with fvgs.Server(memory_budget_bytes=SERVE_BUDGET, max_inflight=args.sessions) as sv:
@@ -1065,10 +1164,12 @@ def run_serving(args, fvgs, S, torch, dev):
             t += rng.exponential(1.0 / hz)
             if t > SERVE_SECONDS and r > 0:  # at least one request per session
                 break
-            f = w["frames"][r % len(w["frames"])]
-            preqs.append((i, r, f, ETA if r % MAP_EVERY == MAP_EVERY - 1 else None))
+            preqs.append((i, r, None, ETA if r % MAP_EVERY == MAP_EVERY - 1 else None))
             arrivals.append(t)
             r += 1
+    # every session's Poisson requests track the frames of their map epochs
+    serving_epochs(fvgs, S, torch, dev, ws, max(q[1] for q in preqs) // MAP_EVERY + 1)
+    preqs = [(i, r, ws[i]["epochs"][r // MAP_EVERY][r % SERVE_FRAMES], eta) for i, r, _, eta in preqs]
     poi = served("dev", preqs, arrivals)
     out = {
         "sessions": len(ws), "footprint_gb": total_bytes / 1e9,
@@ -1077,7 +1178,8 @@ def run_serving(args, fvgs, S, torch, dev):
         "served_frames_per_s": sat["frames_per_s"], "served_span_s": sat["span_s"],
         "plain_frames_per_s": len(reqs) / plain_s, "plain_span_s": plain_s,
         "e2e_frames_per_s": e2e["frames_per_s"],
-        "h2d_bytes_per_round": int(sum(w["frames"][0]["packed_bytes"] for w in ws)),
+        "h2d_bytes_per_round": int(sum(w["epochs"][0][0]["packed_bytes"] for w in ws)),
+        "map_epochs": len(ws[0]["epochs"]),
         "d2h_bytes_per_round": 160 * len(ws),
         "launches": sat["launches"], "clocks": clk,
         "pose_error": {"plain": err_stats(plain_errs), "served": err_stats(sat["errs"]),
