@@ -917,11 +917,18 @@ def run_visual_inertial(args, fvgs, S, torch, dev, stream, world, sess, K, W, H)
 
 def run_batching(args, fvgs, S, torch, dev, world):
     """The batching workload: 64 keyframes (sessions) with maps of N
-    log-uniform in [20k, 2M], 640x480 and 1280x720 alternately; one step =
-    one coarse-to-fine tracking frame (20 GN iterations) of every keyframe,
-    either as 64 sequential plain frames (fvgs_track_frame_pyramid) or as one
-    fvgs_frames_run_pyramid call (all frames in flight together, each replayed
-    from its captured graph)."""
+    log-uniform in [20k, 2M], 640x480 and 1280x720 alternately, each starting
+    from a pose 1 deg / 2 cm from its own; one step = one coarse-to-fine
+    tracking frame (20 GN iterations) of every keyframe, as
+     * batched: one fvgs_batch_run_pyramid call -- every iteration bins all
+       keyframes concurrently, then ONE persistent launch runs the tiles of
+       all 64 (tile shape and staging batch per level chosen by the batch
+       autotuner), then one launch reduces and steps every pose; the whole
+       frame replayed from one captured CUDA graph;
+     * sequential: 64 plain frames (fvgs_track_frame_pyramid) one after the
+       other, with the same tile shapes (results bit-identical);
+     * streams: one fvgs_frames_run_pyramid call (each keyframe's frame from
+       its own captured graph on its own stream)."""
     rng = np.random.default_rng(41)
     ns = np.exp(rng.uniform(np.log(BATCH_N_MIN), np.log(BATCH_N_MAX), args.batch_sessions)).astype(int)
     ws = []
@@ -933,7 +940,7 @@ def run_batching(args, fvgs, S, torch, dev, world):
         traj = S.trajectory(3, seed=6000 + i)
         frames = []
         for k in range(2):
-            frames.append({"prev": S.perturb(traj[k + 1], PRED_DEG, PRED_CM, rng), "pose": traj[k + 1],
+            frames.append({"prev": S.perturb(traj[k + 1], 1.0, 2.0, rng), "pose": traj[k + 1],
                            "dev": to_device(torch, dev, render_pyramid(S, sess, traj[k + 1], K, W, H, rng))})
         ws.append({"sess": sess, "W": W, "H": H, "K": K, "frames": frames})
     torch.cuda.synchronize()
@@ -942,7 +949,15 @@ def run_batching(args, fvgs, S, torch, dev, world):
         for w in ws:
             set_pyramid(fvgs, w["sess"], w["frames"][k % 2]["dev"], w["W"], w["H"])
 
+    bt = fvgs.Batch([w["sess"] for w in ws])
+    load(0)
+    tuned, tuned_ms = bt.autotune([w["frames"][0]["prev"] for w in ws], [w["K"] for w in ws], PYR, reps=3)
+
     def batched(k):
+        load(k)
+        return bt.run_pyramid([w["frames"][k % 2]["prev"] for w in ws], [w["K"] for w in ws], PYR)
+
+    def streams(k):
         load(k)
         return fvgs.frames_run_pyramid([w["sess"] for w in ws], [w["frames"][k % 2]["prev"] for w in ws],
                                        [w["K"] for w in ws], PYR)
@@ -956,35 +971,49 @@ def run_batching(args, fvgs, S, torch, dev, world):
 
     for k in range(max(4, args.warmup + 1)):  # both buffer parities of both frames captured
         batched(k)
+        streams(k)
     sequential(0)
     steps = max(1, args.steps)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(steps):
-        seq = sequential(k)
-    torch.cuda.synchronize()
-    seq_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for k in range(steps):
-        bat = batched(k)
-    torch.cuda.synchronize()
-    bat_s = time.perf_counter() - t0
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            res = fn(k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, res
+
+    seq_s, seq = timed(sequential)
+    bat_s, bat = timed(batched)
+    str_s, strm = timed(streams)
     same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(seq, bat))
+    same_streams = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(seq, strm))
     k_last = steps - 1
     errs = [S.pose_error(p, w["frames"][k_last % 2]["pose"]) for p, w in zip(bat, ws)]
-    graphed = sum(w["sess"].frame_stats()["graphed"] for w in ws)
+    st = bt.stats()
+    bt.close()
     for w in ws:
         w["sess"].close()
-    seq_s, bat_s = max_over_ranks([seq_s, bat_s], dev, world)
+    seq_s, bat_s, str_s = max_over_ranks([seq_s, bat_s, str_s], dev, world)
     n = steps * len(ws)
+    levels = {"level%d" % l: {"tile": "%dx%d" % c[:2], "smem_batch": c[2],
+                              "ms_per_launch": {"%dx%d" % sh: {str(bb): round(float(tuned_ms[l][i][j]), 4)
+                                                              for j, bb in enumerate(fvgs.STAGE_BATCHES)}
+                                                for i, sh in enumerate(fvgs.TILE_SHAPES)}}
+              for l, c in sorted(tuned.items())}
     return {"workload": "%d keyframes, N log-uniform in [20k, 2M] (%d Gaussians in total), 640x480 / 1280x720, "
-                        "20 GN iterations coarse-to-fine per frame; one step = one frame of every keyframe"
-                        % (len(ws), int(ns.sum())),
+                        "each from a pose 1 deg / 2 cm away; 20 GN iterations coarse-to-fine per frame; one step = "
+                        "one frame of every keyframe" % (len(ws), int(ns.sum())),
             "batched_frames_per_s": world * n / bat_s, "sequential_frames_per_s": world * n / seq_s,
+            "streams_frames_per_s": world * n / str_s,
             "speedup_batched_over_sequential": seq_s / bat_s, "poses_identical": bool(same),
-            "pose_error": err_stats(errs), "graphed_frames": graphed,
-            "form": "fvgs_frames_run_pyramid: every keyframe's frame on its own stream from its captured graph, "
-                    "against fvgs_track_frame_pyramid one keyframe after the other"}
+            "streams_poses_identical": bool(same_streams),
+            "pose_error": err_stats(errs), "batch_stats": st, "autotuned": levels,
+            "form": "fvgs_batch_run_pyramid: per Gauss-Newton iteration every keyframe binned concurrently, ONE "
+                    "persistent launch over the (keyframe, tile) work list, one batched reduction + pose step; the "
+                    "frame replayed from one CUDA graph; against fvgs_track_frame_pyramid one keyframe after the "
+                    "other (same tile shapes) and fvgs_frames_run_pyramid (per-keyframe graphs on separate streams)"}
 
 
 def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session):

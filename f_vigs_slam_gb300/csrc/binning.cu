@@ -365,7 +365,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_final_kernel(const uint32_t
 // Key emission: a warp takes 32 consecutive Gaussians, whose instances are
 // contiguous in the output, and walks their concatenated tile lists 32 at a
 // time.  Each lane finds its owning Gaussian by a 5-step shuffle search.
-// key = tile << 32 | bits(fmaf(phy, dy, fmaf(phx, dx, z))), dx = tile centre - u.
+// key = tile << 32 | bits(fmaf(phx, dx, z) + phy * dy), dx = tile centre - u
+// (tile_depth).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) emit_keys_kernel(EmitArgs a) {
     const int gbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
@@ -417,11 +418,7 @@ __global__ void __launch_bounds__(256) emit_keys_kernel(EmitArgs a) {
             const int w = x1 - x0 + 1;
             const int tx = x0 + (int)(local % (uint32_t)w);
             const int ty = y0 + (int)(local / (uint32_t)w);
-            const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)a.tw);
-            const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)a.th);
-            const float dx = __fsub_rn(tcx, u);
-            const float dy = __fsub_rn(tcy, v);
-            const float d = __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+            const float d = tile_depth(tx, ty, a.tw, a.th, u, v, z, phx, phy_bits);
             const uint32_t tile = (uint32_t)(ty * a.ntx + tx);
             const uint64_t dst = (uint64_t)warp_off + m;
             if (dst < cap) {

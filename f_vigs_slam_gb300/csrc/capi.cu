@@ -10,6 +10,7 @@
 // estimate and grow when the device reports an overflow; the affected call is
 // then re-run, so results never depend on the capacity.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -35,6 +36,8 @@ struct FrameLevel {
     // frames of tuned_w x tuned_h (0 until tuned)
     int track_variant = 0, tuned_w = 0, tuned_h = 0;
     float tuned_ms[kTrackVariants] = {};
+    // tile shape of this level's tracking binnings (16 x 16, 8 x 8 or 32 x 8)
+    int tile_w = 16, tile_h = 16;
     float* rgb = nullptr;
     float* depth = nullptr;
     float* gx = nullptr;
@@ -126,7 +129,8 @@ struct fvgs_session {
     uint32_t* vals = nullptr;
     SortWorkspace sort{};
 
-    int cap_tiles = 0;
+    int cap_tiles = 0;    // tiles of the largest frame at the smallest tracking tile (8 x 8)
+    int cap_tiles16 = 0;  // tiles of the largest frame at 16 x 16 (mapping)
     uint2* ranges = nullptr;
     uint2* ranges_prev = nullptr;  // swapped with ranges per binning (vals with sort.vals_alt)
     float* tile_out = nullptr;
@@ -143,7 +147,8 @@ struct fvgs_session {
     uint32_t enter_cap = 0;
     bool hist_ok = false;  // the last binning left valid (bins, counts, ranges, vals) for the next one
     bool keys_valid = false;  // keys[] holds the last binning's reference-format keys
-    int hist_ntx = 0, hist_nty = 0;
+    int hist_ntx = 0, hist_nty = 0, hist_tw = 0, hist_th = 0;
+    int bin_tw = 16, bin_th = 16;  // tile shape of the last binning
 
     FrameLevel lv[kMaxLevels];
     // frame preprocessing: 8-bit colour pyramid and the raw depth of a frame
@@ -454,17 +459,19 @@ void collect_timing(fvgs_session* s) {
 }
 
 // Enqueue binning for the pose already in s->pose.
-int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
+int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H, int tw, int th) {
     const fvgs_params& P = s->params;
-    const int ntx = (W + P.tile_w - 1) / P.tile_w;
-    const int nty = (H + P.tile_h - 1) / P.tile_h;
+    if (!track_tile_supported(tw, th)) return FVGS_E_INVALID;
+    const int ntx = (W + tw - 1) / tw;
+    const int nty = (H + th - 1) / th;
     const int T = ntx * nty;
     const bool radix = (s->debug & FVGS_DEBUG_RADIX_SORT) != 0;
     // Incremental binning needs the previous binning of the same Gaussians on
     // the same tile grid, with true per-tile ranges (not the reference's
     // culled-slot or range-launch behaviours).
     const bool literal = (s->params.quirks & (FVGS_Q_CULLED_SLOTS | FVGS_Q_RANGE_LAUNCH)) != 0;
-    const bool hist = !radix && !literal && s->hist_ok && s->hist_ntx == ntx && s->hist_nty == nty;
+    const bool hist = !radix && !literal && s->hist_ok && s->hist_ntx == ntx && s->hist_nty == nty &&
+                      s->hist_tw == tw && s->hist_th == th;
     s->hist_ok = false;  // until this binning is fully enqueued
     if (!radix) {
         std::swap(s->ranges, s->ranges_prev);
@@ -484,10 +491,10 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     pa.K = *K;
     pa.W = W;
     pa.H = H;
-    pa.tw = P.tile_w;
-    pa.th = P.tile_h;
-    pa.inv_tw = (P.tile_w > 0 && (P.tile_w & (P.tile_w - 1)) == 0) ? 1.0f / (float)P.tile_w : 0.0f;
-    pa.inv_th = (P.tile_h > 0 && (P.tile_h & (P.tile_h - 1)) == 0) ? 1.0f / (float)P.tile_h : 0.0f;
+    pa.tw = tw;
+    pa.th = th;
+    pa.inv_tw = (tw & (tw - 1)) == 0 ? 1.0f / (float)tw : 0.0f;
+    pa.inv_th = (th & (th - 1)) == 0 ? 1.0f / (float)th : 0.0f;
     pa.ntx = ntx;
     pa.nty = nty;
     pa.radius_sigma = P.radius_sigma;
@@ -524,8 +531,8 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     ea.offsets = s->offsets;
     ea.n = (int)s->n_g;
     ea.ntx = ntx;
-    ea.tw = P.tile_w;
-    ea.th = P.tile_h;
+    ea.tw = tw;
+    ea.th = th;
     ea.capacity = s->cap_inst;
     const uint32_t cap32 = (uint32_t)std::min<uint64_t>(s->cap_inst, 0xffffffffu);
     if (!radix) {
@@ -553,8 +560,8 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         inc.enter_keys = s->enter_keys;
         inc.bins = s->bins;
         inc.ntx = ntx;
-        inc.tw = P.tile_w;
-        inc.th = P.tile_h;
+        inc.tw = tw;
+        inc.th = th;
         inc.n_gauss = s->n_g;
         inc.capacity = s->cap_inst;
         {
@@ -566,7 +573,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
         if (P.quirks & FVGS_Q_RANGE_LAUNCH) {
             // the literal range pass reads the reference-format keys
             KScope k(s, FVGS_K_RANGES, 2);
-            FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, T, ntx, P.tile_w, P.tile_h, s->st, s->keys,
+            FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, T, ntx, tw, th, s->st, s->keys,
                                    s->stream));
             FV_CK(launch_ranges(s->keys, s->st, T, P.quirks, s->ranges, s->num_sms * 8, s->stream));
             s->keys_valid = true;
@@ -600,13 +607,16 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H) {
     s->hist_ok = !radix && !literal;
     s->hist_ntx = ntx;
     s->hist_nty = nty;
+    s->hist_tw = s->bin_tw = tw;
+    s->hist_th = s->bin_th = th;
     s->has_binning = true;
     s->dbg_proj_valid = (s->debug & FVGS_DEBUG_PROJECTION) != 0;
     return FVGS_OK;
 }
 
-int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
-                  bool images) {
+// Arguments of the tracking kernel on the binning just enqueued.
+TrackArgs make_track_args(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
+                          bool images) {
     const fvgs_params& P = s->params;
     TrackArgs ta{};
     ta.rec0 = s->rec0;
@@ -624,8 +634,11 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
     ta.K = *K;
     ta.W = f.W;
     ta.H = f.H;
-    ta.ntx = (f.W + P.tile_w - 1) / P.tile_w;
-    ta.nty = (f.H + P.tile_h - 1) / P.tile_h;
+    // the tile grid of the binning just enqueued
+    ta.tile_w = s->bin_tw;
+    ta.tile_h = s->bin_th;
+    ta.ntx = (f.W + s->bin_tw - 1) / s->bin_tw;
+    ta.nty = (f.H + s->bin_th - 1) / s->bin_th;
     ta.bg[0] = P.bg[0];
     ta.bg[1] = P.bg[1];
     ta.bg[2] = P.bg[2];
@@ -643,9 +656,20 @@ int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f
     ta.quirks = P.quirks;
     ta.geo0 = s->geo0;
     ta.geo1 = s->geo1;
+    // precision form: the analytic Jacobian's accumulations compensated (16 x 16 tiles)
+    ta.compensated = (s->precision == FVGS_PRECISION_REDUCED && !render_only &&
+                      !(P.quirks & FVGS_Q_POSE_JAC_APPROX) && ta.tile_w == 16 && ta.tile_h == 16)
+                         ? 1
+                         : 0;
     ta.variant = (f.tuned_w == f.W && f.tuned_h == f.H) ? f.track_variant : 0;
     if (ta.variant == 2 && !s->rec_maps_ok) ta.variant = 0;
     ta.st_flags = &s->st->flags;
+    return ta;
+}
+
+int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
+                  bool images) {
+    const TrackArgs ta = make_track_args(s, K, f, render_only, images);
     KScope k(s, render_only ? FVGS_K_RENDER : FVGS_K_TRACK, 1);
     FV_CK(launch_track(ta, s->rec_maps_ok ? &s->rec_maps : nullptr, s->stream));
     return FVGS_OK;
@@ -701,8 +725,8 @@ int ensure_map_buffers(fvgs_session* s, size_t px, bool cap) {
     }
     // checkpoint slots: 8 per tile with MAP_CAP256, else one per 32 instances
     // of every tile (bounded by capacity/32 + tiles)
-    const size_t slots = cap ? (size_t)s->cap_tiles * map_cap_buckets()
-                             : (size_t)(s->cap_inst / 32 + 1) + (size_t)s->cap_tiles;
+    const size_t slots = cap ? (size_t)s->cap_tiles16 * map_cap_buckets()
+                             : (size_t)(s->cap_inst / 32 + 1) + (size_t)s->cap_tiles16;
     if (slots > s->m_sampled_slots) {
         dev_free(s, s->m_sampled, s->m_sampled_slots * 256);
         FV_TRY(dev_alloc(s, &s->m_sampled, slots * 256));
@@ -860,6 +884,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
         return FVGS_E_INVALID;
     }
     FV_CK(cudaSetDevice(device));
+    FV_CK(track_configure_device());
     fvgs_session* s = new (std::nothrow) fvgs_session();
     if (!s) return FVGS_E_NOMEM;
     s->params = P;
@@ -894,8 +919,11 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
     FV_A(s->partials, scan_partials_size((int)N) + 1);
-    const int ntx = (max_width + P.tile_w - 1) / P.tile_w, nty = (max_height + P.tile_h - 1) / P.tile_h;
+    // tile-indexed buffers hold the largest frame at the smallest tracking
+    // tile (8 x 8); mapping runs on 16 x 16 tiles
+    const int ntx = (max_width + 7) / 8, nty = (max_height + 7) / 8;
     s->cap_tiles = ntx * nty;
+    s->cap_tiles16 = ((max_width + P.tile_w - 1) / P.tile_w) * ((max_height + P.tile_h - 1) / P.tile_h);
     FV_A(s->ranges, (size_t)s->cap_tiles);
     FV_A(s->ranges_prev, (size_t)s->cap_tiles);
     s->tile_diff_cells = tile_diff_words(ntx, nty);
@@ -1006,6 +1034,15 @@ int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int*
     if (incremental) *incremental = st.mode == kBinIncremental ? 1 : 0;
     if (n_entering) *n_entering = st.n_enter;
     if (n_changed) *n_changed = st.n_changed;
+    return FVGS_OK;
+}
+
+int fvgs_session_binning_grid(const fvgs_session* s, int* tile_w, int* tile_h, int* num_tiles) {
+    if (!s) return FVGS_E_INVALID;
+    if (!s->has_binning) return FVGS_E_STATE;
+    if (tile_w) *tile_w = s->bin_tw;
+    if (tile_h) *tile_h = s->bin_th;
+    if (num_tiles) *num_tiles = s->last_T;
     return FVGS_OK;
 }
 
@@ -1179,7 +1216,7 @@ int fvgs_project_bin(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsi
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, width, height));
+        FV_TRY(enqueue_bin(s, K, width, height, s->params.tile_w, s->params.tile_h));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
         collect_timing(s);
@@ -1238,9 +1275,9 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
     if (n_instances) *n_instances = n;
     if ((keys || values) && n > max_instances) return FVGS_E_CAPACITY;
     if (keys && n && !s->keys_valid) {
-        const int ntx = (s->last_W + s->params.tile_w - 1) / s->params.tile_w;
-        FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, s->last_T, ntx, s->params.tile_w,
-                               s->params.tile_h, s->st, s->keys, s->stream));
+        const int ntx = (s->last_W + s->bin_tw - 1) / s->bin_tw;
+        FV_CK(launch_make_keys(s->bins, s->ranges, s->vals, s->n_g, s->last_T, ntx, s->bin_tw,
+                               s->bin_th, s->st, s->keys, s->stream));
         s->keys_valid = true;
     }
     if (keys && n) FV_CK(cudaMemcpyAsync(keys, s->keys, sizeof(uint64_t) * n, cudaMemcpyDefault, s->stream));
@@ -1261,7 +1298,7 @@ int fvgs_track_jacobian(fvgs_session* s, const fvgs_pose* pose, const fvgs_intri
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H, f.tile_w, f.tile_h));
         FV_TRY(enqueue_track(s, K, f, false, images));
         {
             KScope k(s, FVGS_K_REDUCE, 1);
@@ -1320,7 +1357,7 @@ int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics
         if (attempt == 4) return FVGS_E_CAPACITY;
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H, f.tile_w, f.tile_h));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
         collect_timing(s);
@@ -1426,7 +1463,7 @@ int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
     for (int l = kMaxLevels - 1; l >= 0; --l) {
         const FrameLevel& f = s->lv[l];
         for (int it = 0; it < r.iters[l]; ++it) {
-            FV_TRY(enqueue_bin(s, &r.K[l], f.W, f.H));
+            FV_TRY(enqueue_bin(s, &r.K[l], f.W, f.H, f.tile_w, f.tile_h));
             FV_TRY(enqueue_track(s, &r.K[l], f, false, false));
             KScope k(s, FVGS_K_GN, 1);
             FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step,
@@ -1435,7 +1472,7 @@ int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
     }
     if (r.eta >= 0.f) {
         const FrameLevel& f = s->lv[r.map_level];
-        FV_TRY(enqueue_bin(s, &r.K[r.map_level], f.W, f.H));
+        FV_TRY(enqueue_bin(s, &r.K[r.map_level], f.W, f.H, s->params.tile_w, s->params.tile_h));
         FV_TRY(enqueue_map(s, &r.K[r.map_level], f, r.eta));
     }
     FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
@@ -1457,8 +1494,11 @@ bool entry_incremental(const fvgs_session* s, const fvgs_session::FrameRequest& 
     const int l0 = first_level(r);
     if (l0 < 0 || !s->hist_ok) return false;
     const FrameLevel& f = s->lv[l0];
-    return s->hist_ntx == (f.W + s->params.tile_w - 1) / s->params.tile_w &&
-           s->hist_nty == (f.H + s->params.tile_h - 1) / s->params.tile_h;
+    bool tracked = false;  // else the frame's first binning is the mapping step's
+    for (int l = 0; l < kMaxLevels; ++l) tracked = tracked || r.iters[l] > 0;
+    const int tw = tracked ? f.tile_w : s->params.tile_w, th = tracked ? f.tile_h : s->params.tile_h;
+    return s->hist_tw == tw && s->hist_th == th && s->hist_ntx == (f.W + tw - 1) / tw &&
+           s->hist_nty == (f.H + th - 1) / th;
 }
 
 bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
@@ -1824,6 +1864,615 @@ int fvgs_frames_run_pyramid(fvgs_session* const* sessions, fvgs_pose* poses, con
     });
 }
 
+int fvgs_session_set_track_tiles(fvgs_session* s, int level, int tile_w, int tile_h) {
+    if (!s || level < 0 || level >= kMaxLevels || !track_tile_supported(tile_w, tile_h)) return FVGS_E_INVALID;
+    FrameLevel& f = s->lv[level];
+    f.tile_w = tile_w;
+    f.tile_h = tile_h;
+    ++s->gen;  // captured frames bin on the previous grid
+    return FVGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batching form: the frames of many sessions in lockstep, each Gauss-Newton
+// iteration binning every session on its own stream and then blending and
+// differentiating the tiles of all of them in one persistent launch.
+// ---------------------------------------------------------------------------
+struct fvgs_batch {
+    std::vector<fvgs_session*> s;
+    int device = 0, num_sms = 0;
+    bool analytic = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    std::vector<cudaEvent_t> ev_join;
+    int tw[kMaxLevels], th[kMaxLevels], variant[kMaxLevels];
+    uint32_t* counters = nullptr;  // the persistent kernel's work counters
+    // job tables, one region per Gauss-Newton iteration: host (pinned)
+    // staging, the eager path's device copy and the captured frame's
+    int cap_iters = 0;
+    TrackJob* h_jobs = nullptr;
+    uint32_t* h_begin = nullptr;
+    ReduceJob* h_rjobs = nullptr;
+    TrackJob *d_jobs = nullptr, *g_jobs = nullptr;
+    uint32_t *d_begin = nullptr, *g_begin = nullptr;
+    ReduceJob *d_rjobs = nullptr, *g_rjobs = nullptr;
+    struct Exit {  // one session's key and the host-side binning state its captured frame leaves
+        uint64_t gen = 0;
+        uint32_t n_g = 0;
+        uint32_t* vals_in = nullptr;
+        uint2* ranges_in = nullptr;
+        bool entry_incremental = false;
+        int W[kMaxLevels] = {}, H[kMaxLevels] = {};
+        fvgs_intrinsics K[kMaxLevels] = {};
+        int ntx = 0, nty = 0, tw = 0, th = 0, last_W = 0, last_H = 0, last_T = 0;
+        uint32_t *vals = nullptr, *vals_alt = nullptr;
+        uint2 *ranges = nullptr, *ranges_prev = nullptr;
+        uint64_t launches[FVGS_K_COUNT] = {};
+    };
+    struct Graph {
+        bool valid = false;
+        int iters[kMaxLevels] = {};
+        int tw[kMaxLevels] = {}, th[kMaxLevels] = {}, variant[kMaxLevels] = {};
+        std::vector<Exit> exit;
+        uint64_t batch_launches = 0;
+        cudaGraphExec_t exec = nullptr;
+    } graph;
+    uint64_t graphed = 0, eager = 0, batch_launches = 0;
+};
+
+namespace {
+
+void batch_free_tables(fvgs_batch* b) {
+    if (b->h_jobs) cudaFreeHost(b->h_jobs);
+    if (b->h_begin) cudaFreeHost(b->h_begin);
+    if (b->h_rjobs) cudaFreeHost(b->h_rjobs);
+    for (void* p : {(void*)b->d_jobs, (void*)b->g_jobs, (void*)b->d_begin, (void*)b->g_begin, (void*)b->d_rjobs,
+                    (void*)b->g_rjobs})
+        if (p) cudaFree(p);
+    b->h_jobs = nullptr;
+    b->h_begin = nullptr;
+    b->h_rjobs = nullptr;
+    b->d_jobs = b->g_jobs = nullptr;
+    b->d_begin = b->g_begin = nullptr;
+    b->d_rjobs = b->g_rjobs = nullptr;
+    b->cap_iters = 0;
+}
+
+void batch_drop_graph(fvgs_batch* b) {
+    if (b->graph.exec) cudaGraphExecDestroy(b->graph.exec);
+    b->graph.exec = nullptr;
+    b->graph.valid = false;
+}
+
+int batch_ensure_tables(fvgs_batch* b, int iters) {
+    if (iters <= b->cap_iters) return FVGS_OK;
+    batch_drop_graph(b);
+    batch_free_tables(b);
+    const size_t n = b->s.size(), it = (size_t)iters;
+    if (cudaMallocHost(&b->h_jobs, sizeof(TrackJob) * n * it) != cudaSuccess ||
+        cudaMallocHost(&b->h_begin, sizeof(uint32_t) * (n + 1) * it) != cudaSuccess ||
+        cudaMallocHost(&b->h_rjobs, sizeof(ReduceJob) * n * it) != cudaSuccess ||
+        cudaMalloc(&b->d_jobs, sizeof(TrackJob) * n * it) != cudaSuccess ||
+        cudaMalloc(&b->g_jobs, sizeof(TrackJob) * n * it) != cudaSuccess ||
+        cudaMalloc(&b->d_begin, sizeof(uint32_t) * (n + 1) * it) != cudaSuccess ||
+        cudaMalloc(&b->g_begin, sizeof(uint32_t) * (n + 1) * it) != cudaSuccess ||
+        cudaMalloc(&b->d_rjobs, sizeof(ReduceJob) * n * it) != cudaSuccess ||
+        cudaMalloc(&b->g_rjobs, sizeof(ReduceJob) * n * it) != cudaSuccess) {
+        cudaGetLastError();
+        batch_free_tables(b);
+        return FVGS_E_NOMEM;
+    }
+    b->cap_iters = iters;
+    return FVGS_OK;
+}
+
+// Push a level's tile shape and staging batch to every session, so each one's
+// plain frames blend exactly as the batch does.
+void batch_apply_level(fvgs_batch* b, int l) {
+    for (fvgs_session* s : b->s) {
+        FrameLevel& f = s->lv[l];
+        f.tile_w = b->tw[l];
+        f.tile_h = b->th[l];
+        f.track_variant = b->variant[l];
+        f.tuned_w = f.W;
+        f.tuned_h = f.H;
+        ++s->gen;
+    }
+    batch_drop_graph(b);
+}
+
+// Fork the sessions' streams off the batch stream / join them back.
+int batch_fork(fvgs_batch* b) {
+    FV_CK(cudaEventRecord(b->ev_fork, b->stream));
+    for (fvgs_session* s : b->s) FV_CK(cudaStreamWaitEvent(s->stream, b->ev_fork, 0));
+    return FVGS_OK;
+}
+
+int batch_join(fvgs_batch* b) {
+    for (size_t i = 0; i < b->s.size(); ++i) {
+        FV_CK(cudaEventRecord(b->ev_join[i], b->s[i]->stream));
+        FV_CK(cudaStreamWaitEvent(b->stream, b->ev_join[i], 0));
+    }
+    return FVGS_OK;
+}
+
+// Bin every session at level l (pose already on the device) and fill job
+// table region `it`; returns the iteration's tile total in *total.
+int batch_bin_level(fvgs_batch* b, const Request* reqs, int l, int it, uint32_t* total) {
+    const size_t n = b->s.size();
+    uint32_t t = 0;
+    for (size_t i = 0; i < n; ++i) {
+        fvgs_session* s = b->s[i];
+        const FrameLevel& f = s->lv[l];
+        FV_TRY(enqueue_bin(s, &reqs[i].K[l], f.W, f.H, b->tw[l], b->th[l]));
+        TrackJob& j = b->h_jobs[(size_t)it * n + i];
+        j.a = make_track_args(s, &reqs[i].K[l], f, false, false);
+        j.a.variant = b->variant[l];
+        b->h_begin[(size_t)it * (n + 1) + i] = t;
+        t += (uint32_t)s->last_T;
+        ReduceJob& r = b->h_rjobs[(size_t)it * n + i];
+        r.tile_out = s->tile_out;
+        r.num_tiles = s->last_T;
+        r.pose = s->pose;
+        r.out = s->jj;
+        r.eig_eps = s->params.eig_eps;
+        r.step_out = s->step;
+    }
+    b->h_begin[(size_t)it * (n + 1) + n] = t;
+    *total = t;
+    return FVGS_OK;
+}
+
+// One batched frame: the sessions' start poses (their pinned h_pose) to the
+// device, the Gauss-Newton iterations of every level from the coarsest down,
+// then every session's pose, last step and status back to pinned memory.
+// Job tables: uploaded per iteration (eager) or read from the captured
+// frame's tables (capture: filled on the host, uploaded after the capture).
+int enqueue_batch_frame(fvgs_batch* b, const Request* reqs, bool capture) {
+    const size_t n = b->s.size();
+    TrackJob* jobs = capture ? b->g_jobs : b->d_jobs;
+    uint32_t* begin = capture ? b->g_begin : b->d_begin;
+    ReduceJob* rjobs = capture ? b->g_rjobs : b->d_rjobs;
+    FV_TRY(batch_fork(b));
+    for (fvgs_session* s : b->s) {
+        FV_TRY(reset_status(s));
+        FV_CK(cudaMemcpyAsync(s->d_pose_in, s->h_pose, sizeof(fvgs_pose), cudaMemcpyHostToDevice, s->stream));
+        FV_CK(launch_chained(set_pose_dev_kernel, dim3(1), dim3(1), 0, s->stream, s->pose,
+                             static_cast<const fvgs_pose*>(s->d_pose_in)));
+    }
+    int it = 0;
+    for (int l = kMaxLevels - 1; l >= 0; --l) {
+        for (int k = 0; k < reqs[0].iters[l]; ++k, ++it) {
+            uint32_t total = 0;
+            FV_TRY(batch_bin_level(b, reqs, l, it, &total));
+            FV_TRY(batch_join(b));
+            if (!capture) {
+                FV_CK(cudaMemcpyAsync(jobs + (size_t)it * n, b->h_jobs + (size_t)it * n, sizeof(TrackJob) * n,
+                                      cudaMemcpyHostToDevice, b->stream));
+                FV_CK(cudaMemcpyAsync(begin + (size_t)it * (n + 1), b->h_begin + (size_t)it * (n + 1),
+                                      sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, b->stream));
+                FV_CK(cudaMemcpyAsync(rjobs + (size_t)it * n, b->h_rjobs + (size_t)it * n, sizeof(ReduceJob) * n,
+                                      cudaMemcpyHostToDevice, b->stream));
+            }
+            FV_CK(launch_track_batch(jobs + (size_t)it * n, begin + (size_t)it * (n + 1), (int)n, total, b->tw[l],
+                                     b->th[l], b->analytic, b->variant[l], b->counters, b->num_sms, b->stream));
+            FV_CK(launch_track_reduce_batch(rjobs + (size_t)it * n, (int)n, b->stream));
+            b->batch_launches += 2;
+            FV_TRY(batch_fork(b));
+        }
+    }
+    for (fvgs_session* s : b->s) {
+        FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
+        FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+    }
+    return batch_join(b);
+}
+
+bool batch_key_matches(const fvgs_batch* b, const Request* reqs) {
+    const fvgs_batch::Graph& g = b->graph;
+    if (!g.valid) return false;
+    for (int l = 0; l < kMaxLevels; ++l)
+        if (g.iters[l] != reqs[0].iters[l] || g.tw[l] != b->tw[l] || g.th[l] != b->th[l] ||
+            g.variant[l] != b->variant[l])
+            return false;
+    for (size_t i = 0; i < b->s.size(); ++i) {
+        const fvgs_session* s = b->s[i];
+        const fvgs_batch::Exit& e = g.exit[i];
+        if (e.gen != s->gen || e.n_g != s->n_g || e.vals_in != s->vals || e.ranges_in != s->ranges ||
+            e.entry_incremental != entry_incremental(s, reqs[i]))
+            return false;
+        for (int l = 0; l < kMaxLevels; ++l) {
+            if (reqs[i].iters[l] == 0) continue;
+            const FrameLevel& f = s->lv[l];
+            if (e.W[l] != f.W || e.H[l] != f.H || e.K[l].fx != reqs[i].K[l].fx || e.K[l].fy != reqs[i].K[l].fy ||
+                e.K[l].cx != reqs[i].K[l].cx || e.K[l].cy != reqs[i].K[l].cy)
+                return false;
+        }
+    }
+    return true;
+}
+
+// Host-side binning state of a session (restored when a capture fails).
+struct HostBinState {
+    uint32_t *vals, *vals_alt;
+    uint2 *ranges, *ranges_prev;
+    bool hist, clean, keys, binned;
+    int ntx, nty, tw, th, btw, bth, lw, lh, lt;
+    uint64_t launches[FVGS_K_COUNT];
+    void save(const fvgs_session* s) {
+        vals = s->vals;
+        vals_alt = s->sort.vals_alt;
+        ranges = s->ranges;
+        ranges_prev = s->ranges_prev;
+        hist = s->hist_ok;
+        clean = s->diff_clean;
+        keys = s->keys_valid;
+        binned = s->has_binning;
+        ntx = s->hist_ntx;
+        nty = s->hist_nty;
+        tw = s->hist_tw;
+        th = s->hist_th;
+        btw = s->bin_tw;
+        bth = s->bin_th;
+        lw = s->last_W;
+        lh = s->last_H;
+        lt = s->last_T;
+        std::memcpy(launches, s->launches, sizeof(launches));
+    }
+    void restore(fvgs_session* s) const {
+        s->vals = vals;
+        s->sort.vals_alt = vals_alt;
+        s->ranges = ranges;
+        s->ranges_prev = ranges_prev;
+        s->hist_ok = hist;
+        s->diff_clean = clean;
+        s->keys_valid = keys;
+        s->has_binning = binned;
+        s->hist_ntx = ntx;
+        s->hist_nty = nty;
+        s->hist_tw = tw;
+        s->hist_th = th;
+        s->bin_tw = btw;
+        s->bin_th = bth;
+        s->last_W = lw;
+        s->last_H = lh;
+        s->last_T = lt;
+        std::memcpy(s->launches, launches, sizeof(launches));
+    }
+};
+
+// Launch the batched frame: replay the captured graph, or capture it, or
+// (when some session cannot run from a graph) enqueue it eagerly.
+int batch_launch(fvgs_batch* b, const Request* reqs) {
+    const size_t n = b->s.size();
+    bool graphable = true;
+    for (size_t i = 0; i < n; ++i) graphable = graphable && frame_graphable(b->s[i], reqs[i]);
+    if (!graphable) {
+        ++b->eager;
+        return enqueue_batch_frame(b, reqs, false);
+    }
+    if (batch_key_matches(b, reqs)) {
+        FV_CK(cudaGraphLaunch(b->graph.exec, b->stream));
+        for (size_t i = 0; i < n; ++i) {
+            fvgs_session* s = b->s[i];
+            const fvgs_batch::Exit& e = b->graph.exit[i];
+            s->vals = e.vals;
+            s->sort.vals_alt = e.vals_alt;
+            s->ranges = e.ranges;
+            s->ranges_prev = e.ranges_prev;
+            s->hist_ok = true;
+            s->hist_ntx = e.ntx;
+            s->hist_nty = e.nty;
+            s->hist_tw = s->bin_tw = e.tw;
+            s->hist_th = s->bin_th = e.th;
+            s->last_W = e.last_W;
+            s->last_H = e.last_H;
+            s->last_T = e.last_T;
+            s->keys_valid = false;
+            s->has_binning = true;
+            for (int c = 0; c < FVGS_K_COUNT; ++c) s->launches[c] += e.launches[c];
+        }
+        b->batch_launches += b->graph.batch_launches;
+        ++b->graphed;
+        return FVGS_OK;
+    }
+    batch_drop_graph(b);
+    std::vector<HostBinState> before(n);
+    std::vector<fvgs_batch::Exit> exit(n);
+    for (size_t i = 0; i < n; ++i) {
+        fvgs_session* s = b->s[i];
+        before[i].save(s);
+        fvgs_batch::Exit& e = exit[i];
+        e.gen = s->gen;
+        e.n_g = s->n_g;
+        e.vals_in = s->vals;
+        e.ranges_in = s->ranges;
+        e.entry_incremental = entry_incremental(s, reqs[i]);
+        for (int l = 0; l < kMaxLevels; ++l) {
+            e.W[l] = s->lv[l].W;
+            e.H[l] = s->lv[l].H;
+            e.K[l] = reqs[i].K[l];
+        }
+    }
+    const uint64_t launches0 = b->batch_launches;
+    cudaGraph_t graph = nullptr;
+    int rc = FVGS_OK;
+    cudaError_t ec = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (ec == cudaSuccess) {
+        rc = enqueue_batch_frame(b, reqs, true);
+        ec = cudaStreamEndCapture(b->stream, &graph);
+    }
+    if (rc == FVGS_OK && ec == cudaSuccess && graph) ec = cudaGraphInstantiate(&b->graph.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc == FVGS_OK && ec == cudaSuccess && b->graph.exec) {
+        // the captured launches read the tables filled on the host during the capture
+        const int iters = total_iterations(reqs[0]);
+        if (cudaMemcpy(b->g_jobs, b->h_jobs, sizeof(TrackJob) * n * iters, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->g_begin, b->h_begin, sizeof(uint32_t) * (n + 1) * iters, cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaMemcpy(b->g_rjobs, b->h_rjobs, sizeof(ReduceJob) * n * iters, cudaMemcpyHostToDevice) != cudaSuccess)
+            ec = cudaErrorUnknown;
+    }
+    if (rc != FVGS_OK || ec != cudaSuccess || !b->graph.exec) {
+        cudaGetLastError();
+        batch_drop_graph(b);
+        for (size_t i = 0; i < n; ++i) before[i].restore(b->s[i]);
+        b->batch_launches = launches0;
+        ++b->eager;
+        return enqueue_batch_frame(b, reqs, false);
+    }
+    for (size_t i = 0; i < n; ++i) {
+        fvgs_session* s = b->s[i];
+        fvgs_batch::Exit& e = exit[i];
+        e.ntx = s->hist_ntx;
+        e.nty = s->hist_nty;
+        e.tw = s->bin_tw;
+        e.th = s->bin_th;
+        e.last_W = s->last_W;
+        e.last_H = s->last_H;
+        e.last_T = s->last_T;
+        e.vals = s->vals;
+        e.vals_alt = s->sort.vals_alt;
+        e.ranges = s->ranges;
+        e.ranges_prev = s->ranges_prev;
+        for (int c = 0; c < FVGS_K_COUNT; ++c) e.launches[c] = s->launches[c] - before[i].launches[c];
+    }
+    fvgs_batch::Graph& g = b->graph;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        g.iters[l] = reqs[0].iters[l];
+        g.tw[l] = b->tw[l];
+        g.th[l] = b->th[l];
+        g.variant[l] = b->variant[l];
+    }
+    g.exit = exit;
+    g.batch_launches = b->batch_launches - launches0;
+    g.valid = true;
+    FV_CK(cudaGraphLaunch(g.exec, b->stream));
+    ++b->graphed;
+    return FVGS_OK;
+}
+
+int batch_requests(fvgs_batch* b, const fvgs_pose* poses, const fvgs_intrinsics* K0, const int* iterations,
+                   int levels, std::vector<Request>& reqs) {
+    const size_t n = b->s.size();
+    reqs.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        FV_TRY(pyramid_request(&poses[i], &K0[i], iterations, levels, -1.f, &reqs[i]));
+        fvgs_session* s = b->s[i];
+        // the persistent kernel has no compensated (precision-form) variant
+        if (s->n_g == 0 || s->frame_pending || s->precision != FVGS_PRECISION_FP32) return FVGS_E_STATE;
+        for (int l = 0; l < kMaxLevels; ++l)
+            if (reqs[i].iters[l] > 0 && !s->lv[l].rgb) return FVGS_E_STATE;
+    }
+    return FVGS_OK;
+}
+
+}  // namespace
+
+int fvgs_batch_create(fvgs_session* const* sessions, int n, fvgs_batch** out) {
+    if (!sessions || n <= 0 || !out) return FVGS_E_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!sessions[i] || sessions[i]->device != sessions[0]->device) return FVGS_E_INVALID;
+        if ((sessions[i]->params.quirks ^ sessions[0]->params.quirks) & FVGS_Q_POSE_JAC_APPROX) return FVGS_E_INVALID;
+        for (int k = 0; k < i; ++k)
+            if (sessions[k] == sessions[i]) return FVGS_E_INVALID;
+    }
+    FV_CK(cudaSetDevice(sessions[0]->device));
+    fvgs_batch* b = new (std::nothrow) fvgs_batch();
+    if (!b) return FVGS_E_NOMEM;
+    b->s.assign(sessions, sessions + n);
+    b->device = sessions[0]->device;
+    b->num_sms = sessions[0]->num_sms;
+    b->analytic = !(sessions[0]->params.quirks & FVGS_Q_POSE_JAC_APPROX);
+    for (int l = 0; l < kMaxLevels; ++l) {
+        b->tw[l] = b->th[l] = 16;
+        b->variant[l] = 0;
+    }
+    b->ev_join.assign(n, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaMalloc(&b->counters, 2 * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMemset(b->counters, 0, 2 * sizeof(uint32_t)) == cudaSuccess;
+    for (int i = 0; ok && i < n; ++i) ok = cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        fvgs_batch_destroy(b);
+        return FVGS_E_CUDA;
+    }
+    for (int l = 0; l < kMaxLevels; ++l) batch_apply_level(b, l);
+    *out = b;
+    return FVGS_OK;
+}
+
+int fvgs_batch_destroy(fvgs_batch* b) {
+    if (!b) return FVGS_E_INVALID;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graph(b);
+    batch_free_tables(b);
+    if (b->counters) cudaFree(b->counters);
+    for (cudaEvent_t e : b->ev_join)
+        if (e) cudaEventDestroy(e);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return FVGS_OK;
+}
+
+int fvgs_batch_set_level(fvgs_batch* b, int level, int tile_w, int tile_h, int batch_gaussians) {
+    if (!b || level < 0 || level >= kMaxLevels || !track_tile_supported(tile_w, tile_h)) return FVGS_E_INVALID;
+    if (batch_gaussians != 128 && batch_gaussians != 256 && batch_gaussians != 512) return FVGS_E_INVALID;
+    b->tw[level] = tile_w;
+    b->th[level] = tile_h;
+    b->variant[level] = batch_gaussians == 128 ? 3 : (batch_gaussians == 512 ? 4 : 0);
+    batch_apply_level(b, level);
+    return FVGS_OK;
+}
+
+int fvgs_batch_run_pyramid(fvgs_batch* b, fvgs_pose* poses, const fvgs_intrinsics* K0, const int* iterations,
+                           int levels) {
+    if (!b || !poses || !K0 || !iterations) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(b->device));
+    std::vector<Request> reqs;
+    FV_TRY(batch_requests(b, poses, K0, iterations, levels, reqs));
+    const size_t n = b->s.size();
+    FV_TRY(batch_ensure_tables(b, std::max(1, total_iterations(reqs[0]))));
+    for (size_t i = 0; i < n; ++i) *b->s[i]->h_pose = reqs[i].pose;
+    FV_TRY(batch_launch(b, reqs.data()));
+    FV_CK(cudaStreamSynchronize(b->stream));
+    int first_error = FVGS_OK;
+    for (size_t i = 0; i < n; ++i) {
+        fvgs_session* s = b->s[i];
+        collect_timing(s);
+        int retry = 0;
+        int rc = check_status(s, &retry);
+        if (rc == FVGS_OK && retry) {
+            // instance overflow (buffers grown) or an inconsistent incremental
+            // binning: this session's frame again, alone, with the same tiles
+            ++s->frames_eager;
+            rc = run_request_eager(s, reqs[i], &poses[i], nullptr);
+        } else if (rc == FVGS_OK) {
+            for (int k = 0; k < 3; ++k) poses[i].position[k] = s->h_devpose->t[k];
+            for (int k = 0; k < 4; ++k) poses[i].orientation[k] = s->h_devpose->q[k];
+            s->has_track = true;
+        }
+        if (rc != FVGS_OK && first_error == FVGS_OK) first_error = rc;
+    }
+    return first_error;
+}
+
+int fvgs_batch_autotune(fvgs_batch* b, const fvgs_pose* poses, const fvgs_intrinsics* K0, const int* iterations,
+                        int levels, int reps, int* config_out, float* ms_out) {
+    if (!b || !poses || !K0 || !iterations) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(b->device));
+    std::vector<Request> reqs;
+    FV_TRY(batch_requests(b, poses, K0, iterations, levels, reqs));
+    FV_TRY(batch_ensure_tables(b, std::max(1, total_iterations(reqs[0]))));
+    reps = std::max(1, std::min(reps, 16));
+    const size_t n = b->s.size();
+    const int shapes[3][2] = {{16, 16}, {8, 8}, {32, 8}};
+    const int variants[3] = {3, 0, 4};  // batches of 128, 256, 512
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps, nullptr);
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto& e2 : ev)
+                if (e2) cudaEventDestroy(e2);
+            return FVGS_E_CUDA;
+        }
+    int rc = FVGS_OK;
+    for (int l = 0; l < levels && l < kMaxLevels && rc == FVGS_OK; ++l) {
+        if (reqs[0].iters[l] == 0) continue;
+        float best = INFINITY;
+        int best_shape = 0, best_variant = 0;
+        for (int sh = 0; sh < 3 && rc == FVGS_OK; ++sh) {
+            b->tw[l] = shapes[sh][0];
+            b->th[l] = shapes[sh][1];
+            uint32_t total = 0;
+            // bin every session at its pose with this tile shape (again after an overflow)
+            for (int attempt = 0;; ++attempt) {
+                if (attempt == 4) {
+                    rc = FVGS_E_CAPACITY;
+                    break;
+                }
+                if ((rc = batch_fork(b)) != FVGS_OK) break;
+                for (size_t i = 0; i < n && rc == FVGS_OK; ++i) {
+                    rc = reset_status(b->s[i]);
+                    if (rc == FVGS_OK) rc = set_pose(b->s[i], &reqs[i].pose);
+                }
+                if (rc == FVGS_OK) rc = batch_bin_level(b, reqs.data(), l, 0, &total);
+                if (rc == FVGS_OK) rc = batch_join(b);
+                for (size_t i = 0; i < n && rc == FVGS_OK; ++i)
+                    if (cudaMemcpyAsync(b->s[i]->h_st, b->s[i]->st, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                                        b->stream) != cudaSuccess)
+                        rc = FVGS_E_CUDA;
+                if (rc == FVGS_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = FVGS_E_CUDA;
+                if (rc != FVGS_OK) break;
+                int any = 0;
+                for (size_t i = 0; i < n && rc == FVGS_OK; ++i) {
+                    collect_timing(b->s[i]);
+                    int retry = 0;
+                    rc = check_status(b->s[i], &retry);
+                    any |= retry;
+                }
+                if (rc != FVGS_OK || !any) break;
+            }
+            if (rc != FVGS_OK) break;
+            if (cudaMemcpy(b->d_jobs, b->h_jobs, sizeof(TrackJob) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(b->d_begin, b->h_begin, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice) !=
+                    cudaSuccess) {
+                rc = FVGS_E_CUDA;
+                break;
+            }
+            for (int vi = 0; vi < 3 && rc == FVGS_OK; ++vi) {
+                const int v = variants[vi];
+                for (int r = 0; r < reps && rc == FVGS_OK; ++r) {
+                    if (cudaEventRecord(ev[2 * r], b->stream) != cudaSuccess ||
+                        launch_track_batch(b->d_jobs, b->d_begin, (int)n, total, b->tw[l], b->th[l], b->analytic, v,
+                                           b->counters, b->num_sms, b->stream) != cudaSuccess ||
+                        cudaEventRecord(ev[2 * r + 1], b->stream) != cudaSuccess)
+                        rc = FVGS_E_CUDA;
+                }
+                if (rc == FVGS_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = FVGS_E_CUDA;
+                if (rc != FVGS_OK) break;
+                std::vector<float> t(reps);
+                for (int r = 0; r < reps; ++r) cudaEventElapsedTime(&t[r], ev[2 * r], ev[2 * r + 1]);
+                std::sort(t.begin(), t.end());
+                const float med = t[reps / 2];
+                if (ms_out) ms_out[l * 9 + sh * 3 + vi] = med;
+                if (med < best) {
+                    best = med;
+                    best_shape = sh;
+                    best_variant = v;
+                }
+            }
+        }
+        if (rc != FVGS_OK) break;
+        b->tw[l] = shapes[best_shape][0];
+        b->th[l] = shapes[best_shape][1];
+        b->variant[l] = best_variant;
+        if (config_out) {
+            config_out[3 * l] = b->tw[l];
+            config_out[3 * l + 1] = b->th[l];
+            config_out[3 * l + 2] = track_variant_batch(best_variant);
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int l = 0; l < kMaxLevels; ++l) batch_apply_level(b, l);
+    if (rc != FVGS_OK) cudaGetLastError();
+    return rc;
+}
+
+int fvgs_batch_stats(const fvgs_batch* b, uint64_t* graphed, uint64_t* eager, uint64_t* batch_launches) {
+    if (!b) return FVGS_E_INVALID;
+    if (graphed) *graphed = b->graphed;
+    if (eager) *eager = b->eager;
+    if (batch_launches) *batch_launches = b->batch_launches;
+    return FVGS_OK;
+}
+
 int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager) {
     if (!s) return FVGS_E_INVALID;
     if (graphed) *graphed = s->frames_graphed;
@@ -1844,7 +2493,7 @@ int fvgs_render(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, width, height));
+        FV_TRY(enqueue_bin(s, K, width, height, s->params.tile_w, s->params.tile_h));
         FV_TRY(enqueue_track(s, K, view, true, true));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
@@ -1874,7 +2523,7 @@ int fvgs_render_view(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsi
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, width, height));
+        FV_TRY(enqueue_bin(s, K, width, height, s->params.tile_w, s->params.tile_h));
         RenderArgs ra{};
         ra.rec0 = s->rec0;
         ra.rec1 = s->rec1;
@@ -1948,7 +2597,7 @@ int fvgs_map_step(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics*
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H, s->params.tile_w, s->params.tile_h));
         FV_TRY(enqueue_map(s, K, f, eta));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaStreamSynchronize(s->stream));
@@ -1997,7 +2646,7 @@ int visibility_pass(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsic
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, W, H));
+        FV_TRY(enqueue_bin(s, K, W, H, s->params.tile_w, s->params.tile_h));
         FV_CK(cudaMemsetAsync(vis, 0, s->n_g, s->stream));
         VisArgs va{};
         va.rec0 = s->rec0;
@@ -2155,7 +2804,7 @@ int fvgs_remove_outliers(fvgs_session* s, const fvgs_pose* pose, const fvgs_intr
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, f.W, f.H));
+        FV_TRY(enqueue_bin(s, K, f.W, f.H, s->params.tile_w, s->params.tile_h));
         FV_CK(cudaMemsetAsync(s->mk_total_alpha, 0, sizeof(float) * s->n_g, s->stream));
         FV_CK(cudaMemsetAsync(s->mk_outlier_prob, 0, sizeof(float) * s->n_g, s->stream));
         OutlierArgs oa{};
@@ -2324,7 +2973,7 @@ int fvgs_densify(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* 
     for (int attempt = 0; attempt < 4; ++attempt) {
         FV_TRY(reset_status(s));
         FV_TRY(set_pose(s, pose));
-        FV_TRY(enqueue_bin(s, K, W, H));
+        FV_TRY(enqueue_bin(s, K, W, H, s->params.tile_w, s->params.tile_h));
         DensityArgs da{};
         da.rec0 = s->rec0;
         da.rec1 = s->rec1;

@@ -157,15 +157,18 @@ __device__ __forceinline__ void entering_tile(const EnterSplit& e, uint32_t loca
 }
 
 // Depth of a Gaussian at the centre of tile (tx, ty) -- the sort key of the
-// reference's generateTileHashes_kernel (src/GSCudaKernels.cu:596-667):
-// fmaf(phy, dy, fmaf(phx, dx, z)), d = tile centre - projected mean.
+// reference's generateTileHashes_kernel (src/GSCudaKernels.cu:596-667),
+// z + pHat.x * dx + pHat.y * dy with d = tile centre - projected mean, as the
+// reference's nvcc build evaluates it: the first product fused with z, the
+// second rounded and added, fmaf(phx, dx, z) + phy * dy (matched bit for bit
+// against keys of that build).
 __device__ __forceinline__ float tile_depth(int tx, int ty, int tw, int th, float u, float v, float z, float phx,
                                             uint32_t phy_bits) {
     const float tcx = __fmul_rn(__fadd_rn((float)tx, 0.5f), (float)tw);
     const float tcy = __fmul_rn(__fadd_rn((float)ty, 0.5f), (float)th);
     const float dx = __fsub_rn(tcx, u);
     const float dy = __fsub_rn(tcy, v);
-    return __fmaf_rn(__uint_as_float(phy_bits), dy, __fmaf_rn(phx, dx, z));
+    return __fadd_rn(__fmaf_rn(phx, dx, z), __fmul_rn(__uint_as_float(phy_bits), dy));
 }
 
 // Programmatic dependent launch.  Kernels of the binning / tracking / mapping

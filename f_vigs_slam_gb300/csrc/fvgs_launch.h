@@ -222,8 +222,25 @@ struct TrackArgs {
     // records written by the projection (ProjectArgs::geo0 / geo1)
     const float4* geo0;
     const float4* geo1;
+    // tile shape of the binning the lists come from: 16 x 16 (also 0 x 0),
+    // 8 x 8 or 32 x 8 (the TMA-staged variant only for 16 x 16)
+    int tile_w, tile_h;
+    // precision form: compensated accumulation of the per-pixel colour
+    // Jacobian and of the in-tile sums (analytic Jacobian, 16 x 16 tiles)
+    int compensated;
 };
 constexpr int kTrackVariants = 5;
+// Whether the tracking kernel runs tiles of this shape.
+inline bool track_tile_supported(int tw, int th) {
+    return (tw == 16 && th == 16) || (tw == 8 && th == 8) || (tw == 32 && th == 8);
+}
+// Gaussians staged per shared-memory batch by a launch variant: 3 -> 128,
+// 4 -> 512, otherwise 256.
+inline int track_variant_batch(int variant) { return variant == 3 ? 128 : (variant == 4 ? 512 : 256); }
+// Set the dynamic shared-memory limits of the tracking kernels on the current
+// device (their batches can exceed the 48 KB default); once per device,
+// before any launch or capture.
+cudaError_t track_configure_device();
 // Tensor maps of the three record planes (2-D: 4 floats x capacity rows,
 // 16-byte rows, one-row boxes) for the TMA-staged variant.
 struct RecMaps {
@@ -239,6 +256,32 @@ cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* p
                                 cudaStream_t s);
 // The same reduction followed by one eigen-regularised Gauss-Newton update of
 // the device pose (step_out[6] nullable).
+// One session's frame reduction + Gauss-Newton step in a batched launch.
+struct ReduceJob {
+    const float* tile_out;
+    int num_tiles;
+    DevPose* pose;
+    double* out;
+    double eig_eps;
+    double* step_out;
+};
+// launch_track_reduce_gn for n_jobs sessions at once (device array of jobs).
+cudaError_t launch_track_reduce_batch(const ReduceJob* jobs, int n_jobs, cudaStream_t s);
+// One session's tracking launch in a persistent batched launch: its
+// arguments and the first work item (tile) of its range.
+struct TrackJob {
+    TrackArgs a;
+};
+// The tiles of n_jobs sessions in one persistent launch: work item i is tile
+// i - begin[j] of job j for begin[j] <= i < begin[j + 1] (begin: n_jobs + 1
+// device words).  Every job must use tile shape (tile_w, tile_h), the same
+// Jacobian mode (analytic) and staging batch (variant).  counters: two
+// device words, zero before the first launch; every launch leaves them zero.
+cudaError_t launch_track_batch(const TrackJob* jobs, const uint32_t* begin, int n_jobs, uint32_t total_tiles,
+                               int tile_w, int tile_h, bool analytic, int variant, uint32_t* counters, int num_sms,
+                               cudaStream_t s);
+// Kernel attributes of the persistent kernels on the current device.
+cudaError_t track_batch_configure_device();
 cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
                                    double eig_eps, double* step_out, cudaStream_t s);
 

@@ -282,6 +282,13 @@ class Session:
         tw, th = self.tile
         return ((W + tw - 1) // tw) * ((H + th - 1) // th)
 
+    def binning_grid(self):
+        """(tile_w, tile_h, number of tiles) of the last binning."""
+        tw, th, T = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.fvgs_session_binning_grid(self.h, C.byref(tw), C.byref(th), C.byref(T)),
+               "fvgs_session_binning_grid")
+        return int(tw.value), int(th.value), int(T.value)
+
     def download_binning(self, W, H, max_instances: int | None = None):
         n = C.c_uint32()
         _check(self.lib.fvgs_download_binning(self.h, None, None, None, C.c_uint64(0), C.byref(n)),
@@ -289,14 +296,14 @@ class Session:
         cnt = int(n.value)
         keys = np.zeros(max(cnt, 1), np.uint64)
         vals = np.zeros(max(cnt, 1), np.uint32)
-        T = self.num_tiles(W, H)
-        ranges = np.zeros((T, 2), np.uint32)
+        T = self.binning_grid()[2]
+        ranges = np.zeros((max(T, 1), 2), np.uint32)
         _check(
             self.lib.fvgs_download_binning(self.h, _ptr(keys), _ptr(vals), _ptr(ranges), C.c_uint64(cnt),
                                            C.byref(n)),
             "fvgs_download_binning",
         )
-        return keys[:cnt], vals[:cnt], ranges
+        return keys[:cnt], vals[:cnt], ranges[:T]
 
     # ------------------------------------------------------------- tracking
     def track_jacobian(self, pose, K, level: int = 0):
@@ -514,6 +521,11 @@ class Session:
         _check(self.lib.fvgs_frame_wait(self.h, C.byref(p), _ptr(step)), "fvgs_frame_wait")
         return (np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)), step
 
+    def set_track_tiles(self, level: int, tile_w: int, tile_h: int):
+        """Tile shape of a pyramid level's tracking (fvgs_session_set_track_tiles): 16x16, 8x8 or 32x8."""
+        _check(self.lib.fvgs_session_set_track_tiles(self.h, C.c_int(level), C.c_int(tile_w), C.c_int(tile_h)),
+               "fvgs_session_set_track_tiles")
+
     def frame_stats(self) -> dict:
         g, e = C.c_uint64(), C.c_uint64()
         _check(self.lib.fvgs_session_frame_stats(self.h, C.byref(g), C.byref(e)), "fvgs_session_frame_stats")
@@ -545,6 +557,64 @@ def frames_run_pyramid(sessions, poses, K0s, iterations=(4, 4, 6, 6), map_etas=N
     _check(lib.fvgs_frames_run_pyramid(hs, ps, ks, it, C.c_int(len(iterations)), et, C.c_int(n)),
            "fvgs_frames_run_pyramid")
     return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
+
+
+TILE_SHAPES = ((16, 16), (8, 8), (32, 8))
+STAGE_BATCHES = (128, 256, 512)
+
+
+class Batch:
+    """Keyframe batching in one persistent launch per Gauss-Newton iteration (fvgs_batch_*)."""
+
+    def __init__(self, sessions):
+        self.lib = load_library()
+        self.sessions = list(sessions)
+        n = len(self.sessions)
+        hs = (C.c_void_p * n)(*[s.h for s in self.sessions])
+        self.h = C.c_void_p()
+        _check(self.lib.fvgs_batch_create(hs, C.c_int(n), C.byref(self.h)), "fvgs_batch_create")
+
+    def close(self):
+        if self.h:
+            _check(self.lib.fvgs_batch_destroy(self.h), "fvgs_batch_destroy")
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_level(self, level: int, tile_w: int, tile_h: int, batch: int = 256):
+        _check(self.lib.fvgs_batch_set_level(self.h, C.c_int(level), C.c_int(tile_w), C.c_int(tile_h),
+                                             C.c_int(batch)), "fvgs_batch_set_level")
+
+    def autotune(self, poses, K0s, iterations=(4, 4, 6, 6), reps: int = 5):
+        """Per level: the fastest (tile_w, tile_h, batch) and the 9 medians (ms, shape-major)."""
+        n = len(self.sessions)
+        ps = (Pose * n)(*[make_pose(p) for p in poses])
+        ks = (Intrinsics * n)(*[make_intr(k) for k in K0s])
+        it = (C.c_int * len(iterations))(*iterations)
+        cfg = np.zeros(3 * MAX_LEVELS, np.int32)
+        ms = np.full(9 * MAX_LEVELS, np.nan, np.float32)
+        _check(self.lib.fvgs_batch_autotune(self.h, ps, ks, it, C.c_int(len(iterations)), C.c_int(reps),
+                                            _ptr(cfg), _ptr(ms)), "fvgs_batch_autotune")
+        return ({l: tuple(int(v) for v in cfg[3 * l:3 * l + 3]) for l in range(len(iterations)) if iterations[l] > 0},
+                {l: ms[9 * l:9 * l + 9].reshape(3, 3) for l in range(len(iterations)) if iterations[l] > 0})
+
+    def run_pyramid(self, poses, K0s, iterations=(4, 4, 6, 6)):
+        n = len(self.sessions)
+        ps = (Pose * n)(*[make_pose(p) for p in poses])
+        ks = (Intrinsics * n)(*[make_intr(k) for k in K0s])
+        it = (C.c_int * len(iterations))(*iterations)
+        _check(self.lib.fvgs_batch_run_pyramid(self.h, ps, ks, it, C.c_int(len(iterations))),
+               "fvgs_batch_run_pyramid")
+        return [(np.array(p.position[:], np.float32), np.array(p.orientation[:], np.float32)) for p in ps]
+
+    def stats(self) -> dict:
+        g, e, bl = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(self.lib.fvgs_batch_stats(self.h, C.byref(g), C.byref(e), C.byref(bl)), "fvgs_batch_stats")
+        return dict(graphed=int(g.value), eager=int(e.value), batch_launches=int(bl.value))
 
 
 def pack_pyramid(levels):

@@ -159,7 +159,8 @@ int fvgs_project_bin(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsi
 int fvgs_download_projection(fvgs_session* s, float* uv, float* cov2d, float* inv2d, float* depth, float* phat,
                              uint8_t* visible, uint32_t* tile_counts);
 /* Sorted keys (hashes_), values (gaussian_indices_) and ranges[2T]
- * (tile_ranges_) of the last binning.  Any pointer may be null. */
+ * (tile_ranges_) of the last binning, T its tile count
+ * (fvgs_session_binning_grid).  Any pointer may be null. */
 int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uint32_t* ranges,
                           uint64_t max_instances, uint32_t* n_instances);
 /* How the last binning whose status the host has read (every call that
@@ -168,6 +169,10 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
  * instances that entered a tile since that binning, and the Gaussians with
  * such instances.  Any pointer may be null.  No reference counterpart: the
  * reference rebuilds every binning from scratch. */
+/* Tile shape and tile count of the last binning (a tracking level may bin on
+ * 8 x 8 or 32 x 8 tiles: fvgs_session_set_track_tiles).  Any pointer may be
+ * null.  No reference counterpart (its tiles are always 16 x 16). */
+int fvgs_session_binning_grid(const fvgs_session* s, int* tile_w, int* tile_h, int* num_tiles);
 int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
                               uint32_t* n_changed);
 
@@ -241,6 +246,55 @@ int fvgs_frames_run_pyramid(fvgs_session* const* sessions, fvgs_pose* poses, con
                             const int* iterations, int levels, const float* map_etas, int n);
 /* Frames of the session that ran from a captured graph / eagerly. */
 int fvgs_session_frame_stats(const fvgs_session* s, uint64_t* graphed, uint64_t* eager);
+
+/*
+ * Tile shape of one pyramid level's tracking (batching form): 16 x 16 (the
+ * reference's TILE_SIZE, src/GSCudaKernels.cu:6, and the default), 8 x 8 or
+ * 32 x 8.  That level's binnings and Jacobian kernel use the shape: tile
+ * rectangles, tile-centre depth keys (src/GSCudaKernels.cu:617-639 with the
+ * tile's own width and height) and tile lists follow it, so a pixel blends
+ * its own tile's list -- another shape rasterizes the same map differently,
+ * and parity holds against the oracle binned at the same shape.  Mapping,
+ * rendering and map maintenance keep 16 x 16.  No reference counterpart.
+ */
+int fvgs_session_set_track_tiles(fvgs_session* s, int level, int tile_w, int tile_h);
+
+/*
+ * Keyframe batching in one persistent launch (batching form).  A batch holds
+ * n sessions on one device, all with the same Jacobian mode.
+ * fvgs_batch_run_pyramid runs one coarse-to-fine frame (iterations[levels],
+ * as fvgs_track_frame_pyramid) on every session in lockstep: each
+ * Gauss-Newton iteration bins every session (on the sessions' own streams,
+ * concurrently), then ONE persistent launch blends and differentiates the
+ * tiles of all sessions -- its CTAs take (session, tile) work items from a
+ * shared counter, so uneven maps and frame sizes balance across the SMs --
+ * and one launch reduces every session's tiles and applies its pose step.
+ * The whole frame is captured once as one CUDA graph and replayed while the
+ * sessions' binning state allows.  poses[i] is read and overwritten.  A
+ * session whose instance buffers overflow is repeated alone on the plain
+ * path after they grow.
+ * Each level's tile shape and staging batch (128, 256 or 512 Gaussians per
+ * shared-memory batch) belong to the batch and are pushed to its sessions
+ * (fvgs_session_set_track_tiles and the launch variant), so a session's plain
+ * frames give the batched result bit for bit.  fvgs_batch_set_level sets
+ * them; fvgs_batch_autotune times the persistent launch for every shape x
+ * batch (9 combinations) on every level the schedule uses, at the given
+ * poses (reps launches each), and keeps the fastest per level; config_out
+ * (nullable, 3 ints per level: tile_w, tile_h, batch) and ms_out (nullable,
+ * 9 floats per level: shapes 16x16, 8x8, 32x8, each with batches 128, 256,
+ * 512) report the outcome.  fvgs_batch_stats: frames replayed / enqueued
+ * eagerly, batched kernel launches.  The reference tracks one frame of one
+ * map per launch; no counterpart.
+ */
+typedef struct fvgs_batch fvgs_batch;
+int fvgs_batch_create(fvgs_session* const* sessions, int n, fvgs_batch** out);
+int fvgs_batch_destroy(fvgs_batch* b);
+int fvgs_batch_set_level(fvgs_batch* b, int level, int tile_w, int tile_h, int batch_gaussians);
+int fvgs_batch_autotune(fvgs_batch* b, const fvgs_pose* poses, const fvgs_intrinsics* K0, const int* iterations,
+                        int levels, int reps, int* config_out, float* ms_out);
+int fvgs_batch_run_pyramid(fvgs_batch* b, fvgs_pose* poses, const fvgs_intrinsics* K0, const int* iterations,
+                           int levels);
+int fvgs_batch_stats(const fvgs_batch* b, uint64_t* graphed, uint64_t* eager, uint64_t* batch_launches);
 
 /*
  * The viewer's image: binning + the render-form forward pass

@@ -302,7 +302,10 @@ int oracle_count(const float* uv, const float* cov2d, const uint8_t* visible, in
  * Keys in generation order (exclusive scan of counts, then
  * generateTileHashes_kernel, src/GSCudaKernels.cu:596-667):
  * key = tile_id << 32 | bits(z + phx*dx + phy*dy), dx,dy = tile centre - uv,
- * the depth evaluated as fmaf(phy, dy, fmaf(phx, dx, z)).  Row-major tile loop.
+ * the depth evaluated as the reference's nvcc build does: the first product
+ * fused with z, the second rounded and added, fmaf(phx, dx, z) + phy*dy
+ * (matched bit for bit against that build's keys; without FMA, the source's
+ * one rounding per operation).  Row-major tile loop.
  * Returns the instance count, or -1 if it exceeds cap.
  */
 int64_t oracle_emit_keys(const float* uv, const float* depth, const float* phat, const uint32_t* count,
@@ -326,7 +329,7 @@ int64_t oracle_emit_keys(const float* uv, const float* depth, const float* phat,
                 const float tcx = ((float)tx + 0.5f) * (float)tw;
                 const float tcy = ((float)ty + 0.5f) * (float)th;
                 const float dx = tcx - u, dy = tcy - v;
-                const float d = f_fma(phy, dy, f_fma(phx, dx, z));
+                const float d = f_fma(phx, dx, z) + phy * dy;
                 const uint32_t tile = (uint32_t)(ty * ntx + tx);
                 keys[w] = ((uint64_t)tile << 32) | (uint64_t)f2u(d);
                 vals[w] = (uint32_t)i;

@@ -85,6 +85,25 @@ def test_track_jacobian_parity(oracle, fvgs_lib, quirks):
     s.close()
 
 
+@pytest.mark.parametrize("quirks", [REF, INTENDED], ids=["ref", "analytic"])
+def test_track_jacobian_parity_moved_pose(oracle, fvgs_lib, quirks):
+    """Away from the identity: the camera translated and rotated, so the
+    per-Gaussian depths z + dx phat.x + dy phat.y of the reference's Jacobian
+    cancel for other pixels, and screen offsets dx = u - x round in FP32
+    where |dx| > |u|."""
+    W, H, K, scene, P, frame, s = _setup(oracle, fvgs_lib, 20_000, 0.5, 31, quirks)
+    for pose in ((np.array([0.003, -0.002, 0.001], np.float32), S.IDENTITY_Q),
+                 S.perturb((np.zeros(3), S.IDENTITY_Q), 0.5, 1.0, np.random.default_rng(33))):
+        JtJ, Jtr = s.track_jacobian(pose, K, 0)
+        b = oracle.prepare(scene, pose, K, W, H, P)
+        r = oracle.track(b, frame, pose, K, W, H, P, images=False)
+        e1, e2 = rel_err(JtJ, r.JtJ), rel_err(Jtr, r.Jtr)
+        print("JtJ rel", e1, "Jtr rel", e2)
+        assert e1 <= JAC_RTOL, e1
+        assert e2 <= JAC_RTOL, e2
+    s.close()
+
+
 def test_track_deterministic(oracle, fvgs_lib):
     W, H, K, scene, P, frame, s = _setup(oracle, fvgs_lib, 10_000, 0.5, 5)
     pose = (np.array([0.01, 0, 0], np.float32), S.IDENTITY_Q)
@@ -258,6 +277,7 @@ def test_track_tiles_room_1m_hd(oracle, fvgs_lib, quirks):
         rgb, d = S.add_noise(col, dep, rng)
         gx, gy = S.sobel3(rgb)
         s.set_frame(0, rgb, d, gx, gy)
+        s.upload(scene)  # no binning history: the first evaluation bins in full
         got = {}
         for name, pose in (("full", pose_a), ("incremental", pose_b)):
             s.track_jacobian(pose, K, 0)
