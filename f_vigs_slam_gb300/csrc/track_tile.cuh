@@ -202,6 +202,37 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
     return false;
 }
 
+// The warps of a TW x TH tile (8 x 4 pixel blocks, row-major) whose pixels a
+// staged Gaussian can reach: those whose block meets the axis-aligned box of
+// the ellipse v <= vreject (v = a dx^2 + 2 b dx dy + c dy^2, half-widths
+// sqrt(V c / det) and sqrt(V a / det)).  Every pixel outside it rejects the
+// Gaussian in both passes (v > vreject), so a warp whose block misses the box
+// may skip it without changing any result.  V = 1.05 vreject + 1e-3 and the
+// widths grow by 1% + 0.01 px: when det >= 1e-4 a c the FP32 evaluation of v
+// errs by less than 1.6% of v, so no pixel the kernel would keep falls
+// outside.  Forms that are not positive definite, nearly singular ones and
+// non-finite values reach every warp.
+template <int TW, int TH>
+__device__ __forceinline__ uint32_t warp_block_mask(float u, float v, float a, float b, float c, float vrej,
+                                                    float x0, float y0) {
+    constexpr int NW = TW * TH / 32, WX = TW / 8;
+    constexpr uint32_t kAll = (1u << NW) - 1u;
+    const float det = a * c - b * b;
+    const float vm = fmaf(vrej, 1.05f, 1e-3f);
+    if (!(a > 0.f && c > 0.f && det > 1e-4f * (a * c) && vm > 0.f && vm < INFINITY && isfinite(u) && isfinite(v)))
+        return kAll;
+    const float inv = __frcp_rn(det);
+    const float hx = fmaf(sqrtf(vm * c * inv), 1.01f, 0.01f), hy = fmaf(sqrtf(vm * a * inv), 1.01f, 0.01f);
+    if (!(hx < INFINITY && hy < INFINITY)) return kAll;
+    uint32_t m = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        const float bx = x0 + (float)((w % WX) * 8), by = y0 + (float)((w / WX) * 4);
+        if (bx <= u + hx && bx + 7.0f >= u - hx && by <= v + hy && by + 3.0f >= v - hy) m |= 1u << w;
+    }
+    return m;
+}
+
 // Shared-memory batch of Gaussians, repacked so a rejected pair needs two
 // loads: sA = (u, v, c.x, c.y), sB = (c.z, vreject, log2(opacity), z),
 // sC = (phat.x, phat.y, r, g), sD = b, s_orig = index in the tile's list;
@@ -212,6 +243,11 @@ __device__ __forceinline__ bool tile_prunable(float u, float v, float ca, float 
 // the camera-frame pose update and the mean's (x, y) (see stage_deriv).
 template <int BATCH = kBatch, int NX = 1, int NT = kPix>
 struct TrackBatch {
+    // wm[j]: the warps (8 x 4 pixel blocks) whose pixels staged Gaussian j
+    // can reach (warp_block_mask); bm[w][g]: bit k set when entry 32 g + k
+    // is in warp w's mask -- each warp walks only its own entries
+    uint8_t wm[BATCH];
+    uint32_t bm[NT / 32][BATCH / 32];
     float4 A[BATCH];
     float4 B[BATCH];
     float4 C[BATCH];
@@ -292,9 +328,12 @@ __device__ __forceinline__ void stage_deriv(const TrackArgs& a, const float4& r0
     out[7] = make_float4(dc[4], dc[5], x, y);
 }
 
-template <int STAGE, int BATCH, int NX, int NT>
+template <int STAGE, int TW, int TH, int BATCH, int NX, int NT>
 __device__ __forceinline__ void put_staged(const TrackArgs& a, TrackBatch<BATCH, NX, NT>& sb, int pos, const float4& r0,
-                                           const float4& r1, const float4& r2, float vrej, int li, uint32_t g) {
+                                           const float4& r1, const float4& r2, float vrej, int li, uint32_t g,
+                                           float x0, float y0) {
+    static_assert(TW * TH == NT, "tile shape of the staged batch");
+    sb.wm[pos] = (uint8_t)warp_block_mask<TW, TH>(r0.x, r0.y, r1.x, r1.y, r1.z, vrej, x0, y0);
     sb.A[pos] = make_float4(r0.x, r0.y, r1.x, r1.y);
     sb.B[pos] = make_float4(r1.z, vrej, log2_opacity(r0.w), r0.z);
     sb.C[pos] = make_float4(r1.w, r2.x, r2.y, r2.z);
@@ -349,7 +388,8 @@ __device__ __forceinline__ int stage_batch(const TrackArgs& a, TrackBatch<BATCH,
             round_total += c;
         }
         if (keep)
-            put_staged<STAGE>(a, sb, total + wbase + __popc(bal & lanemask_lt()), r0v, r1, r2, vrej, li, g);
+            put_staged<STAGE, TW, TH>(a, sb, total + wbase + __popc(bal & lanemask_lt()), r0v, r1, r2, vrej, li, g,
+                                      x0, y0);
         total += round_total;
         __syncthreads();
     }
@@ -480,7 +520,9 @@ __device__ __forceinline__ int stage_batch_tma(const TrackArgs& a, const RecMaps
         wbase += (k < w) ? c : 0;
         total += c;
     }
-    if (keep) put_staged<FORWARD ? kStageNone : kStageRay>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2, vrej, li, g);
+    if (keep)
+        put_staged<FORWARD ? kStageNone : kStageRay, kTW, kTH>(a, sb, wbase + __popc(bal & lanemask_lt()), r0, r1, r2,
+                                                             vrej, li, g, x0, y0);
     const bool next = ready && base + kBatch < limit;
     if (next && tid == 0) tma_bar_expect(&ts.bar, kTmaBatchBytes);
     __syncthreads();
@@ -530,6 +572,20 @@ __device__ __forceinline__ float depth_weight(float derr, float thr, float z_obs
     return w / z_obs;
 }
 
+// Per-warp bitmaps of a staged batch of cnt entries (after its barrier; every
+// lane of the CTA takes part).  A warp writes and reads only its own rows.
+template <int BATCH, int NX, int NT>
+__device__ __forceinline__ void build_warp_bitmaps(TrackBatch<BATCH, NX, NT>& sb, int cnt) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int g = 0; g * 32 < cnt; ++g) {
+        const int j = g * 32 + lane;
+        const bool rel = j < cnt && ((sb.wm[j] >> w) & 1u);
+        const uint32_t b = __ballot_sync(kFullMask, rel);
+        if (lane == 0) sb.bm[w][g] = b;
+    }
+    __syncwarp();
+}
+
 // Shared-memory batch of the body below (dynamic shared memory: the analytic
 // Jacobian's batch of 512 exceeds the static limit).
 template <int TW, int TH, int BATCH, bool ANALYTIC>
@@ -552,10 +608,10 @@ __device__ __forceinline__ TmaStage& body_tma_stage(unsigned char* dyn) {
 // per pixel; each warp covers an 8 x 4 pixel block).  Tile shapes: 16 x 16
 // (the reference's), 8 x 8 and 32 x 8; the binning must use the same shape.
 // Ends with the tile's 27 partials written to a.tile_out[tile].
-// COMP (precision form, analytic Jacobian only): the per-pixel colour
-// Jacobian accumulated over the blended Gaussians with Kahan summation and
-// the in-tile sums of the 27 partials compensated (warp_reduce_scatter32_comp,
-// then TwoSum across warps).
+// COMP (precision form, analytic Jacobian only): the forward blend's colour
+// accumulated with Kahan summation, and the in-tile sums of the 27 J^T J /
+// J^T r partials compensated (warp_reduce_scatter32_comp, then TwoSum across
+// warps); the tile-to-frame sum is compensated in every form.
 template <int TW, int TH, bool RENDER_ONLY, bool REF_LAYOUT, bool TMA, int BATCH, bool ANALYTIC,
           bool COMP = false>
 __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMaps& maps, int tile,
@@ -593,6 +649,7 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
 
     // ------------------------- pass 1: forward blend -------------------------
     float T = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, depth = 0.f;
+    float ccr = 0.f, ccg = 0.f, ccb = 0.f;  // Kahan carries of the colour (COMP)
     uint32_t last = 0;
     bool done = !inside;
     float final_T = 1.f;
@@ -606,6 +663,7 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                 cnt = stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm);
             else
                 cnt = stage_batch<REF_LAYOUT, true, kStageNone, TW, TH>(a, sb, range.x, base, n, x0, y0);
+            build_warp_bitmaps(sb, cnt);
             if (!done) {
                 int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
@@ -617,44 +675,61 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                     if (test_T < 0.0001f) return false;
                     const float4 rC = sb.C[j];
                     const float aT = alpha * T;
-                    cr += rC.z * aT;
-                    cg += rC.w * aT;
-                    cb += sb.D[j] * aT;
+                    if constexpr (COMP) {
+                        kahan_add(cr, ccr, rC.z * aT);
+                        kahan_add(cg, ccg, rC.w * aT);
+                        kahan_add(cb, ccb, sb.D[j] * aT);
+                    } else {
+                        cr += rC.z * aT;
+                        cg += rC.w * aT;
+                        cb += sb.D[j] * aT;
+                    }
                     if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, sb.A[j].x, xf, rC.x, sb.A[j].y, yf, rC.y);
                     T = test_T;
                     last_j = j;
                     return true;
                 };
-                int j = 0;
-                // two Gaussians per iteration: both quadratic forms are evaluated
-                // before the (mostly rejecting) branches, in list order
-                for (; j + 1 < cnt; j += 2) {
-                    const float4 rA0 = sb.A[j], rA1 = sb.A[j + 1];
-                    const float2 rB0 = *reinterpret_cast<const float2*>(&sb.B[j]);
-                    const float2 rB1 = *reinterpret_cast<const float2*>(&sb.B[j + 1]);
-                    const float dx0 = rA0.x - xf, dy0 = rA0.y - yf;
-                    const float dx1 = rA1.x - xf, dy1 = rA1.y - yf;
-                    float q0, q1;
-                    const float v0 = conic_form(rA0.z, rA0.w, rB0.x, dx0, dy0, q0, q1);
-                    const float v1 = conic_form(rA1.z, rA1.w, rB1.x, dx1, dy1, q0, q1);
-                    const bool k0 = !(v0 > rB0.y || v0 <= 0.0f);
-                    const bool k1 = !(v1 > rB1.y || v1 <= 0.0f);
-                    if (k0 && !blend(j, dx0, dy0, v0)) {
-                        done = true;
-                        break;
+                // the warp's own entries (its bitmap), two per iteration: both
+                // quadratic forms are evaluated before the (mostly rejecting)
+                // branches, in list order
+                for (int g = 0; g * 32 < cnt && !done; ++g) {
+                    uint32_t bits = sb.bm[wq][g];
+                    while (bits) {
+                        const int j0 = g * 32 + __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        if (bits) {
+                            const int j1 = g * 32 + __ffs(bits) - 1;
+                            bits &= bits - 1;
+                            const float4 rA0 = sb.A[j0], rA1 = sb.A[j1];
+                            const float2 rB0 = *reinterpret_cast<const float2*>(&sb.B[j0]);
+                            const float2 rB1 = *reinterpret_cast<const float2*>(&sb.B[j1]);
+                            const float dx0 = rA0.x - xf, dy0 = rA0.y - yf;
+                            const float dx1 = rA1.x - xf, dy1 = rA1.y - yf;
+                            float q0, q1;
+                            const float v0 = conic_form(rA0.z, rA0.w, rB0.x, dx0, dy0, q0, q1);
+                            const float v1 = conic_form(rA1.z, rA1.w, rB1.x, dx1, dy1, q0, q1);
+                            const bool k0 = !(v0 > rB0.y || v0 <= 0.0f);
+                            const bool k1 = !(v1 > rB1.y || v1 <= 0.0f);
+                            if (k0 && !blend(j0, dx0, dy0, v0)) {
+                                done = true;
+                                break;
+                            }
+                            if (k1 && !blend(j1, dx1, dy1, v1)) {
+                                done = true;
+                                break;
+                            }
+                        } else {
+                            const float4 rA = sb.A[j0];
+                            const float2 rB = *reinterpret_cast<const float2*>(&sb.B[j0]);
+                            const float dx = rA.x - xf, dy = rA.y - yf;
+                            float q0, q1;
+                            const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, q0, q1);
+                            if (!(v > rB.y || v <= 0.0f) && !blend(j0, dx, dy, v)) {
+                                done = true;
+                                break;
+                            }
+                        }
                     }
-                    if (k1 && !blend(j + 1, dx1, dy1, v1)) {
-                        done = true;
-                        break;
-                    }
-                }
-                if (!done && j < cnt) {
-                    const float4 rA = sb.A[j];
-                    const float2 rB = *reinterpret_cast<const float2*>(&sb.B[j]);
-                    const float dx = rA.x - xf, dy = rA.y - yf;
-                    float q0, q1;
-                    const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, q0, q1);
-                    if (!(v > rB.y || v <= 0.0f) && !blend(j, dx, dy, v)) done = true;
                 }
                 if (last_j >= 0) last = (uint32_t)sb.orig[last_j] + 1u;
             }
@@ -763,11 +838,6 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
         // the staged derivatives; jd is the derivative of
         // d = z + dx phat.x + dy phat.y of the Gaussian where T crosses 0.5.
         float jc[3][6], jd[6];
-        float jcc[COMP ? 3 : 1][COMP ? 6 : 1];  // Kahan carries of jc (precision form)
-        if constexpr (COMP) {
-#pragma unroll
-            for (int k = 0; k < 6; ++k) jcc[0][k] = jcc[1][k] = jcc[2][k] = 0.f;
-        }
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             jc[0][k] = jc[1][k] = jc[2][k] = 0.f;
@@ -778,96 +848,11 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
         for (int base = 0; base < nmax; base += BATCH) {
             if (__syncthreads_and(done2)) break;
             const int cnt = stage_batch<false, true, kStageDeriv, TW, TH>(a, sb, range.x, base, nmax, x0, y0);
+            build_warp_bitmaps(sb, cnt);
             if (done2) continue;
-            for (int j = 0; j < cnt; ++j) {
-                if (sb.orig[j] >= (int)n_contrib) {
-                    done2 = true;
-                    break;
-                }
-                const float4 rA = sb.A[j];
-                const float4 rB = sb.B[j];
-                const float dx = rA.x - xf, dy = rA.y - yf;
-                float dl0, dl1;
-                const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
-                if (v > rB.y || v <= 0.0f) continue;
-                const float raw = gauss_weight(rB.z, v);
-                const float alpha = fminf(0.99f, raw);
-                if (alpha < kInv255) continue;
-                const float4 rC = sb.C[j];
-                float d0 = rC.z * prod, d1 = rC.w * prod, d2 = sb.D[j] * prod;
-                remr -= alpha * d0;
-                remg -= alpha * d1;
-                remb -= alpha * d2;
-                const float inv1m = rcp_approx(1.0f - alpha);
-                const float kf = (raw > 0.99f) ? 0.0f : -0.5f * alpha;
-                const float k0 = kf * (d0 - remr * inv1m), k1 = kf * (d1 - remg * inv1m),
-                            k2 = kf * (d2 - remb * inv1m);
-                const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
-                const float4 X0 = sb.X[0][j], X1 = sb.X[1][j], X2 = sb.X[2][j], X3 = sb.X[3][j];
-                const float4 X4 = sb.X[4][j], X5 = sb.X[5][j], X6 = sb.X[6][j], X7 = sb.X[7][j];
-                const float du[6] = {X0.x, X0.y, X0.z, X0.w, X1.x, X1.y};
-                const float dv[6] = {X1.z, X1.w, X2.x, X2.y, X2.z, X2.w};
-                const float da[6] = {X3.x, X3.y, X3.z, X3.w, X4.x, X4.y};
-                const float db[6] = {X4.z, X4.w, X5.x, X5.y, X5.z, X5.w};
-                const float dc[6] = {X6.x, X6.y, X6.z, X6.w, X7.x, X7.y};
-                float gv[6];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    gv[k] = cu * du[k] + cv * dv[k] + ca * da[k] + cb2 * db[k] + cc * dc[k];
-                    if constexpr (COMP) {
-                        kahan_add(jc[0][k], jcc[0][k], k0 * gv[k]);
-                        kahan_add(jc[1][k], jcc[1][k], k1 * gv[k]);
-                        kahan_add(jc[2][k], jcc[2][k], k2 * gv[k]);
-                    } else {
-                        jc[0][k] += k0 * gv[k];
-                        jc[1][k] += k1 * gv[k];
-                        jc[2][k] += k2 * gv[k];
-                    }
-                }
-                const float np = prod * (1.0f - alpha);
-                if (prod > 0.5f && np < 0.5f) {
-                    // d phat = (dp_x / z^2 - 2 x dp_z / z^3, dp_y / z^2 - 2 y dp_z / z^3)
-                    const float z = rB.w, x = X7.z, y = X7.w;
-                    const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) {
-                        const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
-                        const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
-                        const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
-                        const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
-                        const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
-                        jd[k] = dpz + rC.x * du[k] + dx * dphx + rC.y * dv[k] + dy * dphy;
-                    }
-                }
-                prod = np;
-            }
-        }
-        if (do_jac) {
-            int idx = 0;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-#pragma unroll
-                for (int k = i; k < 6; ++k)
-                    A[idx++] = wc * (jc[0][i] * jc[0][k] + jc[1][i] * jc[1][k] + jc[2][i] * jc[2][k]) +
-                               wd * jd[i] * jd[k];
-                bv[i] = -(wc * (jc[0][i] * e0 + jc[1][i] * e1 + jc[2][i] * e2) + wd * jd[i] * derr);
-            }
-        }
-    } else {
-        // rem = final colour minus the colour accumulated so far (running)
-        float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
-        bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
-        bool done2 = !do_jac;
-        if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
-        for (int base = 0; base < nmax; base += BATCH) {
-            if (__syncthreads_and(done2)) break;
-            int cnt;
-            if constexpr (TMA)
-                cnt = stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm);
-            else
-                cnt = stage_batch<REF_LAYOUT, false, kStageRay, TW, TH>(a, sb, range.x, base, nmax, x0, y0);
-            if (!done2) {
-                for (int j = 0; j < cnt; ++j) {
+            for (int g = 0; g * 32 < cnt && !done2; ++g) {
+                for (uint32_t bits = sb.bm[wq][g]; bits; bits &= bits - 1) {
+                    const int j = g * 32 + __ffs(bits) - 1;
                     if (sb.orig[j] >= (int)n_contrib) {
                         done2 = true;
                         break;
@@ -877,66 +862,153 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                     const float dx = rA.x - xf, dy = rA.y - yf;
                     float dl0, dl1;
                     const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
-                    if (v > rB.y) continue;
-                    const float alpha = gauss_alpha(rB.z, v);
+                    if (v > rB.y || v <= 0.0f) continue;
+                    const float raw = gauss_weight(rB.z, v);
+                    const float alpha = fminf(0.99f, raw);
                     if (alpha < kInv255) continue;
                     const float4 rC = sb.C[j];
-                    const float4 rE = sb.X[0][j];
-                    const float d = depth_fast(rB.w, dx, rC.x, dy, rC.y, rA.x, xf, rA.y, yf);
-                    float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
-                    remr -= alpha * da0;
-                    remg -= alpha * da1;
-                    remb -= alpha * da2;
+                    float d0 = rC.z * prod, d1 = rC.w * prod, d2 = sb.D[j] * prod;
+                    remr -= alpha * d0;
+                    remg -= alpha * d1;
+                    remb -= alpha * d2;
                     const float inv1m = rcp_approx(1.0f - alpha);
-                    da0 -= remr * inv1m;
-                    da1 -= remg * inv1m;
-                    da2 -= remb * inv1m;
-                    // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
-                    // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
-                    // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
-                    const float g0 = fx * dl0, g1 = fy * dl1, g2 = rE.z * dl0 + rE.w * dl1;
-                    const float inv_d = rcp_approx(d);
-                    const float u0 = g0 * inv_d, u1 = g1 * inv_d, u2 = g2 * inv_d;
-                    const float u3 = rE.y * g2 - g1, u4 = g0 - rE.x * g2, u5 = rE.x * g1 - rE.y * g0;
-                    const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
-                    {
-                        const float u[6] = {u0, u1, u2, u3, u4, u5};
-                        int idx = 0;
+                    const float kf = (raw > 0.99f) ? 0.0f : -0.5f * alpha;
+                    const float k0 = kf * (d0 - remr * inv1m), k1 = kf * (d1 - remg * inv1m),
+                                k2 = kf * (d2 - remb * inv1m);
+                    const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
+                    const float4 X0 = sb.X[0][j], X1 = sb.X[1][j], X2 = sb.X[2][j], X3 = sb.X[3][j];
+                    const float4 X4 = sb.X[4][j], X5 = sb.X[5][j], X6 = sb.X[6][j], X7 = sb.X[7][j];
+                    const float du[6] = {X0.x, X0.y, X0.z, X0.w, X1.x, X1.y};
+                    const float dv[6] = {X1.z, X1.w, X2.x, X2.y, X2.z, X2.w};
+                    const float da[6] = {X3.x, X3.y, X3.z, X3.w, X4.x, X4.y};
+                    const float db[6] = {X4.z, X4.w, X5.x, X5.y, X5.z, X5.w};
+                    const float dc[6] = {X6.x, X6.y, X6.z, X6.w, X7.x, X7.y};
+                    float gv[6];
     #pragma unroll
-                        for (int i = 0; i < 6; ++i) {
-                            const float wu = w * u[i];
+                    for (int k = 0; k < 6; ++k) {
+                        gv[k] = cu * du[k] + cv * dv[k] + ca * da[k] + cb2 * db[k] + cc * dc[k];
+                        jc[0][k] += k0 * gv[k];
+                        jc[1][k] += k1 * gv[k];
+                        jc[2][k] += k2 * gv[k];
+                    }
+                    const float np = prod * (1.0f - alpha);
+                    if (prod > 0.5f && np < 0.5f) {
+                        // d phat = (dp_x / z^2 - 2 x dp_z / z^3, dp_y / z^2 - 2 y dp_z / z^3)
+                        const float z = rB.w, x = X7.z, y = X7.w;
+                        const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
     #pragma unroll
-                            for (int k = i; k < 6; ++k) A[idx++] += wu * u[k];
+                        for (int k = 0; k < 6; ++k) {
+                            const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
+                            const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
+                            const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
+                            const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
+                            const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
+                            jd[k] = dpz + rC.x * du[k] + dx * dphx + rC.y * dv[k] + dy * dphy;
                         }
                     }
-                    const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
-                    bv[0] += coef * u0;
-                    bv[1] += coef * u1;
-                    bv[2] += coef * u2;
-                    bv[3] += coef * u3;
-                    bv[4] += coef * u4;
-                    bv[5] += coef * u5;
-                    prod_alpha *= (1.0f - alpha);
-                    if (depth_pending && prod_alpha <= 0.5f) {
-                        // the depth term wd * derr * r: its rotation part d (r x r) is zero
-                        depth_pending = false;
-                        const float r[3] = {rE.x, rE.y, 1.0f};
-                        int idx = 0;
+                    prod = np;
+                }
+                }
+            }
+            if (do_jac) {
+                int idx = 0;
     #pragma unroll
-                        for (int i = 0; i < 3; ++i) {
+                for (int i = 0; i < 6; ++i) {
     #pragma unroll
-                            for (int jj = i; jj < 6; ++jj) {
-                                if (jj < 3) A[idx] += wd * r[i] * r[jj];
-                                ++idx;
+                    for (int k = i; k < 6; ++k)
+                        A[idx++] = wc * (jc[0][i] * jc[0][k] + jc[1][i] * jc[1][k] + jc[2][i] * jc[2][k]) +
+                                   wd * jd[i] * jd[k];
+                    bv[i] = -(wc * (jc[0][i] * e0 + jc[1][i] * e1 + jc[2][i] * e2) + wd * jd[i] * derr);
+                }
+            }
+        } else {
+            // rem = final colour minus the colour accumulated so far (running)
+            float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
+            bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
+            bool done2 = !do_jac;
+            if (TMA) tma_begin(a, maps, ts, range.x, nmax, tm);
+            for (int base = 0; base < nmax; base += BATCH) {
+                if (__syncthreads_and(done2)) break;
+                int cnt;
+                if constexpr (TMA)
+                    cnt = stage_batch_tma<false>(a, maps, sb, ts, range.x, base, nmax, x0, y0, tm);
+                else
+                    cnt = stage_batch<REF_LAYOUT, false, kStageRay, TW, TH>(a, sb, range.x, base, nmax, x0, y0);
+                build_warp_bitmaps(sb, cnt);
+                if (!done2) {
+                    for (int g = 0; g * 32 < cnt && !done2; ++g) {
+                        for (uint32_t bits = sb.bm[wq][g]; bits; bits &= bits - 1) {
+                            const int j = g * 32 + __ffs(bits) - 1;
+                        if (sb.orig[j] >= (int)n_contrib) {
+                            done2 = true;
+                            break;
+                        }
+                        const float4 rA = sb.A[j];
+                        const float4 rB = sb.B[j];
+                        const float dx = rA.x - xf, dy = rA.y - yf;
+                        float dl0, dl1;
+                        const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
+                        if (v > rB.y) continue;
+                        const float alpha = gauss_alpha(rB.z, v);
+                        if (alpha < kInv255) continue;
+                        const float4 rC = sb.C[j];
+                        const float4 rE = sb.X[0][j];
+                        const float d = depth_fast(rB.w, dx, rC.x, dy, rC.y, rA.x, xf, rA.y, yf);
+                        float da0 = rC.z * prod_alpha, da1 = rC.w * prod_alpha, da2 = sb.D[j] * prod_alpha;
+                        remr -= alpha * da0;
+                        remg -= alpha * da1;
+                        remb -= alpha * da2;
+                        const float inv1m = rcp_approx(1.0f - alpha);
+                        da0 -= remr * inv1m;
+                        da1 -= remg * inv1m;
+                        da2 -= remb * inv1m;
+                        // The reference's per-Gaussian row is u = (jt, d (r x jt)) with
+                        // jt = g / d, g = (fx dl0, fy dl1, -fx rgx dl0 - fy rgy dl1) and
+                        // r = (rgx, rgy, 1): the same vector as (g / d, r x g).
+                        const float g0 = fx * dl0, g1 = fy * dl1, g2 = rE.z * dl0 + rE.w * dl1;
+                        const float inv_d = rcp_approx(d);
+                        const float u0 = g0 * inv_d, u1 = g1 * inv_d, u2 = g2 * inv_d;
+                        const float u3 = rE.y * g2 - g1, u4 = g0 - rE.x * g2, u5 = rE.x * g1 - rE.y * g0;
+                        const float w = wc * alpha * alpha * (da0 * da0 + da1 * da1 + da2 * da2);
+                        {
+                            const float u[6] = {u0, u1, u2, u3, u4, u5};
+                            int idx = 0;
+        #pragma unroll
+                            for (int i = 0; i < 6; ++i) {
+                                const float wu = w * u[i];
+        #pragma unroll
+                                for (int k = i; k < 6; ++k) A[idx++] += wu * u[k];
                             }
                         }
-                        bv[0] += wd * derr * rE.x;
-                        bv[1] += wd * derr * rE.y;
-                        bv[2] += wd * derr;
-                    }
-                    if (prod_alpha < 0.001f) {
-                        done2 = true;
-                        break;
+                        const float coef = -wc * alpha * (da0 * e0 + da1 * e1 + da2 * e2);
+                        bv[0] += coef * u0;
+                        bv[1] += coef * u1;
+                        bv[2] += coef * u2;
+                        bv[3] += coef * u3;
+                        bv[4] += coef * u4;
+                        bv[5] += coef * u5;
+                        prod_alpha *= (1.0f - alpha);
+                        if (depth_pending && prod_alpha <= 0.5f) {
+                            // the depth term wd * derr * r: its rotation part d (r x r) is zero
+                            depth_pending = false;
+                            const float r[3] = {rE.x, rE.y, 1.0f};
+                            int idx = 0;
+        #pragma unroll
+                            for (int i = 0; i < 3; ++i) {
+        #pragma unroll
+                                for (int jj = i; jj < 6; ++jj) {
+                                    if (jj < 3) A[idx] += wd * r[i] * r[jj];
+                                    ++idx;
+                                }
+                            }
+                            bv[0] += wd * derr * rE.x;
+                            bv[1] += wd * derr * rE.y;
+                            bv[2] += wd * derr;
+                        }
+                        if (prod_alpha < 0.001f) {
+                            done2 = true;
+                            break;
+                        }
                     }
                 }
             }

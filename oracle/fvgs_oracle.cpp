@@ -7,11 +7,15 @@
  * compared against, and the timed CPU baseline.  No product code path may
  * call it.
  *
- * PARITY STATUS: parity unpinned by reference outputs.  The reference ships no
- * tests, golden vectors or fixtures, and its implementation cannot be built or
- * run here (its device code needs Eigen, its host code OpenCV-CUDA, Ceres and
- * ROS 2).  This restatement is pinned instead by known-answer tests derived by
- * hand from the reference source (tests/test_oracle_kat.py).
+ * PARITY STATUS: the binning is pinned to the reference's own code.  The
+ * reference ships no tests, golden vectors or fixtures and cannot be built
+ * whole here (its device code needs Eigen, its host code OpenCV-CUDA, Ceres
+ * and ROS 2), but its binning kernels can: oracle/ref_build.py compiles them
+ * from its sources for the host (compared with this file's no-FMA build in
+ * every field, tests/test_ref_pin.py) and with nvcc for the GPU (keys, sorted
+ * indices and ranges compared bit for bit, tests/test_ref_pin_gpu.py).  The
+ * FP64 paths downstream are pinned by known-answer tests derived by hand from
+ * the reference source (tests/test_oracle_kat.py) and by finite differences.
  *
  * Two precisions:
  *  - FP32, reference operation order, for projection, tile counts and tile
@@ -43,7 +47,9 @@ namespace {
 // default --fmad=true: a multiply feeding an add becomes one FMA, and in a sum
 // of two products the first product is fused: a*b + c*d = fma(a, b, c*d),
 // a*b - c*d = fma(a, b, -(c*d)), a*b + c*d + e*f = fma(e, f, fma(a, b, c*d)),
-// acc += a*b*c = fma(a*b, c, acc).  Built with FVGS_ORACLE_NO_FMA every
+// acc += a*b*c = fma(a*b, c, acc); the tile-centre depth of the keys,
+// z + a*b + c*d, is fma(a, b, z) + c*d (oracle_emit_keys; matched against the
+// keys of the reference's nvcc build).  Built with FVGS_ORACLE_NO_FMA every
 // product and sum rounds on its own instead (what the reference's source
 // gives compiled with contraction off; oracle/ref_host.cpp).
 #ifndef FVGS_ORACLE_NO_FMA
