@@ -235,33 +235,90 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
     }
 }
 
-// Grid-stride over the Gaussians with the next position and previous count
-// loaded one step ahead: only the position decides visibility, so the
-// dependent-load chain of one thread is short and overlapped.
-__global__ void __launch_bounds__(256) project_count_kernel(ProjectArgs a) {
+// Whether Gaussian i at position p lands in the image (the reference's
+// culling, src/GSCudaKernels.cu:381,391), with project_one's arithmetic.
+__device__ __forceinline__ bool in_view(const ProjectArgs& a, float4 p, const float (&R)[3][3], const float (&tw)[3]) {
+    const float d0 = __fsub_rn(p.x, tw[0]);
+    const float d1 = __fsub_rn(p.y, tw[1]);
+    const float d2 = __fsub_rn(p.z, tw[2]);
+    const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[0][0], d0, __fmul_rn(R[1][0], d1)));
+    const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[0][1], d0, __fmul_rn(R[1][1], d1)));
+    const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[0][2], d0, __fmul_rn(R[1][2], d1)));
+    if (!(pcz > 0.0f)) return false;
+    const float inv_z = __fdiv_rn(1.0f, pcz);
+    const float uu = __fmaf_rn(a.K.fx, __fmul_rn(pcx, inv_z), a.K.cx);
+    const float vv = __fmaf_rn(a.K.fy, __fmul_rn(pcy, inv_z), a.K.cy);
+    return !(uu < 0.0f || uu >= (float)a.W || vv < 0.0f || vv >= (float)a.H);
+}
+
+// Chunks of kProjChunk Gaussians per CTA round.  Phase 1: every thread loads
+// the positions (and previous counts) of its Gaussians, all loads in flight
+// together, and culls them; a Gaussian out of view is finished right there
+// (count 0, its binning record cleared where it had instances), the others
+// are queued in shared memory.  Phase 2: the CTA runs project_one over the
+// queue with full warps -- most of a large map is out of view, so in Gaussian
+// order only a few lanes of a warp would take the projection's long path.
+// Queue order does not matter: every output is indexed by the Gaussian, the
+// tile counts are sums, and the changed list is consumed order-free.
+// Culled-slot binning and the debug outputs take project_one for every
+// Gaussian.
+constexpr int kProjThreads = 256, kProjPerThread = 2, kProjChunk = kProjThreads * kProjPerThread;
+
+__global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectArgs a) {
     pdl_begin();
+    __shared__ uint32_t q_i[kProjChunk], q_prev[kProjChunk];
+    __shared__ int q_n;
     const DevPose* P = a.pose;
     const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
     float R[3][3];
     quat_to_R(qc, R);
     const float tw[3] = {P->t[0], P->t[1], P->t[2]};
-    const int stride = gridDim.x * blockDim.x;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
-    uint32_t c_next = 0;
-    if (i < a.n) {
-        p_next = a.pos[i];
-        if (a.hist) c_next = a.counts[i];
-    }
-    for (; i < a.n; i += stride) {
-        const float4 p = p_next;
-        const uint32_t c = c_next;
-        const int j = i + stride;
-        if (j < a.n) {
-            p_next = a.pos[j];
-            if (a.hist) c_next = a.counts[j];
+    const bool all_slow = (a.quirks & FVGS_Q_CULLED_SLOTS) || a.dbg_cov;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * kProjChunk; base < a.n; base += gridDim.x * kProjChunk) {
+        if (threadIdx.x == 0) q_n = 0;
+        __syncthreads();
+        float4 p[kProjPerThread];
+        uint32_t c[kProjPerThread];
+#pragma unroll
+        for (int k = 0; k < kProjPerThread; ++k) {
+            const int i = base + k * kProjThreads + (int)threadIdx.x;
+            p[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            c[k] = 0;
+            if (i < a.n) {
+                p[k] = a.pos[i];
+                if (a.hist) c[k] = a.counts[i];
+            }
         }
-        project_one(a, i, p, c, R, tw);
+#pragma unroll
+        for (int k = 0; k < kProjPerThread; ++k) {
+            const int i = base + k * kProjThreads + (int)threadIdx.x;
+            const bool valid = i < a.n;
+            const bool queue = valid && (all_slow || in_view(a, p[k], R, tw));
+            if (valid && !queue && (!a.hist || c[k])) {
+                // out of view, no instances now: project_one's record for it
+                a.bins[i].r = make_uint4(0u, 0u, 0u, 0u);
+                a.counts[i] = 0;
+            }
+            const uint32_t bal = __ballot_sync(kFullMask, queue);
+            if (bal) {
+                const int leader = __ffs(bal) - 1;
+                int slot = 0;
+                if (lane == leader) slot = atomicAdd(&q_n, __popc(bal));
+                slot = __shfl_sync(kFullMask, slot, leader) + __popc(bal & lanemask_lt());
+                if (queue) {
+                    q_i[slot] = (uint32_t)i;
+                    q_prev[slot] = c[k];
+                }
+            }
+        }
+        __syncthreads();
+        const int nq = q_n;
+        for (int k = threadIdx.x; k < nq; k += kProjThreads) {
+            const uint32_t i = q_i[k];
+            project_one(a, (int)i, a.pos[i], q_prev[k], R, tw);
+        }
+        __syncthreads();  // the queue is consumed before the next chunk's
     }
 }
 
@@ -740,7 +797,7 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
 // ------------------------------- launchers ---------------------------------
 cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
-    const int need = (a.n + 255) / 256;
+    const int need = (a.n + kProjChunk - 1) / kProjChunk;
     return launch_chained(project_count_kernel, dim3(max_ctas > 0 && max_ctas < need ? max_ctas : need), dim3(256), 0,
                           s, a);
 }
