@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kMPix) map_forward_kernel(MapArgs a) {
 }
 
 template <bool CAP>
-__global__ void __launch_bounds__(kMPix) map_backward_kernel(MapArgs a) {
+__global__ void __launch_bounds__(kMPix, 4) map_backward_kernel(MapArgs a) {
     pdl_begin();
     __shared__ float4 s_pc[kMPix];  // final colour (incl. background), median depth
     __shared__ float4 s_pe[kMPix];  // colour error, observed depth
@@ -305,13 +305,16 @@ __global__ void __launch_bounds__(256) map_update_kernel(MapUpdateArgs a, const 
     // step with larger buffers, so the parameters must stay untouched.
     if (st->flags & kErrOverflow) return;
     const float4* D4 = reinterpret_cast<const float4*>(a.delta2d + (size_t)i * 16);
-    const float4 q0 = D4[0], q1 = D4[1], q2 = D4[2], q3 = D4[3];
+    // the contributor count first: most of a large map has no gradient, and
+    // then only this one sector of the record is read
+    const float4 q3 = D4[3];
     const uint32_t nn = __float_as_uint(q3.x);
     if (nn == 0) {
         if (a.dbg_delta3d)
             for (int k = 0; k < 16; ++k) a.dbg_delta3d[(size_t)i * 16 + k] = 0.f;
         return;
     }
+    const float4 q0 = D4[0], q1 = D4[1], q2 = D4[2];
     const float d_mean[2] = {q0.x, q0.y};
     const float d_inv[3] = {q0.z, q0.w, q1.x};
     const float d_col[3] = {q1.y, q1.z, q1.w};
