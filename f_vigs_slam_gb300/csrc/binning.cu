@@ -32,9 +32,11 @@ __device__ __forceinline__ void add_rect(int* d, int gw, int x0, int y0, int x1,
 }
 
 // One Gaussian: p is its position, prev_count its instance count in the
-// previous binning (incremental mode), R and tw the camera pose.
+// previous binning (incremental mode), R and tw the camera pose; grid: the
+// count and entering difference grids (a.tile_diff, or the CTA's copy in
+// shared memory).
 __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 p, uint32_t prev_count,
-                                            const float (&R)[3][3], const float (&tw)[3]) {
+                                            const float (&R)[3][3], const float (&tw)[3], int* grid) {
     const fvgs_intrinsics K = a.K;
 
     float u = 0.f, v = 0.f, z = 0.f, cxx = 0.f, cyy = 0.f, cxy = 0.f;
@@ -186,7 +188,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
     if (a.tile_diff) {
         const int gw = a.ntx + 1;
         const size_t cells = (size_t)gw * (a.nty + 1);
-        if (count) add_rect(a.tile_diff, gw, x0, y0, x1, y1);
+        if (count) add_rect(grid, gw, x0, y0, x1, y1);
         if (a.hist) {
             // instances entering a tile: the new rectangle minus the previous one
             uint32_t n_enter = 0;
@@ -194,7 +196,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
                 const EnterSplit es = enter_split(x0, y0, x1, y1, old_count != 0, (int)(old_r.x & 0xffffu),
                                                   (int)(old_r.x >> 16), (int)(old_r.y & 0xffffu), (int)(old_r.y >> 16));
                 n_enter = entering_count(es);
-                int* e = a.tile_diff + cells;
+                int* e = grid + cells;
                 if (es.whole) {
                     add_rect(e, gw, x0, y0, x1, y1);
                 } else {
@@ -263,11 +265,24 @@ __device__ __forceinline__ bool in_view(const ProjectArgs& a, float4 p, const fl
 // Culled-slot binning and the debug outputs take project_one for every
 // Gaussian.
 constexpr int kProjThreads = 256, kProjPerThread = 2, kProjChunk = kProjThreads * kProjPerThread;
+// Difference grids of at most this many cells (both grids together) are
+// accumulated in shared memory and added to the global ones once per CTA: at
+// the coarse pyramid levels every Gaussian in view adds its rectangle's
+// corners to a few dozen cells, and same-address global atomics from every
+// SM serialise (level 3 of a 1280x720 frame: 77 cells).
+constexpr int kProjSmemCells = 2048;
 
 __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectArgs a) {
     pdl_begin();
     __shared__ uint32_t q_i[kProjChunk], q_prev[kProjChunk];
     __shared__ int q_n;
+    __shared__ int s_grid[kProjSmemCells];
+    const int cells = a.tile_diff ? (a.ntx + 1) * (a.nty + 1) : 0;
+    const int grid_cells = (a.hist ? 2 : 1) * cells;
+    const bool smem_grid = a.tile_diff && grid_cells <= kProjSmemCells;
+    int* grid = smem_grid ? s_grid : a.tile_diff;
+    if (smem_grid)
+        for (int c = threadIdx.x; c < grid_cells; c += kProjThreads) s_grid[c] = 0;
     const DevPose* P = a.pose;
     const float qc[4] = {P->q[0], P->q[1], P->q[2], P->q[3]};
     float R[3][3];
@@ -316,9 +331,16 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
         const int nq = q_n;
         for (int k = threadIdx.x; k < nq; k += kProjThreads) {
             const uint32_t i = q_i[k];
-            project_one(a, (int)i, a.pos[i], q_prev[k], R, tw);
+            project_one(a, (int)i, a.pos[i], q_prev[k], R, tw, grid);
         }
         __syncthreads();  // the queue is consumed before the next chunk's
+    }
+    if (smem_grid) {
+        __syncthreads();
+        for (int c = threadIdx.x; c < grid_cells; c += kProjThreads) {
+            const int v = s_grid[c];
+            if (v) atomicAdd(&a.tile_diff[c], v);
+        }
     }
 }
 
