@@ -137,3 +137,36 @@ def test_batch_autotune(fvgs_lib):
         np.testing.assert_array_equal(p[1], q[1])
         err = S.pose_error(p, w["true"])
         assert err[0] <= POSE_TOL and err[1] <= POSE_TOL, err
+
+
+def test_batch_instance_overflow_and_reduced_precision(fvgs_lib):
+    """A session whose instance buffers overflow inside the batched frame is
+    repeated alone after they grow, and the batch still equals the plain
+    frames; a session in the precision form is refused (the persistent
+    kernel has no compensated variant)."""
+    fv = fvgs_lib
+    specs = [(150_000, S.CAM_HD), (60_000, S.CAM_VGA)]
+    ws = _sessions(fv, INTENDED, specs, 90)
+    try:
+        # splats three times larger: about ten times the instances, past the
+        # initial capacity of max(1 M, 8 N) instances
+        big = S.room(150_000, seed=90)
+        big.scales *= 3.0
+        ws[0]["s"].upload(big)
+        _level_frames(ws[0]["s"], ws[0]["true"], ws[0]["K0"], S.CAM_HD.width, S.CAM_HD.height,
+                      np.random.default_rng(91))
+        with fv.Batch([w["s"] for w in ws]) as bt:
+            got = [bt.run_pyramid([w["start"] for w in ws], [w["K0"] for w in ws], PYR) for _ in range(2)]
+            ws[1]["s"].set_precision(fv.PRECISION_REDUCED)
+            with pytest.raises(fv.FvgsError):
+                bt.run_pyramid([w["start"] for w in ws], [w["K0"] for w in ws], PYR)
+            ws[1]["s"].set_precision(fv.PRECISION_FP32)
+        assert ws[0]["s"].binning_info()["n_instances"] > 1_200_000
+        plain = [w["s"].track_frame_pyramid(w["start"], w["K0"], PYR)[0] for w in ws]
+    finally:
+        for w in ws:
+            w["s"].close()
+    for run in got:
+        for p, q in zip(run, plain):
+            np.testing.assert_array_equal(p[0], q[0])
+            np.testing.assert_array_equal(p[1], q[1])
