@@ -4,17 +4,19 @@ batched versus plain tracking frames/s, with p50/p99 latency and the pose
 error of every form.
 
 Every form tracks with the analytic pose Jacobian (all reference quirks off,
-FVGS_QUIRKS_INTENDED) and coarse-to-fine over four pyramid levels, the level
-loop of GSSlam::optimizeWithCeres: 6 + 6 + 4 + 4 = 20 Gauss-Newton
-iterations from level 3 down to level 0 (intrinsics scaled by 2^-level).
-The observed frame of every level is rendered at the true pose at that
-level's resolution, plus N(0,0.01) colour and N(0,0.005 m) depth noise
-(synthetic data; the reference names no dataset).  Where mapping steps
-change a map (the serving and large plain workloads), the frames a request
-tracks are rendered from the map as it stands at that request (replayed
-outside the timed region), so the observations follow the map the tracker
-sees.  The pose error criterion is 1e-4 rad and 1e-4 m after the 20
-iterations.
+FVGS_QUIRKS_INTENDED), 20 Gauss-Newton iterations per frame coarse-to-fine
+over the reference's pyramid (three levels, intrinsics scaled by 2^-level)
+and with its level range: a tracking frame stops at level 1 (levels 2, 1:
+10 + 10), a keyframe -- a frame followed by a mapping step -- goes down to
+level 0 (7 + 7 + 6); the small camera-box case, which starts 1 deg / 2 cm
+away, adds a coarser fourth level (6 + 6 + 4 + 4 from level 3).  The
+observed frame of every level is rendered at the true pose at that level's
+resolution, plus N(0,0.01) colour and N(0,0.005 m) depth noise (synthetic
+data; the reference names no dataset).  Where mapping steps change a map (the
+serving and large plain workloads), the frames a request tracks are rendered
+from the map as it stands at that request (replayed outside the timed
+region), so the observations follow the map the tracker sees.  The pose
+error criterion is 1e-4 rad and 1e-4 m after the 20 iterations.
 
 Serving workload (the `value`): sessions, each its own map of N Gaussians
 (log-uniform in [100k, 3M], room scenes), 640x480 or 1280x720 frames (fx =
@@ -22,15 +24,15 @@ fy = 525 / 1050), a random-walk trajectory (1 cm / 0.5 deg per frame); each
 frame starts from its predicted pose (the true pose perturbed by 0.05 deg /
 1 mm: the reference seeds every frame with the IMU prediction).  A
 request = one frame of one session = the 20 coarse-to-fine iterations
-(binning + fused Jacobian kernel + on-device 6x6 pseudo-factor step each),
-with a mapping step (forward, backward, 2D->3D, Adam) on every 10th frame of
-a session.  One step = one request per session.
+(binning + fused Jacobian kernel + on-device 6x6 pseudo-factor step each);
+every 10th frame of a session is a keyframe, followed by a mapping step
+(forward, backward, 2D->3D, Adam).  One step = one request per session.
  * value: the continuous-batching server (fvgs_server) with every
    session's requests in flight together and frames replayed from captured
    CUDA graphs, frames in HBM;
  * plain: the same requests one at a time through the plain per-frame path
    (fvgs_track_frame_pyramid / fvgs_map_step);
- * e2e: the server with each request carrying its four-level frame in one
+ * e2e: the server with each request carrying its three-level frame in one
    pinned host buffer (host->device copies inside the timed region);
  * p50/p99: request latency (arrival to result) of the server under Poisson
    arrivals, 30 Hz per session or 70% of the measured capacity if lower;
@@ -38,10 +40,12 @@ a session.  One step = one request per session.
 Beside it: `small_plain` (N = 50k camera-frame box, 640x480, target 1 deg /
 2 cm away: 20 iterations then a mapping step; also run whole in the CPU
 restatement, and with the reference's approximate Jacobian for contrast),
-`large_plain` (N = 1 M room, 1280x720, 20 iterations + a mapping step per
-frame; the roofline entry is its dominant kernel), `batching` (64 keyframes,
-N log-uniform in [20k, 2M], one fvgs_frames_run_pyramid call against
-sequential frames), `precision` (N = 2 M with BF16/FP16 attributes against
+`large_plain` (N = 1 M room, 1280x720, every frame a keyframe: 20 iterations
++ a mapping step; the roofline entry is its dominant kernel), `batching` (64
+keyframes, N log-uniform in [20k, 2M], one fvgs_batch_run_pyramid call --
+one persistent launch per iteration -- against sequential frames and
+per-keyframe graphs on streams), `precision` (N = 2 M, keyframe schedule,
+with BF16/FP16 attributes against
 FP32, and the visual-inertial solve with 200 Hz IMU data) and `maintenance`
 (outlier removal, covisibility, prune on the 1 M map).
 
@@ -73,14 +77,24 @@ sys.path.insert(0, ROOT)
 METRIC = "tracking frames/s & p99 latency, served+batched vs plain, 1 GB300, same pose err"
 N_GAUSS = 1_000_000
 QUIRKS = 0               # FVGS_QUIRKS_INTENDED: analytic pose Jacobian, every reference quirk off
-PYR = (4, 4, 6, 6)       # Gauss-Newton iterations at pyramid levels 0..3, run from level 3 down
+# Gauss-Newton iterations per pyramid level (index = level, run from the
+# coarsest down), 20 per frame.  Room frames use the reference's three levels
+# (nb_pyr_levels_ = 3, include/f_vigs_slam/GSSlam.cuh:275) and its level
+# range: a tracking frame stops at level 1 (GSSlam::compute calls
+# optimizeWithCeres(1, ...), src/GSSlam.cu:925), a keyframe -- here a frame
+# with a mapping step -- goes down to level 0 (src/GSSlam.cu:947).  The small
+# camera-box case starts 1 deg / 2 cm away and adds a fourth, coarser level.
+PYR_REG = (0, 10, 10)
+PYR_KEY = (6, 7, 7)
+PYR_SMALL = (4, 4, 6, 6)
+ROOM_LEVELS = 3
 # Initial pose of a room frame: the reference seeds every frame with the IMU
 # prediction (GSSlam::compute, src/GSSlam.cu:880-897); modelled as the true
 # pose perturbed by 0.05 deg / 1 mm in random directions (a tenth of a
 # trajectory step, above the error of preintegrating the configured IMU noise
 # over one 33 ms frame interval).
 PRED_DEG, PRED_CM = 0.05, 0.1
-ITERS = sum(PYR)
+ITERS = 20
 POSE_TOL = 1e-4          # rad and m
 ETA = 0.002
 # serving configuration
@@ -122,7 +136,12 @@ def dist_info():
 # ----------------------------------------------------------------------------
 # workload
 # ----------------------------------------------------------------------------
-def level_dims(W, H, levels=len(PYR)):
+def sched(eta):
+    """The level schedule of a room frame: a keyframe (mapping step) down to level 0, else to level 1."""
+    return PYR_KEY if eta is not None else PYR_REG
+
+
+def level_dims(W, H, levels=ROOM_LEVELS):
     """Frame sizes of the pyramid levels (cv::pyrDown's (n + 1) / 2)."""
     out, w, h = [], W, H
     for _ in range(levels):
@@ -138,12 +157,12 @@ def level_K(K0, level):
     return tuple(float(np.float32(k) * sc) for k in K0)
 
 
-def render_pyramid(S, sess, pose, K0, W, H, rng):
+def render_pyramid(S, sess, pose, K0, W, H, rng, levels=ROOM_LEVELS):
     """Observed frames of every level: the session's render at `pose` at that
     level's resolution, + N(0,0.01) colour / N(0,0.005 m) depth noise, Sobel
     gradients.  Level 0 first."""
     out = []
-    for lv, (w, h) in enumerate(level_dims(W, H)):
+    for lv, (w, h) in enumerate(level_dims(W, H, levels)):
         col, dep, _, _ = sess.render(pose, level_K(K0, lv), w, h)
         rgb, d = S.add_noise(col, dep, rng)
         gx, gy = S.sobel3(rgb)
@@ -167,14 +186,14 @@ def set_frame_tensors(fvgs, sess, level, fr, W, H):
 
 
 def set_pyramid(fvgs, sess, pyr, W, H):
-    for lv, (w, h) in enumerate(level_dims(W, H)):
+    for lv, (w, h) in enumerate(level_dims(W, H, len(pyr))):
         set_frame_tensors(fvgs, sess, lv, pyr[lv], w, h)
 
 
-def packed_levels(packed, W, H):
+def packed_levels(packed, W, H, levels=ROOM_LEVELS):
     """Per-level views {rgb, depth, gx, gy} of a pack_pyramid buffer (level 0 first)."""
     out, off = [], 0
-    for w, h in level_dims(W, H):
+    for w, h in level_dims(W, H, levels):
         P = w * h
         lv = {}
         for k, n in (("rgb", 3 * P), ("depth", P), ("gx", 3 * P), ("gy", 3 * P)):
@@ -217,7 +236,7 @@ def make_workload(fvgs, S, torch, dev, sess, n_frames, seed, map_eta=None, world
         frames.append(f)
         if map_eta is not None:
             set_pyramid(fvgs, sess, f["dev"], W, H)
-            pose, _ = sess.track_frame_pyramid(f["prev"], K, PYR)
+            pose, _ = sess.track_frame_pyramid(f["prev"], K, sched(map_eta))
             sess.map_step(pose, K, map_eta)
     if map_eta is not None:
         sess.upload(world)
@@ -239,9 +258,9 @@ def serving_sessions(n_sessions, seed=SERVE_SEED):
 def serving_config(n_sessions):
     return {"workload": ("serving: %d sessions, maps of 100k-3M Gaussians (log-uniform, room scenes), 640x480 / "
                          "1280x720 frames; a request = one frame of one session = 20 Gauss-Newton iterations "
-                         "coarse-to-fine (levels 3..0: %d/%d/%d/%d) with the analytic pose Jacobian, plus a "
-                         "mapping step every %d-th frame; one step = one request per session"
-                         % ((n_sessions,) + tuple(reversed(PYR)) + (MAP_EVERY,))),
+                         "coarse-to-fine with the analytic pose Jacobian (levels 2, 1: %d/%d; every %d-th frame a "
+                         "keyframe: levels 2, 1, 0: %d/%d/%d, then a mapping step); one step = one request per "
+                         "session" % ((n_sessions, PYR_REG[2], PYR_REG[1], MAP_EVERY) + tuple(reversed(PYR_KEY)))),
             "quirks": "FVGS_QUIRKS_INTENDED (analytic pose Jacobian, Tukey depth weight, every reference quirk off)",
             "initial_pose": "the predicted pose: the true pose perturbed by %.2f deg / %.1f mm (the reference seeds "
                             "each frame with the IMU prediction)" % (PRED_DEG, 10 * PRED_CM),
@@ -399,17 +418,19 @@ def replica_throughput(steps, world, max_ms):
 # ----------------------------------------------------------------------------
 # CPU baseline (the CPU restatement of the reference, FP64, all host threads)
 # ----------------------------------------------------------------------------
-def cpu_pyramid_frame(O, S, scene, start, frames, K0, W, H, P, map_eta=None):
+def cpu_pyramid_frame(O, S, scene, start, frames, K0, W, H, P, map_eta=None, schedule=None):
     """One whole frame in the CPU restatement: the 20 coarse-to-fine
-    iterations of binning + Jacobian + pseudo-factor Gauss-Newton step, then
-    optionally the mapping step at the tracked pose.  frames: per level
-    (rgb, depth, gx, gy).  Returns the tracked pose (FP64)."""
+    iterations of binning + Jacobian + pseudo-factor Gauss-Newton step (the
+    frame's level schedule), then optionally the mapping step at the tracked
+    pose.  frames: per level (rgb, depth, gx, gy).  Returns the tracked pose
+    (FP64)."""
+    pyr = schedule if schedule is not None else sched(map_eta)
     pose = (np.asarray(start[0], np.float64), np.asarray(start[1], np.float64))
-    dims = level_dims(W, H)
-    for lv in reversed(range(len(PYR))):
+    dims = level_dims(W, H, len(pyr))
+    for lv in reversed(range(len(pyr))):
         K = level_K(K0, lv)
         w, h = dims[lv]
-        for _ in range(PYR[lv]):
+        for _ in range(pyr[lv]):
             pf = (pose[0].astype(np.float32), pose[1].astype(np.float32))
             b = O.prepare(scene, pf, K, w, h, P)
             r = O.track(b, frames[lv], pf, K, w, h, P, images=False)
@@ -421,10 +442,10 @@ def cpu_pyramid_frame(O, S, scene, start, frames, K0, W, H, P, map_eta=None):
     return pose
 
 
-def cpu_oracle_pyramid(O, S, scene, pose, K0, W, H, P, rng):
+def cpu_oracle_pyramid(O, S, scene, pose, K0, W, H, P, rng, levels=ROOM_LEVELS):
     """Observed frames of every level rendered by the oracle at `pose` (+ noise)."""
     out = []
-    for lv, (w, h) in enumerate(level_dims(W, H)):
+    for lv, (w, h) in enumerate(level_dims(W, H, levels)):
         K = level_K(K0, lv)
         b = O.prepare(scene, pose, K, w, h, P)
         col, dep, _, _ = O.render(b, pose, K, w, h, P)
@@ -527,7 +548,7 @@ def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
     sess = fvgs.Session(scene.n, W, H, fvgs.default_params(QUIRKS), device=dev.index or 0)
     sess.set_stream(stream.cuda_stream)
     sess.upload(scene)
-    pyr = render_pyramid(S, sess, true_pose, K, W, H, rng)
+    pyr = render_pyramid(S, sess, true_pose, K, W, H, rng, levels=len(PYR_SMALL))
     set_pyramid(fvgs, sess, to_device(torch, dev, pyr), W, H)
     ms, poses = [], []
     for i in range(args.warmup + args.steps):
@@ -535,7 +556,7 @@ def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        pose, _ = sess.track_frame_pyramid(start, K, PYR)
+        pose, _ = sess.track_frame_pyramid(start, K, PYR_SMALL)
         sess.map_step(pose, K, ETA)
         e1.record(stream)
         torch.cuda.synchronize()
@@ -550,12 +571,12 @@ def run_small(args, fvgs, S, torch, dev, stream, world, with_cpu):
     ref.set_stream(stream.cuda_stream)
     ref.upload(scene)
     set_pyramid(fvgs, ref, to_device(torch, dev, pyr), W, H)
-    ref_pose, _ = ref.track_frame_pyramid(start, K, PYR)
+    ref_pose, _ = ref.track_frame_pyramid(start, K, PYR_SMALL)
     ref.close()
     ref_err = S.pose_error(ref_pose, true_pose)
     out = {"workload": "cam-frame box N=50000, 640x480, target 1 deg / 2 cm away + noise; 20 GN iterations "
                        "coarse-to-fine (levels 3..0: %d/%d/%d/%d), then one mapping forward + backward step "
-                       "(fvgs_track_frame_pyramid + fvgs_map_step)" % tuple(reversed(PYR)),
+                       "(fvgs_track_frame_pyramid + fvgs_map_step)" % tuple(reversed(PYR_SMALL)),
            "gpu_ms_per_run": ms_run, "runs_per_s": replica_throughput(1, world, ms_run),
            "pose_error": {"rad": err[0], "m": err[1]},
            "reference_jacobian_pose_error": {"rad": ref_err[0], "m": ref_err[1],
@@ -585,7 +606,7 @@ def cpu_small_run(S, scene, start, pyr, K, W, H):
     P = O.default_params(QUIRKS)
     frames = [(lv["rgb"], lv["depth"], lv["gx"], lv["gy"]) for lv in pyr]
     t0 = time.perf_counter()
-    pose = cpu_pyramid_frame(O, S, scene, start, frames, K, W, H, P, ETA)
+    pose = cpu_pyramid_frame(O, S, scene, start, frames, K, W, H, P, ETA, schedule=PYR_SMALL)
     t = time.perf_counter() - t0
     return {"s_per_run": t, "cores": os.cpu_count() or 1, "kind": "port", "pose": pose,
             "sample": "the whole run (20 coarse-to-fine binnings, Jacobians and GN steps, 1 mapping step), FP64 "
@@ -627,7 +648,7 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
 
     def step(k, src):
         set_pyramid(fvgs, sess, src[k % len(src)], W, H)
-        pose, _ = sess.track_frame_pyramid(frames[k % len(frames)]["prev"], K, PYR)
+        pose, _ = sess.track_frame_pyramid(frames[k % len(frames)]["prev"], K, PYR_KEY)
         sess.map_step(pose, K, ETA)
         return pose
 
@@ -845,7 +866,7 @@ def run_precision(args, fvgs, S, torch, dev, stream, world):
 
         def step(k):
             set_pyramid(fvgs, sess, dframes[k], W, H)
-            return sess.track_frame_pyramid(frames[k]["prev"], K, PYR)[0]
+            return sess.track_frame_pyramid(frames[k]["prev"], K, PYR_KEY)[0]
 
         for k in range(args.warmup):
             step(k)
@@ -970,22 +991,22 @@ def run_batching(args, fvgs, S, torch, dev, world):
 
     bt = fvgs.Batch([w["sess"] for w in ws])
     load(0)
-    tuned, tuned_ms = bt.autotune([w["frames"][0]["prev"] for w in ws], [w["K"] for w in ws], PYR, reps=3)
+    tuned, tuned_ms = bt.autotune([w["frames"][0]["prev"] for w in ws], [w["K"] for w in ws], PYR_KEY, reps=3)
 
     def batched(k):
         load(k)
-        return bt.run_pyramid([w["frames"][k % 2]["prev"] for w in ws], [w["K"] for w in ws], PYR)
+        return bt.run_pyramid([w["frames"][k % 2]["prev"] for w in ws], [w["K"] for w in ws], PYR_KEY)
 
     def streams(k):
         load(k)
         return fvgs.frames_run_pyramid([w["sess"] for w in ws], [w["frames"][k % 2]["prev"] for w in ws],
-                                       [w["K"] for w in ws], PYR)
+                                       [w["K"] for w in ws], PYR_KEY)
 
     def sequential(k):
         out = []
         for w in ws:
             set_pyramid(fvgs, w["sess"], w["frames"][k % 2]["dev"], w["W"], w["H"])
-            out.append(w["sess"].track_frame_pyramid(w["frames"][k % 2]["prev"], w["K"], PYR)[0])
+            out.append(w["sess"].track_frame_pyramid(w["frames"][k % 2]["prev"], w["K"], PYR_KEY)[0])
         return out
 
     for k in range(max(4, args.warmup + 1)):  # both buffer parities of both frames captured
@@ -1065,7 +1086,7 @@ def serving_epochs(fvgs, S, torch, dev, ws, n_epochs):
     rendered from the untouched world instead, the frames after a mapping
     step would measure how far the mapping objective (photometric, depth,
     distortion and isotropy terms, Adam) moves a map that already is the
-    world.  Each frame's four levels are packed in one buffer in HBM and one
+    world.  Each frame's three levels are packed in one buffer in HBM and one
     in pinned host memory.  Sessions end reset to their world."""
     for w in ws:
         if len(w["epochs"]) >= n_epochs:
@@ -1089,7 +1110,7 @@ def serving_epochs(fvgs, S, torch, dev, ws, n_epochs):
             if e + 1 < n_epochs:
                 f = w["epochs"][e][(MAP_EVERY * e + MAP_EVERY - 1) % F]
                 set_pyramid(fvgs, sess, packed_levels(f["packed_dev"], W, H), W, H)
-                pose, _ = sess.track_frame_pyramid(f["prev"], K, PYR)
+                pose, _ = sess.track_frame_pyramid(f["prev"], K, PYR_KEY)
                 sess.map_step(pose, K, ETA)
         sess.upload(w["world"])
     torch.cuda.synchronize()
@@ -1106,7 +1127,7 @@ def serving_reset(fvgs, ws):
         for w in ws:
             f = w["epochs"][0][j % len(w["epochs"][0])]
             set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
-            w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR)
+            w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR_REG)
         for w in ws:
             w["sess"].frame_wait()
 
@@ -1139,7 +1160,7 @@ def run_serving(args, fvgs, S, torch, dev):
         for j, eta in enumerate(warm):
             f = w["epochs"][0][j % SERVE_FRAMES]
             set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
-            w["sess"].frame_submit_pyramid(f["prev"], w["K"], PYR, map_eta=eta)
+            w["sess"].frame_submit_pyramid(f["prev"], w["K"], sched(eta), map_eta=eta)
             w["sess"].frame_wait()
     torch.cuda.synchronize()
     reqs = serving_requests(ws, rounds, 0)
@@ -1152,7 +1173,7 @@ def run_serving(args, fvgs, S, torch, dev):
     for i, r, f, eta in reqs:
         w = ws[i]
         set_pyramid(fvgs, w["sess"], packed_levels(f["packed_dev"], w["W"], w["H"]), w["W"], w["H"])
-        pose, _ = w["sess"].track_frame_pyramid(f["prev"], w["K"], PYR)
+        pose, _ = w["sess"].track_frame_pyramid(f["prev"], w["K"], sched(eta))
         if eta is not None:
             w["sess"].map_step(pose, w["K"], eta)
         plain_errs.append(S.pose_error(pose, f["pose"]))
@@ -1178,9 +1199,9 @@ def run_serving(args, fvgs, S, torch, dev):
                             break
                         time.sleep(min(1e-3, t_start + arrivals[j] - now))
                     kw["t_arrival"] = t_start + arrivals[j]
-                # the request's four-level frame: from HBM (device-to-device copies) or pinned host memory
+                # the request's three-level frame: from HBM (device-to-device copies) or pinned host memory
                 src = f["packed"] if frames_key == "host" else f["packed_dev"]
-                sv.submit(slots[i], f["prev"], w["K"], map_eta=eta, tag=j, pyramid=PYR,
+                sv.submit(slots[i], f["prev"], w["K"], map_eta=eta, tag=j, pyramid=sched(eta),
                           pyramid_frames=(src.data_ptr(), w["W"], w["H"]), **kw)
             res = []
             while len(res) < len(reqs_):
@@ -1305,7 +1326,7 @@ def run_ours(args):
             "latency": srv["poisson"],
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": srv["h2d_bytes_per_round"],
                     "d2h_bytes_per_step": srv["d2h_bytes_per_round"],
-                    "path": "server requests carrying each frame's four pyramid levels in one pinned host buffer "
+                    "path": "server requests carrying each frame's three pyramid levels in one pinned host buffer "
                             "(fvgs_server_submit), copies inside the timed region"},
             "gpu_launches": srv["launches"],
             "graphed_frames": srv["graphed_frames"],
