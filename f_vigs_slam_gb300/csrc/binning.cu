@@ -238,14 +238,17 @@ __device__ __forceinline__ void project_one(const ProjectArgs& a, int i, float4 
 }
 
 // Whether Gaussian i at position p lands in the image (the reference's
-// culling, src/GSCudaKernels.cu:381,391), with project_one's arithmetic.
-__device__ __forceinline__ bool in_view(const ProjectArgs& a, float4 p, const float (&R)[3][3], const float (&tw)[3]) {
+// culling, src/GSCudaKernels.cu:381,391), with project_one's arithmetic;
+// pc: its camera-frame position.
+__device__ __forceinline__ bool in_view(const ProjectArgs& a, float4 p, const float (&R)[3][3], const float (&tw)[3],
+                                        float3& pc) {
     const float d0 = __fsub_rn(p.x, tw[0]);
     const float d1 = __fsub_rn(p.y, tw[1]);
     const float d2 = __fsub_rn(p.z, tw[2]);
     const float pcx = __fmaf_rn(R[2][0], d2, __fmaf_rn(R[0][0], d0, __fmul_rn(R[1][0], d1)));
     const float pcy = __fmaf_rn(R[2][1], d2, __fmaf_rn(R[0][1], d0, __fmul_rn(R[1][1], d1)));
     const float pcz = __fmaf_rn(R[2][2], d2, __fmaf_rn(R[0][2], d0, __fmul_rn(R[1][2], d1)));
+    pc = make_float3(pcx, pcy, pcz);
     if (!(pcz > 0.0f)) return false;
     const float inv_z = __fdiv_rn(1.0f, pcz);
     const float uu = __fmaf_rn(a.K.fx, __fmul_rn(pcx, inv_z), a.K.cx);
@@ -272,6 +275,40 @@ constexpr int kProjThreads = 256, kProjPerThread = 2, kProjChunk = kProjThreads 
 // SM serialise (level 3 of a 1280x720 frame: 77 cells).
 constexpr int kProjSmemCells = 2048;
 
+// A list is built for the current view cone widened by this margin, so that
+// the pyramid levels of one camera (whose corner half-angles differ by a
+// fraction of a pixel) share it.
+constexpr float kCandConeMargin = 0.0174533f;  // 1 degree
+
+// Candidate test of a Gaussian at camera-frame position pc for the view cone
+// of half-angle cone: in it, widened by the largest rotation kCandMaxAngle
+// and by the bearing change asin(kCandMaxShift / |pc|) of the largest shift,
+// or within kCandNear of the camera.  A Gaussian in view at any pose within
+// that rotation and shift of this one, with a view cone no wider, passes:
+// its bearing at this pose is within cone + rotation + asin(shift / |pc|) of
+// the optical axis.  An extra 0.5 degree covers the FP32 evaluation.
+__device__ __forceinline__ bool candidate(float3 pc, float cone) {
+    const float r = sqrtf(pc.x * pc.x + pc.y * pc.y + pc.z * pc.z);
+    if (!(r > kCandNear)) return true;
+    const float ang = cone + kCandMaxAngle + 0.0087f + asinf(fminf(1.0f, kCandMaxShift / r));
+    if (ang >= 3.14159f) return true;
+    return pc.z >= r * cosf(ang);
+}
+
+// Whether the current pose is within the candidate list's bounds of the pose
+// the list was built at (rotation angle and shift), and the view cone no
+// wider: every Gaussian in view now is on the list.
+__device__ __forceinline__ bool cand_reusable(const CandState& c, const DevPose& P, float cone) {
+    if (!c.valid || !(cone <= c.cone)) return false;
+    const float dx = P.t[0] - c.t[0], dy = P.t[1] - c.t[1], dz = P.t[2] - c.t[2];
+    if (!(dx * dx + dy * dy + dz * dz <= kCandMaxShift * kCandMaxShift)) return false;
+    // angle between the two rotations: 2 acos |q0 . q1| for unit quaternions
+    const float n0 = c.q[0] * c.q[0] + c.q[1] * c.q[1] + c.q[2] * c.q[2] + c.q[3] * c.q[3];
+    const float n1 = P.q[0] * P.q[0] + P.q[1] * P.q[1] + P.q[2] * P.q[2] + P.q[3] * P.q[3];
+    const float d = c.q[0] * P.q[0] + c.q[1] * P.q[1] + c.q[2] * P.q[2] + c.q[3] * P.q[3];
+    return fabsf(d) * rsqrtf(n0 * n1) >= cosf(0.5f * kCandMaxAngle);
+}
+
 __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectArgs a) {
     pdl_begin();
     __shared__ uint32_t q_i[kProjChunk], q_prev[kProjChunk];
@@ -290,14 +327,33 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
     const float tw[3] = {P->t[0], P->t[1], P->t[2]};
     const bool all_slow = (a.quirks & FVGS_Q_CULLED_SLOTS) || a.dbg_cov;
     const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * kProjChunk; base < a.n; base += gridDim.x * kProjChunk) {
+    // Candidate list: while the pose stays within its bounds, only the
+    // Gaussians on it are projected (the others stay out of view, with count
+    // 0 since the launch that built it); otherwise every Gaussian is, and
+    // the list is rebuilt.  Every CTA reads the same state (it changes only
+    // when the last CTA of a building launch has finished).
+    const bool use_cand = a.cand && a.cst && !all_slow;
+    const bool reuse = use_cand && cand_reusable(*a.cst, *P, a.cone);
+    const bool build = use_cand && !reuse;
+    const float cone_b = a.cone + kCandConeMargin;
+    // A launch that projects every Gaussian without building a list drops
+    // the one held: Gaussians off it may have records from this pose.
+    if (a.cst && !use_cand && blockIdx.x == 0 && threadIdx.x == 0) a.cst->valid = 0;
+    const int n_items = reuse ? (int)a.cst->n : a.n;
+    for (int base = blockIdx.x * kProjChunk; base < n_items; base += gridDim.x * kProjChunk) {
         if (threadIdx.x == 0) q_n = 0;
         __syncthreads();
         float4 p[kProjPerThread];
         uint32_t c[kProjPerThread];
+        int gi[kProjPerThread];
 #pragma unroll
         for (int k = 0; k < kProjPerThread; ++k) {
-            const int i = base + k * kProjThreads + (int)threadIdx.x;
+            const int item = base + k * kProjThreads + (int)threadIdx.x;
+            gi[k] = item < n_items ? (reuse ? (int)a.cand[item] : item) : a.n;
+        }
+#pragma unroll
+        for (int k = 0; k < kProjPerThread; ++k) {
+            const int i = gi[k];
             p[k] = make_float4(0.f, 0.f, 0.f, 0.f);
             c[k] = 0;
             if (i < a.n) {
@@ -307,9 +363,23 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
         }
 #pragma unroll
         for (int k = 0; k < kProjPerThread; ++k) {
-            const int i = base + k * kProjThreads + (int)threadIdx.x;
+            const int i = gi[k];
             const bool valid = i < a.n;
-            const bool queue = valid && (all_slow || in_view(a, p[k], R, tw));
+            float3 pc;
+            const bool seen = valid && in_view(a, p[k], R, tw, pc);
+            const bool queue = valid && (all_slow || seen);
+            if (build) {
+                // warp-aggregated append of the Gaussians that may come into view
+                const bool cand = valid && (seen || candidate(pc, cone_b));
+                const uint32_t cb = __ballot_sync(kFullMask, cand);
+                if (cb) {
+                    const int leader = __ffs(cb) - 1;
+                    uint32_t slot = 0;
+                    if (lane == leader) slot = atomicAdd(&a.cst->n_build, (uint32_t)__popc(cb));
+                    slot = __shfl_sync(kFullMask, slot, leader) + (uint32_t)__popc(cb & lanemask_lt());
+                    if (cand) a.cand[slot] = (uint32_t)i;
+                }
+            }
             if (valid && !queue && (!a.hist || c[k])) {
                 // out of view, no instances now: project_one's record for it
                 a.bins[i].r = make_uint4(0u, 0u, 0u, 0u);
@@ -340,6 +410,20 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
         for (int c = threadIdx.x; c < grid_cells; c += kProjThreads) {
             const int v = s_grid[c];
             if (v) atomicAdd(&a.tile_diff[c], v);
+        }
+    }
+    if (build && threadIdx.x == 0) {
+        // the last CTA to finish publishes the list for the pose it was built at
+        __threadfence();
+        if (atomicAdd(&a.cst->done, 1u) == gridDim.x - 1) {
+            CandState* cs = a.cst;
+            cs->n = atomicExch(&cs->n_build, 0u);
+            for (int k = 0; k < 3; ++k) cs->t[k] = P->t[k];
+            for (int k = 0; k < 4; ++k) cs->q[k] = P->q[k];
+            cs->cone = cone_b;
+            cs->done = 0;
+            __threadfence();
+            cs->valid = 1;
         }
     }
 }

@@ -121,6 +121,10 @@ struct fvgs_session {
     float4 *geo0 = nullptr, *geo1 = nullptr;
     BinRec* bins = nullptr;  // binning records; bins[i].r.z == counts[i] after every binning
     uint32_t *counts = nullptr, *offsets = nullptr, *partials = nullptr;
+    // the projection's candidate list (Gaussians that may be in view near the
+    // pose it was built at) and its state; cleared when the Gaussians change
+    uint32_t* cand = nullptr;
+    CandState* cst = nullptr;
     float *dbg_cov = nullptr, *dbg_inv = nullptr;
     uint8_t* dbg_vis = nullptr;
 
@@ -458,6 +462,17 @@ void collect_timing(fvgs_session* s) {
     s->ev_used = 0;
 }
 
+// Drop the projection's candidate list (the Gaussians changed).
+cudaError_t cand_drop(fvgs_session* s) { return cudaMemsetAsync(s->cst, 0, sizeof(CandState), s->stream); }
+
+// The largest angle from the optical axis of a ray through the W x H image
+// of K: the ray through its farthest corner.
+float view_cone(const fvgs_intrinsics* K, int W, int H) {
+    const double ex = std::max(std::fabs((double)K->cx), std::fabs((double)W - K->cx)) / K->fx;
+    const double ey = std::max(std::fabs((double)K->cy), std::fabs((double)H - K->cy)) / K->fy;
+    return (float)std::atan(std::sqrt(ex * ex + ey * ey));
+}
+
 // Enqueue binning for the pose already in s->pose.
 int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H, int tw, int th) {
     const fvgs_params& P = s->params;
@@ -506,6 +521,9 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H, int tw,
     pa.counts = s->counts;
     pa.geo0 = s->geo0;
     pa.geo1 = s->geo1;
+    pa.cst = s->cst;
+    if (!(s->debug & FVGS_DEBUG_NO_CANDIDATES)) pa.cand = s->cand;
+    pa.cone = view_cone(K, W, H);
     if (s->debug & FVGS_DEBUG_PROJECTION) {
         pa.dbg_cov = s->dbg_cov;
         pa.dbg_inv = s->dbg_inv;
@@ -797,6 +815,7 @@ int enqueue_map(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, 
     ua.beta2 = P.adam_beta2;
     ua.eps = P.adam_eps;
     ua.dbg_delta3d = (s->debug & FVGS_DEBUG_MAPPING) ? s->dbg_delta3d : nullptr;
+    ua.cst = s->cst;
     if (s->precision == FVGS_PRECISION_REDUCED) {
         ua.attr_sr = s->attr_sr;
         ua.attr_c = s->attr_c;
@@ -918,6 +937,8 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->bins, N);
     FV_A(s->counts, N);
     FV_A(s->offsets, N);
+    FV_A(s->cand, N);
+    FV_A(s->cst, 1);
     FV_A(s->partials, scan_partials_size((int)N) + 1);
     // tile-indexed buffers hold the largest frame at the smallest tracking
     // tile (8 x 8); mapping runs on 16 x 16 tiles
@@ -976,6 +997,7 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     const uint64_t cap0 = std::max<uint64_t>(1u << 20, 8ull * N);
     if ((rc = alloc_instances(s, std::min<uint64_t>(cap0, 0xffffffffull))) != FVGS_OK) return fail(rc);
     if (cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
+    if (cudaMemsetAsync(s->cst, 0, sizeof(CandState), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
     *out = s;
     return FVGS_OK;
@@ -1046,6 +1068,22 @@ int fvgs_session_binning_grid(const fvgs_session* s, int* tile_w, int* tile_h, i
     return FVGS_OK;
 }
 
+int fvgs_session_candidates(fvgs_session* s, int* valid, uint32_t* n, fvgs_pose* pose, float* cone) {
+    if (!s) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    CandState c{};
+    FV_CK(cudaMemcpyAsync(&c, s->cst, sizeof(CandState), cudaMemcpyDeviceToHost, s->stream));
+    FV_CK(cudaStreamSynchronize(s->stream));
+    if (valid) *valid = c.valid ? 1 : 0;
+    if (n) *n = c.valid ? c.n : 0u;
+    if (pose) {
+        for (int k = 0; k < 3; ++k) pose->position[k] = c.t[k];
+        for (int k = 0; k < 4; ++k) pose->orientation[k] = c.q[k];
+    }
+    if (cone) *cone = c.cone;
+    return FVGS_OK;
+}
+
 int fvgs_session_footprint(const fvgs_session* s, uint64_t* bytes) {
     if (!s || !bytes) return FVGS_E_INVALID;
     *bytes = s->footprint;
@@ -1060,6 +1098,7 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     s->n_g = n;
     s->has_binning = s->has_track = false;
     s->hist_ok = false;
+    FV_CK(cand_drop(s));
     if (n == 0) return FVGS_OK;
     // Stage through rec planes (free until the next binning) so host arrays of
     // the reference's float3 layout become 16-byte vectors on the device.
@@ -1102,6 +1141,7 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
     FV_CK(cudaMemcpyAsync(orientations, tmp3, sizeof(float) * 4 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(colors, tmp4, sizeof(float) * 3 * n, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(opacities, tmp5, sizeof(float) * n, cudaMemcpyDefault, s->stream));
+    FV_CK(cand_drop(s));  // out-of-view Gaussians' records are no longer cleared
     FV_CK(cudaStreamSynchronize(s->stream));
     s->has_binning = s->has_track = false;  // staging overwrote the records
     s->hist_ok = false;
@@ -2725,6 +2765,7 @@ int finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
     std::swap(s->col, s->col_alt);
     if (!(s->params.quirks & FVGS_Q_ADAM_STAY)) std::swap(s->adam, s->adam_alt);
     s->n_g = s->h_mk_ctr[0];
+    FV_CK(cand_drop(s));
     // every per-Gaussian index of the last binning is stale now
     s->has_binning = s->has_track = s->has_map = false;
     s->hist_ok = false;
@@ -2930,6 +2971,7 @@ int enqueue_seed(fvgs_session* s, SeedMode mode, const SeedArgs& a) {
 
 int map_grew(fvgs_session* s, uint32_t n) {
     s->n_g = n;
+    FV_CK(cand_drop(s));
     s->has_binning = s->has_track = s->has_map = false;
     s->hist_ok = false;  // the new Gaussians have no previous binning
     s->keys_valid = false;

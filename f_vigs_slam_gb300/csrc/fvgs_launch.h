@@ -42,6 +42,24 @@ struct __align__(32) BinRec {
     float4 p;
 };
 
+// The Gaussians a projection may find in view while the pose stays near the
+// one they were culled at (the projection's candidate list, see
+// project_count_kernel).  All zero = no list.
+struct CandState {
+    uint32_t valid;    // the list in cand[] holds n entries for pose (t, q) and cone
+    uint32_t n;
+    uint32_t n_build;  // entries appended by the building launch (0 between launches)
+    uint32_t done;     // CTAs of the building launch that have finished (0 between launches)
+    float t[3];
+    float q[4];
+    float cone;        // the view cone's half-angle (radians) the list was built for
+};
+// Pose change within which a candidate list stays complete, and the
+// distance within which every Gaussian is a candidate.
+constexpr float kCandMaxAngle = 0.0349066f;  // 2 degrees
+constexpr float kCandMaxShift = 0.05f;       // metres
+constexpr float kCandNear = 0.1f;            // metres
+
 struct ProjectArgs {
     const float4* pos;
     const float4* scale;
@@ -81,6 +99,12 @@ struct ProjectArgs {
     // the camera-frame 3D covariance and mean (z is rec0.z)
     float4* geo0;
     float4* geo1;
+    // optional candidate list (capacity n) and its state; cone: the current
+    // view's largest angle from the optical axis (its farthest image corner),
+    // radians -- a list built for a cone at least as wide is reused
+    uint32_t* cand;
+    CandState* cst;
+    float cone;
 };
 
 struct EmitArgs {
@@ -347,6 +371,7 @@ struct MapUpdateArgs {
     float* dbg_delta3d;  // optional [N][16]
     uint4* attr_sr;      // optional: refresh the reduced-precision planes of updated Gaussians
     uint2* attr_c;
+    CandState* cst;      // optional: the projection's candidate list, stale once positions move
 };
 cudaError_t launch_map_forward(const MapArgs& a, bool cap, cudaStream_t s);
 cudaError_t launch_map_backward(const MapArgs& a, bool cap, cudaStream_t s);

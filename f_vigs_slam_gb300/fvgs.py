@@ -43,6 +43,7 @@ DEBUG_PROJECTION = 0x1
 DEBUG_IMAGES = 0x2
 DEBUG_MAPPING = 0x4
 DEBUG_RADIX_SORT = 0x8
+DEBUG_NO_CANDIDATES = 0x10
 
 TRACK_VARIANTS = 5  # FVGS_TRACK_VARIANTS
 KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
@@ -288,6 +289,14 @@ class Session:
         _check(self.lib.fvgs_session_binning_grid(self.h, C.byref(tw), C.byref(th), C.byref(T)),
                "fvgs_session_binning_grid")
         return int(tw.value), int(th.value), int(T.value)
+
+    def candidates(self):
+        """The projection's candidate list after the work enqueued so far:
+        (held, length, position[3], orientation[4], view-cone half-angle)."""
+        valid, n, p, cone = C.c_int(), C.c_uint32(), Pose(), C.c_float()
+        _check(self.lib.fvgs_session_candidates(self.h, C.byref(valid), C.byref(n), C.byref(p), C.byref(cone)),
+               "fvgs_session_candidates")
+        return bool(valid.value), int(n.value), list(p.position), list(p.orientation), float(cone.value)
 
     def download_binning(self, W, H, max_instances: int | None = None):
         n = C.c_uint32()

@@ -32,6 +32,7 @@ typedef struct fvgs_session fvgs_session;
 #define FVGS_DEBUG_MAPPING 0x4u    /* mapping step keeps its 3D deltas */
 #define FVGS_DEBUG_RADIX_SORT 0x8u /* bin with the global LSD radix sort instead of per-tile sorting
                                       (an independent implementation of the same order, for checking) */
+#define FVGS_DEBUG_NO_CANDIDATES 0x10u /* project every Gaussian at every binning (no candidate list) */
 
 /* Kernel classes for launch accounting and timing. */
 enum {
@@ -169,12 +170,21 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
  * instances that entered a tile since that binning, and the Gaussians with
  * such instances.  Any pointer may be null.  No reference counterpart: the
  * reference rebuilds every binning from scratch. */
+int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
+                              uint32_t* n_changed);
 /* Tile shape and tile count of the last binning (a tracking level may bin on
  * 8 x 8 or 32 x 8 tiles: fvgs_session_set_track_tiles).  Any pointer may be
  * null.  No reference counterpart (its tiles are always 16 x 16). */
 int fvgs_session_binning_grid(const fvgs_session* s, int* tile_w, int* tile_h, int* num_tiles);
-int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
-                              uint32_t* n_changed);
+/* The projection's candidate list after the work enqueued so far (waits for
+ * the session's stream): whether one is held, its length, and the pose and
+ * view-cone half-angle (radians) it was built at.  A binning whose pose is
+ * within 2 degrees and 5 cm of that pose, with a view cone no wider, projects
+ * only the listed Gaussians; any other binning projects all of them and
+ * rebuilds the list; a change to the Gaussians drops it.  Any pointer may be
+ * null.  No reference counterpart: the reference projects every Gaussian at
+ * every render. */
+int fvgs_session_candidates(fvgs_session* s, int* valid, uint32_t* n, fvgs_pose* pose, float* cone);
 
 /*
  * One RGB-D pose Jacobian evaluation at `pose` against the frame of `level`:
