@@ -123,6 +123,10 @@ def parse():
     ap.add_argument("--sessions", type=int, default=32)
     ap.add_argument("--plain-only", action="store_true",
                     help="only the large plain workload (for profiling runs; not the benchmark line)")
+    ap.add_argument("--track-case", default=None, metavar="LEVEL:VARIANT",
+                    help="profiling case: the large plain workload's frame at one pyramid level, three Jacobian "
+                         "evaluations with a fixed launch variant (launches: one render, then the evaluations; "
+                         "not the benchmark line)")
     ap.add_argument("--prec-n", type=int, default=PREC_N, help="Gaussians of the precision-form workload")
     ap.add_argument("--batch-sessions", type=int, default=BATCH_SESSIONS, help="keyframes of the batching workload")
     return ap.parse_args()
@@ -325,18 +329,25 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(cls, n_g, n_vis, n_inst, visited, W, H):
+def algorithmic_bytes(cls, n_g, n_vis, n_inst, visited, W, H, n_cand=None):
     """Bytes one launch of a kernel class must move on the frame's level-0
     binning, with the basis they are counted on; None where a class has no
     meaningful byte count.  n_vis: Gaussians with instances; visited: the
     instances the blending kernels must read (per tile, the list prefix up to
-    its deepest pixel's last blended Gaussian)."""
+    its deepest pixel's last blended Gaussian); n_cand: the length of the
+    projection's candidate list where the timed launches reuse one."""
     P = W * H
     T = ((W + 15) // 16) * ((H + 15) // 16)
+    if n_cand is None:
+        proj = (20 * n_g + 160 * n_vis,
+                "20 B per Gaussian (position, previous count) + per visible Gaussian 48 B of attributes in and "
+                "112 B out (blending 48, binning 32, geometry 32 records)")
+    else:
+        proj = (24 * n_cand + 160 * n_vis,
+                "candidate list reused: 24 B per listed Gaussian (index, position, previous count) + per visible "
+                "Gaussian 48 B of attributes in and 112 B out (blending 48, binning 32, geometry 32 records)")
     table = {
-        "project": (20 * n_g + 160 * n_vis,
-                    "20 B per Gaussian (position, previous count) + per visible Gaussian 48 B of attributes in and "
-                    "112 B out (blending 48, binning 32, geometry 32 records)"),
+        "project": proj,
         "sort": (8 * n_inst + 32 * n_vis,
                  "incremental per-tile sort: 4 B in + 4 B out per instance + each visible Gaussian's 32-byte "
                  "binning record"),
@@ -732,6 +743,9 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         sess.track_jacobian(last["pose"], K, 0)
     l0 = sess.get_timing(reset=True)
     sess.set_timing(())
+    # every timed binning was at the pose of the list the first one left
+    cand_held, n_cand = sess.candidates()[:2]
+    n_cand = n_cand if cand_held else None
 
     maint = measure_maintenance(fvgs, sess, frames, K, W, H, reps=max(3, args.steps),
                                 with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
@@ -741,7 +755,7 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
     traffic = load_traffic()
     per_class = {}
     for c, t in timing.items():
-        ab = algorithmic_bytes(c, args.n, n_vis, n_inst, visited, W, H)
+        ab = algorithmic_bytes(c, args.n, n_vis, n_inst, visited, W, H, n_cand)
         if not t["timed"] or ab is None:
             continue
         algo_c, basis = ab
@@ -757,7 +771,7 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         per_class[c] = e
     td = l0[dominant] if dominant in l0 and l0[dominant]["timed"] else timing[dominant]
     per_launch_ms = td["ms"] / max(1, td["timed"])
-    algo, basis = algorithmic_bytes(dominant, args.n, n_vis, n_inst, visited, W, H)
+    algo, basis = algorithmic_bytes(dominant, args.n, n_vis, n_inst, visited, W, H, n_cand)
     achieved = algo / (per_launch_ms / 1000.0) / 1e9
     sess.close()
     return {
@@ -770,6 +784,7 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         "pose_error": err_stats(errs), "e2e_pose_error": err_stats(e2e_errs),
         "instances_per_binning": n_inst, "visible_gaussians": n_vis,
         "track_records_read": visited, "track_records_listed": listed,
+        "projection_candidates": n_cand,
         "gpu_launches": int(sum(v["launches"] for v in timed_launches.values())),
         "kernel_share": {c: round(v["ms"] / max(1e-9, sum(x["ms"] for x in timing.values())), 4)
                          for c, v in timing.items() if v["ms"] > 0},
@@ -780,6 +795,38 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
         "kernel_rooflines": per_class,
         "maintenance": maint,
     }
+
+
+def run_track_case(args, fvgs, S):
+    """Profiling case: the room map of the large plain workload, the frame of
+    one pyramid level rendered at the first trajectory pose (one render
+    launch), then three Jacobian evaluations at the predicted pose with the
+    tracking kernel's launch variant fixed (the autotuner off)."""
+    level, variant = (int(x) for x in args.track_case.split(":"))
+    cam = S.CAM_HD
+    W, H, K0 = cam.width, cam.height, cam.intrinsics
+    sess = fvgs.Session(args.n, W, H, fvgs.default_params(fvgs.QUIRKS_INTENDED))
+    sess.upload(S.room(args.n, seed=0))
+    true = S.trajectory(2, seed=3)[1]
+    rng = np.random.default_rng(5)
+    w, h = level_dims(W, H, ROOM_LEVELS)[level]
+    K = level_K(K0, level)
+    col, dep, _, _ = sess.render(true, K, w, h)
+    rgb, d = S.add_noise(col, dep, rng)
+    gx, gy = S.sobel3(rgb)
+    sess.set_frame(level, rgb, d, gx, gy)
+    sess.set_autotune(False)
+    sess.set_track_variant(level, variant)
+    pose = S.perturb(true, PRED_DEG, PRED_CM, rng)
+    sess.set_timing(["track"])
+    for _ in range(3):
+        sess.track_jacobian(pose, K, level)
+    t = sess.get_timing(reset=True)["track"]
+    sess.close()
+    return {"metric": "tracking kernel profiling case (not the benchmark line)",
+            "workload": "room N=%d, %dx%d (pyramid level %d of 1280x720), launch variant %d" % (args.n, w, h, level,
+                                                                                             variant),
+            "track_ms_per_launch": t["ms"] / max(1, t["timed"])}
 
 
 def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
@@ -1283,6 +1330,10 @@ def run_ours(args):
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
 
+    if args.track_case:
+        if rank == 0:
+            print(json.dumps(run_track_case(args, fvgs, S)), flush=True)
+        return 0
     large = run_large(args, fvgs, S, torch, dev, stream, rank, world)
     if args.plain_only:
         if rank == 0:

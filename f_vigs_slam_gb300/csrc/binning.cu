@@ -340,7 +340,12 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
     // the one held: Gaussians off it may have records from this pose.
     if (a.cst && !use_cand && blockIdx.x == 0 && threadIdx.x == 0) a.cst->valid = 0;
     const int n_items = reuse ? (int)a.cst->n : a.n;
-    for (int base = blockIdx.x * kProjChunk; base < n_items; base += gridDim.x * kProjChunk) {
+    // every CTA takes one contiguous span of the items (a multiple of a warp),
+    // in chunks: a short candidate list then spreads over the whole grid
+    // instead of filling a few CTAs' chunks
+    const int span = ((n_items + (int)gridDim.x - 1) / (int)gridDim.x + 31) & ~31;
+    const int b1 = min(n_items, (int)blockIdx.x * span + span);
+    for (int base = (int)blockIdx.x * span; base < b1; base += kProjChunk) {
         if (threadIdx.x == 0) q_n = 0;
         __syncthreads();
         float4 p[kProjPerThread];
@@ -349,7 +354,7 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_count_kernel(ProjectA
 #pragma unroll
         for (int k = 0; k < kProjPerThread; ++k) {
             const int item = base + k * kProjThreads + (int)threadIdx.x;
-            gi[k] = item < n_items ? (reuse ? (int)a.cand[item] : item) : a.n;
+            gi[k] = item < b1 ? (reuse ? (int)a.cand[item] : item) : a.n;
         }
 #pragma unroll
         for (int k = 0; k < kProjPerThread; ++k) {

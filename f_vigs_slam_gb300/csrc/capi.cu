@@ -233,6 +233,7 @@ struct fvgs_session {
     std::vector<Pending> pending;
 
     int last_W = 0, last_H = 0, last_T = 0;
+    int last_split = 1;  // partial rows per tile of the last tracking launch (TrackArgs::split)
     bool has_binning = false, has_track = false, dbg_proj_valid = false, has_map = false;
 
     // Asynchronous frames (fvgs_frame_submit / fvgs_frame_wait).  A frame
@@ -249,7 +250,7 @@ struct fvgs_session {
         float eta = -1.f;
         uint64_t gen = 0;
         // host-side binning state the frame leaves (the tile grid of its last binning)
-        int exit_ntx = 0, exit_nty = 0, exit_W = 0, exit_H = 0, exit_T = 0;
+        int exit_ntx = 0, exit_nty = 0, exit_W = 0, exit_H = 0, exit_T = 0, exit_split = 1;
         uint32_t *vals_in = nullptr, *vals_out = nullptr, *vals_alt_out = nullptr;
         uint2 *ranges_in = nullptr, *ranges_out = nullptr, *ranges_prev_out = nullptr;
         uint64_t launches[FVGS_K_COUNT] = {};
@@ -632,6 +633,11 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H, int tw,
     return FVGS_OK;
 }
 
+// Whether a tracking launch may split its 16 x 16 list tiles over several CTAs.
+bool split_ok(const TrackArgs& a) {
+    return a.tile_w == 16 && a.tile_h == 16 && !a.compensated && !a.render_only;
+}
+
 // Arguments of the tracking kernel on the binning just enqueued.
 TrackArgs make_track_args(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
                           bool images) {
@@ -681,6 +687,11 @@ TrackArgs make_track_args(fvgs_session* s, const fvgs_intrinsics* K, const Frame
                          : 0;
     ta.variant = (f.tuned_w == f.W && f.tuned_h == f.H) ? f.track_variant : 0;
     if (ta.variant == 2 && !s->rec_maps_ok) ta.variant = 0;
+    ta.split = 1;
+    if (track_variant_split(ta.variant) > 1) {
+        if (split_ok(ta)) ta.split = track_variant_split(ta.variant);
+        else ta.variant = 3;  // the same staging batch, one CTA per tile
+    }
     ta.st_flags = &s->st->flags;
     return ta;
 }
@@ -688,6 +699,7 @@ TrackArgs make_track_args(fvgs_session* s, const fvgs_intrinsics* K, const Frame
 int enqueue_track(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, bool render_only,
                   bool images) {
     const TrackArgs ta = make_track_args(s, K, f, render_only, images);
+    if (!render_only) s->last_split = ta.split;
     KScope k(s, render_only ? FVGS_K_RENDER : FVGS_K_TRACK, 1);
     FV_CK(launch_track(ta, s->rec_maps_ok ? &s->rec_maps : nullptr, s->stream));
     return FVGS_OK;
@@ -957,7 +969,9 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     FV_A(s->changed, (size_t)s->enter_cap);
     FV_A(s->seg.large_list, (size_t)s->cap_tiles);
     FV_A(s->seg.large_ctrl, 4);  // [0..1] large-bucket list control, [2] scatter chunk counter
-    FV_A(s->tile_out, (size_t)s->cap_tiles * FVGS_POSEDATA_FLOATS);
+    // partial rows: a tile of the smallest tracking tile each, or four per
+    // 16 x 16 tile split over 8 x 8 CTAs
+    FV_A(s->tile_out, (size_t)std::max(s->cap_tiles, 4 * s->cap_tiles16) * FVGS_POSEDATA_FLOATS);
     FV_A(s->pose, 1);
     FV_A(s->d_pose_in, 1);
     FV_A(s->jj, 48);
@@ -1342,7 +1356,7 @@ int fvgs_track_jacobian(fvgs_session* s, const fvgs_pose* pose, const fvgs_intri
         FV_TRY(enqueue_track(s, K, f, false, images));
         {
             KScope k(s, FVGS_K_REDUCE, 1);
-            FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->pose, s->jj, s->stream));
+            FV_CK(launch_track_reduce(s->tile_out, s->last_T, s->last_split, s->pose, s->jj, s->stream));
         }
         FV_CK(cudaMemcpyAsync(s->h_jj, s->jj, sizeof(double) * 42, cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
@@ -1364,8 +1378,22 @@ int fvgs_download_tile_partials(fvgs_session* s, float* tiles, int num_tiles) {
     if (!s->has_track) return FVGS_E_STATE;
     if (num_tiles < s->last_T) return FVGS_E_CAPACITY;
     FV_CK(cudaSetDevice(s->device));
-    FV_CK(cudaMemcpyAsync(tiles, s->tile_out, sizeof(float) * 27 * s->last_T, cudaMemcpyDefault, s->stream));
+    const int split = std::max(1, s->last_split);
+    if (split == 1) {
+        FV_CK(cudaMemcpyAsync(tiles, s->tile_out, sizeof(float) * 27 * s->last_T, cudaMemcpyDefault, s->stream));
+        FV_CK(cudaStreamSynchronize(s->stream));
+        return FVGS_OK;
+    }
+    // tiles split over several CTAs: add each tile's partial rows in the
+    // frame reduction's order (FP32 adds, the same on host and device)
+    std::vector<float> rows((size_t)27 * s->last_T * split);
+    FV_CK(cudaMemcpyAsync(rows.data(), s->tile_out, sizeof(float) * rows.size(), cudaMemcpyDefault, s->stream));
     FV_CK(cudaStreamSynchronize(s->stream));
+    for (int t = 0; t < s->last_T; ++t)
+        for (int c = 0; c < 27; ++c) {
+            const float* r = rows.data() + ((size_t)t * split) * 27 + c;
+            tiles[(size_t)t * 27 + c] = split == 2 ? r[0] + r[27] : (r[0] + r[27]) + (r[54] + r[81]);
+        }
     return FVGS_OK;
 }
 
@@ -1389,6 +1417,21 @@ namespace {
 // CUDA events on the session's stream), keep the fastest median for frames
 // of this shape.  Every variant computes the same values in the same order,
 // so the choice changes only the time.
+// Whether launch variant v is a distinct choice for the level's frames: the
+// TMA-staged one needs the record tensor maps; the split ones need 16 x 16
+// tiles without compensated sums.
+bool variant_applies(const fvgs_session* s, const FrameLevel& f, int v) {
+    if (v == 2) return s->rec_maps_ok;
+    if (track_variant_split(v) > 1) {
+        TrackArgs a{};
+        a.tile_w = f.tile_w ? f.tile_w : 16;
+        a.tile_h = f.tile_h ? f.tile_h : 16;
+        a.compensated = s->precision == FVGS_PRECISION_REDUCED && !(s->params.quirks & FVGS_Q_POSE_JAC_APPROX);
+        return split_ok(a);
+    }
+    return true;
+}
+
 int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int reps) {
     FrameLevel& f = s->lv[level];
     if (!f.rgb) return FVGS_E_STATE;
@@ -1415,7 +1458,7 @@ int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics
         f.tuned_h = f.H;
         for (int r = 0; r < reps && rc == FVGS_OK; ++r)
             for (int v = 0; v < kTrackVariants && rc == FVGS_OK; ++v) {
-                if (v == 2 && !s->rec_maps_ok) continue;
+                if (!variant_applies(s, f, v)) continue;
                 f.track_variant = v;
                 const size_t k = 2 * ((size_t)r * kTrackVariants + v);
                 if (cudaEventRecord(ev[k], s->stream) != cudaSuccess) rc = FVGS_E_CUDA;
@@ -1445,7 +1488,7 @@ int autotune_track(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics
     }
     int best = 0;
     for (int v = 1; v < kTrackVariants; ++v)
-        if ((v != 2 || s->rec_maps_ok) && med[v] < med[best]) best = v;
+        if (variant_applies(s, f, v) && med[v] < med[best]) best = v;
     f.track_variant = best;
     for (int v = 0; v < kTrackVariants; ++v) f.tuned_ms[v] = med[v];
     ++s->gen;  // captured frame graphs hold the previous kernel
@@ -1506,8 +1549,8 @@ int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
             FV_TRY(enqueue_bin(s, &r.K[l], f.W, f.H, f.tile_w, f.tile_h));
             FV_TRY(enqueue_track(s, &r.K[l], f, false, false));
             KScope k(s, FVGS_K_GN, 1);
-            FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->pose, s->jj, s->params.eig_eps, s->step,
-                                         s->stream));
+            FV_CK(launch_track_reduce_gn(s->tile_out, s->last_T, s->last_split, s->pose, s->jj, s->params.eig_eps,
+                                         s->step, s->stream));
         }
     }
     if (r.eta >= 0.f) {
@@ -1592,6 +1635,7 @@ int launch_frame(fvgs_session* s) {
         s->last_W = g.exit_W;
         s->last_H = g.exit_H;
         s->last_T = g.exit_T;
+        s->last_split = g.exit_split;
         s->keys_valid = false;
         s->has_binning = true;
         ++s->frames_graphed;
@@ -1622,6 +1666,7 @@ int launch_frame(fvgs_session* s) {
     uint2* const ranges_prev0 = s->ranges_prev;
     const bool hist0 = s->hist_ok, clean0 = s->diff_clean, keys0 = s->keys_valid, binned0 = s->has_binning;
     const int ntx0 = s->hist_ntx, nty0 = s->hist_nty, lw0 = s->last_W, lh0 = s->last_H, lt0 = s->last_T;
+    const int ls0 = s->last_split;
     g.vals_in = s->vals;
     g.ranges_in = s->ranges;
     g.n_g = s->n_g;
@@ -1653,6 +1698,7 @@ int launch_frame(fvgs_session* s) {
         s->last_W = lw0;
         s->last_H = lh0;
         s->last_T = lt0;
+        s->last_split = ls0;
         ++s->frames_eager;
         return enqueue_frame(s, r);
     }
@@ -1670,6 +1716,7 @@ int launch_frame(fvgs_session* s) {
     g.exit_W = s->last_W;
     g.exit_H = s->last_H;
     g.exit_T = s->last_T;
+    g.exit_split = s->last_split;
     g.vals_out = s->vals;
     g.vals_alt_out = s->sort.vals_alt;
     g.ranges_out = s->ranges;
@@ -2048,11 +2095,13 @@ int batch_bin_level(fvgs_batch* b, const Request* reqs, int l, int it, uint32_t*
         TrackJob& j = b->h_jobs[(size_t)it * n + i];
         j.a = make_track_args(s, &reqs[i].K[l], f, false, false);
         j.a.variant = b->variant[l];
+        j.a.split = 1;  // the persistent launch runs one work item per tile
         b->h_begin[(size_t)it * (n + 1) + i] = t;
         t += (uint32_t)s->last_T;
         ReduceJob& r = b->h_rjobs[(size_t)it * n + i];
         r.tile_out = s->tile_out;
         r.num_tiles = s->last_T;
+        r.split = 1;
         r.pose = s->pose;
         r.out = s->jj;
         r.eig_eps = s->params.eig_eps;
@@ -2138,7 +2187,7 @@ struct HostBinState {
     uint32_t *vals, *vals_alt;
     uint2 *ranges, *ranges_prev;
     bool hist, clean, keys, binned;
-    int ntx, nty, tw, th, btw, bth, lw, lh, lt;
+    int ntx, nty, tw, th, btw, bth, lw, lh, lt, ls;
     uint64_t launches[FVGS_K_COUNT];
     void save(const fvgs_session* s) {
         vals = s->vals;
@@ -2158,6 +2207,7 @@ struct HostBinState {
         lw = s->last_W;
         lh = s->last_H;
         lt = s->last_T;
+        ls = s->last_split;
         std::memcpy(launches, s->launches, sizeof(launches));
     }
     void restore(fvgs_session* s) const {
@@ -2178,6 +2228,7 @@ struct HostBinState {
         s->last_W = lw;
         s->last_H = lh;
         s->last_T = lt;
+        s->last_split = ls;
         std::memcpy(s->launches, launches, sizeof(launches));
     }
 };
@@ -2209,6 +2260,7 @@ int batch_launch(fvgs_batch* b, const Request* reqs) {
             s->last_W = e.last_W;
             s->last_H = e.last_H;
             s->last_T = e.last_T;
+            s->last_split = 1;  // batched launches run one CTA per tile
             s->keys_valid = false;
             s->has_binning = true;
             for (int c = 0; c < FVGS_K_COUNT; ++c) s->launches[c] += e.launches[c];

@@ -252,15 +252,28 @@ struct TrackArgs {
     // precision form: compensated accumulation of the per-pixel colour
     // Jacobian and of the in-tile sums (analytic Jacobian, 16 x 16 tiles)
     int compensated;
+    // CTAs per list tile (0 or 1: one; 2: 16 x 8 pixel halves; 4: 8 x 8
+    // quarters of a 16 x 16 list tile).  CTA c of list tile c / split writes
+    // partial row c of tile_out; the frame reduction adds a tile's rows in
+    // the fixed order of a whole tile's in-CTA sum, so the sums are the same
+    // bits for every split.
+    int split;
 };
-constexpr int kTrackVariants = 5;
+constexpr int kTrackVariants = 8;
 // Whether the tracking kernel runs tiles of this shape.
 inline bool track_tile_supported(int tw, int th) {
     return (tw == 16 && th == 16) || (tw == 8 && th == 8) || (tw == 32 && th == 8);
 }
-// Gaussians staged per shared-memory batch by a launch variant: 3 -> 128,
-// 4 -> 512, otherwise 256.
-inline int track_variant_batch(int variant) { return variant == 3 ? 128 : (variant == 4 ? 512 : 256); }
+// Gaussians staged per shared-memory batch by a launch variant: 3, 5, 6 ->
+// 128, 4 -> 512, otherwise 256.
+inline int track_variant_batch(int variant) {
+    return (variant == 3 || variant == 5 || variant == 6) ? 128 : (variant == 4 ? 512 : 256);
+}
+// CTAs per 16 x 16 list tile of a launch variant: 5 -> 2 (16 x 8 pixel
+// halves), 6 -> 4 (8 x 8 quarters), otherwise 1.  More, smaller CTAs fill
+// the SMs at the coarse pyramid levels, where a frame has a few hundred
+// tiles with long lists; every CTA stages its tile's whole list.
+inline int track_variant_split(int variant) { return variant == 5 ? 2 : (variant == 6 ? 4 : 1); }
 // Set the dynamic shared-memory limits of the tracking kernels on the current
 // device (their batches can exceed the 48 KB default); once per device,
 // before any launch or capture.
@@ -276,14 +289,18 @@ cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s
 cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s);
 // Sum tile partials in FP64, rotate to the world frame, write out[42] =
 // JtJ[36] (symmetric) then Jtr[6] (negated, as the reference host code does).
-cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
+// split: partial rows per tile (TrackArgs::split).
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, int split, DevPose* pose, double* out,
                                 cudaStream_t s);
 // The same reduction followed by one eigen-regularised Gauss-Newton update of
 // the device pose (step_out[6] nullable).
+cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, int split, DevPose* pose, double* out,
+                                   double eig_eps, double* step_out, cudaStream_t s);
 // One session's frame reduction + Gauss-Newton step in a batched launch.
 struct ReduceJob {
     const float* tile_out;
     int num_tiles;
+    int split;
     DevPose* pose;
     double* out;
     double eig_eps;
@@ -306,8 +323,6 @@ cudaError_t launch_track_batch(const TrackJob* jobs, const uint32_t* begin, int 
                                cudaStream_t s);
 // Kernel attributes of the persistent kernels on the current device.
 cudaError_t track_batch_configure_device();
-cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
-                                   double eig_eps, double* step_out, cudaStream_t s);
 
 // ---- render form (render.cu) ----
 struct RenderArgs {

@@ -155,7 +155,7 @@ extern "C" int fvgs_rgbd_pose_jacobians_noalloc(
     ta.quirks = P.quirks | FVGS_Q_POSE_JAC_APPROX;
     ta.variant = 0;
     if (fvgs::launch_track_ref_layout(ta, s) != cudaSuccess) return cuda_failed();
-    if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), dpose, out, s) != cudaSuccess) return cuda_failed();
+    if (fvgs::launch_track_reduce(tiles, (int)(ntx * nty), 1, dpose, out, s) != cudaSuccess) return cuda_failed();
     if (cudaMemcpyAsync(JtJ, out, sizeof(double) * 36, cudaMemcpyDefault, s) != cudaSuccess ||
         cudaMemcpyAsync(Jtr, out + 36, sizeof(double) * 6, cudaMemcpyDefault, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

@@ -227,9 +227,23 @@ __device__ __forceinline__ bool warp_ldl6(double& m, int li, int lj, double& inv
 // eigen-decomposition that drops the small eigenvalues.
 constexpr int kRedCtas = 8;
 constexpr int kRedUnroll = 28;
+
+// Column col of list tile t's partial sum from its `split` partial rows, in
+// the order of a whole 16 x 16 CTA's sum (cta_partial_sum): 2 rows = the
+// upper and lower 16 x 8 halves; 4 rows = the 8 x 8 quarters in row-major
+// order, ((q00 + q10) + (q01 + q11)).
+__device__ __forceinline__ float tile_partial_sum(const float* __restrict__ tile_out, int t, int split, int col) {
+    const float* r = tile_out + (size_t)t * split * FVGS_POSEDATA_FLOATS + col;
+    if (split == 2) return __fadd_rn(r[0], r[FVGS_POSEDATA_FLOATS]);
+    if (split == 4)
+        return __fadd_rn(__fadd_rn(r[0], r[FVGS_POSEDATA_FLOATS]),
+                         __fadd_rn(r[2 * FVGS_POSEDATA_FLOATS], r[3 * FVGS_POSEDATA_FLOATS]));
+    return r[0];
+}
+
 template <bool DO_GN>
-__device__ __forceinline__ void track_reduce_body(const float* __restrict__ tile_out, int num_tiles, DevPose* pose,
-                                                  double* out, double eig_eps, double* step_out) {
+__device__ __forceinline__ void track_reduce_body(const float* __restrict__ tile_out, int num_tiles, int split,
+                                                  DevPose* pose, double* out, double eig_eps, double* step_out) {
     __shared__ double s_w[8][32];
     __shared__ double s_part[32];
     __shared__ double s_tot[27];
@@ -259,7 +273,7 @@ __device__ __forceinline__ void track_reduce_body(const float* __restrict__ tile
 #pragma unroll
         for (int u = 0; u < kRedUnroll; ++u) {
             const int t = t0 + u * stride;
-            x[u] = t < num_tiles ? tile_out[(size_t)t * FVGS_POSEDATA_FLOATS + col] : 0.f;
+            x[u] = t < num_tiles ? tile_partial_sum(tile_out, t, split, col) : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < kRedUnroll; ++u) {
@@ -452,10 +466,10 @@ __device__ __forceinline__ void track_reduce_body(const float* __restrict__ tile
 
 template <bool DO_GN>
 __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
-    track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles, DevPose* pose, double* out,
+    track_reduce_kernel(const float* __restrict__ tile_out, int num_tiles, int split, DevPose* pose, double* out,
                         double eig_eps, double* step_out) {
     pdl_begin();
-    track_reduce_body<DO_GN>(tile_out, num_tiles, pose, out, eig_eps, step_out);
+    track_reduce_body<DO_GN>(tile_out, num_tiles, split, pose, out, eig_eps, step_out);
 }
 
 // The frame reduction and Gauss-Newton step of many sessions in one launch:
@@ -464,7 +478,7 @@ __global__ void __cluster_dims__(kRedCtas, 1, 1) __launch_bounds__(256)
     track_reduce_batch_kernel(const ReduceJob* __restrict__ jobs) {
     pdl_begin();
     const ReduceJob& j = jobs[blockIdx.x / kRedCtas];
-    track_reduce_body<true>(j.tile_out, j.num_tiles, j.pose, j.out, j.eig_eps, j.step_out);
+    track_reduce_body<true>(j.tile_out, j.num_tiles, j.split > 1 ? j.split : 1, j.pose, j.out, j.eig_eps, j.step_out);
 }
 
 namespace {
@@ -485,10 +499,11 @@ KernelPick pick() {
 }
 
 // Tiles of 8 x 8 and 32 x 8: the staging batch is the only launch choice;
-// MIN_CTAS keeps the register budget of the 16 x 16 kernels (64 per thread).
+// MIN_CTAS gives the register budget of the 16 x 16 kernels' variant 1 for
+// the analytic Jacobian (80 per thread) and of variant 0 otherwise (64).
 template <int TW, int TH, bool ANALYTIC>
 KernelPick pick_shape(int variant) {
-    constexpr int M = 1024 / (TW * TH);
+    constexpr int M = (ANALYTIC ? 768 : 1024) / (TW * TH);
     const int batch = track_variant_batch(variant);
     if (batch == 128) return pick<TW, TH, false, false, M, false, 128, ANALYTIC>();
     if (batch == 512) return pick<TW, TH, false, false, M, false, 512, ANALYTIC>();
@@ -502,6 +517,8 @@ KernelPick pick_track(const TrackArgs& a, bool have_maps) {
     const bool analytic = !(a.quirks & FVGS_Q_POSE_JAC_APPROX);
     const int tw = a.tile_w ? a.tile_w : kTW, th = a.tile_h ? a.tile_h : kTH;
     if (a.compensated && (!analytic || tw != kTW || th != kTH)) return {};
+    const int split = a.split > 1 ? a.split : 1;
+    if (split > 1 && (a.compensated || a.render_only || tw != kTW || th != kTH)) return {};
     if (a.render_only) {
         if (tw != kTW || th != kTH) return {};
         return pick<16, 16, true, false, 4, false, kBatch, false>();
@@ -510,15 +527,25 @@ KernelPick pick_track(const TrackArgs& a, bool have_maps) {
     if (tw == 32 && th == 8)
         return analytic ? pick_shape<32, 8, true>(a.variant) : pick_shape<32, 8, false>(a.variant);
     if (tw != kTW || th != kTH) return {};
-    if (analytic && a.compensated) return pick<16, 16, false, false, 4, false, 256, true, true>();
+    if (analytic && a.compensated) return pick<16, 16, false, false, 3, false, 256, true, true>();
+    // 16 x 16 lists over 2 or 4 CTAs (the split matches the variant)
+    if (split != track_variant_split(a.variant)) return {};
+    if (a.variant == 5)
+        return analytic ? pick<16, 8, false, false, 6, false, 128, true>()
+                        : pick<16, 8, false, false, 8, false, 128, false>();
+    if (a.variant == 6)
+        return analytic ? pick<8, 8, false, false, 12, false, 128, true>()
+                        : pick<8, 8, false, false, 16, false, 128, false>();
     if (analytic) {
         // analytic Jacobian: plain staging (no TMA variant)
         if (a.variant == 1) return pick<16, 16, false, false, 3, false, 256, true>();
+        if (a.variant == 7) return pick<16, 16, false, false, 2, false, 256, true>();
         if (a.variant == 3) return pick<16, 16, false, false, 4, false, 128, true>();
         if (a.variant == 4) return pick<16, 16, false, false, 4, false, 512, true>();
         return pick<16, 16, false, false, 4, false, 256, true>();
     }
     if (a.variant == 1) return pick<16, 16, false, false, 3, false, 256, false>();
+    if (a.variant == 7) return pick<16, 16, false, false, 2, false, 256, false>();
     if (a.variant == 3) return pick<16, 16, false, false, 4, false, 128, false>();
     if (a.variant == 4) return pick<16, 16, false, false, 4, false, 512, false>();
     if (a.variant == 2 && have_maps) return pick<16, 16, false, false, 4, true, 256, false>();
@@ -540,6 +567,7 @@ cudaError_t track_configure_device() {
                     a.tile_w = shape == 0 ? 16 : (shape == 1 ? 8 : 32);
                     a.tile_h = shape == 0 ? 16 : 8;
                     a.variant = v % kTrackVariants;
+                    if (shape == 0 && !a.compensated && !render) a.split = track_variant_split(a.variant);
                     const KernelPick k = pick_track(a, true);
                     if (!k.fn) continue;
                     const cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k.fn),
@@ -555,7 +583,7 @@ cudaError_t track_configure_device() {
 }
 
 cudaError_t launch_track(const TrackArgs& a, const RecMaps* maps, cudaStream_t s) {
-    const int T = a.ntx * a.nty;
+    const int T = a.ntx * a.nty * (a.split > 1 ? a.split : 1);
     if (T <= 0) return cudaSuccess;
     if (!a.render_only && !(a.quirks & FVGS_Q_POSE_JAC_APPROX) && (!a.geo0 || !a.geo1)) return cudaErrorInvalidValue;
     if (a.variant == 2 && !a.render_only && (a.quirks & FVGS_Q_POSE_JAC_APPROX) &&
@@ -575,10 +603,10 @@ cudaError_t launch_track_ref_layout(const TrackArgs& a, cudaStream_t s) {
                           body_smem_bytes<16, 16, kBatch, false, false>(), s, a, RecMaps{});
 }
 
-cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, DevPose* pose, double* out,
+cudaError_t launch_track_reduce(const float* tile_out, int num_tiles, int split, DevPose* pose, double* out,
                                 cudaStream_t s) {
-    return launch_chained(track_reduce_kernel<false>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles, pose, out,
-                          0.0, static_cast<double*>(nullptr));
+    return launch_chained(track_reduce_kernel<false>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles,
+                          split > 1 ? split : 1, pose, out, 0.0, static_cast<double*>(nullptr));
 }
 
 cudaError_t launch_track_reduce_batch(const ReduceJob* jobs, int n_jobs, cudaStream_t s) {
@@ -586,10 +614,10 @@ cudaError_t launch_track_reduce_batch(const ReduceJob* jobs, int n_jobs, cudaStr
     return launch_chained(track_reduce_batch_kernel, dim3(kRedCtas * n_jobs), dim3(256), 0, s, jobs);
 }
 
-cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, DevPose* pose, double* out,
+cudaError_t launch_track_reduce_gn(const float* tile_out, int num_tiles, int split, DevPose* pose, double* out,
                                    double eig_eps, double* step_out, cudaStream_t s) {
-    return launch_chained(track_reduce_kernel<true>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles, pose, out,
-                          eig_eps, step_out);
+    return launch_chained(track_reduce_kernel<true>, dim3(kRedCtas), dim3(256), 0, s, tile_out, num_tiles,
+                          split > 1 ? split : 1, pose, out, eig_eps, step_out);
 }
 
 }  // namespace fvgs

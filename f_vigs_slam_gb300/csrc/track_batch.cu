@@ -82,9 +82,11 @@ struct BatchPick {
     size_t smem = 0;
 };
 
+// Register budget: 64 per thread for the reference Jacobian, 80 for the
+// analytic one (its single fused pass holds the colour-Jacobian sums).
 template <int TW, int TH, int BATCH, bool ANALYTIC>
 BatchPick bpick() {
-    return {track_batch_kernel<TW, TH, BATCH, ANALYTIC, 1024 / (TW * TH)>, TW * TH,
+    return {track_batch_kernel<TW, TH, BATCH, ANALYTIC, (ANALYTIC ? 768 : 1024) / (TW * TH)>, TW * TH,
             body_smem_bytes<TW, TH, BATCH, ANALYTIC, false>()};
 }
 

@@ -269,7 +269,9 @@ enum StageExtra { kStageNone = 0, kStageRay = 1, kStageDeriv = 2 };
 //   d Sigma2D = dJ M + (dJ M)^T (+ the rotated-covariance terms
 //   2 J0 x M0, J0 x M1 + J1 x M0, 2 J1 x M1 for dtheta), dQ = -Q dSigma2D Q.
 // r0, r1: the blending record; g0, g1: the geometry record (camera-frame
-// covariance and mean).  out: du[6], dv[6], da[6], db[6], dc[6], x, y.
+// covariance and mean).  out: du, dv, da, db, dc grouped by pairs of pose
+// coordinates (2m, 2m + 1), each quantity's pair adjacent (the order the
+// fused pass reads them in, deriv_pairs), then the mean's x, y.
 __device__ __forceinline__ void stage_deriv(const TrackArgs& a, const float4& r0, const float4& r1, const float4& g0,
                                             const float4& g1, float4 (&out)[8]) {
     const bool swap = (a.quirks & FVGS_Q_INVSIGMA_SWAP) != 0;
@@ -318,14 +320,31 @@ __device__ __forceinline__ void stage_deriv(const TrackArgs& a, const float4& r0
         db[k] = swap ? dq11 : dq01;
         dc[k] = swap ? dq01 : dq11;
     }
-    out[0] = make_float4(du[0], du[1], du[2], du[3]);
-    out[1] = make_float4(du[4], du[5], dv[0], dv[1]);
-    out[2] = make_float4(dv[2], dv[3], dv[4], dv[5]);
-    out[3] = make_float4(da[0], da[1], da[2], da[3]);
-    out[4] = make_float4(da[4], da[5], db[0], db[1]);
-    out[5] = make_float4(db[2], db[3], db[4], db[5]);
-    out[6] = make_float4(dc[0], dc[1], dc[2], dc[3]);
+    out[0] = make_float4(du[0], du[1], dv[0], dv[1]);
+    out[1] = make_float4(da[0], da[1], db[0], db[1]);
+    out[2] = make_float4(dc[0], dc[1], du[2], du[3]);
+    out[3] = make_float4(dv[2], dv[3], da[2], da[3]);
+    out[4] = make_float4(db[2], db[3], dc[2], dc[3]);
+    out[5] = make_float4(du[4], du[5], dv[4], dv[5]);
+    out[6] = make_float4(da[4], da[5], db[4], db[5]);
     out[7] = make_float4(dc[4], dc[5], x, y);
+}
+
+// The derivatives of pose-coordinate pair m (2m, 2m + 1) of staged Gaussian
+// j (stage_deriv's layout): du, dv, da, db, dc as float2 (register pairs).
+struct DerivPair {
+    float2 du, dv, da, db, dc;
+};
+template <int BATCH, int NX>
+__device__ __forceinline__ void deriv_pairs(const float4 (&X)[NX][BATCH], int j, DerivPair (&d)[3]) {
+    const float4 p0 = X[0][j], p1 = X[1][j], p2 = X[2][j], p3 = X[3][j];
+    const float4 p4 = X[4][j], p5 = X[5][j], p6 = X[6][j], p7 = X[7][j];
+    d[0] = {make_float2(p0.x, p0.y), make_float2(p0.z, p0.w), make_float2(p1.x, p1.y), make_float2(p1.z, p1.w),
+            make_float2(p2.x, p2.y)};
+    d[1] = {make_float2(p2.z, p2.w), make_float2(p3.x, p3.y), make_float2(p3.z, p3.w), make_float2(p4.x, p4.y),
+            make_float2(p4.z, p4.w)};
+    d[2] = {make_float2(p5.x, p5.y), make_float2(p5.z, p5.w), make_float2(p6.x, p6.y), make_float2(p6.z, p6.w),
+            make_float2(p7.x, p7.y)};
 }
 
 template <int STAGE, int TW, int TH, int BATCH, int NX, int NT>
@@ -606,12 +625,40 @@ __device__ __forceinline__ TmaStage& body_tma_stage(unsigned char* dyn) {
 
 // One tile of the fused tracking kernel, run by a CTA of TW * TH threads (one
 // per pixel; each warp covers an 8 x 4 pixel block).  Tile shapes: 16 x 16
-// (the reference's), 8 x 8 and 32 x 8; the binning must use the same shape.
-// Ends with the tile's 27 partials written to a.tile_out[tile].
+// (the reference's), 8 x 8 and 32 x 8; the binning must use the same shape,
+// except that a 16 x 16 list tile may be split over a.split CTAs of 16 x 8
+// or 8 x 8 pixels (CTA `tile` covers part (tile % split) of list tile
+// tile / split).  Ends with the CTA's 27 partials written to
+// a.tile_out[tile]: the sum over its warps in the order of tile_partial_sum.
 // COMP (precision form, analytic Jacobian only): the forward blend's colour
 // accumulated with Kahan summation, and the in-tile sums of the 27 J^T J /
 // J^T r partials compensated (warp_reduce_scatter32_comp, then TwoSum across
 // warps); the tile-to-frame sum is compensated in every form.
+// The sum of a CTA's warp partials (column col of s_red).  16 pixels wide:
+// per 8-row band, (left 8 x 8 quadrant + right quadrant), each quadrant its
+// upper + lower warp, then band 0 + band 1 -- so a 16 x 16 tile's sum is
+// ((q00 + q10) + (q01 + q11)) whether one CTA forms it or the frame
+// reduction adds the partials of 16 x 8 or 8 x 8 CTAs (tile_partial_sum).
+// Other widths: the warps in order.
+template <int TW, int TH>
+__device__ __forceinline__ float cta_partial_sum(const float (*s_red)[32], int col) {
+    constexpr int NW = TW * TH / 32;
+    if constexpr (TW == 16) {
+        float s = __fadd_rn(__fadd_rn(s_red[0][col], s_red[2][col]), __fadd_rn(s_red[1][col], s_red[3][col]));
+        if constexpr (TH == 16)
+            s = __fadd_rn(s, __fadd_rn(__fadd_rn(s_red[4][col], s_red[6][col]),
+                                       __fadd_rn(s_red[5][col], s_red[7][col])));
+        return s;
+    } else if constexpr (TW == 8 && TH == 8) {
+        return __fadd_rn(s_red[0][col], s_red[1][col]);
+    } else {
+        float s = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) s += s_red[w][col];
+        return s;
+    }
+}
+
 template <int TW, int TH, bool RENDER_ONLY, bool REF_LAYOUT, bool TMA, int BATCH, bool ANALYTIC,
           bool COMP = false>
 __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMaps& maps, int tile,
@@ -619,6 +666,7 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
     constexpr int NT = TW * TH;
     static_assert(!COMP || ANALYTIC, "compensated accumulation: analytic Jacobian");
     static_assert(TW % 8 == 0 && TH % 4 == 0 && NT % 32 == 0 && NT <= 256, "tile of 8 x 4 pixel warps");
+    static_assert(TW != 16 || TH == 8 || TH == 16, "16-wide CTAs: 8-row bands");
     static_assert(!TMA || (BATCH == kBatch && TW == kTW && TH == kTH),
                   "the TMA staging gathers batches of kBatch records for 16 x 16 tiles");
     static_assert(BATCH % 128 == 0 && BATCH <= 512, "batch of 128, 256 or 512 Gaussians");
@@ -630,15 +678,26 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
     TmaStage& ts = body_tma_stage<TW, TH, BATCH, ANALYTIC>(dyn);
     TmaState tm;
 
-    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    // the list tile and this CTA's pixel block in it
+    const int split = a.split > 1 ? a.split : 1;
+    const int lt = split == 1 ? tile : tile / split;
+    int bx = 0, by = 0, ltw = TW, lth = TH;
+    if (split > 1) {
+        const int sub = tile - lt * split;
+        bx = (sub % (16 / TW)) * TW;
+        by = (sub / (16 / TW)) * TH;
+        ltw = lth = 16;
+    }
+    const int tx = lt % a.ntx, ty = lt / a.ntx;
+    const int px0 = tx * ltw + bx, py0 = ty * lth + by;
     const int tid = threadIdx.x;
     // each warp covers an 8 x 4 pixel block (compact footprint: less divergence)
     const int wq = tid >> 5, lq = tid & 31;
-    const int x = tx * TW + (wq % (TW / 8)) * 8 + (lq & 7), y = ty * TH + (wq / (TW / 8)) * 4 + (lq >> 3);
-    const float x0 = (float)(tx * TW), y0 = (float)(ty * TH);
+    const int x = px0 + (wq % (TW / 8)) * 8 + (lq & 7), y = py0 + (wq / (TW / 8)) * 4 + (lq >> 3);
+    const float x0 = (float)px0, y0 = (float)py0;
     const bool in_bounds = (x < a.W && y < a.H);
     const size_t p = (size_t)y * a.W + x;
-    uint2 range = a.ranges[tile];
+    uint2 range = a.ranges[lt];
     range.y = min(range.y, a.n_list);
     const int n = range.y > range.x ? (int)(range.y - range.x) : 0;
     const float xf = (float)x, yf = (float)y;
@@ -648,12 +707,29 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
     const bool inside = RENDER_ONLY ? in_bounds : (in_bounds && img_depth > 0.1f);
 
     // ------------------------- pass 1: forward blend -------------------------
+    // FUSED (analytic Jacobian): the colour and depth Jacobians are
+    // accumulated in this pass, so there is no second pass over the list.
+    // Each blended Gaussian contributes
+    //   kf (c T - (C - A) / (1 - alpha)) dv/dpose
+    // per channel (A: colour accumulated up to and including it, C: the final
+    // colour with background, kf = dalpha/dv = -alpha / 2, 0 where alpha is
+    // clamped at 0.99); C is known only at the end, so with it factored out
+    //   S1 += (kf c T + kf A / (1 - alpha)) dv/dpose,  S2 += kf / (1 - alpha) dv/dpose,
+    // and the colour Jacobian is S1 - C S2.  (The reference's second pass
+    // walks the list again with the remaining colour C - A.)
+    constexpr bool FUSED = ANALYTIC && !RENDER_ONLY;
     float T = 1.f, cr = 0.f, cg = 0.f, cb = 0.f, depth = 0.f;
     float ccr = 0.f, ccg = 0.f, ccb = 0.f;  // Kahan carries of the colour (COMP)
     uint32_t last = 0;
     bool done = !inside;
     float final_T = 1.f;
     uint32_t n_contrib = 0;
+    float2 fs1[3][3], fs2[3];  // FUSED: S1 (channel, pose pair) and S2 (pose pair)
+    float fjd[6];              // FUSED: depth Jacobian
+#pragma unroll
+    for (int m = 0; m < 3; ++m) fs1[0][m] = fs1[1][m] = fs1[2][m] = fs2[m] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) fjd[k] = 0.f;
     if (n > 0) {
         if (TMA) tma_begin(a, maps, ts, range.x, n, tm);
         for (int base = 0; base < n; base += BATCH) {
@@ -662,9 +738,123 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
             if constexpr (TMA)
                 cnt = stage_batch_tma<true>(a, maps, sb, ts, range.x, base, n, x0, y0, tm);
             else
-                cnt = stage_batch<REF_LAYOUT, true, kStageNone, TW, TH>(a, sb, range.x, base, n, x0, y0);
+                cnt = stage_batch<REF_LAYOUT, true, FUSED ? kStageDeriv : kStageNone, TW, TH>(a, sb, range.x,
+                                                                                                 base, n, x0, y0);
             build_warp_bitmaps(sb, cnt);
-            if (!done) {
+            if (FUSED && !done) {
+                int last_j = -1;
+                // one staged Gaussian with its conic-form gradient (dl0, dl1):
+                // returns false when the pixel terminates
+                auto blend_jac = [&](int j, float dx, float dy, float dl0, float dl1, float v) -> bool {
+                    const float4 rB = sb.B[j];
+                    const float raw = gauss_weight(rB.z, v);
+                    const float alpha = fminf(0.99f, raw);
+                    if (alpha < kInv255) return true;
+                    const float test_T = T * (1.0f - alpha);
+                    if (test_T < 0.0001f) return false;
+                    const float4 rC = sb.C[j];
+                    const float cB = sb.D[j];
+                    const float aT = alpha * T;
+                    if constexpr (COMP) {
+                        kahan_add(cr, ccr, rC.z * aT);
+                        kahan_add(cg, ccg, rC.w * aT);
+                        kahan_add(cb, ccb, cB * aT);
+                    } else {
+                        cr += rC.z * aT;
+                        cg += rC.w * aT;
+                        cb += cB * aT;
+                    }
+                    const float inv1m = rcp_approx(1.0f - alpha);
+                    const float kf = (raw > 0.99f) ? 0.0f : -0.5f * alpha;
+                    const float kfi = kf * inv1m;
+                    const float kT = kf * T;
+                    const float2 w0 = make_float2(kT * rC.z + kfi * cr, kT * rC.z + kfi * cr);
+                    const float2 w1 = make_float2(kT * rC.w + kfi * cg, kT * rC.w + kfi * cg);
+                    const float2 w2 = make_float2(kT * cB + kfi * cb, kT * cB + kfi * cb);
+                    const float2 wi = make_float2(kfi, kfi);
+                    const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
+                    const float2 cu2 = make_float2(cu, cu), cv2 = make_float2(cv, cv), ca2 = make_float2(ca, ca),
+                                 cb22 = make_float2(cb2, cb2), cc2 = make_float2(cc, cc);
+                    DerivPair d[3];
+                    deriv_pairs(sb.X, j, d);
+#pragma unroll
+                    for (int m = 0; m < 3; ++m) {
+                        // dv/dpose = cu du + cv dv + ca da + cb2 db + cc dc for pose pair m
+                        float2 gv = __fmul2_rn(cu2, d[m].du);
+                        gv = __ffma2_rn(cv2, d[m].dv, gv);
+                        gv = __ffma2_rn(ca2, d[m].da, gv);
+                        gv = __ffma2_rn(cb22, d[m].db, gv);
+                        gv = __ffma2_rn(cc2, d[m].dc, gv);
+                        fs1[0][m] = __ffma2_rn(w0, gv, fs1[0][m]);
+                        fs1[1][m] = __ffma2_rn(w1, gv, fs1[1][m]);
+                        fs1[2][m] = __ffma2_rn(w2, gv, fs1[2][m]);
+                        fs2[m] = __ffma2_rn(wi, gv, fs2[m]);
+                    }
+                    if (T > 0.5f && test_T < 0.5f) {
+                        const float4 rA = sb.A[j];
+                        depth = depth_at(rB.w, rA.x, xf, rC.x, rA.y, yf, rC.y);
+                        // d depth = d z + phat . d(dx, dy) + (dx, dy) . d phat, with
+                        // d phat = (dp_x / z^2 - 2 x dp_z / z^3, dp_y / z^2 - 2 y dp_z / z^3)
+                        const float z = rB.w, x = sb.X[7][j].z, y = sb.X[7][j].w;
+                        const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) {
+                            const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
+                            const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
+                            const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
+                            const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
+                            const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
+                            const float du_k = (k & 1) ? d[k >> 1].du.y : d[k >> 1].du.x;
+                            const float dv_k = (k & 1) ? d[k >> 1].dv.y : d[k >> 1].dv.x;
+                            fjd[k] = dpz + rC.x * du_k + dx * dphx + rC.y * dv_k + dy * dphy;
+                        }
+                    }
+                    T = test_T;
+                    last_j = j;
+                    return true;
+                };
+                for (int g = 0; g * 32 < cnt && !done; ++g) {
+                    uint32_t bits = sb.bm[wq][g];
+                    while (bits) {
+                        const int j0 = g * 32 + __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        if (bits) {
+                            const int j1 = g * 32 + __ffs(bits) - 1;
+                            bits &= bits - 1;
+                            const float4 rA0 = sb.A[j0], rA1 = sb.A[j1];
+                            const float2 rB0 = *reinterpret_cast<const float2*>(&sb.B[j0]);
+                            const float2 rB1 = *reinterpret_cast<const float2*>(&sb.B[j1]);
+                            const float dx0 = rA0.x - xf, dy0 = rA0.y - yf;
+                            const float dx1 = rA1.x - xf, dy1 = rA1.y - yf;
+                            float l00, l01, l10, l11;
+                            const float v0 = conic_form(rA0.z, rA0.w, rB0.x, dx0, dy0, l00, l01);
+                            const float v1 = conic_form(rA1.z, rA1.w, rB1.x, dx1, dy1, l10, l11);
+                            const bool k0 = !(v0 > rB0.y || v0 <= 0.0f);
+                            const bool k1 = !(v1 > rB1.y || v1 <= 0.0f);
+                            if (k0 && !blend_jac(j0, dx0, dy0, l00, l01, v0)) {
+                                done = true;
+                                break;
+                            }
+                            if (k1 && !blend_jac(j1, dx1, dy1, l10, l11, v1)) {
+                                done = true;
+                                break;
+                            }
+                        } else {
+                            const float4 rA = sb.A[j0];
+                            const float2 rB = *reinterpret_cast<const float2*>(&sb.B[j0]);
+                            const float dx = rA.x - xf, dy = rA.y - yf;
+                            float l0, l1;
+                            const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, l0, l1);
+                            if (!(v > rB.y || v <= 0.0f) && !blend_jac(j0, dx, dy, l0, l1, v)) {
+                                done = true;
+                                break;
+                            }
+                        }
+                    }
+                }
+                if (last_j >= 0) last = (uint32_t)sb.orig[last_j] + 1u;
+            }
+            if (!FUSED && !done) {
                 int last_j = -1;  // staged slot of the last blended Gaussian in this batch
                 // one staged Gaussian: returns false when the pixel terminates
                 auto blend = [&](int j, float dx, float dy, float v) -> bool {
@@ -675,15 +865,9 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                     if (test_T < 0.0001f) return false;
                     const float4 rC = sb.C[j];
                     const float aT = alpha * T;
-                    if constexpr (COMP) {
-                        kahan_add(cr, ccr, rC.z * aT);
-                        kahan_add(cg, ccg, rC.w * aT);
-                        kahan_add(cb, ccb, sb.D[j] * aT);
-                    } else {
-                        cr += rC.z * aT;
-                        cg += rC.w * aT;
-                        cb += sb.D[j] * aT;
-                    }
+                    cr += rC.z * aT;
+                    cg += rC.w * aT;
+                    cb += sb.D[j] * aT;
                     if (T > 0.5f && test_T < 0.5f) depth = depth_at(rB.w, sb.A[j].x, xf, rC.x, sb.A[j].y, yf, rC.y);
                     T = test_T;
                     last_j = j;
@@ -823,105 +1007,50 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
         bv[5] += img_depth * (rx * Jr1 - ry * Jr0);
     }
 
-    // ------------------- pass 2: per-Gaussian terms --------------------------
-    if (tid == 0) s_nmax = 0;
-    __syncthreads();
-    if (do_jac && n_contrib > 0) atomicMax(&s_nmax, n_contrib);
-    __syncthreads();
-    const int nmax = (int)min((uint32_t)n, s_nmax);
+    // ------------------- pass 2 (reference Jacobian): per-Gaussian terms ---
+    int nmax = 0;
+    if constexpr (!FUSED) {
+        if (tid == 0) s_nmax = 0;
+        __syncthreads();
+        if (do_jac && n_contrib > 0) atomicMax(&s_nmax, n_contrib);
+        __syncthreads();
+        nmax = (int)min((uint32_t)n, s_nmax);
+    }
     if constexpr (ANALYTIC) {
-        // Colour Jacobian jc (3 x 6) and depth Jacobian jd of the pixel over
-        // the Gaussians the forward pass blended, in its order: for each,
-        // dC/dalpha = c T - (C - A) / (1 - alpha) (A: colour accumulated up
-        // to and including it, C: final colour with background), dalpha/dv =
-        // -alpha / 2 (0 where alpha is clamped at 0.99) and dv/ddelta from
-        // the staged derivatives; jd is the derivative of
-        // d = z + dx phat.x + dy phat.y of the Gaussian where T crosses 0.5.
-        float jc[3][6], jd[6];
+        // Colour Jacobian jc (3 x 6) of the pixel from the fused pass's sums:
+        // jc = S1 - C S2 (C: the final colour with background); jd: the depth
+        // Jacobian of the Gaussian where T crossed 0.5.  Pose coordinates in
+        // pairs (2m, 2m + 1), packed FP32 FMAs (two IEEE round-to-nearest
+        // FMAs each, the results of __fmaf_rn).
+        float2 jc2[3][3];
+        const float2 nr = make_float2(-cr, -cr), ng = make_float2(-cg, -cg), nb = make_float2(-cb, -cb);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            jc[0][k] = jc[1][k] = jc[2][k] = 0.f;
-            jd[k] = 0.f;
+        for (int m = 0; m < 3; ++m) {
+            jc2[0][m] = __ffma2_rn(nr, fs2[m], fs1[0][m]);
+            jc2[1][m] = __ffma2_rn(ng, fs2[m], fs1[1][m]);
+            jc2[2][m] = __ffma2_rn(nb, fs2[m], fs1[2][m]);
         }
-        float prod = 1.f, remr = cr, remg = cg, remb = cb;
-        bool done2 = !do_jac;
-        for (int base = 0; base < nmax; base += BATCH) {
-            if (__syncthreads_and(done2)) break;
-            const int cnt = stage_batch<false, true, kStageDeriv, TW, TH>(a, sb, range.x, base, nmax, x0, y0);
-            build_warp_bitmaps(sb, cnt);
-            if (done2) continue;
-            for (int g = 0; g * 32 < cnt && !done2; ++g) {
-                for (uint32_t bits = sb.bm[wq][g]; bits; bits &= bits - 1) {
-                    const int j = g * 32 + __ffs(bits) - 1;
-                    if (sb.orig[j] >= (int)n_contrib) {
-                        done2 = true;
-                        break;
-                    }
-                    const float4 rA = sb.A[j];
-                    const float4 rB = sb.B[j];
-                    const float dx = rA.x - xf, dy = rA.y - yf;
-                    float dl0, dl1;
-                    const float v = conic_form(rA.z, rA.w, rB.x, dx, dy, dl0, dl1);
-                    if (v > rB.y || v <= 0.0f) continue;
-                    const float raw = gauss_weight(rB.z, v);
-                    const float alpha = fminf(0.99f, raw);
-                    if (alpha < kInv255) continue;
-                    const float4 rC = sb.C[j];
-                    float d0 = rC.z * prod, d1 = rC.w * prod, d2 = sb.D[j] * prod;
-                    remr -= alpha * d0;
-                    remg -= alpha * d1;
-                    remb -= alpha * d2;
-                    const float inv1m = rcp_approx(1.0f - alpha);
-                    const float kf = (raw > 0.99f) ? 0.0f : -0.5f * alpha;
-                    const float k0 = kf * (d0 - remr * inv1m), k1 = kf * (d1 - remg * inv1m),
-                                k2 = kf * (d2 - remb * inv1m);
-                    const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
-                    const float4 X0 = sb.X[0][j], X1 = sb.X[1][j], X2 = sb.X[2][j], X3 = sb.X[3][j];
-                    const float4 X4 = sb.X[4][j], X5 = sb.X[5][j], X6 = sb.X[6][j], X7 = sb.X[7][j];
-                    const float du[6] = {X0.x, X0.y, X0.z, X0.w, X1.x, X1.y};
-                    const float dv[6] = {X1.z, X1.w, X2.x, X2.y, X2.z, X2.w};
-                    const float da[6] = {X3.x, X3.y, X3.z, X3.w, X4.x, X4.y};
-                    const float db[6] = {X4.z, X4.w, X5.x, X5.y, X5.z, X5.w};
-                    const float dc[6] = {X6.x, X6.y, X6.z, X6.w, X7.x, X7.y};
-                    float gv[6];
-    #pragma unroll
-                    for (int k = 0; k < 6; ++k) {
-                        gv[k] = cu * du[k] + cv * dv[k] + ca * da[k] + cb2 * db[k] + cc * dc[k];
-                        jc[0][k] += k0 * gv[k];
-                        jc[1][k] += k1 * gv[k];
-                        jc[2][k] += k2 * gv[k];
-                    }
-                    const float np = prod * (1.0f - alpha);
-                    if (prod > 0.5f && np < 0.5f) {
-                        // d phat = (dp_x / z^2 - 2 x dp_z / z^3, dp_y / z^2 - 2 y dp_z / z^3)
-                        const float z = rB.w, x = X7.z, y = X7.w;
-                        const float iz = __frcp_rn(z), iz2 = iz * iz, iz3 = iz2 * iz;
-    #pragma unroll
-                        for (int k = 0; k < 6; ++k) {
-                            const float dpx = k == 0 ? -1.f : (k == 4 ? -z : (k == 5 ? y : 0.f));
-                            const float dpy = k == 1 ? -1.f : (k == 3 ? z : (k == 5 ? -x : 0.f));
-                            const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
-                            const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
-                            const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
-                            jd[k] = dpz + rC.x * du[k] + dx * dphx + rC.y * dv[k] + dy * dphy;
-                        }
-                    }
-                    prod = np;
+        const float (&jd)[6] = fjd;
+        if (do_jac) {
+            float jc[3][6];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    jc[c][2 * m] = jc2[c][m].x;
+                    jc[c][2 * m + 1] = jc2[c][m].y;
                 }
-                }
+            int idx = 0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+#pragma unroll
+                for (int k = i; k < 6; ++k)
+                    A[idx++] = wc * (jc[0][i] * jc[0][k] + jc[1][i] * jc[1][k] + jc[2][i] * jc[2][k]) +
+                               wd * jd[i] * jd[k];
+                bv[i] = -(wc * (jc[0][i] * e0 + jc[1][i] * e1 + jc[2][i] * e2) + wd * jd[i] * derr);
             }
-            if (do_jac) {
-                int idx = 0;
-    #pragma unroll
-                for (int i = 0; i < 6; ++i) {
-    #pragma unroll
-                    for (int k = i; k < 6; ++k)
-                        A[idx++] = wc * (jc[0][i] * jc[0][k] + jc[1][i] * jc[1][k] + jc[2][i] * jc[2][k]) +
-                                   wd * jd[i] * jd[k];
-                    bv[i] = -(wc * (jc[0][i] * e0 + jc[1][i] * e1 + jc[2][i] * e2) + wd * jd[i] * derr);
-                }
-            }
-        } else {
+        }
+    } else {
             // rem = final colour minus the colour accumulated so far (running)
             float prod_alpha = 1.f, remr = cr, remg = cg, remb = cb;
             bool depth_pending = img_depth > 0.5f;  // the depth term is added once, where T first falls to 0.5
@@ -1047,12 +1176,8 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
         const float mine = warp_reduce_scatter32(vals);
         s_red[tid >> 5][tid & 31] = mine;
         __syncthreads();
-        if (tid < FVGS_POSEDATA_FLOATS) {
-            float s = 0.f;
-#pragma unroll
-            for (int w = 0; w < NT / 32; ++w) s += s_red[w][tid];
-            a.tile_out[(size_t)tile * FVGS_POSEDATA_FLOATS + tid] = s;
-        }
+        if (tid < FVGS_POSEDATA_FLOATS)
+            a.tile_out[(size_t)tile * FVGS_POSEDATA_FLOATS + tid] = cta_partial_sum<TW, TH>(s_red, tid);
     }
 }
 

@@ -45,7 +45,7 @@ DEBUG_MAPPING = 0x4
 DEBUG_RADIX_SORT = 0x8
 DEBUG_NO_CANDIDATES = 0x10
 
-TRACK_VARIANTS = 5  # FVGS_TRACK_VARIANTS
+TRACK_VARIANTS = 8  # FVGS_TRACK_VARIANTS
 KERNEL_CLASSES = ["project", "scan", "emit", "sort", "ranges", "track", "reduce", "gn", "map_fwd", "map_bwd",
                   "map_update", "render", "maint"]
 K = {name: i for i, name in enumerate(KERNEL_CLASSES)}

@@ -100,13 +100,18 @@ int fvgs_session_set_precision(fvgs_session* s, int precision);
 
 /*
  * Launch autotuner of the Jacobian kernel (batching form).  The kernel has
- * five launch variants with the same arithmetic in the same order:
+ * eight launch variants with the same arithmetic in the same order:
  *   0: four CTAs of 256 threads per SM at 64 registers, batches of 256
  *      Gaussians staged in shared memory;
  *   1: three CTAs per SM at 80 registers;
  *   2: as 0, each batch of records gathered into shared memory by TMA while
  *      the previous batch is blended;
- *   3, 4: as 0 with batches of 128 and 512 Gaussians.
+ *   3, 4: as 0 with batches of 128 and 512 Gaussians;
+ *   5, 6: each 16 x 16 tile's list run by 2 CTAs of 16 x 8 pixels (5) or 4
+ *      CTAs of 8 x 8 pixels (6), batches of 128 Gaussians: more CTAs for the
+ *      few hundred tiles of a coarse pyramid level (16 x 16 tiles without
+ *      compensated sums only; otherwise they run as 3);
+ *   7: two CTAs per SM at 128 registers.
  * Which is faster depends on the map and frame.  On the first frame of a new frame shape of a
  * pyramid level (fvgs_track_frame, fvgs_frame_submit) the session bins the
  * frame at the request's pose, times every variant on that binning and keeps
@@ -117,7 +122,7 @@ int fvgs_session_set_precision(fvgs_session* s, int precision);
  * shapes; fvgs_session_set_track_variant restores a known choice.  No
  * reference counterpart.
  */
-#define FVGS_TRACK_VARIANTS 5
+#define FVGS_TRACK_VARIANTS 8
 int fvgs_session_autotune(fvgs_session* s, const fvgs_pose* pose, const fvgs_intrinsics* K, int level, int reps,
                           int* variant, float* ms);
 int fvgs_session_set_autotune(fvgs_session* s, int enabled);
