@@ -537,12 +537,14 @@ KernelPick pick_track(const TrackArgs& a, bool have_maps) {
         return analytic ? pick<8, 8, false, false, 12, false, 128, true>()
                         : pick<8, 8, false, false, 16, false, 128, false>();
     if (analytic) {
-        // analytic Jacobian: plain staging (no TMA variant)
-        if (a.variant == 1) return pick<16, 16, false, false, 3, false, 256, true>();
-        if (a.variant == 7) return pick<16, 16, false, false, 2, false, 256, true>();
-        if (a.variant == 3) return pick<16, 16, false, false, 4, false, 128, true>();
-        if (a.variant == 4) return pick<16, 16, false, false, 4, false, 512, true>();
-        return pick<16, 16, false, false, 4, false, 256, true>();
+        // analytic Jacobian: plain staging (no TMA variant), one CTA per SM
+        // fewer than the reference Jacobian's variants (its fused pass holds
+        // the colour-Jacobian sums: 80 registers at three CTAs, 128 at two)
+        if (a.variant == 1) return pick<16, 16, false, false, 2, false, 256, true>();
+        if (a.variant == 7) return pick<16, 16, false, false, 2, false, 128, true>();
+        if (a.variant == 3) return pick<16, 16, false, false, 3, false, 128, true>();
+        if (a.variant == 4) return pick<16, 16, false, false, 3, false, 512, true>();
+        return pick<16, 16, false, false, 3, false, 256, true>();
     }
     if (a.variant == 1) return pick<16, 16, false, false, 3, false, 256, false>();
     if (a.variant == 7) return pick<16, 16, false, false, 2, false, 256, false>();

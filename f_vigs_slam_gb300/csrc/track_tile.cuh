@@ -335,16 +335,25 @@ __device__ __forceinline__ void stage_deriv(const TrackArgs& a, const float4& r0
 struct DerivPair {
     float2 du, dv, da, db, dc;
 };
+// One pair at a time (three or two 16-byte and one 8-byte shared load), so
+// the fused pass holds one pair's ten values rather than all thirty.
 template <int BATCH, int NX>
-__device__ __forceinline__ void deriv_pairs(const float4 (&X)[NX][BATCH], int j, DerivPair (&d)[3]) {
-    const float4 p0 = X[0][j], p1 = X[1][j], p2 = X[2][j], p3 = X[3][j];
-    const float4 p4 = X[4][j], p5 = X[5][j], p6 = X[6][j], p7 = X[7][j];
-    d[0] = {make_float2(p0.x, p0.y), make_float2(p0.z, p0.w), make_float2(p1.x, p1.y), make_float2(p1.z, p1.w),
-            make_float2(p2.x, p2.y)};
-    d[1] = {make_float2(p2.z, p2.w), make_float2(p3.x, p3.y), make_float2(p3.z, p3.w), make_float2(p4.x, p4.y),
-            make_float2(p4.z, p4.w)};
-    d[2] = {make_float2(p5.x, p5.y), make_float2(p5.z, p5.w), make_float2(p6.x, p6.y), make_float2(p6.z, p6.w),
-            make_float2(p7.x, p7.y)};
+__device__ __forceinline__ DerivPair deriv_pair(const float4 (&X)[NX][BATCH], int j, int m) {
+    auto lo = [&](int plane) { return *reinterpret_cast<const float2*>(&X[plane][j].x); };
+    auto hi = [&](int plane) { return *reinterpret_cast<const float2*>(&X[plane][j].z); };
+    if (m == 0) {
+        const float4 p0 = X[0][j], p1 = X[1][j];
+        return {make_float2(p0.x, p0.y), make_float2(p0.z, p0.w), make_float2(p1.x, p1.y), make_float2(p1.z, p1.w),
+                lo(2)};
+    }
+    if (m == 1) {
+        const float4 p3 = X[3][j], p4 = X[4][j];
+        return {hi(2), make_float2(p3.x, p3.y), make_float2(p3.z, p3.w), make_float2(p4.x, p4.y),
+                make_float2(p4.z, p4.w)};
+    }
+    const float4 p5 = X[5][j], p6 = X[6][j];
+    return {make_float2(p5.x, p5.y), make_float2(p5.z, p5.w), make_float2(p6.x, p6.y), make_float2(p6.z, p6.w),
+            lo(7)};
 }
 
 template <int STAGE, int TW, int TH, int BATCH, int NX, int NT>
@@ -725,11 +734,15 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
     float final_T = 1.f;
     uint32_t n_contrib = 0;
     float2 fs1[3][3], fs2[3];  // FUSED: S1 (channel, pose pair) and S2 (pose pair)
-    float fjd[6];              // FUSED: depth Jacobian
 #pragma unroll
     for (int m = 0; m < 3; ++m) fs1[0][m] = fs1[1][m] = fs1[2][m] = fs2[m] = make_float2(0.f, 0.f);
+    // FUSED: the depth Jacobian, written once where T crosses 0.5 (each
+    // thread its own column: no barrier needed)
+    __shared__ float s_jd[FUSED ? 6 : 1][FUSED ? NT : 1];
+    if constexpr (FUSED) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) fjd[k] = 0.f;
+        for (int k = 0; k < 6; ++k) s_jd[k][tid] = 0.f;
+    }
     if (n > 0) {
         if (TMA) tma_begin(a, maps, ts, range.x, n, tm);
         for (int base = 0; base < n; base += BATCH) {
@@ -775,16 +788,15 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                     const float cu = 2.0f * dl0, cv = 2.0f * dl1, ca = dx * dx, cb2 = 2.0f * dx * dy, cc = dy * dy;
                     const float2 cu2 = make_float2(cu, cu), cv2 = make_float2(cv, cv), ca2 = make_float2(ca, ca),
                                  cb22 = make_float2(cb2, cb2), cc2 = make_float2(cc, cc);
-                    DerivPair d[3];
-                    deriv_pairs(sb.X, j, d);
 #pragma unroll
                     for (int m = 0; m < 3; ++m) {
                         // dv/dpose = cu du + cv dv + ca da + cb2 db + cc dc for pose pair m
-                        float2 gv = __fmul2_rn(cu2, d[m].du);
-                        gv = __ffma2_rn(cv2, d[m].dv, gv);
-                        gv = __ffma2_rn(ca2, d[m].da, gv);
-                        gv = __ffma2_rn(cb22, d[m].db, gv);
-                        gv = __ffma2_rn(cc2, d[m].dc, gv);
+                        const DerivPair d = deriv_pair(sb.X, j, m);
+                        float2 gv = __fmul2_rn(cu2, d.du);
+                        gv = __ffma2_rn(cv2, d.dv, gv);
+                        gv = __ffma2_rn(ca2, d.da, gv);
+                        gv = __ffma2_rn(cb22, d.db, gv);
+                        gv = __ffma2_rn(cc2, d.dc, gv);
                         fs1[0][m] = __ffma2_rn(w0, gv, fs1[0][m]);
                         fs1[1][m] = __ffma2_rn(w1, gv, fs1[1][m]);
                         fs1[2][m] = __ffma2_rn(w2, gv, fs1[2][m]);
@@ -804,9 +816,10 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
                             const float dpz = k == 2 ? -1.f : (k == 3 ? -y : (k == 4 ? x : 0.f));
                             const float dphx = dpx * iz2 - 2.f * x * iz3 * dpz;
                             const float dphy = dpy * iz2 - 2.f * y * iz3 * dpz;
-                            const float du_k = (k & 1) ? d[k >> 1].du.y : d[k >> 1].du.x;
-                            const float dv_k = (k & 1) ? d[k >> 1].dv.y : d[k >> 1].dv.x;
-                            fjd[k] = dpz + rC.x * du_k + dx * dphx + rC.y * dv_k + dy * dphy;
+                            const DerivPair d = deriv_pair(sb.X, j, k >> 1);
+                            const float du_k = (k & 1) ? d.du.y : d.du.x;
+                            const float dv_k = (k & 1) ? d.dv.y : d.dv.x;
+                            s_jd[k][tid] = dpz + rC.x * du_k + dx * dphx + rC.y * dv_k + dy * dphy;
                         }
                     }
                     T = test_T;
@@ -1030,7 +1043,9 @@ __device__ __forceinline__ void track_tile_body(const TrackArgs& a, const RecMap
             jc2[1][m] = __ffma2_rn(ng, fs2[m], fs1[1][m]);
             jc2[2][m] = __ffma2_rn(nb, fs2[m], fs1[2][m]);
         }
-        const float (&jd)[6] = fjd;
+        float jd[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) jd[k] = s_jd[k][tid];
         if (do_jac) {
             float jc[3][6];
 #pragma unroll

@@ -112,8 +112,12 @@ int fvgs_session_set_precision(fvgs_session* s, int precision);
  *      few hundred tiles of a coarse pyramid level (16 x 16 tiles without
  *      compensated sums only; otherwise they run as 3);
  *   7: two CTAs per SM at 128 registers.
- * Which is faster depends on the map and frame.  On the first frame of a new frame shape of a
- * pyramid level (fvgs_track_frame, fvgs_frame_submit) the session bins the
+ * With the analytic Jacobian (whose single fused pass holds the colour
+ * Jacobian's sums) every variant runs one CTA per SM fewer: 0, 3, 4 at three
+ * CTAs and 80 registers, 1 at two CTAs and 128 registers, 7 at two CTAs with
+ * batches of 128; 2 runs as 0.
+ * Which is faster depends on the map and frame.  On the first frame of a new
+ * frame shape of a pyramid level (fvgs_track_frame, fvgs_frame_submit) the session bins the
  * frame at the request's pose, times every variant on that binning and keeps
  * the fastest for that level and shape; results do not depend on the choice.
  * fvgs_session_autotune runs the tuning explicitly (reps timed launches per
