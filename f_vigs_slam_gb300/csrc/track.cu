@@ -10,8 +10,10 @@
 //
 // Per-pixel semantics are the reference's (each pixel scans its tile list,
 // thresholds 0.99 / 1/255 / 1e-4 / 0.5 / 1e-3, the pass-1-only v<=0 skip, the
-// second pass over the first n_contrib entries).  The arithmetic is
-// reorganised for the GPU without changing the mathematics:
+// reference Jacobian's second pass over the first n_contrib entries; the
+// analytic Jacobian accumulates its terms in the forward pass, with the final
+// colour factored out -- track_tile.cuh).  The arithmetic is reorganised for
+// the GPU without changing the mathematics:
 //  * every per-Gaussian colour term is rank one (Jt_cam = jt_dl (x) alpha*dC),
 //    so J_pose * JtJ_cam * J_pose^T becomes one 21-FMA update with
 //    u = (jt_dl, d * (ray x jt_dl)) instead of the reference's 3x3 and 6x3

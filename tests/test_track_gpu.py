@@ -104,6 +104,35 @@ def test_track_jacobian_parity_moved_pose(oracle, fvgs_lib, quirks):
     s.close()
 
 
+@pytest.mark.parametrize("quirks", [REF, INTENDED], ids=["ref", "analytic"])
+def test_track_jacobian_parity_opaque_splats(oracle, fvgs_lib, quirks):
+    """Nearly opaque Gaussians (opacity in [0.9, 1]): alpha reaches the 0.99
+    clamp and 1 / (1 - alpha) reaches 100, the largest factor the analytic
+    Jacobian's single pass (S1 - C S2) and the reference's running remaining
+    colour put on a term's rounding; pixels terminate after a few
+    contributors."""
+    fv = fvgs_lib
+    W, H, K = scaled_camera(0.5)
+    base = S.cam_box(20_000, seed=41)
+    rng = np.random.default_rng(42)
+    scene = S.Scene(base.positions, base.scales, base.orientations, base.colors,
+                    rng.uniform(0.9, 1.0, base.n).astype(np.float32))
+    P = oracle.default_params(quirks)
+    true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
+    frame = make_frame(oracle, scene, true_pose, K, W, H, P)
+    pose = S.perturb(true_pose, 0.5, 1.0, rng)
+    with fv.Session(scene.n, W, H, fv.default_params(quirks)) as s:
+        s.upload(scene)
+        s.set_frame(0, *frame)
+        JtJ, Jtr = s.track_jacobian(pose, K, 0)
+    b = oracle.prepare(scene, pose, K, W, H, P)
+    r = oracle.track(b, frame, pose, K, W, H, P, images=False)
+    e1, e2 = rel_err(JtJ, r.JtJ), rel_err(Jtr, r.Jtr)
+    print("JtJ rel", e1, "Jtr rel", e2)
+    assert e1 <= JAC_RTOL, e1
+    assert e2 <= JAC_RTOL, e2
+
+
 def test_track_deterministic(oracle, fvgs_lib):
     W, H, K, scene, P, frame, s = _setup(oracle, fvgs_lib, 10_000, 0.5, 5)
     pose = (np.array([0.01, 0, 0], np.float32), S.IDENTITY_Q)
