@@ -905,7 +905,28 @@ __global__ void __launch_bounds__(256) emit_scatter_kernel(EmitArgs a, uint32_t*
         scatter_chunks<false>(a, fill, a.keys, a.capacity, (uint32_t)a.n, chunk_counter);
 }
 
+// Copy a binning's sorted lists (the instances of every tile's range) and its
+// ranges into the other buffer pair; positions are unchanged.
+__global__ void __launch_bounds__(256) copy_lists_kernel(const uint2* __restrict__ ranges, int T,
+                                                         const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                                         uint2* __restrict__ ranges_dst, uint64_t capacity) {
+    pdl_begin();
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        const uint2 r = ranges[t];
+        if (threadIdx.x == 0) ranges_dst[t] = r;
+        const uint64_t end = min((uint64_t)r.y, capacity);
+        for (uint64_t i = (uint64_t)r.x + threadIdx.x; i < end; i += blockDim.x) dst[i] = src[i];
+    }
+}
+
 // ------------------------------- launchers ---------------------------------
+cudaError_t launch_copy_lists(const uint2* ranges, int T, const uint32_t* src, uint32_t* dst, uint2* ranges_dst,
+                              uint64_t capacity, int max_ctas, cudaStream_t s) {
+    if (T <= 0) return cudaSuccess;
+    const int grid = T < max_ctas ? T : max_ctas;
+    return launch_chained(copy_lists_kernel, dim3(grid), dim3(256), 0, s, ranges, T, src, dst, ranges_dst, capacity);
+}
+
 cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s) {
     if (a.n <= 0) return cudaSuccess;
     const int need = (a.n + kProjChunk - 1) / kProjChunk;

@@ -28,6 +28,8 @@ using namespace fvgs;
 namespace {
 
 constexpr int kMaxLevels = 4;
+// binning contexts per session: one per tile grid in use (the pyramid levels)
+constexpr int kBinCtx = 4;
 
 struct FrameLevel {
     int W = 0, H = 0;
@@ -100,6 +102,32 @@ int bits_for(int v) {  // bits needed to represent values 0..v-1
     return b;
 }
 
+// A binning context: the state of the binnings of one tile grid (frame size
+// and tile shape) -- its binning records, counts, candidate list, sorted
+// lists (ping-pong) and history -- so the first binning at a pyramid level
+// continues that level's previous binning instead of starting over.
+struct BinCtx {
+    int W = 0, H = 0, tw = 0, th = 0;  // the grid it is bound to (0: none)
+    uint64_t last_use = 0;
+    BinRec* bins = nullptr;
+    uint32_t *counts = nullptr, *cand = nullptr;
+    CandState* cst = nullptr;
+    uint2 *ranges = nullptr, *ranges_prev = nullptr;
+    uint32_t *vals = nullptr, *vals_alt = nullptr;
+    // the pair member a frame leaves the current lists in (ctx_normalize)
+    uint2* ranges_home = nullptr;
+    uint32_t* vals_home = nullptr;
+    bool hist_ok = false;
+    int hist_ntx = 0, hist_nty = 0, hist_tw = 0, hist_th = 0;
+};
+
+// Host-side binning state of every context and the active one (graph entry
+// and exit, capture fallback).
+struct BinSnap {
+    BinCtx c[kBinCtx];
+    int cur = 0;
+};
+
 }  // namespace
 
 struct fvgs_session {
@@ -153,6 +181,14 @@ struct fvgs_session {
     bool keys_valid = false;  // keys[] holds the last binning's reference-format keys
     int hist_ntx = 0, hist_nty = 0, hist_tw = 0, hist_th = 0;
     int bin_tw = 16, bin_th = 16;  // tile shape of the last binning
+    // Binning contexts, one per tile grid (frame size and tile shape) in use
+    // (BinCtx).  The fields bins, counts, cand, cst, ranges, ranges_prev,
+    // vals, sort.vals_alt and hist_* above are the active context's
+    // (ctx_select).
+    BinCtx bctx[kBinCtx];
+    int bctx_cur = 0;
+    uint64_t bctx_clock = 0;
+    CandState* cst_all = nullptr;  // the contexts' candidate-list states, contiguous
 
     FrameLevel lv[kMaxLevels];
     // frame preprocessing: 8-bit colour pyramid and the raw depth of a frame
@@ -244,22 +280,24 @@ struct fvgs_session {
         bool valid = false;
         int iters[kMaxLevels] = {}, W[kMaxLevels] = {}, H[kMaxLevels] = {};
         int map_level = 0;
-        bool entry_incremental = false;  // the frame's first binning continues the previous one
         uint32_t n_g = 0;  // launch shapes and kernel arguments depend on the Gaussian count
         fvgs_intrinsics K[kMaxLevels] = {};
         float eta = -1.f;
         uint64_t gen = 0;
-        // host-side binning state the frame leaves (the tile grid of its last binning)
-        int exit_ntx = 0, exit_nty = 0, exit_W = 0, exit_H = 0, exit_T = 0, exit_split = 1;
-        uint32_t *vals_in = nullptr, *vals_out = nullptr, *vals_alt_out = nullptr;
-        uint2 *ranges_in = nullptr, *ranges_out = nullptr, *ranges_prev_out = nullptr;
+        // the binning contexts the capture started from and left (buffers,
+        // histories), and the frame's last binning
+        BinSnap entry, exit;
+        int exit_W = 0, exit_H = 0, exit_T = 0, exit_split = 1, exit_tw = 16, exit_th = 16;
         uint64_t launches[FVGS_K_COUNT] = {};
         uint64_t last_use = 0;
         cudaGraphExec_t exec = nullptr;
     };
-    // frame shapes x ping-pong parities in use (a frame with an odd number of
-    // binnings swaps the parity for the next one)
-    FrameGraph graphs[4];
+    // frame shapes (regular frame, keyframe) x the binning histories they
+    // start from (a frame leaves every context's lists at the same pair
+    // member, ctx_normalize; after a reset the contexts regain their
+    // histories over the first frames)
+    static constexpr int kFrameGraphs = 6;
+    FrameGraph graphs[kFrameGraphs];
     uint64_t graph_clock = 0;
     uint64_t gen = 1;
     fvgs_pose* d_pose_in = nullptr;
@@ -367,21 +405,153 @@ int refresh_reduced(fvgs_session* s) {
     return FVGS_OK;
 }
 
-int alloc_instances(fvgs_session* s, uint64_t cap) {
+// ---- binning contexts -----------------------------------------------------
+// The active context's state lives in the session's fields; these move it
+// between the fields and the context table.
+void ctx_store(fvgs_session* s) {
+    BinCtx& c = s->bctx[s->bctx_cur];
+    c.bins = s->bins;
+    c.counts = s->counts;
+    c.cand = s->cand;
+    c.cst = s->cst;
+    c.ranges = s->ranges;
+    c.ranges_prev = s->ranges_prev;
+    c.vals = s->vals;
+    c.vals_alt = s->sort.vals_alt;
+    c.hist_ok = s->hist_ok;
+    c.hist_ntx = s->hist_ntx;
+    c.hist_nty = s->hist_nty;
+    c.hist_tw = s->hist_tw;
+    c.hist_th = s->hist_th;
+}
+
+void ctx_load(fvgs_session* s, int i) {
+    s->bctx_cur = i;
+    const BinCtx& c = s->bctx[i];
+    s->bins = c.bins;
+    s->counts = c.counts;
+    s->cand = c.cand;
+    s->cst = c.cst;
+    s->ranges = c.ranges;
+    s->ranges_prev = c.ranges_prev;
+    s->vals = c.vals;
+    s->sort.vals_alt = c.vals_alt;
+    s->hist_ok = c.hist_ok;
+    s->hist_ntx = c.hist_ntx;
+    s->hist_nty = c.hist_nty;
+    s->hist_tw = c.hist_tw;
+    s->hist_th = c.hist_th;
+}
+
+// Make the context of a W x H frame binned on tw x th tiles the active one:
+// the context bound to that grid, else the least recently used one, rebound
+// (its history is for another grid).
+void ctx_select(fvgs_session* s, int W, int H, int tw, int th) {
+    const auto bound = [&](const BinCtx& c) { return c.W == W && c.H == H && c.tw == tw && c.th == th; };
+    if (bound(s->bctx[s->bctx_cur])) {
+        s->bctx[s->bctx_cur].last_use = ++s->bctx_clock;
+        return;
+    }
+    ctx_store(s);
+    int pick = -1;
+    for (int i = 0; i < kBinCtx && pick < 0; ++i)
+        if (bound(s->bctx[i])) pick = i;
+    if (pick < 0) {
+        pick = 0;
+        for (int i = 1; i < kBinCtx; ++i)
+            if (s->bctx[i].last_use < s->bctx[pick].last_use) pick = i;
+        BinCtx& c = s->bctx[pick];
+        c.W = W;
+        c.H = H;
+        c.tw = tw;
+        c.th = th;
+        c.hist_ok = false;
+    }
+    s->bctx[pick].last_use = ++s->bctx_clock;
+    ctx_load(s, pick);
+    s->keys_valid = false;  // keys[] holds another context's binning
+}
+
+// Leave every context's current lists in its home pair member (copying them
+// where the frame's binnings left them in the other): a frame with an odd
+// number of binnings at a level would otherwise swap that context's
+// ping-pong parity, and a captured frame holds the buffer addresses of the
+// parity it was captured at.
+int ctx_normalize(fvgs_session* s) {
+    ctx_store(s);
+    for (auto& c : s->bctx) {
+        if (c.vals == c.vals_home && c.ranges == c.ranges_home) continue;
+        // (a member already at home is copied onto itself: same values)
+        if (c.hist_ok)
+            FV_CK(launch_copy_lists(c.ranges, c.hist_ntx * c.hist_nty, c.vals, c.vals_home, c.ranges_home,
+                                    s->cap_inst, s->num_sms * 8, s->stream));
+        if (c.vals != c.vals_home) std::swap(c.vals, c.vals_alt);
+        if (c.ranges != c.ranges_home) std::swap(c.ranges, c.ranges_prev);
+    }
+    ctx_load(s, s->bctx_cur);
+    return FVGS_OK;
+}
+
+// Every context's binning history is stale (the Gaussians or the instance
+// buffers changed).
+void ctx_drop_history(fvgs_session* s) {
+    for (auto& c : s->bctx) c.hist_ok = false;
     s->hist_ok = false;
+}
+
+void snap_take(fvgs_session* s, BinSnap& b) {
+    ctx_store(s);
+    for (int i = 0; i < kBinCtx; ++i) b.c[i] = s->bctx[i];
+    b.cur = s->bctx_cur;
+}
+void snap_put(fvgs_session* s, const BinSnap& b) {
+    for (int i = 0; i < kBinCtx; ++i) {
+        const uint64_t used = s->bctx[i].last_use;
+        s->bctx[i] = b.c[i];
+        s->bctx[i].last_use = used;
+    }
+    ctx_load(s, b.cur);
+}
+// Whether two snapshots bind the same grids to the same buffers with the same
+// histories (what a captured frame's binnings depend on).
+bool snap_same(const BinSnap& a, const BinSnap& b) {
+    for (int i = 0; i < kBinCtx; ++i) {
+        const BinCtx &x = a.c[i], &y = b.c[i];
+        // a context without history is binned in full from whatever pair
+        // member it holds, and the frame's exit state replaces it
+        if (!x.hist_ok && !y.hist_ok) continue;
+        if (x.W != y.W || x.H != y.H || x.tw != y.tw || x.th != y.th || x.bins != y.bins || x.ranges != y.ranges ||
+            x.ranges_prev != y.ranges_prev || x.vals != y.vals || x.vals_alt != y.vals_alt || x.hist_ok != y.hist_ok ||
+            x.hist_ntx != y.hist_ntx || x.hist_nty != y.hist_nty || x.hist_tw != y.hist_tw || x.hist_th != y.hist_th)
+            return false;
+    }
+    return true;
+}
+
+int alloc_instances(fvgs_session* s, uint64_t cap) {
+    ctx_store(s);
+    ctx_drop_history(s);
     if (s->keys) {
         FV_CK(cudaStreamSynchronize(s->stream));
         dev_free(s, s->keys, s->cap_inst);
-        dev_free(s, s->vals, s->cap_inst);
+        for (auto& c : s->bctx) {
+            dev_free(s, c.vals, s->cap_inst);
+            dev_free(s, c.vals_alt, s->cap_inst);
+        }
         dev_free(s, s->sort.keys_alt, s->cap_inst);
-        dev_free(s, s->sort.vals_alt, s->cap_inst);
         dev_free(s, s->sort.lookback, sort_lookback_words(s->cap_inst));
     }
     s->cap_inst = cap;
     FV_TRY(dev_alloc(s, &s->keys, cap));
-    FV_TRY(dev_alloc(s, &s->vals, cap));
+    for (auto& c : s->bctx) {
+        FV_TRY(dev_alloc(s, &c.vals, cap));
+        FV_TRY(dev_alloc(s, &c.vals_alt, cap));
+        c.vals_home = c.vals;
+        // the ranges pair in the same parity as the values
+        if (c.ranges != c.ranges_home) std::swap(c.ranges, c.ranges_prev);
+    }
+    ctx_load(s, s->bctx_cur);
     FV_TRY(dev_alloc(s, &s->sort.keys_alt, cap));
-    FV_TRY(dev_alloc(s, &s->sort.vals_alt, cap));
     FV_TRY(dev_alloc(s, &s->sort.lookback, sort_lookback_words(cap)));
     FV_CK(cudaMemsetAsync(s->sort.lookback, 0, sizeof(uint64_t) * sort_lookback_words(cap), s->stream));
     s->sort.max_items = cap;
@@ -464,7 +634,9 @@ void collect_timing(fvgs_session* s) {
 }
 
 // Drop the projection's candidate list (the Gaussians changed).
-cudaError_t cand_drop(fvgs_session* s) { return cudaMemsetAsync(s->cst, 0, sizeof(CandState), s->stream); }
+cudaError_t cand_drop(fvgs_session* s) {
+    return cudaMemsetAsync(s->cst_all, 0, sizeof(CandState) * kBinCtx, s->stream);
+}
 
 // The largest angle from the optical axis of a ray through the W x H image
 // of K: the ray through its farthest corner.
@@ -482,6 +654,7 @@ int enqueue_bin(fvgs_session* s, const fvgs_intrinsics* K, int W, int H, int tw,
     const int nty = (H + th - 1) / th;
     const int T = ntx * nty;
     const bool radix = (s->debug & FVGS_DEBUG_RADIX_SORT) != 0;
+    ctx_select(s, W, H, tw, th);
     // Incremental binning needs the previous binning of the same Gaussians on
     // the same tile grid, with true per-tile ranges (not the reference's
     // culled-slot or range-launch behaviours).
@@ -722,8 +895,8 @@ int check_status(fvgs_session* s, int* retry) {
     if (st.flags & kErrTimeout) return FVGS_E_TIMEOUT;
     if (st.flags & kErrBounds) {
         // an incremental binning did not find the instance count of a tile:
-        // drop the history and repeat the call with full binnings
-        s->hist_ok = false;
+        // drop the histories and repeat the call with full binnings
+        ctx_drop_history(s);
         *retry = 1;
         return FVGS_OK;
     }
@@ -827,7 +1000,8 @@ int enqueue_map(fvgs_session* s, const fvgs_intrinsics* K, const FrameLevel& f, 
     ua.beta2 = P.adam_beta2;
     ua.eps = P.adam_eps;
     ua.dbg_delta3d = (s->debug & FVGS_DEBUG_MAPPING) ? s->dbg_delta3d : nullptr;
-    ua.cst = s->cst;
+    ua.cst = s->cst_all;
+    ua.n_cst = kBinCtx;
     if (s->precision == FVGS_PRECISION_REDUCED) {
         ua.attr_sr = s->attr_sr;
         ua.attr_c = s->attr_c;
@@ -946,19 +1120,27 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
         FV_A(s->geo0, N);
         FV_A(s->geo1, N);
     }
-    FV_A(s->bins, N);
-    FV_A(s->counts, N);
     FV_A(s->offsets, N);
-    FV_A(s->cand, N);
-    FV_A(s->cst, 1);
+    FV_A(s->cst_all, kBinCtx);
+    for (int c = 0; c < kBinCtx; ++c) {
+        BinCtx& b = s->bctx[c];
+        FV_A(b.bins, N);
+        FV_A(b.counts, N);
+        FV_A(b.cand, N);
+        b.cst = s->cst_all + c;
+    }
     FV_A(s->partials, scan_partials_size((int)N) + 1);
     // tile-indexed buffers hold the largest frame at the smallest tracking
     // tile (8 x 8); mapping runs on 16 x 16 tiles
     const int ntx = (max_width + 7) / 8, nty = (max_height + 7) / 8;
     s->cap_tiles = ntx * nty;
     s->cap_tiles16 = ((max_width + P.tile_w - 1) / P.tile_w) * ((max_height + P.tile_h - 1) / P.tile_h);
-    FV_A(s->ranges, (size_t)s->cap_tiles);
-    FV_A(s->ranges_prev, (size_t)s->cap_tiles);
+    for (int c = 0; c < kBinCtx; ++c) {
+        FV_A(s->bctx[c].ranges, (size_t)s->cap_tiles);
+        FV_A(s->bctx[c].ranges_prev, (size_t)s->cap_tiles);
+        s->bctx[c].ranges_home = s->bctx[c].ranges;
+    }
+    ctx_load(s, 0);
     s->tile_diff_cells = tile_diff_words(ntx, nty);
     FV_A(s->tile_diff, s->tile_diff_cells);
     FV_A(s->tile_fill, (size_t)s->cap_tiles);
@@ -1011,7 +1193,8 @@ int fvgs_session_create(const fvgs_params* params, int device, uint32_t capacity
     const uint64_t cap0 = std::max<uint64_t>(1u << 20, 8ull * N);
     if ((rc = alloc_instances(s, std::min<uint64_t>(cap0, 0xffffffffull))) != FVGS_OK) return fail(rc);
     if (cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
-    if (cudaMemsetAsync(s->cst, 0, sizeof(CandState), s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
+    if (cudaMemsetAsync(s->cst_all, 0, sizeof(CandState) * kBinCtx, s->stream) != cudaSuccess)
+        return fail(FVGS_E_CUDA);
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(FVGS_E_CUDA);
     *out = s;
     return FVGS_OK;
@@ -1111,7 +1294,7 @@ int fvgs_upload_gaussians(fvgs_session* s, const float* positions, const float* 
     FV_CK(cudaSetDevice(s->device));
     s->n_g = n;
     s->has_binning = s->has_track = false;
-    s->hist_ok = false;
+    ctx_drop_history(s);
     FV_CK(cand_drop(s));
     if (n == 0) return FVGS_OK;
     // Stage through rec planes (free until the next binning) so host arrays of
@@ -1558,6 +1741,7 @@ int enqueue_frame(fvgs_session* s, const fvgs_session::FrameRequest& r) {
         FV_TRY(enqueue_bin(s, &r.K[r.map_level], f.W, f.H, s->params.tile_w, s->params.tile_h));
         FV_TRY(enqueue_map(s, &r.K[r.map_level], f, r.eta));
     }
+    FV_TRY(ctx_normalize(s));
     FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
     FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
     FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
@@ -1571,24 +1755,12 @@ int first_level(const fvgs_session::FrameRequest& r) {
     return r.eta >= 0.f ? r.map_level : -1;
 }
 
-// Whether the frame's first binning continues the session's last one
-// (incremental binning on the same tile grid).
-bool entry_incremental(const fvgs_session* s, const fvgs_session::FrameRequest& r) {
-    const int l0 = first_level(r);
-    if (l0 < 0 || !s->hist_ok) return false;
-    const FrameLevel& f = s->lv[l0];
-    bool tracked = false;  // else the frame's first binning is the mapping step's
-    for (int l = 0; l < kMaxLevels; ++l) tracked = tracked || r.iters[l] > 0;
-    const int tw = tracked ? f.tile_w : s->params.tile_w, th = tracked ? f.tile_h : s->params.tile_h;
-    return s->hist_tw == tw && s->hist_th == th && s->hist_ntx == (f.W + tw - 1) / tw &&
-           s->hist_nty == (f.H + th - 1) / th;
-}
-
-bool frame_key_matches(const fvgs_session::FrameGraph& g, const fvgs_session* s,
-                       const fvgs_session::FrameRequest& r) {
-    if (!(g.valid && g.gen == s->gen && g.map_level == r.map_level && g.eta == r.eta && g.n_g == s->n_g &&
-          g.vals_in == s->vals && g.ranges_in == s->ranges && g.entry_incremental == entry_incremental(s, r)))
+bool frame_key_matches(const fvgs_session::FrameGraph& g, fvgs_session* s, const fvgs_session::FrameRequest& r) {
+    if (!(g.valid && g.gen == s->gen && g.map_level == r.map_level && g.eta == r.eta && g.n_g == s->n_g))
         return false;
+    BinSnap now;
+    snap_take(s, now);
+    if (!snap_same(g.entry, now)) return false;
     for (int l = 0; l < kMaxLevels; ++l) {
         const bool used = r.iters[l] > 0 || (r.eta >= 0.f && l == r.map_level);
         if (g.iters[l] != r.iters[l]) return false;
@@ -1624,14 +1796,10 @@ int launch_frame(fvgs_session* s) {
         if (!frame_key_matches(g, s, r)) continue;
         FV_CK(cudaGraphLaunch(g.exec, s->stream));
         g.last_use = ++s->graph_clock;
-        s->vals = g.vals_out;
-        s->sort.vals_alt = g.vals_alt_out;
-        s->ranges = g.ranges_out;
-        s->ranges_prev = g.ranges_prev_out;
+        snap_put(s, g.exit);
         for (int c = 0; c < FVGS_K_COUNT; ++c) s->launches[c] += g.launches[c];
-        s->hist_ok = true;
-        s->hist_ntx = g.exit_ntx;
-        s->hist_nty = g.exit_nty;
+        s->bin_tw = g.exit_tw;
+        s->bin_th = g.exit_th;
         s->last_W = g.exit_W;
         s->last_H = g.exit_H;
         s->last_T = g.exit_T;
@@ -1643,7 +1811,7 @@ int launch_frame(fvgs_session* s) {
     }
     // capture this frame shape into a free or the least recently used slot
     int victim = 0;
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < fvgs_session::kFrameGraphs; ++i) {
         if (!s->graphs[i].valid || s->graphs[i].gen != s->gen) {
             victim = i;
             break;
@@ -1660,17 +1828,11 @@ int launch_frame(fvgs_session* s) {
     // so if it fails the frame runs eagerly from exactly this state
     uint64_t before[FVGS_K_COUNT];
     std::memcpy(before, s->launches, sizeof(before));
-    uint32_t* const vals0 = s->vals;
-    uint32_t* const vals_alt0 = s->sort.vals_alt;
-    uint2* const ranges0 = s->ranges;
-    uint2* const ranges_prev0 = s->ranges_prev;
-    const bool hist0 = s->hist_ok, clean0 = s->diff_clean, keys0 = s->keys_valid, binned0 = s->has_binning;
-    const int ntx0 = s->hist_ntx, nty0 = s->hist_nty, lw0 = s->last_W, lh0 = s->last_H, lt0 = s->last_T;
-    const int ls0 = s->last_split;
-    g.vals_in = s->vals;
-    g.ranges_in = s->ranges;
+    snap_take(s, g.entry);
+    const bool clean0 = s->diff_clean, keys0 = s->keys_valid, binned0 = s->has_binning;
+    const int lw0 = s->last_W, lh0 = s->last_H, lt0 = s->last_T, ls0 = s->last_split;
+    const int btw0 = s->bin_tw, bth0 = s->bin_th;
     g.n_g = s->n_g;
-    g.entry_incremental = entry_incremental(s, r);
     cudaGraph_t graph = nullptr;
     int rc = FVGS_OK;
     cudaError_t ec = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
@@ -1685,16 +1847,12 @@ int launch_frame(fvgs_session* s) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
         std::memcpy(s->launches, before, sizeof(before));
-        s->vals = vals0;
-        s->sort.vals_alt = vals_alt0;
-        s->ranges = ranges0;
-        s->ranges_prev = ranges_prev0;
-        s->hist_ok = hist0;
+        snap_put(s, g.entry);
         s->diff_clean = clean0;
         s->keys_valid = keys0;
         s->has_binning = binned0;
-        s->hist_ntx = ntx0;
-        s->hist_nty = nty0;
+        s->bin_tw = btw0;
+        s->bin_th = bth0;
         s->last_W = lw0;
         s->last_H = lh0;
         s->last_T = lt0;
@@ -1711,16 +1869,13 @@ int launch_frame(fvgs_session* s) {
     g.map_level = r.map_level;
     g.eta = r.eta;
     g.gen = s->gen;
-    g.exit_ntx = s->hist_ntx;
-    g.exit_nty = s->hist_nty;
+    snap_take(s, g.exit);
+    g.exit_tw = s->bin_tw;
+    g.exit_th = s->bin_th;
     g.exit_W = s->last_W;
     g.exit_H = s->last_H;
     g.exit_T = s->last_T;
     g.exit_split = s->last_split;
-    g.vals_out = s->vals;
-    g.vals_alt_out = s->sort.vals_alt;
-    g.ranges_out = s->ranges;
-    g.ranges_prev_out = s->ranges_prev;
     for (int c = 0; c < FVGS_K_COUNT; ++c) g.launches[c] = s->launches[c] - before[c];
     g.valid = true;
     g.last_use = ++s->graph_clock;
@@ -1986,14 +2141,10 @@ struct fvgs_batch {
     struct Exit {  // one session's key and the host-side binning state its captured frame leaves
         uint64_t gen = 0;
         uint32_t n_g = 0;
-        uint32_t* vals_in = nullptr;
-        uint2* ranges_in = nullptr;
-        bool entry_incremental = false;
+        BinSnap entry, exit;  // the session's binning contexts before and after the frame
         int W[kMaxLevels] = {}, H[kMaxLevels] = {};
         fvgs_intrinsics K[kMaxLevels] = {};
-        int ntx = 0, nty = 0, tw = 0, th = 0, last_W = 0, last_H = 0, last_T = 0;
-        uint32_t *vals = nullptr, *vals_alt = nullptr;
-        uint2 *ranges = nullptr, *ranges_prev = nullptr;
+        int tw = 0, th = 0, last_W = 0, last_H = 0, last_T = 0;
         uint64_t launches[FVGS_K_COUNT] = {};
     };
     struct Graph {
@@ -2151,6 +2302,7 @@ int enqueue_batch_frame(fvgs_batch* b, const Request* reqs, bool capture) {
         }
     }
     for (fvgs_session* s : b->s) {
+        FV_TRY(ctx_normalize(s));
         FV_CK(cudaMemcpyAsync(s->h_devpose, s->pose, sizeof(DevPose), cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_jj + 42, s->step, sizeof(double) * 6, cudaMemcpyDeviceToHost, s->stream));
         FV_CK(cudaMemcpyAsync(s->h_st, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
@@ -2158,7 +2310,7 @@ int enqueue_batch_frame(fvgs_batch* b, const Request* reqs, bool capture) {
     return batch_join(b);
 }
 
-bool batch_key_matches(const fvgs_batch* b, const Request* reqs) {
+bool batch_key_matches(fvgs_batch* b, const Request* reqs) {
     const fvgs_batch::Graph& g = b->graph;
     if (!g.valid) return false;
     for (int l = 0; l < kMaxLevels; ++l)
@@ -2166,11 +2318,12 @@ bool batch_key_matches(const fvgs_batch* b, const Request* reqs) {
             g.variant[l] != b->variant[l])
             return false;
     for (size_t i = 0; i < b->s.size(); ++i) {
-        const fvgs_session* s = b->s[i];
+        fvgs_session* s = b->s[i];
         const fvgs_batch::Exit& e = g.exit[i];
-        if (e.gen != s->gen || e.n_g != s->n_g || e.vals_in != s->vals || e.ranges_in != s->ranges ||
-            e.entry_incremental != entry_incremental(s, reqs[i]))
-            return false;
+        if (e.gen != s->gen || e.n_g != s->n_g) return false;
+        BinSnap now;
+        snap_take(s, now);
+        if (!snap_same(e.entry, now)) return false;
         for (int l = 0; l < kMaxLevels; ++l) {
             if (reqs[i].iters[l] == 0) continue;
             const FrameLevel& f = s->lv[l];
@@ -2184,24 +2337,15 @@ bool batch_key_matches(const fvgs_batch* b, const Request* reqs) {
 
 // Host-side binning state of a session (restored when a capture fails).
 struct HostBinState {
-    uint32_t *vals, *vals_alt;
-    uint2 *ranges, *ranges_prev;
-    bool hist, clean, keys, binned;
-    int ntx, nty, tw, th, btw, bth, lw, lh, lt, ls;
+    BinSnap snap;
+    bool clean, keys, binned;
+    int btw, bth, lw, lh, lt, ls;
     uint64_t launches[FVGS_K_COUNT];
-    void save(const fvgs_session* s) {
-        vals = s->vals;
-        vals_alt = s->sort.vals_alt;
-        ranges = s->ranges;
-        ranges_prev = s->ranges_prev;
-        hist = s->hist_ok;
+    void save(fvgs_session* s) {
+        snap_take(s, snap);
         clean = s->diff_clean;
         keys = s->keys_valid;
         binned = s->has_binning;
-        ntx = s->hist_ntx;
-        nty = s->hist_nty;
-        tw = s->hist_tw;
-        th = s->hist_th;
         btw = s->bin_tw;
         bth = s->bin_th;
         lw = s->last_W;
@@ -2211,18 +2355,10 @@ struct HostBinState {
         std::memcpy(launches, s->launches, sizeof(launches));
     }
     void restore(fvgs_session* s) const {
-        s->vals = vals;
-        s->sort.vals_alt = vals_alt;
-        s->ranges = ranges;
-        s->ranges_prev = ranges_prev;
-        s->hist_ok = hist;
+        snap_put(s, snap);
         s->diff_clean = clean;
         s->keys_valid = keys;
         s->has_binning = binned;
-        s->hist_ntx = ntx;
-        s->hist_nty = nty;
-        s->hist_tw = tw;
-        s->hist_th = th;
         s->bin_tw = btw;
         s->bin_th = bth;
         s->last_W = lw;
@@ -2248,15 +2384,9 @@ int batch_launch(fvgs_batch* b, const Request* reqs) {
         for (size_t i = 0; i < n; ++i) {
             fvgs_session* s = b->s[i];
             const fvgs_batch::Exit& e = b->graph.exit[i];
-            s->vals = e.vals;
-            s->sort.vals_alt = e.vals_alt;
-            s->ranges = e.ranges;
-            s->ranges_prev = e.ranges_prev;
-            s->hist_ok = true;
-            s->hist_ntx = e.ntx;
-            s->hist_nty = e.nty;
-            s->hist_tw = s->bin_tw = e.tw;
-            s->hist_th = s->bin_th = e.th;
+            snap_put(s, e.exit);
+            s->bin_tw = e.tw;
+            s->bin_th = e.th;
             s->last_W = e.last_W;
             s->last_H = e.last_H;
             s->last_T = e.last_T;
@@ -2278,9 +2408,7 @@ int batch_launch(fvgs_batch* b, const Request* reqs) {
         fvgs_batch::Exit& e = exit[i];
         e.gen = s->gen;
         e.n_g = s->n_g;
-        e.vals_in = s->vals;
-        e.ranges_in = s->ranges;
-        e.entry_incremental = entry_incremental(s, reqs[i]);
+        snap_take(s, e.entry);
         for (int l = 0; l < kMaxLevels; ++l) {
             e.W[l] = s->lv[l].W;
             e.H[l] = s->lv[l].H;
@@ -2317,17 +2445,12 @@ int batch_launch(fvgs_batch* b, const Request* reqs) {
     for (size_t i = 0; i < n; ++i) {
         fvgs_session* s = b->s[i];
         fvgs_batch::Exit& e = exit[i];
-        e.ntx = s->hist_ntx;
-        e.nty = s->hist_nty;
+        snap_take(s, e.exit);
         e.tw = s->bin_tw;
         e.th = s->bin_th;
         e.last_W = s->last_W;
         e.last_H = s->last_H;
         e.last_T = s->last_T;
-        e.vals = s->vals;
-        e.vals_alt = s->sort.vals_alt;
-        e.ranges = s->ranges;
-        e.ranges_prev = s->ranges_prev;
         for (int c = 0; c < FVGS_K_COUNT; ++c) e.launches[c] = s->launches[c] - before[i].launches[c];
     }
     fvgs_batch::Graph& g = b->graph;
@@ -2820,7 +2943,7 @@ int finish_compact(fvgs_session* s, bool remove, uint32_t* n_marked) {
     FV_CK(cand_drop(s));
     // every per-Gaussian index of the last binning is stale now
     s->has_binning = s->has_track = s->has_map = false;
-    s->hist_ok = false;
+    ctx_drop_history(s);
     s->keys_valid = false;
     s->dbg_proj_valid = false;
     ++s->gen;  // captured frame graphs hold the old plane addresses
@@ -3025,7 +3148,7 @@ int map_grew(fvgs_session* s, uint32_t n) {
     s->n_g = n;
     FV_CK(cand_drop(s));
     s->has_binning = s->has_track = s->has_map = false;
-    s->hist_ok = false;  // the new Gaussians have no previous binning
+    ctx_drop_history(s);  // the new Gaussians have no previous binning
     s->keys_valid = false;
     s->dbg_proj_valid = false;
     ++s->gen;

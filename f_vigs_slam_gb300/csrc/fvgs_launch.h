@@ -123,6 +123,10 @@ struct EmitArgs {
     uint32_t enter_cap;
 };
 
+// Copy a binning's ranges[T] and the sorted indices they cover into another
+// buffer pair (same positions).
+cudaError_t launch_copy_lists(const uint2* ranges, int T, const uint32_t* src, uint32_t* dst, uint2* ranges_dst,
+                              uint64_t capacity, int max_ctas, cudaStream_t s);
 // max_ctas caps the grid (the kernel strides over the Gaussians); <= 0: one thread per Gaussian.
 cudaError_t launch_project_count(const ProjectArgs& a, int max_ctas, cudaStream_t s);
 size_t scan_partials_size(int n);
@@ -386,7 +390,8 @@ struct MapUpdateArgs {
     float* dbg_delta3d;  // optional [N][16]
     uint4* attr_sr;      // optional: refresh the reduced-precision planes of updated Gaussians
     uint2* attr_c;
-    CandState* cst;      // optional: the projection's candidate list, stale once positions move
+    CandState* cst;      // optional: n_cst candidate-list states, all stale once positions move
+    int n_cst;
 };
 cudaError_t launch_map_forward(const MapArgs& a, bool cap, cudaStream_t s);
 cudaError_t launch_map_backward(const MapArgs& a, bool cap, cudaStream_t s);

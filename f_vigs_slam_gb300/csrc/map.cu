@@ -300,7 +300,7 @@ __device__ __forceinline__ float adam_step(float& m, float& v, float g, float et
 __global__ void __launch_bounds__(256) map_update_kernel(MapUpdateArgs a, const DevStatus* st) {
     pdl_begin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0 && a.cst) a.cst->valid = 0;
+    if (i < a.n_cst && a.cst) a.cst[i].valid = 0;
     if (i >= a.n) return;
     // An instance overflow leaves the binning incomplete; the host re-runs the
     // step with larger buffers, so the parameters must stay untouched.

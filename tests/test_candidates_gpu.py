@@ -110,9 +110,11 @@ def test_walk_rebuilds_past_the_bounds(oracle, fvgs_lib):
     assert reuses > 0 and rebuilds > 0
 
 
-def test_pyramid_levels_share_a_list(oracle, fvgs_lib):
-    """A coarser pyramid level of the same camera (the same view cone to a
-    fraction of a pixel) reuses the list; a wider view cone rebuilds it."""
+def test_each_tile_grid_keeps_its_list(oracle, fvgs_lib):
+    """Every tile grid (pyramid level) bins in its own context with its own
+    list: a coarser level builds one at its first binning, the finer level's
+    list is still reused afterwards, and a wider view cone on the same grid
+    rebuilds it."""
     fv = fvgs_lib
     W, H, K = scaled_camera(0.5)
     W2, H2, K2 = scaled_camera(0.25)
@@ -123,12 +125,18 @@ def test_pyramid_levels_share_a_list(oracle, fvgs_lib):
         s.project_bin(pose0, K, W, H)
         _, n, _, _, cone = _held_pose(s)
         pose = S.perturb(pose0, 1.0, 2.0, np.random.default_rng(1))
-        s.project_bin(pose, K2, W2, H2)
+        s.project_bin(pose, K2, W2, H2)          # another grid: its own list, built here
         _expect_equal(oracle, scene, pose, K2, W2, H2, P, s)
-        v2, n2, t2, _, cone2 = _held_pose(s)
-        assert v2 and n2 == n and cone2 == cone
-        np.testing.assert_array_equal(t2, pose0[0])
-        # half the focal length: a much wider view
+        v2, _, t2, _, _ = _held_pose(s)
+        assert v2
+        np.testing.assert_array_equal(t2, pose[0])
+        s.project_bin(pose, K, W, H)             # back on the first grid: its list reused
+        _expect_equal(oracle, scene, pose, K, W, H, P, s)
+        v1, n1, t1, _, cone1 = _held_pose(s)
+        assert v1 and n1 == n and cone1 == cone
+        np.testing.assert_array_equal(t1, pose0[0])
+        assert s.binning_info()["incremental"]    # and its history: the binning continued
+        # half the focal length: a much wider view on the same grid
         Kw = (K[0] * 0.5, K[1] * 0.5, K[2], K[3])
         s.project_bin(pose, Kw, W, H)
         _expect_equal(oracle, scene, pose, Kw, W, H, P, s)

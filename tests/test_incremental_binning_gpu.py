@@ -105,22 +105,38 @@ def test_incremental_large_tiles(oracle, fvgs_lib):
             _expect_equal(oracle, scene, pose, K, W, H, P, keys, vals, ranges)
 
 
-def test_history_invalidated(oracle, fvgs_lib):
-    """A different tile grid, a re-upload or a literal reference quirk makes
-    the next binning a full one."""
+def test_history_per_grid_and_invalidated(oracle, fvgs_lib):
+    """Every tile grid keeps its own binning history (up to four grids, the
+    least recently used one rebound): a new grid's first binning is a full
+    one, going back to a grid continues its history.  A re-upload or a
+    literal reference quirk makes the next binning a full one."""
     fv = fvgs_lib
     W, H, K = scaled_camera(0.5)
     W2, H2, K2 = scaled_camera(0.25)
     scene = S.cam_box(5000, seed=2)
     P = oracle.default_params()
     pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, np.random.default_rng(2))
+    rng = np.random.default_rng(3)
     with fv.Session(scene.n, W, H) as s:
         s.upload(scene)
         s.project_bin(pose, K, W, H)
-        s.project_bin(pose, K2, W2, H2)          # another tile grid
+        s.project_bin(pose, K2, W2, H2)          # another tile grid: full
         assert not s.binning_info()["incremental"]
+        pose = _walk(pose, rng, 0.002, 0.1)
+        s.project_bin(pose, K, W, H)             # back to the first grid: its history continues
+        assert s.binning_info()["incremental"]
+        keys, vals, ranges = s.download_binning(W, H)
+        _expect_equal(oracle, scene, pose, K, W, H, P, keys, vals, ranges)
+        for sc in (0.125, 0.375, 0.3):           # three more grids: the second grid is rebound
+            Wx, Hx, Kx = scaled_camera(sc)
+            s.project_bin(pose, Kx, Wx, Hx)
+            assert not s.binning_info()["incremental"]
         s.project_bin(pose, K, W, H)
+        assert s.binning_info()["incremental"]
+        s.project_bin(pose, K2, W2, H2)
         assert not s.binning_info()["incremental"]
+        keys, vals, ranges = s.download_binning(W2, H2)
+        _expect_equal(oracle, scene, pose, K2, W2, H2, P, keys, vals, ranges)
         s.project_bin(pose, K, W, H)
         assert s.binning_info()["incremental"]
         s.upload(scene)                            # re-upload
