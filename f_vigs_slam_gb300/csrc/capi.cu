@@ -480,11 +480,13 @@ void ctx_select(fvgs_session* s, int W, int H, int tw, int th) {
 int ctx_normalize(fvgs_session* s) {
     ctx_store(s);
     for (auto& c : s->bctx) {
-        if (c.vals == c.vals_home && c.ranges == c.ranges_home) continue;
+        // a context without history needs no particular member (its next
+        // binning is a full one, and graph keys ignore it); its lists may be
+        // the last binning's, which downloads read
+        if (!c.hist_ok || (c.vals == c.vals_home && c.ranges == c.ranges_home)) continue;
         // (a member already at home is copied onto itself: same values)
-        if (c.hist_ok)
-            FV_CK(launch_copy_lists(c.ranges, c.hist_ntx * c.hist_nty, c.vals, c.vals_home, c.ranges_home,
-                                    s->cap_inst, s->num_sms * 8, s->stream));
+        FV_CK(launch_copy_lists(c.ranges, c.hist_ntx * c.hist_nty, c.vals, c.vals_home, c.ranges_home, s->cap_inst,
+                                s->num_sms * 8, s->stream));
         if (c.vals != c.vals_home) std::swap(c.vals, c.vals_alt);
         if (c.ranges != c.ranges_home) std::swap(c.ranges, c.ranges_prev);
     }
