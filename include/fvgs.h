@@ -185,14 +185,16 @@ int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int*
  * 8 x 8 or 32 x 8 tiles: fvgs_session_set_track_tiles).  Any pointer may be
  * null.  No reference counterpart (its tiles are always 16 x 16). */
 int fvgs_session_binning_grid(const fvgs_session* s, int* tile_w, int* tile_h, int* num_tiles);
-/* The projection's candidate list after the work enqueued so far (waits for
- * the session's stream): whether one is held, its length, and the pose and
- * view-cone half-angle (radians) it was built at.  A binning whose pose is
- * within 2 degrees and 5 cm of that pose, with a view cone no wider, projects
- * only the listed Gaussians; any other binning projects all of them and
- * rebuilds the list; a change to the Gaussians drops it.  Any pointer may be
- * null.  No reference counterpart: the reference projects every Gaussian at
- * every render. */
+/* The projection's candidate list of the tile grid binned last, after the
+ * work enqueued so far (waits for the session's stream): whether one is held,
+ * its length, and the pose and view-cone half-angle (radians) it was built
+ * at.  Every tile grid (frame size and tile shape; up to four, the least
+ * recently binned one replaced) keeps its own list and binning history.  A
+ * binning whose pose is within 2 degrees and 5 cm of its grid's list pose,
+ * with a view cone no wider, projects only the listed Gaussians; any other
+ * binning projects all of them and rebuilds the list; a change to the
+ * Gaussians drops every list.  Any pointer may be null.  No reference
+ * counterpart: the reference projects every Gaussian at every render. */
 int fvgs_session_candidates(fvgs_session* s, int* valid, uint32_t* n, fvgs_pose* pose, float* cone);
 
 /*
