@@ -175,9 +175,9 @@ int fvgs_download_binning(fvgs_session* s, uint64_t* keys, uint32_t* values, uin
                           uint64_t max_instances, uint32_t* n_instances);
 /* How the last binning whose status the host has read (every call that
  * waits for the device reads it) was formed: its instance count, whether it
- * was incremental (1: built from the binning before it, 0: full), the
- * instances that entered a tile since that binning, and the Gaussians with
- * such instances.  Any pointer may be null.  No reference counterpart: the
+ * was incremental (1: built from the previous binning of the same tile grid,
+ * 0: full), the instances that entered a tile since that binning, and the
+ * Gaussians with such instances.  Any pointer may be null.  No reference counterpart: the
  * reference rebuilds every binning from scratch. */
 int fvgs_session_binning_info(const fvgs_session* s, uint32_t* n_instances, int* incremental, uint32_t* n_entering,
                               uint32_t* n_changed);
