@@ -117,9 +117,10 @@ int fvgs_session_set_precision(fvgs_session* s, int precision);
  * CTAs and 80 registers, 1 at two CTAs and 128 registers, 7 at two CTAs with
  * batches of 128; 2 runs as 0.
  * Which is faster depends on the map and frame.  On the first frame of a new
- * frame shape of a pyramid level (fvgs_track_frame, fvgs_frame_submit) the session bins the
- * frame at the request's pose, times every variant on that binning and keeps
- * the fastest for that level and shape; results do not depend on the choice.
+ * frame shape of a pyramid level (fvgs_track_frame, fvgs_frame_submit) the
+ * session bins the frame at the request's pose, times every variant on that
+ * binning and keeps the fastest for that level and shape; results do not
+ * depend on the choice.
  * fvgs_session_autotune runs the tuning explicitly (reps timed launches per
  * variant; variant and per-variant median ms (FVGS_TRACK_VARIANTS floats) may
  * be null); fvgs_session_set_autotune(s, 0) keeps variant 0 for untuned
