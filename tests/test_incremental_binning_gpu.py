@@ -183,3 +183,38 @@ def test_tracking_loop_uses_incremental_binning(oracle, fvgs_lib):
         assert s.binning_info()["incremental"]
     ang, tr = S.pose_error(dev_pose, pose)
     assert ang < 1e-6 and tr < 1e-6, (ang, tr)
+
+
+def test_frame_end_leaves_lists_that_later_binnings_continue(oracle, fvgs_lib):
+    """A frame with an odd number of binnings at a level copies that grid's
+    current lists back into the buffer the grid started the frame with (so
+    captured frames keep matching); the next binning of each grid continues
+    from the copy, incrementally, and still equals a full binning."""
+    from test_track_gpu import _target_pyramid, INTENDED
+
+    fv = fvgs_lib
+    W, H, K0 = scaled_camera(0.5)
+    scene = S.cam_box(20_000, seed=31)
+    P = oracle.default_params(INTENDED)
+    rng = np.random.default_rng(32)
+    true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
+    iters = (1, 3, 3)  # odd at every level
+    frames = _target_pyramid(oracle, scene, true_pose, K0, W, H, P, len(iters), 33)
+    with fv.Session(scene.n, W, H, fv.default_params(INTENDED)) as s:
+        s.upload(scene)
+        for lv, fr in enumerate(frames):
+            s.set_frame(lv, *fr)
+        start = S.perturb(true_pose, 0.2, 0.5, rng)
+        for _ in range(3):  # captured (no history), captured (histories), replayed
+            s.frame_submit_pyramid(start, K0, iters)
+            pose, _ = s.frame_wait()
+        assert s.frame_stats()["graphed"] >= 2
+        for lv in (2, 1, 0):
+            sc = 1.0 / (1 << lv)
+            K = tuple(np.float32(k * sc) for k in K0)
+            w, h = W >> lv, H >> lv
+            p = _walk(pose, rng, 0.001, 0.05)
+            s.project_bin(p, K, w, h)
+            assert s.binning_info()["incremental"]
+            keys, vals, ranges = s.download_binning(w, h)
+            _expect_equal(oracle, scene, p, K, w, h, P, keys, vals, ranges)
