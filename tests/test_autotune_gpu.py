@@ -67,3 +67,31 @@ def test_first_frame_of_a_shape_is_tuned(oracle, fvgs_lib):
         assert t == 2 + fv.TRACK_VARIANTS * 5  # two iterations + five timed launches per variant
         s.track_frame(pose, K, iterations=2)
         assert s.get_timing(reset=True)["track"]["launches"] == 2
+
+
+@pytest.mark.parametrize("analytic", [False, True], ids=["ref_jacobian", "analytic_jacobian"])
+def test_split_tiles_give_the_same_tile_partials(oracle, fvgs_lib, analytic):
+    """Variants 5 and 6 run each 16 x 16 tile's list on 2 or 4 CTAs; the
+    per-tile partials (their rows added in a whole tile's order) and the
+    systems are the same bits as one CTA per tile."""
+    fv = fvgs_lib
+    W, H, K = scaled_camera(0.5)
+    scene = S.cam_box(30_000, seed=75)
+    quirks = fv.QUIRKS_INTENDED if analytic else fv.QUIRKS_DEFAULT
+    P = oracle.default_params(quirks)
+    rng = np.random.default_rng(76)
+    true_pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, rng)
+    start = S.perturb(true_pose, 0.5, 1.0, rng)
+    frame = make_frame(oracle, scene, true_pose, K, W, H, P)
+    T = ((W + 15) // 16) * ((H + 15) // 16)
+    with fv.Session(scene.n, W, H, fv.default_params(quirks)) as s:
+        s.upload(scene)
+        s.set_frame(0, *frame)
+        out = {}
+        for variant in (0, 5, 6):
+            s.set_track_variant(0, variant)
+            JtJ, Jtr = s.track_jacobian(start, K, 0)
+            out[variant] = (JtJ, Jtr, s.download_tile_partials(T))
+    for v in (5, 6):
+        for x, y in zip(out[0], out[v]):
+            np.testing.assert_array_equal(x, y)
