@@ -1130,10 +1130,9 @@ def make_serving_workload(fvgs, S, torch, dev, n_sessions, frames_per_session):
 
 def touch_host_frames(torch, dev, ws):
     """Copy every pinned host frame of the sessions' epochs to the device once
-    (untimed): the first DMA from freshly pinned pages pays for their
-    translation, which a camera pipeline reusing its pinned frame buffers
-    does not (measured: the first end-to-end pass over new buffers ran 10-15%
-    below the passes after it)."""
+    (untimed): a camera pipeline reuses its pinned frame buffers, so the first
+    DMA from newly pinned pages (their address translation) is not part of a
+    frame's cost."""
     scratch = None
     for w in ws:
         for ep in w["epochs"]:
