@@ -189,6 +189,8 @@ struct fvgs_session {
     int bctx_cur = 0;
     uint64_t bctx_clock = 0;
     CandState* cst_all = nullptr;  // the contexts' candidate-list states, contiguous
+    float* frame_stage = nullptr;  // packed frames from host memory (fvgs_set_frames_packed)
+    size_t frame_stage_cap = 0;
 
     FrameLevel lv[kMaxLevels];
     // frame preprocessing: 8-bit colour pyramid and the raw depth of a frame
@@ -1444,6 +1446,37 @@ int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* de
     FV_CK(cudaMemcpyAsync(f.depth, depth, sizeof(float) * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.gx, grad_x, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(f.gy, grad_y, sizeof(float) * 3 * px, cudaMemcpyDefault, s->stream));
+    return FVGS_OK;
+}
+
+int fvgs_set_frames_packed(fvgs_session* s, const float* frames, int levels, int width, int height) {
+    if (!s || !frames || levels < 1 || levels > kMaxLevels || width <= 0 || height <= 0) return FVGS_E_INVALID;
+    FV_CK(cudaSetDevice(s->device));
+    size_t total = 0;
+    for (int l = 0, w = width, h = height; l < levels; ++l, w = (w + 1) / 2, h = (h + 1) / 2)
+        total += 10 * (size_t)w * h;
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, frames) != cudaSuccess) {
+        cudaGetLastError();
+        attr.type = cudaMemoryTypeUnregistered;
+    }
+    const float* src = frames;
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) {
+        // host memory: one copy to the device, then the levels from there
+        if (total > s->frame_stage_cap) {
+            dev_free(s, s->frame_stage, s->frame_stage_cap);
+            s->frame_stage_cap = 0;
+            FV_TRY(dev_alloc(s, &s->frame_stage, total));
+            s->frame_stage_cap = total;
+        }
+        FV_CK(cudaMemcpyAsync(s->frame_stage, frames, sizeof(float) * total, cudaMemcpyDefault, s->stream));
+        src = s->frame_stage;
+    }
+    for (int l = 0, w = width, h = height; l < levels; ++l, w = (w + 1) / 2, h = (h + 1) / 2) {
+        const size_t px = (size_t)w * h;
+        FV_TRY(fvgs_set_frame(s, l, src, src + 3 * px, src + 4 * px, src + 7 * px, w, h));
+        src += 10 * px;
+    }
     return FVGS_OK;
 }
 

@@ -253,6 +253,14 @@ class Session:
             "fvgs_set_frame",
         )
 
+    def set_frames_packed(self, packed, levels: int, W: int, H: int):
+        """Frames of levels 0..levels-1 from one packed buffer (pack_pyramid's
+        layout): a numpy array (host memory: one copy to the device) or a
+        device pointer (int)."""
+        ptr = C.c_void_p(packed) if isinstance(packed, int) else _ptr(_f32(packed))
+        _check(self.lib.fvgs_set_frames_packed(self.h, ptr, C.c_int(levels), C.c_int(W), C.c_int(H)),
+               "fvgs_set_frames_packed")
+
     # -------------------------------------------------------------- binning
     def project_bin(self, pose, K, W, H) -> int:
         n = C.c_uint32()

@@ -154,6 +154,14 @@ int fvgs_download_gaussians(fvgs_session* s, float* positions, float* scales, fl
  */
 int fvgs_set_frame(fvgs_session* s, int level, const float* rgb, const float* depth, const float* grad_x,
                    const float* grad_y, int width, int height);
+/* Observed frames of levels 0..levels-1 from one packed buffer: per level
+ * rgb[3P], depth[P], grad_x[3P], grad_y[3P], level l of size
+ * ceil(width / 2^l) x ceil(height / 2^l), level 0 first (the layout of
+ * fvgs_server_request.pyr_frames).  A buffer in host memory crosses to the
+ * device in one copy (into a staging buffer the session keeps), then each
+ * level is copied on the device.  No reference counterpart (the reference
+ * builds its pyramid from the camera frame; fvgs_preprocess_frame). */
+int fvgs_set_frames_packed(fvgs_session* s, const float* frames, int levels, int width, int height);
 
 /*
  * Projection, tile binning, stable depth-key sort and per-tile ranges for

@@ -63,3 +63,31 @@ def test_preprocess_matches_oracle(oracle, fvgs_lib, depth_mm, double_scale):
             for name, g, w in zip(("rgb", "depth", "gx", "gy"), got, want[lv]):
                 assert g.shape == w.shape, (lv, name)
                 np.testing.assert_array_equal(g, w, err_msg="level %d %s" % (lv, name))
+
+
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_packed_frames_equal_per_level(oracle, fvgs_lib, where):
+    """fvgs_set_frames_packed (one buffer, pack_pyramid's layout; from host
+    memory one copy to the device) sets every level exactly as fvgs_set_frame
+    per level does."""
+    import torch
+
+    fv = fvgs_lib
+    rng = np.random.default_rng(8)
+    H, W = 123, 171
+    color = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    depth = rng.uniform(0.1, 8.0, (H, W)).astype(np.float32)
+    levels = oracle.preprocess(color, depth, levels=3, depth_mm=False, double_scale=False)
+    packed = fv.pack_pyramid(levels)
+    with fv.Session(1000, W, H) as s:
+        if where == "host":
+            s.set_frames_packed(packed, 3, W, H)
+        else:
+            dev = torch.from_numpy(packed).to("cuda:0")
+            torch.cuda.synchronize()
+            s.set_frames_packed(dev.data_ptr(), 3, W, H)
+        for lv in range(3):
+            got = s.download_frame(lv)
+            for name, g, w in zip(("rgb", "depth", "gx", "gy"), got, levels[lv]):
+                assert g.shape == w.shape, (lv, name)
+                np.testing.assert_array_equal(g, w, err_msg="level %d %s" % (lv, name))
