@@ -46,8 +46,10 @@ keyframes, N log-uniform in [20k, 2M], one fvgs_batch_run_pyramid call --
 one persistent launch per iteration -- against sequential frames and
 per-keyframe graphs on streams), `precision` (N = 2 M, keyframe schedule,
 with BF16/FP16 attributes against
-FP32, and the visual-inertial solve with 200 Hz IMU data) and `maintenance`
-(outlier removal, covisibility, prune on the 1 M map).
+FP32, and the visual-inertial solve with 200 Hz IMU data), `maintenance`
+(outlier removal, covisibility, prune on the 1 M map) and `render_preprocess`
+(the render-form view and the preprocessing of a camera frame into the three
+pyramid levels, on the same map and frame size).
 
 The CPU arm (--impl reference) and `cpu_baseline` time the CPU restatement
 (FP64, all host threads) on whole frames of the same serving mix, session
@@ -127,6 +129,9 @@ def parse():
                     help="profiling case: the large plain workload's frame at one pyramid level, three Jacobian "
                          "evaluations with a fixed launch variant (launches: one render, then the evaluations; "
                          "not the benchmark line)")
+    ap.add_argument("--render-case", action="store_true",
+                    help="profiling case: the large plain workload's map, three render-form views and three "
+                         "preprocessed camera frames (not the benchmark line)")
     ap.add_argument("--prec-n", type=int, default=PREC_N, help="Gaussians of the precision-form workload")
     ap.add_argument("--batch-sessions", type=int, default=BATCH_SESSIONS, help="keyframes of the batching workload")
     return ap.parse_args()
@@ -755,6 +760,8 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
 
     maint = measure_maintenance(fvgs, sess, frames, K, W, H, reps=max(3, args.steps),
                                 with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+    rp = measure_render_preprocess(fvgs, sess, frames[-1], K, W, H, max(3, args.steps), torch, dev, stream,
+                                   with_cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
     dominant = max((c for c in timing if timing[c]["timed"]), key=lambda c: timing[c]["ms"])
     peak, peak_kind = load_peaks()
@@ -800,6 +807,7 @@ def run_large(args, fvgs, S, torch, dev, stream, rank, world):
                      "issue": issue_roofline(dominant, per_launch_ms, dev)},
         "kernel_rooflines": per_class,
         "maintenance": maint,
+        "render_preprocess": rp,
     }
 
 
@@ -833,6 +841,31 @@ def run_track_case(args, fvgs, S):
             "workload": "room N=%d, %dx%d (pyramid level %d of 1280x720), launch variant %d" % (args.n, w, h, level,
                                                                                              variant),
             "track_ms_per_launch": t["ms"] / max(1, t["timed"])}
+
+
+def run_render_case(args, fvgs, S):
+    """Profiling case: the room map of the large plain workload at 1280x720,
+    the frame rendered at the first trajectory pose (one tracking-kernel
+    render launch), three render-form views at that pose (fvgs_render_view),
+    then three preprocessings of that frame as a camera frame of 8-bit colour
+    and uint16 millimetre depth (fvgs_preprocess_frame, three levels)."""
+    cam = S.CAM_HD
+    W, H, K = cam.width, cam.height, cam.intrinsics
+    sess = fvgs.Session(args.n, W, H, fvgs.default_params(QUIRKS))
+    sess.upload(S.room(args.n, seed=0))
+    true = S.trajectory(2, seed=3)[1]
+    col, dep, _, _ = sess.render(true, K, W, H)
+    rgb, d = S.add_noise(col, dep, np.random.default_rng(5))
+    c8 = np.clip(np.rint(rgb * 255.0), 0, 255).astype(np.uint8)
+    mm = np.clip(np.rint(d * 1000.0), 0, 65535).astype(np.uint16)
+    for _ in range(3):
+        sess.render_view(true, K, W, H)
+    for _ in range(3):
+        sess.preprocess_frame(c8, mm, levels=ROOM_LEVELS)
+    n = sess.n
+    sess.close()
+    return {"metric": "render-form and preprocessing profiling case (not the benchmark line)",
+            "workload": "room N=%d, %dx%d, 3 render-form views, 3 preprocessed camera frames" % (n, W, H)}
 
 
 def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
@@ -878,6 +911,133 @@ def measure_maintenance(fvgs, sess, frames, K, W, H, reps, with_cpu):
     if with_cpu:
         out["cpu_baseline"] = cpu_outlier_sample(sess, pose, K, W, H, frames[-1]["host"][0]["depth"].numpy())
     return out
+
+
+def preprocess_bytes(W, H, levels=ROOM_LEVELS):
+    """Bytes fvgs_preprocess_frame must move for one camera frame: 8-bit
+    colour (3 B) and uint16 millimetre depth (2 B) per pixel in, per level
+    40 B per pixel out (colour 12, depth 4, two gradient images 12 each)."""
+    return 5 * W * H + 40 * sum(w * h for w, h in level_dims(W, H, levels))
+
+
+def measure_render_preprocess(fvgs, sess, frame, K, W, H, reps, torch, dev, stream, with_cpu):
+    """The steps either side of the tracking path, on the large workload's map
+    (after the maintenance removals) and last frame: the render form
+    (fvgs_render_view: binning, then render_view_kernel, the viewer's image)
+    and frame preprocessing (fvgs_preprocess_frame: a camera frame of 8-bit
+    colour and uint16 millimetre depth -> three pyramid levels of colour,
+    depth and Sobel gradients)."""
+    pose = frame["pose"]
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic()
+    out = {}
+    # render form: wall time of the synchronous call (image copied back to
+    # pageable host memory) and CUDA-event times of its kernels by class
+    sess.render_view(pose, K, W, H)
+    classes = ["project", "scan", "emit", "sort", "ranges", "render"]
+    sess.set_timing(classes)
+    sess.get_timing(reset=True)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        col, dep = sess.render_view(pose, K, W, H)
+        ts.append(time.perf_counter() - t0)
+    t = sess.get_timing(reset=True)
+    sess.set_timing(())
+    rk = t["render"]
+    render_ms = rk["ms"] / max(1, rk["timed"])
+    rv = {"call_ms": 1000.0 * float(np.median(ts)), "render_kernel_ms": render_ms,
+          "binning_kernels_ms": sum(t[c]["ms"] for c in classes if c != "render") / reps,
+          "pixels": W * H, "instances": int(sess.binning_info()["n_instances"]), "gaussians": sess.n,
+          "pixels_per_s": W * H / (render_ms / 1000.0),
+          "depth_crossed_share": float(np.mean(dep < 1e9))}
+    if traffic.get("render_view"):
+        rv["ncu_dram_bytes_per_launch"] = traffic["render_view"]
+        rv["ncu_dram_gbs"] = traffic["render_view"] / (render_ms / 1000.0) / 1e9
+        rv["ncu_dram_frac"] = rv["ncu_dram_gbs"] / peak
+    rv["issue"] = issue_roofline("render_view", render_ms, dev)
+    out["render_view"] = rv
+
+    # preprocessing: the frame's level-0 observation as a camera frame
+    import ctypes
+
+    rgb = frame["host"][0]["rgb"].numpy().reshape(H, W, 3)
+    d = frame["host"][0]["depth"].numpy().reshape(H, W)
+    c8 = np.clip(np.rint(rgb * 255.0), 0, 255).astype(np.uint8)
+    mm = np.clip(np.rint(d * 1000.0), 0, 65535).astype(np.uint16)
+    host = (torch.from_numpy(c8).pin_memory(), torch.from_numpy(mm).pin_memory())
+    devc = (host[0].to(dev), host[1].to(dev))
+
+    def pre(src):
+        st = sess.lib.fvgs_preprocess_frame(sess.h, ctypes.c_void_p(src[0].data_ptr()),
+                                            ctypes.c_void_p(src[1].data_ptr()), 1, W, H, ROOM_LEVELS, 0)
+        if st != 0:
+            raise fvgs.FvgsError(st, "fvgs_preprocess_frame")
+
+    algo = preprocess_bytes(W, H)
+    pp = {"camera_frame": "%dx%d, 8-bit colour + uint16 mm depth, %d levels" % (W, H, ROOM_LEVELS),
+          "algorithmic_bytes": algo,
+          "bytes_basis": "5 B per camera pixel in; per level 40 B per pixel out (colour, depth, two gradients)"}
+    for name, src in (("device", devc), ("host", host)):
+        for _ in range(3):
+            pre(src)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            pre(src)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        pp[name] = {"ms_per_frame": ms, "frames_per_s": 1000.0 / ms}
+    ms = pp["device"]["ms_per_frame"]
+    pp["device"].update({"achieved_gbs": algo / (ms / 1000.0) / 1e9, "peak": peak, "peak_kind": peak_kind,
+                         "frac": algo / (ms / 1000.0) / 1e9 / peak,
+                         "note": "inputs in HBM; the call copies them into the session's buffers, then "
+                                 "%d kernel launches (one per level)" % ROOM_LEVELS})
+    pp["host"]["note"] = "inputs in pinned host memory: the %d bytes cross the link inside the timed call" % (
+        5 * W * H)
+    if traffic.get("preprocess"):
+        pp["ncu_dram_bytes_per_frame"] = traffic["preprocess"]
+    out["preprocess"] = pp
+    if with_cpu:
+        out["cpu_baseline"] = cpu_render_preprocess_sample(fvgs, sess, pose, K, W, H, c8, mm)
+    return out
+
+
+def cpu_render_preprocess_sample(fvgs, sess, pose, K, W, H, c8, mm, band_rows=64):
+    """The oracle's render form (forwardPassTileKernel restated, FP64, one
+    thread) on a band of rows through the image centre, scaled to the frame,
+    and its preprocessing of the whole camera frame (one thread); the device
+    levels of the last preprocessing are compared with the oracle's, bit for
+    bit."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from f_vigs_slam_gb300 import synthetic as S
+
+    O.build()
+    pos, scl, rot, col, opa = sess.download()
+    scene = S.Scene(pos, scl, rot, col, opa)
+    P = O.default_params(QUIRKS)
+    y0 = ((H - band_rows) // 2 // 16) * 16
+    K_band = (K[0], K[1], K[2], K[3] - y0)
+    b = O.prepare(scene, pose, K_band, W, band_rows, P)
+    t0 = time.perf_counter()
+    O.render_view(scene, b, W, band_rows, P)
+    tr = time.perf_counter() - t0
+    n, tp = 0, 0.0
+    while tp < 2.0 or n < 3:
+        t0 = time.perf_counter()
+        want = O.preprocess(c8, mm, levels=ROOM_LEVELS, depth_mm=True)
+        tp += time.perf_counter() - t0
+        n += 1
+    exact = all(all(np.array_equal(g, w) for g, w in zip(sess.download_frame(lv), want[lv]))
+                for lv in range(ROOM_LEVELS))
+    return {"render_ms_per_frame": 1000.0 * tr * H / band_rows,
+            "preprocess_ms_per_frame": 1000.0 * tp / n, "cores": 1, "kind": "port",
+            "sample": "render: %d rows of %d, %.1f ms, scaled by rows (binning not timed); preprocessing: the "
+                      "whole frame %d times" % (band_rows, H, 1000.0 * tr, n),
+            "preprocess_levels_bit_exact": bool(exact)}
 
 
 def cpu_outlier_sample(sess, pose, K, W, H, depth, band_rows=64):
@@ -1361,6 +1521,10 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps(run_track_case(args, fvgs, S)), flush=True)
         return 0
+    if args.render_case:
+        if rank == 0:
+            print(json.dumps(run_render_case(args, fvgs, S)), flush=True)
+        return 0
     large = run_large(args, fvgs, S, torch, dev, stream, rank, world)
     if args.plain_only:
         if rank == 0:
@@ -1410,8 +1574,10 @@ def run_ours(args):
             "graphed_frames": srv["graphed_frames"],
             "roofline": large["roofline"],
             "small_plain": small,
-            "large_plain": {k: v for k, v in large.items() if k not in ("roofline", "maintenance")},
+            "large_plain": {k: v for k, v in large.items()
+                            if k not in ("roofline", "maintenance", "render_preprocess")},
             "maintenance": large["maintenance"],
+            "render_preprocess": large["render_preprocess"],
             "precision": prec,
             "batching": batch,
             "clocks": srv["clocks"],

@@ -1403,15 +1403,14 @@ int fvgs_preprocess_frame(fvgs_session* s, const uint8_t* color, const void* dep
     s->pre_h = height;
     FV_CK(cudaMemcpyAsync(s->pre_u8[0], color, 3 * px0, cudaMemcpyDefault, s->stream));
     FV_CK(cudaMemcpyAsync(s->pre_raw, depth, raw_bytes, cudaMemcpyDefault, s->stream));
-    FV_CK(launch_depth_in(s->pre_raw, depth_u16_mm, px0, s->lv[0].depth, s->stream));
-    for (int l = 0; l < levels; ++l) {
+    // one launch per level (pyrDown, colour, Sobel and depth together), chained
+    FV_CK(launch_prep_level0(s->pre_u8[0], s->pre_raw, depth_u16_mm, width, height, double_scale, s->lv[0].rgb,
+                             s->lv[0].gx, s->lv[0].gy, s->lv[0].depth, s->stream));
+    for (int l = 1; l < levels; ++l) {
         FrameLevel& f = s->lv[l];
-        if (l > 0) {
-            const FrameLevel& g = s->lv[l - 1];
-            FV_CK(launch_pyrdown_u8(s->pre_u8[l - 1], g.W, g.H, 3, s->pre_u8[l], s->stream));
-            FV_CK(launch_pyrdown_f32(g.depth, g.W, g.H, f.depth, s->stream));
-        }
-        FV_CK(launch_color_sobel(s->pre_u8[l], f.W, f.H, double_scale, f.rgb, f.gx, f.gy, s->stream));
+        const FrameLevel& g = s->lv[l - 1];
+        FV_CK(launch_prep_level(s->pre_u8[l - 1], g.depth, g.W, g.H, double_scale, s->pre_u8[l], f.rgb, f.gx, f.gy,
+                                f.depth, s->stream));
     }
     return FVGS_OK;
 }

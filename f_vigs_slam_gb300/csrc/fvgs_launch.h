@@ -345,11 +345,14 @@ struct RenderArgs {
 cudaError_t launch_render_view(const RenderArgs& a, cudaStream_t s);
 
 // ---- frame preprocessing (preprocess.cu) ----
-cudaError_t launch_pyrdown_u8(const uint8_t* src, int W, int H, int c, uint8_t* dst, cudaStream_t s);
-cudaError_t launch_pyrdown_f32(const float* src, int W, int H, float* dst, cudaStream_t s);
-cudaError_t launch_depth_in(const void* src, int u16_mm, size_t n, float* dst, cudaStream_t s);
-cudaError_t launch_color_sobel(const uint8_t* img, int W, int H, int double_scale, float* rgb, float* gx, float* gy,
-                               cudaStream_t s);
+// Level 0 of a W x H camera frame: depth in metres (float, or uint16 mm), the
+// colour (/255, twice with double_scale) and its Sobel derivatives.
+cudaError_t launch_prep_level0(const uint8_t* img, const void* raw_depth, int u16_mm, int W, int H, int double_scale,
+                               float* rgb, float* gx, float* gy, float* depth, cudaStream_t s);
+// The next level from a Wp x Hp level: its 8-bit colour and depth by pyrDown,
+// then the same colour, Sobel and depth outputs.
+cudaError_t launch_prep_level(const uint8_t* prev, const float* prev_depth, int Wp, int Hp, int double_scale,
+                              uint8_t* cur, float* rgb, float* gx, float* gy, float* depth, cudaStream_t s);
 
 // ---- mapping (map.cu) ----
 struct MapArgs {

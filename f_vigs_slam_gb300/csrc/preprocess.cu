@@ -6,7 +6,11 @@
 // level the colour as float / 255 and its 3x3 Sobel derivatives
 // (cv::Sobel(.., CV_32F, 1, 0, 3) and (0, 1, 3)), uploaded as the tracking
 // inputs.  Here the camera frame is copied to the device once and every level
-// is produced there:
+// is produced there, one launch per level (chained by programmatic dependent
+// launch): level 0 stages its 8-bit tile and Sobel halo in shared memory;
+// every coarser level stages the finer level's 8-bit window under its pixels
+// and halo, filters its own 8-bit colour there (stored for the next level),
+// and takes the Sobel from shared memory.
 //  * pyrDown: 5-tap binomial [1 4 6 4 1]/16 in x and y, reflect-101 borders,
 //    output ((W + 1) / 2, (H + 1) / 2); 8-bit images in integers with
 //    (sum + 128) >> 8, float images as row sums then column sums, times 1/256,
@@ -32,108 +36,151 @@ __device__ __forceinline__ int reflect101(int i, int n) {
     return i;
 }
 
-__global__ void pyrdown_u8_kernel(const uint8_t* __restrict__ src, int W, int H, int c, uint8_t* __restrict__ dst) {
-    const int W2 = (W + 1) / 2, H2 = (H + 1) / 2;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W2 || y >= H2) return;
-    const int wts[5] = {1, 4, 6, 4, 1};
-    int xs[5], ys[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        xs[k] = reflect101(2 * x + k - 2, W);
-        ys[k] = reflect101(2 * y + k - 2, H);
-    }
-    for (int ch = 0; ch < c; ++ch) {
-        int s = 0;
-#pragma unroll
-        for (int ky = 0; ky < 5; ++ky) {
-            int r = 0;
-#pragma unroll
-            for (int kx = 0; kx < 5; ++kx) r += wts[kx] * src[((size_t)ys[ky] * W + xs[kx]) * c + ch];
-            s += wts[ky] * r;
-        }
-        dst[((size_t)y * W2 + x) * c + ch] = (uint8_t)((s + 128) >> 8);
-    }
-}
+constexpr int kTW = 32, kTH = 8;              // output pixels of one CTA, one per thread
+constexpr int kHW = kTW + 2, kHH = kTH + 2;    // with the Sobel halo
+constexpr int kSW = 2 * kTW + 7, kSH = 2 * kTH + 7;  // finer-level window of a pyrDown CTA
 
-__global__ void pyrdown_f32_kernel(const float* __restrict__ src, int W, int H, float* __restrict__ dst) {
-    const int W2 = (W + 1) / 2, H2 = (H + 1) / 2;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W2 || y >= H2) return;
-    const float wts[5] = {1.f, 4.f, 6.f, 4.f, 1.f};
-    int xs[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) xs[k] = reflect101(2 * x + k - 2, W);
-    float s = 0.f;
-#pragma unroll
-    for (int ky = 0; ky < 5; ++ky) {
-        const float* row = src + (size_t)reflect101(2 * y + ky - 2, H) * W;
-        float r = 0.f;
-#pragma unroll
-        for (int kx = 0; kx < 5; ++kx) r = __fadd_rn(r, __fmul_rn(wts[kx], row[xs[kx]]));
-        s = __fadd_rn(s, __fmul_rn(wts[ky], r));
-    }
-    dst[(size_t)y * W2 + x] = __fmul_rn(s, 1.0f / 256.0f);
-}
+__device__ __forceinline__ float u8f(uint8_t v) { return __fmul_rn((float)v, 1.0f / 255.0f); }
 
-// Depth of the camera frame in metres: float as is, or uint16 millimetres.
-__global__ void depth_in_kernel(const void* __restrict__ src, int u16_mm, size_t n, float* __restrict__ dst) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    dst[i] = u16_mm ? __fmul_rn((float)static_cast<const uint16_t*>(src)[i], 0.001f)
-                    : static_cast<const float*>(src)[i];
-}
-
-__device__ __forceinline__ float u8f(const uint8_t* img, int W, int x, int y, int ch) {
-    return __fmul_rn((float)img[((size_t)y * W + x) * 3 + ch], 1.0f / 255.0f);
-}
-
-// Colour to float (/255, and /255 again for the observed image with
-// double_scale) and its Sobel derivatives, one pixel per thread.
-__global__ void color_sobel_kernel(const uint8_t* __restrict__ img, int W, int H, int double_scale,
-                                   float* __restrict__ rgb, float* __restrict__ gx, float* __restrict__ gy) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const int xm = reflect101(x - 1, W), xp = reflect101(x + 1, W);
-    const int ym = reflect101(y - 1, H), yp = reflect101(y + 1, H);
-    const size_t p = (size_t)y * W + x;
+// Colour (/255, and /255 again for the observed image with double_scale) and
+// its Sobel derivatives at tile cell (hx, hy) of a (kHH x kHW x 3) 8-bit
+// tile whose cells around it are the reflect-101 neighbours.
+__device__ __forceinline__ void color_sobel_at(const uint8_t (*t)[kHW * 3], int hx, int hy, int double_scale,
+                                               size_t p, float* __restrict__ rgb, float* __restrict__ gx,
+                                               float* __restrict__ gy) {
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
-        const float f = u8f(img, W, x, y, ch);
+        const int xm = 3 * (hx - 1) + ch, xc = 3 * hx + ch, xp = 3 * (hx + 1) + ch;
+        const float f = u8f(t[hy][xc]);
         rgb[3 * p + ch] = double_scale ? __fmul_rn(f, 1.0f / 255.0f) : f;
-        const float a = __fsub_rn(u8f(img, W, xp, ym, ch), u8f(img, W, xm, ym, ch));
-        const float b = __fsub_rn(u8f(img, W, xp, y, ch), u8f(img, W, xm, y, ch));
-        const float c = __fsub_rn(u8f(img, W, xp, yp, ch), u8f(img, W, xm, yp, ch));
+        const float a = __fsub_rn(u8f(t[hy - 1][xp]), u8f(t[hy - 1][xm]));
+        const float b = __fsub_rn(u8f(t[hy][xp]), u8f(t[hy][xm]));
+        const float c = __fsub_rn(u8f(t[hy + 1][xp]), u8f(t[hy + 1][xm]));
         gx[3 * p + ch] = __fadd_rn(__fadd_rn(a, __fmul_rn(2.0f, b)), c);
-        const float d = __fsub_rn(u8f(img, W, xm, yp, ch), u8f(img, W, xm, ym, ch));
-        const float e = __fsub_rn(u8f(img, W, x, yp, ch), u8f(img, W, x, ym, ch));
-        const float f2 = __fsub_rn(u8f(img, W, xp, yp, ch), u8f(img, W, xp, ym, ch));
+        const float d = __fsub_rn(u8f(t[hy + 1][xm]), u8f(t[hy - 1][xm]));
+        const float e = __fsub_rn(u8f(t[hy + 1][xc]), u8f(t[hy - 1][xc]));
+        const float f2 = __fsub_rn(u8f(t[hy + 1][xp]), u8f(t[hy - 1][xp]));
         gy[3 * p + ch] = __fadd_rn(__fadd_rn(d, __fmul_rn(2.0f, e)), f2);
     }
 }
 
-static dim3 grid2(int W, int H) { return dim3((W + 31) / 32, (H + 7) / 8); }
-
-cudaError_t launch_pyrdown_u8(const uint8_t* src, int W, int H, int c, uint8_t* dst, cudaStream_t s) {
-    pyrdown_u8_kernel<<<grid2((W + 1) / 2, (H + 1) / 2), dim3(32, 8), 0, s>>>(src, W, H, c, dst);
-    return cudaGetLastError();
+// Level 0: the camera frame's 8-bit tile with its halo staged in shared
+// memory (reflect-101), then per pixel the depth in metres and the colour /
+// Sobel outputs.
+__global__ void __launch_bounds__(kTW * kTH) prep_level0_kernel(const uint8_t* __restrict__ img,
+                                                                const void* __restrict__ raw_depth, int u16_mm,
+                                                                int W, int H, int double_scale,
+                                                                float* __restrict__ rgb, float* __restrict__ gx,
+                                                                float* __restrict__ gy, float* __restrict__ depth) {
+    pdl_begin();
+    __shared__ uint8_t t[kHH][kHW * 3];
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    for (int i = threadIdx.x; i < kHH * kHW; i += kTW * kTH) {
+        const int hy = i / kHW, hx = i - hy * kHW;
+        // cells past the image's far edge are not read; clamp them in range
+        const int xs = reflect101(min(x0 + hx - 1, W), W), ys = reflect101(min(y0 + hy - 1, H), H);
+        const uint8_t* q = img + ((size_t)ys * W + xs) * 3;
+        t[hy][3 * hx] = q[0];
+        t[hy][3 * hx + 1] = q[1];
+        t[hy][3 * hx + 2] = q[2];
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kTW, ly = threadIdx.x / kTW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= W || y >= H) return;
+    const size_t p = (size_t)y * W + x;
+    depth[p] = u16_mm ? __fmul_rn((float)static_cast<const uint16_t*>(raw_depth)[p], 0.001f)
+                      : static_cast<const float*>(raw_depth)[p];
+    color_sobel_at(t, lx + 1, ly + 1, double_scale, p, rgb, gx, gy);
 }
 
-cudaError_t launch_pyrdown_f32(const float* src, int W, int H, float* dst, cudaStream_t s) {
-    pyrdown_f32_kernel<<<grid2((W + 1) / 2, (H + 1) / 2), dim3(32, 8), 0, s>>>(src, W, H, dst);
-    return cudaGetLastError();
+// One pyrDown level and its outputs.  The CTA's window of the finer 8-bit
+// level (the 5-tap footprint of its pixels and of their Sobel halo, read
+// through reflect-101) is staged in shared memory; the level's 8-bit colour
+// is computed there for the pixels and the halo (halo cells at the level's
+// own reflect-101 positions), stored for the next level, and fed to the
+// Sobel; the depth is filtered per pixel from the finer level's depth.
+__global__ void __launch_bounds__(kTW * kTH) prep_level_kernel(const uint8_t* __restrict__ prev,
+                                                               const float* __restrict__ prev_depth, int Wp, int Hp,
+                                                               int double_scale, uint8_t* __restrict__ cur,
+                                                               float* __restrict__ rgb, float* __restrict__ gx,
+                                                               float* __restrict__ gy, float* __restrict__ depth) {
+    pdl_begin();
+    __shared__ uint8_t sp[kSH][kSW * 3];
+    __shared__ uint8_t t[kHH][kHW * 3];
+    const int W = (Wp + 1) / 2, H = (Hp + 1) / 2;
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    // the window starts at the first tap of level pixel x0 - 1
+    const int cx0 = 2 * x0 - 4, cy0 = 2 * y0 - 4;
+    for (int i = threadIdx.x; i < kSH * kSW; i += kTW * kTH) {
+        const int sy = i / kSW, sx = i - sy * kSW;
+        // taps of the level's pixels and halo lie in [-2, Wp + 1]; clamp the
+        // window's unused cells into that range before reflecting
+        const int xs = reflect101(max(-2, min(cx0 + sx, Wp + 1)), Wp);
+        const int ys = reflect101(max(-2, min(cy0 + sy, Hp + 1)), Hp);
+        const uint8_t* q = prev + ((size_t)ys * Wp + xs) * 3;
+        sp[sy][3 * sx] = q[0];
+        sp[sy][3 * sx + 1] = q[1];
+        sp[sy][3 * sx + 2] = q[2];
+    }
+    __syncthreads();
+    const int wts[5] = {1, 4, 6, 4, 1};
+    for (int i = threadIdx.x; i < kHH * kHW; i += kTW * kTH) {
+        const int hy = i / kHW, hx = i - hy * kHW;
+        const int xl = reflect101(min(x0 + hx - 1, W), W), yl = reflect101(min(y0 + hy - 1, H), H);
+        const int bx = 2 * xl - 2 - cx0, by = 2 * yl - 2 - cy0;  // first tap in the window
+        const bool own = hx >= 1 && hx <= kTW && hy >= 1 && hy <= kTH && x0 + hx - 1 < W && y0 + hy - 1 < H;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            int s = 0;
+#pragma unroll
+            for (int ky = 0; ky < 5; ++ky) {
+                int r = 0;
+#pragma unroll
+                for (int kx = 0; kx < 5; ++kx) r += wts[kx] * sp[by + ky][3 * (bx + kx) + ch];
+                s += wts[ky] * r;
+            }
+            const uint8_t v = (uint8_t)((s + 128) >> 8);
+            t[hy][3 * hx + ch] = v;
+            if (own) cur[((size_t)(y0 + hy - 1) * W + (x0 + hx - 1)) * 3 + ch] = v;
+        }
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kTW, ly = threadIdx.x / kTW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= W || y >= H) return;
+    const size_t p = (size_t)y * W + x;
+    // depth: row sums then column sums, times 1/256, each op rounded
+    const float fw[5] = {1.f, 4.f, 6.f, 4.f, 1.f};
+    int xs[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) xs[k] = reflect101(2 * x + k - 2, Wp);
+    float s = 0.f;
+#pragma unroll
+    for (int ky = 0; ky < 5; ++ky) {
+        const float* row = prev_depth + (size_t)reflect101(2 * y + ky - 2, Hp) * Wp;
+        float r = 0.f;
+#pragma unroll
+        for (int kx = 0; kx < 5; ++kx) r = __fadd_rn(r, __fmul_rn(fw[kx], row[xs[kx]]));
+        s = __fadd_rn(s, __fmul_rn(fw[ky], r));
+    }
+    depth[p] = __fmul_rn(s, 1.0f / 256.0f);
+    color_sobel_at(t, lx + 1, ly + 1, double_scale, p, rgb, gx, gy);
 }
 
-cudaError_t launch_depth_in(const void* src, int u16_mm, size_t n, float* dst, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    depth_in_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, u16_mm, n, dst);
-    return cudaGetLastError();
+cudaError_t launch_prep_level0(const uint8_t* img, const void* raw_depth, int u16_mm, int W, int H, int double_scale,
+                               float* rgb, float* gx, float* gy, float* depth, cudaStream_t s) {
+    if (W <= 0 || H <= 0) return cudaSuccess;
+    return launch_chained(prep_level0_kernel, dim3((W + kTW - 1) / kTW, (H + kTH - 1) / kTH), dim3(kTW * kTH), 0,
+                          s, img, raw_depth, u16_mm, W, H, double_scale, rgb, gx, gy, depth);
 }
 
-cudaError_t launch_color_sobel(const uint8_t* img, int W, int H, int double_scale, float* rgb, float* gx, float* gy,
-                               cudaStream_t s) {
-    color_sobel_kernel<<<grid2(W, H), dim3(32, 8), 0, s>>>(img, W, H, double_scale, rgb, gx, gy);
-    return cudaGetLastError();
+cudaError_t launch_prep_level(const uint8_t* prev, const float* prev_depth, int Wp, int Hp, int double_scale,
+                              uint8_t* cur, float* rgb, float* gx, float* gy, float* depth, cudaStream_t s) {
+    const int W = (Wp + 1) / 2, H = (Hp + 1) / 2;
+    if (Wp <= 0 || Hp <= 0) return cudaSuccess;
+    return launch_chained(prep_level_kernel, dim3((W + kTW - 1) / kTW, (H + kTH - 1) / kTH), dim3(kTW * kTH), 0, s,
+                          prev, prev_depth, Wp, Hp, double_scale, cur, rgb, gx, gy, depth);
 }
 
 }  // namespace fvgs

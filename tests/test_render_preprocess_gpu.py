@@ -45,11 +45,43 @@ def test_render_view_matches_oracle(oracle, fvgs_lib, quirks):
     assert np.abs(c8.astype(int) - expect8.astype(int)).max() <= 1
 
 
-@pytest.mark.parametrize("depth_mm,double_scale", [(False, False), (True, False), (False, True)])
-def test_preprocess_matches_oracle(oracle, fvgs_lib, depth_mm, double_scale):
+def test_render_view_signed_opacities(oracle, fvgs_lib):
+    """Zero and negative opacities (outside the sigmoid's range, but valid
+    input): the render form blends their weights o exp(-q/2) with the sign,
+    as the reference's kernel does; same tolerances."""
+    fv = fvgs_lib
+    W, H, K = scaled_camera(0.5)
+    scene = S.cam_box(20_000, seed=22)
+    rng = np.random.default_rng(4)
+    o = scene.opacities.copy()
+    pick = rng.random(o.size)
+    o[pick < 0.05] *= -0.2
+    o[(pick >= 0.05) & (pick < 0.08)] = 0.0
+    scene = S.Scene(scene.positions, scene.scales, scene.orientations, scene.colors, o.astype(np.float32))
+    P = oracle.default_params(0x8)
+    pose = S.perturb((np.zeros(3), S.IDENTITY_Q), 1.0, 2.0, np.random.default_rng(3))
+    b = oracle.prepare(scene, pose, K, W, H, P)
+    col_o, dep_o = oracle.render_view(scene, b, W, H, P)
+    with fv.Session(scene.n, W, H, fv.default_params(0x8)) as s:
+        s.upload(scene)
+        col, dep = s.render_view(pose, K, W, H)
+    assert rel_err(col, col_o) <= 1e-5
+    crossed_o, crossed = dep_o < 1e9, dep < 1e9
+    assert (crossed != crossed_o).mean() <= 1e-4
+    both = crossed & crossed_o
+    d = np.abs(dep[both] - dep_o[both]) / np.maximum(np.abs(dep_o[both]), 1.0)
+    assert np.quantile(d, 0.999) <= 1e-5
+
+
+@pytest.mark.parametrize("depth_mm,double_scale,H,W", [(False, False, 123, 171), (True, False, 123, 171),
+                                                     (False, True, 123, 171), (True, False, 9, 70),
+                                                     (False, False, 3, 2)])
+def test_preprocess_matches_oracle(oracle, fvgs_lib, depth_mm, double_scale, H, W):
+    """Odd sizes exercise the reflect-101 borders and the (n+1)/2 levels; 9 x 70
+    gives levels narrower than one 32 x 8 block row and partial blocks, 3 x 2
+    levels of 2 x 1 and 1 x 1 pixels."""
     fv = fvgs_lib
     rng = np.random.default_rng(7)
-    H, W = 123, 171  # odd sizes exercise the reflect-101 borders and the (n+1)/2 levels
     color = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
     if depth_mm:
         depth = rng.integers(0, 8000, (H, W), dtype=np.uint16)
