@@ -1212,6 +1212,13 @@ int fvgs_session_set_stream(fvgs_session* s, void* stream) {
     return FVGS_OK;
 }
 
+int fvgs_session_stream(fvgs_session* s, void** stream, int* device) {
+    if (!s) return FVGS_E_INVALID;
+    if (stream) *stream = s->stream;
+    if (device) *device = s->device;
+    return FVGS_OK;
+}
+
 int fvgs_session_sync(fvgs_session* s) {
     if (!s) return FVGS_E_INVALID;
     FV_CK(cudaSetDevice(s->device));

@@ -71,6 +71,9 @@ int fvgs_session_destroy(fvgs_session* s);
 /* Run all further work of the session on this cudaStream_t (NULL = the
  * session's own stream). */
 int fvgs_session_set_stream(fvgs_session* s, void* cuda_stream);
+/* The cudaStream_t the session's work runs on and its CUDA device, for
+ * callers that order their own copies or kernels against it. */
+int fvgs_session_stream(fvgs_session* s, void** cuda_stream, int* device);
 int fvgs_session_sync(fvgs_session* s);
 int fvgs_session_set_debug(fvgs_session* s, uint32_t flags);
 /* Time the kernel classes in class_mask (bit k = class k) with CUDA events on
