@@ -39,8 +39,10 @@ constexpr int kMPix = 256;  // 16 x 16 pixels per tile
 
 __global__ void __launch_bounds__(kMPix) visibility_kernel(VisArgs a) {
     pdl_begin();
-    __shared__ float4 sA[kMPix];  // u, v, opacity, c.x
-    __shared__ float2 sB[kMPix];  // c.y, c.z
+    // alpha = min(0.99, o exp(-q/2)) as one ex2.approx of log2(o) + the
+    // conic pre-scaled by -log2(e)/2 (the tracking kernels' weight)
+    __shared__ float4 sA[kMPix];  // u, v, log2(opacity), c'.x
+    __shared__ float2 sB[kMPix];  // 2 c'.y, c'.z
     __shared__ int sHit[kMPix];
     const int tile = blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
@@ -65,8 +67,9 @@ __global__ void __launch_bounds__(kMPix) visibility_kernel(VisArgs a) {
                 r0 = a.rec0[g];
                 r1 = a.rec1[g];
             }
-            sA[tid] = make_float4(r0.x, r0.y, r0.w, r1.x);
-            sB[tid] = make_float2(r1.y, r1.z);
+            constexpr float kNegHalfLog2e = -0.72134752044448170368f;
+            sA[tid] = make_float4(r0.x, r0.y, log2_opacity(r0.w), kNegHalfLog2e * r1.x);
+            sB[tid] = make_float2(2.0f * kNegHalfLog2e * r1.y, kNegHalfLog2e * r1.z);
         }
         sHit[tid] = 0;
         __syncthreads();
@@ -75,8 +78,11 @@ __global__ void __launch_bounds__(kMPix) visibility_kernel(VisArgs a) {
             const float4 gA = sA[j];
             const float2 gB = sB[j];
             const float dx = gA.x - px, dy = gA.y - py;
-            const float v = gA.w * dx * dx + 2.0f * gB.x * dx * dy + gB.y * dy * dy;
-            const float alpha = fminf(0.99f, gA.z * expf(-0.5f * v));
+            const float t = __fmaf_rn(dx, __fmaf_rn(gA.w, dx, __fmul_rn(gB.x, dy)),
+                                      __fmaf_rn(__fmul_rn(gB.y, dy), dy, gA.z));
+            float w;
+            asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(t));
+            const float alpha = fminf(0.99f, w);
             if (alpha < 1.0f / 255.0f) continue;
             sHit[j] = 1;
             T *= 1.0f - alpha;

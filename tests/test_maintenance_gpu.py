@@ -6,8 +6,9 @@ the marked Gaussians (GSSlam::removeOutliers / prune).
 
 Tolerances.  Prune marks are FP32 comparisons done in the same order on both
 sides: bit-exact.  Compaction moves data: bit-exact.  Visibility and outlier
-marks come from thresholds on exp() of FP32 values (CUDA's expf on the GPU,
-FP64 in the oracle), so an evaluation within a few ulp of a threshold may
+marks come from thresholds on exp() of FP32 values (one ex2.approx of an
+FP32 exponent on the GPU, FP64 in the oracle), so an evaluation within a few
+ulp of a threshold may
 fall either way; such flips are rare (about one per ten million evaluations)
 and the tests require >= 99.9 % agreement, and exact agreement wherever the
 oracle's decision has a margin.  Outlier scores are FP32 sums (per tile in a
