@@ -97,9 +97,10 @@ __global__ void __launch_bounds__(kTW * kTH) prep_level0_kernel(const uint8_t* _
 // One pyrDown level and its outputs.  The CTA's window of the finer 8-bit
 // level (the 5-tap footprint of its pixels and of their Sobel halo, read
 // through reflect-101) is staged in shared memory; the level's 8-bit colour
-// is computed there for the pixels and the halo (halo cells at the level's
-// own reflect-101 positions), stored for the next level, and fed to the
-// Sobel; the depth is filtered per pixel from the finer level's depth.
+// is filtered there (separably, exact in integers) for the pixels and the
+// halo (halo cells at the level's own reflect-101 positions), stored for the
+// next level, and fed to the Sobel; the depth is filtered per pixel from the
+// finer level's depth.
 __global__ void __launch_bounds__(kTW * kTH) prep_level_kernel(const uint8_t* __restrict__ prev,
                                                                const float* __restrict__ prev_depth, int Wp, int Hp,
                                                                int double_scale, uint8_t* __restrict__ cur,
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(kTW * kTH) prep_level_kernel(const uint8_t* __
                                                                float* __restrict__ gy, float* __restrict__ depth) {
     pdl_begin();
     __shared__ uint8_t sp[kSH][kSW * 3];
+    __shared__ uint16_t hs[kSH][kHW * 3];
     __shared__ uint8_t t[kHH][kHW * 3];
     const int W = (Wp + 1) / 2, H = (Hp + 1) / 2;
     const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
@@ -124,25 +126,34 @@ __global__ void __launch_bounds__(kTW * kTH) prep_level_kernel(const uint8_t* __
         sp[sy][3 * sx + 2] = q[2];
     }
     __syncthreads();
+    // separable filter, exact in integers: horizontal 5-tap sums (at most
+    // 16 * 255) of every window row at every level column of the pixels and
+    // halo, then the vertical sums of those
     const int wts[5] = {1, 4, 6, 4, 1};
+    for (int i = threadIdx.x; i < kSH * kHW; i += kTW * kTH) {
+        const int r = i / kHW, hx = i - r * kHW;
+        const int bx = 2 * reflect101(min(x0 + hx - 1, W), W) - 2 - cx0;  // first tap in the window
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            int h = 0;
+#pragma unroll
+            for (int kx = 0; kx < 5; ++kx) h += wts[kx] * sp[r][3 * (bx + kx) + ch];
+            hs[r][3 * hx + ch] = (uint16_t)h;
+        }
+    }
+    __syncthreads();
     for (int i = threadIdx.x; i < kHH * kHW; i += kTW * kTH) {
         const int hy = i / kHW, hx = i - hy * kHW;
-        const int xl = reflect101(min(x0 + hx - 1, W), W), yl = reflect101(min(y0 + hy - 1, H), H);
-        const int bx = 2 * xl - 2 - cx0, by = 2 * yl - 2 - cy0;  // first tap in the window
+        const int by = 2 * reflect101(min(y0 + hy - 1, H), H) - 2 - cy0;
         const bool own = hx >= 1 && hx <= kTW && hy >= 1 && hy <= kTH && x0 + hx - 1 < W && y0 + hy - 1 < H;
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
-            int s = 0;
+            int v = 0;
 #pragma unroll
-            for (int ky = 0; ky < 5; ++ky) {
-                int r = 0;
-#pragma unroll
-                for (int kx = 0; kx < 5; ++kx) r += wts[kx] * sp[by + ky][3 * (bx + kx) + ch];
-                s += wts[ky] * r;
-            }
-            const uint8_t v = (uint8_t)((s + 128) >> 8);
-            t[hy][3 * hx + ch] = v;
-            if (own) cur[((size_t)(y0 + hy - 1) * W + (x0 + hx - 1)) * 3 + ch] = v;
+            for (int ky = 0; ky < 5; ++ky) v += wts[ky] * hs[by + ky][3 * hx + ch];
+            const uint8_t u = (uint8_t)((v + 128) >> 8);
+            t[hy][3 * hx + ch] = u;
+            if (own) cur[((size_t)(y0 + hy - 1) * W + (x0 + hx - 1)) * 3 + ch] = u;
         }
     }
     __syncthreads();
