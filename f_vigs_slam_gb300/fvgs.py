@@ -169,6 +169,12 @@ class Session:
     def set_stream(self, stream_handle: int | None):
         _check(self.lib.fvgs_session_set_stream(self.h, C.c_void_p(stream_handle or 0)), "fvgs_session_set_stream")
 
+    def stream(self):
+        """(cudaStream_t as an int, CUDA device) the session's work runs on (fvgs_session_stream)."""
+        st, dev = C.c_void_p(), C.c_int()
+        _check(self.lib.fvgs_session_stream(self.h, C.byref(st), C.byref(dev)), "fvgs_session_stream")
+        return int(st.value or 0), int(dev.value)
+
     def sync(self):
         _check(self.lib.fvgs_session_sync(self.h), "fvgs_session_sync")
 

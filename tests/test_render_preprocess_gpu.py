@@ -123,3 +123,19 @@ def test_packed_frames_equal_per_level(oracle, fvgs_lib, where):
             for name, g, w in zip(("rgb", "depth", "gx", "gy"), got, levels[lv]):
                 assert g.shape == w.shape, (lv, name)
                 np.testing.assert_array_equal(g, w, err_msg="level %d %s" % (lv, name))
+
+
+def test_session_stream_follows_set_stream(fvgs_lib):
+    """fvgs_session_stream returns the stream set by fvgs_session_set_stream,
+    and the session's own (non-null) stream after a reset to NULL."""
+    import torch
+
+    fv = fvgs_lib
+    with fv.Session(1000, 64, 48) as s:
+        own, dev = s.stream()
+        assert own != 0 and dev == 0
+        st = torch.cuda.Stream(device="cuda:0")
+        s.set_stream(st.cuda_stream)
+        assert s.stream() == (st.cuda_stream, 0)
+        s.set_stream(None)
+        assert s.stream() == (own, 0)
